@@ -1,0 +1,90 @@
+"""Regenerates the golden fixtures in this directory from the GreenPeas sources.
+
+Run from the repository root with the reference checkout available:
+
+    python tests/golden/make_golden.py --reference /path/to/GreenPeas
+
+It writes:
+
+* ``dems/surface{3,5}_L{0,1,2}.dem`` -- the reference's golden DEMs
+  (data/dems/*.dem, pinned by python/tests/test_error_analysis.py:27-45),
+  rewritten in canonical form: targets sorted within an error, errors sorted
+  by target list, probabilities printed with ``repr`` (exact round trip).
+* ``circuits.json`` -- SHA-256 digests of the reference's fixture circuits
+  (data/circuits/*.stim).  Surface-code circuits are hashed whole; BB-code
+  circuits are hashed with their OBSERVABLE_INCLUDE lines removed, because
+  this project's BB logical basis is its own.
+* ``kats.json`` -- known-answer values from the reference's unit tests.
+
+The tests never read the reference checkout; they read only these files.
+"""
+
+from __future__ import annotations
+
+import argparse
+import hashlib
+import json
+import re
+from pathlib import Path
+
+HERE = Path(__file__).resolve().parent
+
+
+def canonical_dem(text: str) -> str:
+    rows = []
+    for line in text.splitlines():
+        line = line.strip()
+        if not line or line.startswith("#"):
+            continue
+        m = re.fullmatch(r"error\(([^)]*)\)\s*(.*)", line)
+        if not m:
+            raise ValueError(f"unexpected DEM line: {line!r}")
+        p = float(m.group(1))
+        dets, obs = [], []
+        for t in m.group(2).split():
+            (dets if t[0] == "D" else obs).append(int(t[1:]))
+        rows.append((tuple(sorted(dets)), tuple(sorted(obs)), p))
+    rows.sort(key=lambda r: (r[0], r[1]))
+    out = []
+    for dets, obs, p in rows:
+        ts = " ".join([f"D{d}" for d in dets] + [f"L{o}" for o in obs])
+        out.append(f"error({p!r}) {ts}")
+    return "\n".join(out) + "\n"
+
+
+def strip_observables(text: str) -> str:
+    return "\n".join(l for l in text.splitlines() if not l.startswith("OBSERVABLE_INCLUDE")) + "\n"
+
+
+def main() -> None:
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--reference", required=True, type=Path)
+    args = ap.parse_args()
+    ref = args.reference
+    (HERE / "dems").mkdir(exist_ok=True)
+    for name in ("surface3", "surface5"):
+        for lvl in ("L0", "L1", "L2"):
+            src = ref / "data" / "dems" / f"{name}_{lvl}.dem"
+            (HERE / "dems" / f"{name}_{lvl}.dem").write_text(canonical_dem(src.read_text()))
+    circ = {}
+    for path in sorted((ref / "data" / "circuits").glob("*.stim")):
+        text = path.read_text()
+        if path.stem.startswith("surface"):
+            circ[path.stem] = {"sha256": hashlib.sha256(text.encode()).hexdigest(), "observables": True}
+        elif path.stem.startswith("bb"):
+            circ[path.stem] = {"sha256": hashlib.sha256(strip_observables(text).encode()).hexdigest(),
+                               "observables": False}
+    (HERE / "circuits.json").write_text(json.dumps(circ, indent=1, sort_keys=True) + "\n")
+    kats = {
+        "dep1_split_p1e-3": {"value": 0.00033344451858030588, "tol": 1e-15,
+                             "source": "tests/QEC/ErrorAnalysis/MixerTest.cpp:112"},
+        "dep2_split_p1e-3": {"value": 6.6697798534409714e-05, "tol": 1e-15,
+                             "source": "tests/QEC/ErrorAnalysis/MixerTest.cpp:144"},
+        "xor_merge_0.25_0.75": {"value": 0.625, "tol": 0.0,
+                                "source": "tests/QEC/ErrorAnalysis/STEPGTest.cpp:199-210"},
+    }
+    (HERE / "kats.json").write_text(json.dumps(kats, indent=1, sort_keys=True) + "\n")
+
+
+if __name__ == "__main__":
+    main()

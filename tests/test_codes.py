@@ -1,0 +1,58 @@
+"""Circuit generators against the reference's fixture circuits (data/circuits/*.stim).
+
+Surface-code circuits must match byte for byte; BB-code circuits must match on
+every line except OBSERVABLE_INCLUDE (this project computes its own logical basis).
+"""
+
+from __future__ import annotations
+
+import hashlib
+import json
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+from greenpeas_gb300.codes import BBCode, SurfaceCode
+
+CIRC = json.loads((GOLDEN / "circuits.json").read_text())
+
+
+def _strip_obs(text):
+    return "\n".join(l for l in text.splitlines() if not l.startswith("OBSERVABLE_INCLUDE")) + "\n"
+
+
+@pytest.mark.parametrize("d", [3, 5, 7, 9])
+def test_surface_matches_reference(d):
+    text = SurfaceCode(d).get_memory(rounds=d, p=0.001)
+    assert hashlib.sha256(text.encode()).hexdigest() == CIRC[f"surface{d}"]["sha256"]
+
+
+@pytest.mark.parametrize("d", [6, 10, 12])
+def test_bb_matches_reference_except_observables(d):
+    text = BBCode(d).get_memory(rounds=d, p=0.001)
+    assert hashlib.sha256(_strip_obs(text).encode()).hexdigest() == CIRC[f"bb{d}"]["sha256"]
+
+
+@pytest.mark.parametrize("d,k", [(6, 12), (10, 8), (12, 12), (18, 12)])
+def test_bb_logicals_valid(d, k):
+    c = BBCode(d)
+    n = c.num_data
+    hx = np.zeros((c.num_x, n), dtype=np.uint8)
+    for r, s in enumerate(c.x_support):
+        hx[r, s] = 1
+    assert len(c.logical_z) == k
+    for sup in c.logical_z:
+        v = np.zeros(n, dtype=np.uint8)
+        v[sup] = 1
+        assert not ((hx.astype(int) @ v) % 2).any()
+
+
+def test_uniform_noise_counts():
+    """Uniform noise: raw mechanisms = 15*CX + 3*data*rounds + 2*(resets + measurements)."""
+    from oracle import oracle as O
+    d, r = 3, 3
+    text = SurfaceCode(d).get_memory(rounds=r, p=1e-3, noise="uniform")
+    res = O.compile_text(text, 2)
+    assert res.num_raw == 15 * 4 * d * (d - 1) * r + 3 * d * d * r + 2 * ((d * d - 1) * r + d * d)
+    assert res.num_qubits == 2 * d * d - 1 and res.num_detectors == r * (d * d - 1)
