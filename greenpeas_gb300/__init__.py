@@ -1,0 +1,15 @@
+"""GB300-native detector-error-model compiler with GreenPeas' Python surface.
+
+    import greenpeas_gb300 as gp
+    driver = gp.get_driver(circuit)                  # circuit: stim.Circuit or stim text
+    dem = driver.compile_detector_error_model(circuit)
+
+See ``error_analysis`` (the compile path), ``codes`` (circuit generators) and
+``dem`` (the DEM type returned when stim is not installed).
+"""
+
+from .codes import BBCode, SurfaceCode
+from .dem import DetectorErrorModel
+from .error_analysis import CorrelationLevel, Driver, Tape, get_driver
+
+__all__ = ["BBCode", "CorrelationLevel", "DetectorErrorModel", "Driver", "SurfaceCode", "Tape", "get_driver"]

@@ -1,0 +1,107 @@
+"""ctypes binding of the C ABI in include/gpc.h (libgpc.so, built in tree).
+
+The library is loaded from ``greenpeas_gb300/_lib/libgpc.so``; if it is
+missing this module raises instead of falling back to anything else --
+run ``python -c "import __graft_entry__ as g; g.build()"`` (or
+``python greenpeas_gb300/build.py``) first.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from pathlib import Path
+
+LIB_PATH = Path(__file__).resolve().parent / "_lib" / "libgpc.so"
+
+GPC_OK = 0
+STATUS_NAMES = {
+    -1: "GPC_ERR_INVALID", -2: "GPC_ERR_PARSE", -3: "GPC_ERR_UNSUPPORTED", -4: "GPC_ERR_CUDA",
+    -5: "GPC_ERR_OOM", -6: "GPC_ERR_COLLISION", -7: "GPC_ERR_TIMEOUT", -8: "GPC_ERR_CAPACITY",
+}
+
+# every symbol include/gpc.h declares
+EXPORTS = [
+    "gpc_get_driver", "gpc_compile", "gpc_compile_batch", "gpc_dem_arrays", "gpc_dem_info",
+    "gpc_dem_text", "gpc_dem_free", "gpc_driver_destroy", "gpc_last_error", "gpc_prepare",
+    "gpc_run_device", "gpc_fetch", "gpc_driver_stream", "gpc_last_timings", "gpc_last_sizes",
+    "gpc_tape_lower", "gpc_tape_get_view", "gpc_tape_free", "gpc_tape_last_error",
+]
+
+
+class GpcError(RuntimeError):
+    """A C-ABI call returned a non-zero gpc_status."""
+
+    def __init__(self, status: int, message: str):
+        self.status = status
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("sort_bits", ctypes.c_int32), ("reserved", ctypes.c_int32 * 6)]
+
+
+class TapeView(ctypes.Structure):
+    _fields_ = [
+        ("num_qubits", ctypes.c_uint32), ("qpad", ctypes.c_uint32), ("num_measurements", ctypes.c_uint32),
+        ("num_detectors", ctypes.c_uint32), ("num_observables", ctypes.c_uint32), ("words", ctypes.c_uint32),
+        ("num_epochs", ctypes.c_uint32), ("kmax", ctypes.c_uint32), ("num_points", ctypes.c_uint32),
+        ("num_mechanisms", ctypes.c_uint32), ("num_ops", ctypes.c_uint64),
+        ("ops", ctypes.POINTER(ctypes.c_uint64)), ("ep_opoff", ctypes.POINTER(ctypes.c_uint32)),
+        ("ep_k", ctypes.POINTER(ctypes.c_uint32)), ("ep_ptoff", ctypes.POINTER(ctypes.c_uint32)),
+        ("meas_off", ctypes.POINTER(ctypes.c_uint32)), ("meas_bits", ctypes.POINTER(ctypes.c_uint32)),
+        ("inj_lo", ctypes.POINTER(ctypes.c_uint32)), ("inj_hi", ctypes.POINTER(ctypes.c_uint32)),
+        ("desc", ctypes.POINTER(ctypes.c_uint64)), ("prob", ctypes.POINTER(ctypes.c_double)),
+    ]
+
+
+_lib = None
+
+
+def lib() -> ctypes.CDLL:
+    """Loads libgpc.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise ImportError(f"{LIB_PATH} is missing: build the native library first "
+                          "(python greenpeas_gb300/build.py)")
+    L = ctypes.CDLL(str(LIB_PATH))
+    vp, sz, i32, u32 = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int32, ctypes.c_uint32
+    u32p, u64p = ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint64)
+    L.gpc_get_driver.argtypes = [ctypes.c_char_p, sz, i32, ctypes.POINTER(Options), ctypes.POINTER(vp)]
+    L.gpc_compile.argtypes = [vp, ctypes.c_char_p, sz, ctypes.POINTER(vp)]
+    L.gpc_compile_batch.argtypes = [vp, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(sz), i32, ctypes.POINTER(vp)]
+    L.gpc_dem_arrays.argtypes = [vp, ctypes.POINTER(u32p), ctypes.POINTER(u32p),
+                                 ctypes.POINTER(ctypes.POINTER(ctypes.c_double)), u32p]
+    L.gpc_dem_info.argtypes = [vp, u32p, u32p, u64p]
+    L.gpc_dem_text.argtypes = [vp, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(sz)]
+    L.gpc_dem_free.argtypes = [vp]
+    L.gpc_dem_free.restype = None
+    L.gpc_driver_destroy.argtypes = [vp]
+    L.gpc_driver_destroy.restype = None
+    L.gpc_last_error.restype = ctypes.c_char_p
+    L.gpc_prepare.argtypes = [vp, ctypes.c_char_p, sz]
+    L.gpc_run_device.argtypes = [vp]
+    L.gpc_fetch.argtypes = [vp, ctypes.POINTER(vp)]
+    L.gpc_driver_stream.argtypes = [vp]
+    L.gpc_driver_stream.restype = vp
+    L.gpc_last_timings.argtypes = [vp, ctypes.POINTER(ctypes.c_float)]
+    L.gpc_last_sizes.argtypes = [vp, u64p, u64p, u32p, u32p, u32p]
+    L.gpc_tape_lower.argtypes = [ctypes.c_char_p, sz, i32, ctypes.POINTER(vp)]
+    L.gpc_tape_get_view.argtypes = [vp, ctypes.POINTER(TapeView)]
+    L.gpc_tape_free.argtypes = [vp]
+    L.gpc_tape_free.restype = None
+    L.gpc_tape_last_error.restype = ctypes.c_char_p
+    for f in ("gpc_get_driver", "gpc_compile", "gpc_compile_batch", "gpc_dem_arrays", "gpc_dem_info",
+              "gpc_dem_text", "gpc_prepare", "gpc_run_device", "gpc_fetch", "gpc_last_timings",
+              "gpc_last_sizes", "gpc_tape_lower", "gpc_tape_get_view"):
+        getattr(L, f).restype = i32
+    _lib = L
+    return L
+
+
+def check(status: int, tape: bool = False) -> None:
+    if status != GPC_OK:
+        L = lib()
+        msg = (L.gpc_tape_last_error() if tape else L.gpc_last_error()) or b""
+        raise GpcError(status, msg.decode(errors="replace"))

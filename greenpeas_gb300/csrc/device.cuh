@@ -1,0 +1,97 @@
+// device.cuh -- structures shared by the host driver and the sm_103a kernels.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace gpc {
+
+// Device error bits (one word per pipeline run).
+enum : uint32_t {
+  DEV_ERR_TIMEOUT = 1u,    // a bounded wait (mbarrier or look-back) gave up
+  DEV_ERR_COLLISION = 2u,  // equal 128-bit keys, different symptoms
+  DEV_FLAG_MIXED = 4u,     // equal sort keys, different 128-bit keys: re-sort on 128 bits
+  DEV_FLAG_TG_OVF = 8u,    // target buffer too small: grow and re-run the merge
+};
+
+// One circuit as the kernels see it.  All arrays are device pointers.
+struct CircuitDev {
+  const uint64_t *ops;        // tape, epoch-major, [slot][qubit] inside an epoch
+  const uint32_t *ep_opoff;   // [n_epochs]
+  const uint32_t *ep_k;       // [n_epochs]
+  const uint32_t *ep_ptoff;   // [n_epochs + 1]
+  const uint32_t *meas_off;   // [nmeas + 1]
+  const uint32_t *meas_bits;  // bit indices of each measurement
+  const uint32_t *inj_lo;     // [w] first epoch injecting into word j (0xFFFFFFFF: none)
+  const uint32_t *inj_hi;     // [w] last epoch injecting into word j
+  ulonglong2 *snap;           // [w][npoints] (X row, Z row) at each point
+  uint2 *band;                // [w] point range written by the walk of word j
+  const uint64_t *desc;       // [M] mechanism descriptors
+  const double *prob;         // [M]
+  uint32_t nq, qpad, n_epochs, w;
+  uint32_t npoints, M;
+  uint32_t mech_base;  // first global mechanism index of this circuit
+  uint32_t pad_;
+};
+
+// Sizes of the sort / merge scratch for n items.
+constexpr int SORT_THREADS = 256;
+constexpr int SORT_IPT = 8;
+constexpr int SORT_TILE = SORT_THREADS * SORT_IPT;
+constexpr int RADIX_BITS = 8;
+constexpr int RADIX = 1 << RADIX_BITS;
+constexpr int MERGE_THREADS = 256;
+
+inline uint32_t sort_tiles(uint32_t n) { return (n + SORT_TILE - 1) / SORT_TILE; }
+inline uint32_t merge_tiles(uint32_t n) { return (n + MERGE_THREADS - 1) / MERGE_THREADS; }
+
+// ---- launch wrappers (defined in the .cu files) ----------------------------
+struct WalkLaunch {
+  const CircuitDev *circs;  // device array
+  const uint2 *items;       // device array of (circuit, word)
+  uint32_t n_items;
+  uint32_t threads, qpt, qpad;
+  uint32_t ring_slots, slot_bytes;
+  uint32_t *err;
+};
+cudaError_t launch_walk(const WalkLaunch &L, cudaStream_t s);
+size_t walk_smem_bytes(uint32_t qpad, uint32_t ring_slots, uint32_t slot_bytes);
+
+// Key kernel: one thread per mechanism of a single circuit.
+cudaError_t launch_keys(const CircuitDev *c_dev, uint32_t M, uint32_t w, ulonglong2 *key, uint64_t *sortkey,
+                        uint32_t *perm, cudaStream_t s);
+
+// Onesweep radix sort of (u64 key, u32 value) pairs on the low `bits` bits.
+struct SortScratch {
+  uint32_t *hist;        // [passes][RADIX]
+  uint32_t *status;      // [passes][tiles][RADIX]
+  uint32_t *tile_ctr;    // [passes]
+  uint32_t *err;
+};
+size_t sort_scratch_words(uint32_t n, uint32_t bits);
+cudaError_t launch_sort(uint64_t *keys, uint64_t *keys_alt, uint32_t *vals, uint32_t *vals_alt, uint32_t n,
+                        uint32_t bits, const SortScratch &scr, cudaStream_t s, bool *result_in_alt);
+
+// Gathers key128[perm[i]].y into out[i] (second pass of a 128-bit sort).
+cudaError_t launch_gather_hi(const ulonglong2 *key, const uint32_t *perm, uint64_t *out, uint32_t n, cudaStream_t s);
+
+struct MergeLaunch {
+  const CircuitDev *c_dev;  // single circuit
+  uint32_t w;
+  const uint32_t *perm;     // sorted mechanism ids
+  const uint64_t *sortkey;  // sorted keys (for the mixed-run check)
+  uint64_t sort_mask;       // key bits the sort compared (0: skip the mixed-run check)
+  const ulonglong2 *key;    // 128-bit key per mechanism
+  uint32_t n;
+  double *out_prob;
+  uint32_t *out_off;
+  uint32_t *out_tg;
+  uint32_t tg_cap;
+  unsigned long long *status;  // [tiles]
+  uint32_t *tile_ctr;
+  uint32_t *totals;  // [0] groups, [1] targets
+  uint32_t *err;
+};
+cudaError_t launch_merge(const MergeLaunch &L, cudaStream_t s);
+
+}  // namespace gpc

@@ -1,0 +1,611 @@
+// driver.cu -- the compile driver behind the C ABI (include/gpc.h).
+//
+// Counterpart of GreenPeas' Driver (QEC/ErrorAnalysis/Driver.hpp:37-219):
+// it owns the device buffers (one arena that grows on demand instead of the
+// reference's throw-on-overflow fitto, Driver.hpp:104-112), copies the tape
+// host -> device with one asynchronous copy from pinned memory, runs the
+// kernel pipeline on its own stream and copies back only the merged
+// mechanisms (the reference copies the whole node x 32 class matrix,
+// Driver.hpp:158-161).
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include "../../include/gpc.h"
+#include "device.cuh"
+#include "lower.hpp"
+
+using gpc::CircuitDev;
+using gpc::Tape;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+gpc_status fail(gpc_status code, const std::string &msg) {
+  g_last_error = msg;
+  return code;
+}
+
+struct CudaError : std::runtime_error {
+  explicit CudaError(const std::string &m) : std::runtime_error(m) {}
+};
+
+#define CK(x)                                                                                          \
+  do {                                                                                                 \
+    cudaError_t e_ = (x);                                                                              \
+    if (e_ != cudaSuccess) throw CudaError(std::string(#x) + ": " + cudaGetErrorString(e_));          \
+  } while (0)
+
+size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Grow-only device allocation.
+struct DevBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  void ensure(size_t bytes) {
+    if (bytes <= cap) return;
+    if (p) CK(cudaFree(p));
+    p = nullptr;
+    cap = 0;
+    size_t want = std::max(bytes, cap + cap / 2);
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e != cudaSuccess) {
+      (void)cudaGetLastError();
+      e = cudaMalloc(&p, bytes);
+      if (e != cudaSuccess) {
+        (void)cudaGetLastError();
+        throw gpc::Error(GPC_ERR_OOM, "device allocation of " + std::to_string(bytes) + " bytes failed");
+      }
+      want = bytes;
+    }
+    cap = want;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+// Grow-only pinned host allocation.
+struct HostBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  void ensure(size_t bytes) {
+    if (bytes <= cap) return;
+    if (p) CK(cudaFreeHost(p));
+    p = nullptr;
+    cap = 0;
+    size_t want = std::max(bytes, cap + cap / 2);
+    if (cudaHostAlloc(&p, want, cudaHostAllocDefault) != cudaSuccess) {
+      (void)cudaGetLastError();
+      throw gpc::Error(GPC_ERR_OOM, "pinned host allocation failed");
+    }
+    cap = want;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+  }
+};
+
+// Byte offsets of every array inside the arena (inputs first, so the whole
+// input region is one contiguous H2D copy).
+struct Layout {
+  size_t ops, ep_opoff, ep_k, ep_ptoff, meas_off, meas_bits, inj_lo, inj_hi, desc, prob, cdev, items;
+  size_t in_bytes;
+  size_t snap, band, key, sk0, sk1, pm0, pm1, hik;
+  size_t zero, err, totals, sort_scr, merge_status, merge_ctr, zero_bytes;
+  size_t out_prob, out_off;
+  size_t total;
+  uint32_t sort_tiles, merge_tiles;
+  size_t sort_words;
+};
+
+}  // namespace
+
+struct gpc_dem {
+  std::vector<double> probs;
+  std::vector<uint32_t> offsets;
+  std::vector<uint32_t> targets;
+  uint32_t num_detectors = 0, num_observables = 0;
+  uint64_t num_raw = 0;
+  std::string text;
+  bool text_ready = false;
+};
+
+struct gpc_driver {
+  int device = 0;
+  int level = 2;
+  uint32_t sort_bits = 64;
+  cudaStream_t stream = nullptr;
+  gpc::Parsed parsed;
+  Tape tape;
+  bool have_tape = false;
+  bool prepared = false;
+  bool ran = false;
+  Layout L{};
+  DevBuf arena, tgbuf;
+  HostBuf pin_in, pin_out;
+  uint32_t tg_cap = 0;
+  cudaEvent_t ev[5] = {};
+  float timings[5] = {};
+  // last run's sort result
+  uint32_t *perm_sorted = nullptr;
+  uint64_t *sk_sorted = nullptr;
+  uint64_t sort_mask = ~0ull;
+  uint32_t ring_slots = 1, slot_bytes = 0, threads = 32, qpt = 1;
+
+  ~gpc_driver() {
+    if (stream) cudaStreamSynchronize(stream);
+    arena.release();
+    tgbuf.release();
+    pin_in.release();
+    pin_out.release();
+    for (auto &e : ev)
+      if (e) cudaEventDestroy(e);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  template <typename T>
+  T *dptr(size_t off) const {
+    return reinterpret_cast<T *>(static_cast<char *>(arena.p) + off);
+  }
+
+  void layout() {
+    const Tape &T = tape;
+    const uint32_t M = (uint32_t)T.desc.size();
+    size_t o = 0;
+    auto take = [&](size_t bytes) {
+      size_t r = o;
+      o = align256(o + bytes);
+      return r;
+    };
+    L.ops = take(T.ops.size() * 8);
+    L.ep_opoff = take(T.ep_opoff.size() * 4);
+    L.ep_k = take(T.ep_k.size() * 4);
+    L.ep_ptoff = take(T.ep_ptoff.size() * 4);
+    L.meas_off = take(T.meas_off.size() * 4);
+    L.meas_bits = take(T.meas_bits.size() * 4);
+    L.inj_lo = take(T.inj_lo.size() * 4);
+    L.inj_hi = take(T.inj_hi.size() * 4);
+    L.desc = take((size_t)M * 8);
+    L.prob = take((size_t)M * 8);
+    L.cdev = take(sizeof(CircuitDev));
+    L.items = take((size_t)T.w * sizeof(uint2));
+    L.in_bytes = o;
+    L.snap = take((size_t)T.w * T.npoints * 16);
+    L.band = take((size_t)T.w * 8);
+    L.key = take((size_t)M * 16);
+    L.sk0 = take((size_t)M * 8);
+    L.sk1 = take((size_t)M * 8);
+    L.pm0 = take((size_t)M * 4);
+    L.pm1 = take((size_t)M * 4);
+    L.hik = take((size_t)M * 8);
+    L.sort_tiles = gpc::sort_tiles(M);
+    L.merge_tiles = gpc::merge_tiles(M);
+    L.sort_words = gpc::sort_scratch_words(M, 64);
+    L.zero = o;
+    L.err = take(4);
+    L.totals = take(8);
+    L.sort_scr = take(L.sort_words * 4);
+    L.merge_status = take((size_t)L.merge_tiles * 8);
+    L.merge_ctr = take(4);
+    L.zero_bytes = o - L.zero;
+    L.out_prob = take((size_t)M * 8);
+    L.out_off = take((size_t)(M + 1) * 4);
+    L.total = o;
+  }
+
+  void stage_inputs() {
+    const Tape &T = tape;
+    pin_in.ensure(L.in_bytes);
+    char *h = static_cast<char *>(pin_in.p);
+    auto put = [&](size_t off, const void *src, size_t bytes) {
+      if (bytes) memcpy(h + off, src, bytes);
+    };
+    put(L.ops, T.ops.data(), T.ops.size() * 8);
+    put(L.ep_opoff, T.ep_opoff.data(), T.ep_opoff.size() * 4);
+    put(L.ep_k, T.ep_k.data(), T.ep_k.size() * 4);
+    put(L.ep_ptoff, T.ep_ptoff.data(), T.ep_ptoff.size() * 4);
+    put(L.meas_off, T.meas_off.data(), T.meas_off.size() * 4);
+    put(L.meas_bits, T.meas_bits.data(), T.meas_bits.size() * 4);
+    put(L.inj_lo, T.inj_lo.data(), T.inj_lo.size() * 4);
+    put(L.inj_hi, T.inj_hi.data(), T.inj_hi.size() * 4);
+    put(L.desc, T.desc.data(), T.desc.size() * 8);
+    put(L.prob, T.prob.data(), T.prob.size() * 8);
+    CircuitDev c{};
+    c.ops = dptr<uint64_t>(L.ops);
+    c.ep_opoff = dptr<uint32_t>(L.ep_opoff);
+    c.ep_k = dptr<uint32_t>(L.ep_k);
+    c.ep_ptoff = dptr<uint32_t>(L.ep_ptoff);
+    c.meas_off = dptr<uint32_t>(L.meas_off);
+    c.meas_bits = dptr<uint32_t>(L.meas_bits);
+    c.inj_lo = dptr<uint32_t>(L.inj_lo);
+    c.inj_hi = dptr<uint32_t>(L.inj_hi);
+    c.snap = dptr<ulonglong2>(L.snap);
+    c.band = dptr<uint2>(L.band);
+    c.desc = dptr<uint64_t>(L.desc);
+    c.prob = dptr<double>(L.prob);
+    c.nq = T.nq;
+    c.qpad = T.qpad;
+    c.n_epochs = T.n_epochs;
+    c.w = T.w;
+    c.npoints = T.npoints;
+    c.M = (uint32_t)T.desc.size();
+    c.mech_base = 0;
+    put(L.cdev, &c, sizeof(c));
+    std::vector<uint2> items(T.w);
+    for (uint32_t j = 0; j < T.w; ++j) items[j] = make_uint2(0u, j);
+    put(L.items, items.data(), items.size() * sizeof(uint2));
+  }
+
+  void prepare(const char *text, size_t len) {
+    CK(cudaSetDevice(device));
+    prepared = false;
+    ran = false;
+    if (text) {
+      parsed = gpc::parse_stim(text, len);
+      gpc::LowerOptions lo;
+      lo.level = level;
+      tape = gpc::lower(parsed, lo);
+      have_tape = true;
+    } else if (!have_tape) {
+      throw gpc::Error(GPC_ERR_INVALID, "no circuit to compile");
+    }
+    layout();
+    // The stream may still be reading the old arena: finish before regrowing.
+    CK(cudaStreamSynchronize(stream));
+    arena.ensure(L.total);
+    const uint32_t M = (uint32_t)tape.desc.size();
+    uint32_t want_tg = std::max<uint32_t>(1024u, std::min<uint64_t>(0xFFFFFFF0ull, (uint64_t)M * 16));
+    if (want_tg > tg_cap) {
+      tgbuf.ensure((size_t)want_tg * 4);
+      tg_cap = want_tg;
+    }
+    stage_inputs();
+    CK(cudaMemcpyAsync(arena.p, pin_in.p, L.in_bytes, cudaMemcpyHostToDevice, stream));
+    // walk launch geometry
+    qpt = tape.qpad <= 1024 ? 1 : tape.qpad <= 2048 ? 2 : 4;
+    threads = tape.qpad / qpt;
+    slot_bytes = std::max<uint32_t>(1, tape.kmax) * tape.qpad * 8;
+    const size_t budget = 200 * 1024;
+    const size_t fixed = (size_t)2 * tape.qpad * 16 + 128;
+    size_t slots = budget > fixed ? (budget - fixed) / slot_bytes : 0;
+    if (slots < 1) throw gpc::Error(GPC_ERR_CAPACITY, "tape epoch too large for shared memory");
+    ring_slots = (uint32_t)std::min<size_t>(8, slots);
+    prepared = true;
+  }
+
+  void run() {
+    if (!prepared) throw gpc::Error(GPC_ERR_INVALID, "no circuit prepared");
+    CK(cudaSetDevice(device));
+    const Tape &T = tape;
+    const uint32_t M = (uint32_t)T.desc.size();
+    CK(cudaMemsetAsync(dptr<char>(L.zero), 0, L.zero_bytes, stream));
+    CK(cudaEventRecord(ev[0], stream));
+    gpc::WalkLaunch wl{};
+    wl.circs = dptr<CircuitDev>(L.cdev);
+    wl.items = dptr<uint2>(L.items);
+    wl.n_items = T.w;
+    wl.threads = threads;
+    wl.qpt = qpt;
+    wl.qpad = T.qpad;
+    wl.ring_slots = ring_slots;
+    wl.slot_bytes = slot_bytes;
+    wl.err = dptr<uint32_t>(L.err);
+    if (T.n_epochs > 0) CK(gpc::launch_walk(wl, stream));
+    else CK(cudaMemsetAsync(dptr<char>(L.band), 0, (size_t)T.w * 8, stream));
+    CK(cudaEventRecord(ev[1], stream));
+    CK(gpc::launch_keys(dptr<CircuitDev>(L.cdev), M, T.w, dptr<ulonglong2>(L.key), dptr<uint64_t>(L.sk0),
+                        dptr<uint32_t>(L.pm0), stream));
+    CK(cudaEventRecord(ev[2], stream));
+    sort_and_merge(false);
+    ran = true;
+  }
+
+  // Sorts (on sort_bits, or on the full 128-bit key when `full`) and merges.
+  void sort_and_merge(bool full) {
+    const uint32_t M = (uint32_t)tape.desc.size();
+    uint32_t *sw = dptr<uint32_t>(L.sort_scr);
+    const uint32_t passes = 8;
+    const size_t one = (size_t)passes * gpc::RADIX + (size_t)passes * L.sort_tiles * gpc::RADIX + passes;
+    gpc::SortScratch s1{sw, sw + passes * gpc::RADIX, sw + passes * gpc::RADIX + (size_t)passes * L.sort_tiles * gpc::RADIX,
+                        dptr<uint32_t>(L.err)};
+    gpc::SortScratch s2{sw + one, sw + one + passes * gpc::RADIX,
+                        sw + one + passes * gpc::RADIX + (size_t)passes * L.sort_tiles * gpc::RADIX, dptr<uint32_t>(L.err)};
+    uint64_t *k0 = dptr<uint64_t>(L.sk0), *k1 = dptr<uint64_t>(L.sk1);
+    uint32_t *p0 = dptr<uint32_t>(L.pm0), *p1 = dptr<uint32_t>(L.pm1);
+    bool alt = false;
+    CK(gpc::launch_sort(k0, k1, p0, p1, M, full ? 64 : sort_bits, s1, stream, &alt));
+    uint64_t *ks = alt ? k1 : k0;
+    uint32_t *ps = alt ? p1 : p0;
+    if (full) {
+      // second key: the high 64 bits, gathered in the current order, sorted stably
+      uint64_t *hk = dptr<uint64_t>(L.hik);
+      uint64_t *hk_alt = alt ? k0 : k1;
+      uint32_t *ps_alt = alt ? p0 : p1;
+      CK(gpc::launch_gather_hi(dptr<ulonglong2>(L.key), ps, hk, M, stream));
+      bool alt2 = false;
+      CK(gpc::launch_sort(hk, hk_alt, ps, ps_alt, M, 64, s2, stream, &alt2));
+      ks = alt2 ? hk_alt : hk;
+      ps = alt2 ? ps_alt : ps;
+    }
+    perm_sorted = ps;
+    sk_sorted = ks;
+    const uint32_t b = full ? 0 : sort_bits;
+    sort_mask = b == 0 ? 0ull : (b >= 64 ? ~0ull : ((1ull << b) - 1));
+    CK(cudaEventRecord(ev[3], stream));
+    launch_merge_now();
+    CK(cudaEventRecord(ev[4], stream));
+  }
+
+  void launch_merge_now() {
+    const uint32_t M = (uint32_t)tape.desc.size();
+    gpc::MergeLaunch ml{};
+    ml.c_dev = dptr<CircuitDev>(L.cdev);
+    ml.w = tape.w;
+    ml.perm = perm_sorted;
+    ml.sortkey = sk_sorted;
+    ml.sort_mask = sort_mask;
+    ml.key = dptr<ulonglong2>(L.key);
+    ml.n = M;
+    ml.out_prob = dptr<double>(L.out_prob);
+    ml.out_off = dptr<uint32_t>(L.out_off);
+    ml.out_tg = static_cast<uint32_t *>(tgbuf.p);
+    ml.tg_cap = tg_cap;
+    ml.status = dptr<unsigned long long>(L.merge_status);
+    ml.tile_ctr = dptr<uint32_t>(L.merge_ctr);
+    ml.totals = dptr<uint32_t>(L.totals);
+    ml.err = dptr<uint32_t>(L.err);
+    CK(gpc::launch_merge(ml, stream));
+  }
+
+  void reset_merge_scratch() {
+    CK(cudaMemsetAsync(dptr<char>(L.merge_status), 0, (size_t)L.merge_tiles * 8, stream));
+    CK(cudaMemsetAsync(dptr<char>(L.merge_ctr), 0, 4, stream));
+    CK(cudaMemsetAsync(dptr<char>(L.totals), 0, 8, stream));
+  }
+
+  // Reads flags and totals; handles the rare re-sort / target-buffer growth.
+  void finish(uint32_t *groups, uint32_t *targets) {
+    pin_out.ensure(64);
+    uint32_t *h = static_cast<uint32_t *>(pin_out.p);
+    bool did_full = false;
+    for (int attempt = 0; attempt < 4; ++attempt) {
+      CK(cudaMemcpyAsync(h, dptr<char>(L.err), 4, cudaMemcpyDeviceToHost, stream));
+      CK(cudaMemcpyAsync(h + 1, dptr<char>(L.totals), 8, cudaMemcpyDeviceToHost, stream));
+      CK(cudaStreamSynchronize(stream));
+      const uint32_t err = h[0];
+      if (err & gpc::DEV_ERR_TIMEOUT) throw gpc::Error(GPC_ERR_TIMEOUT, "a bounded device wait timed out");
+      if (err & gpc::DEV_ERR_COLLISION)
+        throw gpc::Error(GPC_ERR_COLLISION, "two different symptoms share a 128-bit key");
+      if ((err & gpc::DEV_FLAG_MIXED) && !did_full) {
+        // equal sort keys with different full keys: sort on all 128 bits
+        CK(cudaMemsetAsync(dptr<char>(L.zero), 0, L.zero_bytes, stream));
+        sort_and_merge(true);
+        did_full = true;
+        continue;
+      }
+      if (err & gpc::DEV_FLAG_TG_OVF) {
+        const uint32_t need = h[2];
+        tgbuf.ensure((size_t)need * 4 + 1024);
+        tg_cap = (uint32_t)std::min<size_t>(0xFFFFFFF0ull, tgbuf.cap / 4);
+        CK(cudaMemsetAsync(dptr<char>(L.err), 0, 4, stream));
+        reset_merge_scratch();
+        launch_merge_now();
+        continue;
+      }
+      const uint32_t M = (uint32_t)tape.desc.size();
+      if (h[1] > M || h[2] > tg_cap) throw gpc::Error(GPC_ERR_CUDA, "inconsistent merge totals");
+      *groups = h[1];
+      *targets = h[2];
+      return;
+    }
+    throw gpc::Error(GPC_ERR_CUDA, "merge did not converge");
+  }
+
+  gpc_dem *fetch() {
+    if (!ran) throw gpc::Error(GPC_ERR_INVALID, "nothing has been run");
+    CK(cudaSetDevice(device));
+    uint32_t C = 0, NT = 0;
+    finish(&C, &NT);
+    auto dem = std::make_unique<gpc_dem>();
+    dem->num_detectors = tape.ndet;
+    dem->num_observables = tape.nobs;
+    dem->num_raw = tape.desc.size();
+    const size_t bytes = (size_t)C * 8 + (size_t)C * 4 + (size_t)NT * 4 + 64;
+    pin_out.ensure(bytes);
+    char *h = static_cast<char *>(pin_out.p);
+    if (C) {
+      CK(cudaMemcpyAsync(h, dptr<char>(L.out_prob), (size_t)C * 8, cudaMemcpyDeviceToHost, stream));
+      CK(cudaMemcpyAsync(h + (size_t)C * 8, dptr<char>(L.out_off), (size_t)C * 4, cudaMemcpyDeviceToHost, stream));
+    }
+    if (NT) CK(cudaMemcpyAsync(h + (size_t)C * 12, tgbuf.p, (size_t)NT * 4, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    dem->probs.assign(reinterpret_cast<double *>(h), reinterpret_cast<double *>(h) + C);
+    dem->offsets.resize((size_t)C + 1);
+    memcpy(dem->offsets.data(), h + (size_t)C * 8, (size_t)C * 4);
+    dem->offsets[C] = NT;
+    dem->targets.assign(reinterpret_cast<uint32_t *>(h + (size_t)C * 12),
+                        reinterpret_cast<uint32_t *>(h + (size_t)C * 12) + NT);
+    return dem.release();
+  }
+};
+
+namespace {
+
+template <typename F>
+gpc_status guarded(F &&f) {
+  try {
+    f();
+    g_last_error.clear();
+    return GPC_OK;
+  } catch (const gpc::Error &e) {
+    return fail(e.code, e.what());
+  } catch (const CudaError &e) {
+    return fail(GPC_ERR_CUDA, e.what());
+  } catch (const std::bad_alloc &) {
+    return fail(GPC_ERR_OOM, "host allocation failed");
+  } catch (const std::exception &e) {
+    return fail(GPC_ERR_INVALID, e.what());
+  }
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *gpc_last_error(void) { return g_last_error.c_str(); }
+
+gpc_status gpc_get_driver(const char *stim_text, size_t len, int32_t correlation_level, const gpc_options *options,
+                          gpc_driver **out) {
+  if (!out) return fail(GPC_ERR_INVALID, "out is null");
+  *out = nullptr;
+  if (!stim_text) return fail(GPC_ERR_INVALID, "circuit text is null");
+  if (correlation_level < 0 || correlation_level > 2) return fail(GPC_ERR_INVALID, "correlation level must be 0, 1 or 2");
+  std::unique_ptr<gpc_driver> d(new (std::nothrow) gpc_driver());
+  if (!d) return fail(GPC_ERR_OOM, "host allocation failed");
+  d->level = correlation_level;
+  if (options) {
+    d->device = options->device;
+    if (options->sort_bits < 0 || options->sort_bits > 64) return fail(GPC_ERR_INVALID, "sort_bits must be in 0..64");
+    if (options->sort_bits) d->sort_bits = (uint32_t)options->sort_bits;
+  }
+  gpc_status st = guarded([&] {
+    int n = 0;
+    CK(cudaGetDeviceCount(&n));
+    if (d->device < 0 || d->device >= n) throw gpc::Error(GPC_ERR_CUDA, "no such CUDA device");
+    CK(cudaSetDevice(d->device));
+    CK(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking));
+    for (auto &e : d->ev) CK(cudaEventCreate(&e));
+    d->prepare(stim_text, len);
+  });
+  if (st != GPC_OK) return st;
+  *out = d.release();
+  return GPC_OK;
+}
+
+gpc_status gpc_prepare(gpc_driver *driver, const char *stim_text, size_t len) {
+  if (!driver) return fail(GPC_ERR_INVALID, "driver is null");
+  return guarded([&] { driver->prepare(stim_text, len); });
+}
+
+gpc_status gpc_run_device(gpc_driver *driver) {
+  if (!driver) return fail(GPC_ERR_INVALID, "driver is null");
+  return guarded([&] { driver->run(); });
+}
+
+gpc_status gpc_fetch(gpc_driver *driver, gpc_dem **out) {
+  if (!driver || !out) return fail(GPC_ERR_INVALID, "null argument");
+  *out = nullptr;
+  return guarded([&] { *out = driver->fetch(); });
+}
+
+gpc_status gpc_compile(gpc_driver *driver, const char *stim_text, size_t len, gpc_dem **out) {
+  if (!driver || !out) return fail(GPC_ERR_INVALID, "null argument");
+  *out = nullptr;
+  return guarded([&] {
+    if (stim_text || !driver->prepared) driver->prepare(stim_text, len);
+    else driver->prepare(nullptr, 0);  // re-upload the parsed circuit, as the reference re-copies it
+    driver->run();
+    *out = driver->fetch();
+  });
+}
+
+gpc_status gpc_compile_batch(gpc_driver *driver, const char *const *texts, const size_t *lens, int32_t n,
+                             gpc_dem **outs) {
+  if (!driver || !texts || !lens || !outs || n < 0) return fail(GPC_ERR_INVALID, "null argument");
+  for (int32_t i = 0; i < n; ++i) outs[i] = nullptr;
+  for (int32_t i = 0; i < n; ++i) {
+    gpc_status st = gpc_compile(driver, texts[i], lens[i], &outs[i]);
+    if (st != GPC_OK) {
+      for (int32_t k = 0; k < i; ++k) {
+        gpc_dem_free(outs[k]);
+        outs[k] = nullptr;
+      }
+      return st;
+    }
+  }
+  return GPC_OK;
+}
+
+gpc_status gpc_dem_arrays(const gpc_dem *dem, const uint32_t **offsets, const uint32_t **targets, const double **probs,
+                          uint32_t *num_errors) {
+  if (!dem) return fail(GPC_ERR_INVALID, "dem is null");
+  if (offsets) *offsets = dem->offsets.data();
+  if (targets) *targets = dem->targets.data();
+  if (probs) *probs = dem->probs.data();
+  if (num_errors) *num_errors = (uint32_t)dem->probs.size();
+  return GPC_OK;
+}
+
+gpc_status gpc_dem_info(const gpc_dem *dem, uint32_t *num_detectors, uint32_t *num_observables,
+                        uint64_t *num_raw_mechanisms) {
+  if (!dem) return fail(GPC_ERR_INVALID, "dem is null");
+  if (num_detectors) *num_detectors = dem->num_detectors;
+  if (num_observables) *num_observables = dem->num_observables;
+  if (num_raw_mechanisms) *num_raw_mechanisms = dem->num_raw;
+  return GPC_OK;
+}
+
+gpc_status gpc_dem_text(const gpc_dem *dem_c, const char **text, size_t *len) {
+  if (!dem_c || !text) return fail(GPC_ERR_INVALID, "null argument");
+  gpc_dem *dem = const_cast<gpc_dem *>(dem_c);
+  return guarded([&] {
+    if (!dem->text_ready) {
+      std::string s;
+      s.reserve(dem->probs.size() * 48);
+      char buf[64];
+      for (size_t i = 0; i < dem->probs.size(); ++i) {
+        int n = snprintf(buf, sizeof buf, "error(%.17g)", dem->probs[i]);
+        s.append(buf, (size_t)n);
+        for (uint32_t k = dem->offsets[i]; k < dem->offsets[i + 1]; ++k) {
+          uint32_t t = dem->targets[k];
+          n = t < dem->num_detectors ? snprintf(buf, sizeof buf, " D%u", t)
+                                     : snprintf(buf, sizeof buf, " L%u", t - dem->num_detectors);
+          s.append(buf, (size_t)n);
+        }
+        s.push_back('\n');
+      }
+      dem->text = std::move(s);
+      dem->text_ready = true;
+    }
+    *text = dem->text.c_str();
+    if (len) *len = dem->text.size();
+  });
+}
+
+void gpc_dem_free(gpc_dem *dem) { delete dem; }
+
+void gpc_driver_destroy(gpc_driver *driver) { delete driver; }
+
+void *gpc_driver_stream(gpc_driver *driver) { return driver ? (void *)driver->stream : nullptr; }
+
+gpc_status gpc_last_timings(gpc_driver *driver, float *ms5) {
+  if (!driver || !ms5) return fail(GPC_ERR_INVALID, "null argument");
+  if (!driver->ran) return fail(GPC_ERR_INVALID, "nothing has been run");
+  return guarded([&] {
+    CK(cudaEventSynchronize(driver->ev[4]));
+    for (int i = 0; i < 4; ++i) CK(cudaEventElapsedTime(&ms5[i], driver->ev[i], driver->ev[i + 1]));
+    CK(cudaEventElapsedTime(&ms5[4], driver->ev[0], driver->ev[4]));
+  });
+}
+
+gpc_status gpc_last_sizes(gpc_driver *driver, uint64_t *raw, uint64_t *points, uint32_t *epochs, uint32_t *words,
+                          uint32_t *qubits) {
+  if (!driver) return fail(GPC_ERR_INVALID, "driver is null");
+  if (raw) *raw = driver->tape.desc.size();
+  if (points) *points = driver->tape.npoints;
+  if (epochs) *epochs = driver->tape.n_epochs;
+  if (words) *words = driver->tape.w;
+  if (qubits) *qubits = driver->tape.nq;
+  return GPC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,662 @@
+// lower.cpp -- stim text parser and the tick-tape lowering (see lower.hpp).
+#include "lower.hpp"
+
+#include <algorithm>
+#include <cctype>
+#include <cmath>
+#include <cstdlib>
+#include <cstring>
+#include <string_view>
+#include <unordered_map>
+
+#include "../../include/gpc.h"
+
+namespace gpc {
+namespace {
+
+enum Kind : uint8_t { G_NOP, G_TICK, G_DET, G_OBS, G_PAULI, G_C1, G_C2, G_M, G_MR, G_R, G_N1, G_N2, G_CORR, G_MPAD };
+enum { N1_X, N1_Y, N1_Z, N1_DEP1, N1_PC1 };
+
+// Pauli masks: bit0 = X, bit1 = Z.  Two-qubit masks: bit0 Xa, bit1 Za, bit2 Xb, bit3 Zb.
+struct Gate {
+  const char *name;
+  Kind kind;
+  uint8_t a, b;       // C1: image masks of X and Z;  M/MR/R: basis;  N1: channel
+  uint8_t img[4];     // C2: images of Xa, Za, Xb, Zb
+  uint8_t nargs_min, nargs_max;
+};
+
+constexpr uint8_t XA = 1, ZA = 2, XB = 4, ZB = 8;
+
+const Gate kGates[] = {
+    {"TICK", G_TICK, 0, 0, {}, 0, 0},
+    {"DETECTOR", G_DET, 0, 0, {}, 0, 255},
+    {"OBSERVABLE_INCLUDE", G_OBS, 0, 0, {}, 1, 1},
+    {"QUBIT_COORDS", G_NOP, 0, 0, {}, 0, 255},
+    {"SHIFT_COORDS", G_NOP, 0, 0, {}, 0, 255},
+    {"MPAD", G_MPAD, 0, 0, {}, 0, 1},
+    {"I", G_PAULI, 0, 0, {}, 0, 0},
+    {"X", G_PAULI, 0, 0, {}, 0, 0},
+    {"Y", G_PAULI, 0, 0, {}, 0, 0},
+    {"Z", G_PAULI, 0, 0, {}, 0, 0},
+    {"H", G_C1, 2, 1, {}, 0, 0},
+    {"H_XZ", G_C1, 2, 1, {}, 0, 0},
+    {"H_XY", G_C1, 3, 2, {}, 0, 0},
+    {"H_YZ", G_C1, 1, 3, {}, 0, 0},
+    {"S", G_C1, 3, 2, {}, 0, 0},
+    {"SQRT_Z", G_C1, 3, 2, {}, 0, 0},
+    {"S_DAG", G_C1, 3, 2, {}, 0, 0},
+    {"SQRT_Z_DAG", G_C1, 3, 2, {}, 0, 0},
+    {"SQRT_X", G_C1, 1, 3, {}, 0, 0},
+    {"SQRT_X_DAG", G_C1, 1, 3, {}, 0, 0},
+    {"SQRT_Y", G_C1, 2, 1, {}, 0, 0},
+    {"SQRT_Y_DAG", G_C1, 2, 1, {}, 0, 0},
+    {"C_XYZ", G_C1, 3, 1, {}, 0, 0},
+    {"C_ZYX", G_C1, 2, 3, {}, 0, 0},
+    {"CX", G_C2, 0, 0, {XA | XB, ZA, XB, ZA | ZB}, 0, 0},
+    {"CNOT", G_C2, 0, 0, {XA | XB, ZA, XB, ZA | ZB}, 0, 0},
+    {"ZCX", G_C2, 0, 0, {XA | XB, ZA, XB, ZA | ZB}, 0, 0},
+    {"CZ", G_C2, 0, 0, {XA | ZB, ZA, ZA | XB, ZB}, 0, 0},
+    {"ZCZ", G_C2, 0, 0, {XA | ZB, ZA, ZA | XB, ZB}, 0, 0},
+    {"CY", G_C2, 0, 0, {XA | XB | ZB, ZA, ZA | XB, ZA | ZB}, 0, 0},
+    {"ZCY", G_C2, 0, 0, {XA | XB | ZB, ZA, ZA | XB, ZA | ZB}, 0, 0},
+    {"XCZ", G_C2, 0, 0, {XA, ZA | ZB, XA | XB, ZB}, 0, 0},
+    {"XCX", G_C2, 0, 0, {XA, ZA | XB, XB, XA | ZB}, 0, 0},
+    {"SWAP", G_C2, 0, 0, {XB, ZB, XA, ZA}, 0, 0},
+    {"M", G_M, 0, 0, {}, 0, 1},
+    {"MZ", G_M, 0, 0, {}, 0, 1},
+    {"MX", G_M, 1, 0, {}, 0, 1},
+    {"MY", G_M, 2, 0, {}, 0, 1},
+    {"MR", G_MR, 0, 0, {}, 0, 1},
+    {"MRZ", G_MR, 0, 0, {}, 0, 1},
+    {"MRX", G_MR, 1, 0, {}, 0, 1},
+    {"MRY", G_MR, 2, 0, {}, 0, 1},
+    {"R", G_R, 0, 0, {}, 0, 0},
+    {"RZ", G_R, 0, 0, {}, 0, 0},
+    {"RX", G_R, 1, 0, {}, 0, 0},
+    {"RY", G_R, 2, 0, {}, 0, 0},
+    {"X_ERROR", G_N1, N1_X, 0, {}, 1, 1},
+    {"Y_ERROR", G_N1, N1_Y, 0, {}, 1, 1},
+    {"Z_ERROR", G_N1, N1_Z, 0, {}, 1, 1},
+    {"DEPOLARIZE1", G_N1, N1_DEP1, 0, {}, 1, 1},
+    {"PAULI_CHANNEL_1", G_N1, N1_PC1, 0, {}, 3, 3},
+    {"DEPOLARIZE2", G_N2, 0, 0, {}, 1, 1},
+    {"E", G_CORR, 0, 0, {}, 1, 1},
+    {"CORRELATED_ERROR", G_CORR, 0, 0, {}, 1, 1},
+};
+constexpr int kNumGates = sizeof(kGates) / sizeof(kGates[0]);
+
+const std::unordered_map<std::string_view, int> &gateIndex() {
+  static const std::unordered_map<std::string_view, int> m = [] {
+    std::unordered_map<std::string_view, int> r;
+    for (int i = 0; i < kNumGates; ++i) r.emplace(kGates[i].name, i);
+    return r;
+  }();
+  return m;
+}
+
+// Target encoding in the pool: qubit q -> q; rec[-k] -> kRec | k;
+// Pauli target P q -> kPau | P << 24 | q (P: 1 X, 2 Z, 3 Y).
+constexpr uint32_t kRec = 0x80000000u;
+constexpr uint32_t kPau = 0x40000000u;
+constexpr uint32_t kMaxQubit = 1u << 24;
+
+struct TextParser {
+  const char *s, *e;
+  size_t line = 1;
+  Parsed *out;
+
+  [[noreturn]] void fail(int code, const std::string &m) { throw Error(code, "line " + std::to_string(line) + ": " + m); }
+  void sp() {
+    while (s < e && (*s == ' ' || *s == '\t' || *s == '\r')) ++s;
+  }
+  uint32_t uint() {
+    if (s >= e || *s < '0' || *s > '9') fail(GPC_ERR_PARSE, "expected an integer");
+    uint64_t v = 0;
+    while (s < e && *s >= '0' && *s <= '9') {
+      v = v * 10 + (uint64_t)(*s++ - '0');
+      if (v > 0xFFFFFFFull) fail(GPC_ERR_PARSE, "integer out of range");
+    }
+    return (uint32_t)v;
+  }
+
+  // Parses statements into `dst` until '}' or the end of the text.
+  void block(std::vector<Instr> &dst, bool inner, int depth) {
+    if (depth > 64) fail(GPC_ERR_PARSE, "REPEAT nesting too deep");
+    char name[40];
+    while (true) {
+      sp();
+      if (s >= e) {
+        if (inner) fail(GPC_ERR_PARSE, "unterminated REPEAT block");
+        return;
+      }
+      char c = *s;
+      if (c == '\n') {
+        ++s;
+        ++line;
+        continue;
+      }
+      if (c == '#') {
+        while (s < e && *s != '\n') ++s;
+        continue;
+      }
+      if (c == '}') {
+        if (!inner) fail(GPC_ERR_PARSE, "unmatched '}'");
+        ++s;
+        return;
+      }
+      size_t n = 0;
+      while (s < e && (isalnum((unsigned char)*s) || *s == '_')) {
+        if (n + 1 >= sizeof(name)) fail(GPC_ERR_PARSE, "instruction name too long");
+        name[n++] = (char)toupper((unsigned char)*s++);
+      }
+      name[n] = 0;
+      if (n == 0) fail(GPC_ERR_PARSE, std::string("unexpected character '") + c + "'");
+      if (s < e && *s == '[') {  // tag: ignored
+        while (s < e && *s != ']' && *s != '\n') ++s;
+        if (s >= e || *s != ']') fail(GPC_ERR_PARSE, "unterminated tag");
+        ++s;
+      }
+      std::string_view nv(name, n);
+      if (nv == "REPEAT") {
+        sp();
+        uint32_t reps = uint();
+        sp();
+        if (s >= e || *s != '{') fail(GPC_ERR_PARSE, "expected '{' after REPEAT count");
+        ++s;
+        std::vector<Instr> body;
+        block(body, true, depth + 1);
+        if ((uint64_t)reps * body.size() + dst.size() > (1ull << 31)) fail(GPC_ERR_CAPACITY, "circuit too long");
+        dst.reserve(dst.size() + (size_t)reps * body.size());
+        for (uint32_t r = 0; r < reps; ++r) dst.insert(dst.end(), body.begin(), body.end());
+        continue;
+      }
+      auto it = gateIndex().find(nv);
+      if (it == gateIndex().end()) fail(GPC_ERR_UNSUPPORTED, "unsupported instruction " + std::string(nv));
+      const Gate &g = kGates[it->second];
+      Instr in{};
+      in.gate = (uint16_t)it->second;
+      double args[3];
+      int na = 0;
+      if (s < e && *s == '(') {
+        ++s;
+        while (true) {
+          sp();
+          char *endp = nullptr;
+          double v = strtod(s, &endp);
+          if (endp == s) fail(GPC_ERR_PARSE, "bad argument");
+          s = endp;
+          if (na < 3) args[na] = v;
+          ++na;
+          sp();
+          if (s < e && *s == ',') {
+            ++s;
+            continue;
+          }
+          if (s < e && *s == ')') {
+            ++s;
+            break;
+          }
+          fail(GPC_ERR_PARSE, "bad argument list");
+        }
+      }
+      if (g.nargs_max != 255 && (na < g.nargs_min || na > g.nargs_max))
+        fail(GPC_ERR_PARSE, std::string(g.name) + ": wrong number of arguments");
+      in.nargs = (uint8_t)std::min(na, 3);
+      for (int i = 0; i < in.nargs; ++i) in.args[i] = args[i];
+      in.t0 = (uint32_t)out->pool.size();
+      while (true) {
+        sp();
+        if (s >= e || *s == '\n' || *s == '#') break;
+        if (*s == '!') ++s;  // inverted measurement result: no effect on sensitivities
+        if (s >= e) fail(GPC_ERR_PARSE, "bad target");
+        if (*s == '*') fail(GPC_ERR_UNSUPPORTED, "combiner targets are not supported");
+        if (e - s >= 4 && memcmp(s, "rec[", 4) == 0) {
+          s += 4;
+          if (s >= e || *s != '-') fail(GPC_ERR_PARSE, "expected rec[-k]");
+          ++s;
+          uint32_t k = uint();
+          if (s >= e || *s != ']' || k == 0) fail(GPC_ERR_PARSE, "bad record target");
+          ++s;
+          out->pool.push_back(kRec | k);
+        } else if (*s == 'X' || *s == 'Y' || *s == 'Z' || *s == 'x' || *s == 'y' || *s == 'z') {
+          char p = (char)toupper((unsigned char)*s++);
+          uint32_t q = uint();
+          if (q >= kMaxQubit) fail(GPC_ERR_CAPACITY, "qubit index too large");
+          out->pool.push_back(kPau | ((uint32_t)(p == 'X' ? 1 : p == 'Z' ? 2 : 3) << 24) | q);
+        } else if (*s >= '0' && *s <= '9') {
+          uint32_t q = uint();
+          if (q >= kMaxQubit) fail(GPC_ERR_CAPACITY, "qubit index too large");
+          out->pool.push_back(q);
+        } else if (e - s >= 6 && memcmp(s, "sweep[", 6) == 0) {
+          fail(GPC_ERR_UNSUPPORTED, "sweep targets are not supported");
+        } else {
+          fail(GPC_ERR_PARSE, "bad target");
+        }
+      }
+      in.tn = (uint32_t)out->pool.size() - in.t0;
+      dst.push_back(in);
+    }
+  }
+};
+
+double split_dep1(double p) { return 0.5 - 0.5 * std::sqrt(1.0 - (4.0 * p) / 3.0); }
+double split_dep2(double p) { return 0.5 - 0.5 * std::pow(1.0 - (16.0 * p) / 15.0, 0.125); }
+
+// Independent X, Y, Z probabilities equivalent to the disjoint channel
+// (px, py, pz): with lambda_P = 1 - 2 P(anticommuting with P), independent
+// channels give lambda_X = (1-2qy)(1-2qz), so 1-2qx = sqrt(lambda_Y lambda_Z / lambda_X).
+bool pc1_independent(double px, double py, double pz, double q[3]) {
+  double lx = 1 - 2 * (py + pz), ly = 1 - 2 * (px + pz), lz = 1 - 2 * (px + py);
+  if (lx <= 0 || ly <= 0 || lz <= 0) return false;
+  q[0] = 0.5 - 0.5 * std::sqrt(ly * lz / lx);
+  q[1] = 0.5 - 0.5 * std::sqrt(lx * lz / ly);
+  q[2] = 0.5 - 0.5 * std::sqrt(lx * ly / lz);
+  return q[0] >= 0 && q[1] >= 0 && q[2] >= 0;
+}
+
+// Components of DEPOLARIZE2 kept at each correlation level (Mixer.hpp:13-20):
+// L0 drops every component with a Y or an X/Z mix; L1 adds IY, YI, XZ, ZX.
+bool dep2_kept(int level, int pa, int pb) {
+  if (level >= 2) return true;
+  bool y = pa == 3 || pb == 3;
+  bool mixXZ = (pa == 1 && pb == 2) || (pa == 2 && pb == 1);
+  if (level == 0) return !y && !mixXZ;
+  bool extra = (pa == 0 && pb == 3) || (pa == 3 && pb == 0) || mixXZ;
+  return (!y && !mixXZ) || extra;
+}
+
+// Swaps the qubit halves of a two-qubit mask (Xa,Za,Xb,Zb) -> (Xb,Zb,Xa,Za).
+uint32_t swap_halves(uint32_t m) { return ((m >> 2) & 3u) | ((m & 3u) << 2); }
+
+struct Entry {
+  uint32_t epoch;
+  uint64_t op;
+};
+
+struct QState {
+  int64_t last = -1;   // epoch of the latest entry
+  uint32_t cnt = 0;    // entries in that epoch
+  uint32_t open = kNone;  // point holding the current rows (until a row-changing op)
+};
+
+}  // namespace
+
+Parsed parse_stim(const char *text, size_t len) {
+  Parsed p;
+  if (!text && len) throw Error(GPC_ERR_INVALID, "null circuit text");
+  TextParser tp{text, text + len, 1, &p};
+  tp.block(p.ins, false, 0);
+  return p;
+}
+
+Tape lower(const Parsed &P, const LowerOptions &opt) {
+  if (opt.level < 0 || opt.level > 2) throw Error(GPC_ERR_INVALID, "correlation level must be 0, 1 or 2");
+  Tape T;
+  uint32_t kcap = std::max<uint32_t>(1, opt.kcap);
+
+  // ---- forward pass: qubits, measurements, detectors, observables --------
+  std::vector<uint32_t> measBase(P.ins.size());
+  std::vector<std::pair<uint32_t, uint32_t>> detPairs;  // (measurement, detector)
+  std::vector<std::pair<uint32_t, uint32_t>> obsPairs;  // (measurement, observable)
+  uint32_t m = 0, ndet = 0, nobs = 0;
+  uint32_t nq = 0;
+  for (size_t i = 0; i < P.ins.size(); ++i) {
+    const Instr &in = P.ins[i];
+    const Gate &g = kGates[in.gate];
+    const uint32_t *t = P.pool.data() + in.t0;
+    measBase[i] = m;
+    for (uint32_t k = 0; k < in.tn; ++k) {
+      uint32_t v = t[k];
+      if (v & kRec) {
+        if (g.kind != G_DET && g.kind != G_OBS)
+          throw Error(GPC_ERR_UNSUPPORTED, std::string("record targets are not supported on ") + g.name);
+        continue;
+      }
+      if (g.kind == G_DET || g.kind == G_OBS)
+        throw Error(GPC_ERR_PARSE, std::string(g.name) + " takes record targets only");
+      if (g.kind == G_MPAD) {
+        if (v > 1) throw Error(GPC_ERR_PARSE, "MPAD targets must be 0 or 1");
+        continue;
+      }
+      if ((v & kPau) && g.kind != G_CORR)
+        throw Error(GPC_ERR_PARSE, std::string("Pauli targets are not allowed on ") + g.name);
+      if (!(v & kPau) && g.kind == G_CORR) throw Error(GPC_ERR_PARSE, "E takes Pauli targets");
+      nq = std::max(nq, (v & 0xFFFFFFu) + 1);
+    }
+    switch (g.kind) {
+      case G_M:
+      case G_MR:
+      case G_MPAD:
+        m += in.tn;
+        break;
+      case G_DET:
+        for (uint32_t k = 0; k < in.tn; ++k) {
+          uint32_t back = t[k] & ~kRec;
+          if (back > m) throw Error(GPC_ERR_PARSE, "record lookback beyond the start of the circuit");
+          detPairs.push_back({m - back, ndet});
+        }
+        ++ndet;
+        break;
+      case G_OBS: {
+        double a = in.args[0];
+        if (!(a >= 0) || a != std::floor(a) || a > 1e6) throw Error(GPC_ERR_PARSE, "bad observable index");
+        uint32_t kk = (uint32_t)a;
+        for (uint32_t k = 0; k < in.tn; ++k) {
+          uint32_t back = t[k] & ~kRec;
+          if (back > m) throw Error(GPC_ERR_PARSE, "record lookback beyond the start of the circuit");
+          obsPairs.push_back({m - back, kk});
+        }
+        nobs = std::max(nobs, kk + 1);
+        break;
+      }
+      case G_C2:
+      case G_N2:
+        if (in.tn % 2) throw Error(GPC_ERR_PARSE, std::string(g.name) + " needs an even number of targets");
+        for (uint32_t k = 0; k < in.tn; k += 2)
+          if (t[k] == t[k + 1]) throw Error(GPC_ERR_PARSE, std::string(g.name) + " on a single qubit");
+        break;
+      default:
+        break;
+    }
+    // probability checks
+    auto prob = [&](double p) {
+      if (!(p >= 0 && p <= 1)) throw Error(GPC_ERR_PARSE, std::string(g.name) + ": probability out of range");
+    };
+    if (g.kind == G_N1 || g.kind == G_N2 || g.kind == G_CORR || ((g.kind == G_M || g.kind == G_MR || g.kind == G_MPAD) && in.nargs))
+      for (int k = 0; k < in.nargs; ++k) prob(in.args[k]);
+    if (g.kind == G_N1 && g.a == N1_DEP1 && in.args[0] > 0.75) throw Error(GPC_ERR_PARSE, "DEPOLARIZE1 p > 0.75");
+    if (g.kind == G_N2 && in.args[0] > 0.9375) throw Error(GPC_ERR_PARSE, "DEPOLARIZE2 p > 0.9375");
+    if (g.kind == G_N1 && g.a == N1_PC1) {
+      double q[3];
+      if (!pc1_independent(in.args[0], in.args[1], in.args[2], q))
+        throw Error(GPC_ERR_UNSUPPORTED, "PAULI_CHANNEL_1 is not a product of independent X, Y, Z channels");
+    }
+    if (g.kind == G_MPAD && in.nargs && in.args[0] > 0)
+      throw Error(GPC_ERR_UNSUPPORTED, "noisy MPAD is not supported");
+  }
+  T.nq = nq;
+  T.nmeas = m;
+  T.ndet = ndet;
+  T.nobs = nobs;
+  T.nbits = ndet + nobs;
+  T.w = std::max<uint32_t>(1, (T.nbits + 63) / 64);
+  if (nq > 4096) throw Error(GPC_ERR_CAPACITY, "more than 4096 qubits");
+  {
+    uint32_t qpt = nq <= 1024 ? 1 : nq <= 2048 ? 2 : 4;
+    uint32_t per = (nq + qpt - 1) / qpt;
+    uint32_t threads = std::max<uint32_t>(32, (per + 31) / 32 * 32);
+    T.qpad = threads * qpt;
+    // an epoch (kcap slots x qpad ops) must fit a shared-memory ring slot of <= 96 KiB
+    kcap = std::min<uint32_t>(kcap, std::max<uint32_t>(1, 98304u / (T.qpad * 8u)));
+  }
+
+  // measurement -> bits (XOR: a measurement listed twice in one detector cancels)
+  {
+    std::vector<std::pair<uint32_t, uint32_t>> mb;
+    mb.reserve(detPairs.size() + obsPairs.size());
+    for (auto &d : detPairs) mb.push_back(d);
+    for (auto &o : obsPairs) mb.push_back({o.first, ndet + o.second});
+    std::sort(mb.begin(), mb.end());
+    T.meas_off.assign(m + 1, 0);
+    std::vector<std::pair<uint32_t, uint32_t>> kept;
+    for (size_t i = 0; i < mb.size();) {
+      size_t j = i;
+      while (j < mb.size() && mb[j] == mb[i]) ++j;
+      if ((j - i) & 1) kept.push_back(mb[i]);
+      i = j;
+    }
+    for (auto &k : kept) T.meas_off[k.first + 1]++;
+    for (uint32_t i = 0; i < m; ++i) T.meas_off[i + 1] += T.meas_off[i];
+    T.meas_bits.resize(kept.size());
+    for (size_t i = 0; i < kept.size(); ++i) T.meas_bits[i] = kept[i].second;  // already grouped by meas
+  }
+
+  // ---- backward pass: epoch scheduling and mechanisms ---------------------
+  std::vector<std::vector<Entry>> ent(nq);
+  std::vector<QState> st(nq);
+  std::vector<uint32_t> measEpoch(m, kNone);
+  uint32_t nprov = 0;  // provisional point ids
+  std::vector<uint64_t> &desc = T.desc;
+  std::vector<double> &prob = T.prob;
+
+  auto place1 = [&](uint32_t q, uint64_t op) -> uint32_t {
+    QState &s = st[q];
+    uint32_t e;
+    if (s.last < 0) {
+      e = 0;
+      s.cnt = 0;
+    } else if (s.cnt >= kcap) {
+      e = (uint32_t)s.last + 1;
+      s.cnt = 0;
+    } else {
+      e = (uint32_t)s.last;
+    }
+    ent[q].push_back({e, op});
+    s.last = e;
+    s.cnt++;
+    return e;
+  };
+  auto point = [&](uint32_t q) -> uint32_t {
+    QState &s = st[q];
+    if (s.open != kNone) return s.open;
+    uint32_t id = nprov++;
+    place1(q, make_op(OP_SNAP, 0, id));
+    s.open = id;
+    return id;
+  };
+  auto mech = [&](uint32_t pa, uint32_t Pa, uint32_t pb, uint32_t Pb, double p) {
+    desc.push_back(make_desc(pa, Pa, pb, Pb));
+    prob.push_back(p);
+  };
+
+  for (size_t ii = P.ins.size(); ii-- > 0;) {
+    const Instr &in = P.ins[ii];
+    const Gate &g = kGates[in.gate];
+    const uint32_t *t = P.pool.data() + in.t0;
+    switch (g.kind) {
+      case G_C1:
+        for (uint32_t k = in.tn; k-- > 0;) {
+          uint32_t q = t[k];
+          place1(q, make_op(OP_C1, (uint32_t)g.a | ((uint32_t)g.b << 2), 0));
+          st[q].open = kNone;
+        }
+        break;
+      case G_C2:
+        for (uint32_t k = in.tn; k >= 2; k -= 2) {
+          uint32_t a = t[k - 2], b = t[k - 1];
+          int64_t E = std::max(st[a].last, st[b].last) + 1;
+          uint32_t subA = (uint32_t)g.img[0] | ((uint32_t)g.img[1] << 4);
+          uint32_t subB = swap_halves(g.img[2]) | (swap_halves(g.img[3]) << 4);
+          ent[a].push_back({(uint32_t)E, make_op(OP_C2, subA, b)});
+          ent[b].push_back({(uint32_t)E, make_op(OP_C2, subB, a)});
+          st[a].last = st[b].last = E;
+          st[a].cnt = st[b].cnt = 1;
+          st[a].open = st[b].open = kNone;
+        }
+        break;
+      case G_R:
+        for (uint32_t k = in.tn; k-- > 0;) {
+          place1(t[k], make_op(OP_R, 0, 0));
+          st[t[k]].open = kNone;
+        }
+        break;
+      case G_M:
+      case G_MR: {
+        double p = in.nargs ? in.args[0] : 0.0;
+        for (uint32_t k = in.tn; k-- > 0;) {
+          uint32_t q = t[k];
+          uint32_t meas = measBase[ii] + k;
+          uint32_t e = place1(q, make_op(g.kind == G_MR ? OP_MR : OP_M, g.a, meas));
+          measEpoch[meas] = e;
+          st[q].open = kNone;
+          if (p > 0 && T.meas_off[meas + 1] > T.meas_off[meas]) {
+            uint32_t id = nprov++;
+            place1(q, make_op(OP_SNAPD, 0, id));
+            mech(id, 1, 0, 0, p);
+          }
+        }
+        break;
+      }
+      case G_N1: {
+        for (uint32_t k = in.tn; k-- > 0;) {
+          uint32_t q = t[k];
+          double px = 0, py = 0, pz = 0;
+          switch (g.a) {
+            case N1_X: px = in.args[0]; break;
+            case N1_Y: py = in.args[0]; break;
+            case N1_Z: pz = in.args[0]; break;
+            case N1_DEP1: {
+              double s = split_dep1(in.args[0]);
+              px = pz = s;
+              py = opt.level >= 1 ? s : 0.0;
+              break;
+            }
+            case N1_PC1: {
+              double qq[3];
+              pc1_independent(in.args[0], in.args[1], in.args[2], qq);
+              px = qq[0];
+              py = qq[1];
+              pz = qq[2];
+              break;
+            }
+          }
+          if (px > 0 || py > 0 || pz > 0) {
+            uint32_t pt = point(q);
+            if (px > 0) mech(pt, 1, 0, 0, px);
+            if (py > 0) mech(pt, 3, 0, 0, py);
+            if (pz > 0) mech(pt, 2, 0, 0, pz);
+          }
+        }
+        break;
+      }
+      case G_N2: {
+        double s = split_dep2(in.args[0]);
+        if (!(s > 0)) break;
+        // stim's order of the 15 Paulis: IX IY IZ XI XX XY XZ YI YX YY YZ ZI ZX ZY ZZ
+        static const uint8_t order[4] = {0, 1, 3, 2};  // I X Y Z in X|Z masks
+        for (uint32_t k = in.tn; k >= 2; k -= 2) {
+          uint32_t a = t[k - 2], b = t[k - 1];
+          uint32_t pa = point(a), pb = point(b);
+          for (int i = 0; i < 4; ++i)
+            for (int j = 0; j < 4; ++j) {
+              int A = order[i], B = order[j];
+              if (A == 0 && B == 0) continue;
+              if (!dep2_kept(opt.level, A, B)) continue;
+              if (A == 0)
+                mech(pb, (uint32_t)B, 0, 0, s);
+              else if (B == 0)
+                mech(pa, (uint32_t)A, 0, 0, s);
+              else
+                mech(pa, (uint32_t)A, pb, (uint32_t)B, s);
+            }
+        }
+        break;
+      }
+      case G_CORR: {
+        double p = in.args[0];
+        if (!(p > 0)) break;
+        uint32_t q0 = kNone, q1 = kNone, P0 = 0, P1 = 0;
+        for (uint32_t k = 0; k < in.tn; ++k) {
+          uint32_t q = t[k] & 0xFFFFFFu, Pv = (t[k] >> 24) & 3u;
+          if (q0 == kNone || q0 == q) {
+            q0 = q;
+            P0 ^= Pv;
+          } else if (q1 == kNone || q1 == q) {
+            q1 = q;
+            P1 ^= Pv;
+          } else {
+            throw Error(GPC_ERR_UNSUPPORTED, "correlated errors on more than two qubits are not supported");
+          }
+        }
+        uint32_t pa = P0 ? point(q0) : 0, pb = P1 ? point(q1) : 0;
+        if (P0 && P1)
+          mech(pa, P0, pb, P1, p);
+        else if (P0)
+          mech(pa, P0, 0, 0, p);
+        else if (P1)
+          mech(pb, P1, 0, 0, p);
+        break;
+      }
+      default:
+        break;
+    }
+  }
+
+  // ---- assemble epochs -------------------------------------------------
+  uint32_t nE = 0;
+  for (uint32_t q = 0; q < nq; ++q)
+    if (!ent[q].empty()) nE = std::max(nE, ent[q].back().epoch + 1);
+  T.n_epochs = nE;
+  T.ep_k.assign(nE, 0);
+  for (uint32_t q = 0; q < nq; ++q) {
+    const auto &v = ent[q];
+    for (size_t i = 0; i < v.size();) {
+      size_t j = i;
+      while (j < v.size() && v[j].epoch == v[i].epoch) ++j;
+      T.ep_k[v[i].epoch] = std::max<uint32_t>(T.ep_k[v[i].epoch], (uint32_t)(j - i));
+      i = j;
+    }
+  }
+  for (auto &k : T.ep_k) k = std::max<uint32_t>(k, 1);  // every epoch copies at least one slot
+  T.ep_opoff.assign(nE, 0);
+  uint64_t total = 0;
+  for (uint32_t e = 0; e < nE; ++e) {
+    T.ep_opoff[e] = (uint32_t)total;
+    total += (uint64_t)T.ep_k[e] * T.qpad;
+    T.kmax = std::max(T.kmax, T.ep_k[e]);
+    if (total > 0xFFFFFFFFull) throw Error(GPC_ERR_CAPACITY, "tape too long");
+  }
+  T.ops.assign(total, 0);
+  for (uint32_t q = 0; q < nq; ++q) {
+    const auto &v = ent[q];
+    uint32_t k = 0;
+    for (size_t i = 0; i < v.size(); ++i) {
+      if (i == 0 || v[i].epoch != v[i - 1].epoch) k = 0;
+      T.ops[(size_t)T.ep_opoff[v[i].epoch] + (size_t)k * T.qpad + q] = v[i].op;
+      ++k;
+    }
+  }
+  // points: renumber in walk order (epoch, slot, qubit) so each epoch owns a contiguous range
+  std::vector<uint32_t> remap(nprov, kNone);
+  T.ep_ptoff.assign(nE + 1, 0);
+  uint32_t next = 0;
+  for (uint32_t e = 0; e < nE; ++e) {
+    T.ep_ptoff[e] = next;
+    uint64_t *base = T.ops.data() + T.ep_opoff[e];
+    for (uint32_t k = 0; k < T.ep_k[e]; ++k)
+      for (uint32_t q = 0; q < T.qpad; ++q) {
+        uint64_t &op = base[(size_t)k * T.qpad + q];
+        uint32_t opc = (uint32_t)(op & 0xFF);
+        if (opc == OP_SNAP || opc == OP_SNAPD) {
+          uint32_t prov = (uint32_t)(op >> 32);
+          remap[prov] = next;
+          op = (op & 0xFFFFFFFFull) | ((uint64_t)next << 32);
+          ++next;
+        }
+      }
+  }
+  T.ep_ptoff[nE] = next;
+  T.npoints = next;
+  if (next >= (1u << 30)) throw Error(GPC_ERR_CAPACITY, "too many snapshot points");
+  for (auto &d : desc) {
+    uint32_t pa = (uint32_t)(d & 0x3FFFFFFFu), Pa = (uint32_t)((d >> 30) & 3);
+    uint32_t pb = (uint32_t)((d >> 32) & 0x3FFFFFFFu), Pb = (uint32_t)(d >> 62);
+    d = make_desc(remap[pa], Pa, Pb ? remap[pb] : 0, Pb);
+  }
+  // injection range of each word
+  T.inj_lo.assign(T.w, kNone);
+  T.inj_hi.assign(T.w, kNone);
+  for (uint32_t mm = 0; mm < m; ++mm) {
+    uint32_t e = measEpoch[mm];
+    if (e == kNone) continue;
+    for (uint32_t i = T.meas_off[mm]; i < T.meas_off[mm + 1]; ++i) {
+      uint32_t j = T.meas_bits[i] >> 6;
+      if (T.inj_lo[j] == kNone || e < T.inj_lo[j]) T.inj_lo[j] = e;
+      if (T.inj_hi[j] == kNone || e > T.inj_hi[j]) T.inj_hi[j] = e;
+    }
+  }
+  return T;
+}
+
+}  // namespace gpc

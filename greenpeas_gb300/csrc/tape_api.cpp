@@ -1,0 +1,70 @@
+// tape_api.cpp -- host-only C ABI that exposes the lowered tape (include/gpc.h).
+#include <memory>
+#include <new>
+#include <string>
+
+#include "../../include/gpc.h"
+#include "lower.hpp"
+
+struct gpc_tape {
+  gpc::Tape t;
+};
+
+namespace {
+thread_local std::string g_tape_error;
+}
+
+extern "C" {
+
+gpc_status gpc_tape_lower(const char *stim_text, size_t len, int32_t correlation_level, gpc_tape **out) {
+  if (!out || !stim_text) return GPC_ERR_INVALID;
+  *out = nullptr;
+  try {
+    gpc::Parsed p = gpc::parse_stim(stim_text, len);
+    gpc::LowerOptions lo;
+    lo.level = correlation_level;
+    std::unique_ptr<gpc_tape> t(new gpc_tape{gpc::lower(p, lo)});
+    *out = t.release();
+    return GPC_OK;
+  } catch (const gpc::Error &e) {
+    g_tape_error = e.what();
+    return e.code;
+  } catch (const std::bad_alloc &) {
+    return GPC_ERR_OOM;
+  } catch (const std::exception &e) {
+    g_tape_error = e.what();
+    return GPC_ERR_INVALID;
+  }
+}
+
+const char *gpc_tape_last_error(void) { return g_tape_error.c_str(); }
+
+gpc_status gpc_tape_get_view(const gpc_tape *tape, gpc_tape_view *v) {
+  if (!tape || !v) return GPC_ERR_INVALID;
+  const gpc::Tape &T = tape->t;
+  v->num_qubits = T.nq;
+  v->qpad = T.qpad;
+  v->num_measurements = T.nmeas;
+  v->num_detectors = T.ndet;
+  v->num_observables = T.nobs;
+  v->words = T.w;
+  v->num_epochs = T.n_epochs;
+  v->kmax = T.kmax;
+  v->num_points = T.npoints;
+  v->num_mechanisms = (uint32_t)T.desc.size();
+  v->num_ops = T.ops.size();
+  v->ops = T.ops.data();
+  v->ep_opoff = T.ep_opoff.data();
+  v->ep_k = T.ep_k.data();
+  v->ep_ptoff = T.ep_ptoff.data();
+  v->meas_off = T.meas_off.data();
+  v->meas_bits = T.meas_bits.data();
+  v->inj_lo = T.inj_lo.data();
+  v->inj_hi = T.inj_hi.data();
+  v->desc = T.desc.data();
+  v->prob = T.prob.data();
+  return GPC_OK;
+}
+
+void gpc_tape_free(gpc_tape *tape) { delete tape; }
+}

@@ -1,0 +1,187 @@
+"""``get_driver(circuit).compile_detector_error_model(circuit)`` on the GB300 path.
+
+Python surface of GreenPeas' error-analysis bindings
+(source/QEC/ErrorAnalysis/ErrorAnalysis.pybind.cu:47-79): ``CorrelationLevel``,
+``Driver`` with the one- and zero-argument ``compile_detector_error_model``
+overloads, and ``get_driver(circuit, correlation_level=CorrelationLevel.L2)``.
+Circuits cross the boundary as stim text (a ``stim.Circuit`` is converted with
+``str()``), the compile runs in libgpc.so through the C ABI, and the result is
+a ``stim.DetectorErrorModel`` when stim is importable, else this package's
+``DetectorErrorModel`` with the same text form.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import enum
+
+import numpy as np
+
+from . import _native
+from .dem import DetectorErrorModel
+
+
+class CorrelationLevel(enum.IntEnum):
+    """Pauli components kept per depolarizing channel (Mixer.hpp:13-20)."""
+
+    L0 = 0  # X, Z, IX, IZ, XI, XX, ZI, ZZ
+    L1 = 1  # + Y, IY, XZ, YI, ZX
+    L2 = 2  # all 3 / 15 components
+
+
+def _text(circuit) -> bytes:
+    if circuit is None:
+        return None
+    if isinstance(circuit, bytes):
+        return circuit
+    return str(circuit).encode()
+
+
+def _stim_available() -> bool:
+    try:
+        import stim  # noqa: F401
+        return True
+    except ImportError:
+        return False
+
+
+def dem_from_handle(h: ctypes.c_void_p) -> DetectorErrorModel:
+    """Copies a gpc_dem into a DetectorErrorModel and frees the handle."""
+    L = _native.lib()
+    try:
+        offs = ctypes.POINTER(ctypes.c_uint32)()
+        tg = ctypes.POINTER(ctypes.c_uint32)()
+        pr = ctypes.POINTER(ctypes.c_double)()
+        n = ctypes.c_uint32()
+        _native.check(L.gpc_dem_arrays(h, ctypes.byref(offs), ctypes.byref(tg), ctypes.byref(pr), ctypes.byref(n)))
+        nd, no = ctypes.c_uint32(), ctypes.c_uint32()
+        raw = ctypes.c_uint64()
+        _native.check(L.gpc_dem_info(h, ctypes.byref(nd), ctypes.byref(no), ctypes.byref(raw)))
+        ne = n.value
+        offsets = np.ctypeslib.as_array(offs, shape=(ne + 1,)).copy()
+        nt = int(offsets[-1])
+        targets = np.ctypeslib.as_array(tg, shape=(nt,)).copy() if nt else np.zeros(0, np.uint32)
+        probs = np.ctypeslib.as_array(pr, shape=(ne,)).copy() if ne else np.zeros(0)
+        return DetectorErrorModel(probs, offsets, targets, nd.value, no.value, raw.value)
+    finally:
+        L.gpc_dem_free(h)
+
+
+class Driver:
+    """Owns a libgpc driver: device buffers, a CUDA stream, the parsed circuit."""
+
+    def __init__(self, circuit, correlation_level: CorrelationLevel = CorrelationLevel.L2, *,
+                 device: int = 0, sort_bits: int = 0):
+        L = _native.lib()
+        self._h = ctypes.c_void_p()
+        self.correlation_level = CorrelationLevel(correlation_level)
+        opts = _native.Options()
+        opts.device = device
+        opts.sort_bits = sort_bits
+        text = _text(circuit)
+        _native.check(L.gpc_get_driver(text, len(text), int(self.correlation_level), ctypes.byref(opts),
+                                       ctypes.byref(self._h)))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) and self._h.value:
+            _native.lib().gpc_driver_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def handle(self) -> ctypes.c_void_p:
+        return self._h
+
+    def compile(self, circuit=None) -> DetectorErrorModel:
+        """Compiles ``circuit`` (or the driver's current circuit) to this package's DEM type."""
+        L = _native.lib()
+        out = ctypes.c_void_p()
+        text = _text(circuit)
+        _native.check(L.gpc_compile(self._h, text, len(text) if text else 0, ctypes.byref(out)))
+        return dem_from_handle(out)
+
+    def compile_detector_error_model(self, circuit=None):
+        """Reference-compatible entry point: a stim.DetectorErrorModel when stim is importable."""
+        dem = self.compile(circuit)
+        return dem.to_stim() if _stim_available() else dem
+
+    def compile_batch(self, circuits) -> list:
+        L = _native.lib()
+        texts = [_text(c) for c in circuits]
+        n = len(texts)
+        arr = (ctypes.c_char_p * n)(*texts)
+        lens = (ctypes.c_size_t * n)(*[len(t) for t in texts])
+        outs = (ctypes.c_void_p * n)()
+        _native.check(L.gpc_compile_batch(self._h, arr, lens, n, outs))
+        return [dem_from_handle(ctypes.c_void_p(outs[i])) for i in range(n)]
+
+    # device-resident stages
+    def prepare(self, circuit=None) -> None:
+        text = _text(circuit)
+        _native.check(_native.lib().gpc_prepare(self._h, text, len(text) if text else 0))
+
+    def run_device(self) -> None:
+        _native.check(_native.lib().gpc_run_device(self._h))
+
+    def fetch(self) -> DetectorErrorModel:
+        out = ctypes.c_void_p()
+        _native.check(_native.lib().gpc_fetch(self._h, ctypes.byref(out)))
+        return dem_from_handle(out)
+
+    def last_timings(self) -> dict:
+        ms = (ctypes.c_float * 5)()
+        _native.check(_native.lib().gpc_last_timings(self._h, ms))
+        return dict(zip(("walk", "key", "sort", "merge", "total"), [float(x) for x in ms]))
+
+    def last_sizes(self) -> dict:
+        raw, pts = ctypes.c_uint64(), ctypes.c_uint64()
+        ep, w, nq = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+        _native.check(_native.lib().gpc_last_sizes(self._h, ctypes.byref(raw), ctypes.byref(pts), ctypes.byref(ep),
+                                                   ctypes.byref(w), ctypes.byref(nq)))
+        return {"raw": raw.value, "points": pts.value, "epochs": ep.value, "words": w.value, "qubits": nq.value}
+
+    @property
+    def stream(self) -> int:
+        return _native.lib().gpc_driver_stream(self._h) or 0
+
+
+def get_driver(circuit, correlation_level: CorrelationLevel = CorrelationLevel.L2, **kw) -> Driver:
+    """greenpeas.get_driver: a driver sized for ``circuit`` (stim.Circuit or stim text)."""
+    return Driver(circuit, correlation_level, **kw)
+
+
+class Tape:
+    """The lowered device tape of a circuit, as numpy arrays (host only, no GPU)."""
+
+    def __init__(self, circuit, correlation_level: int = 2):
+        L = _native.lib()
+        h = ctypes.c_void_p()
+        text = _text(circuit)
+        _native.check(L.gpc_tape_lower(text, len(text), int(correlation_level), ctypes.byref(h)), tape=True)
+        try:
+            v = _native.TapeView()
+            _native.check(L.gpc_tape_get_view(h, ctypes.byref(v)), tape=True)
+
+            def arr(ptr, n):
+                return np.ctypeslib.as_array(ptr, shape=(n,)).copy() if n else np.zeros(0, dtype=ptr._type_)
+
+            for f in ("num_qubits", "qpad", "num_measurements", "num_detectors", "num_observables", "words",
+                      "num_epochs", "kmax", "num_points", "num_mechanisms"):
+                setattr(self, f, int(getattr(v, f)))
+            self.ops = arr(v.ops, int(v.num_ops))
+            self.ep_opoff = arr(v.ep_opoff, v.num_epochs)
+            self.ep_k = arr(v.ep_k, v.num_epochs)
+            self.ep_ptoff = arr(v.ep_ptoff, v.num_epochs + 1)
+            self.meas_off = arr(v.meas_off, v.num_measurements + 1)
+            self.meas_bits = arr(v.meas_bits, int(self.meas_off[-1]) if v.num_measurements else 0)
+            self.inj_lo = arr(v.inj_lo, v.words)
+            self.inj_hi = arr(v.inj_hi, v.words)
+            self.desc = arr(v.desc, v.num_mechanisms)
+            self.prob = arr(v.prob, v.num_mechanisms)
+        finally:
+            L.gpc_tape_free(h)

@@ -1,0 +1,149 @@
+/* gpc.h -- C ABI of the GB300 detector-error-model compiler.
+ *
+ * This is the drop-in boundary for GreenPeas' DEM-compilation path.  Each
+ * entry point names the reference interface it replaces:
+ *
+ *   gpc_get_driver          <- greenpeas.get_driver(circuit, correlation_level)
+ *                              (source/QEC/ErrorAnalysis/ErrorAnalysis.pybind.cu:72-78,
+ *                               getDriver 26-41, Driver::fromStimCircuit
+ *                               QEC/ErrorAnalysis/Driver.hpp:216-218)
+ *   gpc_compile             <- Driver.compile_detector_error_model(circuit) and its
+ *                              no-argument overload
+ *                              (ErrorAnalysis.pybind.cu:56-70; Driver.hpp:199-211)
+ *   gpc_dem_*               <- the stim::DetectorErrorModel the reference builds in
+ *                              Driver::getDetectorErrorModel (Driver.hpp:166-194):
+ *                              one error per merged symptom, target index
+ *                              >= num_detectors is observable (index - num_detectors)
+ *   gpc_driver_destroy      <- destruction of the pybind-owned Driver variant
+ *
+ * Circuits are passed as stim circuit text and DEMs come back as arrays (or
+ * stim DEM text), so no C++ or Python object crosses the boundary.
+ *
+ * Conventions: every function returns a gpc_status (0 = success, < 0 =
+ * error) and never throws; gpc_last_error() gives a thread-local message for
+ * the most recent failure on the calling thread.  A driver owns one CUDA
+ * stream and its device buffers; different drivers may be used from
+ * different threads concurrently, one driver may not.  A driver's buffers
+ * grow when a larger circuit is compiled (the reference throws instead).
+ */
+#ifndef GPC_H
+#define GPC_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t gpc_status;
+
+enum {
+  GPC_OK = 0,
+  GPC_ERR_INVALID = -1,     /* bad argument (null pointer, bad level, ...) */
+  GPC_ERR_PARSE = -2,       /* circuit text does not parse */
+  GPC_ERR_UNSUPPORTED = -3, /* instruction outside the supported gate set */
+  GPC_ERR_CUDA = -4,        /* CUDA runtime error or no device */
+  GPC_ERR_OOM = -5,         /* device or host allocation failed */
+  GPC_ERR_COLLISION = -6,   /* two different symptoms share a 128-bit key */
+  GPC_ERR_TIMEOUT = -7,     /* a bounded device wait gave up */
+  GPC_ERR_CAPACITY = -8     /* a size limit of this build was exceeded */
+};
+
+/* Correlation levels, as greenpeas.CorrelationLevel (Mixer.hpp:13-20). */
+enum { GPC_L0 = 0, GPC_L1 = 1, GPC_L2 = 2 };
+
+typedef struct gpc_driver gpc_driver;
+typedef struct gpc_dem gpc_dem;
+
+typedef struct gpc_options {
+  int32_t device;    /* CUDA device ordinal (default 0) */
+  int32_t sort_bits; /* key bits sorted before the merge: 0 = default (64) */
+  int32_t reserved[6];
+} gpc_options;
+
+/* Parses `stim_text` (length `len`), sizes device buffers for it and returns
+ * a driver bound to `correlation_level`.  `options` may be NULL. */
+gpc_status gpc_get_driver(const char *stim_text, size_t len, int32_t correlation_level,
+                          const gpc_options *options, gpc_driver **out);
+
+/* Compiles a circuit to a DEM.  With `stim_text` == NULL the driver's
+ * current (last parsed) circuit is compiled again, like the reference's
+ * no-argument overload.  The result is owned by the caller. */
+gpc_status gpc_compile(gpc_driver *driver, const char *stim_text, size_t len, gpc_dem **out);
+
+/* Compiles `n` circuits in one batched pipeline (one walk launch, one
+ * segmented sort, one merge).  outs[i] receives circuit i's DEM. */
+gpc_status gpc_compile_batch(gpc_driver *driver, const char *const *texts, const size_t *lens,
+                             int32_t n, gpc_dem **outs);
+
+/* Merged mechanisms as CSR arrays owned by the DEM: error i has targets
+ * targets[offsets[i] .. offsets[i+1]) (ascending) and probability probs[i]. */
+gpc_status gpc_dem_arrays(const gpc_dem *dem, const uint32_t **offsets, const uint32_t **targets,
+                          const double **probs, uint32_t *num_errors);
+
+/* Circuit counts of the compiled DEM. */
+gpc_status gpc_dem_info(const gpc_dem *dem, uint32_t *num_detectors, uint32_t *num_observables,
+                        uint64_t *num_raw_mechanisms);
+
+/* stim DEM text ("error(p) D0 D3 L0" lines); the buffer is owned by the DEM. */
+gpc_status gpc_dem_text(const gpc_dem *dem, const char **text, size_t *len);
+
+void gpc_dem_free(gpc_dem *dem);
+void gpc_driver_destroy(gpc_driver *driver);
+
+/* Thread-local message of the last failure on this thread ("" if none). */
+const char *gpc_last_error(void);
+
+/* ---- device-resident stages (benchmarking and serving) -------------------
+ * gpc_prepare parses and uploads a circuit; gpc_run_device runs the kernel
+ * pipeline on the uploaded tape with results left on the device;
+ * gpc_fetch copies the last device result into a new DEM.  gpc_compile is
+ * gpc_prepare + gpc_run_device + gpc_fetch. */
+gpc_status gpc_prepare(gpc_driver *driver, const char *stim_text, size_t len);
+gpc_status gpc_run_device(gpc_driver *driver);
+gpc_status gpc_fetch(gpc_driver *driver, gpc_dem **out);
+
+/* The driver's CUDA stream (a cudaStream_t), for callers that time it. */
+void *gpc_driver_stream(gpc_driver *driver);
+
+/* Kernel timing of the last gpc_run_device, in milliseconds (CUDA events on
+ * the driver's stream): [0] walk, [1] key, [2] sort, [3] merge, [4] total. */
+gpc_status gpc_last_timings(gpc_driver *driver, float *ms5);
+
+/* Sizes of the last prepared circuit: raw mechanisms, snapshot points,
+ * epochs, words per bitset, qubits. */
+gpc_status gpc_last_sizes(gpc_driver *driver, uint64_t *raw, uint64_t *points, uint32_t *epochs,
+                          uint32_t *words, uint32_t *qubits);
+
+/* ---- tape inspection (host only, no GPU needed) ---------------------------
+ * Lowers a circuit to the device tick tape without compiling it, for tools
+ * and tests that check the lowering.  Arrays are owned by the tape. */
+typedef struct gpc_tape gpc_tape;
+typedef struct gpc_tape_view {
+  uint32_t num_qubits, qpad, num_measurements, num_detectors, num_observables, words;
+  uint32_t num_epochs, kmax, num_points, num_mechanisms;
+  uint64_t num_ops;
+  const uint64_t *ops;        /* epoch-major; epoch e is ep_k[e] slots x qpad ops */
+  const uint32_t *ep_opoff;   /* [num_epochs] */
+  const uint32_t *ep_k;       /* [num_epochs] */
+  const uint32_t *ep_ptoff;   /* [num_epochs + 1] */
+  const uint32_t *meas_off;   /* [num_measurements + 1] */
+  const uint32_t *meas_bits;
+  const uint32_t *inj_lo;     /* [words] */
+  const uint32_t *inj_hi;     /* [words] */
+  const uint64_t *desc;       /* [num_mechanisms] */
+  const double *prob;         /* [num_mechanisms] */
+} gpc_tape_view;
+
+gpc_status gpc_tape_lower(const char *stim_text, size_t len, int32_t correlation_level, gpc_tape **out);
+gpc_status gpc_tape_get_view(const gpc_tape *tape, gpc_tape_view *view);
+void gpc_tape_free(gpc_tape *tape);
+/* Thread-local message of the last gpc_tape_lower failure. */
+const char *gpc_tape_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GPC_H */

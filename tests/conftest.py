@@ -49,3 +49,11 @@ def compare_errors(actual: dict, expected: dict, rel: float = 1e-12):
         worst = max(worst, err)
     assert worst <= rel, f"max relative probability error {worst:.3e} > {rel:.0e}"
     return worst
+
+
+@pytest.fixture(scope="session", autouse=True)
+def _built():
+    """Builds libgpc.so and the oracle once per session (no-op when up to date)."""
+    import __graft_entry__
+    __graft_entry__.build()
+    yield

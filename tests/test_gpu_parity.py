@@ -1,0 +1,91 @@
+"""CUDA path parity against the CPU FP64 oracle and the reference golden DEMs (needs a GPU).
+
+Comparison rule: symptom sets bit-exact, merged probabilities within 1e-12
+relative, same detector / observable counts.
+"""
+
+from __future__ import annotations
+
+import pytest
+
+import greenpeas_gb300 as gp
+from conftest import GOLDEN, compare_errors, load_canonical_dem, to_named
+from oracle import oracle as O
+from test_lowering import SMALL
+
+pytestmark = pytest.mark.gpu
+REL = 1e-12
+
+
+def _check(dem, text, level=2):
+    ref = O.compile_text(text, level)
+    assert dem.num_detectors == ref.num_detectors and dem.num_observables == ref.num_observables
+    compare_errors(dict(dem.errors()), dict(ref.errors()), rel=REL)
+
+
+@pytest.mark.parametrize("text", SMALL)
+def test_small(text):
+    _check(gp.get_driver(text).compile(text), text)
+
+
+@pytest.mark.parametrize("d", [3, 5])
+@pytest.mark.parametrize("level", [0, 1, 2])
+def test_reference_golden(d, level):
+    """python/tests/test_error_analysis.py:27-45 on the GPU path."""
+    text = gp.SurfaceCode(d).get_memory(d, 1e-3)
+    dem = gp.get_driver(text, gp.CorrelationLevel(level)).compile_detector_error_model(text)
+    got = {n: p for n, p in dem.named_errors()}
+    compare_errors(got, load_canonical_dem(GOLDEN / "dems" / f"surface{d}_L{level}.dem"), rel=REL)
+
+
+@pytest.mark.parametrize("level", [0, 1, 2])
+def test_driver_reuse(level):
+    """python/tests/test_error_analysis.py:48-59: a d5-sized driver compiles d3."""
+    d5 = gp.SurfaceCode(5).get_memory(5, 1e-3)
+    d3 = gp.SurfaceCode(3).get_memory(3, 1e-3)
+    drv = gp.get_driver(d5, gp.CorrelationLevel(level))
+    dem = drv.compile(d3)
+    got = {n: p for n, p in dem.named_errors()}
+    compare_errors(got, load_canonical_dem(GOLDEN / "dems" / f"surface3_L{level}.dem"), rel=REL)
+    # and back to the larger circuit, then the no-argument overload
+    _check(drv.compile(d5), d5, level)
+    _check(drv.compile(), d5, level)
+
+
+@pytest.mark.parametrize("code,d", [("surface", 7), ("bb", 6), ("bb", 12)])
+@pytest.mark.parametrize("noise", ["uniform", "reference"])
+def test_codes(code, d, noise):
+    c = gp.SurfaceCode(d) if code == "surface" else gp.BBCode(d)
+    text = c.get_memory(d, 1e-3, noise=noise)
+    _check(gp.get_driver(text).compile(text), text)
+
+
+def test_deterministic():
+    text = gp.BBCode(6).get_memory(6, 1e-3, noise="uniform")
+    drv = gp.get_driver(text)
+    a, b = drv.compile(text), drv.compile(text)
+    assert a == b  # same order, same bits
+
+
+@pytest.mark.parametrize("bits", [8, 16])
+def test_short_sort_keys_fall_back_to_full_keys(bits):
+    """Sorting on a few key bits makes runs of different symptoms; the merge must detect them and re-sort."""
+    text = gp.SurfaceCode(5).get_memory(5, 1e-3, noise="uniform")
+    _check(gp.get_driver(text, sort_bits=bits).compile(text), text)
+
+
+def test_empty_and_noiseless():
+    for text in ["R 0\nM 0\nDETECTOR rec[-1]\n", "TICK\n", "R 0\nZ_ERROR(0.1) 0\nM 0\nDETECTOR rec[-1]\n"]:
+        dem = gp.get_driver(text).compile(text)
+        assert dem.num_errors == 0
+
+
+def test_device_stages_and_timings():
+    text = gp.BBCode(6).get_memory(6, 1e-3, noise="uniform")
+    drv = gp.get_driver(text)
+    drv.prepare(text)
+    drv.run_device()
+    dem = drv.fetch()
+    t = drv.last_timings()
+    assert t["total"] > 0 and all(v >= 0 for v in t.values())
+    _check(dem, text)

@@ -1,0 +1,63 @@
+"""Host lowering (libgpc.so, no GPU) checked by interpreting the tape on the CPU."""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN, compare_errors, load_canonical_dem, to_named
+from greenpeas_gb300 import BBCode, SurfaceCode, Tape
+from greenpeas_gb300._native import GpcError
+from oracle import oracle as O
+from tape_interp import compile_tape
+
+SMALL = [
+    "R 0\nX_ERROR(0.1) 0\nM 0\nDETECTOR rec[-1]\n",
+    "R 0 1\nX_ERROR(0.2) 0\nCX 0 1\nM 0 1\nDETECTOR rec[-1]\nDETECTOR rec[-2]\n",
+    "R 0 1 2\nH 0\nDEPOLARIZE1(0.01) 0 1 2\nCZ 0 1\nCY 1 2\nS 2\nDEPOLARIZE2(0.02) 0 2\n"
+    "SWAP 0 1\nSQRT_X 0\nMX(0.03) 0\nMY 1\nMR 2\nDETECTOR rec[-1]\nDETECTOR rec[-2] rec[-3]\n"
+    "OBSERVABLE_INCLUDE(1) rec[-2]\n",
+    "RX 0\nRY 1\nPAULI_CHANNEL_1(0.01,0.02,0.03) 0 1\nE(0.05) X0 Z1\nC_XYZ 0\nH_YZ 1\nXCX 0 1\nXCZ 1 0\n"
+    "M 0 1\nDETECTOR rec[-1]\nDETECTOR rec[-2]\n",
+    "REPEAT 3 {\nR 0 1\nDEPOLARIZE1(0.001) 0 1\nCX 0 1 1 0\nM(0.01) 0 1\nDETECTOR rec[-1]\n}\n",
+]
+
+
+def _oracle(text, level=2):
+    r = O.compile_text(text, level)
+    return {t: p for t, p in r.errors()}
+
+
+@pytest.mark.parametrize("text", SMALL)
+def test_small_circuits_match_oracle(text):
+    compare_errors(compile_tape(Tape(text)), _oracle(text))
+
+
+@pytest.mark.parametrize("d", [3, 5])
+@pytest.mark.parametrize("level", [0, 1, 2])
+def test_surface_golden(d, level):
+    text = SurfaceCode(d).get_memory(d, 1e-3)
+    t = Tape(text, level)
+    got = {to_named(k, t.num_detectors): p for k, p in compile_tape(t).items()}
+    compare_errors(got, load_canonical_dem(GOLDEN / "dems" / f"surface{d}_L{level}.dem"))
+
+
+def test_bb6_uniform_matches_oracle():
+    text = BBCode(6).get_memory(6, 1e-3, noise="uniform")
+    compare_errors(compile_tape(Tape(text)), _oracle(text))
+
+
+def test_tape_shapes():
+    t = Tape(SurfaceCode(3).get_memory(3, 1e-3, noise="uniform"))
+    assert t.num_mechanisms == 1227  # raw mechanisms of the surface d=3 r=3 config
+    assert t.qpad % 32 == 0 and len(t.ops) == int(np.sum(t.ep_k)) * t.qpad
+    assert t.ep_ptoff[-1] == t.num_points
+
+
+@pytest.mark.parametrize("bad,code", [("FOO 0\n", -3), ("CX 0\n", -2), ("DEPOLARIZE1(0.9) 0\n", -2),
+                                      ("REPEAT 2 {\nH 0\n", -2), ("M 0\nDETECTOR rec[-2]\n", -2),
+                                      ("CX rec[-1] 0\n", -3)])
+def test_rejects_bad_input(bad, code):
+    with pytest.raises(GpcError) as ei:
+        Tape(bad)
+    assert ei.value.status == code
