@@ -24,7 +24,8 @@ EXPORTS = [
     "gpc_get_driver", "gpc_compile", "gpc_compile_batch", "gpc_dem_arrays", "gpc_dem_info",
     "gpc_dem_text", "gpc_dem_free", "gpc_driver_destroy", "gpc_last_error", "gpc_prepare",
     "gpc_run_device", "gpc_fetch", "gpc_driver_stream", "gpc_last_timings", "gpc_last_sizes",
-    "gpc_tape_lower", "gpc_tape_get_view", "gpc_tape_free", "gpc_tape_last_error",
+    "gpc_tape_lower", "gpc_tape_get_view", "gpc_tape_free", "gpc_tape_last_error", "gpc_last_traffic",
+    "gpc_last_io_bytes",
 ]
 
 
@@ -37,7 +38,8 @@ class GpcError(RuntimeError):
 
 
 class Options(ctypes.Structure):
-    _fields_ = [("device", ctypes.c_int32), ("sort_bits", ctypes.c_int32), ("reserved", ctypes.c_int32 * 6)]
+    _fields_ = [("device", ctypes.c_int32), ("sort_bits", ctypes.c_int32), ("global_sort", ctypes.c_int32),
+                ("reserved", ctypes.c_int32 * 5)]
 
 
 class TapeView(ctypes.Structure):
@@ -45,12 +47,12 @@ class TapeView(ctypes.Structure):
         ("num_qubits", ctypes.c_uint32), ("qpad", ctypes.c_uint32), ("num_measurements", ctypes.c_uint32),
         ("num_detectors", ctypes.c_uint32), ("num_observables", ctypes.c_uint32), ("words", ctypes.c_uint32),
         ("num_epochs", ctypes.c_uint32), ("kmax", ctypes.c_uint32), ("num_points", ctypes.c_uint32),
-        ("num_mechanisms", ctypes.c_uint32), ("num_ops", ctypes.c_uint64),
+        ("num_mechanisms", ctypes.c_uint32), ("num_records", ctypes.c_uint32), ("num_ops", ctypes.c_uint64),
         ("ops", ctypes.POINTER(ctypes.c_uint64)), ("ep_opoff", ctypes.POINTER(ctypes.c_uint32)),
         ("ep_k", ctypes.POINTER(ctypes.c_uint32)), ("ep_ptoff", ctypes.POINTER(ctypes.c_uint32)),
-        ("meas_off", ctypes.POINTER(ctypes.c_uint32)), ("meas_bits", ctypes.POINTER(ctypes.c_uint32)),
         ("inj_lo", ctypes.POINTER(ctypes.c_uint32)), ("inj_hi", ctypes.POINTER(ctypes.c_uint32)),
-        ("desc", ctypes.POINTER(ctypes.c_uint64)), ("prob", ctypes.POINTER(ctypes.c_double)),
+        ("rec", ctypes.POINTER(ctypes.c_uint64)), ("rec_p", ctypes.POINTER(ctypes.c_double)),
+        ("rec_moff", ctypes.POINTER(ctypes.c_uint32)),
     ]
 
 
@@ -87,6 +89,8 @@ def lib() -> ctypes.CDLL:
     L.gpc_driver_stream.restype = vp
     L.gpc_last_timings.argtypes = [vp, ctypes.POINTER(ctypes.c_float)]
     L.gpc_last_sizes.argtypes = [vp, u64p, u64p, u32p, u32p, u32p]
+    L.gpc_last_traffic.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
+    L.gpc_last_io_bytes.argtypes = [vp, u64p, u64p]
     L.gpc_tape_lower.argtypes = [ctypes.c_char_p, sz, i32, ctypes.POINTER(vp)]
     L.gpc_tape_get_view.argtypes = [vp, ctypes.POINTER(TapeView)]
     L.gpc_tape_free.argtypes = [vp]
@@ -94,7 +98,7 @@ def lib() -> ctypes.CDLL:
     L.gpc_tape_last_error.restype = ctypes.c_char_p
     for f in ("gpc_get_driver", "gpc_compile", "gpc_compile_batch", "gpc_dem_arrays", "gpc_dem_info",
               "gpc_dem_text", "gpc_prepare", "gpc_run_device", "gpc_fetch", "gpc_last_timings",
-              "gpc_last_sizes", "gpc_tape_lower", "gpc_tape_get_view"):
+              "gpc_last_sizes", "gpc_tape_lower", "gpc_tape_get_view", "gpc_last_traffic", "gpc_last_io_bytes"):
         getattr(L, f).restype = i32
     _lib = L
     return L

@@ -12,6 +12,8 @@ enum : uint32_t {
   DEV_ERR_COLLISION = 2u,  // equal 128-bit keys, different symptoms
   DEV_FLAG_MIXED = 4u,     // equal sort keys, different 128-bit keys: re-sort on 128 bits
   DEV_FLAG_TG_OVF = 8u,    // target buffer too small: grow and re-run the merge
+  DEV_FLAG_BIG_BUCKET = 16u,  // a bucket exceeds the in-CTA capacity: use the global sort
+  DEV_FLAG_LONG = 32u,        // a symptom has more targets than the target-list stride: widen it
 };
 
 // One circuit as the kernels see it.  All arrays are device pointers.
@@ -20,27 +22,30 @@ struct CircuitDev {
   const uint32_t *ep_opoff;   // [n_epochs]
   const uint32_t *ep_k;       // [n_epochs]
   const uint32_t *ep_ptoff;   // [n_epochs + 1]
-  const uint32_t *meas_off;   // [nmeas + 1]
-  const uint32_t *meas_bits;  // bit indices of each measurement
   const uint32_t *inj_lo;     // [w] first epoch injecting into word j (0xFFFFFFFF: none)
   const uint32_t *inj_hi;     // [w] last epoch injecting into word j
   ulonglong2 *snap;           // [w][npoints] (X row, Z row) at each point
   uint2 *band;                // [w] point range written by the walk of word j
-  const uint64_t *desc;       // [M] mechanism descriptors
-  const double *prob;         // [M]
+  const uint64_t *rec;        // [R] noise records
+  const double *rec_p;        // [R]
+  const uint32_t *rec_moff;   // [R + 1]
+  uint64_t *mdesc;            // [M] mechanism descriptors (written by the key kernel)
+  double *mp;                 // [M] mechanism probabilities (written by the key kernel)
+  uint32_t *tl;               // [M][tcap] targets of each mechanism, ascending (written by the key kernel)
+  uint32_t *tn;               // [M] number of targets of each mechanism
   uint32_t nq, qpad, n_epochs, w;
-  uint32_t npoints, M;
-  uint32_t mech_base;  // first global mechanism index of this circuit
-  uint32_t pad_;
+  uint32_t npoints, M, R;
+  uint32_t tcap;              // stride of tl (0: no target lists, merge from snapshots)
 };
 
-// Sizes of the sort / merge scratch for n items.
 constexpr int SORT_THREADS = 256;
 constexpr int SORT_IPT = 8;
 constexpr int SORT_TILE = SORT_THREADS * SORT_IPT;
 constexpr int RADIX_BITS = 8;
 constexpr int RADIX = 1 << RADIX_BITS;
 constexpr int MERGE_THREADS = 256;
+constexpr int BUCKET_THREADS = 128;
+constexpr int BUCKET_CAP = 1024;  // items one CTA sorts in shared memory
 
 inline uint32_t sort_tiles(uint32_t n) { return (n + SORT_TILE - 1) / SORT_TILE; }
 inline uint32_t merge_tiles(uint32_t n) { return (n + MERGE_THREADS - 1) / MERGE_THREADS; }
@@ -52,25 +57,67 @@ struct WalkLaunch {
   uint32_t n_items;
   uint32_t threads, qpt, qpad;
   uint32_t ring_slots, slot_bytes;
+  uint32_t max_epochs;      // largest n_epochs of the launch (sizes the epoch table in shared memory)
   uint32_t *err;
 };
 cudaError_t launch_walk(const WalkLaunch &L, cudaStream_t s);
-size_t walk_smem_bytes(uint32_t qpad, uint32_t ring_slots, uint32_t slot_bytes);
+size_t walk_smem_bytes(uint32_t qpad, uint32_t ring_slots, uint32_t slot_bytes, uint32_t max_epochs);
 
-// Key kernel: one thread per mechanism of a single circuit.
-cudaError_t launch_keys(const CircuitDev *c_dev, uint32_t M, uint32_t w, ulonglong2 *key, uint64_t *sortkey,
-                        uint32_t *perm, cudaStream_t s);
+// Key kernel: one thread per noise record; expands the record into its
+// mechanisms (mdesc, mp), computes each mechanism's 128-bit key, and counts
+// non-empty keys per bucket (top `bucket_bits` bits of key.x).
+struct KeyLaunch {
+  const CircuitDev *c_dev;
+  uint32_t R, w;
+  ulonglong2 *key;          // [M]
+  uint32_t *bucket_count;   // [1 << bucket_bits] (zeroed)
+  uint32_t bucket_bits;
+  uint32_t *list_total;     // += targets written to the lists (for traffic accounting)
+  uint32_t *err;
+};
+cudaError_t launch_keys(const KeyLaunch &L, cudaStream_t s);
 
+// Exclusive scan of the bucket counts into bucket offsets (+ total at [nb]).
+cudaError_t launch_bucket_scan(const uint32_t *count, uint32_t *offset, uint32_t nb, cudaStream_t s);
+
+// Moves every non-empty mechanism to its bucket: items (key, m).
+cudaError_t launch_bucket_scatter(const ulonglong2 *key, uint32_t M, uint32_t bucket_bits, const uint32_t *offset,
+                                  uint32_t *cursor, ulonglong2 *bkey, uint32_t *bm, cudaStream_t s);
+
+struct BucketMergeLaunch {
+  const CircuitDev *c_dev;
+  uint32_t w;
+  const ulonglong2 *bkey;   // bucketed keys
+  const uint32_t *bm;       // bucketed mechanism ids
+  const uint32_t *count;    // [nb]
+  const uint32_t *offset;   // [nb]
+  uint32_t nb;
+  uint32_t max_groups;      // capacity of out_prob / out_off (the mechanism count)
+  double *out_prob;
+  uint32_t *out_off;
+  uint32_t *out_tg;
+  uint32_t tg_cap;
+  unsigned long long *status;  // [nb]
+  uint32_t *ticket;
+  uint32_t *totals;  // [0] groups, [1] targets
+  uint32_t *err;
+};
+cudaError_t launch_bucket_merge(const BucketMergeLaunch &L, cudaStream_t s);
+
+// ---- global path (used when a bucket is too large for one CTA) -------------
 // Onesweep radix sort of (u64 key, u32 value) pairs on the low `bits` bits.
 struct SortScratch {
-  uint32_t *hist;        // [passes][RADIX]
-  uint32_t *status;      // [passes][tiles][RADIX]
-  uint32_t *tile_ctr;    // [passes]
+  uint32_t *hist;      // [passes][RADIX]
+  uint32_t *status;    // [passes][tiles][RADIX]
+  uint32_t *tile_ctr;  // [passes]
   uint32_t *err;
 };
 size_t sort_scratch_words(uint32_t n, uint32_t bits);
 cudaError_t launch_sort(uint64_t *keys, uint64_t *keys_alt, uint32_t *vals, uint32_t *vals_alt, uint32_t n,
                         uint32_t bits, const SortScratch &scr, cudaStream_t s, bool *result_in_alt);
+
+// sortkey[m] = key[m].x, perm[m] = m (inputs of the global sort).
+cudaError_t launch_sort_init(const ulonglong2 *key, uint64_t *sortkey, uint32_t *perm, uint32_t M, cudaStream_t s);
 
 // Gathers key128[perm[i]].y into out[i] (second pass of a 128-bit sort).
 cudaError_t launch_gather_hi(const ulonglong2 *key, const uint32_t *perm, uint64_t *out, uint32_t n, cudaStream_t s);

@@ -97,13 +97,15 @@ struct HostBuf {
 // Byte offsets of every array inside the arena (inputs first, so the whole
 // input region is one contiguous H2D copy).
 struct Layout {
-  size_t ops, ep_opoff, ep_k, ep_ptoff, meas_off, meas_bits, inj_lo, inj_hi, desc, prob, cdev, items;
+  size_t ops, ep_opoff, ep_k, ep_ptoff, inj_lo, inj_hi, rec, rec_p, rec_moff, cdev, items;
   size_t in_bytes;
-  size_t snap, band, key, sk0, sk1, pm0, pm1, hik;
-  size_t zero, err, totals, sort_scr, merge_status, merge_ctr, zero_bytes;
+  size_t snap, band, mdesc, mp, tl, tn, key, boff, bkey, bm;
+  size_t sk0, sk1, pm0, pm1, hik;  // global path
+  size_t zero, err, totals, bcount, bcursor, bstatus, bticket, zero_bytes;
+  size_t gzero, sort_scr, merge_status, merge_ctr, gzero_bytes;  // global path scratch
   size_t out_prob, out_off;
   size_t total;
-  uint32_t sort_tiles, merge_tiles;
+  uint32_t sort_tiles, merge_tiles, nb, bucket_bits;
   size_t sort_words;
 };
 
@@ -140,6 +142,11 @@ struct gpc_driver {
   uint64_t *sk_sorted = nullptr;
   uint64_t sort_mask = ~0ull;
   uint32_t ring_slots = 1, slot_bytes = 0, threads = 32, qpt = 1;
+  bool force_global = false;  // debug/test option: skip the bucket path
+  uint32_t tcap = 32;         // target-list stride (grows when a symptom is longer)
+  bool lists_off = false;     // symptoms too long for target lists: merge from snapshots
+  uint64_t last_d2h = 0;      // bytes copied device -> host by the last fetch
+  bool used_global = false;
 
   ~gpc_driver() {
     if (stream) cudaStreamSynchronize(stream);
@@ -159,7 +166,7 @@ struct gpc_driver {
 
   void layout() {
     const Tape &T = tape;
-    const uint32_t M = (uint32_t)T.desc.size();
+    const uint32_t M = T.M, R = (uint32_t)T.rec.size();
     size_t o = 0;
     auto take = [&](size_t bytes) {
       size_t r = o;
@@ -170,18 +177,40 @@ struct gpc_driver {
     L.ep_opoff = take(T.ep_opoff.size() * 4);
     L.ep_k = take(T.ep_k.size() * 4);
     L.ep_ptoff = take(T.ep_ptoff.size() * 4);
-    L.meas_off = take(T.meas_off.size() * 4);
-    L.meas_bits = take(T.meas_bits.size() * 4);
     L.inj_lo = take(T.inj_lo.size() * 4);
     L.inj_hi = take(T.inj_hi.size() * 4);
-    L.desc = take((size_t)M * 8);
-    L.prob = take((size_t)M * 8);
+    L.rec = take((size_t)R * 8);
+    L.rec_p = take((size_t)R * 8);
+    L.rec_moff = take((size_t)(R + 1) * 4);
     L.cdev = take(sizeof(CircuitDev));
     L.items = take((size_t)T.w * sizeof(uint2));
     L.in_bytes = o;
+    // buckets: about 96 mechanisms each, a power of two between 2^4 and 2^16
+    uint32_t bb = 4;
+    while (bb < 16 && ((uint64_t)96 << bb) < M) ++bb;
+    L.bucket_bits = bb;
+    L.nb = 1u << bb;
     L.snap = take((size_t)T.w * T.npoints * 16);
     L.band = take((size_t)T.w * 8);
+    L.mdesc = take((size_t)M * 8);
+    L.mp = take((size_t)M * 8);
+    L.tl = take((size_t)M * tcap * 4);
+    L.tn = take((size_t)M * 4);
     L.key = take((size_t)M * 16);
+    L.boff = take((size_t)(L.nb + 1) * 4);
+    L.bkey = take((size_t)M * 16);
+    L.bm = take((size_t)M * 4);
+    L.zero = o;
+    L.err = take(4);
+    L.totals = take(16);
+    L.bcount = take((size_t)L.nb * 4);
+    L.bcursor = take((size_t)L.nb * 4);
+    L.bstatus = take((size_t)L.nb * 8);
+    L.bticket = take(4);
+    L.zero_bytes = o - L.zero;
+    L.out_prob = take((size_t)M * 8);
+    L.out_off = take((size_t)(M + 1) * 4);
+    // global path (only touched when a bucket overflows or it is forced)
     L.sk0 = take((size_t)M * 8);
     L.sk1 = take((size_t)M * 8);
     L.pm0 = take((size_t)M * 4);
@@ -190,15 +219,11 @@ struct gpc_driver {
     L.sort_tiles = gpc::sort_tiles(M);
     L.merge_tiles = gpc::merge_tiles(M);
     L.sort_words = gpc::sort_scratch_words(M, 64);
-    L.zero = o;
-    L.err = take(4);
-    L.totals = take(8);
+    L.gzero = o;
     L.sort_scr = take(L.sort_words * 4);
     L.merge_status = take((size_t)L.merge_tiles * 8);
     L.merge_ctr = take(4);
-    L.zero_bytes = o - L.zero;
-    L.out_prob = take((size_t)M * 8);
-    L.out_off = take((size_t)(M + 1) * 4);
+    L.gzero_bytes = o - L.gzero;
     L.total = o;
   }
 
@@ -213,32 +238,35 @@ struct gpc_driver {
     put(L.ep_opoff, T.ep_opoff.data(), T.ep_opoff.size() * 4);
     put(L.ep_k, T.ep_k.data(), T.ep_k.size() * 4);
     put(L.ep_ptoff, T.ep_ptoff.data(), T.ep_ptoff.size() * 4);
-    put(L.meas_off, T.meas_off.data(), T.meas_off.size() * 4);
-    put(L.meas_bits, T.meas_bits.data(), T.meas_bits.size() * 4);
     put(L.inj_lo, T.inj_lo.data(), T.inj_lo.size() * 4);
     put(L.inj_hi, T.inj_hi.data(), T.inj_hi.size() * 4);
-    put(L.desc, T.desc.data(), T.desc.size() * 8);
-    put(L.prob, T.prob.data(), T.prob.size() * 8);
+    put(L.rec, T.rec.data(), T.rec.size() * 8);
+    put(L.rec_p, T.rec_p.data(), T.rec_p.size() * 8);
+    put(L.rec_moff, T.rec_moff.data(), T.rec_moff.size() * 4);
     CircuitDev c{};
     c.ops = dptr<uint64_t>(L.ops);
     c.ep_opoff = dptr<uint32_t>(L.ep_opoff);
     c.ep_k = dptr<uint32_t>(L.ep_k);
     c.ep_ptoff = dptr<uint32_t>(L.ep_ptoff);
-    c.meas_off = dptr<uint32_t>(L.meas_off);
-    c.meas_bits = dptr<uint32_t>(L.meas_bits);
     c.inj_lo = dptr<uint32_t>(L.inj_lo);
     c.inj_hi = dptr<uint32_t>(L.inj_hi);
     c.snap = dptr<ulonglong2>(L.snap);
     c.band = dptr<uint2>(L.band);
-    c.desc = dptr<uint64_t>(L.desc);
-    c.prob = dptr<double>(L.prob);
+    c.rec = dptr<uint64_t>(L.rec);
+    c.rec_p = dptr<double>(L.rec_p);
+    c.rec_moff = dptr<uint32_t>(L.rec_moff);
+    c.mdesc = dptr<uint64_t>(L.mdesc);
+    c.mp = dptr<double>(L.mp);
+    c.tl = dptr<uint32_t>(L.tl);
+    c.tn = dptr<uint32_t>(L.tn);
+    c.tcap = tcap;
     c.nq = T.nq;
     c.qpad = T.qpad;
     c.n_epochs = T.n_epochs;
     c.w = T.w;
     c.npoints = T.npoints;
-    c.M = (uint32_t)T.desc.size();
-    c.mech_base = 0;
+    c.M = T.M;
+    c.R = (uint32_t)T.rec.size();
     put(L.cdev, &c, sizeof(c));
     std::vector<uint2> items(T.w);
     for (uint32_t j = 0; j < T.w; ++j) items[j] = make_uint2(0u, j);
@@ -250,6 +278,8 @@ struct gpc_driver {
     prepared = false;
     ran = false;
     if (text) {
+      tcap = 32;
+      lists_off = false;
       parsed = gpc::parse_stim(text, len);
       gpc::LowerOptions lo;
       lo.level = level;
@@ -262,7 +292,7 @@ struct gpc_driver {
     // The stream may still be reading the old arena: finish before regrowing.
     CK(cudaStreamSynchronize(stream));
     arena.ensure(L.total);
-    const uint32_t M = (uint32_t)tape.desc.size();
+    const uint32_t M = tape.M;
     uint32_t want_tg = std::max<uint32_t>(1024u, std::min<uint64_t>(0xFFFFFFF0ull, (uint64_t)M * 16));
     if (want_tg > tg_cap) {
       tgbuf.ensure((size_t)want_tg * 4);
@@ -275,7 +305,7 @@ struct gpc_driver {
     threads = tape.qpad / qpt;
     slot_bytes = std::max<uint32_t>(1, tape.kmax) * tape.qpad * 8;
     const size_t budget = 200 * 1024;
-    const size_t fixed = (size_t)2 * tape.qpad * 16 + 128;
+    const size_t fixed = gpc::walk_smem_bytes(tape.qpad, 0, 0, tape.n_epochs);
     size_t slots = budget > fixed ? (budget - fixed) / slot_bytes : 0;
     if (slots < 1) throw gpc::Error(GPC_ERR_CAPACITY, "tape epoch too large for shared memory");
     ring_slots = (uint32_t)std::min<size_t>(8, slots);
@@ -286,7 +316,6 @@ struct gpc_driver {
     if (!prepared) throw gpc::Error(GPC_ERR_INVALID, "no circuit prepared");
     CK(cudaSetDevice(device));
     const Tape &T = tape;
-    const uint32_t M = (uint32_t)T.desc.size();
     CK(cudaMemsetAsync(dptr<char>(L.zero), 0, L.zero_bytes, stream));
     CK(cudaEventRecord(ev[0], stream));
     gpc::WalkLaunch wl{};
@@ -298,20 +327,70 @@ struct gpc_driver {
     wl.qpad = T.qpad;
     wl.ring_slots = ring_slots;
     wl.slot_bytes = slot_bytes;
+    wl.max_epochs = T.n_epochs;
     wl.err = dptr<uint32_t>(L.err);
     if (T.n_epochs > 0) CK(gpc::launch_walk(wl, stream));
     else CK(cudaMemsetAsync(dptr<char>(L.band), 0, (size_t)T.w * 8, stream));
     CK(cudaEventRecord(ev[1], stream));
-    CK(gpc::launch_keys(dptr<CircuitDev>(L.cdev), M, T.w, dptr<ulonglong2>(L.key), dptr<uint64_t>(L.sk0),
-                        dptr<uint32_t>(L.pm0), stream));
+    gpc::KeyLaunch kl{};
+    kl.c_dev = dptr<CircuitDev>(L.cdev);
+    kl.R = (uint32_t)T.rec.size();
+    kl.w = T.w;
+    kl.key = dptr<ulonglong2>(L.key);
+    kl.bucket_count = dptr<uint32_t>(L.bcount);
+    kl.bucket_bits = L.bucket_bits;
+    kl.list_total = dptr<uint32_t>(L.totals) + 2;
+    kl.err = dptr<uint32_t>(L.err);
+    CK(gpc::launch_keys(kl, stream));
     CK(cudaEventRecord(ev[2], stream));
-    sort_and_merge(false);
+    used_global = false;
+    if (force_global || lists_off) {
+      run_global(false);
+    } else {
+      CK(gpc::launch_bucket_scan(dptr<uint32_t>(L.bcount), dptr<uint32_t>(L.boff), L.nb, stream));
+      CK(gpc::launch_bucket_scatter(dptr<ulonglong2>(L.key), T.M, L.bucket_bits, dptr<uint32_t>(L.boff),
+                                    dptr<uint32_t>(L.bcursor), dptr<ulonglong2>(L.bkey), dptr<uint32_t>(L.bm),
+                                    stream));
+      CK(cudaEventRecord(ev[3], stream));
+      launch_bucket_merge_now();
+      CK(cudaEventRecord(ev[4], stream));
+    }
     ran = true;
+  }
+
+  void launch_bucket_merge_now() {
+    gpc::BucketMergeLaunch bl{};
+    bl.c_dev = dptr<CircuitDev>(L.cdev);
+    bl.w = tape.w;
+    bl.bkey = dptr<ulonglong2>(L.bkey);
+    bl.bm = dptr<uint32_t>(L.bm);
+    bl.count = dptr<uint32_t>(L.bcount);
+    bl.offset = dptr<uint32_t>(L.boff);
+    bl.nb = L.nb;
+    bl.max_groups = tape.M;
+    bl.out_prob = dptr<double>(L.out_prob);
+    bl.out_off = dptr<uint32_t>(L.out_off);
+    bl.out_tg = static_cast<uint32_t *>(tgbuf.p);
+    bl.tg_cap = tg_cap;
+    bl.status = dptr<unsigned long long>(L.bstatus);
+    bl.ticket = dptr<uint32_t>(L.bticket);
+    bl.totals = dptr<uint32_t>(L.totals);
+    bl.err = dptr<uint32_t>(L.err);
+    CK(gpc::launch_bucket_merge(bl, stream));
+  }
+
+  // Global path: sort every mechanism (on sort_bits, or all 128 bits) and merge.
+  void run_global(bool full) {
+    used_global = true;
+    CK(cudaMemsetAsync(dptr<char>(L.gzero), 0, L.gzero_bytes, stream));
+    CK(cudaMemsetAsync(dptr<char>(L.totals), 0, 8, stream));
+    CK(gpc::launch_sort_init(dptr<ulonglong2>(L.key), dptr<uint64_t>(L.sk0), dptr<uint32_t>(L.pm0), tape.M, stream));
+    sort_and_merge(full);
   }
 
   // Sorts (on sort_bits, or on the full 128-bit key when `full`) and merges.
   void sort_and_merge(bool full) {
-    const uint32_t M = (uint32_t)tape.desc.size();
+    const uint32_t M = tape.M;
     uint32_t *sw = dptr<uint32_t>(L.sort_scr);
     const uint32_t passes = 8;
     const size_t one = (size_t)passes * gpc::RADIX + (size_t)passes * L.sort_tiles * gpc::RADIX + passes;
@@ -346,7 +425,7 @@ struct gpc_driver {
   }
 
   void launch_merge_now() {
-    const uint32_t M = (uint32_t)tape.desc.size();
+    const uint32_t M = tape.M;
     gpc::MergeLaunch ml{};
     ml.c_dev = dptr<CircuitDev>(L.cdev);
     ml.w = tape.w;
@@ -372,12 +451,13 @@ struct gpc_driver {
     CK(cudaMemsetAsync(dptr<char>(L.totals), 0, 8, stream));
   }
 
-  // Reads flags and totals; handles the rare re-sort / target-buffer growth.
+  // Reads flags and totals; handles the rare fallbacks (bucket overflow,
+  // short sort keys, target-buffer growth).
   void finish(uint32_t *groups, uint32_t *targets) {
     pin_out.ensure(64);
     uint32_t *h = static_cast<uint32_t *>(pin_out.p);
     bool did_full = false;
-    for (int attempt = 0; attempt < 4; ++attempt) {
+    for (int attempt = 0; attempt < 6; ++attempt) {
       CK(cudaMemcpyAsync(h, dptr<char>(L.err), 4, cudaMemcpyDeviceToHost, stream));
       CK(cudaMemcpyAsync(h + 1, dptr<char>(L.totals), 8, cudaMemcpyDeviceToHost, stream));
       CK(cudaStreamSynchronize(stream));
@@ -385,10 +465,29 @@ struct gpc_driver {
       if (err & gpc::DEV_ERR_TIMEOUT) throw gpc::Error(GPC_ERR_TIMEOUT, "a bounded device wait timed out");
       if (err & gpc::DEV_ERR_COLLISION)
         throw gpc::Error(GPC_ERR_COLLISION, "two different symptoms share a 128-bit key");
-      if ((err & gpc::DEV_FLAG_MIXED) && !did_full) {
+      if ((err & gpc::DEV_FLAG_LONG) && !used_global) {
+        // a symptom longer than the target-list stride: widen it (or give up on
+        // lists and merge from the snapshots) and run again
+        if (tcap < 256) {
+          tcap *= 4;
+        } else {
+          tcap = 0;
+          lists_off = true;
+        }
+        prepare(nullptr, 0);
+        run();
+        continue;
+      }
+      if ((err & gpc::DEV_FLAG_BIG_BUCKET) && !used_global) {
+        // a symptom repeated more often than one CTA holds: sort globally
+        CK(cudaMemsetAsync(dptr<char>(L.err), 0, 4, stream));
+        run_global(false);
+        continue;
+      }
+      if (used_global && (err & gpc::DEV_FLAG_MIXED) && !did_full) {
         // equal sort keys with different full keys: sort on all 128 bits
-        CK(cudaMemsetAsync(dptr<char>(L.zero), 0, L.zero_bytes, stream));
-        sort_and_merge(true);
+        CK(cudaMemsetAsync(dptr<char>(L.err), 0, 4, stream));
+        run_global(true);
         did_full = true;
         continue;
       }
@@ -397,17 +496,55 @@ struct gpc_driver {
         tgbuf.ensure((size_t)need * 4 + 1024);
         tg_cap = (uint32_t)std::min<size_t>(0xFFFFFFF0ull, tgbuf.cap / 4);
         CK(cudaMemsetAsync(dptr<char>(L.err), 0, 4, stream));
-        reset_merge_scratch();
-        launch_merge_now();
+        if (used_global) {
+          reset_merge_scratch();
+          launch_merge_now();
+        } else {
+          CK(cudaMemsetAsync(dptr<char>(L.bstatus), 0, (size_t)L.nb * 8, stream));
+          CK(cudaMemsetAsync(dptr<char>(L.bticket), 0, 4, stream));
+          CK(cudaMemsetAsync(dptr<char>(L.totals), 0, 8, stream));
+          launch_bucket_merge_now();
+        }
         continue;
       }
-      const uint32_t M = (uint32_t)tape.desc.size();
+      const uint32_t M = tape.M;
       if (h[1] > M || h[2] > tg_cap) throw gpc::Error(GPC_ERR_CUDA, "inconsistent merge totals");
       *groups = h[1];
       *targets = h[2];
       return;
     }
     throw gpc::Error(GPC_ERR_CUDA, "merge did not converge");
+  }
+
+  // Algorithmic bytes of each kernel of the last run (walk, key, bucket scan+scatter,
+  // merge): what the design must move, counted from the run's own sizes.
+  void traffic(double out[4]) {
+    const Tape &T = tape;
+    CK(cudaStreamSynchronize(stream));
+    std::vector<uint2> band(T.w);
+    uint32_t tot[4] = {0, 0, 0, 0};
+    uint32_t nonempty = 0;
+    CK(cudaMemcpy(band.data(), dptr<char>(L.band), (size_t)T.w * 8, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(tot, dptr<char>(L.totals), 12, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(&nonempty, dptr<char>(L.boff) + (size_t)L.nb * 4, 4, cudaMemcpyDeviceToHost));
+    const uint64_t opsBytes = T.ops.size() * 8;
+    double walk = 0, pts = 0;
+    for (uint32_t j = 0; j < T.w; ++j) {
+      if (band[j].y <= band[j].x) continue;
+      const uint32_t e0 = T.inj_lo[j];
+      // last epoch walked: the one whose points end at band.y
+      uint32_t e1 = (uint32_t)(std::lower_bound(T.ep_ptoff.begin(), T.ep_ptoff.end(), band[j].y) - T.ep_ptoff.begin());
+      if (e1 > T.n_epochs) e1 = T.n_epochs;
+      const uint64_t a = T.ep_opoff[e0], b = e1 < T.n_epochs ? T.ep_opoff[e1] : opsBytes / 8;
+      walk += (double)(b - a) * 8 + 16.0 * (band[j].y - band[j].x);
+      pts += band[j].y - band[j].x;
+    }
+    const double R = (double)T.rec.size(), M = T.M;
+    const double lists = tot[2];
+    out[0] = walk;
+    out[1] = R * 20 + 16.0 * pts + M * (16 + 8 + 8 + 4) + 4.0 * lists;
+    out[2] = (double)L.nb * 12 + M * 16 + (double)nonempty * 20;
+    out[3] = (double)nonempty * (20 + 4 + 8) + 8.0 * lists + (double)tot[0] * 12 + (double)tot[1] * 4;
   }
 
   gpc_dem *fetch() {
@@ -418,8 +555,9 @@ struct gpc_driver {
     auto dem = std::make_unique<gpc_dem>();
     dem->num_detectors = tape.ndet;
     dem->num_observables = tape.nobs;
-    dem->num_raw = tape.desc.size();
+    dem->num_raw = tape.M;
     const size_t bytes = (size_t)C * 8 + (size_t)C * 4 + (size_t)NT * 4 + 64;
+    last_d2h = (uint64_t)C * 12 + (uint64_t)NT * 4 + 12;  // results + flags and totals
     pin_out.ensure(bytes);
     char *h = static_cast<char *>(pin_out.p);
     if (C) {
@@ -476,6 +614,7 @@ gpc_status gpc_get_driver(const char *stim_text, size_t len, int32_t correlation
     d->device = options->device;
     if (options->sort_bits < 0 || options->sort_bits > 64) return fail(GPC_ERR_INVALID, "sort_bits must be in 0..64");
     if (options->sort_bits) d->sort_bits = (uint32_t)options->sort_bits;
+    d->force_global = options->global_sort != 0;
   }
   gpc_status st = guarded([&] {
     int n = 0;
@@ -597,10 +736,23 @@ gpc_status gpc_last_timings(gpc_driver *driver, float *ms5) {
   });
 }
 
+gpc_status gpc_last_traffic(gpc_driver *driver, double *bytes4) {
+  if (!driver || !bytes4) return fail(GPC_ERR_INVALID, "null argument");
+  if (!driver->ran) return fail(GPC_ERR_INVALID, "nothing has been run");
+  return guarded([&] { driver->traffic(bytes4); });
+}
+
+gpc_status gpc_last_io_bytes(gpc_driver *driver, uint64_t *h2d, uint64_t *d2h) {
+  if (!driver) return fail(GPC_ERR_INVALID, "driver is null");
+  if (h2d) *h2d = driver->L.in_bytes;
+  if (d2h) *d2h = driver->last_d2h;
+  return GPC_OK;
+}
+
 gpc_status gpc_last_sizes(gpc_driver *driver, uint64_t *raw, uint64_t *points, uint32_t *epochs, uint32_t *words,
                           uint32_t *qubits) {
   if (!driver) return fail(GPC_ERR_INVALID, "driver is null");
-  if (raw) *raw = driver->tape.desc.size();
+  if (raw) *raw = driver->tape.M;
   if (points) *points = driver->tape.npoints;
   if (epochs) *epochs = driver->tape.n_epochs;
   if (words) *words = driver->tape.w;

@@ -269,15 +269,35 @@ bool dep2_kept(int level, int pa, int pb) {
 // Swaps the qubit halves of a two-qubit mask (Xa,Za,Xb,Zb) -> (Xb,Zb,Xa,Za).
 uint32_t swap_halves(uint32_t m) { return ((m >> 2) & 3u) | ((m & 3u) << 2); }
 
+// One tape entry placed by the backward scheduler: qubit, epoch, slot, op.
 struct Entry {
-  uint32_t epoch;
+  uint32_t q, e, k;
   uint64_t op;
 };
 
 struct QState {
-  int64_t last = -1;   // epoch of the latest entry
-  uint32_t cnt = 0;    // entries in that epoch
+  int64_t last = -1;      // epoch of the latest entry
+  uint32_t cnt = 0;       // entries in that epoch
   uint32_t open = kNone;  // point holding the current rows (until a row-changing op)
+};
+
+// Memoises the last split so uniform noise costs one sqrt/pow per distinct p.
+struct SplitCache {
+  double p1 = -1, s1 = 0, p2 = -1, s2 = 0;
+  double dep1(double p) {
+    if (p != p1) {
+      p1 = p;
+      s1 = split_dep1(p);
+    }
+    return s1;
+  }
+  double dep2(double p) {
+    if (p != p2) {
+      p2 = p;
+      s2 = split_dep2(p);
+    }
+    return s2;
+  }
 };
 
 }  // namespace
@@ -382,6 +402,7 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
   T.nbits = ndet + nobs;
   T.w = std::max<uint32_t>(1, (T.nbits + 63) / 64);
   if (nq > 4096) throw Error(GPC_ERR_CAPACITY, "more than 4096 qubits");
+  if (T.nbits >= (1u << 24)) throw Error(GPC_ERR_CAPACITY, "more than 2^24 detectors and observables");
   {
     uint32_t qpt = nq <= 1024 ? 1 : nq <= 2048 ? 2 : 4;
     uint32_t per = (nq + qpt - 1) / qpt;
@@ -392,33 +413,37 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
   }
 
   // measurement -> bits (XOR: a measurement listed twice in one detector cancels)
+  std::vector<uint32_t> moff(m + 1, 0), mbits;
   {
     std::vector<std::pair<uint32_t, uint32_t>> mb;
     mb.reserve(detPairs.size() + obsPairs.size());
     for (auto &d : detPairs) mb.push_back(d);
     for (auto &o : obsPairs) mb.push_back({o.first, ndet + o.second});
     std::sort(mb.begin(), mb.end());
-    T.meas_off.assign(m + 1, 0);
     std::vector<std::pair<uint32_t, uint32_t>> kept;
+    kept.reserve(mb.size());
     for (size_t i = 0; i < mb.size();) {
       size_t j = i;
       while (j < mb.size() && mb[j] == mb[i]) ++j;
       if ((j - i) & 1) kept.push_back(mb[i]);
       i = j;
     }
-    for (auto &k : kept) T.meas_off[k.first + 1]++;
-    for (uint32_t i = 0; i < m; ++i) T.meas_off[i + 1] += T.meas_off[i];
-    T.meas_bits.resize(kept.size());
-    for (size_t i = 0; i < kept.size(); ++i) T.meas_bits[i] = kept[i].second;  // already grouped by meas
+    for (auto &k : kept) moff[k.first + 1]++;
+    for (uint32_t i = 0; i < m; ++i) moff[i + 1] += moff[i];
+    mbits.resize(kept.size());
+    for (size_t i = 0; i < kept.size(); ++i) mbits[i] = kept[i].second;
   }
 
-  // ---- backward pass: epoch scheduling and mechanisms ---------------------
-  std::vector<std::vector<Entry>> ent(nq);
+  // ---- backward pass: epoch scheduling and noise records -----------------
+  std::vector<Entry> ent;
+  ent.reserve(P.pool.size() * 2 + 16);
   std::vector<QState> st(nq);
-  std::vector<uint32_t> measEpoch(m, kNone);
-  uint32_t nprov = 0;  // provisional point ids
-  std::vector<uint64_t> &desc = T.desc;
-  std::vector<double> &prob = T.prob;
+  std::vector<uint32_t> measLo(m, kNone), measHi(m, kNone);
+  uint32_t nprov = 0;  // provisional point ids (creation order)
+  T.rec.reserve(P.pool.size());
+  T.rec_p.reserve(P.pool.size());
+  std::vector<uint32_t> ep_k;  // slots per epoch, grown on demand
+  SplitCache split;
 
   auto place1 = [&](uint32_t q, uint64_t op) -> uint32_t {
     QState &s = st[q];
@@ -432,7 +457,9 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
     } else {
       e = (uint32_t)s.last;
     }
-    ent[q].push_back({e, op});
+    ent.push_back({q, e, s.cnt, op});
+    if (e >= ep_k.size()) ep_k.resize((size_t)e + 1, 0);
+    ep_k[e] = std::max(ep_k[e], s.cnt + 1);
     s.last = e;
     s.cnt++;
     return e;
@@ -445,10 +472,12 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
     s.open = id;
     return id;
   };
-  auto mech = [&](uint32_t pa, uint32_t Pa, uint32_t pb, uint32_t Pb, double p) {
-    desc.push_back(make_desc(pa, Pa, pb, Pb));
-    prob.push_back(p);
+  auto record = [&](uint32_t pa, uint32_t pb, uint32_t type, uint32_t Pa, uint32_t Pb, double p) {
+    T.rec.push_back(make_rec(pa, pb, type, Pa, Pb));
+    T.rec_p.push_back(p);
   };
+  const uint32_t dep1Type = opt.level == 0 ? REC_DEP1_L0 : REC_DEP1_L12;
+  const uint32_t dep2Type = opt.level == 0 ? REC_DEP2_L0 : opt.level == 1 ? REC_DEP2_L1 : REC_DEP2_L2;
 
   for (size_t ii = P.ins.size(); ii-- > 0;) {
     const Instr &in = P.ins[ii];
@@ -465,11 +494,13 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
       case G_C2:
         for (uint32_t k = in.tn; k >= 2; k -= 2) {
           uint32_t a = t[k - 2], b = t[k - 1];
-          int64_t E = std::max(st[a].last, st[b].last) + 1;
+          uint32_t E = (uint32_t)(std::max(st[a].last, st[b].last) + 1);
           uint32_t subA = (uint32_t)g.img[0] | ((uint32_t)g.img[1] << 4);
           uint32_t subB = swap_halves(g.img[2]) | (swap_halves(g.img[3]) << 4);
-          ent[a].push_back({(uint32_t)E, make_op(OP_C2, subA, b)});
-          ent[b].push_back({(uint32_t)E, make_op(OP_C2, subB, a)});
+          ent.push_back({a, E, 0, make_op(OP_C2, subA, b)});
+          ent.push_back({b, E, 0, make_op(OP_C2, subB, a)});
+          if (E >= ep_k.size()) ep_k.resize((size_t)E + 1, 0);
+          ep_k[E] = std::max<uint32_t>(ep_k[E], 1);
           st[a].last = st[b].last = E;
           st[a].cnt = st[b].cnt = 1;
           st[a].open = st[b].open = kNone;
@@ -484,16 +515,26 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
       case G_M:
       case G_MR: {
         double p = in.nargs ? in.args[0] : 0.0;
+        uint32_t sub = (uint32_t)g.a | (g.kind == G_MR ? 4u : 0u);
         for (uint32_t k = in.tn; k-- > 0;) {
           uint32_t q = t[k];
           uint32_t meas = measBase[ii] + k;
-          uint32_t e = place1(q, make_op(g.kind == G_MR ? OP_MR : OP_M, g.a, meas));
-          measEpoch[meas] = e;
+          const uint32_t b0 = moff[meas], b1 = moff[meas + 1];
+          // bits beyond the first ride on OP_INJ slots placed before the OP_M
+          uint32_t first = b0 < b1 ? mbits[b0] : kNone;
+          uint32_t lo = kNone;
+          for (uint32_t b = b0 + 1; b < b1; b += 2) {
+            uint32_t e = place1(q, make_inj(mbits[b], b + 1 < b1 ? mbits[b + 1] : 0xFFFFFFu));
+            if (lo == kNone) lo = e;
+          }
+          uint32_t e = place1(q, make_op(OP_M, sub, first));
+          measLo[meas] = lo == kNone ? e : lo;
+          measHi[meas] = e;
           st[q].open = kNone;
-          if (p > 0 && T.meas_off[meas + 1] > T.meas_off[meas]) {
+          if (p > 0 && b1 > b0) {
             uint32_t id = nprov++;
             place1(q, make_op(OP_SNAPD, 0, id));
-            mech(id, 1, 0, 0, p);
+            record(id, 0, REC_PAULI, 1, 0, p);
           }
         }
         break;
@@ -501,55 +542,37 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
       case G_N1: {
         for (uint32_t k = in.tn; k-- > 0;) {
           uint32_t q = t[k];
-          double px = 0, py = 0, pz = 0;
           switch (g.a) {
-            case N1_X: px = in.args[0]; break;
-            case N1_Y: py = in.args[0]; break;
-            case N1_Z: pz = in.args[0]; break;
-            case N1_DEP1: {
-              double s = split_dep1(in.args[0]);
-              px = pz = s;
-              py = opt.level >= 1 ? s : 0.0;
+            case N1_X:
+            case N1_Y:
+            case N1_Z:
+              if (in.args[0] > 0) record(point(q), 0, REC_PAULI, g.a == N1_X ? 1 : g.a == N1_Z ? 2 : 3, 0, in.args[0]);
               break;
-            }
+            case N1_DEP1:
+              if (in.args[0] > 0) record(point(q), 0, dep1Type, 0, 0, split.dep1(in.args[0]));
+              break;
             case N1_PC1: {
               double qq[3];
               pc1_independent(in.args[0], in.args[1], in.args[2], qq);
-              px = qq[0];
-              py = qq[1];
-              pz = qq[2];
+              if (qq[0] > 0 || qq[1] > 0 || qq[2] > 0) {
+                uint32_t pt = point(q);
+                if (qq[0] > 0) record(pt, 0, REC_PAULI, 1, 0, qq[0]);
+                if (qq[1] > 0) record(pt, 0, REC_PAULI, 3, 0, qq[1]);
+                if (qq[2] > 0) record(pt, 0, REC_PAULI, 2, 0, qq[2]);
+              }
               break;
             }
-          }
-          if (px > 0 || py > 0 || pz > 0) {
-            uint32_t pt = point(q);
-            if (px > 0) mech(pt, 1, 0, 0, px);
-            if (py > 0) mech(pt, 3, 0, 0, py);
-            if (pz > 0) mech(pt, 2, 0, 0, pz);
           }
         }
         break;
       }
       case G_N2: {
-        double s = split_dep2(in.args[0]);
-        if (!(s > 0)) break;
-        // stim's order of the 15 Paulis: IX IY IZ XI XX XY XZ YI YX YY YZ ZI ZX ZY ZZ
-        static const uint8_t order[4] = {0, 1, 3, 2};  // I X Y Z in X|Z masks
+        if (!(in.args[0] > 0)) break;
+        const double sp = split.dep2(in.args[0]);
         for (uint32_t k = in.tn; k >= 2; k -= 2) {
           uint32_t a = t[k - 2], b = t[k - 1];
           uint32_t pa = point(a), pb = point(b);
-          for (int i = 0; i < 4; ++i)
-            for (int j = 0; j < 4; ++j) {
-              int A = order[i], B = order[j];
-              if (A == 0 && B == 0) continue;
-              if (!dep2_kept(opt.level, A, B)) continue;
-              if (A == 0)
-                mech(pb, (uint32_t)B, 0, 0, s);
-              else if (B == 0)
-                mech(pa, (uint32_t)A, 0, 0, s);
-              else
-                mech(pa, (uint32_t)A, pb, (uint32_t)B, s);
-            }
+          record(pa, pb, dep2Type, 0, 0, sp);
         }
         break;
       }
@@ -569,13 +592,12 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
             throw Error(GPC_ERR_UNSUPPORTED, "correlated errors on more than two qubits are not supported");
           }
         }
-        uint32_t pa = P0 ? point(q0) : 0, pb = P1 ? point(q1) : 0;
         if (P0 && P1)
-          mech(pa, P0, pb, P1, p);
+          record(point(q0), point(q1), REC_PAULI, P0, P1, p);
         else if (P0)
-          mech(pa, P0, 0, 0, p);
+          record(point(q0), 0, REC_PAULI, P0, 0, p);
         else if (P1)
-          mech(pb, P1, 0, 0, p);
+          record(point(q1), 0, REC_PAULI, P1, 0, p);
         break;
       }
       default:
@@ -584,21 +606,10 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
   }
 
   // ---- assemble epochs -------------------------------------------------
-  uint32_t nE = 0;
-  for (uint32_t q = 0; q < nq; ++q)
-    if (!ent[q].empty()) nE = std::max(nE, ent[q].back().epoch + 1);
+  const uint32_t nE = (uint32_t)ep_k.size();
   T.n_epochs = nE;
-  T.ep_k.assign(nE, 0);
-  for (uint32_t q = 0; q < nq; ++q) {
-    const auto &v = ent[q];
-    for (size_t i = 0; i < v.size();) {
-      size_t j = i;
-      while (j < v.size() && v[j].epoch == v[i].epoch) ++j;
-      T.ep_k[v[i].epoch] = std::max<uint32_t>(T.ep_k[v[i].epoch], (uint32_t)(j - i));
-      i = j;
-    }
-  }
-  for (auto &k : T.ep_k) k = std::max<uint32_t>(k, 1);  // every epoch copies at least one slot
+  for (auto &k : ep_k) k = std::max<uint32_t>(k, 1);  // every epoch copies at least one slot
+  T.ep_k = std::move(ep_k);
   T.ep_opoff.assign(nE, 0);
   uint64_t total = 0;
   for (uint32_t e = 0; e < nE; ++e) {
@@ -608,15 +619,7 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
     if (total > 0xFFFFFFFFull) throw Error(GPC_ERR_CAPACITY, "tape too long");
   }
   T.ops.assign(total, 0);
-  for (uint32_t q = 0; q < nq; ++q) {
-    const auto &v = ent[q];
-    uint32_t k = 0;
-    for (size_t i = 0; i < v.size(); ++i) {
-      if (i == 0 || v[i].epoch != v[i - 1].epoch) k = 0;
-      T.ops[(size_t)T.ep_opoff[v[i].epoch] + (size_t)k * T.qpad + q] = v[i].op;
-      ++k;
-    }
-  }
+  for (const Entry &x : ent) T.ops[(size_t)T.ep_opoff[x.e] + (size_t)x.k * T.qpad + x.q] = x.op;
   // points: renumber in walk order (epoch, slot, qubit) so each epoch owns a contiguous range
   std::vector<uint32_t> remap(nprov, kNone);
   T.ep_ptoff.assign(nE + 1, 0);
@@ -624,36 +627,45 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
   for (uint32_t e = 0; e < nE; ++e) {
     T.ep_ptoff[e] = next;
     uint64_t *base = T.ops.data() + T.ep_opoff[e];
-    for (uint32_t k = 0; k < T.ep_k[e]; ++k)
-      for (uint32_t q = 0; q < T.qpad; ++q) {
-        uint64_t &op = base[(size_t)k * T.qpad + q];
-        uint32_t opc = (uint32_t)(op & 0xFF);
-        if (opc == OP_SNAP || opc == OP_SNAPD) {
-          uint32_t prov = (uint32_t)(op >> 32);
-          remap[prov] = next;
-          op = (op & 0xFFFFFFFFull) | ((uint64_t)next << 32);
-          ++next;
-        }
+    const size_t n = (size_t)T.ep_k[e] * T.qpad;
+    for (size_t i = 0; i < n; ++i) {
+      uint64_t &op = base[i];
+      uint32_t opc = (uint32_t)(op & 0xFF);
+      if (opc == OP_SNAP || opc == OP_SNAPD) {
+        remap[(uint32_t)(op >> 32)] = next;
+        op = (op & 0xFFFFFFFFull) | ((uint64_t)next << 32);
+        ++next;
       }
+    }
   }
   T.ep_ptoff[nE] = next;
   T.npoints = next;
-  if (next >= (1u << 30)) throw Error(GPC_ERR_CAPACITY, "too many snapshot points");
-  for (auto &d : desc) {
-    uint32_t pa = (uint32_t)(d & 0x3FFFFFFFu), Pa = (uint32_t)((d >> 30) & 3);
-    uint32_t pb = (uint32_t)((d >> 32) & 0x3FFFFFFFu), Pb = (uint32_t)(d >> 62);
-    d = make_desc(remap[pa], Pa, Pb ? remap[pb] : 0, Pb);
+  if (next > kMaxPoint28) throw Error(GPC_ERR_CAPACITY, "too many snapshot points");
+  const size_t R = T.rec.size();
+  T.rec_moff.resize(R + 1);
+  uint64_t mm = 0;
+  for (size_t r = 0; r < R; ++r) {
+    uint64_t &d = T.rec[r];
+    const uint32_t pa = (uint32_t)(d & kMaxPoint28), pb = (uint32_t)((d >> 28) & kMaxPoint28);
+    const uint32_t type = (uint32_t)((d >> 56) & 15u), Pb = (uint32_t)(d >> 62);
+    const bool hasB = type >= REC_DEP2_L0 || Pb != 0;
+    d = (d & ~(((uint64_t)kMaxPoint28) | ((uint64_t)kMaxPoint28 << 28))) | (uint64_t)remap[pa] |
+        ((uint64_t)(hasB ? remap[pb] : 0) << 28);
+    T.rec_moff[r] = (uint32_t)mm;
+    mm += kRecComps[type];
   }
+  if (mm >= 0xFFFFFFFFull) throw Error(GPC_ERR_CAPACITY, "too many error mechanisms");
+  T.rec_moff[R] = (uint32_t)mm;
+  T.M = (uint32_t)mm;
   // injection range of each word
   T.inj_lo.assign(T.w, kNone);
   T.inj_hi.assign(T.w, kNone);
-  for (uint32_t mm = 0; mm < m; ++mm) {
-    uint32_t e = measEpoch[mm];
-    if (e == kNone) continue;
-    for (uint32_t i = T.meas_off[mm]; i < T.meas_off[mm + 1]; ++i) {
-      uint32_t j = T.meas_bits[i] >> 6;
-      if (T.inj_lo[j] == kNone || e < T.inj_lo[j]) T.inj_lo[j] = e;
-      if (T.inj_hi[j] == kNone || e > T.inj_hi[j]) T.inj_hi[j] = e;
+  for (uint32_t k = 0; k < m; ++k) {
+    if (measLo[k] == kNone) continue;
+    for (uint32_t i = moff[k]; i < moff[k + 1]; ++i) {
+      uint32_t j = mbits[i] >> 6;
+      if (T.inj_lo[j] == kNone || measLo[k] < T.inj_lo[j]) T.inj_lo[j] = measLo[k];
+      if (T.inj_hi[j] == kNone || measHi[k] > T.inj_hi[j]) T.inj_hi[j] = measHi[k];
     }
   }
   return T;

@@ -32,14 +32,15 @@ struct Error : std::runtime_error {
 };
 
 // ---- tape op encoding (u64) ----------------------------------------------
-// bits 0-7 opcode, bits 8-15 sub, bits 32-63 operand.
+// bits 0-7 opcode, bits 8-15 sub, bits 16-31 aux, bits 32-63 operand.
 enum : uint32_t {
   OP_NOP = 0,
   OP_C1 = 1,     // sub: newX mask (bits 0-1 over X,Z) | newZ mask << 2
   OP_C2 = 2,     // sub: newX mask (4 bits over selfX,selfZ,partX,partZ) | newZ mask << 4; operand: partner qubit
   OP_R = 3,      // clear both rows
-  OP_M = 4,      // sub: basis 0=Z 1=X 2=Y; operand: measurement index; rows ^= bits of that measurement
-  OP_MR = 5,     // clear, then as OP_M
+  OP_M = 4,      // sub: basis (0 Z, 1 X, 2 Y) | 4 (clear first: MR); operand: one bit of the measurement
+                 // (0xFFFFFFFF: none); the bits of preceding OP_INJ ops are added; rows ^= bits in word j
+  OP_INJ = 5,    // two more bits of the next OP_M: operand, and bits 8-31 (0xFFFFFF: none)
   OP_SNAP = 6,   // operand: point; point <- (X, Z)
   OP_SNAPD = 7,  // operand: point; point <- (bits of the last measurement, 0)
 };
@@ -47,12 +48,34 @@ enum : uint32_t {
 inline uint64_t make_op(uint32_t opc, uint32_t sub, uint32_t operand) {
   return (uint64_t)opc | ((uint64_t)(sub & 0xFF) << 8) | ((uint64_t)operand << 32);
 }
+inline uint64_t make_inj(uint32_t bit1, uint32_t bit2) {
+  return (uint64_t)OP_INJ | ((uint64_t)(bit2 & 0xFFFFFFu) << 8) | ((uint64_t)bit1 << 32);
+}
 
-// Mechanism descriptor: point a (30 bits) | Pauli a (2 bits) | point b | Pauli b.
-// Pauli: 0 none, 1 X, 2 Z, 3 Y (X|Z).
+// Mechanism descriptor (device, one per mechanism): point a (30 bits) |
+// Pauli a (2 bits) | point b | Pauli b.  Pauli: 0 none, 1 X, 2 Z, 3 Y (X|Z).
 inline uint64_t make_desc(uint32_t pa, uint32_t Pa, uint32_t pb, uint32_t Pb) {
   return (uint64_t)(pa & 0x3FFFFFFFu) | ((uint64_t)(Pa & 3) << 30) | ((uint64_t)(pb & 0x3FFFFFFFu) << 32) |
          ((uint64_t)(Pb & 3) << 62);
+}
+
+// Noise record (host -> device, one per noise instance): point a (28 bits) |
+// point b (28 bits) << 28 | type (4 bits) << 56 | Pauli a << 60 | Pauli b << 62.
+// The device expands a record into its mechanisms (components).
+enum : uint32_t {
+  REC_PAULI = 0,     // one mechanism: Pauli a on point a, Pauli b on point b (b optional)
+  REC_DEP1_L0 = 1,   // X, Z on point a
+  REC_DEP1_L12 = 2,  // X, Y, Z on point a
+  REC_DEP2_L0 = 3,   // IX IZ XI XX ZI ZZ on (a, b)
+  REC_DEP2_L1 = 4,   // + IY XZ YI ZX
+  REC_DEP2_L2 = 5,   // all 15
+};
+constexpr uint32_t kRecComps[6] = {1, 2, 3, 6, 10, 15};
+constexpr uint32_t kMaxPoint28 = (1u << 28) - 1;
+
+inline uint64_t make_rec(uint32_t pa, uint32_t pb, uint32_t type, uint32_t Pa, uint32_t Pb) {
+  return (uint64_t)(pa & kMaxPoint28) | ((uint64_t)(pb & kMaxPoint28) << 28) | ((uint64_t)(type & 15u) << 56) |
+         ((uint64_t)(Pa & 3u) << 60) | ((uint64_t)(Pb & 3u) << 62);
 }
 
 constexpr uint32_t kNone = 0xFFFFFFFFu;
@@ -81,13 +104,13 @@ struct Tape {
   std::vector<uint32_t> ep_opoff;   // [n_epochs]     first op of epoch e
   std::vector<uint32_t> ep_k;       // [n_epochs]     slots in epoch e
   std::vector<uint32_t> ep_ptoff;   // [n_epochs + 1] first point of epoch e
-  std::vector<uint32_t> meas_off;   // [nmeas + 1]
-  std::vector<uint32_t> meas_bits;  // bits of each measurement
   std::vector<uint32_t> inj_lo;     // [w] first epoch (walk order) injecting into word j, kNone if none
   std::vector<uint32_t> inj_hi;     // [w] last such epoch
   uint32_t npoints = 0;
-  std::vector<uint64_t> desc;  // [M] mechanism descriptors
-  std::vector<double> prob;    // [M] mechanism probabilities
+  std::vector<uint64_t> rec;        // [R] noise records
+  std::vector<double> rec_p;        // [R] probability of each of the record's mechanisms
+  std::vector<uint32_t> rec_moff;   // [R + 1] first mechanism of each record
+  uint32_t M = 0;                   // mechanisms (components)
 };
 
 struct LowerOptions {

@@ -1,27 +1,30 @@
-// sortmerge.cu -- symptom keys, onesweep radix sort, segmented merge (sm_103a).
+// sortmerge.cu -- symptom keys, radix bucketing / onesweep sort, merge (sm_103a).
 //
 // Replaces the reference's K3-K7 (Policies/Compute/CUDA.hpp:184-189,276-343,
 // 422-497; CUDAHandlers.hpp:67-139): set-bit extraction truncated at 32 bits
 // + a 64-bit FNV hash with no collision check, CUB radix sort, a gather of
 // probabilities, CUB reduce-by-key and a gather of the full class matrix.
 //
-//  * key_kernel: one thread per mechanism computes its symptom words from
-//    the walk's snapshots (word j of mechanism m is the XOR of the selected
-//    rows of its one or two points, zero outside word j's band) and folds them
-//    into a 128-bit key  K = XOR_j H(j, word_j), H(j, 0) = 0, so the empty
-//    symptom has key 0 and the key is independent of padding.
-//  * onesweep radix sort (one histogram kernel + one kernel per 8-bit digit):
-//    every tile ranks its items per digit with warp match/popc, publishes its
-//    digit counts and resolves its global offsets by decoupled look-back on
-//    the preceding tiles' status words.  Stable, so equal keys keep
-//    ascending mechanism order.
-//  * merge_kernel: one thread per sorted item.  A group is a run of equal
-//    128-bit keys; every item checks its full symptom against its
-//    predecessor (collision check).  Group heads fold the probabilities of
-//    their run left to right with p <- p(1-q) + q(1-p) (CUDAHandlers.hpp:
-//    635-640) in FP64, extract the targets of the symptom, and get their
-//    output slot from a block scan plus decoupled look-back.  The empty
-//    symptom (key 0) is dropped (Driver.hpp:185).
+//  * key_kernel: one thread per noise record.  It expands the record into
+//    its mechanisms (the Pauli components of the channel), computes each
+//    mechanism's symptom words from the walk's snapshots -- word j is the
+//    XOR of the selected rows of its one or two points, zero outside word
+//    j's band -- and folds them into a 128-bit key K = XOR_j H(j, word_j)
+//    with H(j, 0) = 0, so the empty symptom has key 0.  Non-empty keys are
+//    counted per bucket (the top bits of K: one MSD radix digit).
+//  * bucket scan + scatter: the radix partition pass.
+//  * bucket_merge_kernel: one CTA per bucket sorts its items in shared memory
+//    by (K, mechanism), so a group (run of equal K) keeps ascending mechanism
+//    order; every item checks its full symptom against its predecessor
+//    (collision check); group heads fold their run's probabilities left to
+//    right with p <- p(1-q) + q(1-p) (CUDAHandlers.hpp:635-640) in FP64,
+//    extract their targets and get an output slot from a block scan plus a
+//    warp-wide decoupled look-back over the preceding buckets.  The empty
+//    symptom is dropped (Driver.hpp:185).
+//  * global path, used when a bucket exceeds one CTA (a symptom repeated
+//    more than BUCKET_CAP times): LSD onesweep radix sort of all keys (one
+//    kernel per 8-bit digit, tile ranks by warp match/popc, decoupled
+//    look-back for digit offsets) and a merge kernel over the sorted run.
 #include <cstdint>
 
 #include "device.cuh"
@@ -69,25 +72,151 @@ __device__ __forceinline__ uint64_t symptom_word(const CircuitDev &C, uint64_t d
   return v;
 }
 
-__global__ void key_kernel(const CircuitDev *__restrict__ cdev, uint32_t M, uint32_t w, ulonglong2 *__restrict__ key,
-                           uint64_t *__restrict__ sortkey, uint32_t *__restrict__ perm) {
+__device__ __forceinline__ uint64_t mk_desc(uint32_t pa, uint32_t Pa, uint32_t pb, uint32_t Pb) {
+  return (uint64_t)(pa & 0x3FFFFFFFu) | ((uint64_t)(Pa & 3u) << 30) | ((uint64_t)(pb & 0x3FFFFFFFu) << 32) |
+         ((uint64_t)(Pb & 3u) << 62);
+}
+
+// Components of each record type as (Pauli a | Pauli b << 2); Pauli: 1 X, 2 Z, 3 Y.
+// Two-qubit lists follow stim's order IX IY IZ XI XX XY XZ YI YX YY YZ ZI ZX ZY ZZ,
+// restricted to the correlation level's set (Mixer.hpp:13-20).
+#define PP(a, b) ((a) | ((b) << 2))
+__constant__ uint8_t kComp[6][15] = {
+    {0},
+    {PP(1, 0), PP(2, 0)},
+    {PP(1, 0), PP(3, 0), PP(2, 0)},
+    {PP(0, 1), PP(0, 2), PP(1, 0), PP(1, 1), PP(2, 0), PP(2, 2)},
+    {PP(0, 1), PP(0, 3), PP(0, 2), PP(1, 0), PP(1, 1), PP(1, 2), PP(3, 0), PP(2, 0), PP(2, 1), PP(2, 2)},
+    {PP(0, 1), PP(0, 3), PP(0, 2), PP(1, 0), PP(1, 1), PP(1, 3), PP(1, 2), PP(3, 0), PP(3, 1), PP(3, 3), PP(3, 2),
+     PP(2, 0), PP(2, 1), PP(2, 3), PP(2, 2)},
+};
+__constant__ uint8_t kNComp[6] = {1, 2, 3, 6, 10, 15};
+#undef PP
+
+__global__ void __launch_bounds__(256) key_kernel(KeyLaunch L) {
   extern __shared__ uint2 sband[];
-  const CircuitDev C = *cdev;
+  const CircuitDev C = *L.c_dev;
+  const uint32_t w = L.w;
   for (uint32_t j = threadIdx.x; j < w; j += blockDim.x) sband[j] = C.band[j];
   __syncthreads();
-  for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
-    const uint64_t d = __ldg(C.desc + m);
-    uint64_t hx = 0, hy = 0;
+  const uint32_t shift = 64u - L.bucket_bits;
+  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < L.R; r += gridDim.x * blockDim.x) {
+    const uint64_t d = __ldg(C.rec + r);
+    const uint32_t pa = (uint32_t)(d & 0x0FFFFFFFu), pb = (uint32_t)((d >> 28) & 0x0FFFFFFFu);
+    const uint32_t type = (uint32_t)((d >> 56) & 15u);
+    const uint32_t P0 = (uint32_t)((d >> 60) & 3u), P1 = (uint32_t)(d >> 62);
+    const uint32_t nc = type == 0 ? 1u : kNComp[type];
+    const bool hasB = type >= 3u || P1 != 0;
+    uint32_t comp[15];
+#pragma unroll
+    for (int c = 0; c < 15; ++c) comp[c] = type == 0 ? (c == 0 ? (P0 | (P1 << 2)) : 0u) : kComp[type][c];
+    uint64_t hx[15], hy[15];
+    uint32_t cnt[15];
+#pragma unroll
+    for (int c = 0; c < 15; ++c) {
+      hx[c] = hy[c] = 0;
+      cnt[c] = 0;
+    }
+    uint32_t nzmask = 0;
+    const uint32_t m0 = __ldg(C.rec_moff + r);
+    const uint32_t tcap = C.tcap;
     for (uint32_t j = 0; j < w; ++j) {
-      const uint64_t v = symptom_word(C, d, j, sband[j]);
-      if (v) {
-        const ulonglong2 h = word_hash(j, v);
-        hx ^= h.x;
-        hy ^= h.y;
+      const uint2 b = sband[j];
+      const ulonglong2 *sj = C.snap + (size_t)j * C.npoints;
+      ulonglong2 sa = make_ulonglong2(0, 0), sb = make_ulonglong2(0, 0);
+      if (pa - b.x < b.y - b.x) sa = sj[pa];
+      if (hasB && pb - b.x < b.y - b.x) sb = sj[pb];
+      if ((sa.x | sa.y | sb.x | sb.y) == 0) continue;
+#pragma unroll
+      for (int c = 0; c < 15; ++c) {
+        if ((uint32_t)c < nc) {
+          const uint64_t v = pauli_sel(sa, comp[c] & 3u) ^ pauli_sel(sb, comp[c] >> 2);
+          if (v) {
+            const ulonglong2 h = word_hash(j, v);
+            hx[c] ^= h.x;
+            hy[c] ^= h.y;
+            nzmask |= 1u << c;
+            if (tcap) {
+              uint32_t *out = C.tl + (size_t)(m0 + (uint32_t)c) * tcap;
+              uint64_t x = v;
+              while (x) {
+                if (cnt[c] < tcap) out[cnt[c]] = j * 64u + (uint32_t)(__ffsll((long long)x) - 1);
+                ++cnt[c];
+                x &= x - 1;
+              }
+            }
+          }
+        }
       }
     }
-    key[m] = make_ulonglong2(hx, hy);
-    sortkey[m] = hx;
+    const double p = __ldg(C.rec_p + r);
+#pragma unroll
+    for (int c = 0; c < 15; ++c) {
+      if ((uint32_t)c < nc) {
+        const uint32_t m = m0 + (uint32_t)c;
+        const uint32_t Pa = comp[c] & 3u, Pb = comp[c] >> 2;
+        // a component that touches only point b is stored with b as its first point
+        C.mdesc[m] = Pa ? mk_desc(pa, Pa, Pb ? pb : 0u, Pb) : mk_desc(pb, Pb, 0u, 0u);
+        C.mp[m] = p;
+        L.key[m] = make_ulonglong2(hx[c], hy[c]);
+        if (tcap) {
+          C.tn[m] = cnt[c];
+          if (cnt[c] > tcap) atomicOr(L.err, DEV_FLAG_LONG);
+          if (cnt[c]) atomicAdd(L.list_total, cnt[c]);
+        }
+        if ((hx[c] | hy[c]) == 0) {
+          if (nzmask & (1u << c)) atomicOr(L.err, DEV_ERR_COLLISION);  // non-empty symptom hashed to 0
+        } else {
+          atomicAdd(L.bucket_count + (hx[c] >> shift), 1u);
+        }
+      }
+    }
+  }
+}
+
+// Exclusive scan of nb bucket counts (one block); offset[nb] = total.
+__global__ void __launch_bounds__(1024) bucket_scan_kernel(const uint32_t *__restrict__ count,
+                                                           uint32_t *__restrict__ offset, uint32_t nb) {
+  __shared__ uint32_t part[1024];
+  const uint32_t t = threadIdx.x;
+  const uint32_t per = (nb + 1023) / 1024;
+  const uint32_t lo = min(nb, t * per), hi = min(nb, lo + per);
+  uint32_t sum = 0;
+  for (uint32_t i = lo; i < hi; ++i) sum += count[i];
+  part[t] = sum;
+  __syncthreads();
+  for (uint32_t off = 1; off < 1024; off <<= 1) {
+    const uint32_t v = t >= off ? part[t - off] : 0;
+    __syncthreads();
+    part[t] += v;
+    __syncthreads();
+  }
+  uint32_t run = part[t] - sum;
+  for (uint32_t i = lo; i < hi; ++i) {
+    const uint32_t c = count[i];
+    offset[i] = run;
+    run += c;
+  }
+  if (t == 1023) offset[nb] = part[1023];
+}
+
+__global__ void bucket_scatter_kernel(const ulonglong2 *__restrict__ key, uint32_t M, uint32_t shift,
+                                      const uint32_t *__restrict__ offset, uint32_t *__restrict__ cursor,
+                                      ulonglong2 *__restrict__ bkey, uint32_t *__restrict__ bm) {
+  for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
+    const ulonglong2 k = key[m];
+    if ((k.x | k.y) == 0) continue;
+    const uint32_t b = (uint32_t)(k.x >> shift);
+    const uint32_t pos = offset[b] + atomicAdd(cursor + b, 1u);
+    bkey[pos] = k;
+    bm[pos] = m;
+  }
+}
+
+__global__ void sort_init_kernel(const ulonglong2 *__restrict__ key, uint64_t *__restrict__ sortkey,
+                                 uint32_t *__restrict__ perm, uint32_t M) {
+  for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
+    sortkey[m] = key[m].x;
     perm[m] = m;
   }
 }
@@ -263,14 +392,14 @@ __global__ void __launch_bounds__(MERGE_THREADS) merge_kernel(MergeLaunch L) {
   if (i < n) {
     m = L.perm[i];
     k = L.key[m];
-    const uint64_t d = __ldg(C.desc + m);
+    const uint64_t d = __ldg(C.mdesc + m);
     bool newgroup = true;
     if (i > 0) {
       const uint32_t mp = L.perm[i - 1];
       const ulonglong2 kp = L.key[mp];
       if (kp.x == k.x && kp.y == k.y) {
         newgroup = false;
-        const uint64_t dp = __ldg(C.desc + mp);
+        const uint64_t dp = __ldg(C.mdesc + mp);
         for (uint32_t j = 0; j < w; ++j) {
           if (symptom_word(C, d, j, sband[j]) != symptom_word(C, dp, j, sband[j])) {
             atomicOr(L.err, DEV_ERR_COLLISION);
@@ -361,18 +490,18 @@ __global__ void __launch_bounds__(MERGE_THREADS) merge_kernel(MergeLaunch L) {
   if (slot >= n) return;  // only after a timed-out look-back
   const uint32_t toff = s_pre_t + wsum_t[warp] + t_inc - t_in;
   // fold the run's probabilities left to right
-  double p = __ldg(C.prob + m);
+  double p = __ldg(C.mp + m);
   for (uint32_t i2 = i + 1; i2 < n; ++i2) {
     const uint32_t m2 = L.perm[i2];
     const ulonglong2 k2 = L.key[m2];
     if (k2.x != k.x || k2.y != k.y) break;
-    const double q = __ldg(C.prob + m2);
+    const double q = __ldg(C.mp + m2);
     p = p * (1.0 - q) + q * (1.0 - p);
   }
   L.out_prob[slot] = p;
   L.out_off[slot] = toff;
   if (toff + ntg <= L.tg_cap) {
-    const uint64_t d = __ldg(C.desc + m);
+    const uint64_t d = __ldg(C.mdesc + m);
     uint32_t o = toff;
     for (uint32_t j = 0; j < w; ++j) {
       uint64_t v = symptom_word(C, d, j, sband[j]);
@@ -384,15 +513,237 @@ __global__ void __launch_bounds__(MERGE_THREADS) merge_kernel(MergeLaunch L) {
   }
 }
 
+// ---- bucket sort + merge ---------------------------------------------------
+
+// (key, m) order: key.x, then key.y, then mechanism id.
+__device__ __forceinline__ bool item_less(ulonglong2 a, uint32_t ma, ulonglong2 b, uint32_t mb) {
+  if (a.x != b.x) return a.x < b.x;
+  if (a.y != b.y) return a.y < b.y;
+  return ma < mb;
+}
+
+// Warp 0 resolves the exclusive prefix of tile `tile` over tiles [0, tile)
+// by decoupled look-back: 32 predecessors per step.  `agg` is this tile's
+// (count, targets) aggregate.  Returns the prefix in lane 0.
+__device__ __forceinline__ void warp_lookback(unsigned long long *status, uint32_t tile, uint32_t agg_c,
+                                              uint32_t agg_t, uint32_t *err, uint32_t *pre_c, uint32_t *pre_t) {
+  const uint32_t lane = threadIdx.x & 31u;
+  volatile unsigned long long *st = status;
+  if (tile == 0) {
+    if (lane == 0) st[0] = MS_PREFIX | ms_pack(agg_c, agg_t);
+    *pre_c = 0;
+    *pre_t = 0;
+    return;
+  }
+  if (lane == 0) st[tile] = MS_AGG | ms_pack(agg_c, agg_t);
+  uint32_t ec = 0, et = 0;
+  int32_t base = (int32_t)tile - 1;
+  unsigned long long t0 = 0;
+  while (base >= 0) {
+    const int32_t idx = base - (int32_t)lane;
+    const unsigned long long s = idx >= 0 ? st[idx] : (MS_PREFIX | 0ull);
+    const uint32_t flag = (uint32_t)(s >> 62);
+    const uint32_t ready = __ballot_sync(0xFFFFFFFFu, flag != 0);
+    const uint32_t pref = __ballot_sync(0xFFFFFFFFu, flag == 2u);
+    // lanes up to (and including) the nearest prefix must all be ready
+    const uint32_t need = pref ? ((pref & (0u - pref)) << 1) - 1u : 0xFFFFFFFFu;
+    if ((ready & need) != need) {
+      if (t0 == 0) t0 = globaltimer();
+      else if (globaltimer() - t0 > kSpinLimitNs) {
+        if (lane == 0) atomicOr(err, DEV_ERR_TIMEOUT);
+        break;
+      }
+      continue;
+    }
+    t0 = 0;
+    uint32_t c = (need >> lane) & 1u ? (uint32_t)((s >> 32) & 0x3FFFFFFFu) : 0u;
+    uint32_t t = (need >> lane) & 1u ? (uint32_t)s : 0u;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      c += __shfl_xor_sync(0xFFFFFFFFu, c, o);
+      t += __shfl_xor_sync(0xFFFFFFFFu, t, o);
+    }
+    ec += c;
+    et += t;
+    if (pref) break;
+    base -= 32;
+  }
+  if (lane == 0) {
+    __threadfence();
+    st[tile] = MS_PREFIX | ms_pack(ec + agg_c, et + agg_t);
+  }
+  *pre_c = ec;
+  *pre_t = et;
+}
+
+__global__ void __launch_bounds__(BUCKET_THREADS) bucket_merge_kernel(BucketMergeLaunch L) {
+  constexpr int NT = BUCKET_THREADS;
+  constexpr int CHUNK = BUCKET_CAP / NT;  // positions per thread in the scans
+  __shared__ ulonglong2 sk[BUCKET_CAP];
+  __shared__ uint32_t sm[BUCKET_CAP];
+  __shared__ uint16_t ord[BUCKET_CAP];
+  __shared__ uint32_t sntg[BUCKET_CAP];  // targets of the group starting at a sorted position, or ~0u
+  __shared__ uint32_t sc[NT], st_[NT];
+  __shared__ uint32_t s_b, s_pre_c, s_pre_t;
+  extern __shared__ uint2 sband[];
+  const CircuitDev C = *L.c_dev;
+  const uint32_t w = L.w;
+  for (uint32_t j = threadIdx.x; j < w; j += NT) sband[j] = C.band[j];
+  if (threadIdx.x == 0) s_b = atomicAdd(L.ticket, 1u);
+  __syncthreads();
+  const uint32_t b = s_b;
+  uint32_t n = L.count[b];
+  const uint32_t base = L.offset[b];
+  if (n > (uint32_t)BUCKET_CAP) {
+    if (threadIdx.x == 0) atomicOr(L.err, DEV_FLAG_BIG_BUCKET);
+    n = 0;
+  }
+  for (uint32_t i = threadIdx.x; i < n; i += NT) {
+    sk[i] = L.bkey[base + i];
+    sm[i] = L.bm[base + i];
+  }
+  __syncthreads();
+  // rank sort by (key, m): every key is distinct once m is included
+  for (uint32_t i = threadIdx.x; i < n; i += NT) {
+    const ulonglong2 ki = sk[i];
+    const uint32_t mi = sm[i];
+    uint32_t r = 0;
+    for (uint32_t k = 0; k < n; ++k) r += item_less(sk[k], sm[k], ki, mi) ? 1u : 0u;
+    ord[r] = (uint16_t)i;
+  }
+  __syncthreads();
+  // group heads, collision checks (full target lists), target counts
+  const uint32_t tcap = C.tcap;
+  for (uint32_t s = threadIdx.x; s < n; s += NT) {
+    const uint32_t i = ord[s];
+    const uint32_t m = sm[i];
+    const uint32_t nt = __ldg(C.tn + m);
+    bool head = true;
+    if (s > 0) {
+      const uint32_t ip = ord[s - 1];
+      if (sk[ip].x == sk[i].x && sk[ip].y == sk[i].y) {
+        head = false;
+        const uint32_t mq = sm[ip];
+        bool same = __ldg(C.tn + mq) == nt;
+        const uint32_t *a = C.tl + (size_t)m * tcap, *b = C.tl + (size_t)mq * tcap;
+        for (uint32_t k = 0; same && k < nt; ++k) same = __ldg(a + k) == __ldg(b + k);
+        if (!same) atomicOr(L.err, DEV_ERR_COLLISION);
+      }
+    }
+    sntg[s] = head ? nt : ~0u;
+  }
+  __syncthreads();
+  // exclusive scan of (heads, targets) over sorted positions: chunk per thread
+  const uint32_t lo = threadIdx.x * CHUNK;
+  uint32_t cc = 0, tt = 0;
+  for (uint32_t s = lo; s < lo + CHUNK && s < n; ++s)
+    if (sntg[s] != ~0u) {
+      ++cc;
+      tt += sntg[s];
+    }
+  sc[threadIdx.x] = cc;
+  st_[threadIdx.x] = tt;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    // warp 0: scan the NT chunk totals (NT/32 per lane), then look back over buckets
+    constexpr int PER = NT / 32;
+    uint32_t lc = 0, lt = 0;
+    for (int x = 0; x < PER; ++x) {
+      lc += sc[threadIdx.x * PER + x];
+      lt += st_[threadIdx.x * PER + x];
+    }
+    uint32_t ic = lc, it = lt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t a = __shfl_up_sync(0xFFFFFFFFu, ic, o), bb = __shfl_up_sync(0xFFFFFFFFu, it, o);
+      if (threadIdx.x >= (uint32_t)o) {
+        ic += a;
+        it += bb;
+      }
+    }
+    uint32_t rc = ic - lc, rt = it - lt;
+    for (int x = 0; x < PER; ++x) {
+      const uint32_t c = sc[threadIdx.x * PER + x], t = st_[threadIdx.x * PER + x];
+      sc[threadIdx.x * PER + x] = rc;
+      st_[threadIdx.x * PER + x] = rt;
+      rc += c;
+      rt += t;
+    }
+    const uint32_t agg_c = __shfl_sync(0xFFFFFFFFu, ic, 31), agg_t = __shfl_sync(0xFFFFFFFFu, it, 31);
+    uint32_t pc = 0, pt = 0;
+    warp_lookback(L.status, b, agg_c, agg_t, L.err, &pc, &pt);
+    if (threadIdx.x == 0) {
+      s_pre_c = pc;
+      s_pre_t = pt;
+      if (b == L.nb - 1) {
+        L.totals[0] = pc + agg_c;
+        L.totals[1] = pt + agg_t;
+        if (pt + agg_t > L.tg_cap) atomicOr(L.err, DEV_FLAG_TG_OVF);
+      }
+    }
+  }
+  __syncthreads();
+  uint32_t slot = s_pre_c + sc[threadIdx.x], toff = s_pre_t + st_[threadIdx.x];
+  for (uint32_t s = lo; s < lo + CHUNK && s < n; ++s) {
+    const uint32_t ntg = sntg[s];
+    if (ntg == ~0u) continue;
+    if (slot >= L.max_groups) break;  // only after a timed-out look-back
+    const uint32_t i = ord[s];
+    const uint32_t m = sm[i];
+    double p = __ldg(C.mp + m);
+    for (uint32_t s2 = s + 1; s2 < n; ++s2) {
+      const uint32_t i2 = ord[s2];
+      if (sk[i2].x != sk[i].x || sk[i2].y != sk[i].y) break;
+      const double q = __ldg(C.mp + sm[i2]);
+      p = p * (1.0 - q) + q * (1.0 - p);
+    }
+    L.out_prob[slot] = p;
+    L.out_off[slot] = toff;
+    if (toff + ntg <= L.tg_cap) {
+      const uint32_t *src = C.tl + (size_t)m * tcap;
+      for (uint32_t k = 0; k < ntg; ++k) L.out_tg[toff + k] = __ldg(src + k);
+    }
+    ++slot;
+    toff += ntg;
+  }
+}
+
 }  // namespace
 
-cudaError_t launch_keys(const CircuitDev *c_dev, uint32_t M, uint32_t w, ulonglong2 *key, uint64_t *sortkey,
-                        uint32_t *perm, cudaStream_t s) {
+cudaError_t launch_keys(const KeyLaunch &L, cudaStream_t s) {
+  if (L.R == 0) return cudaSuccess;
+  const uint32_t threads = 128;
+  uint32_t blocks = (L.R + threads - 1) / threads;
+  if (blocks > 152u * 32u) blocks = 152u * 32u;
+  key_kernel<<<blocks, threads, (size_t)L.w * sizeof(uint2), s>>>(L);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bucket_scan(const uint32_t *count, uint32_t *offset, uint32_t nb, cudaStream_t s) {
+  bucket_scan_kernel<<<1, 1024, 0, s>>>(count, offset, nb);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bucket_scatter(const ulonglong2 *key, uint32_t M, uint32_t bucket_bits, const uint32_t *offset,
+                                  uint32_t *cursor, ulonglong2 *bkey, uint32_t *bm, cudaStream_t s) {
   if (M == 0) return cudaSuccess;
-  const uint32_t threads = 256;
-  uint32_t blocks = (M + threads - 1) / threads;
+  uint32_t blocks = (M + 255) / 256;
   if (blocks > 152u * 16u) blocks = 152u * 16u;
-  key_kernel<<<blocks, threads, (size_t)w * sizeof(uint2), s>>>(c_dev, M, w, key, sortkey, perm);
+  bucket_scatter_kernel<<<blocks, 256, 0, s>>>(key, M, 64u - bucket_bits, offset, cursor, bkey, bm);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bucket_merge(const BucketMergeLaunch &L, cudaStream_t s) {
+  if (L.nb == 0) return cudaSuccess;
+  bucket_merge_kernel<<<L.nb, BUCKET_THREADS, (size_t)L.w * sizeof(uint2), s>>>(L);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_sort_init(const ulonglong2 *key, uint64_t *sortkey, uint32_t *perm, uint32_t M, cudaStream_t s) {
+  if (M == 0) return cudaSuccess;
+  uint32_t blocks = (M + 255) / 256;
+  if (blocks > 152u * 16u) blocks = 152u * 16u;
+  sort_init_kernel<<<blocks, 256, 0, s>>>(key, sortkey, perm, M);
   return cudaGetLastError();
 }
 

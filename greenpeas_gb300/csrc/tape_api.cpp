@@ -51,18 +51,18 @@ gpc_status gpc_tape_get_view(const gpc_tape *tape, gpc_tape_view *v) {
   v->num_epochs = T.n_epochs;
   v->kmax = T.kmax;
   v->num_points = T.npoints;
-  v->num_mechanisms = (uint32_t)T.desc.size();
+  v->num_mechanisms = T.M;
+  v->num_records = (uint32_t)T.rec.size();
   v->num_ops = T.ops.size();
   v->ops = T.ops.data();
   v->ep_opoff = T.ep_opoff.data();
   v->ep_k = T.ep_k.data();
   v->ep_ptoff = T.ep_ptoff.data();
-  v->meas_off = T.meas_off.data();
-  v->meas_bits = T.meas_bits.data();
   v->inj_lo = T.inj_lo.data();
   v->inj_hi = T.inj_hi.data();
-  v->desc = T.desc.data();
-  v->prob = T.prob.data();
+  v->rec = T.rec.data();
+  v->rec_p = T.rec_p.data();
+  v->rec_moff = T.rec_moff.data();
   return GPC_OK;
 }
 

@@ -20,7 +20,10 @@
 //      mbarrier; waits are bounded by %globaltimer and report DEV_ERR_TIMEOUT;
 //   4. ops: one-qubit Cliffords, two-qubit Cliffords (partner rows from the
 //      published buffer), resets, measurements (XOR in the measurement's bits
-//      of word j), snapshots of (X, Z) at noise points.
+//      that fall in word j; the bits ride in the tape itself), snapshots of
+//      (X, Z) at noise points.
+// The epoch table (slot count and tape offset per epoch) is staged in shared
+// memory at start, so no global load sits on the per-epoch critical path.
 #include <cstdint>
 
 #include "device.cuh"
@@ -89,10 +92,13 @@ __device__ __forceinline__ uint64_t sel4(uint32_t m, uint64_t a, uint64_t b, uin
   return sel2(m & 3u, a, b) ^ sel2((m >> 2) & 3u, c, d);
 }
 
+constexpr uint32_t kEpochTabMax = 6144;  // epochs whose table is staged in shared memory
+
 template <int QPT>
 __global__ void __launch_bounds__(1024) walk_kernel(const CircuitDev *__restrict__ circs,
                                                     const uint2 *__restrict__ items, uint32_t ring_slots,
-                                                    uint32_t slot_bytes, uint32_t *__restrict__ err) {
+                                                    uint32_t slot_bytes, uint32_t tab_epochs,
+                                                    uint32_t *__restrict__ err) {
   extern __shared__ __align__(128) unsigned char smem[];
   const uint2 item = items[blockIdx.x];
   const CircuitDev C = circs[item.x];
@@ -110,25 +116,37 @@ __global__ void __launch_bounds__(1024) walk_kernel(const CircuitDev *__restrict
   const uint32_t elast = C.inj_hi[j];
 
   ulonglong2 *pub = reinterpret_cast<ulonglong2 *>(smem);  // [2][qpad]
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + (size_t)2 * qpad * sizeof(ulonglong2));
-  unsigned char *ring = smem + (size_t)2 * qpad * sizeof(ulonglong2) + 128;  // ring_slots <= 16
+  size_t off = (size_t)2 * qpad * sizeof(ulonglong2);
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + off);  // ring_slots <= 16
+  off += 128;
+  uint2 *etab = reinterpret_cast<uint2 *>(smem + off);  // (opoff, k) of epochs e0.. (if staged)
+  off += ((size_t)tab_epochs * sizeof(uint2) + 127) / 128 * 128;
+  unsigned char *ring = smem + off;
   __shared__ uint32_t s_abort;
 
+  const bool staged = nE - e0 <= tab_epochs;
+  if (staged) {
+    for (uint32_t i = tid; i < nE - e0; i += T) etab[i] = make_uint2(C.ep_opoff[e0 + i], C.ep_k[e0 + i]);
+  }
   if (tid == 0) {
     s_abort = 0;
     for (uint32_t s = 0; s < ring_slots; ++s) mbar_init(&mbar[s], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
+  auto epoch = [&](uint32_t e) -> uint2 {
+    return staged ? etab[e - e0] : make_uint2(__ldg(C.ep_opoff + e), __ldg(C.ep_k + e));
+  };
 
   // Producer state (thread 0 only): next epoch to load, sequences issued.
   uint32_t next_load = e0;
   uint32_t issued = 0;
   auto issue = [&](uint32_t seq) {
     const uint32_t slot = seq % ring_slots;
-    const uint32_t bytes = C.ep_k[next_load] * qpad * (uint32_t)sizeof(uint64_t);
+    const uint2 ek = epoch(next_load);
+    const uint32_t bytes = ek.y * qpad * (uint32_t)sizeof(uint64_t);
     mbar_expect_tx(&mbar[slot], bytes);
-    bulk_g2s(ring + (size_t)slot * slot_bytes, C.ops + C.ep_opoff[next_load], bytes, &mbar[slot]);
+    bulk_g2s(ring + (size_t)slot * slot_bytes, C.ops + ek.x, bytes, &mbar[slot]);
     ++next_load;
     ++issued;
   };
@@ -136,14 +154,12 @@ __global__ void __launch_bounds__(1024) walk_kernel(const CircuitDev *__restrict
     for (uint32_t s = 0; s < ring_slots && next_load < nE; ++s) issue(s);
   }
 
-  uint64_t X[QPT], Z[QPT];
+  uint64_t X[QPT], Z[QPT], acc[QPT], last_inj[QPT];
 #pragma unroll
-  for (int u = 0; u < QPT; ++u) X[u] = Z[u] = 0;
-  uint64_t last_inj[QPT];
-#pragma unroll
-  for (int u = 0; u < QPT; ++u) last_inj[u] = 0;
+  for (int u = 0; u < QPT; ++u) X[u] = Z[u] = acc[u] = last_inj[u] = 0;
 
   ulonglong2 *snap_j = C.snap + (size_t)j * C.npoints;
+  const uint32_t jlo = j * 64u;
   bool timed_out = false;
   uint32_t e = e0;
   uint32_t seq = 0;
@@ -165,19 +181,17 @@ __global__ void __launch_bounds__(1024) walk_kernel(const CircuitDev *__restrict
       break;
     }
     if ((!any && e > elast) || e >= nE) break;
-    // (3) refill the slot freed by epoch e-1, then wait for epoch e
-    if (tid == 0 && seq > 0 && next_load < nE) {
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-      issue(issued);
-    }
+    // (3) refill the slot freed by epoch e-1 (every thread finished reading it
+    //     before the barrier above), then wait for epoch e
+    if (tid == 0 && seq > 0 && next_load < nE) issue(issued);
     const uint32_t slot = seq % ring_slots;
+    const uint32_t K = epoch(e).y;
     if (!mbar_wait_bounded(&mbar[slot], (seq / ring_slots) & 1u)) {
       timed_out = true;
       continue;
     }
     ++consumed;
     const uint64_t *ops = reinterpret_cast<const uint64_t *>(ring + (size_t)slot * slot_bytes);
-    const uint32_t K = C.ep_k[e];
     // (4) execute
     for (uint32_t k = 0; k < K; ++k) {
 #pragma unroll
@@ -204,17 +218,20 @@ __global__ void __launch_bounds__(1024) walk_kernel(const CircuitDev *__restrict
           case OP_R:
             X[u] = Z[u] = 0;
             break;
-          case OP_M:
-          case OP_MR: {
-            if (opc == OP_MR) X[u] = Z[u] = 0;
-            uint64_t inj = 0;
-            const uint32_t b0 = __ldg(C.meas_off + arg), b1 = __ldg(C.meas_off + arg + 1);
-            for (uint32_t b = b0; b < b1; ++b) {
-              const uint32_t bit = __ldg(C.meas_bits + b);
-              if ((bit >> 6) == j) inj |= 1ull << (bit & 63u);
-            }
-            if (sub != 1u) X[u] ^= inj;
-            if (sub != 0u) Z[u] ^= inj;
+          case OP_INJ: {
+            const uint32_t b2 = ((uint32_t)op >> 8) & 0xFFFFFFu;
+            if (arg - jlo < 64u) acc[u] |= 1ull << (arg - jlo);
+            if (b2 != 0xFFFFFFu && b2 - jlo < 64u) acc[u] |= 1ull << (b2 - jlo);
+            break;
+          }
+          case OP_M: {
+            uint64_t inj = acc[u];
+            if (arg - jlo < 64u) inj |= 1ull << (arg - jlo);
+            acc[u] = 0;
+            if (sub & 4u) X[u] = Z[u] = 0;
+            const uint32_t basis = sub & 3u;
+            if (basis != 1u) X[u] ^= inj;
+            if (basis != 0u) Z[u] ^= inj;
             last_inj[u] = inj;
             break;
           }
@@ -245,34 +262,36 @@ __global__ void __launch_bounds__(1024) walk_kernel(const CircuitDev *__restrict
 
 }  // namespace
 
-size_t walk_smem_bytes(uint32_t qpad, uint32_t ring_slots, uint32_t slot_bytes) {
-  return (size_t)2 * qpad * sizeof(ulonglong2) + 128 + (size_t)ring_slots * slot_bytes;
+size_t walk_smem_bytes(uint32_t qpad, uint32_t ring_slots, uint32_t slot_bytes, uint32_t max_epochs) {
+  const uint32_t tab = max_epochs <= kEpochTabMax ? max_epochs : 0;
+  return (size_t)2 * qpad * sizeof(ulonglong2) + 128 + ((size_t)tab * sizeof(uint2) + 127) / 128 * 128 +
+         (size_t)ring_slots * slot_bytes;
 }
 
 cudaError_t launch_walk(const WalkLaunch &L, cudaStream_t s) {
   if (L.n_items == 0) return cudaSuccess;
   if (L.ring_slots < 1 || L.ring_slots > 16) return cudaErrorInvalidValue;
-  const size_t smem = walk_smem_bytes(L.qpad, L.ring_slots, L.slot_bytes);
+  const uint32_t tab = L.max_epochs <= kEpochTabMax ? L.max_epochs : 0;
+  const size_t smem = walk_smem_bytes(L.qpad, L.ring_slots, L.slot_bytes, L.max_epochs);
   cudaError_t e;
+#define GPC_WALK(Q)                                                                                      \
+  e = cudaFuncSetAttribute(walk_kernel<Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);     \
+  if (e != cudaSuccess) return e;                                                                        \
+  walk_kernel<Q><<<L.n_items, L.threads, smem, s>>>(L.circs, L.items, L.ring_slots, L.slot_bytes, tab, L.err)
   switch (L.qpt) {
     case 1:
-      e = cudaFuncSetAttribute(walk_kernel<1>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return e;
-      walk_kernel<1><<<L.n_items, L.threads, smem, s>>>(L.circs, L.items, L.ring_slots, L.slot_bytes, L.err);
+      GPC_WALK(1);
       break;
     case 2:
-      e = cudaFuncSetAttribute(walk_kernel<2>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return e;
-      walk_kernel<2><<<L.n_items, L.threads, smem, s>>>(L.circs, L.items, L.ring_slots, L.slot_bytes, L.err);
+      GPC_WALK(2);
       break;
     case 4:
-      e = cudaFuncSetAttribute(walk_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-      if (e != cudaSuccess) return e;
-      walk_kernel<4><<<L.n_items, L.threads, smem, s>>>(L.circs, L.items, L.ring_slots, L.slot_bytes, L.err);
+      GPC_WALK(4);
       break;
     default:
       return cudaErrorInvalidValue;
   }
+#undef GPC_WALK
   return cudaGetLastError();
 }
 

@@ -71,13 +71,14 @@ class Driver:
     """Owns a libgpc driver: device buffers, a CUDA stream, the parsed circuit."""
 
     def __init__(self, circuit, correlation_level: CorrelationLevel = CorrelationLevel.L2, *,
-                 device: int = 0, sort_bits: int = 0):
+                 device: int = 0, sort_bits: int = 0, global_sort: bool = False):
         L = _native.lib()
         self._h = ctypes.c_void_p()
         self.correlation_level = CorrelationLevel(correlation_level)
         opts = _native.Options()
         opts.device = device
         opts.sort_bits = sort_bits
+        opts.global_sort = 1 if global_sort else 0
         text = _text(circuit)
         _native.check(L.gpc_get_driver(text, len(text), int(self.correlation_level), ctypes.byref(opts),
                                        ctypes.byref(self._h)))
@@ -145,6 +146,17 @@ class Driver:
                                                    ctypes.byref(w), ctypes.byref(nq)))
         return {"raw": raw.value, "points": pts.value, "epochs": ep.value, "words": w.value, "qubits": nq.value}
 
+    def last_traffic(self) -> dict:
+        """Algorithmic bytes per kernel of the last run (see gpc_last_traffic)."""
+        b = (ctypes.c_double * 4)()
+        _native.check(_native.lib().gpc_last_traffic(self._h, b))
+        return dict(zip(("walk", "key", "bucket", "merge"), [float(x) for x in b]))
+
+    def last_io_bytes(self) -> tuple:
+        h2d, d2h = ctypes.c_uint64(), ctypes.c_uint64()
+        _native.check(_native.lib().gpc_last_io_bytes(self._h, ctypes.byref(h2d), ctypes.byref(d2h)))
+        return h2d.value, d2h.value
+
     @property
     def stream(self) -> int:
         return _native.lib().gpc_driver_stream(self._h) or 0
@@ -171,17 +183,16 @@ class Tape:
                 return np.ctypeslib.as_array(ptr, shape=(n,)).copy() if n else np.zeros(0, dtype=ptr._type_)
 
             for f in ("num_qubits", "qpad", "num_measurements", "num_detectors", "num_observables", "words",
-                      "num_epochs", "kmax", "num_points", "num_mechanisms"):
+                      "num_epochs", "kmax", "num_points", "num_mechanisms", "num_records"):
                 setattr(self, f, int(getattr(v, f)))
             self.ops = arr(v.ops, int(v.num_ops))
             self.ep_opoff = arr(v.ep_opoff, v.num_epochs)
             self.ep_k = arr(v.ep_k, v.num_epochs)
             self.ep_ptoff = arr(v.ep_ptoff, v.num_epochs + 1)
-            self.meas_off = arr(v.meas_off, v.num_measurements + 1)
-            self.meas_bits = arr(v.meas_bits, int(self.meas_off[-1]) if v.num_measurements else 0)
             self.inj_lo = arr(v.inj_lo, v.words)
             self.inj_hi = arr(v.inj_hi, v.words)
-            self.desc = arr(v.desc, v.num_mechanisms)
-            self.prob = arr(v.prob, v.num_mechanisms)
+            self.rec = arr(v.rec, v.num_records)
+            self.rec_p = arr(v.rec_p, v.num_records)
+            self.rec_moff = arr(v.rec_moff, v.num_records + 1)
         finally:
             L.gpc_tape_free(h)

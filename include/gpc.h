@@ -57,9 +57,10 @@ typedef struct gpc_driver gpc_driver;
 typedef struct gpc_dem gpc_dem;
 
 typedef struct gpc_options {
-  int32_t device;    /* CUDA device ordinal (default 0) */
-  int32_t sort_bits; /* key bits sorted before the merge: 0 = default (64) */
-  int32_t reserved[6];
+  int32_t device;      /* CUDA device ordinal (default 0) */
+  int32_t sort_bits;   /* global path only: key bits sorted before the merge (0 = 64) */
+  int32_t global_sort; /* 1: always take the global sort path (tests); 0: buckets first */
+  int32_t reserved[5];
 } gpc_options;
 
 /* Parses `stim_text` (length `len`), sizes device buffers for it and returns
@@ -111,6 +112,16 @@ void *gpc_driver_stream(gpc_driver *driver);
  * the driver's stream): [0] walk, [1] key, [2] sort, [3] merge, [4] total. */
 gpc_status gpc_last_timings(gpc_driver *driver, float *ms5);
 
+/* Algorithmic bytes moved by each kernel of the last run, counted from its
+ * sizes: [0] walk (tape read + snapshots written), [1] key (records + snapshot
+ * reads + keys, descriptors, target lists written), [2] bucket scan + scatter,
+ * [3] merge (bucketed items + target lists read, DEM written). */
+gpc_status gpc_last_traffic(gpc_driver *driver, double *bytes4);
+
+/* Bytes copied host -> device by the last gpc_prepare (the tape) and device ->
+ * host by the last gpc_fetch (the DEM arrays and the result flags). */
+gpc_status gpc_last_io_bytes(gpc_driver *driver, uint64_t *h2d, uint64_t *d2h);
+
 /* Sizes of the last prepared circuit: raw mechanisms, snapshot points,
  * epochs, words per bitset, qubits. */
 gpc_status gpc_last_sizes(gpc_driver *driver, uint64_t *raw, uint64_t *points, uint32_t *epochs,
@@ -122,18 +133,17 @@ gpc_status gpc_last_sizes(gpc_driver *driver, uint64_t *raw, uint64_t *points, u
 typedef struct gpc_tape gpc_tape;
 typedef struct gpc_tape_view {
   uint32_t num_qubits, qpad, num_measurements, num_detectors, num_observables, words;
-  uint32_t num_epochs, kmax, num_points, num_mechanisms;
+  uint32_t num_epochs, kmax, num_points, num_mechanisms, num_records;
   uint64_t num_ops;
   const uint64_t *ops;        /* epoch-major; epoch e is ep_k[e] slots x qpad ops */
   const uint32_t *ep_opoff;   /* [num_epochs] */
   const uint32_t *ep_k;       /* [num_epochs] */
   const uint32_t *ep_ptoff;   /* [num_epochs + 1] */
-  const uint32_t *meas_off;   /* [num_measurements + 1] */
-  const uint32_t *meas_bits;
   const uint32_t *inj_lo;     /* [words] */
   const uint32_t *inj_hi;     /* [words] */
-  const uint64_t *desc;       /* [num_mechanisms] */
-  const double *prob;         /* [num_mechanisms] */
+  const uint64_t *rec;        /* [num_records] noise records */
+  const double *rec_p;        /* [num_records] */
+  const uint32_t *rec_moff;   /* [num_records + 1] first mechanism of each record */
 } gpc_tape_view;
 
 gpc_status gpc_tape_lower(const char *stim_text, size_t len, int32_t correlation_level, gpc_tape **out);

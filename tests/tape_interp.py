@@ -11,7 +11,16 @@ from __future__ import annotations
 
 import numpy as np
 
-OP_NOP, OP_C1, OP_C2, OP_R, OP_M, OP_MR, OP_SNAP, OP_SNAPD = range(8)
+OP_NOP, OP_C1, OP_C2, OP_R, OP_M, OP_INJ, OP_SNAP, OP_SNAPD = range(8)
+# components of each record type as (Pauli a, Pauli b); Pauli 1 X, 2 Z, 3 Y
+_T2 = [(0, 1), (0, 3), (0, 2), (1, 0), (1, 1), (1, 3), (1, 2), (3, 0), (3, 1), (3, 3), (3, 2), (2, 0), (2, 1), (2, 3), (2, 2)]
+REC_COMPS = {
+    1: [(1, 0), (2, 0)],
+    2: [(1, 0), (3, 0), (2, 0)],
+    3: [(0, 1), (0, 2), (1, 0), (1, 1), (2, 0), (2, 2)],
+    4: [(0, 1), (0, 3), (0, 2), (1, 0), (1, 1), (1, 2), (3, 0), (2, 0), (2, 1), (2, 2)],
+    5: _T2,
+}
 NONE = 0xFFFFFFFF
 U64 = np.uint64
 
@@ -37,6 +46,7 @@ def walk(t):
         X = np.zeros(qpad, dtype=np.uint64)
         Z = np.zeros(qpad, dtype=np.uint64)
         last = np.zeros(qpad, dtype=np.uint64)
+        acc = np.zeros(qpad, dtype=np.uint64)
         e = e0
         while True:
             pX, pZ = X.copy(), Z.copy()
@@ -59,19 +69,28 @@ def walk(t):
                     s = sub[m]
                     X[m] = _sel2(s & 3, x, z) ^ _sel2((s >> 2) & 3, px, pz)
                     Z[m] = _sel2((s >> 4) & 3, x, z) ^ _sel2((s >> 6) & 3, px, pz)
-                m = (opc == OP_R) | (opc == OP_MR)
+                m = opc == OP_R
                 X[m] = 0
                 Z[m] = 0
-                for q in np.nonzero((opc == OP_M) | (opc == OP_MR))[0]:
-                    meas = int(arg[q])
-                    inj = 0
-                    for b in t.meas_bits[t.meas_off[meas]:t.meas_off[meas + 1]]:
-                        if int(b) >> 6 == j:
-                            inj |= 1 << (int(b) & 63)
+                jlo = 64 * j
+                for q in np.nonzero(opc == OP_INJ)[0]:
+                    b1, b2 = int(arg[q]), (int(t.ops[off + k * qpad + q]) >> 8) & 0xFFFFFF
+                    for b in (b1, b2):
+                        if b != 0xFFFFFF and 0 <= b - jlo < 64:
+                            acc[q] |= U64(1 << (b - jlo))
+                for q in np.nonzero(opc == OP_M)[0]:
+                    inj = int(acc[q])
+                    b1 = int(arg[q])
+                    if 0 <= b1 - jlo < 64:
+                        inj |= 1 << (b1 - jlo)
+                    acc[q] = 0
                     inj = U64(inj)
-                    if sub[q] != 1:
+                    if sub[q] & 4:
+                        X[q] = 0
+                        Z[q] = 0
+                    if (sub[q] & 3) != 1:
                         X[q] ^= inj
-                    if sub[q] != 0:
+                    if (sub[q] & 3) != 0:
                         Z[q] ^= inj
                     last[q] = inj
                 m = opc == OP_SNAP
@@ -87,14 +106,29 @@ def walk(t):
     return snap, band
 
 
-def symptoms(t, snap, band):
+def expand(t):
+    """Per-mechanism (pa, Pa, pb, Pb, p) arrays, expanding records like the key kernel."""
+    pa, Pa, pb, Pb, p = [], [], [], [], []
+    for r in range(t.num_records):
+        d = int(t.rec[r])
+        a, b = d & 0xFFFFFFF, (d >> 28) & 0xFFFFFFF
+        typ, P0, P1 = (d >> 56) & 15, (d >> 60) & 3, d >> 62
+        comps = [(P0, P1)] if typ == 0 else REC_COMPS[typ]
+        assert t.rec_moff[r + 1] - t.rec_moff[r] == len(comps)
+        for ca, cb in comps:
+            pa.append(a if ca else b)
+            Pa.append(ca if ca else cb)
+            pb.append(b if (ca and cb) else 0)
+            Pb.append(cb if ca else 0)
+            p.append(float(t.rec_p[r]))
+    return (np.array(pa, dtype=np.int64), np.array(Pa, dtype=np.uint32), np.array(pb, dtype=np.int64),
+            np.array(Pb, dtype=np.uint32), np.array(p))
+
+
+def symptoms(t, snap, band, mech):
     """[M, w] uint64 symptom words of every mechanism."""
-    d = t.desc
-    pa = (d & U64(0x3FFFFFFF)).astype(np.int64)
-    Pa = ((d >> U64(30)) & U64(3)).astype(np.uint32)
-    pb = ((d >> U64(32)) & U64(0x3FFFFFFF)).astype(np.int64)
-    Pb = (d >> U64(62)).astype(np.uint32)
-    S = np.zeros((t.num_mechanisms, t.words), dtype=np.uint64)
+    pa, Pa, pb, Pb, _ = mech
+    S = np.zeros((len(pa), t.words), dtype=np.uint64)
     for j in range(t.words):
         lo, hi = band[j]
         ina = (pa >= lo) & (pa < hi)
@@ -108,13 +142,17 @@ def symptoms(t, snap, band):
 def compile_tape(t):
     """{targets tuple: p} -- the DEM the GPU pipeline must produce for tape ``t``."""
     snap, band = walk(t)
-    S = symptoms(t, snap, band)
+    mech = expand(t)
+    S = symptoms(t, snap, band, mech)
+    prob = mech[4]
+    if S.shape[0] == 0:
+        return {}
     uniq, inv = np.unique(S, axis=0, return_inverse=True)
     inv = inv.reshape(-1)
     p = np.full(uniq.shape[0], -1.0)
     for m in range(t.num_mechanisms):
         g = inv[m]
-        q = float(t.prob[m])
+        q = float(prob[m])
         p[g] = q if p[g] < 0 else p[g] * (1 - q) + q * (1 - p[g])
     out = {}
     for g in range(uniq.shape[0]):

@@ -67,11 +67,25 @@ def test_deterministic():
     assert a == b  # same order, same bits
 
 
-@pytest.mark.parametrize("bits", [8, 16])
-def test_short_sort_keys_fall_back_to_full_keys(bits):
-    """Sorting on a few key bits makes runs of different symptoms; the merge must detect them and re-sort."""
+@pytest.mark.parametrize("bits", [8, 16, 64])
+def test_global_sort_path(bits):
+    """The global onesweep path (taken when a bucket overflows).  With few sorted key bits, runs of
+    different symptoms interleave; the merge must detect them and re-sort on all 128 bits."""
     text = gp.SurfaceCode(5).get_memory(5, 1e-3, noise="uniform")
-    _check(gp.get_driver(text, sort_bits=bits).compile(text), text)
+    _check(gp.get_driver(text, sort_bits=bits, global_sort=True).compile(text), text)
+
+
+def test_repeated_symptom_overflows_bucket():
+    """More copies of one symptom than a bucket CTA holds: falls back to the global sort."""
+    text = "R 0 1\n" + "X_ERROR(0.0001) 0\nTICK\n" * 3000 + "CX 0 1\nM 0 1\nDETECTOR rec[-1]\nDETECTOR rec[-2]\n"
+    _check(gp.get_driver(text).compile(text), text)
+
+
+def test_bucket_and_global_paths_agree():
+    text = gp.BBCode(6).get_memory(6, 1e-3, noise="uniform")
+    a = gp.get_driver(text).compile(text)
+    b = gp.get_driver(text, global_sort=True).compile(text)
+    assert a.canonical() == b.canonical() or a.approx_equals(b, rtol=1e-15)
 
 
 def test_empty_and_noiseless():
@@ -89,3 +103,13 @@ def test_device_stages_and_timings():
     t = drv.last_timings()
     assert t["total"] > 0 and all(v >= 0 for v in t.values())
     _check(dem, text)
+
+
+def test_long_symptoms_widen_target_lists():
+    """A symptom with more targets than the default target-list stride (32): the key kernel flags it,
+    the driver widens the stride and runs again."""
+    n = 80
+    text = "R " + " ".join(map(str, range(n))) + "\nX_ERROR(0.01) 0\n"
+    text += "".join(f"CX 0 {q}\n" for q in range(1, n))
+    text += "M " + " ".join(map(str, range(n))) + "\n" + "".join(f"DETECTOR rec[-{k}]\n" for k in range(1, n + 1))
+    _check(gp.get_driver(text).compile(text), text)
