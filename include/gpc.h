@@ -127,6 +127,37 @@ gpc_status gpc_last_io_bytes(gpc_driver *driver, uint64_t *h2d, uint64_t *d2h);
 gpc_status gpc_last_sizes(gpc_driver *driver, uint64_t *raw, uint64_t *points, uint32_t *epochs,
                           uint32_t *words, uint32_t *qubits);
 
+/* ---- merging without allocation -------------------------------------------
+ * No counterpart in the reference: GreenPeas always allocates its workspaces
+ * (Driver.hpp:69-76).  This entry point is for callers that cannot allocate
+ * device memory -- for example code running while another runtime owns the
+ * device's memory pool, or a decoder loop whose memory is reserved up front
+ * and must not grow or synchronise the device in an allocation.
+ *
+ * Merges n raw error mechanisms into a DEM on `stream` (a cudaStream_t, NULL
+ * for the default stream) on the current device.  All pointers are device
+ * memory the caller owns:
+ *   num_targets[n], targets[n * stride] (ascending target indices of
+ *   mechanism i at targets[i*stride ...]), probs[n]  -- inputs;
+ *   out_probs[n], out_offsets[n + 1], out_targets[out_target_cap]  -- the
+ *   merged DEM, as gpc_dem_arrays; result[4] = {errors, targets, flags, 0},
+ *   flags != 0 means the output is not valid (1 timeout, 2 hash collision,
+ *   8 out_target_cap too small, 16 one symptom repeated over 1024 times,
+ *   64 a target list is longer than stride or not ascending).
+ * Empty symptoms are dropped; equal symptoms are merged with
+ * p <- p1(1-p2) + p2(1-p1).
+ *
+ * It calls no allocator: all scratch lives in a static device array of about
+ * 2.3 MiB that every GPU loading the library keeps until exit, which limits n
+ * to 65,536 (GPC_ERR_CAPACITY above that).  Every call on a device shares
+ * that array, so calls that overlap on the GPU race: serialise them.  The
+ * first call on each device looks up the array's device address (make it
+ * before any stream capture).  Returns once the work is queued. */
+gpc_status gpc_merge_mechanisms_static(const uint32_t *num_targets, const uint32_t *targets, uint32_t stride,
+                                       const double *probs, uint32_t n, double *out_probs,
+                                       uint32_t *out_offsets, uint32_t *out_targets, uint32_t out_target_cap,
+                                       uint32_t *result, void *stream);
+
 /* ---- tape inspection (host only, no GPU needed) ---------------------------
  * Lowers a circuit to the device tick tape without compiling it, for tools
  * and tests that check the lowering.  Arrays are owned by the tape. */
