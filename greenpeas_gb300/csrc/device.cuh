@@ -22,6 +22,9 @@ struct CircuitDev {
   const uint32_t *ep_opoff;   // [n_epochs]
   const uint32_t *ep_k;       // [n_epochs]
   const uint32_t *ep_ptoff;   // [n_epochs + 1]
+  const uint32_t *ep_chunk;   // [n_epochs] copy chunk of each epoch
+  const uint32_t *ch_off;     // [n_chunks] first op of each chunk
+  const uint32_t *ch_bytes;   // [n_chunks]
   const uint32_t *inj_lo;     // [w] first epoch injecting into word j (0xFFFFFFFF: none)
   const uint32_t *inj_hi;     // [w] last epoch injecting into word j
   ulonglong2 *snap;           // [w][npoints] (X row, Z row) at each point
@@ -36,6 +39,7 @@ struct CircuitDev {
   uint32_t nq, qpad, n_epochs, w;
   uint32_t npoints, M, R;
   uint32_t tcap;              // stride of tl (0: no target lists, merge from snapshots)
+  uint32_t n_chunks, chunk_cap;
 };
 
 constexpr int SORT_THREADS = 256;
@@ -56,19 +60,19 @@ struct WalkLaunch {
   const uint2 *items;       // device array of (circuit, word)
   uint32_t n_items;
   uint32_t threads, qpt, qpad;
-  uint32_t ring_slots, slot_bytes;
-  uint32_t max_epochs;      // largest n_epochs of the launch (sizes the epoch table in shared memory)
+  uint32_t chunk_cap;       // bytes of each of the two chunk buffers
+  uint32_t max_epochs, max_chunks;  // largest tables of the launch (staged in shared memory if they fit)
   uint32_t *err;
 };
 cudaError_t launch_walk(const WalkLaunch &L, cudaStream_t s);
-size_t walk_smem_bytes(uint32_t qpad, uint32_t ring_slots, uint32_t slot_bytes, uint32_t max_epochs);
+size_t walk_smem_bytes(uint32_t qpad, uint32_t chunk_cap);
 
 // Key kernel: one thread per noise record; expands the record into its
 // mechanisms (mdesc, mp), computes each mechanism's 128-bit key, and counts
 // non-empty keys per bucket (top `bucket_bits` bits of key.x).
 struct KeyLaunch {
   const CircuitDev *c_dev;
-  uint32_t R, w;
+  uint32_t R, M, w;
   ulonglong2 *key;          // [M]
   uint32_t *bucket_count;   // [1 << bucket_bits] (zeroed)
   uint32_t bucket_bits;

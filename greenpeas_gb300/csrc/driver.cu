@@ -97,7 +97,7 @@ struct HostBuf {
 // Byte offsets of every array inside the arena (inputs first, so the whole
 // input region is one contiguous H2D copy).
 struct Layout {
-  size_t ops, ep_opoff, ep_k, ep_ptoff, inj_lo, inj_hi, rec, rec_p, rec_moff, cdev, items;
+  size_t ops, ep_opoff, ep_k, ep_ptoff, ep_chunk, ch_off, ch_bytes, inj_lo, inj_hi, rec, rec_p, rec_moff, cdev, items;
   size_t in_bytes;
   size_t snap, band, mdesc, mp, tl, tn, key, boff, bkey, bm;
   size_t sk0, sk1, pm0, pm1, hik;  // global path
@@ -141,7 +141,7 @@ struct gpc_driver {
   uint32_t *perm_sorted = nullptr;
   uint64_t *sk_sorted = nullptr;
   uint64_t sort_mask = ~0ull;
-  uint32_t ring_slots = 1, slot_bytes = 0, threads = 32, qpt = 1;
+  uint32_t threads = 32, qpt = 1;
   bool force_global = false;  // debug/test option: skip the bucket path
   uint32_t tcap = 32;         // target-list stride (grows when a symptom is longer)
   bool lists_off = false;     // symptoms too long for target lists: merge from snapshots
@@ -177,6 +177,9 @@ struct gpc_driver {
     L.ep_opoff = take(T.ep_opoff.size() * 4);
     L.ep_k = take(T.ep_k.size() * 4);
     L.ep_ptoff = take(T.ep_ptoff.size() * 4);
+    L.ep_chunk = take(T.ep_chunk.size() * 4);
+    L.ch_off = take(T.ch_off.size() * 4);
+    L.ch_bytes = take(T.ch_bytes.size() * 4);
     L.inj_lo = take(T.inj_lo.size() * 4);
     L.inj_hi = take(T.inj_hi.size() * 4);
     L.rec = take((size_t)R * 8);
@@ -238,6 +241,9 @@ struct gpc_driver {
     put(L.ep_opoff, T.ep_opoff.data(), T.ep_opoff.size() * 4);
     put(L.ep_k, T.ep_k.data(), T.ep_k.size() * 4);
     put(L.ep_ptoff, T.ep_ptoff.data(), T.ep_ptoff.size() * 4);
+    put(L.ep_chunk, T.ep_chunk.data(), T.ep_chunk.size() * 4);
+    put(L.ch_off, T.ch_off.data(), T.ch_off.size() * 4);
+    put(L.ch_bytes, T.ch_bytes.data(), T.ch_bytes.size() * 4);
     put(L.inj_lo, T.inj_lo.data(), T.inj_lo.size() * 4);
     put(L.inj_hi, T.inj_hi.data(), T.inj_hi.size() * 4);
     put(L.rec, T.rec.data(), T.rec.size() * 8);
@@ -248,6 +254,9 @@ struct gpc_driver {
     c.ep_opoff = dptr<uint32_t>(L.ep_opoff);
     c.ep_k = dptr<uint32_t>(L.ep_k);
     c.ep_ptoff = dptr<uint32_t>(L.ep_ptoff);
+    c.ep_chunk = dptr<uint32_t>(L.ep_chunk);
+    c.ch_off = dptr<uint32_t>(L.ch_off);
+    c.ch_bytes = dptr<uint32_t>(L.ch_bytes);
     c.inj_lo = dptr<uint32_t>(L.inj_lo);
     c.inj_hi = dptr<uint32_t>(L.inj_hi);
     c.snap = dptr<ulonglong2>(L.snap);
@@ -267,6 +276,8 @@ struct gpc_driver {
     c.npoints = T.npoints;
     c.M = T.M;
     c.R = (uint32_t)T.rec.size();
+    c.n_chunks = (uint32_t)T.ch_off.size();
+    c.chunk_cap = T.chunk_cap;
     put(L.cdev, &c, sizeof(c));
     std::vector<uint2> items(T.w);
     for (uint32_t j = 0; j < T.w; ++j) items[j] = make_uint2(0u, j);
@@ -303,12 +314,6 @@ struct gpc_driver {
     // walk launch geometry
     qpt = tape.qpad <= 1024 ? 1 : tape.qpad <= 2048 ? 2 : 4;
     threads = tape.qpad / qpt;
-    slot_bytes = std::max<uint32_t>(1, tape.kmax) * tape.qpad * 8;
-    const size_t budget = 200 * 1024;
-    const size_t fixed = gpc::walk_smem_bytes(tape.qpad, 0, 0, tape.n_epochs);
-    size_t slots = budget > fixed ? (budget - fixed) / slot_bytes : 0;
-    if (slots < 1) throw gpc::Error(GPC_ERR_CAPACITY, "tape epoch too large for shared memory");
-    ring_slots = (uint32_t)std::min<size_t>(8, slots);
     prepared = true;
   }
 
@@ -325,9 +330,9 @@ struct gpc_driver {
     wl.threads = threads;
     wl.qpt = qpt;
     wl.qpad = T.qpad;
-    wl.ring_slots = ring_slots;
-    wl.slot_bytes = slot_bytes;
+    wl.chunk_cap = T.chunk_cap;
     wl.max_epochs = T.n_epochs;
+    wl.max_chunks = (uint32_t)T.ch_off.size();
     wl.err = dptr<uint32_t>(L.err);
     if (T.n_epochs > 0) CK(gpc::launch_walk(wl, stream));
     else CK(cudaMemsetAsync(dptr<char>(L.band), 0, (size_t)T.w * 8, stream));
@@ -335,6 +340,7 @@ struct gpc_driver {
     gpc::KeyLaunch kl{};
     kl.c_dev = dptr<CircuitDev>(L.cdev);
     kl.R = (uint32_t)T.rec.size();
+    kl.M = T.M;
     kl.w = T.w;
     kl.key = dptr<ulonglong2>(L.key);
     kl.bucket_count = dptr<uint32_t>(L.bcount);

@@ -205,9 +205,22 @@ struct TextParser {
       in.nargs = (uint8_t)std::min(na, 3);
       for (int i = 0; i < in.nargs; ++i) in.args[i] = args[i];
       in.t0 = (uint32_t)out->pool.size();
+      std::vector<uint32_t> &pool = out->pool;
       while (true) {
-        sp();
-        if (s >= e || *s == '\n' || *s == '#') break;
+        while (s < e && (*s == ' ' || *s == '\t')) ++s;
+        if (s >= e) break;
+        const char c0 = *s;
+        if ((unsigned)(c0 - '0') < 10u) {  // fast path: a plain qubit index
+          uint32_t q = (uint32_t)(c0 - '0');
+          ++s;
+          while (s < e && (unsigned)(*s - '0') < 10u) {
+            q = q * 10u + (uint32_t)(*s++ - '0');
+            if (q >= kMaxQubit) fail(GPC_ERR_CAPACITY, "qubit index too large");
+          }
+          pool.push_back(q);
+          continue;
+        }
+        if (c0 == '\n' || c0 == '#' || c0 == '\r') break;
         if (*s == '!') ++s;  // inverted measurement result: no effect on sensitivities
         if (s >= e) fail(GPC_ERR_PARSE, "bad target");
         if (*s == '*') fail(GPC_ERR_UNSUPPORTED, "combiner targets are not supported");
@@ -218,16 +231,16 @@ struct TextParser {
           uint32_t k = uint();
           if (s >= e || *s != ']' || k == 0) fail(GPC_ERR_PARSE, "bad record target");
           ++s;
-          out->pool.push_back(kRec | k);
+          pool.push_back(kRec | k);
         } else if (*s == 'X' || *s == 'Y' || *s == 'Z' || *s == 'x' || *s == 'y' || *s == 'z') {
           char p = (char)toupper((unsigned char)*s++);
           uint32_t q = uint();
           if (q >= kMaxQubit) fail(GPC_ERR_CAPACITY, "qubit index too large");
-          out->pool.push_back(kPau | ((uint32_t)(p == 'X' ? 1 : p == 'Z' ? 2 : 3) << 24) | q);
-        } else if (*s >= '0' && *s <= '9') {
+          pool.push_back(kPau | ((uint32_t)(p == 'X' ? 1 : p == 'Z' ? 2 : 3) << 24) | q);
+        } else if ((unsigned)(*s - '0') < 10u) {
           uint32_t q = uint();
           if (q >= kMaxQubit) fail(GPC_ERR_CAPACITY, "qubit index too large");
-          out->pool.push_back(q);
+          pool.push_back(q);
         } else if (e - s >= 6 && memcmp(s, "sweep[", 6) == 0) {
           fail(GPC_ERR_UNSUPPORTED, "sweep targets are not supported");
         } else {
@@ -269,6 +282,17 @@ bool dep2_kept(int level, int pa, int pb) {
 // Swaps the qubit halves of a two-qubit mask (Xa,Za,Xb,Zb) -> (Xb,Zb,Xa,Za).
 uint32_t swap_halves(uint32_t m) { return ((m >> 2) & 3u) | ((m & 3u) << 2); }
 
+// A two-qubit Clifford update for one side, as a single-XOR opcode when the
+// masks allow (bits: 0 self X, 1 self Z, 2 partner X, 3 partner Z; newX in
+// the low nibble, newZ in the high nibble).
+uint64_t c2_op(uint32_t sub, uint32_t partner) {
+  const uint32_t nx = sub & 15u, nz = sub >> 4;
+  if (nz == 2u && nx == (1u | 4u)) return make_op(OP_XPX, 0, partner);
+  if (nx == 1u && nz == (2u | 8u)) return make_op(OP_ZPZ, 0, partner);
+  if (nz == 2u && nx == (1u | 8u)) return make_op(OP_XPZ, 0, partner);
+  return make_op(OP_C2, sub, partner);
+}
+
 // One tape entry placed by the backward scheduler: qubit, epoch, slot, op.
 struct Entry {
   uint32_t q, e, k;
@@ -305,6 +329,8 @@ struct SplitCache {
 Parsed parse_stim(const char *text, size_t len) {
   Parsed p;
   if (!text && len) throw Error(GPC_ERR_INVALID, "null circuit text");
+  p.pool.reserve(len / 3 + 16);
+  p.ins.reserve(len / 64 + 16);
   TextParser tp{text, text + len, 1, &p};
   tp.block(p.ins, false, 0);
   return p;
@@ -408,8 +434,10 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
     uint32_t per = (nq + qpt - 1) / qpt;
     uint32_t threads = std::max<uint32_t>(32, (per + 31) / 32 * 32);
     T.qpad = threads * qpt;
-    // an epoch (kcap slots x qpad ops) must fit a shared-memory ring slot of <= 96 KiB
-    kcap = std::min<uint32_t>(kcap, std::max<uint32_t>(1, 98304u / (T.qpad * 8u)));
+    // an epoch (kcap slots x qpad ops) must fit one shared-memory chunk buffer
+    T.chunk_cap = walk_chunk_cap(T.qpad);
+    if (T.chunk_cap < T.qpad * 8u) throw Error(GPC_ERR_CAPACITY, "too many qubits for the walk's shared memory");
+    kcap = std::min<uint32_t>(kcap, T.chunk_cap / (T.qpad * 8u));
   }
 
   // measurement -> bits (XOR: a measurement listed twice in one detector cancels)
@@ -497,8 +525,8 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
           uint32_t E = (uint32_t)(std::max(st[a].last, st[b].last) + 1);
           uint32_t subA = (uint32_t)g.img[0] | ((uint32_t)g.img[1] << 4);
           uint32_t subB = swap_halves(g.img[2]) | (swap_halves(g.img[3]) << 4);
-          ent.push_back({a, E, 0, make_op(OP_C2, subA, b)});
-          ent.push_back({b, E, 0, make_op(OP_C2, subB, a)});
+          ent.push_back({a, E, 0, c2_op(subA, b)});  // partner operands become slots below
+          ent.push_back({b, E, 0, c2_op(subB, a)});
           if (E >= ep_k.size()) ep_k.resize((size_t)E + 1, 0);
           ep_k[E] = std::max<uint32_t>(ep_k[E], 1);
           st[a].last = st[b].last = E;
@@ -605,6 +633,65 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
     }
   }
 
+  // ---- warp-uniform qubit packing -------------------------------------
+  // Qubits with the same sequence of op kinds (data, X-check, Z-check qubits
+  // of a code) take the same branches in the walk.  Group them, and start
+  // each group on a warp boundary when that costs at most half again as many
+  // slots, so a warp does not mix roles.
+  std::vector<uint32_t> slotOf(nq);
+  {
+    // fine signature: op kinds with their epochs; coarse: op kinds only
+    std::vector<uint64_t> fine(nq, 0xcbf29ce484222325ull), coarse(nq, 0xcbf29ce484222325ull);
+    for (const Entry &x : ent) {
+      const uint32_t opc = (uint32_t)(x.op & 0xFF);
+      if (opc == OP_INJ || opc == OP_SNAPD) continue;  // vary with detector membership only
+      coarse[x.q] = (coarse[x.q] ^ opc) * 0x100000001b3ull;
+      fine[x.q] = (fine[x.q] ^ (opc | ((uint64_t)x.e << 8))) * 0x100000001b3ull;
+    }
+    const uint32_t qptBase = T.qpad <= 1024 ? 1u : T.qpad <= 2048 ? 2u : 4u;
+    // Orders qubits by group (groups in order of their first qubit); returns the
+    // padded slot count, or 0 if padding does not fit.
+    auto plan = [&](const std::vector<uint64_t> &sig, std::vector<uint32_t> &order,
+                    std::vector<std::pair<uint32_t, uint32_t>> &groups) -> uint32_t {
+      order.resize(nq);
+      for (uint32_t q = 0; q < nq; ++q) order[q] = q;
+      std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) {
+        return sig[a] != sig[b] ? sig[a] < sig[b] : a < b;
+      });
+      groups.clear();
+      for (uint32_t i = 0; i < nq;) {
+        uint32_t k = i;
+        while (k < nq && sig[order[k]] == sig[order[i]]) ++k;
+        groups.push_back({i, k - i});
+        i = k;
+      }
+      std::sort(groups.begin(), groups.end(),
+                [&](const std::pair<uint32_t, uint32_t> &a, const std::pair<uint32_t, uint32_t> &b) {
+                  return order[a.first] < order[b.first];
+                });
+      uint32_t padded = 0;
+      for (auto &g : groups) padded += (g.second + 31) / 32 * 32;
+      const uint32_t qptP = padded <= 1024 ? 1u : padded <= 2048 ? 2u : 4u;
+      const uint32_t qpadP = std::max<uint32_t>(32, (padded + 31) / 32 * 32);
+      const bool ok = qptP == qptBase && padded <= 4096 && 2 * (uint64_t)padded <= 3 * (uint64_t)T.qpad &&
+                      (uint64_t)kcap * qpadP * 8 <= walk_chunk_cap(qpadP);
+      return ok ? qpadP : 0u;
+    };
+    std::vector<uint32_t> order;
+    std::vector<std::pair<uint32_t, uint32_t>> groups;
+    uint32_t qpadP = plan(fine, order, groups);
+    if (!qpadP) qpadP = plan(coarse, order, groups);
+    uint32_t next = 0;
+    for (auto &g : groups) {
+      for (uint32_t i = 0; i < g.second; ++i) slotOf[order[g.first + i]] = next++;
+      if (qpadP) next = (next + 31) / 32 * 32;
+    }
+    if (qpadP) {
+      T.qpad = qpadP;
+      T.chunk_cap = walk_chunk_cap(T.qpad);
+    }
+  }
+
   // ---- assemble epochs -------------------------------------------------
   const uint32_t nE = (uint32_t)ep_k.size();
   T.n_epochs = nE;
@@ -619,7 +706,13 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
     if (total > 0xFFFFFFFFull) throw Error(GPC_ERR_CAPACITY, "tape too long");
   }
   T.ops.assign(total, 0);
-  for (const Entry &x : ent) T.ops[(size_t)T.ep_opoff[x.e] + (size_t)x.k * T.qpad + x.q] = x.op;
+  for (const Entry &x : ent) {
+    uint64_t op = x.op;
+    const uint32_t opc = (uint32_t)(op & 0xFF);
+    if (opc == OP_C2 || opc >= OP_XPX)  // partner qubit -> partner slot
+      op = (op & 0xFFFFFFFFull) | ((uint64_t)slotOf[(uint32_t)(op >> 32)] << 32);
+    T.ops[(size_t)T.ep_opoff[x.e] + (size_t)x.k * T.qpad + slotOf[x.q]] = op;
+  }
   // points: renumber in walk order (epoch, slot, qubit) so each epoch owns a contiguous range
   std::vector<uint32_t> remap(nprov, kNone);
   T.ep_ptoff.assign(nE + 1, 0);
@@ -640,6 +733,21 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
   }
   T.ep_ptoff[nE] = next;
   T.npoints = next;
+  // copy chunks: runs of whole epochs of at most chunk_cap bytes
+  T.ep_chunk.assign(nE, 0);
+  for (uint32_t e = 0; e < nE;) {
+    const uint32_t c = (uint32_t)T.ch_off.size();
+    uint64_t bytes = 0;
+    uint32_t f = e;
+    while (f < nE && bytes + (uint64_t)T.ep_k[f] * T.qpad * 8 <= T.chunk_cap) {
+      bytes += (uint64_t)T.ep_k[f] * T.qpad * 8;
+      T.ep_chunk[f] = c;
+      ++f;
+    }
+    T.ch_off.push_back(T.ep_opoff[e]);
+    T.ch_bytes.push_back((uint32_t)bytes);
+    e = f;
+  }
   if (next > kMaxPoint28) throw Error(GPC_ERR_CAPACITY, "too many snapshot points");
   const size_t R = T.rec.size();
   T.rec_moff.resize(R + 1);

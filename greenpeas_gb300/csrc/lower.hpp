@@ -43,6 +43,10 @@ enum : uint32_t {
   OP_INJ = 5,    // two more bits of the next OP_M: operand, and bits 8-31 (0xFFFFFF: none)
   OP_SNAP = 6,   // operand: point; point <- (X, Z)
   OP_SNAPD = 7,  // operand: point; point <- (bits of the last measurement, 0)
+  // two-qubit Cliffords whose update is one XOR (operand: partner qubit)
+  OP_XPX = 8,    // X ^= partner X   (CX control)
+  OP_ZPZ = 9,    // Z ^= partner Z   (CX target)
+  OP_XPZ = 10,   // X ^= partner Z   (CZ, either qubit)
 };
 
 inline uint64_t make_op(uint32_t opc, uint32_t sub, uint32_t operand) {
@@ -104,6 +108,10 @@ struct Tape {
   std::vector<uint32_t> ep_opoff;   // [n_epochs]     first op of epoch e
   std::vector<uint32_t> ep_k;       // [n_epochs]     slots in epoch e
   std::vector<uint32_t> ep_ptoff;   // [n_epochs + 1] first point of epoch e
+  std::vector<uint32_t> ep_chunk;   // [n_epochs]     copy chunk holding epoch e
+  std::vector<uint32_t> ch_off;     // [n_chunks]     first op of each chunk (= ep_opoff of its first epoch)
+  std::vector<uint32_t> ch_bytes;   // [n_chunks]     bytes of each chunk (a whole number of epochs)
+  uint32_t chunk_cap = 0;           // bytes of one shared-memory chunk buffer
   std::vector<uint32_t> inj_lo;     // [w] first epoch (walk order) injecting into word j, kNone if none
   std::vector<uint32_t> inj_hi;     // [w] last such epoch
   uint32_t npoints = 0;
@@ -117,6 +125,19 @@ struct LowerOptions {
   int level = 2;     // correlation level 0/1/2
   uint32_t kcap = 8; // max slots per epoch
 };
+
+// Shared-memory plan of the walk kernel (bytes): double-buffered tape chunks,
+// the published rows, and the epoch/chunk tables when they fit.
+constexpr uint32_t kWalkSmemBudget = 224 * 1024;
+constexpr uint32_t kWalkTableBudget = 32 * 1024;
+constexpr uint32_t kWalkChunkMax = 96 * 1024;
+inline uint32_t walk_chunk_cap(uint32_t qpad) {
+  const uint32_t pub = 2 * qpad * 16 + 128;
+  if (pub + kWalkTableBudget >= kWalkSmemBudget) return 0;
+  uint32_t c = (kWalkSmemBudget - pub - kWalkTableBudget) / 2;
+  c = c < kWalkChunkMax ? c : kWalkChunkMax;
+  return c & ~255u;
+}
 
 Tape lower(const Parsed &p, const LowerOptions &opt);
 

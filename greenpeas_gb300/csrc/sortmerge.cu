@@ -100,76 +100,65 @@ __global__ void __launch_bounds__(256) key_kernel(KeyLaunch L) {
   for (uint32_t j = threadIdx.x; j < w; j += blockDim.x) sband[j] = C.band[j];
   __syncthreads();
   const uint32_t shift = 64u - L.bucket_bits;
-  for (uint32_t r = blockIdx.x * blockDim.x + threadIdx.x; r < L.R; r += gridDim.x * blockDim.x) {
-    const uint64_t d = __ldg(C.rec + r);
-    const uint32_t pa = (uint32_t)(d & 0x0FFFFFFFu), pb = (uint32_t)((d >> 28) & 0x0FFFFFFFu);
-    const uint32_t type = (uint32_t)((d >> 56) & 15u);
-    const uint32_t P0 = (uint32_t)((d >> 60) & 3u), P1 = (uint32_t)(d >> 62);
-    const uint32_t nc = type == 0 ? 1u : kNComp[type];
-    const bool hasB = type >= 3u || P1 != 0;
-    uint32_t comp[15];
-#pragma unroll
-    for (int c = 0; c < 15; ++c) comp[c] = type == 0 ? (c == 0 ? (P0 | (P1 << 2)) : 0u) : kComp[type][c];
-    uint64_t hx[15], hy[15];
-    uint32_t cnt[15];
-#pragma unroll
-    for (int c = 0; c < 15; ++c) {
-      hx[c] = hy[c] = 0;
-      cnt[c] = 0;
+  const uint32_t tcap = C.tcap;
+  const uint32_t R = L.R;
+  for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < C.M; m += gridDim.x * blockDim.x) {
+    // the record holding mechanism m: the last r with rec_moff[r] <= m
+    uint32_t lo = 0, hi = R;  // rec_moff[lo] <= m < rec_moff[hi]
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (__ldg(C.rec_moff + mid) <= m) lo = mid;
+      else hi = mid;
     }
-    uint32_t nzmask = 0;
-    const uint32_t m0 = __ldg(C.rec_moff + r);
-    const uint32_t tcap = C.tcap;
+    const uint32_t r = lo;
+    const uint64_t d = __ldg(C.rec + r);
+    const uint32_t c = m - __ldg(C.rec_moff + r);
+    const uint32_t type = (uint32_t)((d >> 56) & 15u);
+    const uint32_t comp = type == 0 ? (uint32_t)((d >> 60) & 3u) | ((uint32_t)(d >> 62) << 2) : kComp[type][c];
+    uint32_t pa = (uint32_t)(d & 0x0FFFFFFFu), pb = (uint32_t)((d >> 28) & 0x0FFFFFFFu);
+    uint32_t Pa = comp & 3u, Pb = comp >> 2;
+    if (Pa == 0) {  // a component on point b only is stored with b as its first point
+      pa = pb;
+      Pa = Pb;
+      Pb = 0;
+    }
+    if (Pb == 0) pb = 0;
+    C.mdesc[m] = mk_desc(pa, Pa, pb, Pb);
+    C.mp[m] = __ldg(C.rec_p + r);
+    uint64_t hx = 0, hy = 0;
+    uint32_t cnt = 0;
+    bool nonzero = false;
+    uint32_t *out = C.tl + (size_t)m * tcap;
     for (uint32_t j = 0; j < w; ++j) {
       const uint2 b = sband[j];
       const ulonglong2 *sj = C.snap + (size_t)j * C.npoints;
-      ulonglong2 sa = make_ulonglong2(0, 0), sb = make_ulonglong2(0, 0);
-      if (pa - b.x < b.y - b.x) sa = sj[pa];
-      if (hasB && pb - b.x < b.y - b.x) sb = sj[pb];
-      if ((sa.x | sa.y | sb.x | sb.y) == 0) continue;
-#pragma unroll
-      for (int c = 0; c < 15; ++c) {
-        if ((uint32_t)c < nc) {
-          const uint64_t v = pauli_sel(sa, comp[c] & 3u) ^ pauli_sel(sb, comp[c] >> 2);
-          if (v) {
-            const ulonglong2 h = word_hash(j, v);
-            hx[c] ^= h.x;
-            hy[c] ^= h.y;
-            nzmask |= 1u << c;
-            if (tcap) {
-              uint32_t *out = C.tl + (size_t)(m0 + (uint32_t)c) * tcap;
-              uint64_t x = v;
-              while (x) {
-                if (cnt[c] < tcap) out[cnt[c]] = j * 64u + (uint32_t)(__ffsll((long long)x) - 1);
-                ++cnt[c];
-                x &= x - 1;
-              }
-            }
-          }
+      uint64_t v = 0;
+      if (pa - b.x < b.y - b.x) v = pauli_sel(sj[pa], Pa);
+      if (Pb && pb - b.x < b.y - b.x) v ^= pauli_sel(sj[pb], Pb);
+      if (!v) continue;
+      nonzero = true;
+      const ulonglong2 h = word_hash(j, v);
+      hx ^= h.x;
+      hy ^= h.y;
+      if (tcap) {
+        uint64_t x = v;
+        while (x) {
+          if (cnt < tcap) out[cnt] = j * 64u + (uint32_t)(__ffsll((long long)x) - 1);
+          ++cnt;
+          x &= x - 1;
         }
       }
     }
-    const double p = __ldg(C.rec_p + r);
-#pragma unroll
-    for (int c = 0; c < 15; ++c) {
-      if ((uint32_t)c < nc) {
-        const uint32_t m = m0 + (uint32_t)c;
-        const uint32_t Pa = comp[c] & 3u, Pb = comp[c] >> 2;
-        // a component that touches only point b is stored with b as its first point
-        C.mdesc[m] = Pa ? mk_desc(pa, Pa, Pb ? pb : 0u, Pb) : mk_desc(pb, Pb, 0u, 0u);
-        C.mp[m] = p;
-        L.key[m] = make_ulonglong2(hx[c], hy[c]);
-        if (tcap) {
-          C.tn[m] = cnt[c];
-          if (cnt[c] > tcap) atomicOr(L.err, DEV_FLAG_LONG);
-          if (cnt[c]) atomicAdd(L.list_total, cnt[c]);
-        }
-        if ((hx[c] | hy[c]) == 0) {
-          if (nzmask & (1u << c)) atomicOr(L.err, DEV_ERR_COLLISION);  // non-empty symptom hashed to 0
-        } else {
-          atomicAdd(L.bucket_count + (hx[c] >> shift), 1u);
-        }
-      }
+    L.key[m] = make_ulonglong2(hx, hy);
+    if (tcap) {
+      C.tn[m] = cnt;
+      if (cnt > tcap) atomicOr(L.err, DEV_FLAG_LONG);
+      if (cnt) atomicAdd(L.list_total, cnt);
+    }
+    if ((hx | hy) == 0) {
+      if (cnt || (!tcap && nonzero)) atomicOr(L.err, DEV_ERR_COLLISION);  // a non-empty symptom hashed to 0
+    } else {
+      atomicAdd(L.bucket_count + (hx >> shift), 1u);
     }
   }
 }
@@ -576,18 +565,31 @@ __device__ __forceinline__ void warp_lookback(unsigned long long *status, uint32
   *pre_t = et;
 }
 
+// Loads a target list as 16-byte vectors (rows are 16-byte aligned).
+__device__ __forceinline__ bool lists_equal(const uint32_t *a, const uint32_t *b, uint32_t n) {
+  const uint4 *va = reinterpret_cast<const uint4 *>(a), *vb = reinterpret_cast<const uint4 *>(b);
+  for (uint32_t k = 0; k * 4 < n; ++k) {
+    const uint4 x = __ldg(va + k), y = __ldg(vb + k);
+    const uint32_t rem = n - k * 4;
+    if (x.x != y.x || (rem > 1 && x.y != y.y) || (rem > 2 && x.z != y.z) || (rem > 3 && x.w != y.w)) return false;
+  }
+  return true;
+}
+
 __global__ void __launch_bounds__(BUCKET_THREADS) bucket_merge_kernel(BucketMergeLaunch L) {
   constexpr int NT = BUCKET_THREADS;
-  constexpr int CHUNK = BUCKET_CAP / NT;  // positions per thread in the scans
+  constexpr int NW = NT / 32;
   __shared__ ulonglong2 sk[BUCKET_CAP];
   __shared__ uint32_t sm[BUCKET_CAP];
   __shared__ uint16_t ord[BUCKET_CAP];
-  __shared__ uint32_t sntg[BUCKET_CAP];  // targets of the group starting at a sorted position, or ~0u
-  __shared__ uint32_t sc[NT], st_[NT];
+  __shared__ uint32_t sntg[BUCKET_CAP];  // targets of a group starting at a sorted position, else ~0u
+  __shared__ uint2 sexc[BUCKET_CAP];     // exclusive (groups, targets) before each sorted position
+  __shared__ uint32_t wc[NW], wt[NW];
   __shared__ uint32_t s_b, s_pre_c, s_pre_t;
   extern __shared__ uint2 sband[];
   const CircuitDev C = *L.c_dev;
   const uint32_t w = L.w;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   for (uint32_t j = threadIdx.x; j < w; j += NT) sband[j] = C.band[j];
   if (threadIdx.x == 0) s_b = atomicAdd(L.ticket, 1u);
   __syncthreads();
@@ -624,70 +626,65 @@ __global__ void __launch_bounds__(BUCKET_THREADS) bucket_merge_kernel(BucketMerg
       if (sk[ip].x == sk[i].x && sk[ip].y == sk[i].y) {
         head = false;
         const uint32_t mq = sm[ip];
-        bool same = __ldg(C.tn + mq) == nt;
-        const uint32_t *a = C.tl + (size_t)m * tcap, *b = C.tl + (size_t)mq * tcap;
-        for (uint32_t k = 0; same && k < nt; ++k) same = __ldg(a + k) == __ldg(b + k);
-        if (!same) atomicOr(L.err, DEV_ERR_COLLISION);
+        if (__ldg(C.tn + mq) != nt ||
+            !lists_equal(C.tl + (size_t)m * tcap, C.tl + (size_t)mq * tcap, nt))
+          atomicOr(L.err, DEV_ERR_COLLISION);
       }
     }
     sntg[s] = head ? nt : ~0u;
   }
   __syncthreads();
-  // exclusive scan of (heads, targets) over sorted positions: chunk per thread
-  const uint32_t lo = threadIdx.x * CHUNK;
-  uint32_t cc = 0, tt = 0;
-  for (uint32_t s = lo; s < lo + CHUNK && s < n; ++s)
-    if (sntg[s] != ~0u) {
-      ++cc;
-      tt += sntg[s];
-    }
-  sc[threadIdx.x] = cc;
-  st_[threadIdx.x] = tt;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    // warp 0: scan the NT chunk totals (NT/32 per lane), then look back over buckets
-    constexpr int PER = NT / 32;
-    uint32_t lc = 0, lt = 0;
-    for (int x = 0; x < PER; ++x) {
-      lc += sc[threadIdx.x * PER + x];
-      lt += st_[threadIdx.x * PER + x];
-    }
-    uint32_t ic = lc, it = lt;
+  // block-wide exclusive scan of (heads, targets) over sorted positions, NT at a time
+  uint32_t carry_c = 0, carry_t = 0;
+  for (uint32_t r0 = 0; r0 < n; r0 += NT) {
+    const uint32_t s = r0 + threadIdx.x;
+    const uint32_t v = s < n ? sntg[s] : ~0u;
+    const uint32_t c_in = v != ~0u ? 1u : 0u, t_in = v != ~0u ? v : 0u;
+    uint32_t ic = c_in, it = t_in;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
       const uint32_t a = __shfl_up_sync(0xFFFFFFFFu, ic, o), bb = __shfl_up_sync(0xFFFFFFFFu, it, o);
-      if (threadIdx.x >= (uint32_t)o) {
+      if (lane >= (uint32_t)o) {
         ic += a;
         it += bb;
       }
     }
-    uint32_t rc = ic - lc, rt = it - lt;
-    for (int x = 0; x < PER; ++x) {
-      const uint32_t c = sc[threadIdx.x * PER + x], t = st_[threadIdx.x * PER + x];
-      sc[threadIdx.x * PER + x] = rc;
-      st_[threadIdx.x * PER + x] = rt;
-      rc += c;
-      rt += t;
+    if (lane == 31) {
+      wc[warp] = ic;
+      wt[warp] = it;
     }
-    const uint32_t agg_c = __shfl_sync(0xFFFFFFFFu, ic, 31), agg_t = __shfl_sync(0xFFFFFFFFu, it, 31);
+    __syncthreads();
+    uint32_t pc = carry_c, pt = carry_t;
+    for (uint32_t x = 0; x < warp; ++x) {
+      pc += wc[x];
+      pt += wt[x];
+    }
+    if (s < n) sexc[s] = make_uint2(pc + ic - c_in, pt + it - t_in);
+    for (uint32_t x = 0; x < (uint32_t)NW; ++x) {
+      carry_c += wc[x];
+      carry_t += wt[x];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x < 32) {
     uint32_t pc = 0, pt = 0;
-    warp_lookback(L.status, b, agg_c, agg_t, L.err, &pc, &pt);
+    warp_lookback(L.status, b, carry_c, carry_t, L.err, &pc, &pt);
     if (threadIdx.x == 0) {
       s_pre_c = pc;
       s_pre_t = pt;
       if (b == L.nb - 1) {
-        L.totals[0] = pc + agg_c;
-        L.totals[1] = pt + agg_t;
-        if (pt + agg_t > L.tg_cap) atomicOr(L.err, DEV_FLAG_TG_OVF);
+        L.totals[0] = pc + carry_c;
+        L.totals[1] = pt + carry_t;
+        if (pt + carry_t > L.tg_cap) atomicOr(L.err, DEV_FLAG_TG_OVF);
       }
     }
   }
   __syncthreads();
-  uint32_t slot = s_pre_c + sc[threadIdx.x], toff = s_pre_t + st_[threadIdx.x];
-  for (uint32_t s = lo; s < lo + CHUNK && s < n; ++s) {
+  for (uint32_t s = threadIdx.x; s < n; s += NT) {
     const uint32_t ntg = sntg[s];
     if (ntg == ~0u) continue;
-    if (slot >= L.max_groups) break;  // only after a timed-out look-back
+    const uint32_t slot = s_pre_c + sexc[s].x, toff = s_pre_t + sexc[s].y;
+    if (slot >= L.max_groups) continue;  // only after a timed-out look-back
     const uint32_t i = ord[s];
     const uint32_t m = sm[i];
     double p = __ldg(C.mp + m);
@@ -700,21 +697,26 @@ __global__ void __launch_bounds__(BUCKET_THREADS) bucket_merge_kernel(BucketMerg
     L.out_prob[slot] = p;
     L.out_off[slot] = toff;
     if (toff + ntg <= L.tg_cap) {
-      const uint32_t *src = C.tl + (size_t)m * tcap;
-      for (uint32_t k = 0; k < ntg; ++k) L.out_tg[toff + k] = __ldg(src + k);
+      const uint4 *src = reinterpret_cast<const uint4 *>(C.tl + (size_t)m * tcap);
+      for (uint32_t k = 0; k * 4 < ntg; ++k) {
+        const uint4 x = __ldg(src + k);
+        const uint32_t o = toff + k * 4, rem = ntg - k * 4;
+        L.out_tg[o] = x.x;
+        if (rem > 1) L.out_tg[o + 1] = x.y;
+        if (rem > 2) L.out_tg[o + 2] = x.z;
+        if (rem > 3) L.out_tg[o + 3] = x.w;
+      }
     }
-    ++slot;
-    toff += ntg;
   }
 }
 
 }  // namespace
 
 cudaError_t launch_keys(const KeyLaunch &L, cudaStream_t s) {
-  if (L.R == 0) return cudaSuccess;
-  const uint32_t threads = 128;
-  uint32_t blocks = (L.R + threads - 1) / threads;
-  if (blocks > 152u * 32u) blocks = 152u * 32u;
+  if (L.R == 0 || L.M == 0) return cudaSuccess;
+  const uint32_t threads = 256;
+  uint32_t blocks = (L.M + threads - 1) / threads;
+  if (blocks > 152u * 16u) blocks = 152u * 16u;
   key_kernel<<<blocks, threads, (size_t)L.w * sizeof(uint2), s>>>(L);
   return cudaGetLastError();
 }

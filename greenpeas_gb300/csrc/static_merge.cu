@@ -152,6 +152,8 @@ extern "C" gpc_status gpc_merge_mechanisms_static(const uint32_t *num_targets, c
   if (n > kStaticMaxMechanisms) return GPC_ERR_CAPACITY;  // more mechanisms than the static scratch holds
   if (!num_targets || !targets || !probs || !out_probs || !out_offsets || !out_targets || !result || stride == 0)
     return GPC_ERR_INVALID;
+  // target lists are read as 16-byte vectors
+  if (stride % 4 != 0 || (reinterpret_cast<uintptr_t>(targets) & 15u) != 0) return GPC_ERR_INVALID;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || (uint32_t)dev >= kMaxDevices) return GPC_ERR_CUDA;
   char *base;

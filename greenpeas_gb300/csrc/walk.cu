@@ -15,15 +15,18 @@
 //      CTA whether any row is non-zero; once every row is zero and no
 //      measurement of word j remains, the rest of the walk would only see
 //      zeros, so the CTA stops and records the point range it covered;
-//   3. the epoch's ops are read from a shared-memory ring that one thread
-//      fills ahead of time with cp.async.bulk (TMA) copies completing on an
-//      mbarrier; waits are bounded by %globaltimer and report DEV_ERR_TIMEOUT;
+//   3. the epoch's ops are read from shared memory: the tape is cut (on the
+//      host) into chunks of whole epochs, and one thread copies chunk c+1
+//      with a single cp.async.bulk (TMA) into the second of two buffers
+//      while the CTA executes chunk c; a chunk's copy completes on its
+//      buffer's mbarrier, which every thread waits on once per chunk (waits
+//      are bounded by %globaltimer and report DEV_ERR_TIMEOUT);
 //   4. ops: one-qubit Cliffords, two-qubit Cliffords (partner rows from the
 //      published buffer), resets, measurements (XOR in the measurement's bits
 //      that fall in word j; the bits ride in the tape itself), snapshots of
 //      (X, Z) at noise points.
-// The epoch table (slot count and tape offset per epoch) is staged in shared
-// memory at start, so no global load sits on the per-epoch critical path.
+// The epoch and chunk tables are staged in shared memory at start, so no
+// global load sits on the per-epoch critical path.
 #include <cstdint>
 
 #include "device.cuh"
@@ -84,6 +87,18 @@ __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t by
       : "memory");
 }
 
+__device__ __forceinline__ uint64_t lds64(uint32_t a) {
+  uint64_t v;
+  asm volatile("ld.shared.u64 %0, [%1];" : "=l"(v) : "r"(a));
+  return v;
+}
+
+__device__ __forceinline__ ulonglong2 lds128(uint32_t a) {
+  ulonglong2 v;
+  asm volatile("ld.shared.v2.u64 {%0, %1}, [%2];" : "=l"(v.x), "=l"(v.y) : "r"(a));
+  return v;
+}
+
 __device__ __forceinline__ uint64_t sel2(uint32_t m, uint64_t x, uint64_t z) {
   return (x & (0ull - (uint64_t)(m & 1u))) ^ (z & (0ull - (uint64_t)((m >> 1) & 1u)));
 }
@@ -92,12 +107,9 @@ __device__ __forceinline__ uint64_t sel4(uint32_t m, uint64_t a, uint64_t b, uin
   return sel2(m & 3u, a, b) ^ sel2((m >> 2) & 3u, c, d);
 }
 
-constexpr uint32_t kEpochTabMax = 6144;  // epochs whose table is staged in shared memory
-
 template <int QPT>
 __global__ void __launch_bounds__(1024) walk_kernel(const CircuitDev *__restrict__ circs,
-                                                    const uint2 *__restrict__ items, uint32_t ring_slots,
-                                                    uint32_t slot_bytes, uint32_t tab_epochs,
+                                                    const uint2 *__restrict__ items, uint32_t chunk_cap,
                                                     uint32_t *__restrict__ err) {
   extern __shared__ __align__(128) unsigned char smem[];
   const uint2 item = items[blockIdx.x];
@@ -115,43 +127,52 @@ __global__ void __launch_bounds__(1024) walk_kernel(const CircuitDev *__restrict
   }
   const uint32_t elast = C.inj_hi[j];
 
-  ulonglong2 *pub = reinterpret_cast<ulonglong2 *>(smem);  // [2][qpad]
+  // shared memory: [published rows x2][mbarriers][tables][chunk buffer x2]
+  ulonglong2 *pub = reinterpret_cast<ulonglong2 *>(smem);
   size_t off = (size_t)2 * qpad * sizeof(ulonglong2);
-  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + off);  // ring_slots <= 16
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + off);
   off += 128;
-  uint2 *etab = reinterpret_cast<uint2 *>(smem + off);  // (opoff, k) of epochs e0.. (if staged)
-  off += ((size_t)tab_epochs * sizeof(uint2) + 127) / 128 * 128;
-  unsigned char *ring = smem + off;
+  uint2 *etab = reinterpret_cast<uint2 *>(smem + off);  // epoch e0+i: (op offset, slots | chunk << 8)
+  const uint32_t c0 = C.ep_chunk[e0];
+  const uint32_t ne = nE - e0, nc = C.n_chunks - c0;
+  const bool staged = ((size_t)ne + nc) * sizeof(uint2) <= kWalkTableBudget;
+  uint2 *ctab = etab + ne;  // chunk c0+i: (op offset, bytes)
+  off += kWalkTableBudget;
+  unsigned char *buf = smem + off;  // two buffers of chunk_cap bytes
   __shared__ uint32_t s_abort;
 
-  const bool staged = nE - e0 <= tab_epochs;
   if (staged) {
-    for (uint32_t i = tid; i < nE - e0; i += T) etab[i] = make_uint2(C.ep_opoff[e0 + i], C.ep_k[e0 + i]);
+    for (uint32_t i = tid; i < ne; i += T)
+      etab[i] = make_uint2(C.ep_opoff[e0 + i], C.ep_k[e0 + i] | (C.ep_chunk[e0 + i] << 8));
+    for (uint32_t i = tid; i < nc; i += T) ctab[i] = make_uint2(C.ch_off[c0 + i], C.ch_bytes[c0 + i]);
   }
   if (tid == 0) {
     s_abort = 0;
-    for (uint32_t s = 0; s < ring_slots; ++s) mbar_init(&mbar[s], 1);
+    mbar_init(&mbar[0], 1);
+    mbar_init(&mbar[1], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
   auto epoch = [&](uint32_t e) -> uint2 {
-    return staged ? etab[e - e0] : make_uint2(__ldg(C.ep_opoff + e), __ldg(C.ep_k + e));
+    return staged ? etab[e - e0]
+                  : make_uint2(__ldg(C.ep_opoff + e), __ldg(C.ep_k + e) | (__ldg(C.ep_chunk + e) << 8));
   };
-
-  // Producer state (thread 0 only): next epoch to load, sequences issued.
-  uint32_t next_load = e0;
-  uint32_t issued = 0;
-  auto issue = [&](uint32_t seq) {
-    const uint32_t slot = seq % ring_slots;
-    const uint2 ek = epoch(next_load);
-    const uint32_t bytes = ek.y * qpad * (uint32_t)sizeof(uint64_t);
-    mbar_expect_tx(&mbar[slot], bytes);
-    bulk_g2s(ring + (size_t)slot * slot_bytes, C.ops + ek.x, bytes, &mbar[slot]);
-    ++next_load;
+  auto chunk = [&](uint32_t c) -> uint2 {
+    return staged ? ctab[c - c0] : make_uint2(__ldg(C.ch_off + c), __ldg(C.ch_bytes + c));
+  };
+  // Producer (thread 0): chunk c goes to buffer (c - c0) & 1.
+  uint32_t issued = 0;  // chunks c0 .. c0+issued-1 have been issued
+  auto issue = [&]() {
+    const uint32_t c = c0 + issued;
+    const uint2 ck = chunk(c);
+    uint64_t *bar = &mbar[issued & 1u];
+    mbar_expect_tx(bar, ck.y);
+    bulk_g2s(buf + (size_t)(issued & 1u) * chunk_cap, C.ops + ck.x, ck.y, bar);
     ++issued;
   };
   if (tid == 0) {
-    for (uint32_t s = 0; s < ring_slots && next_load < nE; ++s) issue(s);
+    issue();
+    if (nc > 1) issue();
   }
 
   uint64_t X[QPT], Z[QPT], acc[QPT], last_inj[QPT];
@@ -163,14 +184,19 @@ __global__ void __launch_bounds__(1024) walk_kernel(const CircuitDev *__restrict
   bool timed_out = false;
   uint32_t e = e0;
   uint32_t seq = 0;
-  uint32_t consumed = 0;  // sequences whose copy this thread has seen complete
+  uint32_t cur = 0xFFFFFFFFu;  // chunk whose data this thread has waited for
+  uint32_t waited = 0;         // chunks (from c0) whose copy this thread saw complete
+  const unsigned char *cbase = nullptr;
+  uint32_t cbase_off = 0;
+  uint2 ek_next = epoch(e0);
   for (;; ++e, ++seq) {
     // (1) publish rows (the state after epoch e-1)
     ulonglong2 *pb = pub + (size_t)(seq & 1u) * qpad;
     bool nz = false;
 #pragma unroll
     for (int u = 0; u < QPT; ++u) {
-      pb[tid + u * T] = make_ulonglong2(X[u], Z[u]);
+      asm volatile("st.shared.v2.u64 [%0], {%1, %2};" ::"r"(smem_u32(pb + tid + u * T)), "l"(X[u]), "l"(Z[u])
+                   : "memory");
       nz |= (X[u] | Z[u]) != 0;
     }
     if (timed_out) s_abort = 1;
@@ -181,50 +207,62 @@ __global__ void __launch_bounds__(1024) walk_kernel(const CircuitDev *__restrict
       break;
     }
     if ((!any && e > elast) || e >= nE) break;
-    // (3) refill the slot freed by epoch e-1 (every thread finished reading it
-    //     before the barrier above), then wait for epoch e
-    if (tid == 0 && seq > 0 && next_load < nE) issue(issued);
-    const uint32_t slot = seq % ring_slots;
-    const uint32_t K = epoch(e).y;
-    if (!mbar_wait_bounded(&mbar[slot], (seq / ring_slots) & 1u)) {
-      timed_out = true;
-      continue;
+    const uint2 ek = ek_next;
+    if (e + 1 < nE) ek_next = epoch(e + 1);  // used next epoch: its latency hides behind this one
+    const uint32_t K = ek.y & 0xFFu;
+    const uint32_t ch = ek.y >> 8;
+    if (ch != cur) {
+      // (3) first epoch of a chunk: every thread has finished the previous
+      //     chunk (barrier above), so its buffer can take the chunk after this one
+      if (tid == 0 && ch + 1 < C.n_chunks && c0 + issued == ch + 1) issue();
+      const uint32_t i = ch - c0;
+      if (!mbar_wait_bounded(&mbar[i & 1u], (i >> 1) & 1u)) {
+        timed_out = true;
+        continue;
+      }
+      waited = i + 1;
+      cur = ch;
+      cbase = buf + (size_t)(i & 1u) * chunk_cap;
+      cbase_off = chunk(ch).x;
     }
-    ++consumed;
-    const uint64_t *ops = reinterpret_cast<const uint64_t *>(ring + (size_t)slot * slot_bytes);
-    // (4) execute
+    const uint64_t *ops = reinterpret_cast<const uint64_t *>(cbase) + (ek.x - cbase_off);
+    // (4) execute the epoch's ops in order (shared-memory addresses are kept
+    //     as 32-bit shared-window offsets so every load is an ld.shared)
+    const uint32_t ops_s = smem_u32(cbase) + (ek.x - cbase_off) * 8u + tid * 8u;
+    const uint32_t pub_s = smem_u32(pb);
     for (uint32_t k = 0; k < K; ++k) {
 #pragma unroll
       for (int u = 0; u < QPT; ++u) {
-        const uint64_t op = ops[(size_t)k * qpad + tid + u * T];
+        const uint64_t op = lds64(ops_s + (k * qpad + (uint32_t)u * T) * 8u);
         const uint32_t opc = (uint32_t)op & 0xFFu;
         if (opc == OP_NOP) continue;
-        const uint32_t sub = ((uint32_t)op >> 8) & 0xFFu;
         const uint32_t arg = (uint32_t)(op >> 32);
-        switch (opc) {
-          case OP_C1: {
-            const uint64_t x = X[u], z = Z[u];
-            X[u] = sel2(sub & 3u, x, z);
-            Z[u] = sel2(sub >> 2, x, z);
-            break;
-          }
-          case OP_C2: {
-            const ulonglong2 p = pb[arg];
+        if (opc == OP_XPX) {
+          X[u] ^= lds64(pub_s + arg * 16u);
+        } else if (opc == OP_ZPZ) {
+          Z[u] ^= lds64(pub_s + arg * 16u + 8u);
+        } else if (opc == OP_SNAP) {
+          snap_j[arg] = make_ulonglong2(X[u], Z[u]);
+        } else if (opc == OP_XPZ) {
+          X[u] ^= lds64(pub_s + arg * 16u + 8u);
+        } else {
+          const uint32_t sub = ((uint32_t)op >> 8) & 0xFFu;
+          if (opc == OP_C2) {
+            const ulonglong2 p = lds128(pub_s + arg * 16u);
             const uint64_t x = X[u], z = Z[u];
             X[u] = sel4(sub & 15u, x, z, p.x, p.y);
             Z[u] = sel4(sub >> 4, x, z, p.x, p.y);
-            break;
-          }
-          case OP_R:
+          } else if (opc == OP_C1) {
+            const uint64_t x = X[u], z = Z[u];
+            X[u] = sel2(sub & 3u, x, z);
+            Z[u] = sel2(sub >> 2, x, z);
+          } else if (opc == OP_R) {
             X[u] = Z[u] = 0;
-            break;
-          case OP_INJ: {
+          } else if (opc == OP_INJ) {
             const uint32_t b2 = ((uint32_t)op >> 8) & 0xFFFFFFu;
             if (arg - jlo < 64u) acc[u] |= 1ull << (arg - jlo);
             if (b2 != 0xFFFFFFu && b2 - jlo < 64u) acc[u] |= 1ull << (b2 - jlo);
-            break;
-          }
-          case OP_M: {
+          } else if (opc == OP_M) {
             uint64_t inj = acc[u];
             if (arg - jlo < 64u) inj |= 1ull << (arg - jlo);
             acc[u] = 0;
@@ -233,16 +271,9 @@ __global__ void __launch_bounds__(1024) walk_kernel(const CircuitDev *__restrict
             if (basis != 1u) X[u] ^= inj;
             if (basis != 0u) Z[u] ^= inj;
             last_inj[u] = inj;
-            break;
-          }
-          case OP_SNAP:
-            snap_j[arg] = make_ulonglong2(X[u], Z[u]);
-            break;
-          case OP_SNAPD:
+          } else if (opc == OP_SNAPD) {
             snap_j[arg] = make_ulonglong2(last_inj[u], 0ull);
-            break;
-          default:
-            break;
+          }
         }
       }
     }
@@ -251,8 +282,8 @@ __global__ void __launch_bounds__(1024) walk_kernel(const CircuitDev *__restrict
     C.band[j] = make_uint2(C.ep_ptoff[e0], C.ep_ptoff[e < nE ? e : nE]);
     // Copies still in flight target this CTA's shared memory: wait for them
     // (bounded) before the CTA exits.
-    for (uint32_t s = consumed; s < issued; ++s) {
-      if (!mbar_wait_bounded(&mbar[s % ring_slots], (s / ring_slots) & 1u)) {
+    for (uint32_t i = waited; i < issued; ++i) {
+      if (!mbar_wait_bounded(&mbar[i & 1u], (i >> 1) & 1u)) {
         atomicOr(err, DEV_ERR_TIMEOUT);
         break;
       }
@@ -262,22 +293,19 @@ __global__ void __launch_bounds__(1024) walk_kernel(const CircuitDev *__restrict
 
 }  // namespace
 
-size_t walk_smem_bytes(uint32_t qpad, uint32_t ring_slots, uint32_t slot_bytes, uint32_t max_epochs) {
-  const uint32_t tab = max_epochs <= kEpochTabMax ? max_epochs : 0;
-  return (size_t)2 * qpad * sizeof(ulonglong2) + 128 + ((size_t)tab * sizeof(uint2) + 127) / 128 * 128 +
-         (size_t)ring_slots * slot_bytes;
+size_t walk_smem_bytes(uint32_t qpad, uint32_t chunk_cap) {
+  return (size_t)2 * qpad * sizeof(ulonglong2) + 128 + kWalkTableBudget + (size_t)2 * chunk_cap;
 }
 
 cudaError_t launch_walk(const WalkLaunch &L, cudaStream_t s) {
   if (L.n_items == 0) return cudaSuccess;
-  if (L.ring_slots < 1 || L.ring_slots > 16) return cudaErrorInvalidValue;
-  const uint32_t tab = L.max_epochs <= kEpochTabMax ? L.max_epochs : 0;
-  const size_t smem = walk_smem_bytes(L.qpad, L.ring_slots, L.slot_bytes, L.max_epochs);
+  const size_t smem = walk_smem_bytes(L.qpad, L.chunk_cap);
+  if (smem > 227 * 1024) return cudaErrorInvalidValue;
   cudaError_t e;
 #define GPC_WALK(Q)                                                                                      \
   e = cudaFuncSetAttribute(walk_kernel<Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);     \
   if (e != cudaSuccess) return e;                                                                        \
-  walk_kernel<Q><<<L.n_items, L.threads, smem, s>>>(L.circs, L.items, L.ring_slots, L.slot_bytes, tab, L.err)
+  walk_kernel<Q><<<L.n_items, L.threads, smem, s>>>(L.circs, L.items, L.chunk_cap, L.err)
   switch (L.qpt) {
     case 1:
       GPC_WALK(1);

@@ -138,7 +138,8 @@ gpc_status gpc_last_sizes(gpc_driver *driver, uint64_t *raw, uint64_t *points, u
  * for the default stream) on the current device.  All pointers are device
  * memory the caller owns:
  *   num_targets[n], targets[n * stride] (ascending target indices of
- *   mechanism i at targets[i*stride ...]), probs[n]  -- inputs;
+ *   mechanism i at targets[i*stride ...]; stride a multiple of 4 and
+ *   targets 16-byte aligned), probs[n]  -- inputs;
  *   out_probs[n], out_offsets[n + 1], out_targets[out_target_cap]  -- the
  *   merged DEM, as gpc_dem_arrays; result[4] = {errors, targets, flags, 0},
  *   flags != 0 means the output is not valid (1 timeout, 2 hash collision,

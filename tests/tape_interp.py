@@ -11,7 +11,7 @@ from __future__ import annotations
 
 import numpy as np
 
-OP_NOP, OP_C1, OP_C2, OP_R, OP_M, OP_INJ, OP_SNAP, OP_SNAPD = range(8)
+OP_NOP, OP_C1, OP_C2, OP_R, OP_M, OP_INJ, OP_SNAP, OP_SNAPD, OP_XPX, OP_ZPZ, OP_XPZ = range(11)
 # components of each record type as (Pauli a, Pauli b); Pauli 1 X, 2 Z, 3 Y
 _T2 = [(0, 1), (0, 3), (0, 2), (1, 0), (1, 1), (1, 3), (1, 2), (3, 0), (3, 1), (3, 3), (3, 2), (2, 0), (2, 1), (2, 3), (2, 2)]
 REC_COMPS = {
@@ -69,6 +69,12 @@ def walk(t):
                     s = sub[m]
                     X[m] = _sel2(s & 3, x, z) ^ _sel2((s >> 2) & 3, px, pz)
                     Z[m] = _sel2((s >> 4) & 3, x, z) ^ _sel2((s >> 6) & 3, px, pz)
+                m = opc == OP_XPX
+                X[m] ^= pX[arg[m]]
+                m = opc == OP_ZPZ
+                Z[m] ^= pZ[arg[m]]
+                m = opc == OP_XPZ
+                X[m] ^= pZ[arg[m]]
                 m = opc == OP_R
                 X[m] = 0
                 Z[m] = 0
