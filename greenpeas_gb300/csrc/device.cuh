@@ -108,6 +108,38 @@ struct BucketMergeLaunch {
 };
 cudaError_t launch_bucket_merge(const BucketMergeLaunch &L, cudaStream_t s);
 
+// Three-kernel merge of the compile pipeline (no inter-CTA waits):
+//  group: one CTA per bucket sorts its (key, m, p) items, checks collisions,
+//         folds each group's probability and writes per-group records and a
+//         bucket aggregate (groups, targets);
+//  scan:  exclusive scan of the bucket aggregates (one block);
+//  emit:  one CTA per bucket writes its groups' probabilities, offsets and
+//         target lists to the DEM arrays.
+struct GroupLaunch {
+  const CircuitDev *c_dev;
+  const ulonglong2 *bkey;
+  const uint32_t *bm;
+  const double *bp;
+  const uint32_t *count;    // [nb]
+  const uint32_t *offset;   // [nb + 1]
+  uint32_t nb;
+  uint32_t *gm;             // [M] head mechanism of group g of bucket b at offset[b] + g
+  double *gp;               // [M] folded probability
+  uint32_t *gt;             // [M] targets before this group inside its bucket
+  uint2 *bagg;              // [nb] (groups, targets) of each bucket
+  uint2 *bout;              // [nb] exclusive prefix of bagg
+  double *out_prob;
+  uint32_t *out_off;
+  uint32_t *out_tg;
+  uint32_t tg_cap;
+  uint32_t *totals;         // [0] groups, [1] targets
+  uint32_t *err;
+};
+cudaError_t launch_bucket_scatter_p(const ulonglong2 *key, const double *mp, uint32_t M, uint32_t bucket_bits,
+                                    const uint32_t *offset, uint32_t *cursor, ulonglong2 *bkey, uint32_t *bm,
+                                    double *bp, cudaStream_t s);
+cudaError_t launch_group_merge(const GroupLaunch &L, cudaStream_t s);
+
 // ---- global path (used when a bucket is too large for one CTA) -------------
 // Onesweep radix sort of (u64 key, u32 value) pairs on the low `bits` bits.
 struct SortScratch {

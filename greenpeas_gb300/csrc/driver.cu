@@ -99,7 +99,7 @@ struct HostBuf {
 struct Layout {
   size_t ops, ep_opoff, ep_k, ep_ptoff, ep_chunk, ch_off, ch_bytes, inj_lo, inj_hi, rec, rec_p, rec_moff, cdev, items;
   size_t in_bytes;
-  size_t snap, band, mdesc, mp, tl, tn, key, boff, bkey, bm;
+  size_t snap, band, mdesc, mp, tl, tn, key, boff, bkey, bm, bp, gm, gp, gt, bagg, bout;
   size_t sk0, sk1, pm0, pm1, hik;  // global path
   size_t zero, err, totals, bcount, bcursor, bstatus, bticket, zero_bytes;
   size_t gzero, sort_scr, merge_status, merge_ctr, gzero_bytes;  // global path scratch
@@ -203,6 +203,12 @@ struct gpc_driver {
     L.boff = take((size_t)(L.nb + 1) * 4);
     L.bkey = take((size_t)M * 16);
     L.bm = take((size_t)M * 4);
+    L.bp = take((size_t)M * 8);
+    L.gm = take((size_t)M * 4);
+    L.gp = take((size_t)M * 8);
+    L.gt = take((size_t)M * 4);
+    L.bagg = take((size_t)L.nb * 8);
+    L.bout = take((size_t)L.nb * 8);
     L.zero = o;
     L.err = take(4);
     L.totals = take(16);
@@ -354,9 +360,9 @@ struct gpc_driver {
       run_global(false);
     } else {
       CK(gpc::launch_bucket_scan(dptr<uint32_t>(L.bcount), dptr<uint32_t>(L.boff), L.nb, stream));
-      CK(gpc::launch_bucket_scatter(dptr<ulonglong2>(L.key), T.M, L.bucket_bits, dptr<uint32_t>(L.boff),
-                                    dptr<uint32_t>(L.bcursor), dptr<ulonglong2>(L.bkey), dptr<uint32_t>(L.bm),
-                                    stream));
+      CK(gpc::launch_bucket_scatter_p(dptr<ulonglong2>(L.key), dptr<double>(L.mp), T.M, L.bucket_bits,
+                                      dptr<uint32_t>(L.boff), dptr<uint32_t>(L.bcursor), dptr<ulonglong2>(L.bkey),
+                                      dptr<uint32_t>(L.bm), dptr<double>(L.bp), stream));
       CK(cudaEventRecord(ev[3], stream));
       launch_bucket_merge_now();
       CK(cudaEventRecord(ev[4], stream));
@@ -365,24 +371,26 @@ struct gpc_driver {
   }
 
   void launch_bucket_merge_now() {
-    gpc::BucketMergeLaunch bl{};
-    bl.c_dev = dptr<CircuitDev>(L.cdev);
-    bl.w = tape.w;
-    bl.bkey = dptr<ulonglong2>(L.bkey);
-    bl.bm = dptr<uint32_t>(L.bm);
-    bl.count = dptr<uint32_t>(L.bcount);
-    bl.offset = dptr<uint32_t>(L.boff);
-    bl.nb = L.nb;
-    bl.max_groups = tape.M;
-    bl.out_prob = dptr<double>(L.out_prob);
-    bl.out_off = dptr<uint32_t>(L.out_off);
-    bl.out_tg = static_cast<uint32_t *>(tgbuf.p);
-    bl.tg_cap = tg_cap;
-    bl.status = dptr<unsigned long long>(L.bstatus);
-    bl.ticket = dptr<uint32_t>(L.bticket);
-    bl.totals = dptr<uint32_t>(L.totals);
-    bl.err = dptr<uint32_t>(L.err);
-    CK(gpc::launch_bucket_merge(bl, stream));
+    gpc::GroupLaunch gl{};
+    gl.c_dev = dptr<CircuitDev>(L.cdev);
+    gl.bkey = dptr<ulonglong2>(L.bkey);
+    gl.bm = dptr<uint32_t>(L.bm);
+    gl.bp = dptr<double>(L.bp);
+    gl.count = dptr<uint32_t>(L.bcount);
+    gl.offset = dptr<uint32_t>(L.boff);
+    gl.nb = L.nb;
+    gl.gm = dptr<uint32_t>(L.gm);
+    gl.gp = dptr<double>(L.gp);
+    gl.gt = dptr<uint32_t>(L.gt);
+    gl.bagg = dptr<uint2>(L.bagg);
+    gl.bout = dptr<uint2>(L.bout);
+    gl.out_prob = dptr<double>(L.out_prob);
+    gl.out_off = dptr<uint32_t>(L.out_off);
+    gl.out_tg = static_cast<uint32_t *>(tgbuf.p);
+    gl.tg_cap = tg_cap;
+    gl.totals = dptr<uint32_t>(L.totals);
+    gl.err = dptr<uint32_t>(L.err);
+    CK(gpc::launch_group_merge(gl, stream));
   }
 
   // Global path: sort every mechanism (on sort_bits, or all 128 bits) and merge.
@@ -506,9 +514,6 @@ struct gpc_driver {
           reset_merge_scratch();
           launch_merge_now();
         } else {
-          CK(cudaMemsetAsync(dptr<char>(L.bstatus), 0, (size_t)L.nb * 8, stream));
-          CK(cudaMemsetAsync(dptr<char>(L.bticket), 0, 4, stream));
-          CK(cudaMemsetAsync(dptr<char>(L.totals), 0, 8, stream));
           launch_bucket_merge_now();
         }
         continue;

@@ -202,6 +202,21 @@ __global__ void bucket_scatter_kernel(const ulonglong2 *__restrict__ key, uint32
   }
 }
 
+__global__ void bucket_scatter_p_kernel(const ulonglong2 *__restrict__ key, const double *__restrict__ mp,
+                                        uint32_t M, uint32_t shift, const uint32_t *__restrict__ offset,
+                                        uint32_t *__restrict__ cursor, ulonglong2 *__restrict__ bkey,
+                                        uint32_t *__restrict__ bm, double *__restrict__ bp) {
+  for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
+    const ulonglong2 k = key[m];
+    if ((k.x | k.y) == 0) continue;
+    const uint32_t b = (uint32_t)(k.x >> shift);
+    const uint32_t pos = offset[b] + atomicAdd(cursor + b, 1u);
+    bkey[pos] = k;
+    bm[pos] = m;
+    bp[pos] = mp[m];
+  }
+}
+
 __global__ void sort_init_kernel(const ulonglong2 *__restrict__ key, uint64_t *__restrict__ sortkey,
                                  uint32_t *__restrict__ perm, uint32_t M) {
   for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
@@ -710,6 +725,179 @@ __global__ void __launch_bounds__(BUCKET_THREADS) bucket_merge_kernel(BucketMerg
   }
 }
 
+// ---- three-kernel merge -----------------------------------------------------
+
+__global__ void __launch_bounds__(BUCKET_THREADS) group_kernel(GroupLaunch L) {
+  constexpr int NT = BUCKET_THREADS;
+  constexpr int NW = NT / 32;
+  __shared__ ulonglong2 sk[BUCKET_CAP];
+  __shared__ uint32_t sm[BUCKET_CAP];
+  __shared__ double sp[BUCKET_CAP];
+  __shared__ uint16_t ord[BUCKET_CAP];
+  __shared__ uint32_t sntg[BUCKET_CAP];  // targets of a group head at a sorted position, else ~0u
+  __shared__ uint32_t wc[NW], wt[NW];
+  const CircuitDev C = *L.c_dev;
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t b = blockIdx.x;
+  uint32_t n = L.count[b];
+  const uint32_t base = L.offset[b];
+  if (n > (uint32_t)BUCKET_CAP) {
+    if (threadIdx.x == 0) atomicOr(L.err, DEV_FLAG_BIG_BUCKET);
+    n = 0;
+  }
+  for (uint32_t i = threadIdx.x; i < n; i += NT) {
+    sk[i] = L.bkey[base + i];
+    sm[i] = L.bm[base + i];
+    sp[i] = L.bp[base + i];
+  }
+  __syncthreads();
+  // rank sort by (key, m), four comparisons per step
+  for (uint32_t i = threadIdx.x; i < n; i += NT) {
+    const ulonglong2 ki = sk[i];
+    const uint32_t mi = sm[i];
+    uint32_t r = 0;
+    uint32_t k = 0;
+    for (; k + 4 <= n; k += 4) {
+      r += item_less(sk[k], sm[k], ki, mi) ? 1u : 0u;
+      r += item_less(sk[k + 1], sm[k + 1], ki, mi) ? 1u : 0u;
+      r += item_less(sk[k + 2], sm[k + 2], ki, mi) ? 1u : 0u;
+      r += item_less(sk[k + 3], sm[k + 3], ki, mi) ? 1u : 0u;
+    }
+    for (; k < n; ++k) r += item_less(sk[k], sm[k], ki, mi) ? 1u : 0u;
+    ord[r] = (uint16_t)i;
+  }
+  __syncthreads();
+  // group heads, collision checks (full target lists), target counts
+  const uint32_t tcap = C.tcap;
+  for (uint32_t s = threadIdx.x; s < n; s += NT) {
+    const uint32_t i = ord[s];
+    const uint32_t m = sm[i];
+    const uint32_t nt = __ldg(C.tn + m);
+    bool head = true;
+    if (s > 0) {
+      const uint32_t ip = ord[s - 1];
+      if (sk[ip].x == sk[i].x && sk[ip].y == sk[i].y) {
+        head = false;
+        const uint32_t mq = sm[ip];
+        if (__ldg(C.tn + mq) != nt || !lists_equal(C.tl + (size_t)m * tcap, C.tl + (size_t)mq * tcap, nt))
+          atomicOr(L.err, DEV_ERR_COLLISION);
+      }
+    }
+    sntg[s] = head ? nt : ~0u;
+  }
+  __syncthreads();
+  // compact the heads (block scan over sorted positions, NT at a time) and
+  // write one record per group; fold the run's probabilities left to right
+  uint32_t carry_c = 0, carry_t = 0;
+  for (uint32_t r0 = 0; r0 < n; r0 += NT) {
+    const uint32_t s = r0 + threadIdx.x;
+    const uint32_t v = s < n ? sntg[s] : ~0u;
+    const uint32_t c_in = v != ~0u ? 1u : 0u, t_in = v != ~0u ? v : 0u;
+    uint32_t ic = c_in, it = t_in;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t a = __shfl_up_sync(0xFFFFFFFFu, ic, o), bb = __shfl_up_sync(0xFFFFFFFFu, it, o);
+      if (lane >= (uint32_t)o) {
+        ic += a;
+        it += bb;
+      }
+    }
+    if (lane == 31) {
+      wc[warp] = ic;
+      wt[warp] = it;
+    }
+    __syncthreads();
+    uint32_t pc = carry_c, pt = carry_t;
+    for (uint32_t x = 0; x < warp; ++x) {
+      pc += wc[x];
+      pt += wt[x];
+    }
+    if (c_in) {
+      const uint32_t g = pc + ic - 1;
+      const uint32_t i = ord[s];
+      double p = sp[i];
+      for (uint32_t s2 = s + 1; s2 < n; ++s2) {
+        const uint32_t i2 = ord[s2];
+        if (sk[i2].x != sk[i].x || sk[i2].y != sk[i].y) break;
+        const double q = sp[i2];
+        p = p * (1.0 - q) + q * (1.0 - p);
+      }
+      L.gm[base + g] = sm[i];
+      L.gp[base + g] = p;
+      L.gt[base + g] = pt + it - t_in;
+    }
+    for (uint32_t x = 0; x < (uint32_t)NW; ++x) {
+      carry_c += wc[x];
+      carry_t += wt[x];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) L.bagg[b] = make_uint2(carry_c, carry_t);
+}
+
+// Exclusive scan of the nb bucket aggregates (one block of 1024 threads).
+__global__ void __launch_bounds__(1024) group_scan_kernel(GroupLaunch L) {
+  __shared__ uint32_t pc[1024], pt[1024];
+  const uint32_t t = threadIdx.x, nb = L.nb;
+  const uint32_t per = (nb + 1023) / 1024;
+  const uint32_t lo = min(nb, t * per), hi = min(nb, lo + per);
+  uint32_t c = 0, g = 0;
+  for (uint32_t i = lo; i < hi; ++i) {
+    const uint2 a = L.bagg[i];
+    c += a.x;
+    g += a.y;
+  }
+  pc[t] = c;
+  pt[t] = g;
+  __syncthreads();
+  for (uint32_t off = 1; off < 1024; off <<= 1) {
+    const uint32_t a = t >= off ? pc[t - off] : 0, b = t >= off ? pt[t - off] : 0;
+    __syncthreads();
+    pc[t] += a;
+    pt[t] += b;
+    __syncthreads();
+  }
+  uint32_t rc = pc[t] - c, rt = pt[t] - g;
+  for (uint32_t i = lo; i < hi; ++i) {
+    const uint2 a = L.bagg[i];
+    L.bout[i] = make_uint2(rc, rt);
+    rc += a.x;
+    rt += a.y;
+  }
+  if (t == 1023) {
+    L.totals[0] = pc[1023];
+    L.totals[1] = pt[1023];
+    if (pt[1023] > L.tg_cap) atomicOr(L.err, DEV_FLAG_TG_OVF);
+  }
+}
+
+__global__ void __launch_bounds__(BUCKET_THREADS) emit_kernel(GroupLaunch L) {
+  const uint32_t b = blockIdx.x;
+  const uint2 agg = L.bagg[b], out = L.bout[b];
+  const uint32_t base = L.offset[b];
+  const CircuitDev C = *L.c_dev;
+  const uint32_t tcap = C.tcap;
+  for (uint32_t g = threadIdx.x; g < agg.x; g += BUCKET_THREADS) {
+    const uint32_t slot = out.x + g;
+    const uint32_t toff = out.y + L.gt[base + g];
+    const uint32_t m = L.gm[base + g];
+    L.out_prob[slot] = L.gp[base + g];
+    L.out_off[slot] = toff;
+    const uint32_t ntg = __ldg(C.tn + m);
+    if (toff + ntg <= L.tg_cap) {
+      const uint4 *src = reinterpret_cast<const uint4 *>(C.tl + (size_t)m * tcap);
+      for (uint32_t k = 0; k * 4 < ntg; ++k) {
+        const uint4 x = __ldg(src + k);
+        const uint32_t o = toff + k * 4, rem = ntg - k * 4;
+        L.out_tg[o] = x.x;
+        if (rem > 1) L.out_tg[o + 1] = x.y;
+        if (rem > 2) L.out_tg[o + 2] = x.z;
+        if (rem > 3) L.out_tg[o + 3] = x.w;
+      }
+    }
+  }
+}
+
 }  // namespace
 
 cudaError_t launch_keys(const KeyLaunch &L, cudaStream_t s) {
@@ -732,6 +920,24 @@ cudaError_t launch_bucket_scatter(const ulonglong2 *key, uint32_t M, uint32_t bu
   uint32_t blocks = (M + 255) / 256;
   if (blocks > 152u * 16u) blocks = 152u * 16u;
   bucket_scatter_kernel<<<blocks, 256, 0, s>>>(key, M, 64u - bucket_bits, offset, cursor, bkey, bm);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_bucket_scatter_p(const ulonglong2 *key, const double *mp, uint32_t M, uint32_t bucket_bits,
+                                    const uint32_t *offset, uint32_t *cursor, ulonglong2 *bkey, uint32_t *bm,
+                                    double *bp, cudaStream_t s) {
+  if (M == 0) return cudaSuccess;
+  uint32_t blocks = (M + 255) / 256;
+  if (blocks > 152u * 16u) blocks = 152u * 16u;
+  bucket_scatter_p_kernel<<<blocks, 256, 0, s>>>(key, mp, M, 64u - bucket_bits, offset, cursor, bkey, bm, bp);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_group_merge(const GroupLaunch &L, cudaStream_t s) {
+  if (L.nb == 0) return cudaSuccess;
+  group_kernel<<<L.nb, BUCKET_THREADS, 0, s>>>(L);
+  group_scan_kernel<<<1, 1024, 0, s>>>(L);
+  emit_kernel<<<L.nb, BUCKET_THREADS, 0, s>>>(L);
   return cudaGetLastError();
 }
 
