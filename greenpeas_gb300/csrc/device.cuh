@@ -65,6 +65,7 @@ struct WalkLaunch {
   uint32_t *err;
 };
 cudaError_t launch_walk(const WalkLaunch &L, cudaStream_t s);
+cudaError_t walk_set_smem_limit();  // call once per device before launching walks
 size_t walk_smem_bytes(uint32_t qpad, uint32_t chunk_cap);
 
 // Key kernel: one thread per noise record; expands the record into its

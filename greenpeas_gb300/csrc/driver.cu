@@ -143,13 +143,32 @@ struct gpc_driver {
   uint64_t sort_mask = ~0ull;
   uint32_t threads = 32, qpt = 1;
   bool force_global = false;  // debug/test option: skip the bucket path
+  cudaGraph_t graph = nullptr;         // captured kernel sequence of run() for one launch configuration
+  cudaGraphExec_t graph_exec = nullptr;
+  bool use_graph = true;
+  uint64_t cfg_sig = 0, graph_sig = 0, last_run_sig = 0;
   uint32_t tcap = 32;         // target-list stride (grows when a symptom is longer)
   bool lists_off = false;     // symptoms too long for target lists: merge from snapshots
   uint64_t last_d2h = 0;      // bytes copied device -> host by the last fetch
   bool used_global = false;
 
+  bool capturing = false;
+  // Records timing event i on the stream (as a graph event node while capturing).
+  void rec(int i) {
+    if (capturing) CK(cudaEventRecordWithFlags(ev[i], stream, cudaEventRecordExternal));
+    else CK(cudaEventRecord(ev[i], stream));
+  }
+
+  void drop_graph() {
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    if (graph) cudaGraphDestroy(graph);
+    graph_exec = nullptr;
+    graph = nullptr;
+  }
+
   ~gpc_driver() {
     if (stream) cudaStreamSynchronize(stream);
+    drop_graph();
     arena.release();
     tgbuf.release();
     pin_in.release();
@@ -320,15 +339,56 @@ struct gpc_driver {
     // walk launch geometry
     qpt = tape.qpad <= 1024 ? 1 : tape.qpad <= 2048 ? 2 : 4;
     threads = tape.qpad / qpt;
+    // what the captured graph depends on: buffer addresses and launch sizes
+    const uint64_t parts[] = {(uint64_t)(uintptr_t)arena.p, (uint64_t)(uintptr_t)tgbuf.p, tg_cap, L.total,
+                              L.nb, tape.M, tape.rec.size(), tape.w, tape.qpad, tape.n_epochs, tape.chunk_cap,
+                              tcap, (uint64_t)force_global, (uint64_t)lists_off};
+    uint64_t h = 0xcbf29ce484222325ull;
+    for (uint64_t v : parts) h = (h ^ v) * 0x100000001b3ull;
+    cfg_sig = h;
     prepared = true;
   }
 
+  // Runs the pipeline: from a CUDA graph of the kernel sequence when it can
+  // (captured once per prepared circuit), else by direct launches.
   void run() {
     if (!prepared) throw gpc::Error(GPC_ERR_INVALID, "no circuit prepared");
     CK(cudaSetDevice(device));
+    used_global = false;
+    // capture once the same configuration runs a second time in a row
+    const bool graphable = use_graph && !force_global && !lists_off &&
+                           ((graph_exec && graph_sig == cfg_sig) || last_run_sig == cfg_sig);
+    last_run_sig = cfg_sig;
+    if (graphable && graph_sig != cfg_sig) drop_graph();
+    if (graphable && !graph_exec) {
+      CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+      capturing = true;
+      try {
+        enqueue();
+      } catch (...) {
+        capturing = false;
+        cudaGraph_t g = nullptr;
+        cudaStreamEndCapture(stream, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+      }
+      capturing = false;
+      CK(cudaStreamEndCapture(stream, &graph));
+      CK(cudaGraphInstantiate(&graph_exec, graph, 0));
+      graph_sig = cfg_sig;
+    }
+    if (graphable) {
+      CK(cudaGraphLaunch(graph_exec, stream));
+    } else {
+      enqueue();
+    }
+    ran = true;
+  }
+
+  void enqueue() {
     const Tape &T = tape;
     CK(cudaMemsetAsync(dptr<char>(L.zero), 0, L.zero_bytes, stream));
-    CK(cudaEventRecord(ev[0], stream));
+    rec(0);
     gpc::WalkLaunch wl{};
     wl.circs = dptr<CircuitDev>(L.cdev);
     wl.items = dptr<uint2>(L.items);
@@ -342,7 +402,7 @@ struct gpc_driver {
     wl.err = dptr<uint32_t>(L.err);
     if (T.n_epochs > 0) CK(gpc::launch_walk(wl, stream));
     else CK(cudaMemsetAsync(dptr<char>(L.band), 0, (size_t)T.w * 8, stream));
-    CK(cudaEventRecord(ev[1], stream));
+    rec(1);
     gpc::KeyLaunch kl{};
     kl.c_dev = dptr<CircuitDev>(L.cdev);
     kl.R = (uint32_t)T.rec.size();
@@ -354,8 +414,7 @@ struct gpc_driver {
     kl.list_total = dptr<uint32_t>(L.totals) + 2;
     kl.err = dptr<uint32_t>(L.err);
     CK(gpc::launch_keys(kl, stream));
-    CK(cudaEventRecord(ev[2], stream));
-    used_global = false;
+    rec(2);
     if (force_global || lists_off) {
       run_global(false);
     } else {
@@ -363,11 +422,10 @@ struct gpc_driver {
       CK(gpc::launch_bucket_scatter_p(dptr<ulonglong2>(L.key), dptr<double>(L.mp), T.M, L.bucket_bits,
                                       dptr<uint32_t>(L.boff), dptr<uint32_t>(L.bcursor), dptr<ulonglong2>(L.bkey),
                                       dptr<uint32_t>(L.bm), dptr<double>(L.bp), stream));
-      CK(cudaEventRecord(ev[3], stream));
+      rec(3);
       launch_bucket_merge_now();
-      CK(cudaEventRecord(ev[4], stream));
+      rec(4);
     }
-    ran = true;
   }
 
   void launch_bucket_merge_now() {
@@ -433,9 +491,9 @@ struct gpc_driver {
     sk_sorted = ks;
     const uint32_t b = full ? 0 : sort_bits;
     sort_mask = b == 0 ? 0ull : (b >= 64 ? ~0ull : ((1ull << b) - 1));
-    CK(cudaEventRecord(ev[3], stream));
+    rec(3);
     launch_merge_now();
-    CK(cudaEventRecord(ev[4], stream));
+    rec(4);
   }
 
   void launch_merge_now() {
@@ -633,6 +691,7 @@ gpc_status gpc_get_driver(const char *stim_text, size_t len, int32_t correlation
     if (d->device < 0 || d->device >= n) throw gpc::Error(GPC_ERR_CUDA, "no such CUDA device");
     CK(cudaSetDevice(d->device));
     CK(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking));
+    CK(gpc::walk_set_smem_limit());  // per device: the driver's device is current here
     for (auto &e : d->ev) CK(cudaEventCreate(&e));
     d->prepare(stim_text, len);
   });

@@ -128,7 +128,7 @@ struct LowerOptions {
 
 // Shared-memory plan of the walk kernel (bytes): double-buffered tape chunks,
 // the published rows, and the epoch/chunk tables when they fit.
-constexpr uint32_t kWalkSmemBudget = 224 * 1024;
+constexpr uint32_t kWalkSmemBudget = 224 * 1024;  // of 227 KiB per CTA, leaving room for static shared memory
 constexpr uint32_t kWalkTableBudget = 32 * 1024;
 constexpr uint32_t kWalkChunkMax = 96 * 1024;
 inline uint32_t walk_chunk_cap(uint32_t qpad) {

@@ -297,15 +297,32 @@ size_t walk_smem_bytes(uint32_t qpad, uint32_t chunk_cap) {
   return (size_t)2 * qpad * sizeof(ulonglong2) + 128 + kWalkTableBudget + (size_t)2 * chunk_cap;
 }
 
+// Raises the dynamic shared-memory limit of the walk kernels once (not a
+// stream operation, so it is done here rather than inside a graph capture).
+template <int QPT>
+cudaError_t walk_set_limit_one(int optin) {
+  cudaFuncAttributes a{};
+  cudaError_t e = cudaFuncGetAttributes(&a, walk_kernel<QPT>);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(walk_kernel<QPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              optin - (int)a.sharedSizeBytes);
+}
+
+cudaError_t walk_set_smem_limit() {
+  int dev = 0, optin = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e == cudaSuccess) e = walk_set_limit_one<1>(optin);
+  if (e == cudaSuccess) e = walk_set_limit_one<2>(optin);
+  if (e == cudaSuccess) e = walk_set_limit_one<4>(optin);
+  return e;
+}
+
 cudaError_t launch_walk(const WalkLaunch &L, cudaStream_t s) {
   if (L.n_items == 0) return cudaSuccess;
   const size_t smem = walk_smem_bytes(L.qpad, L.chunk_cap);
-  if (smem > 227 * 1024) return cudaErrorInvalidValue;
-  cudaError_t e;
-#define GPC_WALK(Q)                                                                                      \
-  e = cudaFuncSetAttribute(walk_kernel<Q>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);     \
-  if (e != cudaSuccess) return e;                                                                        \
-  walk_kernel<Q><<<L.n_items, L.threads, smem, s>>>(L.circs, L.items, L.chunk_cap, L.err)
+  if (smem > 227 * 1024 - 1024) return cudaErrorInvalidValue;
+#define GPC_WALK(Q) walk_kernel<Q><<<L.n_items, L.threads, smem, s>>>(L.circs, L.items, L.chunk_cap, L.err)
   switch (L.qpt) {
     case 1:
       GPC_WALK(1);
