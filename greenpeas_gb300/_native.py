@@ -25,7 +25,7 @@ EXPORTS = [
     "gpc_dem_text", "gpc_dem_free", "gpc_driver_destroy", "gpc_last_error", "gpc_prepare",
     "gpc_run_device", "gpc_fetch", "gpc_driver_stream", "gpc_last_timings", "gpc_last_sizes",
     "gpc_tape_lower", "gpc_tape_get_view", "gpc_tape_free", "gpc_tape_last_error", "gpc_last_traffic",
-    "gpc_last_io_bytes", "gpc_merge_mechanisms_static",
+    "gpc_last_io_bytes", "gpc_merge_mechanisms_static", "gpc_prepare_batch", "gpc_fetch_batch",
 ]
 
 
@@ -92,6 +92,8 @@ def lib() -> ctypes.CDLL:
     L.gpc_last_traffic.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
     L.gpc_last_io_bytes.argtypes = [vp, u64p, u64p]
     L.gpc_merge_mechanisms_static.argtypes = [vp, vp, u32, vp, u32, vp, vp, vp, u32, vp, vp]
+    L.gpc_prepare_batch.argtypes = [vp, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(sz), i32]
+    L.gpc_fetch_batch.argtypes = [vp, ctypes.POINTER(vp), i32]
     L.gpc_tape_lower.argtypes = [ctypes.c_char_p, sz, i32, ctypes.POINTER(vp)]
     L.gpc_tape_get_view.argtypes = [vp, ctypes.POINTER(TapeView)]
     L.gpc_tape_free.argtypes = [vp]
@@ -100,7 +102,7 @@ def lib() -> ctypes.CDLL:
     for f in ("gpc_get_driver", "gpc_compile", "gpc_compile_batch", "gpc_dem_arrays", "gpc_dem_info",
               "gpc_dem_text", "gpc_prepare", "gpc_run_device", "gpc_fetch", "gpc_last_timings",
               "gpc_last_sizes", "gpc_tape_lower", "gpc_tape_get_view", "gpc_last_traffic", "gpc_last_io_bytes",
-              "gpc_merge_mechanisms_static"):
+              "gpc_merge_mechanisms_static", "gpc_prepare_batch", "gpc_fetch_batch"):
         getattr(L, f).restype = i32
     _lib = L
     return L

@@ -40,7 +40,23 @@ struct CircuitDev {
   uint32_t npoints, M, R;
   uint32_t tcap;              // stride of tl (0: no target lists, merge from snapshots)
   uint32_t n_chunks, chunk_cap;
+  uint32_t mbase;             // first mechanism of this circuit in the batch-wide arrays
+  uint32_t bbase, bbits;      // first bucket of this circuit, log2 of its bucket count
+  uint32_t pad_;
 };
+
+constexpr uint32_t kMaxCircuitsStaged = 2048;  // batch tables staged in shared memory up to this size
+
+// Index of the circuit holding item x: the last c with base[c] <= x (base has n+1 entries).
+__device__ __forceinline__ uint32_t find_circuit(const uint32_t *base, uint32_t n, uint32_t x) {
+  uint32_t lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (base[mid] <= x) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
 
 constexpr int SORT_THREADS = 256;
 constexpr int SORT_IPT = 8;
@@ -72,11 +88,11 @@ size_t walk_smem_bytes(uint32_t qpad, uint32_t chunk_cap);
 // mechanisms (mdesc, mp), computes each mechanism's 128-bit key, and counts
 // non-empty keys per bucket (top `bucket_bits` bits of key.x).
 struct KeyLaunch {
-  const CircuitDev *c_dev;
-  uint32_t R, M, w;
+  const CircuitDev *circs;  // [n_circ]
+  const uint32_t *mbase;    // [n_circ + 1] first mechanism of each circuit (+ total)
+  uint32_t n_circ, M;       // circuits, mechanisms of the whole batch
   ulonglong2 *key;          // [M]
-  uint32_t *bucket_count;   // [1 << bucket_bits] (zeroed)
-  uint32_t bucket_bits;
+  uint32_t *bucket_count;   // [buckets of the batch] (zeroed)
   uint32_t *list_total;     // += targets written to the lists (for traffic accounting)
   uint32_t *err;
 };
@@ -117,7 +133,9 @@ cudaError_t launch_bucket_merge(const BucketMergeLaunch &L, cudaStream_t s);
 //  emit:  one CTA per bucket writes its groups' probabilities, offsets and
 //         target lists to the DEM arrays.
 struct GroupLaunch {
-  const CircuitDev *c_dev;
+  const uint32_t *tl;       // [M][tcap] batch-wide target lists
+  const uint32_t *tn;       // [M]
+  uint32_t tcap;
   const ulonglong2 *bkey;
   const uint32_t *bm;
   const double *bp;
@@ -134,11 +152,15 @@ struct GroupLaunch {
   uint32_t *out_tg;
   uint32_t tg_cap;
   uint32_t *totals;         // [0] groups, [1] targets
+  const uint32_t *cbbase;   // [n_circ] first bucket of each circuit
+  uint32_t n_circ;
+  uint2 *cout;              // [n_circ] (first slot, first target) of each circuit's output
   uint32_t *err;
 };
-cudaError_t launch_bucket_scatter_p(const ulonglong2 *key, const double *mp, uint32_t M, uint32_t bucket_bits,
-                                    const uint32_t *offset, uint32_t *cursor, ulonglong2 *bkey, uint32_t *bm,
-                                    double *bp, cudaStream_t s);
+// Batch-wide scatter: the bucket of mechanism m is its circuit's bbase + top bits.
+cudaError_t launch_bucket_scatter_p(const CircuitDev *circs, const uint32_t *mbase, uint32_t n_circ,
+                                    const ulonglong2 *key, const double *mp, uint32_t M, const uint32_t *offset,
+                                    uint32_t *cursor, ulonglong2 *bkey, uint32_t *bm, double *bp, cudaStream_t s);
 cudaError_t launch_group_merge(const GroupLaunch &L, cudaStream_t s);
 
 // ---- global path (used when a bucket is too large for one CTA) -------------

@@ -8,6 +8,9 @@
 // mechanisms (the reference copies the whole node x 32 class matrix,
 // Driver.hpp:158-161).
 #include <algorithm>
+#include <atomic>
+#include <exception>
+#include <thread>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -94,19 +97,34 @@ struct HostBuf {
   }
 };
 
+// Byte offsets of one circuit's input arrays inside the arena.
+struct CircLayout {
+  size_t ops, ep_opoff, ep_k, ep_ptoff, ep_chunk, ch_off, ch_bytes, inj_lo, inj_hi, rec, rec_p, rec_moff;
+  size_t snap, band;
+  uint32_t mbase, bbase, bbits;
+};
+
+// One walk launch: circuits with the same thread count.
+struct WalkClass {
+  uint32_t qpad, item0, n_items, chunk_cap, max_epochs, max_chunks;
+};
+
 // Byte offsets of every array inside the arena (inputs first, so the whole
 // input region is one contiguous H2D copy).
 struct Layout {
-  size_t ops, ep_opoff, ep_k, ep_ptoff, ep_chunk, ch_off, ch_bytes, inj_lo, inj_hi, rec, rec_p, rec_moff, cdev, items;
+  std::vector<CircLayout> c;
+  size_t cdev, items, mbase, cbbase;
   size_t in_bytes;
-  size_t snap, band, mdesc, mp, tl, tn, key, boff, bkey, bm, bp, gm, gp, gt, bagg, bout;
-  size_t sk0, sk1, pm0, pm1, hik;  // global path
-  size_t zero, err, totals, bcount, bcursor, bstatus, bticket, zero_bytes;
-  size_t gzero, sort_scr, merge_status, merge_ctr, gzero_bytes;  // global path scratch
+  size_t mdesc, mp, tl, tn, key, boff, bkey, bm, bp, gm, gp, gt, bagg, bout, cout;
+  size_t zero, err, totals, bcount, bcursor, zero_bytes;
+  size_t sk0, sk1, pm0, pm1, hik;  // global path (single circuit)
+  size_t gzero, sort_scr, merge_status, merge_ctr, gzero_bytes;
   size_t out_prob, out_off;
   size_t total;
-  uint32_t sort_tiles, merge_tiles, nb, bucket_bits;
+  uint32_t M, nb, n_items;
+  uint32_t sort_tiles, merge_tiles;
   size_t sort_words;
+  std::vector<WalkClass> classes;
 };
 
 }  // namespace
@@ -126,8 +144,11 @@ struct gpc_driver {
   int level = 2;
   uint32_t sort_bits = 64;
   cudaStream_t stream = nullptr;
-  gpc::Parsed parsed;
-  Tape tape;
+  static constexpr int kAux = 4;
+  cudaStream_t aux[kAux] = {};
+  cudaEvent_t fork_ev = nullptr, join_ev[kAux] = {};
+  std::vector<gpc::Parsed> parsed;
+  std::vector<Tape> tapes;
   bool have_tape = false;
   bool prepared = false;
   bool ran = false;
@@ -136,23 +157,22 @@ struct gpc_driver {
   HostBuf pin_in, pin_out;
   uint32_t tg_cap = 0;
   cudaEvent_t ev[5] = {};
-  float timings[5] = {};
-  // last run's sort result
+  // last run's global-path sort result
   uint32_t *perm_sorted = nullptr;
   uint64_t *sk_sorted = nullptr;
   uint64_t sort_mask = ~0ull;
-  uint32_t threads = 32, qpt = 1;
-  bool force_global = false;  // debug/test option: skip the bucket path
-  cudaGraph_t graph = nullptr;         // captured kernel sequence of run() for one launch configuration
+  bool force_global = false;  // test option: skip the bucket path (single circuits)
+  cudaGraph_t graph = nullptr;  // captured kernel sequence of run() for one launch configuration
   cudaGraphExec_t graph_exec = nullptr;
   bool use_graph = true;
   uint64_t cfg_sig = 0, graph_sig = 0, last_run_sig = 0;
-  uint32_t tcap = 32;         // target-list stride (grows when a symptom is longer)
-  bool lists_off = false;     // symptoms too long for target lists: merge from snapshots
-  uint64_t last_d2h = 0;      // bytes copied device -> host by the last fetch
+  uint32_t tcap = 32;      // target-list stride (grows when a symptom is longer)
+  bool lists_off = false;  // symptoms too long for target lists: merge from snapshots
+  uint64_t last_d2h = 0;   // bytes copied device -> host by the last fetch
   bool used_global = false;
-
   bool capturing = false;
+  uint32_t ncirc() const { return (uint32_t)tapes.size(); }
+
   // Records timing event i on the stream (as a graph event node while capturing).
   void rec(int i) {
     if (capturing) CK(cudaEventRecordWithFlags(ev[i], stream, cudaEventRecordExternal));
@@ -164,6 +184,7 @@ struct gpc_driver {
     if (graph) cudaGraphDestroy(graph);
     graph_exec = nullptr;
     graph = nullptr;
+    graph_sig = 0;
   }
 
   ~gpc_driver() {
@@ -175,7 +196,20 @@ struct gpc_driver {
     pin_out.release();
     for (auto &e : ev)
       if (e) cudaEventDestroy(e);
+    if (fork_ev) cudaEventDestroy(fork_ev);
+    for (auto &e : join_ev)
+      if (e) cudaEventDestroy(e);
+    for (auto &a : aux)
+      if (a) cudaStreamDestroy(a);
     if (stream) cudaStreamDestroy(stream);
+  }
+
+  void init_streams() {
+    CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    for (auto &a : aux) CK(cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking));
+    for (auto &e : ev) CK(cudaEventCreate(&e));
+    CK(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
+    for (auto &e : join_ev) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
   }
 
   template <typename T>
@@ -184,142 +218,230 @@ struct gpc_driver {
   }
 
   void layout() {
-    const Tape &T = tape;
-    const uint32_t M = T.M, R = (uint32_t)T.rec.size();
+    const uint32_t N = ncirc();
     size_t o = 0;
     auto take = [&](size_t bytes) {
       size_t r = o;
       o = align256(o + bytes);
       return r;
     };
-    L.ops = take(T.ops.size() * 8);
-    L.ep_opoff = take(T.ep_opoff.size() * 4);
-    L.ep_k = take(T.ep_k.size() * 4);
-    L.ep_ptoff = take(T.ep_ptoff.size() * 4);
-    L.ep_chunk = take(T.ep_chunk.size() * 4);
-    L.ch_off = take(T.ch_off.size() * 4);
-    L.ch_bytes = take(T.ch_bytes.size() * 4);
-    L.inj_lo = take(T.inj_lo.size() * 4);
-    L.inj_hi = take(T.inj_hi.size() * 4);
-    L.rec = take((size_t)R * 8);
-    L.rec_p = take((size_t)R * 8);
-    L.rec_moff = take((size_t)(R + 1) * 4);
-    L.cdev = take(sizeof(CircuitDev));
-    L.items = take((size_t)T.w * sizeof(uint2));
+    L.c.assign(N, CircLayout{});
+    uint64_t M = 0, nb = 0, items = 0;
+    for (uint32_t i = 0; i < N; ++i) {
+      const Tape &T = tapes[i];
+      CircLayout &c = L.c[i];
+      c.ops = take(T.ops.size() * 8);
+      c.ep_opoff = take(T.ep_opoff.size() * 4);
+      c.ep_k = take(T.ep_k.size() * 4);
+      c.ep_ptoff = take(T.ep_ptoff.size() * 4);
+      c.ep_chunk = take(T.ep_chunk.size() * 4);
+      c.ch_off = take(T.ch_off.size() * 4);
+      c.ch_bytes = take(T.ch_bytes.size() * 4);
+      c.inj_lo = take(T.inj_lo.size() * 4);
+      c.inj_hi = take(T.inj_hi.size() * 4);
+      c.rec = take(T.rec.size() * 8);
+      c.rec_p = take(T.rec_p.size() * 8);
+      c.rec_moff = take(T.rec_moff.size() * 4);
+      // buckets: about 96 mechanisms each, a power of two between 2^4 and 2^16
+      uint32_t bb = 4;
+      while (bb < 16 && ((uint64_t)96 << bb) < T.M) ++bb;
+      c.mbase = (uint32_t)M;
+      c.bbase = (uint32_t)nb;
+      c.bbits = bb;
+      M += T.M;
+      nb += 1ull << bb;
+      items += T.w;
+    }
+    if (M >= 0xFFFFFFF0ull || nb >= 0x7FFFFFFFull) throw gpc::Error(GPC_ERR_CAPACITY, "batch too large");
+    L.M = (uint32_t)M;
+    L.nb = (uint32_t)nb;
+    L.n_items = (uint32_t)items;
+    L.cdev = take((size_t)N * sizeof(CircuitDev));
+    L.items = take((size_t)items * sizeof(uint2));
+    L.mbase = take((size_t)(N + 1) * 4);
+    L.cbbase = take((size_t)N * 4);
     L.in_bytes = o;
-    // buckets: about 96 mechanisms each, a power of two between 2^4 and 2^16
-    uint32_t bb = 4;
-    while (bb < 16 && ((uint64_t)96 << bb) < M) ++bb;
-    L.bucket_bits = bb;
-    L.nb = 1u << bb;
-    L.snap = take((size_t)T.w * T.npoints * 16);
-    L.band = take((size_t)T.w * 8);
+    for (uint32_t i = 0; i < N; ++i) {
+      L.c[i].snap = take((size_t)tapes[i].w * tapes[i].npoints * 16);
+      L.c[i].band = take((size_t)tapes[i].w * 8);
+    }
     L.mdesc = take((size_t)M * 8);
     L.mp = take((size_t)M * 8);
     L.tl = take((size_t)M * tcap * 4);
     L.tn = take((size_t)M * 4);
     L.key = take((size_t)M * 16);
-    L.boff = take((size_t)(L.nb + 1) * 4);
+    L.boff = take((size_t)(nb + 1) * 4);
     L.bkey = take((size_t)M * 16);
     L.bm = take((size_t)M * 4);
     L.bp = take((size_t)M * 8);
     L.gm = take((size_t)M * 4);
     L.gp = take((size_t)M * 8);
     L.gt = take((size_t)M * 4);
-    L.bagg = take((size_t)L.nb * 8);
-    L.bout = take((size_t)L.nb * 8);
+    L.bagg = take((size_t)nb * 8);
+    L.bout = take((size_t)nb * 8);
+    L.cout = take((size_t)N * 8);
     L.zero = o;
     L.err = take(4);
     L.totals = take(16);
-    L.bcount = take((size_t)L.nb * 4);
-    L.bcursor = take((size_t)L.nb * 4);
-    L.bstatus = take((size_t)L.nb * 8);
-    L.bticket = take(4);
+    L.bcount = take((size_t)nb * 4);
+    L.bcursor = take((size_t)nb * 4);
     L.zero_bytes = o - L.zero;
     L.out_prob = take((size_t)M * 8);
     L.out_off = take((size_t)(M + 1) * 4);
-    // global path (only touched when a bucket overflows or it is forced)
-    L.sk0 = take((size_t)M * 8);
-    L.sk1 = take((size_t)M * 8);
-    L.pm0 = take((size_t)M * 4);
-    L.pm1 = take((size_t)M * 4);
-    L.hik = take((size_t)M * 8);
-    L.sort_tiles = gpc::sort_tiles(M);
-    L.merge_tiles = gpc::merge_tiles(M);
-    L.sort_words = gpc::sort_scratch_words(M, 64);
+    // global path (single circuit only)
+    const uint32_t Mg = N == 1 ? (uint32_t)M : 0;
+    L.sk0 = take((size_t)Mg * 8);
+    L.sk1 = take((size_t)Mg * 8);
+    L.pm0 = take((size_t)Mg * 4);
+    L.pm1 = take((size_t)Mg * 4);
+    L.hik = take((size_t)Mg * 8);
+    L.sort_tiles = gpc::sort_tiles(Mg);
+    L.merge_tiles = gpc::merge_tiles(Mg);
+    L.sort_words = Mg ? gpc::sort_scratch_words(Mg, 64) : 0;
     L.gzero = o;
     L.sort_scr = take(L.sort_words * 4);
     L.merge_status = take((size_t)L.merge_tiles * 8);
     L.merge_ctr = take(4);
     L.gzero_bytes = o - L.gzero;
     L.total = o;
+    // walk classes: circuits with the same qpad share a launch
+    std::vector<uint32_t> order(N);
+    for (uint32_t i = 0; i < N; ++i) order[i] = i;
+    std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return tapes[a].qpad < tapes[b].qpad; });
+    L.classes.clear();
+    item_order = order;
+    uint32_t item = 0;
+    for (uint32_t k = 0; k < N;) {
+      uint32_t e = k;
+      WalkClass wc{tapes[order[k]].qpad, item, 0, 0, 0, 0};
+      while (e < N && tapes[order[e]].qpad == wc.qpad) {
+        const Tape &T = tapes[order[e]];
+        wc.n_items += T.w;
+        wc.chunk_cap = std::max(wc.chunk_cap, T.chunk_cap);
+        wc.max_epochs = std::max(wc.max_epochs, T.n_epochs);
+        wc.max_chunks = std::max(wc.max_chunks, (uint32_t)T.ch_off.size());
+        ++e;
+      }
+      item += wc.n_items;
+      L.classes.push_back(wc);
+      k = e;
+    }
   }
+  std::vector<uint32_t> item_order;  // circuits in walk-class order
 
   void stage_inputs() {
-    const Tape &T = tape;
+    const uint32_t N = ncirc();
     pin_in.ensure(L.in_bytes);
     char *h = static_cast<char *>(pin_in.p);
     auto put = [&](size_t off, const void *src, size_t bytes) {
       if (bytes) memcpy(h + off, src, bytes);
     };
-    put(L.ops, T.ops.data(), T.ops.size() * 8);
-    put(L.ep_opoff, T.ep_opoff.data(), T.ep_opoff.size() * 4);
-    put(L.ep_k, T.ep_k.data(), T.ep_k.size() * 4);
-    put(L.ep_ptoff, T.ep_ptoff.data(), T.ep_ptoff.size() * 4);
-    put(L.ep_chunk, T.ep_chunk.data(), T.ep_chunk.size() * 4);
-    put(L.ch_off, T.ch_off.data(), T.ch_off.size() * 4);
-    put(L.ch_bytes, T.ch_bytes.data(), T.ch_bytes.size() * 4);
-    put(L.inj_lo, T.inj_lo.data(), T.inj_lo.size() * 4);
-    put(L.inj_hi, T.inj_hi.data(), T.inj_hi.size() * 4);
-    put(L.rec, T.rec.data(), T.rec.size() * 8);
-    put(L.rec_p, T.rec_p.data(), T.rec_p.size() * 8);
-    put(L.rec_moff, T.rec_moff.data(), T.rec_moff.size() * 4);
-    CircuitDev c{};
-    c.ops = dptr<uint64_t>(L.ops);
-    c.ep_opoff = dptr<uint32_t>(L.ep_opoff);
-    c.ep_k = dptr<uint32_t>(L.ep_k);
-    c.ep_ptoff = dptr<uint32_t>(L.ep_ptoff);
-    c.ep_chunk = dptr<uint32_t>(L.ep_chunk);
-    c.ch_off = dptr<uint32_t>(L.ch_off);
-    c.ch_bytes = dptr<uint32_t>(L.ch_bytes);
-    c.inj_lo = dptr<uint32_t>(L.inj_lo);
-    c.inj_hi = dptr<uint32_t>(L.inj_hi);
-    c.snap = dptr<ulonglong2>(L.snap);
-    c.band = dptr<uint2>(L.band);
-    c.rec = dptr<uint64_t>(L.rec);
-    c.rec_p = dptr<double>(L.rec_p);
-    c.rec_moff = dptr<uint32_t>(L.rec_moff);
-    c.mdesc = dptr<uint64_t>(L.mdesc);
-    c.mp = dptr<double>(L.mp);
-    c.tl = dptr<uint32_t>(L.tl);
-    c.tn = dptr<uint32_t>(L.tn);
-    c.tcap = tcap;
-    c.nq = T.nq;
-    c.qpad = T.qpad;
-    c.n_epochs = T.n_epochs;
-    c.w = T.w;
-    c.npoints = T.npoints;
-    c.M = T.M;
-    c.R = (uint32_t)T.rec.size();
-    c.n_chunks = (uint32_t)T.ch_off.size();
-    c.chunk_cap = T.chunk_cap;
-    put(L.cdev, &c, sizeof(c));
-    std::vector<uint2> items(T.w);
-    for (uint32_t j = 0; j < T.w; ++j) items[j] = make_uint2(0u, j);
+    std::vector<CircuitDev> cd(N);
+    std::vector<uint32_t> mb(N + 1), cb(N);
+    for (uint32_t i = 0; i < N; ++i) {
+      const Tape &T = tapes[i];
+      const CircLayout &l = L.c[i];
+      put(l.ops, T.ops.data(), T.ops.size() * 8);
+      put(l.ep_opoff, T.ep_opoff.data(), T.ep_opoff.size() * 4);
+      put(l.ep_k, T.ep_k.data(), T.ep_k.size() * 4);
+      put(l.ep_ptoff, T.ep_ptoff.data(), T.ep_ptoff.size() * 4);
+      put(l.ep_chunk, T.ep_chunk.data(), T.ep_chunk.size() * 4);
+      put(l.ch_off, T.ch_off.data(), T.ch_off.size() * 4);
+      put(l.ch_bytes, T.ch_bytes.data(), T.ch_bytes.size() * 4);
+      put(l.inj_lo, T.inj_lo.data(), T.inj_lo.size() * 4);
+      put(l.inj_hi, T.inj_hi.data(), T.inj_hi.size() * 4);
+      put(l.rec, T.rec.data(), T.rec.size() * 8);
+      put(l.rec_p, T.rec_p.data(), T.rec_p.size() * 8);
+      put(l.rec_moff, T.rec_moff.data(), T.rec_moff.size() * 4);
+      CircuitDev &c = cd[i];
+      c = CircuitDev{};
+      c.ops = dptr<uint64_t>(l.ops);
+      c.ep_opoff = dptr<uint32_t>(l.ep_opoff);
+      c.ep_k = dptr<uint32_t>(l.ep_k);
+      c.ep_ptoff = dptr<uint32_t>(l.ep_ptoff);
+      c.ep_chunk = dptr<uint32_t>(l.ep_chunk);
+      c.ch_off = dptr<uint32_t>(l.ch_off);
+      c.ch_bytes = dptr<uint32_t>(l.ch_bytes);
+      c.inj_lo = dptr<uint32_t>(l.inj_lo);
+      c.inj_hi = dptr<uint32_t>(l.inj_hi);
+      c.snap = dptr<ulonglong2>(l.snap);
+      c.band = dptr<uint2>(l.band);
+      c.rec = dptr<uint64_t>(l.rec);
+      c.rec_p = dptr<double>(l.rec_p);
+      c.rec_moff = dptr<uint32_t>(l.rec_moff);
+      c.mdesc = dptr<uint64_t>(L.mdesc) + l.mbase;
+      c.mp = dptr<double>(L.mp) + l.mbase;
+      c.tl = dptr<uint32_t>(L.tl) + (size_t)l.mbase * tcap;
+      c.tn = dptr<uint32_t>(L.tn) + l.mbase;
+      c.tcap = tcap;
+      c.nq = T.nq;
+      c.qpad = T.qpad;
+      c.n_epochs = T.n_epochs;
+      c.w = T.w;
+      c.npoints = T.npoints;
+      c.M = T.M;
+      c.R = (uint32_t)T.rec.size();
+      c.n_chunks = (uint32_t)T.ch_off.size();
+      c.chunk_cap = T.chunk_cap;
+      c.mbase = l.mbase;
+      c.bbase = l.bbase;
+      c.bbits = l.bbits;
+      mb[i] = l.mbase;
+      cb[i] = l.bbase;
+    }
+    mb[N] = L.M;
+    put(L.cdev, cd.data(), cd.size() * sizeof(CircuitDev));
+    put(L.mbase, mb.data(), mb.size() * 4);
+    put(L.cbbase, cb.data(), cb.size() * 4);
+    std::vector<uint2> items;
+    items.reserve(L.n_items);
+    for (uint32_t i : item_order)
+      for (uint32_t j = 0; j < tapes[i].w; ++j) items.push_back(make_uint2(i, j));
     put(L.items, items.data(), items.size() * sizeof(uint2));
   }
 
-  void prepare(const char *text, size_t len) {
+  // Parses and lowers circuits (in parallel on host threads for batches).
+  void lower_all(const char *const *texts, const size_t *lens, uint32_t n) {
+    std::vector<gpc::Parsed> P(n);
+    std::vector<Tape> T(n);
+    gpc::LowerOptions lo;
+    lo.level = level;
+    auto one = [&](uint32_t i) {
+      P[i] = gpc::parse_stim(texts[i], lens[i]);
+      T[i] = gpc::lower(P[i], lo);
+    };
+    if (n == 1) {
+      one(0);
+    } else {
+      const uint32_t nt = std::max(1u, std::min<uint32_t>(n, std::thread::hardware_concurrency()));
+      std::vector<std::thread> th;
+      std::vector<std::exception_ptr> errs(nt);
+      std::atomic<uint32_t> next{0};
+      for (uint32_t t = 0; t < nt; ++t)
+        th.emplace_back([&, t] {
+          try {
+            for (uint32_t i; (i = next.fetch_add(1)) < n;) one(i);
+          } catch (...) {
+            errs[t] = std::current_exception();
+          }
+        });
+      for (auto &x : th) x.join();
+      for (auto &e : errs)
+        if (e) std::rethrow_exception(e);
+    }
+    parsed = std::move(P);
+    tapes = std::move(T);
+  }
+
+  void prepare(const char *const *texts, const size_t *lens, uint32_t n) {
     CK(cudaSetDevice(device));
     prepared = false;
     ran = false;
-    if (text) {
+    if (texts) {
+      if (n == 0) throw gpc::Error(GPC_ERR_INVALID, "empty batch");
       tcap = 32;
       lists_off = false;
-      parsed = gpc::parse_stim(text, len);
-      gpc::LowerOptions lo;
-      lo.level = level;
-      tape = gpc::lower(parsed, lo);
+      lower_all(texts, lens, n);
       have_tape = true;
     } else if (!have_tape) {
       throw gpc::Error(GPC_ERR_INVALID, "no circuit to compile");
@@ -328,36 +450,43 @@ struct gpc_driver {
     // The stream may still be reading the old arena: finish before regrowing.
     CK(cudaStreamSynchronize(stream));
     arena.ensure(L.total);
-    const uint32_t M = tape.M;
-    uint32_t want_tg = std::max<uint32_t>(1024u, std::min<uint64_t>(0xFFFFFFF0ull, (uint64_t)M * 16));
+    uint32_t want_tg = std::max<uint32_t>(1024u, (uint32_t)std::min<uint64_t>(0xFFFFFFF0ull, (uint64_t)L.M * 16));
     if (want_tg > tg_cap) {
       tgbuf.ensure((size_t)want_tg * 4);
       tg_cap = want_tg;
     }
     stage_inputs();
     CK(cudaMemcpyAsync(arena.p, pin_in.p, L.in_bytes, cudaMemcpyHostToDevice, stream));
-    // walk launch geometry
-    qpt = tape.qpad <= 1024 ? 1 : tape.qpad <= 2048 ? 2 : 4;
-    threads = tape.qpad / qpt;
-    // what the captured graph depends on: buffer addresses and launch sizes
-    const uint64_t parts[] = {(uint64_t)(uintptr_t)arena.p, (uint64_t)(uintptr_t)tgbuf.p, tg_cap, L.total,
-                              L.nb, tape.M, tape.rec.size(), tape.w, tape.qpad, tape.n_epochs, tape.chunk_cap,
-                              tcap, (uint64_t)force_global, (uint64_t)lists_off};
+    // what a captured graph depends on: buffer addresses and launch sizes
     uint64_t h = 0xcbf29ce484222325ull;
-    for (uint64_t v : parts) h = (h ^ v) * 0x100000001b3ull;
+    auto mix = [&](uint64_t v) { h = (h ^ v) * 0x100000001b3ull; };
+    mix((uint64_t)(uintptr_t)arena.p);
+    mix((uint64_t)(uintptr_t)tgbuf.p);
+    mix(tg_cap);
+    mix(L.total);
+    mix(L.nb);
+    mix(L.M);
+    mix(tcap);
+    mix((uint64_t)force_global);
+    mix((uint64_t)lists_off);
+    for (const auto &c : L.classes) {
+      mix(c.qpad);
+      mix(c.n_items);
+      mix(c.chunk_cap);
+    }
     cfg_sig = h;
     prepared = true;
   }
 
   // Runs the pipeline: from a CUDA graph of the kernel sequence when it can
-  // (captured once per prepared circuit), else by direct launches.
+  // (captured once a launch configuration runs twice in a row), else directly.
   void run() {
     if (!prepared) throw gpc::Error(GPC_ERR_INVALID, "no circuit prepared");
     CK(cudaSetDevice(device));
     used_global = false;
-    // capture once the same configuration runs a second time in a row
-    const bool graphable = use_graph && !force_global && !lists_off &&
-                           ((graph_exec && graph_sig == cfg_sig) || last_run_sig == cfg_sig);
+    const bool single_global = ncirc() == 1 && (force_global || lists_off);
+    const bool graphable =
+        use_graph && !single_global && ((graph_exec && graph_sig == cfg_sig) || last_run_sig == cfg_sig);
     last_run_sig = cfg_sig;
     if (graphable && graph_sig != cfg_sig) drop_graph();
     if (graphable && !graph_exec) {
@@ -377,51 +506,68 @@ struct gpc_driver {
       CK(cudaGraphInstantiate(&graph_exec, graph, 0));
       graph_sig = cfg_sig;
     }
-    if (graphable) {
-      CK(cudaGraphLaunch(graph_exec, stream));
-    } else {
-      enqueue();
-    }
+    if (graphable) CK(cudaGraphLaunch(graph_exec, stream));
+    else enqueue();
     ran = true;
   }
 
+  void launch_walks() {
+    const uint32_t nc = (uint32_t)L.classes.size();
+    auto one = [&](const WalkClass &wc, cudaStream_t s) {
+      gpc::WalkLaunch wl{};
+      wl.circs = dptr<CircuitDev>(L.cdev);
+      wl.items = dptr<uint2>(L.items) + wc.item0;
+      wl.n_items = wc.n_items;
+      wl.qpt = wc.qpad <= 1024 ? 1 : wc.qpad <= 2048 ? 2 : 4;
+      wl.threads = wc.qpad / wl.qpt;
+      wl.qpad = wc.qpad;
+      wl.chunk_cap = wc.chunk_cap;
+      wl.max_epochs = wc.max_epochs;
+      wl.max_chunks = wc.max_chunks;
+      wl.err = dptr<uint32_t>(L.err);
+      CK(gpc::launch_walk(wl, s));
+    };
+    if (nc <= 1) {
+      if (nc == 1) one(L.classes[0], stream);
+      return;
+    }
+    // fork: each class on an auxiliary stream, joined back into the main stream
+    CK(cudaEventRecord(fork_ev, stream));
+    const uint32_t used = std::min<uint32_t>(nc, kAux);
+    for (uint32_t a = 0; a < used; ++a) CK(cudaStreamWaitEvent(aux[a], fork_ev, 0));
+    for (uint32_t k = 0; k < nc; ++k) one(L.classes[k], aux[k % kAux]);
+    for (uint32_t a = 0; a < used; ++a) {
+      CK(cudaEventRecord(join_ev[a], aux[a]));
+      CK(cudaStreamWaitEvent(stream, join_ev[a], 0));
+    }
+  }
+
   void enqueue() {
-    const Tape &T = tape;
     CK(cudaMemsetAsync(dptr<char>(L.zero), 0, L.zero_bytes, stream));
+    for (uint32_t i = 0; i < ncirc(); ++i)
+      if (tapes[i].n_epochs == 0) CK(cudaMemsetAsync(dptr<char>(L.c[i].band), 0, (size_t)tapes[i].w * 8, stream));
     rec(0);
-    gpc::WalkLaunch wl{};
-    wl.circs = dptr<CircuitDev>(L.cdev);
-    wl.items = dptr<uint2>(L.items);
-    wl.n_items = T.w;
-    wl.threads = threads;
-    wl.qpt = qpt;
-    wl.qpad = T.qpad;
-    wl.chunk_cap = T.chunk_cap;
-    wl.max_epochs = T.n_epochs;
-    wl.max_chunks = (uint32_t)T.ch_off.size();
-    wl.err = dptr<uint32_t>(L.err);
-    if (T.n_epochs > 0) CK(gpc::launch_walk(wl, stream));
-    else CK(cudaMemsetAsync(dptr<char>(L.band), 0, (size_t)T.w * 8, stream));
+    launch_walks();
     rec(1);
     gpc::KeyLaunch kl{};
-    kl.c_dev = dptr<CircuitDev>(L.cdev);
-    kl.R = (uint32_t)T.rec.size();
-    kl.M = T.M;
-    kl.w = T.w;
+    kl.circs = dptr<CircuitDev>(L.cdev);
+    kl.mbase = dptr<uint32_t>(L.mbase);
+    kl.n_circ = ncirc();
+    kl.M = L.M;
     kl.key = dptr<ulonglong2>(L.key);
     kl.bucket_count = dptr<uint32_t>(L.bcount);
-    kl.bucket_bits = L.bucket_bits;
     kl.list_total = dptr<uint32_t>(L.totals) + 2;
     kl.err = dptr<uint32_t>(L.err);
     CK(gpc::launch_keys(kl, stream));
     rec(2);
-    if (force_global || lists_off) {
+    if (ncirc() == 1 && (force_global || lists_off)) {
       run_global(false);
     } else {
       CK(gpc::launch_bucket_scan(dptr<uint32_t>(L.bcount), dptr<uint32_t>(L.boff), L.nb, stream));
-      CK(gpc::launch_bucket_scatter_p(dptr<ulonglong2>(L.key), dptr<double>(L.mp), T.M, L.bucket_bits,
-                                      dptr<uint32_t>(L.boff), dptr<uint32_t>(L.bcursor), dptr<ulonglong2>(L.bkey),
-                                      dptr<uint32_t>(L.bm), dptr<double>(L.bp), stream));
+      CK(gpc::launch_bucket_scatter_p(dptr<CircuitDev>(L.cdev), dptr<uint32_t>(L.mbase), ncirc(),
+                                      dptr<ulonglong2>(L.key), dptr<double>(L.mp), L.M, dptr<uint32_t>(L.boff),
+                                      dptr<uint32_t>(L.bcursor), dptr<ulonglong2>(L.bkey), dptr<uint32_t>(L.bm),
+                                      dptr<double>(L.bp), stream));
       rec(3);
       launch_bucket_merge_now();
       rec(4);
@@ -430,7 +576,9 @@ struct gpc_driver {
 
   void launch_bucket_merge_now() {
     gpc::GroupLaunch gl{};
-    gl.c_dev = dptr<CircuitDev>(L.cdev);
+    gl.tl = dptr<uint32_t>(L.tl);
+    gl.tn = dptr<uint32_t>(L.tn);
+    gl.tcap = tcap;
     gl.bkey = dptr<ulonglong2>(L.bkey);
     gl.bm = dptr<uint32_t>(L.bm);
     gl.bp = dptr<double>(L.bp);
@@ -447,22 +595,25 @@ struct gpc_driver {
     gl.out_tg = static_cast<uint32_t *>(tgbuf.p);
     gl.tg_cap = tg_cap;
     gl.totals = dptr<uint32_t>(L.totals);
+    gl.cbbase = dptr<uint32_t>(L.cbbase);
+    gl.n_circ = ncirc();
+    gl.cout = dptr<uint2>(L.cout);
     gl.err = dptr<uint32_t>(L.err);
     CK(gpc::launch_group_merge(gl, stream));
   }
 
-  // Global path: sort every mechanism (on sort_bits, or all 128 bits) and merge.
+  // Global path (single circuit): sort every mechanism (on sort_bits, or all
+  // 128 bits) and merge from the snapshots.
   void run_global(bool full) {
     used_global = true;
     CK(cudaMemsetAsync(dptr<char>(L.gzero), 0, L.gzero_bytes, stream));
     CK(cudaMemsetAsync(dptr<char>(L.totals), 0, 8, stream));
-    CK(gpc::launch_sort_init(dptr<ulonglong2>(L.key), dptr<uint64_t>(L.sk0), dptr<uint32_t>(L.pm0), tape.M, stream));
+    CK(gpc::launch_sort_init(dptr<ulonglong2>(L.key), dptr<uint64_t>(L.sk0), dptr<uint32_t>(L.pm0), L.M, stream));
     sort_and_merge(full);
   }
 
-  // Sorts (on sort_bits, or on the full 128-bit key when `full`) and merges.
   void sort_and_merge(bool full) {
-    const uint32_t M = tape.M;
+    const uint32_t M = L.M;
     uint32_t *sw = dptr<uint32_t>(L.sort_scr);
     const uint32_t passes = 8;
     const size_t one = (size_t)passes * gpc::RADIX + (size_t)passes * L.sort_tiles * gpc::RADIX + passes;
@@ -497,15 +648,14 @@ struct gpc_driver {
   }
 
   void launch_merge_now() {
-    const uint32_t M = tape.M;
     gpc::MergeLaunch ml{};
     ml.c_dev = dptr<CircuitDev>(L.cdev);
-    ml.w = tape.w;
+    ml.w = tapes[0].w;
     ml.perm = perm_sorted;
     ml.sortkey = sk_sorted;
     ml.sort_mask = sort_mask;
     ml.key = dptr<ulonglong2>(L.key);
-    ml.n = M;
+    ml.n = L.M;
     ml.out_prob = dptr<double>(L.out_prob);
     ml.out_off = dptr<uint32_t>(L.out_off);
     ml.out_tg = static_cast<uint32_t *>(tgbuf.p);
@@ -523,13 +673,15 @@ struct gpc_driver {
     CK(cudaMemsetAsync(dptr<char>(L.totals), 0, 8, stream));
   }
 
+  enum class Finish { Ok, BatchFallback };
+
   // Reads flags and totals; handles the rare fallbacks (bucket overflow,
-  // short sort keys, target-buffer growth).
-  void finish(uint32_t *groups, uint32_t *targets) {
+  // long symptoms, short sort keys, target-buffer growth).
+  Finish finish(uint32_t *groups, uint32_t *targets) {
     pin_out.ensure(64);
     uint32_t *h = static_cast<uint32_t *>(pin_out.p);
     bool did_full = false;
-    for (int attempt = 0; attempt < 6; ++attempt) {
+    for (int attempt = 0; attempt < 8; ++attempt) {
       CK(cudaMemcpyAsync(h, dptr<char>(L.err), 4, cudaMemcpyDeviceToHost, stream));
       CK(cudaMemcpyAsync(h + 1, dptr<char>(L.totals), 8, cudaMemcpyDeviceToHost, stream));
       CK(cudaStreamSynchronize(stream));
@@ -537,16 +689,18 @@ struct gpc_driver {
       if (err & gpc::DEV_ERR_TIMEOUT) throw gpc::Error(GPC_ERR_TIMEOUT, "a bounded device wait timed out");
       if (err & gpc::DEV_ERR_COLLISION)
         throw gpc::Error(GPC_ERR_COLLISION, "two different symptoms share a 128-bit key");
+      if ((err & (gpc::DEV_FLAG_LONG | gpc::DEV_FLAG_BIG_BUCKET)) && !used_global && ncirc() > 1)
+        return Finish::BatchFallback;  // compile the batch's circuits one by one
       if ((err & gpc::DEV_FLAG_LONG) && !used_global) {
-        // a symptom longer than the target-list stride: widen it (or give up on
-        // lists and merge from the snapshots) and run again
+        // a symptom longer than the target-list stride: widen it (or merge from
+        // the snapshots) and run again
         if (tcap < 256) {
           tcap *= 4;
         } else {
           tcap = 0;
           lists_off = true;
         }
-        prepare(nullptr, 0);
+        prepare(nullptr, nullptr, 0);
         run();
         continue;
       }
@@ -567,6 +721,7 @@ struct gpc_driver {
         const uint32_t need = h[2];
         tgbuf.ensure((size_t)need * 4 + 1024);
         tg_cap = (uint32_t)std::min<size_t>(0xFFFFFFF0ull, tgbuf.cap / 4);
+        drop_graph();  // the target buffer moved
         CK(cudaMemsetAsync(dptr<char>(L.err), 0, 4, stream));
         if (used_global) {
           reset_merge_scratch();
@@ -576,11 +731,10 @@ struct gpc_driver {
         }
         continue;
       }
-      const uint32_t M = tape.M;
-      if (h[1] > M || h[2] > tg_cap) throw gpc::Error(GPC_ERR_CUDA, "inconsistent merge totals");
+      if (h[1] > L.M || h[2] > tg_cap) throw gpc::Error(GPC_ERR_CUDA, "inconsistent merge totals");
       *groups = h[1];
       *targets = h[2];
-      return;
+      return Finish::Ok;
     }
     throw gpc::Error(GPC_ERR_CUDA, "merge did not converge");
   }
@@ -588,60 +742,116 @@ struct gpc_driver {
   // Algorithmic bytes of each kernel of the last run (walk, key, bucket scan+scatter,
   // merge): what the design must move, counted from the run's own sizes.
   void traffic(double out[4]) {
-    const Tape &T = tape;
     CK(cudaStreamSynchronize(stream));
-    std::vector<uint2> band(T.w);
     uint32_t tot[4] = {0, 0, 0, 0};
     uint32_t nonempty = 0;
-    CK(cudaMemcpy(band.data(), dptr<char>(L.band), (size_t)T.w * 8, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(tot, dptr<char>(L.totals), 12, cudaMemcpyDeviceToHost));
     CK(cudaMemcpy(&nonempty, dptr<char>(L.boff) + (size_t)L.nb * 4, 4, cudaMemcpyDeviceToHost));
-    const uint64_t opsBytes = T.ops.size() * 8;
-    double walk = 0, pts = 0;
-    for (uint32_t j = 0; j < T.w; ++j) {
-      if (band[j].y <= band[j].x) continue;
-      const uint32_t e0 = T.inj_lo[j];
-      // last epoch walked: the one whose points end at band.y
-      uint32_t e1 = (uint32_t)(std::lower_bound(T.ep_ptoff.begin(), T.ep_ptoff.end(), band[j].y) - T.ep_ptoff.begin());
-      if (e1 > T.n_epochs) e1 = T.n_epochs;
-      const uint64_t a = T.ep_opoff[e0], b = e1 < T.n_epochs ? T.ep_opoff[e1] : opsBytes / 8;
-      walk += (double)(b - a) * 8 + 16.0 * (band[j].y - band[j].x);
-      pts += band[j].y - band[j].x;
+    double walk = 0, pts = 0, R = 0;
+    for (uint32_t i = 0; i < ncirc(); ++i) {
+      const Tape &T = tapes[i];
+      std::vector<uint2> band(T.w);
+      CK(cudaMemcpy(band.data(), dptr<char>(L.c[i].band), (size_t)T.w * 8, cudaMemcpyDeviceToHost));
+      for (uint32_t j = 0; j < T.w; ++j) {
+        if (band[j].y <= band[j].x) continue;
+        const uint32_t e0 = T.inj_lo[j];
+        uint32_t e1 = (uint32_t)(std::lower_bound(T.ep_ptoff.begin(), T.ep_ptoff.end(), band[j].y) - T.ep_ptoff.begin());
+        if (e1 > T.n_epochs) e1 = T.n_epochs;
+        const uint64_t a = T.ep_opoff[e0], b = e1 < T.n_epochs ? T.ep_opoff[e1] : T.ops.size();
+        walk += (double)(b - a) * 8 + 16.0 * (band[j].y - band[j].x);
+        pts += band[j].y - band[j].x;
+      }
+      R += (double)T.rec.size();
     }
-    const double R = (double)T.rec.size(), M = T.M;
-    const double lists = tot[2];
+    const double M = L.M, lists = tot[2];
     out[0] = walk;
     out[1] = R * 20 + 16.0 * pts + M * (16 + 8 + 8 + 4) + 4.0 * lists;
-    out[2] = (double)L.nb * 12 + M * 16 + (double)nonempty * 20;
-    out[3] = (double)nonempty * (20 + 4 + 8) + 8.0 * lists + (double)tot[0] * 12 + (double)tot[1] * 4;
+    out[2] = (double)L.nb * 12 + M * 16 + (double)nonempty * 36;
+    out[3] = (double)nonempty * (28 + 8 + 4) + 8.0 * lists + (double)tot[0] * 12 + (double)tot[1] * 4;
   }
 
-  gpc_dem *fetch() {
+  // Copies the merged arrays of the last run to the host and splits them per circuit.
+  void fetch_all(std::vector<gpc_dem *> &outs) {
     if (!ran) throw gpc::Error(GPC_ERR_INVALID, "nothing has been run");
     CK(cudaSetDevice(device));
     uint32_t C = 0, NT = 0;
-    finish(&C, &NT);
-    auto dem = std::make_unique<gpc_dem>();
-    dem->num_detectors = tape.ndet;
-    dem->num_observables = tape.nobs;
-    dem->num_raw = tape.M;
-    const size_t bytes = (size_t)C * 8 + (size_t)C * 4 + (size_t)NT * 4 + 64;
-    last_d2h = (uint64_t)C * 12 + (uint64_t)NT * 4 + 12;  // results + flags and totals
+    if (finish(&C, &NT) == Finish::BatchFallback) {
+      batch_fallback(outs);
+      return;
+    }
+    const uint32_t N = ncirc();
+    const size_t bytes = (size_t)C * 8 + (size_t)C * 4 + (size_t)NT * 4 + (size_t)N * 8 + 64;
     pin_out.ensure(bytes);
     char *h = static_cast<char *>(pin_out.p);
+    char *hp = h, *ho = h + (size_t)C * 8, *ht = ho + (size_t)C * 4, *hc = ht + (size_t)NT * 4;
     if (C) {
-      CK(cudaMemcpyAsync(h, dptr<char>(L.out_prob), (size_t)C * 8, cudaMemcpyDeviceToHost, stream));
-      CK(cudaMemcpyAsync(h + (size_t)C * 8, dptr<char>(L.out_off), (size_t)C * 4, cudaMemcpyDeviceToHost, stream));
+      CK(cudaMemcpyAsync(hp, dptr<char>(L.out_prob), (size_t)C * 8, cudaMemcpyDeviceToHost, stream));
+      CK(cudaMemcpyAsync(ho, dptr<char>(L.out_off), (size_t)C * 4, cudaMemcpyDeviceToHost, stream));
     }
-    if (NT) CK(cudaMemcpyAsync(h + (size_t)C * 12, tgbuf.p, (size_t)NT * 4, cudaMemcpyDeviceToHost, stream));
+    if (NT) CK(cudaMemcpyAsync(ht, tgbuf.p, (size_t)NT * 4, cudaMemcpyDeviceToHost, stream));
+    if (N > 1) CK(cudaMemcpyAsync(hc, dptr<char>(L.cout), (size_t)N * 8, cudaMemcpyDeviceToHost, stream));
     CK(cudaStreamSynchronize(stream));
-    dem->probs.assign(reinterpret_cast<double *>(h), reinterpret_cast<double *>(h) + C);
-    dem->offsets.resize((size_t)C + 1);
-    memcpy(dem->offsets.data(), h + (size_t)C * 8, (size_t)C * 4);
-    dem->offsets[C] = NT;
-    dem->targets.assign(reinterpret_cast<uint32_t *>(h + (size_t)C * 12),
-                        reinterpret_cast<uint32_t *>(h + (size_t)C * 12) + NT);
-    return dem.release();
+    last_d2h = (uint64_t)C * 12 + (uint64_t)NT * 4 + 12 + (N > 1 ? (uint64_t)N * 8 : 0);
+    const double *P = reinterpret_cast<const double *>(hp);
+    const uint32_t *O = reinterpret_cast<const uint32_t *>(ho);
+    const uint32_t *TG = reinterpret_cast<const uint32_t *>(ht);
+    const uint2 *CO = reinterpret_cast<const uint2 *>(hc);
+    outs.assign(N, nullptr);
+    try {
+      for (uint32_t i = 0; i < N; ++i) {
+        const uint32_t c0 = N > 1 ? CO[i].x : 0, c1 = (N > 1 && i + 1 < N) ? CO[i + 1].x : C;
+        const uint32_t t0 = N > 1 ? CO[i].y : 0, t1 = (N > 1 && i + 1 < N) ? CO[i + 1].y : NT;
+        if (c1 < c0 || c1 > C || t1 < t0 || t1 > NT) throw gpc::Error(GPC_ERR_CUDA, "inconsistent batch ranges");
+        auto dem = std::make_unique<gpc_dem>();
+        dem->num_detectors = tapes[i].ndet;
+        dem->num_observables = tapes[i].nobs;
+        dem->num_raw = tapes[i].M;
+        dem->probs.assign(P + c0, P + c1);
+        dem->offsets.resize((size_t)(c1 - c0) + 1);
+        for (uint32_t k = c0; k < c1; ++k) dem->offsets[k - c0] = O[k] - t0;
+        dem->offsets[c1 - c0] = t1 - t0;
+        dem->targets.assign(TG + t0, TG + t1);
+        outs[i] = dem.release();
+      }
+    } catch (...) {
+      for (auto &d : outs) delete d;
+      outs.assign(N, nullptr);
+      throw;
+    }
+  }
+
+  // A batch whose merge needs a fallback (a symptom repeated more than a
+  // bucket holds, or a symptom longer than the target lists): compile its
+  // circuits one at a time on the single-circuit path.
+  void batch_fallback(std::vector<gpc_dem *> &outs) {
+    std::vector<gpc::Parsed> P = std::move(parsed);
+    std::vector<Tape> T = std::move(tapes);
+    const uint32_t N = (uint32_t)T.size();
+    outs.assign(N, nullptr);
+    try {
+      for (uint32_t i = 0; i < N; ++i) {
+        parsed.assign(1, P[i]);
+        tapes.assign(1, std::move(T[i]));
+        tcap = 32;
+        lists_off = false;
+        prepare(nullptr, nullptr, 0);
+        run();
+        std::vector<gpc_dem *> one;
+        fetch_all(one);
+        outs[i] = one[0];
+      }
+    } catch (...) {
+      for (auto &d : outs) delete d;
+      outs.assign(N, nullptr);
+      throw;
+    }
+  }
+
+  gpc_dem *fetch() {
+    std::vector<gpc_dem *> outs;
+    fetch_all(outs);
+    for (size_t i = 1; i < outs.size(); ++i) delete outs[i];
+    return outs.empty() ? nullptr : outs[0];
   }
 };
 
@@ -690,10 +900,9 @@ gpc_status gpc_get_driver(const char *stim_text, size_t len, int32_t correlation
     CK(cudaGetDeviceCount(&n));
     if (d->device < 0 || d->device >= n) throw gpc::Error(GPC_ERR_CUDA, "no such CUDA device");
     CK(cudaSetDevice(d->device));
-    CK(cudaStreamCreateWithFlags(&d->stream, cudaStreamNonBlocking));
+    d->init_streams();
     CK(gpc::walk_set_smem_limit());  // per device: the driver's device is current here
-    for (auto &e : d->ev) CK(cudaEventCreate(&e));
-    d->prepare(stim_text, len);
+    d->prepare(&stim_text, &len, 1);
   });
   if (st != GPC_OK) return st;
   *out = d.release();
@@ -702,7 +911,28 @@ gpc_status gpc_get_driver(const char *stim_text, size_t len, int32_t correlation
 
 gpc_status gpc_prepare(gpc_driver *driver, const char *stim_text, size_t len) {
   if (!driver) return fail(GPC_ERR_INVALID, "driver is null");
-  return guarded([&] { driver->prepare(stim_text, len); });
+  return guarded([&] {
+    if (stim_text) driver->prepare(&stim_text, &len, 1);
+    else driver->prepare(nullptr, nullptr, 0);
+  });
+}
+
+gpc_status gpc_prepare_batch(gpc_driver *driver, const char *const *texts, const size_t *lens, int32_t n) {
+  if (!driver || !texts || !lens || n <= 0) return fail(GPC_ERR_INVALID, "bad batch arguments");
+  for (int32_t i = 0; i < n; ++i)
+    if (!texts[i]) return fail(GPC_ERR_INVALID, "null circuit text in batch");
+  return guarded([&] { driver->prepare(texts, lens, (uint32_t)n); });
+}
+
+gpc_status gpc_fetch_batch(gpc_driver *driver, gpc_dem **outs, int32_t n) {
+  if (!driver || !outs || n <= 0) return fail(GPC_ERR_INVALID, "bad batch arguments");
+  for (int32_t i = 0; i < n; ++i) outs[i] = nullptr;
+  return guarded([&] {
+    if ((uint32_t)n != driver->ncirc()) throw gpc::Error(GPC_ERR_INVALID, "batch size differs from the prepared batch");
+    std::vector<gpc_dem *> v;
+    driver->fetch_all(v);
+    for (int32_t i = 0; i < n; ++i) outs[i] = v[i];
+  });
 }
 
 gpc_status gpc_run_device(gpc_driver *driver) {
@@ -720,8 +950,8 @@ gpc_status gpc_compile(gpc_driver *driver, const char *stim_text, size_t len, gp
   if (!driver || !out) return fail(GPC_ERR_INVALID, "null argument");
   *out = nullptr;
   return guarded([&] {
-    if (stim_text || !driver->prepared) driver->prepare(stim_text, len);
-    else driver->prepare(nullptr, 0);  // re-upload the parsed circuit, as the reference re-copies it
+    if (stim_text) driver->prepare(&stim_text, &len, 1);
+    else driver->prepare(nullptr, nullptr, 0);  // re-upload the parsed circuit, as the reference re-copies it
     driver->run();
     *out = driver->fetch();
   });
@@ -729,19 +959,17 @@ gpc_status gpc_compile(gpc_driver *driver, const char *stim_text, size_t len, gp
 
 gpc_status gpc_compile_batch(gpc_driver *driver, const char *const *texts, const size_t *lens, int32_t n,
                              gpc_dem **outs) {
-  if (!driver || !texts || !lens || !outs || n < 0) return fail(GPC_ERR_INVALID, "null argument");
+  if (!driver || !texts || !lens || !outs || n <= 0) return fail(GPC_ERR_INVALID, "bad batch arguments");
   for (int32_t i = 0; i < n; ++i) outs[i] = nullptr;
-  for (int32_t i = 0; i < n; ++i) {
-    gpc_status st = gpc_compile(driver, texts[i], lens[i], &outs[i]);
-    if (st != GPC_OK) {
-      for (int32_t k = 0; k < i; ++k) {
-        gpc_dem_free(outs[k]);
-        outs[k] = nullptr;
-      }
-      return st;
-    }
-  }
-  return GPC_OK;
+  for (int32_t i = 0; i < n; ++i)
+    if (!texts[i]) return fail(GPC_ERR_INVALID, "null circuit text in batch");
+  return guarded([&] {
+    driver->prepare(texts, lens, (uint32_t)n);
+    driver->run();
+    std::vector<gpc_dem *> v;
+    driver->fetch_all(v);
+    for (int32_t i = 0; i < n; ++i) outs[i] = v[i];
+  });
 }
 
 gpc_status gpc_dem_arrays(const gpc_dem *dem, const uint32_t **offsets, const uint32_t **targets, const double **probs,
@@ -822,11 +1050,20 @@ gpc_status gpc_last_io_bytes(gpc_driver *driver, uint64_t *h2d, uint64_t *d2h) {
 gpc_status gpc_last_sizes(gpc_driver *driver, uint64_t *raw, uint64_t *points, uint32_t *epochs, uint32_t *words,
                           uint32_t *qubits) {
   if (!driver) return fail(GPC_ERR_INVALID, "driver is null");
-  if (raw) *raw = driver->tape.M;
-  if (points) *points = driver->tape.npoints;
-  if (epochs) *epochs = driver->tape.n_epochs;
-  if (words) *words = driver->tape.w;
-  if (qubits) *qubits = driver->tape.nq;
+  uint64_t r = 0, p = 0;
+  uint32_t e = 0, w = 0, q = 0;
+  for (const auto &T : driver->tapes) {  // sums over a batch; epochs/words/qubits: the largest circuit
+    r += T.M;
+    p += T.npoints;
+    e = std::max(e, T.n_epochs);
+    w = std::max(w, T.w);
+    q = std::max(q, T.nq);
+  }
+  if (raw) *raw = r;
+  if (points) *points = p;
+  if (epochs) *epochs = e;
+  if (words) *words = w;
+  if (qubits) *qubits = q;
   return GPC_OK;
 }
 

@@ -94,72 +94,91 @@ __constant__ uint8_t kNComp[6] = {1, 2, 3, 6, 10, 15};
 #undef PP
 
 __global__ void __launch_bounds__(256) key_kernel(KeyLaunch L) {
-  extern __shared__ uint2 sband[];
-  const CircuitDev C = *L.c_dev;
-  const uint32_t w = L.w;
-  for (uint32_t j = threadIdx.x; j < w; j += blockDim.x) sband[j] = C.band[j];
+  __shared__ uint32_t smb[kMaxCircuitsStaged + 1];
+  __shared__ uint2 sband[1024];
+  __shared__ uint32_t s_c0, s_c1;
+  const bool staged = L.n_circ <= kMaxCircuitsStaged;
+  for (uint32_t i = threadIdx.x; staged && i <= L.n_circ; i += blockDim.x) smb[i] = L.mbase[i];
   __syncthreads();
-  const uint32_t shift = 64u - L.bucket_bits;
+  const uint32_t *mb = staged ? smb : L.mbase;
+  const uint32_t m0 = blockIdx.x * blockDim.x;
+  const uint32_t mg = m0 + threadIdx.x;
+  // the circuits of this block's first and last mechanisms; one circuit: stage its bands
+  if (threadIdx.x == 0) {
+    s_c0 = find_circuit(mb, L.n_circ, m0);
+    s_c1 = find_circuit(mb, L.n_circ, min(L.M - 1, m0 + blockDim.x - 1));
+  }
+  __syncthreads();
+  const uint32_t c0 = s_c0;
+  const bool oneband = s_c0 == s_c1 && L.circs[c0].w <= 1024;
+  if (oneband)
+    for (uint32_t j = threadIdx.x; j < L.circs[c0].w; j += blockDim.x) sband[j] = L.circs[c0].band[j];
+  __syncthreads();
+  if (mg >= L.M) return;
+  const uint32_t c = oneband ? c0 : find_circuit(mb, L.n_circ, mg);
+  const CircuitDev &C = L.circs[c];
+  const uint32_t m = mg - mb[c];
+  const uint32_t w = C.w;
   const uint32_t tcap = C.tcap;
-  const uint32_t R = L.R;
-  for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < C.M; m += gridDim.x * blockDim.x) {
-    // the record holding mechanism m: the last r with rec_moff[r] <= m
-    uint32_t lo = 0, hi = R;  // rec_moff[lo] <= m < rec_moff[hi]
-    while (hi - lo > 1) {
-      const uint32_t mid = (lo + hi) >> 1;
-      if (__ldg(C.rec_moff + mid) <= m) lo = mid;
-      else hi = mid;
-    }
-    const uint32_t r = lo;
-    const uint64_t d = __ldg(C.rec + r);
-    const uint32_t c = m - __ldg(C.rec_moff + r);
-    const uint32_t type = (uint32_t)((d >> 56) & 15u);
-    const uint32_t comp = type == 0 ? (uint32_t)((d >> 60) & 3u) | ((uint32_t)(d >> 62) << 2) : kComp[type][c];
-    uint32_t pa = (uint32_t)(d & 0x0FFFFFFFu), pb = (uint32_t)((d >> 28) & 0x0FFFFFFFu);
-    uint32_t Pa = comp & 3u, Pb = comp >> 2;
-    if (Pa == 0) {  // a component on point b only is stored with b as its first point
-      pa = pb;
-      Pa = Pb;
-      Pb = 0;
-    }
-    if (Pb == 0) pb = 0;
-    C.mdesc[m] = mk_desc(pa, Pa, pb, Pb);
-    C.mp[m] = __ldg(C.rec_p + r);
-    uint64_t hx = 0, hy = 0;
-    uint32_t cnt = 0;
-    bool nonzero = false;
-    uint32_t *out = C.tl + (size_t)m * tcap;
-    for (uint32_t j = 0; j < w; ++j) {
-      const uint2 b = sband[j];
-      const ulonglong2 *sj = C.snap + (size_t)j * C.npoints;
-      uint64_t v = 0;
-      if (pa - b.x < b.y - b.x) v = pauli_sel(sj[pa], Pa);
-      if (Pb && pb - b.x < b.y - b.x) v ^= pauli_sel(sj[pb], Pb);
-      if (!v) continue;
-      nonzero = true;
-      const ulonglong2 h = word_hash(j, v);
-      hx ^= h.x;
-      hy ^= h.y;
-      if (tcap) {
-        uint64_t x = v;
-        while (x) {
-          if (cnt < tcap) out[cnt] = j * 64u + (uint32_t)(__ffsll((long long)x) - 1);
-          ++cnt;
-          x &= x - 1;
-        }
+  const uint32_t R = C.R;
+  // the record holding mechanism m: the last r with rec_moff[r] <= m
+  uint32_t lo = 0, hi = R;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(C.rec_moff + mid) <= m) lo = mid;
+    else hi = mid;
+  }
+  const uint32_t r = lo;
+  const uint64_t d = __ldg(C.rec + r);
+  const uint32_t ci = m - __ldg(C.rec_moff + r);
+  const uint32_t type = (uint32_t)((d >> 56) & 15u);
+  const uint32_t comp = type == 0 ? (uint32_t)((d >> 60) & 3u) | ((uint32_t)(d >> 62) << 2) : kComp[type][ci];
+  uint32_t pa = (uint32_t)(d & 0x0FFFFFFFu), pb = (uint32_t)((d >> 28) & 0x0FFFFFFFu);
+  uint32_t Pa = comp & 3u, Pb = comp >> 2;
+  if (Pa == 0) {  // a component on point b only is stored with b as its first point
+    pa = pb;
+    Pa = Pb;
+    Pb = 0;
+  }
+  if (Pb == 0) pb = 0;
+  C.mdesc[m] = mk_desc(pa, Pa, pb, Pb);
+  C.mp[m] = __ldg(C.rec_p + r);
+  uint64_t hx = 0, hy = 0;
+  uint32_t cnt = 0;
+  bool nonzero = false;
+  uint32_t *out = C.tl + (size_t)m * tcap;
+  const ulonglong2 *snap = C.snap;
+  const uint32_t np = C.npoints;
+  for (uint32_t j = 0; j < w; ++j) {
+    const uint2 b = oneband ? sband[j] : C.band[j];
+    const ulonglong2 *sj = snap + (size_t)j * np;
+    uint64_t v = 0;
+    if (pa - b.x < b.y - b.x) v = pauli_sel(sj[pa], Pa);
+    if (Pb && pb - b.x < b.y - b.x) v ^= pauli_sel(sj[pb], Pb);
+    if (!v) continue;
+    nonzero = true;
+    const ulonglong2 h = word_hash(j, v);
+    hx ^= h.x;
+    hy ^= h.y;
+    if (tcap) {
+      uint64_t x = v;
+      while (x) {
+        if (cnt < tcap) out[cnt] = j * 64u + (uint32_t)(__ffsll((long long)x) - 1);
+        ++cnt;
+        x &= x - 1;
       }
     }
-    L.key[m] = make_ulonglong2(hx, hy);
-    if (tcap) {
-      C.tn[m] = cnt;
-      if (cnt > tcap) atomicOr(L.err, DEV_FLAG_LONG);
-      if (cnt) atomicAdd(L.list_total, cnt);
-    }
-    if ((hx | hy) == 0) {
-      if (cnt || (!tcap && nonzero)) atomicOr(L.err, DEV_ERR_COLLISION);  // a non-empty symptom hashed to 0
-    } else {
-      atomicAdd(L.bucket_count + (hx >> shift), 1u);
-    }
+  }
+  L.key[mg] = make_ulonglong2(hx, hy);
+  if (tcap) {
+    C.tn[m] = cnt;
+    if (cnt > tcap) atomicOr(L.err, DEV_FLAG_LONG);
+    if (cnt) atomicAdd(L.list_total, cnt);
+  }
+  if ((hx | hy) == 0) {
+    if (cnt || (!tcap && nonzero)) atomicOr(L.err, DEV_ERR_COLLISION);  // a non-empty symptom hashed to 0
+  } else {
+    atomicAdd(L.bucket_count + C.bbase + (uint32_t)(hx >> (64u - C.bbits)), 1u);
   }
 }
 
@@ -202,14 +221,22 @@ __global__ void bucket_scatter_kernel(const ulonglong2 *__restrict__ key, uint32
   }
 }
 
-__global__ void bucket_scatter_p_kernel(const ulonglong2 *__restrict__ key, const double *__restrict__ mp,
-                                        uint32_t M, uint32_t shift, const uint32_t *__restrict__ offset,
-                                        uint32_t *__restrict__ cursor, ulonglong2 *__restrict__ bkey,
-                                        uint32_t *__restrict__ bm, double *__restrict__ bp) {
+__global__ void bucket_scatter_p_kernel(const CircuitDev *__restrict__ circs, const uint32_t *__restrict__ mbase,
+                                        uint32_t n_circ, const ulonglong2 *__restrict__ key,
+                                        const double *__restrict__ mp, uint32_t M,
+                                        const uint32_t *__restrict__ offset, uint32_t *__restrict__ cursor,
+                                        ulonglong2 *__restrict__ bkey, uint32_t *__restrict__ bm,
+                                        double *__restrict__ bp) {
+  __shared__ uint32_t smb[kMaxCircuitsStaged + 1];
+  const bool staged = n_circ <= kMaxCircuitsStaged;
+  for (uint32_t i = threadIdx.x; staged && i <= n_circ; i += blockDim.x) smb[i] = mbase[i];
+  __syncthreads();
+  const uint32_t *mb = staged ? smb : mbase;
   for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
     const ulonglong2 k = key[m];
     if ((k.x | k.y) == 0) continue;
-    const uint32_t b = (uint32_t)(k.x >> shift);
+    const uint32_t c = n_circ == 1 ? 0u : find_circuit(mb, n_circ, m);
+    const uint32_t b = circs[c].bbase + (uint32_t)(k.x >> (64u - circs[c].bbits));
     const uint32_t pos = offset[b] + atomicAdd(cursor + b, 1u);
     bkey[pos] = k;
     bm[pos] = m;
@@ -736,7 +763,6 @@ __global__ void __launch_bounds__(BUCKET_THREADS) group_kernel(GroupLaunch L) {
   __shared__ uint16_t ord[BUCKET_CAP];
   __shared__ uint32_t sntg[BUCKET_CAP];  // targets of a group head at a sorted position, else ~0u
   __shared__ uint32_t wc[NW], wt[NW];
-  const CircuitDev C = *L.c_dev;
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
   const uint32_t b = blockIdx.x;
   uint32_t n = L.count[b];
@@ -768,18 +794,18 @@ __global__ void __launch_bounds__(BUCKET_THREADS) group_kernel(GroupLaunch L) {
   }
   __syncthreads();
   // group heads, collision checks (full target lists), target counts
-  const uint32_t tcap = C.tcap;
+  const uint32_t tcap = L.tcap;
   for (uint32_t s = threadIdx.x; s < n; s += NT) {
     const uint32_t i = ord[s];
     const uint32_t m = sm[i];
-    const uint32_t nt = __ldg(C.tn + m);
+    const uint32_t nt = __ldg(L.tn + m);
     bool head = true;
     if (s > 0) {
       const uint32_t ip = ord[s - 1];
       if (sk[ip].x == sk[i].x && sk[ip].y == sk[i].y) {
         head = false;
         const uint32_t mq = sm[ip];
-        if (__ldg(C.tn + mq) != nt || !lists_equal(C.tl + (size_t)m * tcap, C.tl + (size_t)mq * tcap, nt))
+        if (__ldg(L.tn + mq) != nt || !lists_equal(L.tl + (size_t)m * tcap, L.tl + (size_t)mq * tcap, nt))
           atomicOr(L.err, DEV_ERR_COLLISION);
       }
     }
@@ -869,23 +895,24 @@ __global__ void __launch_bounds__(1024) group_scan_kernel(GroupLaunch L) {
     L.totals[1] = pt[1023];
     if (pt[1023] > L.tg_cap) atomicOr(L.err, DEV_FLAG_TG_OVF);
   }
+  __syncthreads();  // bout written by the whole block
+  for (uint32_t c = t; c < L.n_circ; c += 1024) L.cout[c] = L.bout[L.cbbase[c]];
 }
 
 __global__ void __launch_bounds__(BUCKET_THREADS) emit_kernel(GroupLaunch L) {
   const uint32_t b = blockIdx.x;
   const uint2 agg = L.bagg[b], out = L.bout[b];
   const uint32_t base = L.offset[b];
-  const CircuitDev C = *L.c_dev;
-  const uint32_t tcap = C.tcap;
+  const uint32_t tcap = L.tcap;
   for (uint32_t g = threadIdx.x; g < agg.x; g += BUCKET_THREADS) {
     const uint32_t slot = out.x + g;
     const uint32_t toff = out.y + L.gt[base + g];
     const uint32_t m = L.gm[base + g];
     L.out_prob[slot] = L.gp[base + g];
     L.out_off[slot] = toff;
-    const uint32_t ntg = __ldg(C.tn + m);
+    const uint32_t ntg = __ldg(L.tn + m);
     if (toff + ntg <= L.tg_cap) {
-      const uint4 *src = reinterpret_cast<const uint4 *>(C.tl + (size_t)m * tcap);
+      const uint4 *src = reinterpret_cast<const uint4 *>(L.tl + (size_t)m * tcap);
       for (uint32_t k = 0; k * 4 < ntg; ++k) {
         const uint4 x = __ldg(src + k);
         const uint32_t o = toff + k * 4, rem = ntg - k * 4;
@@ -901,11 +928,10 @@ __global__ void __launch_bounds__(BUCKET_THREADS) emit_kernel(GroupLaunch L) {
 }  // namespace
 
 cudaError_t launch_keys(const KeyLaunch &L, cudaStream_t s) {
-  if (L.R == 0 || L.M == 0) return cudaSuccess;
+  if (L.M == 0) return cudaSuccess;
   const uint32_t threads = 256;
-  uint32_t blocks = (L.M + threads - 1) / threads;
-  if (blocks > 152u * 16u) blocks = 152u * 16u;
-  key_kernel<<<blocks, threads, (size_t)L.w * sizeof(uint2), s>>>(L);
+  const uint32_t blocks = (L.M + threads - 1) / threads;
+  key_kernel<<<blocks, threads, 0, s>>>(L);
   return cudaGetLastError();
 }
 
@@ -923,13 +949,13 @@ cudaError_t launch_bucket_scatter(const ulonglong2 *key, uint32_t M, uint32_t bu
   return cudaGetLastError();
 }
 
-cudaError_t launch_bucket_scatter_p(const ulonglong2 *key, const double *mp, uint32_t M, uint32_t bucket_bits,
-                                    const uint32_t *offset, uint32_t *cursor, ulonglong2 *bkey, uint32_t *bm,
-                                    double *bp, cudaStream_t s) {
+cudaError_t launch_bucket_scatter_p(const CircuitDev *circs, const uint32_t *mbase, uint32_t n_circ,
+                                    const ulonglong2 *key, const double *mp, uint32_t M, const uint32_t *offset,
+                                    uint32_t *cursor, ulonglong2 *bkey, uint32_t *bm, double *bp, cudaStream_t s) {
   if (M == 0) return cudaSuccess;
   uint32_t blocks = (M + 255) / 256;
   if (blocks > 152u * 16u) blocks = 152u * 16u;
-  bucket_scatter_p_kernel<<<blocks, 256, 0, s>>>(key, mp, M, 64u - bucket_bits, offset, cursor, bkey, bm, bp);
+  bucket_scatter_p_kernel<<<blocks, 256, 0, s>>>(circs, mbase, n_circ, key, mp, M, offset, cursor, bkey, bm, bp);
   return cudaGetLastError();
 }
 

@@ -111,14 +111,31 @@ class Driver:
         dem = self.compile(circuit)
         return dem.to_stim() if _stim_available() else dem
 
-    def compile_batch(self, circuits) -> list:
-        L = _native.lib()
+    @staticmethod
+    def _batch_args(circuits):
         texts = [_text(c) for c in circuits]
         n = len(texts)
         arr = (ctypes.c_char_p * n)(*texts)
         lens = (ctypes.c_size_t * n)(*[len(t) for t in texts])
+        return n, arr, lens
+
+    def compile_batch(self, circuits) -> list:
+        """Compiles many circuits in one batched pipeline; one DEM per circuit, in order."""
+        L = _native.lib()
+        n, arr, lens = self._batch_args(circuits)
         outs = (ctypes.c_void_p * n)()
         _native.check(L.gpc_compile_batch(self._h, arr, lens, n, outs))
+        return [dem_from_handle(ctypes.c_void_p(outs[i])) for i in range(n)]
+
+    def prepare_batch(self, circuits) -> None:
+        n, arr, lens = self._batch_args(circuits)
+        self._batch_n = n
+        _native.check(_native.lib().gpc_prepare_batch(self._h, arr, lens, n))
+
+    def fetch_batch(self) -> list:
+        n = self._batch_n
+        outs = (ctypes.c_void_p * n)()
+        _native.check(_native.lib().gpc_fetch_batch(self._h, outs, n))
         return [dem_from_handle(ctypes.c_void_p(outs[i])) for i in range(n)]
 
     # device-resident stages

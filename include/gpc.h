@@ -73,8 +73,12 @@ gpc_status gpc_get_driver(const char *stim_text, size_t len, int32_t correlation
  * no-argument overload.  The result is owned by the caller. */
 gpc_status gpc_compile(gpc_driver *driver, const char *stim_text, size_t len, gpc_dem **out);
 
-/* Compiles `n` circuits in one batched pipeline (one walk launch, one
- * segmented sort, one merge).  outs[i] receives circuit i's DEM. */
+/* Compiles `n` circuits in one batched pipeline: the circuits are lowered on
+ * host threads, uploaded with one copy, walked by one launch per thread-count
+ * class (classes run concurrently), keyed, bucketed and merged by single
+ * launches over the whole batch (buckets are numbered circuit by circuit, so
+ * each circuit's output is contiguous).  outs[i] receives circuit i's DEM.
+ * Batches whose merge needs a fallback are compiled circuit by circuit. */
 gpc_status gpc_compile_batch(gpc_driver *driver, const char *const *texts, const size_t *lens,
                              int32_t n, gpc_dem **outs);
 
@@ -104,6 +108,9 @@ const char *gpc_last_error(void);
 gpc_status gpc_prepare(gpc_driver *driver, const char *stim_text, size_t len);
 gpc_status gpc_run_device(gpc_driver *driver);
 gpc_status gpc_fetch(gpc_driver *driver, gpc_dem **out);
+/* Batched forms of gpc_prepare / gpc_fetch (gpc_run_device runs either). */
+gpc_status gpc_prepare_batch(gpc_driver *driver, const char *const *texts, const size_t *lens, int32_t n);
+gpc_status gpc_fetch_batch(gpc_driver *driver, gpc_dem **outs, int32_t n);
 
 /* The driver's CUDA stream (a cudaStream_t), for callers that time it. */
 void *gpc_driver_stream(gpc_driver *driver);

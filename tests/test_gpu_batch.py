@@ -1,0 +1,61 @@
+"""The batched form: many circuits of uneven sizes in one pipeline (needs a GPU).
+
+Every circuit's DEM from the batch must equal its single-circuit compile
+(same symptoms, same probabilities bit for bit, same order) and the oracle.
+"""
+
+from __future__ import annotations
+
+import pytest
+
+import greenpeas_gb300 as gp
+from conftest import compare_errors
+from oracle import oracle as O
+from test_lowering import SMALL
+
+pytestmark = pytest.mark.gpu
+
+
+def _mixed():
+    circs = [gp.SurfaceCode(d).get_memory(d, 1e-3, noise=nz) for d, nz in
+             [(3, "uniform"), (5, "reference"), (7, "uniform"), (3, "reference")]]
+    circs += [gp.BBCode(6).get_memory(6, 1e-3, noise="uniform")]
+    circs += SMALL
+    return circs
+
+
+def test_batch_matches_single_and_oracle():
+    circs = _mixed()
+    drv = gp.get_driver(circs[0])
+    batch = drv.compile_batch(circs)
+    assert len(batch) == len(circs)
+    for text, dem in zip(circs, batch):
+        single = gp.get_driver(text).compile(text)
+        assert dem.canonical() == single.canonical()
+        ref = O.compile_text(text, 2)
+        assert dem.num_detectors == ref.num_detectors
+        compare_errors(dict(dem.errors()), dict(ref.errors()), rel=1e-12)
+
+
+def test_batch_device_stages_repeat():
+    circs = _mixed()[:5]
+    drv = gp.get_driver(circs[0])
+    drv.prepare_batch(circs)
+    drv.run_device()
+    first = drv.fetch_batch()
+    for _ in range(3):  # later runs come from a captured graph
+        drv.run_device()
+    again = drv.fetch_batch()
+    assert [a == b for a, b in zip(first, again)] == [True] * len(circs)
+
+
+def test_batch_falls_back_per_circuit():
+    """A circuit with a symptom longer than the target lists makes the batch compile one by one."""
+    n = 80
+    long = "R " + " ".join(map(str, range(n))) + "\nX_ERROR(0.01) 0\n"
+    long += "".join(f"CX 0 {q}\n" for q in range(1, n))
+    long += "M " + " ".join(map(str, range(n))) + "\n" + "".join(f"DETECTOR rec[-{k}]\n" for k in range(1, n + 1))
+    circs = [gp.SurfaceCode(3).get_memory(3, 1e-3), long, SMALL[2]]
+    out = gp.get_driver(circs[0]).compile_batch(circs)
+    for text, dem in zip(circs, out):
+        compare_errors(dict(dem.errors()), dict(O.compile_text(text, 2).errors()), rel=1e-12)
