@@ -163,6 +163,94 @@ def cpu_baseline(text: str, budget_s: float = 10.0) -> dict:
             "sample": f"{n} compiles of the workload in {el:.1f} s (CPU FP64 oracle, all host threads)"}
 
 
+def dem_arrays_equal(a, b) -> bool:
+    import numpy as np
+    return (a.num_detectors == b.num_detectors and np.array_equal(a.offsets, b.offsets)
+            and np.array_equal(a.targets, b.targets) and np.array_equal(a.probs, b.probs))
+
+
+def batched_leg(gp, torch, local: int, flush, steps: int, warmup: int) -> dict:
+    """Mixed-size batch: one batched pipeline vs the plain per-circuit path on the same circuits.
+
+    Device rates time only the kernel pipelines (CUDA events on the driver's
+    stream, L2 flushed before each); e2e rates run host text to host arrays.
+    """
+    from greenpeas_gb300.workloads import batch_surface
+    texts = batch_surface()
+    n = len(texts)
+    dev = torch.device("cuda", local)
+    # plain: one circuit per compile, the same driver reused
+    plain = gp.get_driver(texts[0], device=local)
+    ext = torch.cuda.ExternalStream(plain.stream, device=dev)
+    singles = []
+    plain_ms = 0.0
+    for t in texts:
+        plain.prepare(t)
+        plain.run_device()  # warm (and, at the second identical launch shape, graph capture)
+        with torch.cuda.stream(ext):
+            flush.fill_(1.0)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            plain.run_device()
+            e1.record(ext)
+        e1.synchronize()
+        plain_ms += e0.elapsed_time(e1)
+        singles.append(plain.fetch())
+    # plain end to end
+    t0 = time.perf_counter()
+    for t in texts:
+        plain.compile(t)
+    plain_e2e_s = time.perf_counter() - t0
+    raw = sum(d.num_raw_mechanisms for d in singles)
+    merged = sum(d.num_errors for d in singles)
+    del plain
+
+    bdrv = gp.get_driver(texts[0], device=local)
+    bext = torch.cuda.ExternalStream(bdrv.stream, device=dev)
+    bdrv.prepare_batch(texts)
+    for _ in range(warmup):
+        bdrv.run_device()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    with torch.cuda.stream(bext):
+        for i in range(steps):
+            flush.fill_(float(i))
+            ev[i][0].record(bext)
+            bdrv.run_device()
+            ev[i][1].record(bext)
+    torch.cuda.synchronize()
+    batch_ms = [a.elapsed_time(b) for a, b in ev]
+    outs = bdrv.fetch_batch()
+    ok = len(outs) == n and all(dem_arrays_equal(a, b) for a, b in zip(outs, singles))
+    if not ok:
+        raise SystemExit("bench: batched DEMs differ from the plain per-circuit DEMs")
+    bdrv.compile_batch(texts)  # warm the end-to-end path
+    h2d_b = d2h_b = 0
+    t0 = time.perf_counter()
+    e2e_steps = max(1, min(steps, 3))
+    for _ in range(e2e_steps):
+        bdrv.compile_batch(texts)
+    batch_e2e_s = (time.perf_counter() - t0) / e2e_steps
+    h2d_b, d2h_b = bdrv.last_io_bytes()
+    bmean = sum(batch_ms) / len(batch_ms)
+    plain_rate = n / (plain_ms / 1e3)
+    batch_rate = n / (bmean / 1e3)
+    return {
+        "workload": "surface_batch256_seed0_d3-21_logp1e-4..1e-2_switch0.1",
+        "circuits": n, "raw_mechanisms": raw, "merged_mechanisms": merged,
+        "batched": {"value": batch_rate, "unit": UNIT, "ms_per_batch": bmean, "steps": steps,
+                    "mechanisms_per_s": {"raw": batch_rate * raw / n, "merged": batch_rate * merged / n},
+                    "e2e": {"value": n / batch_e2e_s, "unit": UNIT, "h2d_bytes_per_step": h2d_b,
+                            "d2h_bytes_per_step": d2h_b}},
+        "plain": {"value": plain_rate, "unit": UNIT, "ms_total": plain_ms,
+                  "mechanisms_per_s": {"raw": plain_rate * raw / n, "merged": plain_rate * merged / n},
+                  "e2e": {"value": n / plain_e2e_s, "unit": UNIT}},
+        "speedup_device": batch_rate / plain_rate,
+        "speedup_e2e": plain_e2e_s / batch_e2e_s,
+        "bit_exact_vs_plain": ok,
+    }
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -170,6 +258,7 @@ def main() -> None:
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-batch", action="store_true", help="skip the mixed-size batch leg")
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -280,6 +369,9 @@ def main() -> None:
         "gpu_launches": 5 * args.steps,
         "clocks": clocks.summary(),
     }
+    if not args.no_batch:
+        line["batch"] = batched_leg(gp, torch, local, flush, steps=max(3, min(args.steps, 10)),
+                                    warmup=args.warmup)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(text)
     print(json.dumps(line), flush=True)

@@ -158,10 +158,20 @@ class Code:
         return out
 
     def get_memory(self, rounds: int, p: float, include_x_detectors: bool = True,
-                   noise: str = "reference") -> str:
-        """Stim text of a memory-Z experiment with ``rounds`` syndrome rounds."""
+                   noise: str = "reference", p_sampler=None, switch_rounds=()) -> str:
+        """Stim text of a memory-Z experiment with ``rounds`` syndrome rounds.
+
+        ``p_sampler`` (uniform noise only): called once per noise instruction --
+        one channel instance per tick and gate class -- and returns its
+        probability, for time-varying noise.  ``switch_rounds``: rounds (0-based)
+        that take the basis-switch branch, running the Z-check CNOT layers
+        before the X-check layers.
+        """
         if noise not in ("reference", "uniform"):
             raise ValueError("noise must be 'reference' or 'uniform'")
+        if p_sampler is not None and noise != "uniform":
+            raise ValueError("p_sampler needs noise='uniform'")
+        switch = set(switch_rounds)
         if rounds < 1:
             raise ValueError("rounds must be >= 1")
         n, nx, nz, nc = self.num_data, self.num_x, self.num_z, self.num_checks
@@ -179,20 +189,23 @@ class Code:
             a = f"({arg})" if arg is not None else ""
             L.append(f"{name}{a} " + " ".join(map(str, targets)) if targets else f"{name}{a}")
 
-        def round_():
+        def pu():  # probability of the next uniform-noise instruction
+            return fmt_float(p_sampler()) if p_sampler is not None else ps
+
+        def round_(r):
             ins("R", checks)
             ins("TICK", [])
-            ins("X_ERROR", checks, ps)
-            ins("DEPOLARIZE1", data, pi if ref else ps)
+            ins("X_ERROR", checks, ps if ref else pu())
+            ins("DEPOLARIZE1", data, pi if ref else pu())
             if nx:
                 ins("H", xchecks)
                 ins("TICK", [])
                 if ref:
                     ins("DEPOLARIZE1", allq, pi)
-            for layer in xs + zs:
+            for layer in (zs + xs if r in switch else xs + zs):
                 ins("CX", layer)
                 ins("TICK", [])
-                ins("DEPOLARIZE2", layer, ps)
+                ins("DEPOLARIZE2", layer, ps if ref else pu())
                 if ref:
                     active = set(layer)
                     idle = [q for q in allq if q not in active]
@@ -206,21 +219,21 @@ class Code:
             if ref:
                 ins("M", checks, ps)
             else:
-                ins("X_ERROR", checks, ps)
+                ins("X_ERROR", checks, pu())
                 ins("M", checks)
 
         # head
         ins("R", data)
         ins("TICK", [])
-        ins("X_ERROR", data, ps)
+        ins("X_ERROR", data, ps if ref else pu())
         if ref:
             ins("DEPOLARIZE1", checks, pi)
         # rounds
-        round_()
+        round_(0)
         for i in range(nz):
             L.append(f"DETECTOR rec[-{nz - i}]")
-        for _ in range(1, rounds):
-            round_()
+        for r in range(1, rounds):
+            round_(r)
             lo = 0 if include_x_detectors else nx
             for i in range(lo, nc):
                 L.append(f"DETECTOR rec[-{nc - i}] rec[-{2 * nc - i}]")
@@ -228,7 +241,7 @@ class Code:
         if ref:
             ins("M", data, ps)
         else:
-            ins("X_ERROR", data, ps)
+            ins("X_ERROR", data, pu())
             ins("M", data)
         for chk, sup in enumerate(self.z_support):
             if not sup:

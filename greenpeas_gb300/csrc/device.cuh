@@ -65,7 +65,10 @@ constexpr int RADIX_BITS = 8;
 constexpr int RADIX = 1 << RADIX_BITS;
 constexpr int MERGE_THREADS = 256;
 constexpr int BUCKET_THREADS = 128;
-constexpr int BUCKET_CAP = 1024;  // items one CTA sorts in shared memory
+constexpr int BUCKET_CAP = 1024;  // items one CTA sorts in shared memory (allocation-free merge)
+constexpr uint32_t SLOT_CAP = 256;  // slots of one bucket in the compile pipeline
+constexpr uint32_t WARP_CAP = 128;  // bucket items one warp merges; larger buckets take a CTA
+constexpr uint32_t SCAN_TILE = 4096;  // bucket aggregates one scan block covers
 
 inline uint32_t sort_tiles(uint32_t n) { return (n + SORT_TILE - 1) / SORT_TILE; }
 inline uint32_t merge_tiles(uint32_t n) { return (n + MERGE_THREADS - 1) / MERGE_THREADS; }
@@ -87,15 +90,32 @@ size_t walk_smem_bytes(uint32_t qpad, uint32_t chunk_cap);
 // Key kernel: one thread per noise record; expands the record into its
 // mechanisms (mdesc, mp), computes each mechanism's 128-bit key, and counts
 // non-empty keys per bucket (top `bucket_bits` bits of key.x).
+// One bucket slot (32 bytes, one sector): the mechanism's 128-bit key, then
+// (mechanism, target count, probability).  The group stage overwrites the
+// second half of a bucket's first slots with one record per group:
+// (head mechanism, targets before the group inside the bucket, probability).
+struct SlotTail {
+  uint32_t m, t;
+  double p;
+};
+static_assert(sizeof(SlotTail) == 16, "slot tail is 16 bytes");
+
 struct KeyLaunch {
   const CircuitDev *circs;  // [n_circ]
   const uint32_t *mbase;    // [n_circ + 1] first mechanism of each circuit (+ total)
   uint32_t n_circ, M;       // circuits, mechanisms of the whole batch
+  uint32_t *blk_r0;         // [key blocks] record of each key block's first mechanism
   ulonglong2 *key;          // [M]
   uint32_t *bucket_count;   // [buckets of the batch] (zeroed)
+  ulonglong2 *skey;         // [buckets * SLOT_CAP] slot keys
+  SlotTail *stail;          // [buckets * SLOT_CAP] slot tails
   uint32_t *list_total;     // += targets written to the lists (for traffic accounting)
   uint32_t *err;
 };
+constexpr uint32_t KEY_THREADS = 256;
+inline uint32_t key_blocks(uint32_t M) { return (M + KEY_THREADS - 1) / KEY_THREADS; }
+// Finds each key block's first record (one thread per block).
+cudaError_t launch_key_prep(const KeyLaunch &L, cudaStream_t s);
 cudaError_t launch_keys(const KeyLaunch &L, cudaStream_t s);
 
 // Exclusive scan of the bucket counts into bucket offsets (+ total at [nb]).
@@ -125,43 +145,44 @@ struct BucketMergeLaunch {
 };
 cudaError_t launch_bucket_merge(const BucketMergeLaunch &L, cudaStream_t s);
 
-// Three-kernel merge of the compile pipeline (no inter-CTA waits):
-//  group: one CTA per bucket sorts its (key, m, p) items, checks collisions,
-//         folds each group's probability and writes per-group records and a
-//         bucket aggregate (groups, targets);
-//  scan:  exclusive scan of the bucket aggregates (one block);
-//  emit:  one CTA per bucket writes its groups' probabilities, offsets and
+// Merge of the compile pipeline (no inter-CTA waits).  The key kernel has put
+// every non-empty mechanism into a slot of its bucket (SLOT_CAP slots per
+// bucket; more raises DEV_FLAG_BIG_BUCKET).
+//  group: one warp per bucket of <= WARP_CAP items (one CTA per larger bucket)
+//         orders its items (by 64 sub-bins on the top bits of the key's second
+//         half, then by (key, m) inside a sub-bin), checks collisions, folds each group's
+//         probability and overwrites the bucket's first slots with one record
+//         per group (head mechanism, probability, targets before it in the
+//         bucket); bucket aggregates (groups, targets) and their per-tile sums;
+//  scan:  exclusive scan of the bucket aggregates, one block per SCAN_TILE
+//         buckets (tile sums give each block its prefix);
+//  emit:  one warp per bucket writes its groups' probabilities, offsets and
 //         target lists to the DEM arrays.
 struct GroupLaunch {
   const uint32_t *tl;       // [M][tcap] batch-wide target lists
   const uint32_t *tn;       // [M]
   uint32_t tcap;
-  const ulonglong2 *bkey;
-  const uint32_t *bm;
-  const double *bp;
+  const ulonglong2 *skey;   // [nb * SLOT_CAP]
+  SlotTail *stail;          // [nb * SLOT_CAP] items, then group records
   const uint32_t *count;    // [nb]
-  const uint32_t *offset;   // [nb + 1]
   uint32_t nb;
-  uint32_t *gm;             // [M] head mechanism of group g of bucket b at offset[b] + g
-  double *gp;               // [M] folded probability
-  uint32_t *gt;             // [M] targets before this group inside its bucket
   uint2 *bagg;              // [nb] (groups, targets) of each bucket
   uint2 *bout;              // [nb] exclusive prefix of bagg
+  uint2 *tsum;              // [ceil(nb / SCAN_TILE)] (zeroed) per-tile sums of bagg
+  uint32_t *big_n;          // (zeroed) buckets with more than WARP_CAP items
+  uint32_t *big_list;       // [nb]
   double *out_prob;
   uint32_t *out_off;
   uint32_t *out_tg;
   uint32_t tg_cap;
-  uint32_t *totals;         // [0] groups, [1] targets
+  uint32_t *totals;         // [0] groups, [1] targets, [3] += bucketed items
   const uint32_t *cbbase;   // [n_circ] first bucket of each circuit
   uint32_t n_circ;
   uint2 *cout;              // [n_circ] (first slot, first target) of each circuit's output
   uint32_t *err;
 };
-// Batch-wide scatter: the bucket of mechanism m is its circuit's bbase + top bits.
-cudaError_t launch_bucket_scatter_p(const CircuitDev *circs, const uint32_t *mbase, uint32_t n_circ,
-                                    const ulonglong2 *key, const double *mp, uint32_t M, const uint32_t *offset,
-                                    uint32_t *cursor, ulonglong2 *bkey, uint32_t *bm, double *bp, cudaStream_t s);
-cudaError_t launch_group_merge(const GroupLaunch &L, cudaStream_t s);
+cudaError_t launch_group(const GroupLaunch &L, cudaStream_t s);
+cudaError_t launch_scan_emit(const GroupLaunch &L, cudaStream_t s);
 
 // ---- global path (used when a bucket is too large for one CTA) -------------
 // Onesweep radix sort of (u64 key, u32 value) pairs on the low `bits` bits.

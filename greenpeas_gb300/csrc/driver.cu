@@ -115,8 +115,8 @@ struct Layout {
   std::vector<CircLayout> c;
   size_t cdev, items, mbase, cbbase;
   size_t in_bytes;
-  size_t mdesc, mp, tl, tn, key, boff, bkey, bm, bp, gm, gp, gt, bagg, bout, cout;
-  size_t zero, err, totals, bcount, bcursor, zero_bytes;
+  size_t mdesc, mp, tl, tn, key, blk_r0, skey, stail, bagg, bout, cout, big_list;
+  size_t zero, err, totals, bcount, tsum, big_n, zero_bytes;
   size_t sk0, sk1, pm0, pm1, hik;  // global path (single circuit)
   size_t gzero, sort_scr, merge_status, merge_ctr, gzero_bytes;
   size_t out_prob, out_off;
@@ -270,21 +270,20 @@ struct gpc_driver {
     L.tl = take((size_t)M * tcap * 4);
     L.tn = take((size_t)M * 4);
     L.key = take((size_t)M * 16);
-    L.boff = take((size_t)(nb + 1) * 4);
-    L.bkey = take((size_t)M * 16);
-    L.bm = take((size_t)M * 4);
-    L.bp = take((size_t)M * 8);
-    L.gm = take((size_t)M * 4);
-    L.gp = take((size_t)M * 8);
-    L.gt = take((size_t)M * 4);
+    L.blk_r0 = take((size_t)gpc::key_blocks((uint32_t)M) * 4);
+    const size_t slots = (size_t)nb * gpc::SLOT_CAP;
+    L.skey = take(slots * 16);
+    L.stail = take(slots * sizeof(gpc::SlotTail));
     L.bagg = take((size_t)nb * 8);
     L.bout = take((size_t)nb * 8);
     L.cout = take((size_t)N * 8);
+    L.big_list = take((size_t)nb * 4);
     L.zero = o;
     L.err = take(4);
     L.totals = take(16);
+    L.big_n = take(4);
     L.bcount = take((size_t)nb * 4);
-    L.bcursor = take((size_t)nb * 4);
+    L.tsum = take(((size_t)nb + gpc::SCAN_TILE - 1) / gpc::SCAN_TILE * 8);
     L.zero_bytes = o - L.zero;
     L.out_prob = take((size_t)M * 8);
     L.out_off = take((size_t)(M + 1) * 4);
@@ -511,7 +510,9 @@ struct gpc_driver {
     ran = true;
   }
 
-  void launch_walks() {
+  // The walks (one launch per class; several classes run on the auxiliary
+  // streams), and meanwhile the key-block table on the main stream.
+  void launch_walks(const gpc::KeyLaunch &kl) {
     const uint32_t nc = (uint32_t)L.classes.size();
     auto one = [&](const WalkClass &wc, cudaStream_t s) {
       gpc::WalkLaunch wl{};
@@ -528,6 +529,7 @@ struct gpc_driver {
       CK(gpc::launch_walk(wl, s));
     };
     if (nc <= 1) {
+      CK(gpc::launch_key_prep(kl, stream));
       if (nc == 1) one(L.classes[0], stream);
       return;
     }
@@ -536,6 +538,7 @@ struct gpc_driver {
     const uint32_t used = std::min<uint32_t>(nc, kAux);
     for (uint32_t a = 0; a < used; ++a) CK(cudaStreamWaitEvent(aux[a], fork_ev, 0));
     for (uint32_t k = 0; k < nc; ++k) one(L.classes[k], aux[k % kAux]);
+    CK(gpc::launch_key_prep(kl, stream));
     for (uint32_t a = 0; a < used; ++a) {
       CK(cudaEventRecord(join_ev[a], aux[a]));
       CK(cudaStreamWaitEvent(stream, join_ev[a], 0));
@@ -546,9 +549,6 @@ struct gpc_driver {
     CK(cudaMemsetAsync(dptr<char>(L.zero), 0, L.zero_bytes, stream));
     for (uint32_t i = 0; i < ncirc(); ++i)
       if (tapes[i].n_epochs == 0) CK(cudaMemsetAsync(dptr<char>(L.c[i].band), 0, (size_t)tapes[i].w * 8, stream));
-    rec(0);
-    launch_walks();
-    rec(1);
     gpc::KeyLaunch kl{};
     kl.circs = dptr<CircuitDev>(L.cdev);
     kl.mbase = dptr<uint32_t>(L.mbase);
@@ -556,40 +556,40 @@ struct gpc_driver {
     kl.M = L.M;
     kl.key = dptr<ulonglong2>(L.key);
     kl.bucket_count = dptr<uint32_t>(L.bcount);
+    kl.blk_r0 = dptr<uint32_t>(L.blk_r0);
+    kl.skey = dptr<ulonglong2>(L.skey);
+    kl.stail = dptr<gpc::SlotTail>(L.stail);
     kl.list_total = dptr<uint32_t>(L.totals) + 2;
     kl.err = dptr<uint32_t>(L.err);
+    rec(0);
+    launch_walks(kl);
+    rec(1);
     CK(gpc::launch_keys(kl, stream));
     rec(2);
     if (ncirc() == 1 && (force_global || lists_off)) {
       run_global(false);
     } else {
-      CK(gpc::launch_bucket_scan(dptr<uint32_t>(L.bcount), dptr<uint32_t>(L.boff), L.nb, stream));
-      CK(gpc::launch_bucket_scatter_p(dptr<CircuitDev>(L.cdev), dptr<uint32_t>(L.mbase), ncirc(),
-                                      dptr<ulonglong2>(L.key), dptr<double>(L.mp), L.M, dptr<uint32_t>(L.boff),
-                                      dptr<uint32_t>(L.bcursor), dptr<ulonglong2>(L.bkey), dptr<uint32_t>(L.bm),
-                                      dptr<double>(L.bp), stream));
+      CK(gpc::launch_group(group_launch(), stream));
       rec(3);
-      launch_bucket_merge_now();
+      CK(gpc::launch_scan_emit(group_launch(), stream));
       rec(4);
     }
   }
 
-  void launch_bucket_merge_now() {
+  gpc::GroupLaunch group_launch() {
     gpc::GroupLaunch gl{};
     gl.tl = dptr<uint32_t>(L.tl);
     gl.tn = dptr<uint32_t>(L.tn);
     gl.tcap = tcap;
-    gl.bkey = dptr<ulonglong2>(L.bkey);
-    gl.bm = dptr<uint32_t>(L.bm);
-    gl.bp = dptr<double>(L.bp);
+    gl.skey = dptr<ulonglong2>(L.skey);
+    gl.stail = dptr<gpc::SlotTail>(L.stail);
     gl.count = dptr<uint32_t>(L.bcount);
-    gl.offset = dptr<uint32_t>(L.boff);
     gl.nb = L.nb;
-    gl.gm = dptr<uint32_t>(L.gm);
-    gl.gp = dptr<double>(L.gp);
-    gl.gt = dptr<uint32_t>(L.gt);
     gl.bagg = dptr<uint2>(L.bagg);
     gl.bout = dptr<uint2>(L.bout);
+    gl.tsum = dptr<uint2>(L.tsum);
+    gl.big_n = dptr<uint32_t>(L.big_n);
+    gl.big_list = dptr<uint32_t>(L.big_list);
     gl.out_prob = dptr<double>(L.out_prob);
     gl.out_off = dptr<uint32_t>(L.out_off);
     gl.out_tg = static_cast<uint32_t *>(tgbuf.p);
@@ -599,7 +599,7 @@ struct gpc_driver {
     gl.n_circ = ncirc();
     gl.cout = dptr<uint2>(L.cout);
     gl.err = dptr<uint32_t>(L.err);
-    CK(gpc::launch_group_merge(gl, stream));
+    return gl;
   }
 
   // Global path (single circuit): sort every mechanism (on sort_bits, or all
@@ -727,7 +727,7 @@ struct gpc_driver {
           reset_merge_scratch();
           launch_merge_now();
         } else {
-          launch_bucket_merge_now();
+          CK(gpc::launch_scan_emit(group_launch(), stream));  // the groups are already formed
         }
         continue;
       }
@@ -739,14 +739,14 @@ struct gpc_driver {
     throw gpc::Error(GPC_ERR_CUDA, "merge did not converge");
   }
 
-  // Algorithmic bytes of each kernel of the last run (walk, key, bucket scan+scatter,
-  // merge): what the design must move, counted from the run's own sizes.
+  // Algorithmic bytes of each stage of the last run (walk, keys, bucket groups,
+  // scan + emit): what the design must move, counted from the run's own sizes.
   void traffic(double out[4]) {
     CK(cudaStreamSynchronize(stream));
     uint32_t tot[4] = {0, 0, 0, 0};
     uint32_t nonempty = 0;
-    CK(cudaMemcpy(tot, dptr<char>(L.totals), 12, cudaMemcpyDeviceToHost));
-    CK(cudaMemcpy(&nonempty, dptr<char>(L.boff) + (size_t)L.nb * 4, 4, cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(tot, dptr<char>(L.totals), 16, cudaMemcpyDeviceToHost));
+    nonempty = tot[3];
     double walk = 0, pts = 0, R = 0;
     for (uint32_t i = 0; i < ncirc(); ++i) {
       const Tape &T = tapes[i];
@@ -763,11 +763,16 @@ struct gpc_driver {
       }
       R += (double)T.rec.size();
     }
-    const double M = L.M, lists = tot[2];
+    const double M = L.M, lists = tot[2], groups = tot[0], targets = tot[1], nb = L.nb;
+    const double per_list = M > 0 ? lists / M : 0.0;
     out[0] = walk;
-    out[1] = R * 20 + 16.0 * pts + M * (16 + 8 + 8 + 4) + 4.0 * lists;
-    out[2] = (double)L.nb * 12 + M * 16 + (double)nonempty * 36;
-    out[3] = (double)nonempty * (28 + 8 + 4) + 8.0 * lists + (double)tot[0] * 12 + (double)tot[1] * 4;
+    // records, snapshot words in the bands, descriptor/probability/key/count, lists, bucket slots
+    out[1] = R * 20 + 16.0 * pts + M * (16 + 8 + 8 + 4) + 4.0 * lists + (double)nonempty * 32;
+    // slots read, lists compared for the non-head items, group records written, counts and aggregates
+    out[2] = (double)nonempty * 32 + (double)(nonempty - std::min<double>(nonempty, groups)) * 8.0 * per_list +
+             groups * 16 + nb * 12;
+    // aggregates and prefixes, group records, head lists gathered and written, DEM probabilities and offsets
+    out[3] = nb * 24 + groups * (16 + 4) + 8.0 * targets + groups * 12;
   }
 
   // Copies the merged arrays of the last run to the host and splits them per circuit.

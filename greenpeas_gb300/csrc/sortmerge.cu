@@ -90,67 +90,159 @@ __constant__ uint8_t kComp[6][15] = {
     {PP(0, 1), PP(0, 3), PP(0, 2), PP(1, 0), PP(1, 1), PP(1, 3), PP(1, 2), PP(3, 0), PP(3, 1), PP(3, 3), PP(3, 2),
      PP(2, 0), PP(2, 1), PP(2, 3), PP(2, 2)},
 };
-__constant__ uint8_t kNComp[6] = {1, 2, 3, 6, 10, 15};
 #undef PP
 
-__global__ void __launch_bounds__(256) key_kernel(KeyLaunch L) {
-  __shared__ uint32_t smb[kMaxCircuitsStaged + 1];
-  __shared__ uint2 sband[1024];
-  __shared__ uint32_t s_c0, s_c1;
-  const bool staged = L.n_circ <= kMaxCircuitsStaged;
-  for (uint32_t i = threadIdx.x; staged && i <= L.n_circ; i += blockDim.x) smb[i] = L.mbase[i];
-  __syncthreads();
-  const uint32_t *mb = staged ? smb : L.mbase;
-  const uint32_t m0 = blockIdx.x * blockDim.x;
-  const uint32_t mg = m0 + threadIdx.x;
-  // the circuits of this block's first and last mechanisms; one circuit: stage its bands
-  if (threadIdx.x == 0) {
-    s_c0 = find_circuit(mb, L.n_circ, m0);
-    s_c1 = find_circuit(mb, L.n_circ, min(L.M - 1, m0 + blockDim.x - 1));
-  }
-  __syncthreads();
-  const uint32_t c0 = s_c0;
-  const bool oneband = s_c0 == s_c1 && L.circs[c0].w <= 1024;
-  if (oneband)
-    for (uint32_t j = threadIdx.x; j < L.circs[c0].w; j += blockDim.x) sband[j] = L.circs[c0].band[j];
-  __syncthreads();
-  if (mg >= L.M) return;
-  const uint32_t c = oneband ? c0 : find_circuit(mb, L.n_circ, mg);
+constexpr uint32_t KEY_MAX_WORDS = 1024;
+
+// Thread per key block: the record holding the block's first mechanism.
+__global__ void key_prep_kernel(KeyLaunch L) {
+  const uint32_t blk = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t m0 = blk * KEY_THREADS;
+  if (m0 >= L.M) return;
+  const uint32_t c = find_circuit(L.mbase, L.n_circ, m0);
   const CircuitDev &C = L.circs[c];
-  const uint32_t m = mg - mb[c];
-  const uint32_t w = C.w;
-  const uint32_t tcap = C.tcap;
-  const uint32_t R = C.R;
-  // the record holding mechanism m: the last r with rec_moff[r] <= m
-  uint32_t lo = 0, hi = R;
+  const uint32_t m = m0 - L.mbase[c];
+  uint32_t lo = 0, hi = C.R;
   while (hi - lo > 1) {
     const uint32_t mid = (lo + hi) >> 1;
     if (__ldg(C.rec_moff + mid) <= m) lo = mid;
     else hi = mid;
   }
-  const uint32_t r = lo;
-  const uint64_t d = __ldg(C.rec + r);
-  const uint32_t ci = m - __ldg(C.rec_moff + r);
-  const uint32_t type = (uint32_t)((d >> 56) & 15u);
-  const uint32_t comp = type == 0 ? (uint32_t)((d >> 60) & 3u) | ((uint32_t)(d >> 62) << 2) : kComp[type][ci];
-  uint32_t pa = (uint32_t)(d & 0x0FFFFFFFu), pb = (uint32_t)((d >> 28) & 0x0FFFFFFFu);
-  uint32_t Pa = comp & 3u, Pb = comp >> 2;
-  if (Pa == 0) {  // a component on point b only is stored with b as its first point
-    pa = pb;
-    Pa = Pb;
-    Pb = 0;
+  L.blk_r0[blk] = lo;
+}
+  // words of a circuit whose bands a key block stages
+
+// One thread per mechanism (global numbering over the batch).  A block whose
+// mechanisms all belong to one circuit stages that circuit's record offsets
+// for its records and culls the circuit's words to those whose band meets the
+// block's snapshot points; each thread then builds its symptom from those
+// words only.  Writes the mechanism's descriptor, probability, 128-bit key,
+// target list, and its item into a slot of its bucket.
+__global__ void __launch_bounds__(KEY_THREADS) key_kernel(KeyLaunch L) {
+  __shared__ uint32_t smb[kMaxCircuitsStaged + 1];
+  __shared__ uint32_t srm[KEY_THREADS + 1];  // rec_moff of the block's records
+  __shared__ uint16_t swd[KEY_MAX_WORDS];     // candidate words, ascending
+  __shared__ uint2 sbd[KEY_MAX_WORDS];        // their bands
+  __shared__ uint32_t s_c0, s_c1, s_r0, s_pmin, s_pmax;
+  __shared__ uint32_t s_wc[KEY_THREADS / 32];
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
+  const bool staged = L.n_circ <= kMaxCircuitsStaged;
+  for (uint32_t i = tid; staged && i <= L.n_circ; i += KEY_THREADS) smb[i] = L.mbase[i];
+  __syncthreads();
+  const uint32_t *mb = staged ? smb : L.mbase;
+  const uint32_t m0 = blockIdx.x * KEY_THREADS;
+  const uint32_t mg = m0 + tid;
+  const bool valid = mg < L.M;
+  if (tid == 0) {
+    s_c0 = find_circuit(mb, L.n_circ, m0);
+    s_c1 = find_circuit(mb, L.n_circ, min(L.M - 1, m0 + KEY_THREADS - 1));
+    s_pmin = 0xFFFFFFFFu;
+    s_pmax = 0;
+    s_r0 = L.blk_r0[blockIdx.x];  // the record holding the block's first mechanism
   }
-  if (Pb == 0) pb = 0;
-  C.mdesc[m] = mk_desc(pa, Pa, pb, Pb);
-  C.mp[m] = __ldg(C.rec_p + r);
+  __syncthreads();
+  const uint32_t c0 = s_c0;
+  const bool one = s_c0 == s_c1;
+  const uint32_t r0 = s_r0;
+  // every record holds at least one mechanism, so the block's records are r0 .. r0 + KEY_THREADS - 1
+  const uint32_t nr = one ? min(KEY_THREADS, L.circs[c0].R - r0) : 0;
+  if (one)
+    for (uint32_t k = tid; k <= nr; k += KEY_THREADS) srm[k] = __ldg(L.circs[c0].rec_moff + r0 + k);
+  __syncthreads();
+
+  const uint32_t c = one ? c0 : (valid ? find_circuit(mb, L.n_circ, mg) : 0u);
+  const CircuitDev &C = L.circs[c];
+  const uint32_t m = valid ? mg - mb[c] : 0u;
+  uint32_t r;
+  if (one) {
+    uint32_t lo = 0, hi = nr;
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (srm[mid] <= m) lo = mid;
+      else hi = mid;
+    }
+    r = r0 + lo;
+  } else {
+    uint32_t lo = 0, hi = C.R;
+    while (hi - lo > 1) {
+      const uint32_t mid = (lo + hi) >> 1;
+      if (__ldg(C.rec_moff + mid) <= m) lo = mid;
+      else hi = mid;
+    }
+    r = lo;
+  }
+  uint32_t pa = 0, pb = 0, Pa = 0, Pb = 0;
+  double prob = 0.0;
+  if (valid) {
+    const uint64_t d = __ldg(C.rec + r);
+    const uint32_t ci = m - (one ? srm[r - r0] : __ldg(C.rec_moff + r));
+    const uint32_t type = (uint32_t)((d >> 56) & 15u);
+    const uint32_t comp = type == 0 ? (uint32_t)((d >> 60) & 3u) | ((uint32_t)(d >> 62) << 2) : kComp[type][ci];
+    pa = (uint32_t)(d & 0x0FFFFFFFu);
+    pb = (uint32_t)((d >> 28) & 0x0FFFFFFFu);
+    Pa = comp & 3u;
+    Pb = comp >> 2;
+    if (Pa == 0) {  // a component on point b only is stored with b as its first point
+      pa = pb;
+      Pa = Pb;
+      Pb = 0;
+    }
+    if (Pb == 0) pb = 0;
+    prob = __ldg(C.rec_p + r);
+    C.mdesc[m] = mk_desc(pa, Pa, pb, Pb);
+    C.mp[m] = prob;
+  }
+  const uint32_t w = C.w;
+  const bool cull = one && w <= KEY_MAX_WORDS;
+  uint32_t nw = 0;
+  if (cull) {
+    // the block's point range
+    uint32_t lo = valid ? (Pb ? min(pa, pb) : pa) : 0xFFFFFFFFu;
+    uint32_t hi = valid ? (Pb ? max(pa, pb) : pa) : 0u;
+    lo = __reduce_min_sync(0xFFFFFFFFu, lo);
+    hi = __reduce_max_sync(0xFFFFFFFFu, hi);
+    if (lane == 0) {
+      atomicMin(&s_pmin, lo);
+      atomicMax(&s_pmax, hi);
+    }
+    __syncthreads();
+    const uint32_t pmin = s_pmin, pmax = s_pmax;
+    // ordered compaction of the words whose band [x, y) meets [pmin, pmax]
+    for (uint32_t j0 = 0; j0 < w; j0 += KEY_THREADS) {
+      const uint32_t j = j0 + tid;
+      uint2 bd = make_uint2(0, 0);
+      bool hit = false;
+      if (j < w) {
+        bd = C.band[j];
+        hit = bd.y > bd.x && bd.x <= pmax && bd.y > pmin;
+      }
+      const uint32_t bal = __ballot_sync(0xFFFFFFFFu, hit);
+      if (lane == 0) s_wc[warp] = __popc(bal);
+      __syncthreads();
+      uint32_t before = nw;
+      for (uint32_t x = 0; x < warp; ++x) before += s_wc[x];
+      if (hit) {
+        const uint32_t pos = before + __popc(bal & ((1u << lane) - 1u));
+        swd[pos] = (uint16_t)j;
+        sbd[pos] = bd;
+      }
+      for (uint32_t x = 0; x < KEY_THREADS / 32; ++x) nw += s_wc[x];
+      __syncthreads();
+    }
+  }
+  if (!valid) return;
+
+  const uint32_t tcap = C.tcap;
   uint64_t hx = 0, hy = 0;
   uint32_t cnt = 0;
   bool nonzero = false;
   uint32_t *out = C.tl + (size_t)m * tcap;
   const ulonglong2 *snap = C.snap;
   const uint32_t np = C.npoints;
-  for (uint32_t j = 0; j < w; ++j) {
-    const uint2 b = oneband ? sband[j] : C.band[j];
+  const uint32_t nloop = cull ? nw : w;
+  for (uint32_t k = 0; k < nloop; ++k) {
+    const uint32_t j = cull ? (uint32_t)swd[k] : k;
+    const uint2 b = cull ? sbd[k] : C.band[k];
     const ulonglong2 *sj = snap + (size_t)j * np;
     uint64_t v = 0;
     if (pa - b.x < b.y - b.x) v = pauli_sel(sj[pa], Pa);
@@ -169,16 +261,27 @@ __global__ void __launch_bounds__(256) key_kernel(KeyLaunch L) {
       }
     }
   }
-  L.key[mg] = make_ulonglong2(hx, hy);
+  const ulonglong2 key = make_ulonglong2(hx, hy);
+  L.key[mg] = key;
   if (tcap) {
     C.tn[m] = cnt;
     if (cnt > tcap) atomicOr(L.err, DEV_FLAG_LONG);
-    if (cnt) atomicAdd(L.list_total, cnt);
+    const uint32_t am = __activemask();
+    const uint32_t tot = __reduce_add_sync(am, cnt);
+    if (lane == (uint32_t)(__ffs(am) - 1) && tot) atomicAdd(L.list_total, tot);
   }
   if ((hx | hy) == 0) {
     if (cnt || (!tcap && nonzero)) atomicOr(L.err, DEV_ERR_COLLISION);  // a non-empty symptom hashed to 0
   } else {
-    atomicAdd(L.bucket_count + C.bbase + (uint32_t)(hx >> (64u - C.bbits)), 1u);
+    const uint32_t b = C.bbase + (uint32_t)(hx >> (64u - C.bbits));
+    const uint32_t slot = atomicAdd(L.bucket_count + b, 1u);
+    if (slot < SLOT_CAP) {
+      const size_t pos = (size_t)b * SLOT_CAP + slot;
+      L.skey[pos] = key;
+      L.stail[pos] = SlotTail{mg, cnt, prob};
+    } else {
+      atomicOr(L.err, DEV_FLAG_BIG_BUCKET);
+    }
   }
 }
 
@@ -218,29 +321,6 @@ __global__ void bucket_scatter_kernel(const ulonglong2 *__restrict__ key, uint32
     const uint32_t pos = offset[b] + atomicAdd(cursor + b, 1u);
     bkey[pos] = k;
     bm[pos] = m;
-  }
-}
-
-__global__ void bucket_scatter_p_kernel(const CircuitDev *__restrict__ circs, const uint32_t *__restrict__ mbase,
-                                        uint32_t n_circ, const ulonglong2 *__restrict__ key,
-                                        const double *__restrict__ mp, uint32_t M,
-                                        const uint32_t *__restrict__ offset, uint32_t *__restrict__ cursor,
-                                        ulonglong2 *__restrict__ bkey, uint32_t *__restrict__ bm,
-                                        double *__restrict__ bp) {
-  __shared__ uint32_t smb[kMaxCircuitsStaged + 1];
-  const bool staged = n_circ <= kMaxCircuitsStaged;
-  for (uint32_t i = threadIdx.x; staged && i <= n_circ; i += blockDim.x) smb[i] = mbase[i];
-  __syncthreads();
-  const uint32_t *mb = staged ? smb : mbase;
-  for (uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < M; m += gridDim.x * blockDim.x) {
-    const ulonglong2 k = key[m];
-    if ((k.x | k.y) == 0) continue;
-    const uint32_t c = n_circ == 1 ? 0u : find_circuit(mb, n_circ, m);
-    const uint32_t b = circs[c].bbase + (uint32_t)(k.x >> (64u - circs[c].bbits));
-    const uint32_t pos = offset[b] + atomicAdd(cursor + b, 1u);
-    bkey[pos] = k;
-    bm[pos] = m;
-    bp[pos] = mp[m];
   }
 }
 
@@ -752,163 +832,366 @@ __global__ void __launch_bounds__(BUCKET_THREADS) bucket_merge_kernel(BucketMerg
   }
 }
 
-// ---- three-kernel merge -----------------------------------------------------
+// ---- merge of the compile pipeline ---------------------------------------
 
-__global__ void __launch_bounds__(BUCKET_THREADS) group_kernel(GroupLaunch L) {
-  constexpr int NT = BUCKET_THREADS;
-  constexpr int NW = NT / 32;
-  __shared__ ulonglong2 sk[BUCKET_CAP];
-  __shared__ uint32_t sm[BUCKET_CAP];
-  __shared__ double sp[BUCKET_CAP];
-  __shared__ uint16_t ord[BUCKET_CAP];
-  __shared__ uint32_t sntg[BUCKET_CAP];  // targets of a group head at a sorted position, else ~0u
-  __shared__ uint32_t wc[NW], wt[NW];
-  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
-  const uint32_t b = blockIdx.x;
-  uint32_t n = L.count[b];
-  const uint32_t base = L.offset[b];
-  if (n > (uint32_t)BUCKET_CAP) {
-    if (threadIdx.x == 0) atomicOr(L.err, DEV_FLAG_BIG_BUCKET);
-    n = 0;
+constexpr uint32_t GW_WARPS = 8;  // buckets per group/emit block (one warp each)
+
+__device__ __forceinline__ bool key_eq(ulonglong2 a, ulonglong2 b) { return a.x == b.x && a.y == b.y; }
+
+// a(1-b) + b(1-a), written as a + b(1-2a): two fused multiply-adds.
+__device__ __forceinline__ double xor_merge(double a, double b) { return fma(b, fma(-2.0, a, 1.0), a); }
+
+// One warp per bucket of at most WARP_CAP items; larger buckets are listed
+// for group_big_kernel.  Items are ordered by sub-bin (top 6 bits of the
+// key's second half), then by (key, m) inside the sub-bin: equal keys end up
+// adjacent in ascending mechanism order, at O(n) work per bucket.
+__global__ void __launch_bounds__(GW_WARPS * 32) group_warp_kernel(GroupLaunch L) {
+  constexpr uint32_t NBIN = 64;
+  __shared__ ulonglong2 s_k[GW_WARPS][WARP_CAP];
+  __shared__ uint32_t s_m[GW_WARPS][WARP_CAP];
+  __shared__ double s_p[GW_WARPS][WARP_CAP];
+  __shared__ uint32_t s_t[GW_WARPS][WARP_CAP];
+  __shared__ uint8_t s_o[GW_WARPS][WARP_CAP];   // sorted position -> item
+  __shared__ uint8_t s_q[GW_WARPS][WARP_CAP];   // item -> place inside its sub-bin (arrival order)
+  __shared__ uint8_t s_x[GW_WARPS][WARP_CAP];   // items grouped by sub-bin
+  __shared__ uint32_t s_h[GW_WARPS][NBIN];      // sub-bin counts, then offsets
+  const uint32_t lane = threadIdx.x & 31u, wi = threadIdx.x >> 5;
+  const uint32_t b = blockIdx.x * GW_WARPS + wi;
+  if (b >= L.nb) return;
+  const uint32_t n = L.count[b];
+  if (n == 0) {
+    if (lane == 0) L.bagg[b] = make_uint2(0, 0);
+    return;
   }
-  for (uint32_t i = threadIdx.x; i < n; i += NT) {
-    sk[i] = L.bkey[base + i];
-    sm[i] = L.bm[base + i];
-    sp[i] = L.bp[base + i];
-  }
-  __syncthreads();
-  // rank sort by (key, m), four comparisons per step
-  for (uint32_t i = threadIdx.x; i < n; i += NT) {
-    const ulonglong2 ki = sk[i];
-    const uint32_t mi = sm[i];
-    uint32_t r = 0;
-    uint32_t k = 0;
-    for (; k + 4 <= n; k += 4) {
-      r += item_less(sk[k], sm[k], ki, mi) ? 1u : 0u;
-      r += item_less(sk[k + 1], sm[k + 1], ki, mi) ? 1u : 0u;
-      r += item_less(sk[k + 2], sm[k + 2], ki, mi) ? 1u : 0u;
-      r += item_less(sk[k + 3], sm[k + 3], ki, mi) ? 1u : 0u;
-    }
-    for (; k < n; ++k) r += item_less(sk[k], sm[k], ki, mi) ? 1u : 0u;
-    ord[r] = (uint16_t)i;
-  }
-  __syncthreads();
-  // group heads, collision checks (full target lists), target counts
-  const uint32_t tcap = L.tcap;
-  for (uint32_t s = threadIdx.x; s < n; s += NT) {
-    const uint32_t i = ord[s];
-    const uint32_t m = sm[i];
-    const uint32_t nt = __ldg(L.tn + m);
-    bool head = true;
-    if (s > 0) {
-      const uint32_t ip = ord[s - 1];
-      if (sk[ip].x == sk[i].x && sk[ip].y == sk[i].y) {
-        head = false;
-        const uint32_t mq = sm[ip];
-        if (__ldg(L.tn + mq) != nt || !lists_equal(L.tl + (size_t)m * tcap, L.tl + (size_t)mq * tcap, nt))
-          atomicOr(L.err, DEV_ERR_COLLISION);
+  if (n > WARP_CAP) {
+    if (lane == 0) {
+      if (n > SLOT_CAP) {
+        atomicOr(L.err, DEV_FLAG_BIG_BUCKET);  // slots overflowed; the run is redone another way
+        L.bagg[b] = make_uint2(0, 0);
+      } else {
+        L.big_list[atomicAdd(L.big_n, 1u)] = b;
       }
     }
-    sntg[s] = head ? nt : ~0u;
+    return;
   }
-  __syncthreads();
-  // compact the heads (block scan over sorted positions, NT at a time) and
-  // write one record per group; fold the run's probabilities left to right
-  uint32_t carry_c = 0, carry_t = 0;
-  for (uint32_t r0 = 0; r0 < n; r0 += NT) {
-    const uint32_t s = r0 + threadIdx.x;
-    const uint32_t v = s < n ? sntg[s] : ~0u;
-    const uint32_t c_in = v != ~0u ? 1u : 0u, t_in = v != ~0u ? v : 0u;
-    uint32_t ic = c_in, it = t_in;
+  ulonglong2 *K = s_k[wi];
+  uint32_t *Mm = s_m[wi], *T = s_t[wi], *H = s_h[wi];
+  double *P = s_p[wi];
+  uint8_t *O = s_o[wi], *Q = s_q[wi], *X = s_x[wi];
+  const size_t base = (size_t)b * SLOT_CAP;
+  H[lane] = 0;
+  H[lane + 32] = 0;
+  __syncwarp();
+  for (uint32_t i = lane; i < n; i += 32) {
+    const ulonglong2 k = L.skey[base + i];
+    const SlotTail t = L.stail[base + i];
+    K[i] = k;
+    Mm[i] = t.m;
+    T[i] = t.t;
+    P[i] = t.p;
+    Q[i] = (uint8_t)atomicAdd(H + (uint32_t)(k.y >> 58), 1u);
+  }
+  __syncwarp();
+  {  // sub-bin offsets: lane owns bins 2*lane and 2*lane + 1
+    const uint32_t c0 = H[2 * lane], c1 = H[2 * lane + 1];
+    uint32_t inc = c0 + c1;
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t a = __shfl_up_sync(0xFFFFFFFFu, ic, o), bb = __shfl_up_sync(0xFFFFFFFFu, it, o);
-      if (lane >= (uint32_t)o) {
-        ic += a;
-        it += bb;
-      }
+      const uint32_t a = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+      if (lane >= (uint32_t)o) inc += a;
     }
-    if (lane == 31) {
-      wc[warp] = ic;
-      wt[warp] = it;
+    const uint32_t ex = inc - c0 - c1;
+    __syncwarp();
+    H[2 * lane] = ex;
+    H[2 * lane + 1] = ex + c0;
+  }
+  __syncwarp();
+  for (uint32_t i = lane; i < n; i += 32) X[H[(uint32_t)(K[i].y >> 58)] + Q[i]] = (uint8_t)i;
+  __syncwarp();
+  for (uint32_t i = lane; i < n; i += 32) {
+    const ulonglong2 ki = K[i];
+    const uint32_t mi = Mm[i];
+    const uint32_t bin = (uint32_t)(ki.y >> 58);
+    const uint32_t lo = H[bin], hi = bin + 1 < NBIN ? H[bin + 1] : n;
+    uint32_t r = lo;
+    for (uint32_t j = lo; j < hi; ++j) {
+      const uint32_t x = X[j];
+      r += item_less(K[x], Mm[x], ki, mi) ? 1u : 0u;
     }
-    __syncthreads();
-    uint32_t pc = carry_c, pt = carry_t;
-    for (uint32_t x = 0; x < warp; ++x) {
-      pc += wc[x];
-      pt += wt[x];
-    }
-    if (c_in) {
-      const uint32_t g = pc + ic - 1;
-      const uint32_t i = ord[s];
-      double p = sp[i];
-      for (uint32_t s2 = s + 1; s2 < n; ++s2) {
-        const uint32_t i2 = ord[s2];
-        if (sk[i2].x != sk[i].x || sk[i2].y != sk[i].y) break;
-        const double q = sp[i2];
-        p = p * (1.0 - q) + q * (1.0 - p);
-      }
-      L.gm[base + g] = sm[i];
-      L.gp[base + g] = p;
-      L.gt[base + g] = pt + it - t_in;
-    }
-    for (uint32_t x = 0; x < (uint32_t)NW; ++x) {
-      carry_c += wc[x];
-      carry_t += wt[x];
-    }
-    __syncthreads();
+    O[r] = (uint8_t)i;
   }
-  if (threadIdx.x == 0) L.bagg[b] = make_uint2(carry_c, carry_t);
-}
-
-// Exclusive scan of the nb bucket aggregates (one block of 1024 threads).
-__global__ void __launch_bounds__(1024) group_scan_kernel(GroupLaunch L) {
-  __shared__ uint32_t pc[1024], pt[1024];
-  const uint32_t t = threadIdx.x, nb = L.nb;
-  const uint32_t per = (nb + 1023) / 1024;
-  const uint32_t lo = min(nb, t * per), hi = min(nb, lo + per);
-  uint32_t c = 0, g = 0;
-  for (uint32_t i = lo; i < hi; ++i) {
-    const uint2 a = L.bagg[i];
-    c += a.x;
-    g += a.y;
-  }
-  pc[t] = c;
-  pt[t] = g;
-  __syncthreads();
-  for (uint32_t off = 1; off < 1024; off <<= 1) {
-    const uint32_t a = t >= off ? pc[t - off] : 0, b = t >= off ? pt[t - off] : 0;
-    __syncthreads();
-    pc[t] += a;
-    pt[t] += b;
-    __syncthreads();
-  }
-  uint32_t rc = pc[t] - c, rt = pt[t] - g;
-  for (uint32_t i = lo; i < hi; ++i) {
-    const uint2 a = L.bagg[i];
-    L.bout[i] = make_uint2(rc, rt);
-    rc += a.x;
-    rt += a.y;
-  }
-  if (t == 1023) {
-    L.totals[0] = pc[1023];
-    L.totals[1] = pt[1023];
-    if (pt[1023] > L.tg_cap) atomicOr(L.err, DEV_FLAG_TG_OVF);
-  }
-  __syncthreads();  // bout written by the whole block
-  for (uint32_t c = t; c < L.n_circ; c += 1024) L.cout[c] = L.bout[L.cbbase[c]];
-}
-
-__global__ void __launch_bounds__(BUCKET_THREADS) emit_kernel(GroupLaunch L) {
-  const uint32_t b = blockIdx.x;
-  const uint2 agg = L.bagg[b], out = L.bout[b];
-  const uint32_t base = L.offset[b];
+  __syncwarp();
+  // Groups, 32 sorted positions at a time.  Each group's probability is a
+  // segmented inclusive scan of the XOR-merge over its run: log2(longest run
+  // in the chunk) shuffle steps with every lane busy (FP64 throughput is
+  // scarce on this part), plus the value carried in from the previous chunk.
+  // The scan is a tree, so its rounding differs from a left-to-right fold by
+  // a few ulps; it is deterministic.
   const uint32_t tcap = L.tcap;
-  for (uint32_t g = threadIdx.x; g < agg.x; g += BUCKET_THREADS) {
+  uint32_t gcount = 0, tcount = 0;
+  double carry = 0.0;
+  for (uint32_t s0 = 0; s0 < n; s0 += 32) {
+    const uint32_t s = s0 + lane;
+    const bool in = s < n;
+    bool head = false;
+    uint32_t i = 0, nt = 0;
+    if (in) {
+      i = O[s];
+      nt = T[i];
+      head = true;
+      if (s > 0) {
+        const uint32_t ip = O[s - 1];
+        if (key_eq(K[ip], K[i])) {
+          head = false;
+          const uint32_t m = Mm[i], mq = Mm[ip];
+          if (T[ip] != nt || !lists_equal(L.tl + (size_t)m * tcap, L.tl + (size_t)mq * tcap, nt))
+            atomicOr(L.err, DEV_ERR_COLLISION);
+        }
+      }
+    }
+    const uint32_t hb = __ballot_sync(0xFFFFFFFFu, head);
+    const uint32_t tv = head ? nt : 0u;
+    uint32_t inc = tv;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t a = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+      if (lane >= (uint32_t)o) inc += a;
+    }
+    // the run of each position: it starts at lane `seg` of this chunk, or
+    // (seg < 0) continues the run open at the end of the previous chunk
+    const uint32_t le = hb & (0xFFFFFFFFu >> (31u - lane));
+    const int seg = le ? 31 - __clz(le) : -1;
+    const uint32_t seg0 = seg < 0 ? 0u : (uint32_t)seg;
+    double x = in ? P[i] : 0.0;
+    const uint32_t maxlen = __reduce_max_sync(0xFFFFFFFFu, in ? lane - seg0 + 1 : 0u);
+    for (uint32_t d = 1; d < maxlen; d <<= 1) {
+      const double y = __shfl_up_sync(0xFFFFFFFFu, x, d);
+      if (lane >= d && lane - d >= seg0) x = xor_merge(y, x);
+    }
+    if (seg < 0) x = xor_merge(carry, x);
+    const uint32_t gh = gcount + __popc(hb & ((1u << lane) - 1u));  // group of a head at this lane
+    // every slot of this bucket was read into shared memory above
+    if (head) {
+      L.stail[base + gh].m = Mm[i];
+      L.stail[base + gh].t = tcount + inc - tv;
+    }
+    if (in && (s + 1 >= n || !key_eq(K[O[s + 1]], K[i]))) {  // the run's last item holds its value
+      const uint32_t g = seg < 0 ? gcount - 1u : gcount + __popc(hb & ((1u << seg0) - 1u));
+      L.stail[base + g].p = x;
+    }
+    carry = __shfl_sync(0xFFFFFFFFu, x, 31);
+    gcount += __popc(hb);
+    tcount += __shfl_sync(0xFFFFFFFFu, inc, 31);
+  }
+  if (lane == 0) {
+    L.bagg[b] = make_uint2(gcount, tcount);
+    atomicAdd(&L.tsum[b / SCAN_TILE].x, gcount);
+    atomicAdd(&L.tsum[b / SCAN_TILE].y, tcount);
+    atomicAdd(L.totals + 3, n);
+  }
+}
+
+// One CTA per listed bucket (WARP_CAP < items <= SLOT_CAP), persistent over the list.
+__global__ void __launch_bounds__(BUCKET_THREADS) group_big_kernel(GroupLaunch L) {
+  constexpr int NT = BUCKET_THREADS;
+  constexpr int NW = NT / 32;
+  __shared__ ulonglong2 sk[SLOT_CAP];
+  __shared__ uint32_t sm[SLOT_CAP];
+  __shared__ double sp[SLOT_CAP];
+  __shared__ uint32_t st[SLOT_CAP];
+  __shared__ uint16_t ord[SLOT_CAP];
+  __shared__ uint32_t sntg[SLOT_CAP];  // targets of a group head at a sorted position, else ~0u
+  __shared__ uint32_t wc[NW], wt[NW];
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  const uint32_t nbig = *L.big_n;
+  const uint32_t tcap = L.tcap;
+  for (uint32_t k = blockIdx.x; k < nbig; k += gridDim.x) {
+    const uint32_t b = L.big_list[k];
+    const uint32_t n = L.count[b];  // WARP_CAP < n <= SLOT_CAP
+    const size_t base = (size_t)b * SLOT_CAP;
+    for (uint32_t i = threadIdx.x; i < n; i += NT) {
+      sk[i] = L.skey[base + i];
+      const SlotTail t = L.stail[base + i];
+      sm[i] = t.m;
+      st[i] = t.t;
+      sp[i] = t.p;
+    }
+    __syncthreads();
+    for (uint32_t i = threadIdx.x; i < n; i += NT) {
+      const ulonglong2 ki = sk[i];
+      const uint32_t mi = sm[i];
+      uint32_t r = 0;
+      for (uint32_t q = 0; q < n; ++q) r += item_less(sk[q], sm[q], ki, mi) ? 1u : 0u;
+      ord[r] = (uint16_t)i;
+    }
+    __syncthreads();
+    for (uint32_t s = threadIdx.x; s < n; s += NT) {
+      const uint32_t i = ord[s];
+      const uint32_t nt = st[i];
+      bool head = true;
+      if (s > 0) {
+        const uint32_t ip = ord[s - 1];
+        if (key_eq(sk[ip], sk[i])) {
+          head = false;
+          if (st[ip] != nt ||
+              !lists_equal(L.tl + (size_t)sm[i] * tcap, L.tl + (size_t)sm[ip] * tcap, nt))
+            atomicOr(L.err, DEV_ERR_COLLISION);
+        }
+      }
+      sntg[s] = head ? nt : ~0u;
+    }
+    __syncthreads();
+    uint32_t carry_c = 0, carry_t = 0;
+    for (uint32_t r0 = 0; r0 < n; r0 += NT) {
+      const uint32_t s = r0 + threadIdx.x;
+      const uint32_t v = s < n ? sntg[s] : ~0u;
+      const uint32_t c_in = v != ~0u ? 1u : 0u, t_in = v != ~0u ? v : 0u;
+      uint32_t ic = c_in, it = t_in;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t a = __shfl_up_sync(0xFFFFFFFFu, ic, o), bb = __shfl_up_sync(0xFFFFFFFFu, it, o);
+        if (lane >= (uint32_t)o) {
+          ic += a;
+          it += bb;
+        }
+      }
+      if (lane == 31) {
+        wc[warp] = ic;
+        wt[warp] = it;
+      }
+      __syncthreads();
+      uint32_t pc = carry_c, pt = carry_t;
+      for (uint32_t x = 0; x < warp; ++x) {
+        pc += wc[x];
+        pt += wt[x];
+      }
+      if (c_in) {
+        const uint32_t g = pc + ic - 1;
+        const uint32_t i = ord[s];
+        double p = sp[i];
+        for (uint32_t s2 = s + 1; s2 < n; ++s2) {
+          const uint32_t i2 = ord[s2];
+          if (!key_eq(sk[i2], sk[i])) break;
+          const double q = sp[i2];
+          p = p * (1.0 - q) + q * (1.0 - p);
+        }
+        L.stail[base + g] = SlotTail{sm[i], pt + it - t_in, p};
+      }
+      for (uint32_t x = 0; x < (uint32_t)NW; ++x) {
+        carry_c += wc[x];
+        carry_t += wt[x];
+      }
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      L.bagg[b] = make_uint2(carry_c, carry_t);
+      atomicAdd(&L.tsum[b / SCAN_TILE].x, carry_c);
+      atomicAdd(&L.tsum[b / SCAN_TILE].y, carry_t);
+      atomicAdd(L.totals + 3, n);
+    }
+    __syncthreads();
+  }
+}
+
+// Block sum of a pair over 1024 threads (result in every thread).
+__device__ __forceinline__ uint2 block_sum1024(uint2 v, uint2 *scratch) {
+  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  v.x = __reduce_add_sync(0xFFFFFFFFu, v.x);
+  v.y = __reduce_add_sync(0xFFFFFFFFu, v.y);
+  if (lane == 0) scratch[warp] = v;
+  __syncthreads();
+  uint2 a = lane < 32 ? scratch[lane] : make_uint2(0, 0);
+  a.x = __reduce_add_sync(0xFFFFFFFFu, a.x);
+  a.y = __reduce_add_sync(0xFFFFFFFFu, a.y);
+  __syncthreads();
+  return a;
+}
+
+// Exclusive scan of the bucket aggregates: block t covers buckets
+// [t * SCAN_TILE, (t + 1) * SCAN_TILE) and starts from the sum of the tile
+// sums before it.  The last block writes the totals.
+__global__ void __launch_bounds__(1024) group_scan_kernel(GroupLaunch L) {
+  __shared__ uint2 red[32];
+  __shared__ uint2 wsum[32];
+  const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
+  const uint32_t tile = blockIdx.x;
+  uint2 pre = make_uint2(0, 0);
+  for (uint32_t k = t; k < tile; k += 1024) {
+    const uint2 a = L.tsum[k];
+    pre.x += a.x;
+    pre.y += a.y;
+  }
+  pre = block_sum1024(pre, red);
+  constexpr uint32_t PER = SCAN_TILE / 1024;
+  const uint32_t i0 = tile * SCAN_TILE + t * PER;
+  uint2 v[PER];
+  uint2 loc = make_uint2(0, 0);
+#pragma unroll
+  for (uint32_t k = 0; k < PER; ++k) {
+    v[k] = i0 + k < L.nb ? L.bagg[i0 + k] : make_uint2(0, 0);
+    loc.x += v[k].x;
+    loc.y += v[k].y;
+  }
+  // exclusive scan of loc over the block
+  uint2 inc = loc;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const uint32_t ax = __shfl_up_sync(0xFFFFFFFFu, inc.x, o), ay = __shfl_up_sync(0xFFFFFFFFu, inc.y, o);
+    if (lane >= (uint32_t)o) {
+      inc.x += ax;
+      inc.y += ay;
+    }
+  }
+  if (lane == 31) wsum[warp] = inc;
+  __syncthreads();
+  if (warp == 0) {
+    uint2 x = wsum[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t ax = __shfl_up_sync(0xFFFFFFFFu, x.x, o), ay = __shfl_up_sync(0xFFFFFFFFu, x.y, o);
+      if (lane >= (uint32_t)o) {
+        x.x += ax;
+        x.y += ay;
+      }
+    }
+    wsum[lane] = x;  // inclusive prefix over warps
+  }
+  __syncthreads();
+  uint2 run = make_uint2(pre.x + inc.x - loc.x, pre.y + inc.y - loc.y);
+  if (warp > 0) {
+    run.x += wsum[warp - 1].x;
+    run.y += wsum[warp - 1].y;
+  }
+#pragma unroll
+  for (uint32_t k = 0; k < PER; ++k) {
+    if (i0 + k < L.nb) L.bout[i0 + k] = run;
+    run.x += v[k].x;
+    run.y += v[k].y;
+  }
+  if (tile == gridDim.x - 1 && t == 1023) {
+    L.totals[0] = run.x;
+    L.totals[1] = run.y;
+    if (run.y > L.tg_cap) atomicOr(L.err, DEV_FLAG_TG_OVF);
+  }
+}
+
+// One warp per bucket: the bucket's groups to the DEM arrays.  Block 0 also
+// writes each circuit's first output slot and target.
+__global__ void __launch_bounds__(GW_WARPS * 32) emit_kernel(GroupLaunch L) {
+  if (blockIdx.x == 0)
+    for (uint32_t c = threadIdx.x; c < L.n_circ; c += GW_WARPS * 32) L.cout[c] = L.bout[L.cbbase[c]];
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t b = blockIdx.x * GW_WARPS + (threadIdx.x >> 5);
+  if (b >= L.nb) return;
+  const uint2 agg = L.bagg[b], out = L.bout[b];
+  const size_t base = (size_t)b * SLOT_CAP;
+  const uint32_t tcap = L.tcap;
+  for (uint32_t g = lane; g < agg.x; g += 32) {
     const uint32_t slot = out.x + g;
-    const uint32_t toff = out.y + L.gt[base + g];
-    const uint32_t m = L.gm[base + g];
-    L.out_prob[slot] = L.gp[base + g];
+    const SlotTail t = L.stail[base + g];
+    const uint32_t toff = out.y + t.t;
+    const uint32_t m = t.m;
+    L.out_prob[slot] = t.p;
     L.out_off[slot] = toff;
     const uint32_t ntg = __ldg(L.tn + m);
     if (toff + ntg <= L.tg_cap) {
@@ -927,11 +1210,16 @@ __global__ void __launch_bounds__(BUCKET_THREADS) emit_kernel(GroupLaunch L) {
 
 }  // namespace
 
+cudaError_t launch_key_prep(const KeyLaunch &L, cudaStream_t s) {
+  if (L.M == 0) return cudaSuccess;
+  const uint32_t nblk = key_blocks(L.M);
+  key_prep_kernel<<<(nblk + 127) / 128, 128, 0, s>>>(L);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_keys(const KeyLaunch &L, cudaStream_t s) {
   if (L.M == 0) return cudaSuccess;
-  const uint32_t threads = 256;
-  const uint32_t blocks = (L.M + threads - 1) / threads;
-  key_kernel<<<blocks, threads, 0, s>>>(L);
+  key_kernel<<<key_blocks(L.M), KEY_THREADS, 0, s>>>(L);
   return cudaGetLastError();
 }
 
@@ -949,21 +1237,17 @@ cudaError_t launch_bucket_scatter(const ulonglong2 *key, uint32_t M, uint32_t bu
   return cudaGetLastError();
 }
 
-cudaError_t launch_bucket_scatter_p(const CircuitDev *circs, const uint32_t *mbase, uint32_t n_circ,
-                                    const ulonglong2 *key, const double *mp, uint32_t M, const uint32_t *offset,
-                                    uint32_t *cursor, ulonglong2 *bkey, uint32_t *bm, double *bp, cudaStream_t s) {
-  if (M == 0) return cudaSuccess;
-  uint32_t blocks = (M + 255) / 256;
-  if (blocks > 152u * 16u) blocks = 152u * 16u;
-  bucket_scatter_p_kernel<<<blocks, 256, 0, s>>>(circs, mbase, n_circ, key, mp, M, offset, cursor, bkey, bm, bp);
+cudaError_t launch_group(const GroupLaunch &L, cudaStream_t s) {
+  if (L.nb == 0) return cudaSuccess;
+  group_warp_kernel<<<(L.nb + GW_WARPS - 1) / GW_WARPS, GW_WARPS * 32, 0, s>>>(L);
+  group_big_kernel<<<2 * 152, BUCKET_THREADS, 0, s>>>(L);
   return cudaGetLastError();
 }
 
-cudaError_t launch_group_merge(const GroupLaunch &L, cudaStream_t s) {
+cudaError_t launch_scan_emit(const GroupLaunch &L, cudaStream_t s) {
   if (L.nb == 0) return cudaSuccess;
-  group_kernel<<<L.nb, BUCKET_THREADS, 0, s>>>(L);
-  group_scan_kernel<<<1, 1024, 0, s>>>(L);
-  emit_kernel<<<L.nb, BUCKET_THREADS, 0, s>>>(L);
+  group_scan_kernel<<<(L.nb + SCAN_TILE - 1) / SCAN_TILE, 1024, 0, s>>>(L);
+  emit_kernel<<<(L.nb + GW_WARPS - 1) / GW_WARPS, GW_WARPS * 32, 0, s>>>(L);
   return cudaGetLastError();
 }
 

@@ -1,0 +1,70 @@
+"""Seeded synthetic workloads: the batch of mixed-size surface codes and the serving mix.
+
+Batch (seed 0, 256 circuits): rotated surface-code memory-Z with d drawn
+uniformly from {3, 5, ..., 21} and rounds = d; time-varying uniform noise --
+every channel instance (one per tick and gate class, i.e. per noise
+instruction) draws its own p log-uniform in [1e-4, 1e-2]; every round takes
+the basis-switch branch (its Z-check CNOT layers run before its X-check
+layers) independently with probability 0.1.
+
+Serving (seed 2): 50% surface memory with d uniform in {5, ..., 25}, rounds =
+d; 50% bivariate-bicycle memory drawn equally from [[72,12,6]],
+[[144,12,12]], [[288,12,18]] with rounds = d; each circuit with one p
+log-uniform in [1e-4, 1e-2] (uniform noise); Poisson arrival times at a given
+rate.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+
+from .codes import BBCode, SurfaceCode
+
+_surface_cache: dict = {}
+_bb_cache: dict = {}
+
+
+def _surface(d):
+    if d not in _surface_cache:
+        _surface_cache[d] = SurfaceCode(d)
+    return _surface_cache[d]
+
+
+def _bb(d):
+    if d not in _bb_cache:
+        _bb_cache[d] = BBCode(d)
+    return _bb_cache[d]
+
+
+def batch_surface(n: int = 256, seed: int = 0, switch_prob: float = 0.1, p_lo: float = 1e-4,
+                  p_hi: float = 1e-2, distances=tuple(range(3, 23, 2))) -> list[str]:
+    """The mixed-size surface-code batch with time-varying noise and basis-switch branches."""
+    rng = np.random.default_rng(seed)
+    ds = rng.choice(np.array(distances), size=n)
+    lo, hi = np.log10(p_lo), np.log10(p_hi)
+    out = []
+    for d in ds:
+        d = int(d)
+        switch = [r for r in range(d) if rng.random() < switch_prob]
+        out.append(_surface(d).get_memory(d, 1e-3, noise="uniform",
+                                          p_sampler=lambda: float(10 ** rng.uniform(lo, hi)),
+                                          switch_rounds=switch))
+    return out
+
+
+def serving_mix(n: int, rate_hz: float, seed: int = 2, p_lo: float = 1e-4, p_hi: float = 1e-2):
+    """n requests: (arrival time in s, circuit text) with Poisson arrivals at rate_hz."""
+    rng = np.random.default_rng(seed)
+    lo, hi = np.log10(p_lo), np.log10(p_hi)
+    t = np.cumsum(rng.exponential(1.0 / rate_hz, size=n))
+    out = []
+    for i in range(n):
+        p = float(10 ** rng.uniform(lo, hi))
+        if rng.random() < 0.5:
+            d = int(rng.choice(np.arange(5, 26, 2)))
+            text = _surface(d).get_memory(d, p, noise="uniform")
+        else:
+            d = int(rng.choice([6, 12, 18]))
+            text = _bb(d).get_memory(d, p, noise="uniform")
+        out.append((float(t[i]), text))
+    return out

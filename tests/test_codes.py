@@ -56,3 +56,23 @@ def test_uniform_noise_counts():
     res = O.compile_text(text, 2)
     assert res.num_raw == 15 * 4 * d * (d - 1) * r + 3 * d * d * r + 2 * ((d * d - 1) * r + d * d)
     assert res.num_qubits == 2 * d * d - 1 and res.num_detectors == r * (d * d - 1)
+
+
+def test_time_varying_noise_and_switch_rounds():
+    from greenpeas_gb300.workloads import batch_surface, serving_mix
+    code = SurfaceCode(3)
+    base = code.get_memory(3, 1e-3, noise="uniform")
+    ps = iter([1e-4 * (k + 1) for k in range(1000)])
+    tv = code.get_memory(3, 1e-3, noise="uniform", p_sampler=lambda: next(ps))
+    assert base.count("\n") == tv.count("\n") and base != tv
+    # one draw per noise instruction
+    n_noise = sum(1 for ln in base.splitlines() if ln.startswith(("X_ERROR", "DEPOLARIZE")))
+    assert next(ps) == pytest.approx(1e-4 * (n_noise + 1))
+    sw = code.get_memory(3, 1e-3, noise="uniform", switch_rounds=[1])
+    assert sorted(sw.splitlines()) == sorted(base.splitlines()) and sw != base
+    with pytest.raises(ValueError):
+        code.get_memory(3, 1e-3, p_sampler=lambda: 1e-3)
+    a, b = batch_surface(n=4, distances=(3, 5)), batch_surface(n=4, distances=(3, 5))
+    assert a == b  # seeded
+    mix = serving_mix(6, rate_hz=100.0)
+    assert len(mix) == 6 and all(t1 <= t2 for (t1, _), (t2, _) in zip(mix, mix[1:]))

@@ -59,3 +59,14 @@ def test_batch_falls_back_per_circuit():
     out = gp.get_driver(circs[0]).compile_batch(circs)
     for text, dem in zip(circs, out):
         compare_errors(dict(dem.errors()), dict(O.compile_text(text, 2).errors()), rel=1e-12)
+
+
+def test_time_varying_switched_batch_matches_oracle():
+    """Small slice of the mixed batch workload (per-instruction p, basis-switch rounds) against the oracle."""
+    from greenpeas_gb300.workloads import batch_surface
+    circs = batch_surface(n=12, seed=5, switch_prob=0.5, distances=(3, 5, 7))
+    out = gp.get_driver(circs[0]).compile_batch(circs)
+    for text, dem in zip(circs, out):
+        ref = O.compile_text(text, 2)
+        assert dem.num_detectors == ref.num_detectors
+        compare_errors(dict(dem.errors()), dict(ref.errors()), rel=1e-12)

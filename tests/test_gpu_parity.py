@@ -85,7 +85,8 @@ def test_bucket_and_global_paths_agree():
     text = gp.BBCode(6).get_memory(6, 1e-3, noise="uniform")
     a = gp.get_driver(text).compile(text)
     b = gp.get_driver(text, global_sort=True).compile(text)
-    assert a.canonical() == b.canonical() or a.approx_equals(b, rtol=1e-15)
+    # the bucket path folds runs as a tree, the global path left to right: a few ulps apart
+    assert a.canonical() == b.canonical() or a.approx_equals(b, rtol=1e-13)
 
 
 def test_empty_and_noiseless():
