@@ -29,6 +29,7 @@ struct CircuitDev {
   const uint32_t *inj_hi;     // [w] last epoch injecting into word j
   ulonglong2 *snap;           // [w][npoints] (X row, Z row) at each point
   uint2 *band;                // [w] point range written by the walk of word j
+  unsigned long long *nzm;    // [npoints][mw] (zeroed) bit j: word j's rows at the point are non-zero
   const uint64_t *rec;        // [R] noise records
   const double *rec_p;        // [R]
   const uint32_t *rec_moff;   // [R + 1]
@@ -42,7 +43,7 @@ struct CircuitDev {
   uint32_t n_chunks, chunk_cap;
   uint32_t mbase;             // first mechanism of this circuit in the batch-wide arrays
   uint32_t bbase, bbits;      // first bucket of this circuit, log2 of its bucket count
-  uint32_t pad_;
+  uint32_t mw;                // 64-bit mask words per point: ceil(w / 64)
 };
 
 constexpr uint32_t kMaxCircuitsStaged = 2048;  // batch tables staged in shared memory up to this size
@@ -104,7 +105,7 @@ struct KeyLaunch {
   const CircuitDev *circs;  // [n_circ]
   const uint32_t *mbase;    // [n_circ + 1] first mechanism of each circuit (+ total)
   uint32_t n_circ, M;       // circuits, mechanisms of the whole batch
-  uint32_t *blk_r0;         // [key blocks] record of each key block's first mechanism
+  uint2 *blk_info;          // [key blocks] (record of the block's first mechanism, its circuit | spans << 31)
   ulonglong2 *key;          // [M]
   uint32_t *bucket_count;   // [buckets of the batch] (zeroed)
   ulonglong2 *skey;         // [buckets * SLOT_CAP] slot keys

@@ -100,7 +100,7 @@ struct HostBuf {
 // Byte offsets of one circuit's input arrays inside the arena.
 struct CircLayout {
   size_t ops, ep_opoff, ep_k, ep_ptoff, ep_chunk, ch_off, ch_bytes, inj_lo, inj_hi, rec, rec_p, rec_moff;
-  size_t snap, band;
+  size_t snap, band, nzm;
   uint32_t mbase, bbase, bbits;
 };
 
@@ -270,7 +270,7 @@ struct gpc_driver {
     L.tl = take((size_t)M * tcap * 4);
     L.tn = take((size_t)M * 4);
     L.key = take((size_t)M * 16);
-    L.blk_r0 = take((size_t)gpc::key_blocks((uint32_t)M) * 4);
+    L.blk_r0 = take((size_t)gpc::key_blocks((uint32_t)M) * 8);
     const size_t slots = (size_t)nb * gpc::SLOT_CAP;
     L.skey = take(slots * 16);
     L.stail = take(slots * sizeof(gpc::SlotTail));
@@ -284,6 +284,8 @@ struct gpc_driver {
     L.big_n = take(4);
     L.bcount = take((size_t)nb * 4);
     L.tsum = take(((size_t)nb + gpc::SCAN_TILE - 1) / gpc::SCAN_TILE * 8);
+    for (uint32_t i = 0; i < N; ++i)
+      L.c[i].nzm = take((size_t)tapes[i].npoints * ((tapes[i].w + 63) / 64) * 8);
     L.zero_bytes = o - L.zero;
     L.out_prob = take((size_t)M * 8);
     L.out_off = take((size_t)(M + 1) * 4);
@@ -365,6 +367,8 @@ struct gpc_driver {
       c.inj_hi = dptr<uint32_t>(l.inj_hi);
       c.snap = dptr<ulonglong2>(l.snap);
       c.band = dptr<uint2>(l.band);
+      c.nzm = dptr<unsigned long long>(l.nzm);
+      c.mw = (T.w + 63) / 64;
       c.rec = dptr<uint64_t>(l.rec);
       c.rec_p = dptr<double>(l.rec_p);
       c.rec_moff = dptr<uint32_t>(l.rec_moff);
@@ -468,10 +472,14 @@ struct gpc_driver {
     mix(tcap);
     mix((uint64_t)force_global);
     mix((uint64_t)lists_off);
+    mix(L.in_bytes);
+    mix(L.zero_bytes);
     for (const auto &c : L.classes) {
       mix(c.qpad);
       mix(c.n_items);
       mix(c.chunk_cap);
+      mix(c.max_epochs);
+      mix(c.max_chunks);
     }
     cfg_sig = h;
     prepared = true;
@@ -556,7 +564,7 @@ struct gpc_driver {
     kl.M = L.M;
     kl.key = dptr<ulonglong2>(L.key);
     kl.bucket_count = dptr<uint32_t>(L.bcount);
-    kl.blk_r0 = dptr<uint32_t>(L.blk_r0);
+    kl.blk_info = dptr<uint2>(L.blk_r0);
     kl.skey = dptr<ulonglong2>(L.skey);
     kl.stail = dptr<gpc::SlotTail>(L.stail);
     kl.list_total = dptr<uint32_t>(L.totals) + 2;

@@ -92,14 +92,14 @@ __constant__ uint8_t kComp[6][15] = {
 };
 #undef PP
 
-constexpr uint32_t KEY_MAX_WORDS = 1024;
-
-// Thread per key block: the record holding the block's first mechanism.
+// Thread per key block: the record holding the block's first mechanism, the
+// block's circuit, and whether the block spans more than one circuit.
 __global__ void key_prep_kernel(KeyLaunch L) {
   const uint32_t blk = blockIdx.x * blockDim.x + threadIdx.x;
   const uint32_t m0 = blk * KEY_THREADS;
   if (m0 >= L.M) return;
   const uint32_t c = find_circuit(L.mbase, L.n_circ, m0);
+  const uint32_t c1 = find_circuit(L.mbase, L.n_circ, min(L.M - 1, m0 + KEY_THREADS - 1));
   const CircuitDev &C = L.circs[c];
   const uint32_t m = m0 - L.mbase[c];
   uint32_t lo = 0, hi = C.R;
@@ -108,51 +108,32 @@ __global__ void key_prep_kernel(KeyLaunch L) {
     if (__ldg(C.rec_moff + mid) <= m) lo = mid;
     else hi = mid;
   }
-  L.blk_r0[blk] = lo;
+  L.blk_info[blk] = make_uint2(lo, c | (c1 != c ? 0x80000000u : 0u));
 }
-  // words of a circuit whose bands a key block stages
 
-// One thread per mechanism (global numbering over the batch).  A block whose
-// mechanisms all belong to one circuit stages that circuit's record offsets
-// for its records and culls the circuit's words to those whose band meets the
-// block's snapshot points; each thread then builds its symptom from those
-// words only.  Writes the mechanism's descriptor, probability, 128-bit key,
-// target list, and its item into a slot of its bucket.
+// One thread per mechanism (global numbering over the batch).  Writes the
+// mechanism's descriptor, probability, 128-bit key, target list, and its item
+// into a slot of its bucket.  The symptom's words are the words set in the
+// non-zero masks of the mechanism's points (ascending); a block inside one
+// circuit finds its mechanisms' records in shared memory.
 __global__ void __launch_bounds__(KEY_THREADS) key_kernel(KeyLaunch L) {
-  __shared__ uint32_t smb[kMaxCircuitsStaged + 1];
   __shared__ uint32_t srm[KEY_THREADS + 1];  // rec_moff of the block's records
-  __shared__ uint16_t swd[KEY_MAX_WORDS];     // candidate words, ascending
-  __shared__ uint2 sbd[KEY_MAX_WORDS];        // their bands
-  __shared__ uint32_t s_c0, s_c1, s_r0, s_pmin, s_pmax;
-  __shared__ uint32_t s_wc[KEY_THREADS / 32];
-  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
-  const bool staged = L.n_circ <= kMaxCircuitsStaged;
-  for (uint32_t i = tid; staged && i <= L.n_circ; i += KEY_THREADS) smb[i] = L.mbase[i];
-  __syncthreads();
-  const uint32_t *mb = staged ? smb : L.mbase;
+  const uint32_t tid = threadIdx.x, lane = tid & 31u;
   const uint32_t m0 = blockIdx.x * KEY_THREADS;
   const uint32_t mg = m0 + tid;
-  const bool valid = mg < L.M;
-  if (tid == 0) {
-    s_c0 = find_circuit(mb, L.n_circ, m0);
-    s_c1 = find_circuit(mb, L.n_circ, min(L.M - 1, m0 + KEY_THREADS - 1));
-    s_pmin = 0xFFFFFFFFu;
-    s_pmax = 0;
-    s_r0 = L.blk_r0[blockIdx.x];  // the record holding the block's first mechanism
-  }
-  __syncthreads();
-  const uint32_t c0 = s_c0;
-  const bool one = s_c0 == s_c1;
-  const uint32_t r0 = s_r0;
+  const uint2 info = L.blk_info[blockIdx.x];
+  const uint32_t r0 = info.x, c0 = info.y & 0x7FFFFFFFu;
+  const bool one = (info.y >> 31) == 0;
   // every record holds at least one mechanism, so the block's records are r0 .. r0 + KEY_THREADS - 1
   const uint32_t nr = one ? min(KEY_THREADS, L.circs[c0].R - r0) : 0;
   if (one)
     for (uint32_t k = tid; k <= nr; k += KEY_THREADS) srm[k] = __ldg(L.circs[c0].rec_moff + r0 + k);
   __syncthreads();
+  if (mg >= L.M) return;
 
-  const uint32_t c = one ? c0 : (valid ? find_circuit(mb, L.n_circ, mg) : 0u);
+  const uint32_t c = one ? c0 : find_circuit(L.mbase, L.n_circ, mg);
   const CircuitDev &C = L.circs[c];
-  const uint32_t m = valid ? mg - mb[c] : 0u;
+  const uint32_t m = mg - __ldg(L.mbase + c);
   uint32_t r;
   if (one) {
     uint32_t lo = 0, hi = nr;
@@ -171,66 +152,21 @@ __global__ void __launch_bounds__(KEY_THREADS) key_kernel(KeyLaunch L) {
     }
     r = lo;
   }
-  uint32_t pa = 0, pb = 0, Pa = 0, Pb = 0;
-  double prob = 0.0;
-  if (valid) {
-    const uint64_t d = __ldg(C.rec + r);
-    const uint32_t ci = m - (one ? srm[r - r0] : __ldg(C.rec_moff + r));
-    const uint32_t type = (uint32_t)((d >> 56) & 15u);
-    const uint32_t comp = type == 0 ? (uint32_t)((d >> 60) & 3u) | ((uint32_t)(d >> 62) << 2) : kComp[type][ci];
-    pa = (uint32_t)(d & 0x0FFFFFFFu);
-    pb = (uint32_t)((d >> 28) & 0x0FFFFFFFu);
-    Pa = comp & 3u;
-    Pb = comp >> 2;
-    if (Pa == 0) {  // a component on point b only is stored with b as its first point
-      pa = pb;
-      Pa = Pb;
-      Pb = 0;
-    }
-    if (Pb == 0) pb = 0;
-    prob = __ldg(C.rec_p + r);
-    C.mdesc[m] = mk_desc(pa, Pa, pb, Pb);
-    C.mp[m] = prob;
+  const uint64_t d = __ldg(C.rec + r);
+  const uint32_t ci = m - (one ? srm[r - r0] : __ldg(C.rec_moff + r));
+  const uint32_t type = (uint32_t)((d >> 56) & 15u);
+  const uint32_t comp = type == 0 ? (uint32_t)((d >> 60) & 3u) | ((uint32_t)(d >> 62) << 2) : kComp[type][ci];
+  uint32_t pa = (uint32_t)(d & 0x0FFFFFFFu), pb = (uint32_t)((d >> 28) & 0x0FFFFFFFu);
+  uint32_t Pa = comp & 3u, Pb = comp >> 2;
+  if (Pa == 0) {  // a component on point b only is stored with b as its first point
+    pa = pb;
+    Pa = Pb;
+    Pb = 0;
   }
-  const uint32_t w = C.w;
-  const bool cull = one && w <= KEY_MAX_WORDS;
-  uint32_t nw = 0;
-  if (cull) {
-    // the block's point range
-    uint32_t lo = valid ? (Pb ? min(pa, pb) : pa) : 0xFFFFFFFFu;
-    uint32_t hi = valid ? (Pb ? max(pa, pb) : pa) : 0u;
-    lo = __reduce_min_sync(0xFFFFFFFFu, lo);
-    hi = __reduce_max_sync(0xFFFFFFFFu, hi);
-    if (lane == 0) {
-      atomicMin(&s_pmin, lo);
-      atomicMax(&s_pmax, hi);
-    }
-    __syncthreads();
-    const uint32_t pmin = s_pmin, pmax = s_pmax;
-    // ordered compaction of the words whose band [x, y) meets [pmin, pmax]
-    for (uint32_t j0 = 0; j0 < w; j0 += KEY_THREADS) {
-      const uint32_t j = j0 + tid;
-      uint2 bd = make_uint2(0, 0);
-      bool hit = false;
-      if (j < w) {
-        bd = C.band[j];
-        hit = bd.y > bd.x && bd.x <= pmax && bd.y > pmin;
-      }
-      const uint32_t bal = __ballot_sync(0xFFFFFFFFu, hit);
-      if (lane == 0) s_wc[warp] = __popc(bal);
-      __syncthreads();
-      uint32_t before = nw;
-      for (uint32_t x = 0; x < warp; ++x) before += s_wc[x];
-      if (hit) {
-        const uint32_t pos = before + __popc(bal & ((1u << lane) - 1u));
-        swd[pos] = (uint16_t)j;
-        sbd[pos] = bd;
-      }
-      for (uint32_t x = 0; x < KEY_THREADS / 32; ++x) nw += s_wc[x];
-      __syncthreads();
-    }
-  }
-  if (!valid) return;
+  if (Pb == 0) pb = 0;
+  const double prob = __ldg(C.rec_p + r);
+  C.mdesc[m] = mk_desc(pa, Pa, pb, Pb);
+  C.mp[m] = prob;
 
   const uint32_t tcap = C.tcap;
   uint64_t hx = 0, hy = 0;
@@ -238,26 +174,32 @@ __global__ void __launch_bounds__(KEY_THREADS) key_kernel(KeyLaunch L) {
   bool nonzero = false;
   uint32_t *out = C.tl + (size_t)m * tcap;
   const ulonglong2 *snap = C.snap;
-  const uint32_t np = C.npoints;
-  const uint32_t nloop = cull ? nw : w;
-  for (uint32_t k = 0; k < nloop; ++k) {
-    const uint32_t j = cull ? (uint32_t)swd[k] : k;
-    const uint2 b = cull ? sbd[k] : C.band[k];
-    const ulonglong2 *sj = snap + (size_t)j * np;
-    uint64_t v = 0;
-    if (pa - b.x < b.y - b.x) v = pauli_sel(sj[pa], Pa);
-    if (Pb && pb - b.x < b.y - b.x) v ^= pauli_sel(sj[pb], Pb);
-    if (!v) continue;
-    nonzero = true;
-    const ulonglong2 h = word_hash(j, v);
-    hx ^= h.x;
-    hy ^= h.y;
-    if (tcap) {
-      uint64_t x = v;
-      while (x) {
-        if (cnt < tcap) out[cnt] = j * 64u + (uint32_t)(__ffsll((long long)x) - 1);
-        ++cnt;
-        x &= x - 1;
+  const uint32_t np = C.npoints, mw = C.mw;
+  const unsigned long long *ma = C.nzm + (size_t)pa * mw, *mb = C.nzm + (size_t)pb * mw;
+  for (uint32_t i = 0; i < mw; ++i) {
+    // a point's snapshot of word j exists only where its own bit is set
+    const uint64_t ba = __ldg(ma + i), bb = Pb ? __ldg(mb + i) : 0ull;
+    uint64_t bits = ba | bb;
+    while (bits) {
+      const uint32_t bit = (uint32_t)(__ffsll((long long)bits) - 1);
+      const uint32_t j = i * 64u + bit;
+      bits &= bits - 1;
+      const ulonglong2 *sj = snap + (size_t)j * np;
+      uint64_t v = 0;
+      if ((ba >> bit) & 1ull) v = pauli_sel(sj[pa], Pa);
+      if ((bb >> bit) & 1ull) v ^= pauli_sel(sj[pb], Pb);
+      if (!v) continue;
+      nonzero = true;
+      const ulonglong2 h = word_hash(j, v);
+      hx ^= h.x;
+      hy ^= h.y;
+      if (tcap) {
+        uint64_t x = v;
+        while (x) {
+          if (cnt < tcap) out[cnt] = j * 64u + (uint32_t)(__ffsll((long long)x) - 1);
+          ++cnt;
+          x &= x - 1;
+        }
       }
     }
   }

@@ -24,7 +24,9 @@
 //   4. ops: one-qubit Cliffords, two-qubit Cliffords (partner rows from the
 //      published buffer), resets, measurements (XOR in the measurement's bits
 //      that fall in word j; the bits ride in the tape itself), snapshots of
-//      (X, Z) at noise points.
+//      (X, Z) at noise points; a non-zero snapshot also sets word j's bit in
+//      the point's mask (an atomic OR), so later stages visit only the
+//      non-zero words of a point.
 // The epoch and chunk tables are staged in shared memory at start, so no
 // global load sits on the per-epoch critical path.
 #include <cstdint>
@@ -181,6 +183,10 @@ __global__ void __launch_bounds__(1024) walk_kernel(const CircuitDev *__restrict
 
   ulonglong2 *snap_j = C.snap + (size_t)j * C.npoints;
   const uint32_t jlo = j * 64u;
+  // non-zero mask of each point: this word's bit in mask word j / 64
+  unsigned long long *nzm_j = C.nzm + (j >> 6);
+  const uint32_t mw = C.mw;
+  const unsigned long long jbit = 1ull << (j & 63u);
   bool timed_out = false;
   uint32_t e = e0;
   uint32_t seq = 0;
@@ -225,7 +231,6 @@ __global__ void __launch_bounds__(1024) walk_kernel(const CircuitDev *__restrict
       cbase = buf + (size_t)(i & 1u) * chunk_cap;
       cbase_off = chunk(ch).x;
     }
-    const uint64_t *ops = reinterpret_cast<const uint64_t *>(cbase) + (ek.x - cbase_off);
     // (4) execute the epoch's ops in order (shared-memory addresses are kept
     //     as 32-bit shared-window offsets so every load is an ld.shared)
     const uint32_t ops_s = smem_u32(cbase) + (ek.x - cbase_off) * 8u + tid * 8u;
@@ -243,6 +248,7 @@ __global__ void __launch_bounds__(1024) walk_kernel(const CircuitDev *__restrict
           Z[u] ^= lds64(pub_s + arg * 16u + 8u);
         } else if (opc == OP_SNAP) {
           snap_j[arg] = make_ulonglong2(X[u], Z[u]);
+          if (X[u] | Z[u]) atomicOr(nzm_j + (size_t)arg * mw, jbit);
         } else if (opc == OP_XPZ) {
           X[u] ^= lds64(pub_s + arg * 16u + 8u);
         } else {
@@ -273,6 +279,7 @@ __global__ void __launch_bounds__(1024) walk_kernel(const CircuitDev *__restrict
             last_inj[u] = inj;
           } else if (opc == OP_SNAPD) {
             snap_j[arg] = make_ulonglong2(last_inj[u], 0ull);
+            if (last_inj[u]) atomicOr(nzm_j + (size_t)arg * mw, jbit);
           }
         }
       }

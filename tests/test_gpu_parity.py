@@ -114,3 +114,17 @@ def test_long_symptoms_widen_target_lists():
     text += "".join(f"CX 0 {q}\n" for q in range(1, n))
     text += "M " + " ".join(map(str, range(n))) + "\n" + "".join(f"DETECTOR rec[-{k}]\n" for k in range(1, n + 1))
     _check(gp.get_driver(text).compile(text), text)
+
+
+def test_driver_reuse_from_large_to_small_circuits():
+    """One driver compiling circuits of falling size (its arena holds the previous circuit's data)
+    gives exactly what fresh drivers give."""
+    from greenpeas_gb300.workloads import batch_surface
+    circs = [gp.SurfaceCode(9).get_memory(9, 1e-3, noise="uniform")]
+    circs += batch_surface(n=10, seed=3, switch_prob=0.3, distances=(3, 5, 7))
+    drv = gp.get_driver(circs[0])
+    for text in circs:
+        drv.prepare(text)
+        drv.run_device()
+        drv.run_device()  # the second run comes from a captured graph
+        assert drv.fetch() == gp.get_driver(text).compile(text)
