@@ -537,8 +537,13 @@ struct gpc_driver {
       CK(gpc::launch_walk(wl, s));
     };
     if (nc <= 1) {
-      CK(gpc::launch_key_prep(kl, stream));
+      // the key-block table on an auxiliary stream beside the walk
+      CK(cudaEventRecord(fork_ev, stream));
+      CK(cudaStreamWaitEvent(aux[0], fork_ev, 0));
+      CK(gpc::launch_key_prep(kl, aux[0]));
       if (nc == 1) one(L.classes[0], stream);
+      CK(cudaEventRecord(join_ev[0], aux[0]));
+      CK(cudaStreamWaitEvent(stream, join_ev[0], 0));
       return;
     }
     // fork: each class on an auxiliary stream, joined back into the main stream

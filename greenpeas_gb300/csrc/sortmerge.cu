@@ -933,103 +933,139 @@ __global__ void __launch_bounds__(GW_WARPS * 32) group_warp_kernel(GroupLaunch L
   }
 }
 
-// One CTA per listed bucket (WARP_CAP < items <= SLOT_CAP), persistent over the list.
-__global__ void __launch_bounds__(BUCKET_THREADS) group_big_kernel(GroupLaunch L) {
-  constexpr int NT = BUCKET_THREADS;
-  constexpr int NW = NT / 32;
+// One CTA per listed bucket (WARP_CAP < items <= SLOT_CAP), persistent over
+// the list; one thread per slot.  Same order and arithmetic as
+// group_warp_kernel: sub-bin counting sort, rank inside a sub-bin, then each
+// warp takes 32 sorted positions (heads, target offsets, segmented scan of
+// the XOR-merge) and one thread chains the runs across the warps' chunks.
+constexpr uint32_t GB_THREADS = SLOT_CAP;
+__global__ void __launch_bounds__(GB_THREADS) group_big_kernel(GroupLaunch L) {
+  constexpr uint32_t NBIN = 64, NWARP = GB_THREADS / 32;
   __shared__ ulonglong2 sk[SLOT_CAP];
-  __shared__ uint32_t sm[SLOT_CAP];
+  __shared__ uint32_t sm[SLOT_CAP], st[SLOT_CAP];
   __shared__ double sp[SLOT_CAP];
-  __shared__ uint32_t st[SLOT_CAP];
-  __shared__ uint16_t ord[SLOT_CAP];
-  __shared__ uint32_t sntg[SLOT_CAP];  // targets of a group head at a sorted position, else ~0u
-  __shared__ uint32_t wc[NW], wt[NW];
-  const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
+  __shared__ uint16_t ord[SLOT_CAP], sx[SLOT_CAP];
+  __shared__ uint8_t sq[SLOT_CAP];
+  __shared__ uint32_t sh[NBIN];
+  __shared__ uint32_t c_groups[NWARP], c_targets[NWARP], c_head[NWARP], c_gbase[NWARP], c_tbase[NWARP];
+  __shared__ double c_tail[NWARP], c_carry[NWARP];
+  const uint32_t tid = threadIdx.x, lane = tid & 31u, warp = tid >> 5;
   const uint32_t nbig = *L.big_n;
   const uint32_t tcap = L.tcap;
-  for (uint32_t k = blockIdx.x; k < nbig; k += gridDim.x) {
-    const uint32_t b = L.big_list[k];
+  for (uint32_t kb = blockIdx.x; kb < nbig; kb += gridDim.x) {
+    const uint32_t b = L.big_list[kb];
     const uint32_t n = L.count[b];  // WARP_CAP < n <= SLOT_CAP
     const size_t base = (size_t)b * SLOT_CAP;
-    for (uint32_t i = threadIdx.x; i < n; i += NT) {
-      sk[i] = L.skey[base + i];
-      const SlotTail t = L.stail[base + i];
-      sm[i] = t.m;
-      st[i] = t.t;
-      sp[i] = t.p;
+    if (tid < NBIN) sh[tid] = 0;
+    __syncthreads();
+    if (tid < n) {
+      const ulonglong2 k = L.skey[base + tid];
+      const SlotTail t = L.stail[base + tid];
+      sk[tid] = k;
+      sm[tid] = t.m;
+      st[tid] = t.t;
+      sp[tid] = t.p;
+      sq[tid] = (uint8_t)atomicAdd(sh + (uint32_t)(k.y >> 58), 1u);
     }
     __syncthreads();
-    for (uint32_t i = threadIdx.x; i < n; i += NT) {
-      const ulonglong2 ki = sk[i];
-      const uint32_t mi = sm[i];
-      uint32_t r = 0;
-      for (uint32_t q = 0; q < n; ++q) r += item_less(sk[q], sm[q], ki, mi) ? 1u : 0u;
-      ord[r] = (uint16_t)i;
+    if (warp == 0) {
+      const uint32_t c0 = sh[2 * lane], c1 = sh[2 * lane + 1];
+      uint32_t inc = c0 + c1;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t a = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+        if (lane >= (uint32_t)o) inc += a;
+      }
+      const uint32_t ex = inc - c0 - c1;
+      __syncwarp();
+      sh[2 * lane] = ex;
+      sh[2 * lane + 1] = ex + c0;
     }
     __syncthreads();
-    for (uint32_t s = threadIdx.x; s < n; s += NT) {
-      const uint32_t i = ord[s];
-      const uint32_t nt = st[i];
-      bool head = true;
+    if (tid < n) sx[sh[(uint32_t)(sk[tid].y >> 58)] + sq[tid]] = (uint16_t)tid;
+    __syncthreads();
+    if (tid < n) {
+      const ulonglong2 ki = sk[tid];
+      const uint32_t mi = sm[tid];
+      const uint32_t bin = (uint32_t)(ki.y >> 58);
+      const uint32_t lo = sh[bin], hi = bin + 1 < NBIN ? sh[bin + 1] : n;
+      uint32_t r = lo;
+      for (uint32_t j = lo; j < hi; ++j) {
+        const uint32_t x = sx[j];
+        r += item_less(sk[x], sm[x], ki, mi) ? 1u : 0u;
+      }
+      ord[r] = (uint16_t)tid;
+    }
+    __syncthreads();
+    // position s = tid: heads, collisions, per-chunk scans
+    const uint32_t s = tid;
+    const bool in = s < n;
+    bool head = false;
+    uint32_t i = 0, nt = 0;
+    if (in) {
+      i = ord[s];
+      nt = st[i];
+      head = true;
       if (s > 0) {
         const uint32_t ip = ord[s - 1];
         if (key_eq(sk[ip], sk[i])) {
           head = false;
-          if (st[ip] != nt ||
-              !lists_equal(L.tl + (size_t)sm[i] * tcap, L.tl + (size_t)sm[ip] * tcap, nt))
+          if (st[ip] != nt || !lists_equal(L.tl + (size_t)sm[i] * tcap, L.tl + (size_t)sm[ip] * tcap, nt))
             atomicOr(L.err, DEV_ERR_COLLISION);
         }
       }
-      sntg[s] = head ? nt : ~0u;
+    }
+    const uint32_t hb = __ballot_sync(0xFFFFFFFFu, head);
+    const uint32_t tv = head ? nt : 0u;
+    uint32_t inc = tv;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const uint32_t a = __shfl_up_sync(0xFFFFFFFFu, inc, o);
+      if (lane >= (uint32_t)o) inc += a;
+    }
+    const uint32_t le = hb & (0xFFFFFFFFu >> (31u - lane));
+    const int seg = le ? 31 - __clz(le) : -1;
+    const uint32_t seg0 = seg < 0 ? 0u : (uint32_t)seg;
+    double x = in ? sp[i] : 0.0;
+    const uint32_t maxlen = __reduce_max_sync(0xFFFFFFFFu, in ? lane - seg0 + 1 : 0u);
+    for (uint32_t d = 1; d < maxlen; d <<= 1) {
+      const double y = __shfl_up_sync(0xFFFFFFFFu, x, d);
+      if (lane >= d && lane - d >= seg0) x = xor_merge(y, x);
+    }
+    if (lane == 31) {
+      c_groups[warp] = __popc(hb);
+      c_targets[warp] = inc;
+      c_head[warp] = hb != 0u;
+      c_tail[warp] = x;
     }
     __syncthreads();
-    uint32_t carry_c = 0, carry_t = 0;
-    for (uint32_t r0 = 0; r0 < n; r0 += NT) {
-      const uint32_t s = r0 + threadIdx.x;
-      const uint32_t v = s < n ? sntg[s] : ~0u;
-      const uint32_t c_in = v != ~0u ? 1u : 0u, t_in = v != ~0u ? v : 0u;
-      uint32_t ic = c_in, it = t_in;
-#pragma unroll
-      for (int o = 1; o < 32; o <<= 1) {
-        const uint32_t a = __shfl_up_sync(0xFFFFFFFFu, ic, o), bb = __shfl_up_sync(0xFFFFFFFFu, it, o);
-        if (lane >= (uint32_t)o) {
-          ic += a;
-          it += bb;
-        }
+    if (tid == 0) {  // chain the chunks: group/target bases and the run carried into each chunk
+      uint32_t g = 0, t = 0;
+      double run = 0.0;
+      for (uint32_t c = 0; c < NWARP; ++c) {
+        c_gbase[c] = g;
+        c_tbase[c] = t;
+        c_carry[c] = run;
+        g += c_groups[c];
+        t += c_targets[c];
+        run = c_head[c] ? c_tail[c] : xor_merge(run, c_tail[c]);
       }
-      if (lane == 31) {
-        wc[warp] = ic;
-        wt[warp] = it;
-      }
-      __syncthreads();
-      uint32_t pc = carry_c, pt = carry_t;
-      for (uint32_t x = 0; x < warp; ++x) {
-        pc += wc[x];
-        pt += wt[x];
-      }
-      if (c_in) {
-        const uint32_t g = pc + ic - 1;
-        const uint32_t i = ord[s];
-        double p = sp[i];
-        for (uint32_t s2 = s + 1; s2 < n; ++s2) {
-          const uint32_t i2 = ord[s2];
-          if (!key_eq(sk[i2], sk[i])) break;
-          const double q = sp[i2];
-          p = p * (1.0 - q) + q * (1.0 - p);
-        }
-        L.stail[base + g] = SlotTail{sm[i], pt + it - t_in, p};
-      }
-      for (uint32_t x = 0; x < (uint32_t)NW; ++x) {
-        carry_c += wc[x];
-        carry_t += wt[x];
-      }
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-      L.bagg[b] = make_uint2(carry_c, carry_t);
-      atomicAdd(&L.tsum[b / SCAN_TILE].x, carry_c);
-      atomicAdd(&L.tsum[b / SCAN_TILE].y, carry_t);
+      L.bagg[b] = make_uint2(g, t);
+      atomicAdd(&L.tsum[b / SCAN_TILE].x, g);
+      atomicAdd(&L.tsum[b / SCAN_TILE].y, t);
       atomicAdd(L.totals + 3, n);
+    }
+    __syncthreads();
+    if (seg < 0) x = xor_merge(c_carry[warp], x);
+    const uint32_t gb = c_gbase[warp];
+    if (head) {
+      const uint32_t g = gb + __popc(hb & ((1u << lane) - 1u));
+      L.stail[base + g].m = sm[i];
+      L.stail[base + g].t = c_tbase[warp] + inc - tv;
+    }
+    if (in && (s + 1 >= n || !key_eq(sk[ord[s + 1]], sk[i]))) {
+      const uint32_t g = seg < 0 ? gb - 1u : gb + __popc(hb & ((1u << seg0) - 1u));
+      L.stail[base + g].p = x;
     }
     __syncthreads();
   }
@@ -1182,7 +1218,7 @@ cudaError_t launch_bucket_scatter(const ulonglong2 *key, uint32_t M, uint32_t bu
 cudaError_t launch_group(const GroupLaunch &L, cudaStream_t s) {
   if (L.nb == 0) return cudaSuccess;
   group_warp_kernel<<<(L.nb + GW_WARPS - 1) / GW_WARPS, GW_WARPS * 32, 0, s>>>(L);
-  group_big_kernel<<<2 * 152, BUCKET_THREADS, 0, s>>>(L);
+  group_big_kernel<<<2 * 152, GB_THREADS, 0, s>>>(L);
   return cudaGetLastError();
 }
 

@@ -248,7 +248,7 @@ __global__ void __launch_bounds__(1024) walk_kernel(const CircuitDev *__restrict
           Z[u] ^= lds64(pub_s + arg * 16u + 8u);
         } else if (opc == OP_SNAP) {
           snap_j[arg] = make_ulonglong2(X[u], Z[u]);
-          if (X[u] | Z[u]) atomicOr(nzm_j + (size_t)arg * mw, jbit);
+          if (X[u] | Z[u]) atomicOr(nzm_j + arg * mw, jbit);
         } else if (opc == OP_XPZ) {
           X[u] ^= lds64(pub_s + arg * 16u + 8u);
         } else {
@@ -279,7 +279,7 @@ __global__ void __launch_bounds__(1024) walk_kernel(const CircuitDev *__restrict
             last_inj[u] = inj;
           } else if (opc == OP_SNAPD) {
             snap_j[arg] = make_ulonglong2(last_inj[u], 0ull);
-            if (last_inj[u]) atomicOr(nzm_j + (size_t)arg * mw, jbit);
+            if (last_inj[u]) atomicOr(nzm_j + arg * mw, jbit);
           }
         }
       }

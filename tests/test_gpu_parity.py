@@ -81,6 +81,15 @@ def test_repeated_symptom_overflows_bucket():
     _check(gp.get_driver(text).compile(text), text)
 
 
+@pytest.mark.parametrize("copies", [129, 200, 250])
+def test_large_bucket_cta_path(copies):
+    """A symptom repeated more often than one warp merges (128) but within a bucket's slots (256):
+    the bucket goes to the CTA kernel, whose runs cross its warps' 32-position chunks."""
+    text = "R 0 1 2\n" + "X_ERROR(0.001) 0\nTICK\n" * copies + "DEPOLARIZE1(0.01) 1 2\n"
+    text += "CX 0 1\nM 0 1 2\nDETECTOR rec[-1]\nDETECTOR rec[-2]\nDETECTOR rec[-3]\n"
+    _check(gp.get_driver(text).compile(text), text)
+
+
 def test_bucket_and_global_paths_agree():
     text = gp.BBCode(6).get_memory(6, 1e-3, noise="uniform")
     a = gp.get_driver(text).compile(text)
