@@ -4,12 +4,17 @@
     driver = gp.get_driver(circuit)                  # circuit: stim.Circuit or stim text
     dem = driver.compile_detector_error_model(circuit)
 
-See ``error_analysis`` (the compile path), ``codes`` (circuit generators) and
-``dem`` (the DEM type returned when stim is not installed).
+See ``error_analysis`` (the compile path and its batched form), ``autograd``
+(noise-rate gradients), ``serving`` (continuous batching of compile
+requests), ``codes`` and ``workloads`` (circuit generators) and ``dem`` (the
+DEM type returned when stim is not installed).
 """
 
+from ._native import GpcError
+from .autograd import NoiseRateDEM
 from .codes import BBCode, SurfaceCode
 from .dem import DetectorErrorModel
 from .error_analysis import CorrelationLevel, Driver, Tape, get_driver
 
-__all__ = ["BBCode", "CorrelationLevel", "DetectorErrorModel", "Driver", "SurfaceCode", "Tape", "get_driver"]
+__all__ = ["BBCode", "CorrelationLevel", "DetectorErrorModel", "Driver", "GpcError", "NoiseRateDEM", "SurfaceCode",
+           "Tape", "get_driver"]

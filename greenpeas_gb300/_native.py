@@ -26,6 +26,7 @@ EXPORTS = [
     "gpc_run_device", "gpc_fetch", "gpc_driver_stream", "gpc_last_timings", "gpc_last_sizes",
     "gpc_tape_lower", "gpc_tape_get_view", "gpc_tape_free", "gpc_tape_last_error", "gpc_last_traffic",
     "gpc_last_io_bytes", "gpc_merge_mechanisms_static", "gpc_prepare_batch", "gpc_fetch_batch",
+    "gpc_param_prepare", "gpc_param_forward", "gpc_param_probs", "gpc_param_backward",
 ]
 
 
@@ -53,6 +54,8 @@ class TapeView(ctypes.Structure):
         ("inj_lo", ctypes.POINTER(ctypes.c_uint32)), ("inj_hi", ctypes.POINTER(ctypes.c_uint32)),
         ("rec", ctypes.POINTER(ctypes.c_uint64)), ("rec_p", ctypes.POINTER(ctypes.c_double)),
         ("rec_moff", ctypes.POINTER(ctypes.c_uint32)),
+        ("rec_src", ctypes.POINTER(ctypes.c_uint32)),
+        ("num_ticks", ctypes.c_uint32),
     ]
 
 
@@ -99,7 +102,12 @@ def lib() -> ctypes.CDLL:
     L.gpc_tape_free.argtypes = [vp]
     L.gpc_tape_free.restype = None
     L.gpc_tape_last_error.restype = ctypes.c_char_p
-    for f in ("gpc_get_driver", "gpc_compile", "gpc_compile_batch", "gpc_dem_arrays", "gpc_dem_info",
+    L.gpc_param_prepare.argtypes = [vp, ctypes.c_char_p, sz, u32p]
+    L.gpc_param_forward.argtypes = [vp, vp, vp, u32p]
+    L.gpc_param_probs.argtypes = [vp, vp, vp]
+    L.gpc_param_backward.argtypes = [vp, vp, vp, vp]
+    for f in ("gpc_param_prepare", "gpc_param_forward", "gpc_param_probs", "gpc_param_backward",
+              "gpc_get_driver", "gpc_compile", "gpc_compile_batch", "gpc_dem_arrays", "gpc_dem_info",
               "gpc_dem_text", "gpc_prepare", "gpc_run_device", "gpc_fetch", "gpc_last_timings",
               "gpc_last_sizes", "gpc_tape_lower", "gpc_tape_get_view", "gpc_last_traffic", "gpc_last_io_bytes",
               "gpc_merge_mechanisms_static", "gpc_prepare_batch", "gpc_fetch_batch"):

@@ -14,6 +14,7 @@ enum : uint32_t {
   DEV_FLAG_TG_OVF = 8u,    // target buffer too small: grow and re-run the merge
   DEV_FLAG_BIG_BUCKET = 16u,  // a bucket exceeds the in-CTA capacity: use the global sort
   DEV_FLAG_LONG = 32u,        // a symptom has more targets than the target-list stride: widen it
+  DEV_ERR_NOISE = 128u,       // a noise-tensor entry is outside its channel's range
 };
 
 // One circuit as the kernels see it.  All arrays are device pointers.
@@ -163,7 +164,9 @@ struct GroupLaunch {
   const uint32_t *tl;       // [M][tcap] batch-wide target lists
   const uint32_t *tn;       // [M]
   uint32_t tcap;
-  const ulonglong2 *skey;   // [nb * SLOT_CAP]
+  ulonglong2 *skey;         // [nb * SLOT_CAP] keys; afterwards, as 32-bit pairs, the saved
+                            // permutation: [2s] mechanism at sorted position s, [2g+1] first
+                            // sorted position of group g
   SlotTail *stail;          // [nb * SLOT_CAP] items, then group records
   const uint32_t *count;    // [nb]
   uint32_t nb;
@@ -183,6 +186,47 @@ struct GroupLaunch {
   uint32_t *err;
 };
 cudaError_t launch_group(const GroupLaunch &L, cudaStream_t s);
+
+// ---- noise-rate gradients (single circuit) ----------------------------------
+// Record probabilities from a [n_ticks][4] FP64 noise tensor: record r takes
+// its source's rate through its channel's split, looked up in qtab[src][kind]
+// (kind 0: X/Y/Z error or measurement flip, 1: DEPOLARIZE1, 2: DEPOLARIZE2),
+// which the host fills with the same split formulas as the text path.
+// Records without a source keep their probability.
+struct ParamLaunch {
+  const uint64_t *rec;
+  const uint32_t *rec_src;
+  double *rec_p;
+  uint32_t R, n_src;
+  const double *qtab;  // [n_src][3]
+};
+cudaError_t launch_param_rec(const ParamLaunch &L, cudaStream_t s);
+
+// Adjoint of the merge and of the channel splits:
+//  group:  one warp per bucket, a lane per group: dL/dq_m = dL/dp_g *
+//          prod_{j in g, j != m} (1 - 2 q_j) from prefix and suffix products
+//          along the group's run in the saved permutation;
+//  record: dL/dp_r = (sum of its mechanisms' dL/dq) * dq/dp, the split's
+//          slope at the source's rate (stab[src][kind], filled by the host);
+//  source: dL/dnoise[e] = sum over the records of source e, in record order.
+struct AdjointLaunch {
+  const ulonglong2 *skey;  // saved permutation (see GroupLaunch)
+  const uint32_t *count;
+  const uint2 *bagg, *bout;
+  uint32_t nb;
+  const double *mp;        // [M] mechanism probabilities of the forward
+  const double *grad_out;  // [groups] dL/dp of each merged mechanism
+  double *gq;              // [M] (zeroed) dL/dq of each mechanism
+  const uint64_t *rec;
+  const uint32_t *rec_src, *rec_moff;
+  uint32_t R;
+  const double *stab;      // [n_src][3] dq/dp of each source and channel kind
+  double *grad_rec;        // [R]
+  const uint32_t *src_off, *src_rec;  // records of each source (CSR, record order)
+  uint32_t n_src;
+  double *grad_noise;      // [n_src]
+};
+cudaError_t launch_adjoint(const AdjointLaunch &L, cudaStream_t s);
 cudaError_t launch_scan_emit(const GroupLaunch &L, cudaStream_t s);
 
 // ---- global path (used when a bucket is too large for one CTA) -------------

@@ -8,6 +8,7 @@
 // mechanisms (the reference copies the whole node x 32 class matrix,
 // Driver.hpp:158-161).
 #include <algorithm>
+#include <cmath>
 #include <atomic>
 #include <exception>
 #include <thread>
@@ -99,7 +100,7 @@ struct HostBuf {
 
 // Byte offsets of one circuit's input arrays inside the arena.
 struct CircLayout {
-  size_t ops, ep_opoff, ep_k, ep_ptoff, ep_chunk, ch_off, ch_bytes, inj_lo, inj_hi, rec, rec_p, rec_moff;
+  size_t ops, ep_opoff, ep_k, ep_ptoff, ep_chunk, ch_off, ch_bytes, inj_lo, inj_hi, rec, rec_p, rec_moff, rec_src;
   size_t snap, band, nzm;
   uint32_t mbase, bbase, bbits;
 };
@@ -118,6 +119,7 @@ struct Layout {
   size_t mdesc, mp, tl, tn, key, blk_r0, skey, stail, bagg, bout, cout, big_list;
   size_t zero, err, totals, bcount, tsum, big_n, zero_bytes;
   size_t sk0, sk1, pm0, pm1, hik;  // global path (single circuit)
+  size_t src_off, src_rec, gq, grad_rec, ptab;  // noise-rate gradients (single circuit)
   size_t gzero, sort_scr, merge_status, merge_ctr, gzero_bytes;
   size_t out_prob, out_off;
   size_t total;
@@ -162,6 +164,11 @@ struct gpc_driver {
   uint64_t *sk_sorted = nullptr;
   uint64_t sort_mask = ~0ull;
   bool force_global = false;  // test option: skip the bucket path (single circuits)
+  // noise-rate gradients: record probabilities come from a device noise tensor
+  bool param = false;
+  const double *noise_dev = nullptr;
+  uint32_t param_groups = 0;
+  cudaEvent_t caller_ev = nullptr, done_ev = nullptr;
   cudaGraph_t graph = nullptr;  // captured kernel sequence of run() for one launch configuration
   cudaGraphExec_t graph_exec = nullptr;
   bool use_graph = true;
@@ -197,6 +204,8 @@ struct gpc_driver {
     for (auto &e : ev)
       if (e) cudaEventDestroy(e);
     if (fork_ev) cudaEventDestroy(fork_ev);
+    if (caller_ev) cudaEventDestroy(caller_ev);
+    if (done_ev) cudaEventDestroy(done_ev);
     for (auto &e : join_ev)
       if (e) cudaEventDestroy(e);
     for (auto &a : aux)
@@ -242,6 +251,7 @@ struct gpc_driver {
       c.rec = take(T.rec.size() * 8);
       c.rec_p = take(T.rec_p.size() * 8);
       c.rec_moff = take(T.rec_moff.size() * 4);
+      c.rec_src = take(T.rec_src.size() * 4);
       // buckets: about 96 mechanisms each, a power of two between 2^4 and 2^16
       uint32_t bb = 4;
       while (bb < 16 && ((uint64_t)96 << bb) < T.M) ++bb;
@@ -260,6 +270,10 @@ struct gpc_driver {
     L.items = take((size_t)items * sizeof(uint2));
     L.mbase = take((size_t)(N + 1) * 4);
     L.cbbase = take((size_t)N * 4);
+    if (param) {
+      L.src_off = take(((size_t)tapes[0].n_ticks * gpc::SRC_CLASSES + 1) * 4);
+      L.src_rec = take(tapes[0].rec.size() * 4);
+    }
     L.in_bytes = o;
     for (uint32_t i = 0; i < N; ++i) {
       L.c[i].snap = take((size_t)tapes[i].w * tapes[i].npoints * 16);
@@ -299,6 +313,9 @@ struct gpc_driver {
     L.sort_tiles = gpc::sort_tiles(Mg);
     L.merge_tiles = gpc::merge_tiles(Mg);
     L.sort_words = Mg ? gpc::sort_scratch_words(Mg, 64) : 0;
+    L.gq = take(param ? (size_t)M * 8 : 0);
+    L.grad_rec = take(param ? tapes[0].rec.size() * 8 : 0);
+    L.ptab = take(param ? (size_t)tapes[0].n_ticks * gpc::SRC_CLASSES * 6 * 8 : 0);  // q and dq/dp tables
     L.gzero = o;
     L.sort_scr = take(L.sort_words * 4);
     L.merge_status = take((size_t)L.merge_tiles * 8);
@@ -354,6 +371,7 @@ struct gpc_driver {
       put(l.rec, T.rec.data(), T.rec.size() * 8);
       put(l.rec_p, T.rec_p.data(), T.rec_p.size() * 8);
       put(l.rec_moff, T.rec_moff.data(), T.rec_moff.size() * 4);
+      put(l.rec_src, T.rec_src.data(), T.rec_src.size() * 4);
       CircuitDev &c = cd[i];
       c = CircuitDev{};
       c.ops = dptr<uint64_t>(l.ops);
@@ -401,6 +419,21 @@ struct gpc_driver {
     for (uint32_t i : item_order)
       for (uint32_t j = 0; j < tapes[i].w; ++j) items.push_back(make_uint2(i, j));
     put(L.items, items.data(), items.size() * sizeof(uint2));
+    if (param) {
+      // records of each (tick, class) source, in record order
+      const Tape &T = tapes[0];
+      const uint32_t ns = T.n_ticks * gpc::SRC_CLASSES;
+      std::vector<uint32_t> off(ns + 1, 0), lst;
+      for (uint32_t v : T.rec_src)
+        if (v < ns) ++off[v + 1];
+      for (uint32_t e = 0; e < ns; ++e) off[e + 1] += off[e];
+      lst.resize(off[ns]);
+      std::vector<uint32_t> cur(off.begin(), off.end() - 1);
+      for (uint32_t r = 0; r < (uint32_t)T.rec_src.size(); ++r)
+        if (T.rec_src[r] < ns) lst[cur[T.rec_src[r]]++] = r;
+      put(L.src_off, off.data(), off.size() * 4);
+      put(L.src_rec, lst.data(), lst.size() * 4);
+    }
   }
 
   // Parses and lowers circuits (in parallel on host threads for batches).
@@ -436,8 +469,12 @@ struct gpc_driver {
     tapes = std::move(T);
   }
 
-  void prepare(const char *const *texts, const size_t *lens, uint32_t n) {
+  void prepare(const char *const *texts, const size_t *lens, uint32_t n, bool param_mode = false) {
     CK(cudaSetDevice(device));
+    if (texts) {
+      if (param_mode && n != 1) throw gpc::Error(GPC_ERR_INVALID, "noise-rate gradients take one circuit");
+      param = param_mode;
+    }
     prepared = false;
     ran = false;
     if (texts) {
@@ -714,6 +751,7 @@ struct gpc_driver {
           lists_off = true;
         }
         prepare(nullptr, nullptr, 0);
+        if (param && noise_dev) launch_param_rec_now();
         run();
         continue;
       }
@@ -750,6 +788,118 @@ struct gpc_driver {
       return Finish::Ok;
     }
     throw gpc::Error(GPC_ERR_CUDA, "merge did not converge");
+  }
+
+  // ---- noise-rate gradients (one circuit) --------------------------------
+  uint32_t n_src() const { return tapes.empty() ? 0 : tapes[0].n_ticks * gpc::SRC_CLASSES; }
+
+  void launch_param_rec_now() {
+    const Tape &T = tapes[0];
+    gpc::ParamLaunch pl{};
+    pl.rec = dptr<uint64_t>(L.c[0].rec);
+    pl.rec_src = dptr<uint32_t>(L.c[0].rec_src);
+    pl.rec_p = dptr<double>(L.c[0].rec_p);
+    pl.R = (uint32_t)T.rec.size();
+    pl.n_src = n_src();
+    pl.qtab = dptr<double>(L.ptab);
+    CK(gpc::launch_param_rec(pl, stream));
+  }
+
+  // The caller's stream waits for this driver's stream (and the reverse before work starts).
+  void wait_caller(cudaStream_t caller) {
+    if (!caller_ev) CK(cudaEventCreateWithFlags(&caller_ev, cudaEventDisableTiming));
+    CK(cudaEventRecord(caller_ev, caller));
+    CK(cudaStreamWaitEvent(stream, caller_ev, 0));
+  }
+  void signal_caller(cudaStream_t caller) {
+    if (!done_ev) CK(cudaEventCreateWithFlags(&done_ev, cudaEventDisableTiming));
+    CK(cudaEventRecord(done_ev, stream));
+    CK(cudaStreamWaitEvent(caller, done_ev, 0));
+  }
+
+  uint32_t param_forward(const double *noise, cudaStream_t caller) {
+    if (!param || !prepared) throw gpc::Error(GPC_ERR_INVALID, "no circuit prepared for noise-rate gradients");
+    if (!noise) throw gpc::Error(GPC_ERR_INVALID, "noise tensor is null");
+    CK(cudaSetDevice(device));
+    wait_caller(caller);
+    noise_dev = noise;
+    // The rates come to the host (n_ticks x 4 doubles): each source's split
+    // probability and slope per channel kind are evaluated with the same
+    // host formulas as the text path, so a template run with a rate tensor
+    // gives what compiling the instantiated text gives, bit for bit.  (The
+    // DEPOLARIZE2 split 0.5 - 0.5 (1 - 16p/15)^(1/8) cancels: one ulp of the
+    // root moves q by ~1e-12 relative at p ~ 1e-3, so the root must come from
+    // the same pow.)
+    const uint32_t ns = n_src();
+    pin_out.ensure((size_t)ns * 8 * 7);
+    double *h = static_cast<double *>(pin_out.p);
+    CK(cudaMemcpyAsync(h, noise, (size_t)ns * 8, cudaMemcpyDeviceToHost, stream));
+    CK(cudaStreamSynchronize(stream));
+    double *qt = h + ns, *st = h + 4 * (size_t)ns;
+    for (uint32_t e = 0; e < ns; ++e) {
+      const double p = h[e];
+      if (!(p >= 0.0 && p <= 1.0)) throw gpc::Error(GPC_ERR_INVALID, "a noise rate is outside [0, 1]");
+      qt[3 * e] = p;
+      st[3 * e] = 1.0;
+      const bool ok1 = p <= 0.75, ok2 = p <= 0.9375;
+      if (!ok1 && (e % gpc::SRC_CLASSES) == gpc::SRC_DEP1)
+        throw gpc::Error(GPC_ERR_INVALID, "a DEPOLARIZE1 rate is above 3/4");
+      if (!ok2 && (e % gpc::SRC_CLASSES) == gpc::SRC_DEP2)
+        throw gpc::Error(GPC_ERR_INVALID, "a DEPOLARIZE2 rate is above 15/16");
+      const double s1 = ok1 ? std::sqrt(1.0 - 4.0 * p / 3.0) : 1.0;
+      const double x2 = ok2 ? 1.0 - 16.0 * p / 15.0 : 1.0;
+      qt[3 * e + 1] = ok1 ? gpc::split_dep1(p) : 0.0;
+      st[3 * e + 1] = ok1 && s1 > 0 ? 1.0 / (3.0 * s1) : 0.0;
+      qt[3 * e + 2] = ok2 ? gpc::split_dep2(p) : 0.0;
+      st[3 * e + 2] = ok2 && x2 > 0 ? std::pow(x2, 0.125) / (15.0 * x2) : 0.0;
+    }
+    CK(cudaMemcpyAsync(dptr<char>(L.ptab), qt, (size_t)ns * 6 * 8, cudaMemcpyHostToDevice, stream));
+    launch_param_rec_now();
+    run();
+    uint32_t C = 0, NT = 0;
+    if (finish(&C, &NT) != Finish::Ok) throw gpc::Error(GPC_ERR_UNSUPPORTED, "batch fallback in a gradient run");
+    param_groups = C;
+    signal_caller(caller);
+    return C;
+  }
+
+  void param_probs(double *out, cudaStream_t caller) {
+    if (!param || !ran) throw gpc::Error(GPC_ERR_INVALID, "no forward run");
+    if (param_groups) CK(cudaMemcpyAsync(out, dptr<char>(L.out_prob), (size_t)param_groups * 8, cudaMemcpyDeviceToDevice, stream));
+    signal_caller(caller);
+  }
+
+  void param_backward(const double *grad_out, double *grad_noise, cudaStream_t caller) {
+    if (!param || !ran) throw gpc::Error(GPC_ERR_INVALID, "no forward run");
+    if (used_global)
+      throw gpc::Error(GPC_ERR_UNSUPPORTED, "gradients need the bucket merge (this circuit took the global sort)");
+    if (!grad_out || !grad_noise) throw gpc::Error(GPC_ERR_INVALID, "null gradient buffer");
+    CK(cudaSetDevice(device));
+    wait_caller(caller);
+    const Tape &T = tapes[0];
+    CK(cudaMemsetAsync(dptr<char>(L.gq), 0, (size_t)L.M * 8, stream));
+    gpc::AdjointLaunch A{};
+    A.skey = dptr<ulonglong2>(L.skey);
+    A.count = dptr<uint32_t>(L.bcount);
+    A.bagg = dptr<uint2>(L.bagg);
+    A.bout = dptr<uint2>(L.bout);
+    A.nb = L.nb;
+    A.mp = dptr<double>(L.mp);
+    A.grad_out = grad_out;
+    A.gq = dptr<double>(L.gq);
+    A.rec = dptr<uint64_t>(L.c[0].rec);
+    A.rec_src = dptr<uint32_t>(L.c[0].rec_src);
+    A.rec_moff = dptr<uint32_t>(L.c[0].rec_moff);
+    A.R = (uint32_t)T.rec.size();
+    A.stab = dptr<double>(L.ptab) + (size_t)n_src() * 3;
+    A.grad_rec = dptr<double>(L.grad_rec);
+    A.src_off = dptr<uint32_t>(L.src_off);
+    A.src_rec = dptr<uint32_t>(L.src_rec);
+    A.n_src = n_src();
+    A.grad_noise = grad_noise;
+    CK(gpc::launch_adjoint(A, stream));
+    signal_caller(caller);
+    CK(cudaStreamSynchronize(stream));
   }
 
   // Algorithmic bytes of each stage of the last run (walk, keys, bucket groups,
@@ -951,6 +1101,32 @@ gpc_status gpc_fetch_batch(gpc_driver *driver, gpc_dem **outs, int32_t n) {
     driver->fetch_all(v);
     for (int32_t i = 0; i < n; ++i) outs[i] = v[i];
   });
+}
+
+gpc_status gpc_param_prepare(gpc_driver *driver, const char *stim_text, size_t len, uint32_t *num_ticks) {
+  if (!driver || !stim_text) return fail(GPC_ERR_INVALID, "bad arguments");
+  return guarded([&] {
+    driver->prepare(&stim_text, &len, 1, true);
+    if (num_ticks) *num_ticks = driver->tapes[0].n_ticks;
+  });
+}
+
+gpc_status gpc_param_forward(gpc_driver *driver, const double *noise, void *stream, uint32_t *num_errors) {
+  if (!driver) return fail(GPC_ERR_INVALID, "driver is null");
+  return guarded([&] {
+    const uint32_t c = driver->param_forward(noise, static_cast<cudaStream_t>(stream));
+    if (num_errors) *num_errors = c;
+  });
+}
+
+gpc_status gpc_param_probs(gpc_driver *driver, double *probs, void *stream) {
+  if (!driver || !probs) return fail(GPC_ERR_INVALID, "bad arguments");
+  return guarded([&] { driver->param_probs(probs, static_cast<cudaStream_t>(stream)); });
+}
+
+gpc_status gpc_param_backward(gpc_driver *driver, const double *grad_probs, double *grad_noise, void *stream) {
+  if (!driver) return fail(GPC_ERR_INVALID, "driver is null");
+  return guarded([&] { driver->param_backward(grad_probs, grad_noise, static_cast<cudaStream_t>(stream)); });
 }
 
 gpc_status gpc_run_device(gpc_driver *driver) {

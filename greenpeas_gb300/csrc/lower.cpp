@@ -253,8 +253,6 @@ struct TextParser {
   }
 };
 
-double split_dep1(double p) { return 0.5 - 0.5 * std::sqrt(1.0 - (4.0 * p) / 3.0); }
-double split_dep2(double p) { return 0.5 - 0.5 * std::pow(1.0 - (16.0 * p) / 15.0, 0.125); }
 
 // Independent X, Y, Z probabilities equivalent to the disjoint channel
 // (px, py, pz): with lambda_P = 1 - 2 P(anticommuting with P), independent
@@ -325,6 +323,9 @@ struct SplitCache {
 };
 
 }  // namespace
+
+double split_dep1(double p) { return 0.5 - 0.5 * std::sqrt(1.0 - (4.0 * p) / 3.0); }
+double split_dep2(double p) { return 0.5 - 0.5 * std::pow(1.0 - (16.0 * p) / 15.0, 0.125); }
 
 Parsed parse_stim(const char *text, size_t len) {
   Parsed p;
@@ -421,6 +422,51 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
     if (g.kind == G_MPAD && in.nargs && in.args[0] > 0)
       throw Error(GPC_ERR_UNSUPPORTED, "noisy MPAD is not supported");
   }
+  // sources of the noise targets: tick and class (see Tape::rec_src)
+  std::vector<uint32_t> tsrc(P.pool.size(), kNone);
+  {
+    uint32_t tick = 0;
+    std::vector<uint8_t> lastReset(nq, 0);  // the qubit's last operation was a reset
+    for (size_t i = 0; i < P.ins.size(); ++i) {
+      const Instr &in = P.ins[i];
+      const Gate &g = kGates[in.gate];
+      const uint32_t *t = P.pool.data() + in.t0;
+      switch (g.kind) {
+        case G_TICK:
+          ++tick;
+          break;
+        case G_N2:
+          for (uint32_t k = 0; k < in.tn; ++k) tsrc[in.t0 + k] = tick * SRC_CLASSES + SRC_DEP2;
+          break;
+        case G_N1:
+          for (uint32_t k = 0; k < in.tn; ++k) {
+            if (g.a == N1_DEP1)
+              tsrc[in.t0 + k] = tick * SRC_CLASSES + SRC_DEP1;
+            else if (g.a != N1_PC1)
+              tsrc[in.t0 + k] = tick * SRC_CLASSES + (lastReset[t[k]] ? SRC_RESET_FLIP : SRC_MEAS_FLIP);
+          }
+          break;
+        case G_M:
+        case G_MR:
+          for (uint32_t k = 0; k < in.tn; ++k) {
+            tsrc[in.t0 + k] = tick * SRC_CLASSES + SRC_MEAS_FLIP;
+            lastReset[t[k]] = g.kind == G_MR;
+          }
+          break;
+        case G_R:
+          for (uint32_t k = 0; k < in.tn; ++k) lastReset[t[k]] = 1;
+          break;
+        case G_C1:
+        case G_C2:
+        case G_PAULI:
+          for (uint32_t k = 0; k < in.tn; ++k) lastReset[t[k]] = 0;
+          break;
+        default:
+          break;
+      }
+    }
+    T.n_ticks = tick + 1;
+  }
   T.nq = nq;
   T.nmeas = m;
   T.ndet = ndet;
@@ -470,6 +516,7 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
   uint32_t nprov = 0;  // provisional point ids (creation order)
   T.rec.reserve(P.pool.size());
   T.rec_p.reserve(P.pool.size());
+  T.rec_src.reserve(P.pool.size());
   std::vector<uint32_t> ep_k;  // slots per epoch, grown on demand
   SplitCache split;
 
@@ -500,9 +547,10 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
     s.open = id;
     return id;
   };
-  auto record = [&](uint32_t pa, uint32_t pb, uint32_t type, uint32_t Pa, uint32_t Pb, double p) {
+  auto record = [&](uint32_t pa, uint32_t pb, uint32_t type, uint32_t Pa, uint32_t Pb, double p, uint32_t src) {
     T.rec.push_back(make_rec(pa, pb, type, Pa, Pb));
     T.rec_p.push_back(p);
+    T.rec_src.push_back(src);
   };
   const uint32_t dep1Type = opt.level == 0 ? REC_DEP1_L0 : REC_DEP1_L12;
   const uint32_t dep2Type = opt.level == 0 ? REC_DEP2_L0 : opt.level == 1 ? REC_DEP2_L1 : REC_DEP2_L2;
@@ -562,7 +610,7 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
           if (p > 0 && b1 > b0) {
             uint32_t id = nprov++;
             place1(q, make_op(OP_SNAPD, 0, id));
-            record(id, 0, REC_PAULI, 1, 0, p);
+            record(id, 0, REC_PAULI, 1, 0, p, tsrc[in.t0 + k]);
           }
         }
         break;
@@ -574,19 +622,20 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
             case N1_X:
             case N1_Y:
             case N1_Z:
-              if (in.args[0] > 0) record(point(q), 0, REC_PAULI, g.a == N1_X ? 1 : g.a == N1_Z ? 2 : 3, 0, in.args[0]);
+              if (in.args[0] > 0)
+                record(point(q), 0, REC_PAULI, g.a == N1_X ? 1 : g.a == N1_Z ? 2 : 3, 0, in.args[0], tsrc[in.t0 + k]);
               break;
             case N1_DEP1:
-              if (in.args[0] > 0) record(point(q), 0, dep1Type, 0, 0, split.dep1(in.args[0]));
+              if (in.args[0] > 0) record(point(q), 0, dep1Type, 0, 0, split.dep1(in.args[0]), tsrc[in.t0 + k]);
               break;
             case N1_PC1: {
               double qq[3];
               pc1_independent(in.args[0], in.args[1], in.args[2], qq);
               if (qq[0] > 0 || qq[1] > 0 || qq[2] > 0) {
                 uint32_t pt = point(q);
-                if (qq[0] > 0) record(pt, 0, REC_PAULI, 1, 0, qq[0]);
-                if (qq[1] > 0) record(pt, 0, REC_PAULI, 3, 0, qq[1]);
-                if (qq[2] > 0) record(pt, 0, REC_PAULI, 2, 0, qq[2]);
+                if (qq[0] > 0) record(pt, 0, REC_PAULI, 1, 0, qq[0], kNone);
+                if (qq[1] > 0) record(pt, 0, REC_PAULI, 3, 0, qq[1], kNone);
+                if (qq[2] > 0) record(pt, 0, REC_PAULI, 2, 0, qq[2], kNone);
               }
               break;
             }
@@ -600,7 +649,7 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
         for (uint32_t k = in.tn; k >= 2; k -= 2) {
           uint32_t a = t[k - 2], b = t[k - 1];
           uint32_t pa = point(a), pb = point(b);
-          record(pa, pb, dep2Type, 0, 0, sp);
+          record(pa, pb, dep2Type, 0, 0, sp, tsrc[in.t0 + k - 2]);
         }
         break;
       }
@@ -621,11 +670,11 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
           }
         }
         if (P0 && P1)
-          record(point(q0), point(q1), REC_PAULI, P0, P1, p);
+          record(point(q0), point(q1), REC_PAULI, P0, P1, p, kNone);
         else if (P0)
-          record(point(q0), 0, REC_PAULI, P0, 0, p);
+          record(point(q0), 0, REC_PAULI, P0, 0, p, kNone);
         else if (P1)
-          record(point(q1), 0, REC_PAULI, P1, 0, p);
+          record(point(q1), 0, REC_PAULI, P1, 0, p, kNone);
         break;
       }
       default:

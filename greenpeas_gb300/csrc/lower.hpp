@@ -119,7 +119,17 @@ struct Tape {
   std::vector<double> rec_p;        // [R] probability of each of the record's mechanisms
   std::vector<uint32_t> rec_moff;   // [R + 1] first mechanism of each record
   uint32_t M = 0;                   // mechanisms (components)
+  // Source of each record for the noise-rate gradient: tick * 4 + class, or
+  // kNone.  The tick of an instruction is the number of TICKs before it;
+  // classes: 0 DEPOLARIZE2, 1 DEPOLARIZE1, 2 measurement flip (X/Y/Z_ERROR
+  // not directly after a reset of its qubit, or the flip argument of a
+  // measurement), 3 reset flip (X/Y/Z_ERROR whose qubit's last operation was
+  // a reset).  PAULI_CHANNEL_1 and E have no source.
+  std::vector<uint32_t> rec_src;    // [R]
+  uint32_t n_ticks = 1;             // TICK instructions + 1
 };
+
+enum : uint32_t { SRC_DEP2 = 0, SRC_DEP1 = 1, SRC_MEAS_FLIP = 2, SRC_RESET_FLIP = 3, SRC_CLASSES = 4 };
 
 struct LowerOptions {
   int level = 2;     // correlation level 0/1/2
@@ -140,5 +150,10 @@ inline uint32_t walk_chunk_cap(uint32_t qpad) {
 }
 
 Tape lower(const Parsed &p, const LowerOptions &opt);
+
+// Independent-component probability of DEPOLARIZE1(p) and DEPOLARIZE2(p)
+// (Mixer.hpp:164,184): 0.5 - 0.5 sqrt(1 - 4p/3), 0.5 - 0.5 (1 - 16p/15)^(1/8).
+double split_dep1(double p);
+double split_dep2(double p);
 
 }  // namespace gpc

@@ -28,6 +28,7 @@
 #include <cstdint>
 
 #include "device.cuh"
+#include "lower.hpp"
 
 namespace gpc {
 namespace {
@@ -863,6 +864,10 @@ __global__ void __launch_bounds__(GW_WARPS * 32) group_warp_kernel(GroupLaunch L
     O[r] = (uint8_t)i;
   }
   __syncwarp();
+  // the saved permutation for the adjoint: mechanism at each sorted position
+  // (every key of this bucket is in shared memory already)
+  uint32_t *perm = reinterpret_cast<uint32_t *>(L.skey + base);
+  for (uint32_t s = lane; s < n; s += 32) perm[2 * s] = Mm[O[s]];
   // Groups, 32 sorted positions at a time.  Each group's probability is a
   // segmented inclusive scan of the XOR-merge over its run: log2(longest run
   // in the chunk) shuffle steps with every lane busy (FP64 throughput is
@@ -916,6 +921,7 @@ __global__ void __launch_bounds__(GW_WARPS * 32) group_warp_kernel(GroupLaunch L
     if (head) {
       L.stail[base + gh].m = Mm[i];
       L.stail[base + gh].t = tcount + inc - tv;
+      perm[2 * gh + 1] = s;
     }
     if (in && (s + 1 >= n || !key_eq(K[O[s + 1]], K[i]))) {  // the run's last item holds its value
       const uint32_t g = seg < 0 ? gcount - 1u : gcount + __popc(hb & ((1u << seg0) - 1u));
@@ -1058,10 +1064,13 @@ __global__ void __launch_bounds__(GB_THREADS) group_big_kernel(GroupLaunch L) {
     __syncthreads();
     if (seg < 0) x = xor_merge(c_carry[warp], x);
     const uint32_t gb = c_gbase[warp];
+    uint32_t *perm = reinterpret_cast<uint32_t *>(L.skey + base);
+    if (in) perm[2 * s] = sm[i];
     if (head) {
       const uint32_t g = gb + __popc(hb & ((1u << lane) - 1u));
       L.stail[base + g].m = sm[i];
       L.stail[base + g].t = c_tbase[warp] + inc - tv;
+      perm[2 * g + 1] = s;
     }
     if (in && (s + 1 >= n || !key_eq(sk[ord[s + 1]], sk[i]))) {
       const uint32_t g = seg < 0 ? gb - 1u : gb + __popc(hb & ((1u << seg0) - 1u));
@@ -1186,7 +1195,82 @@ __global__ void __launch_bounds__(GW_WARPS * 32) emit_kernel(GroupLaunch L) {
   }
 }
 
+// ---- noise-rate gradients ---------------------------------------------------
+
+// Channel kind of a record type: 0 X/Y/Z error or measurement flip, 1 DEPOLARIZE1, 2 DEPOLARIZE2.
+__device__ __forceinline__ uint32_t channel_kind(uint32_t type) {
+  return (type == REC_DEP1_L0 || type == REC_DEP1_L12) ? 1u : type >= REC_DEP2_L0 ? 2u : 0u;
+}
+
+__global__ void param_rec_kernel(ParamLaunch L) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= L.R) return;
+  const uint32_t src = L.rec_src[r];
+  if (src >= L.n_src) return;
+  L.rec_p[r] = L.qtab[(size_t)src * 3 + channel_kind((uint32_t)((L.rec[r] >> 56) & 15u))];
+}
+
+__global__ void __launch_bounds__(GW_WARPS * 32) adjoint_group_kernel(AdjointLaunch A) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t b = blockIdx.x * GW_WARPS + (threadIdx.x >> 5);
+  if (b >= A.nb) return;
+  const uint32_t n = A.count[b];
+  if (n == 0 || n > SLOT_CAP) return;
+  const uint32_t groups = A.bagg[b].x, out0 = A.bout[b].x;
+  const uint32_t *perm = reinterpret_cast<const uint32_t *>(A.skey + (size_t)b * SLOT_CAP);
+  for (uint32_t g = lane; g < groups; g += 32) {
+    const uint32_t s0 = perm[2 * g + 1], s1 = g + 1 < groups ? perm[2 * (g + 1) + 1] : n;
+    const double dl = A.grad_out[out0 + g];
+    double pre = 1.0;
+    for (uint32_t s = s0; s < s1; ++s) {
+      const uint32_t m = perm[2 * s];
+      A.gq[m] = pre;
+      pre *= 1.0 - 2.0 * A.mp[m];
+    }
+    double suf = 1.0;
+    for (uint32_t s = s1; s-- > s0;) {
+      const uint32_t m = perm[2 * s];
+      A.gq[m] = dl * A.gq[m] * suf;
+      suf *= 1.0 - 2.0 * A.mp[m];
+    }
+  }
+}
+
+__global__ void adjoint_record_kernel(AdjointLaunch A) {
+  const uint32_t r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= A.R) return;
+  const uint32_t src = A.rec_src[r];
+  if (src >= A.n_src) {
+    A.grad_rec[r] = 0.0;
+    return;
+  }
+  double sum = 0.0;
+  for (uint32_t m = A.rec_moff[r]; m < A.rec_moff[r + 1]; ++m) sum += A.gq[m];
+  A.grad_rec[r] = sum * A.stab[(size_t)src * 3 + channel_kind((uint32_t)((A.rec[r] >> 56) & 15u))];
+}
+
+__global__ void adjoint_source_kernel(AdjointLaunch A) {
+  const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+  if (e >= A.n_src) return;
+  double sum = 0.0;
+  for (uint32_t k = A.src_off[e]; k < A.src_off[e + 1]; ++k) sum += A.grad_rec[A.src_rec[k]];
+  A.grad_noise[e] = sum;
+}
+
 }  // namespace
+
+cudaError_t launch_param_rec(const ParamLaunch &L, cudaStream_t s) {
+  if (L.R == 0) return cudaSuccess;
+  param_rec_kernel<<<(L.R + 255) / 256, 256, 0, s>>>(L);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_adjoint(const AdjointLaunch &A, cudaStream_t s) {
+  if (A.nb) adjoint_group_kernel<<<(A.nb + GW_WARPS - 1) / GW_WARPS, GW_WARPS * 32, 0, s>>>(A);
+  if (A.R) adjoint_record_kernel<<<(A.R + 255) / 256, 256, 0, s>>>(A);
+  if (A.n_src) adjoint_source_kernel<<<(A.n_src + 255) / 256, 256, 0, s>>>(A);
+  return cudaGetLastError();
+}
 
 cudaError_t launch_key_prep(const KeyLaunch &L, cudaStream_t s) {
   if (L.M == 0) return cudaSuccess;

@@ -63,6 +63,8 @@ gpc_status gpc_tape_get_view(const gpc_tape *tape, gpc_tape_view *v) {
   v->rec = T.rec.data();
   v->rec_p = T.rec_p.data();
   v->rec_moff = T.rec_moff.data();
+  v->rec_src = T.rec_src.data();
+  v->num_ticks = T.n_ticks;
   return GPC_OK;
 }
 

@@ -211,5 +211,7 @@ class Tape:
             self.rec = arr(v.rec, v.num_records)
             self.rec_p = arr(v.rec_p, v.num_records)
             self.rec_moff = arr(v.rec_moff, v.num_records + 1)
+            self.rec_src = arr(v.rec_src, v.num_records)
+            self.num_ticks = int(v.num_ticks)
         finally:
             L.gpc_tape_free(h)

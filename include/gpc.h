@@ -112,6 +112,34 @@ gpc_status gpc_fetch(gpc_driver *driver, gpc_dem **out);
 gpc_status gpc_prepare_batch(gpc_driver *driver, const char *const *texts, const size_t *lens, int32_t n);
 gpc_status gpc_fetch_batch(gpc_driver *driver, gpc_dem **outs, int32_t n);
 
+/* ---- noise-rate gradients (differentiation form) ------------------------
+ * No counterpart in the reference (GreenPeas computes DEMs only).  A circuit
+ * is prepared as a template: each noise instruction's rate is read from a
+ * device FP64 tensor noise[num_ticks][4] instead of its text argument.  The
+ * tick of an instruction is the number of TICKs before it; classes: 0
+ * DEPOLARIZE2, 1 DEPOLARIZE1, 2 measurement flip (X/Y/Z_ERROR on a qubit
+ * whose last operation was not a reset, or a measurement's flip argument),
+ * 3 reset flip (X/Y/Z_ERROR on a qubit whose last operation was a reset).
+ * The template's noise instructions need non-zero text arguments (a zero
+ * rate creates no mechanisms); PAULI_CHANNEL_1 and E keep their text rates.
+ * All pointers below are device pointers; `stream` is the caller's CUDA
+ * stream (cudaStream_t): the driver's work is ordered after the caller's
+ * prior work on it, and the caller's later work after the driver's.
+ *   gpc_param_prepare  parse and upload the template; *num_ticks = TICKs + 1
+ *   gpc_param_forward  merged mechanisms for noise[] (then gpc_fetch gives
+ *                      the DEM: symptoms and probabilities, host arrays)
+ *   gpc_param_probs    the merged probabilities of the last forward
+ *                      (*num_errors of them, DEM order) into probs[]
+ *   gpc_param_backward grad_noise[num_ticks * 4] = dL/dnoise from
+ *                      grad_probs[*num_errors] = dL/dp of each merged
+ *                      mechanism (FP64 adjoint of the XOR-merge and of the
+ *                      channel splits; deterministic).  Returns after the
+ *                      gradient is written. */
+gpc_status gpc_param_prepare(gpc_driver *driver, const char *stim_text, size_t len, uint32_t *num_ticks);
+gpc_status gpc_param_forward(gpc_driver *driver, const double *noise, void *stream, uint32_t *num_errors);
+gpc_status gpc_param_probs(gpc_driver *driver, double *probs, void *stream);
+gpc_status gpc_param_backward(gpc_driver *driver, const double *grad_probs, double *grad_noise, void *stream);
+
 /* The driver's CUDA stream (a cudaStream_t), for callers that time it. */
 void *gpc_driver_stream(gpc_driver *driver);
 
@@ -119,10 +147,11 @@ void *gpc_driver_stream(gpc_driver *driver);
  * the driver's stream): [0] walk, [1] key, [2] sort, [3] merge, [4] total. */
 gpc_status gpc_last_timings(gpc_driver *driver, float *ms5);
 
-/* Algorithmic bytes moved by each kernel of the last run, counted from its
+/* Algorithmic bytes moved by each stage of the last run, counted from its
  * sizes: [0] walk (tape read + snapshots written), [1] key (records + snapshot
- * reads + keys, descriptors, target lists written), [2] bucket scan + scatter,
- * [3] merge (bucketed items + target lists read, DEM written). */
+ * reads + keys, descriptors, target lists and bucket slots written), [2]
+ * bucket grouping (slots read, lists compared, group records written), [3]
+ * scan + emit (group records and head lists read, DEM written). */
 gpc_status gpc_last_traffic(gpc_driver *driver, double *bytes4);
 
 /* Bytes copied host -> device by the last gpc_prepare (the tape) and device ->
@@ -183,6 +212,8 @@ typedef struct gpc_tape_view {
   const uint64_t *rec;        /* [num_records] noise records */
   const double *rec_p;        /* [num_records] */
   const uint32_t *rec_moff;   /* [num_records + 1] first mechanism of each record */
+  const uint32_t *rec_src;    /* [num_records] tick * 4 + class, 0xFFFFFFFF: no source */
+  uint32_t num_ticks;         /* TICK instructions + 1 */
 } gpc_tape_view;
 
 gpc_status gpc_tape_lower(const char *stim_text, size_t len, int32_t correlation_level, gpc_tape **out);

@@ -301,6 +301,13 @@ struct Result {
   std::vector<double> probs;
   std::vector<uint32_t> offsets;  // CSR over targets, size probs.size()+1
   std::vector<uint32_t> targets;  // detector d -> d, observable k -> numDetectors+k
+  // provenance of every raw component (for the noise-rate gradient)
+  uint32_t numTicks = 1;
+  std::vector<int32_t> rawGroup;  // merged error holding the component, -1 if dropped
+  std::vector<double> rawProb;    // the component's probability
+  std::vector<uint32_t> rawSrc;   // tick * 4 + class, 0xFFFFFFFF if none
+  std::vector<uint8_t> rawChan;   // 0 X/Y/Z error or measurement flip, 1 DEPOLARIZE1, 2 DEPOLARIZE2, 3 other
+  std::vector<double> rawArg;     // the instruction's probability argument
 };
 
 // Component lists for the correlation levels (Mixer.hpp:13-20).  Paulis are
@@ -451,6 +458,8 @@ struct Walker {
   // outputs
   bool counting;
   std::vector<double> *probs;  // filled when counting
+  std::vector<uint64_t> *origin = nullptr;  // (op << 32 | target) of each component, filled when counting
+  uint64_t curOp = 0, curT = 0;
   uint64_t *dense;              // [raw][wTotal] when writing
   uint64_t next = 0;
 
@@ -483,6 +492,7 @@ struct Walker {
   void emit(double p) {
     if (counting) {
       probs->push_back(p);
+      if (origin) origin->push_back(curOp << 32 | curT);
     } else {
       uint64_t *row = dense + next * wTotal + w0;
       for (uint32_t i = 0; i < ww; ++i) row[i] = tmp[i];
@@ -500,6 +510,8 @@ struct Walker {
       const Op &op = c.ops[oi];
       const GateDef *g = op.g;
       size_t nt = op.t.size();
+      curOp = oi;
+      curT = 0;
       switch (g->kind) {
         case K_C1:
           for (size_t ti = nt; ti-- > 0;) {
@@ -538,6 +550,7 @@ struct Walker {
           for (size_t ti = nt; ti-- > 0;) {
             uint32_t q = op.t[ti];
             uint32_t meas = c.measBase[oi] + (uint32_t)ti;
+            curT = ti;
             if (g->kind == K_MR) {
               std::fill(xr(q), xr(q) + ww, 0);
               std::fill(zr(q), zr(q) + ww, 0);
@@ -574,6 +587,7 @@ struct Walker {
         case K_N1: {
           for (size_t ti = nt; ti-- > 0;) {
             uint32_t q = op.t[ti];
+            curT = ti;
             switch (g->a) {
               case N1_X:
                 emitPauli1(q, 1, op.args.at(0));
@@ -607,6 +621,7 @@ struct Walker {
           double ps = splitDep2(op.args.at(0));
           for (size_t ti = nt; ti >= 2; ti -= 2) {
             uint32_t a = op.t[ti - 2], b = op.t[ti - 1];
+            curT = ti - 2;
             for (const Comp2 &cc : kDep2All) {
               if (!dep2Kept(level, cc)) continue;
               clearTmp();
@@ -683,6 +698,72 @@ inline uint64_t mix64(uint64_t x) {
   return x;
 }
 
+// Source of each raw component for the noise-rate gradient: the tick of its
+// instruction (TICKs before it) and its class -- 0 DEPOLARIZE2, 1
+// DEPOLARIZE1, 2 measurement flip (X/Y/Z_ERROR on a qubit whose last
+// operation was not a reset, or a measurement's flip argument), 3 reset flip
+// (X/Y/Z_ERROR on a qubit whose last operation was a reset).
+void provenance(const Circuit &c, const std::vector<uint64_t> &origin, const std::vector<double> &probs, Result &r) {
+  std::vector<std::vector<uint32_t>> src(c.ops.size());
+  std::vector<uint8_t> chan(c.ops.size(), 3);
+  std::vector<bool> afterReset(c.nq, false);
+  uint32_t tick = 0;
+  for (size_t i = 0; i < c.ops.size(); ++i) {
+    const Op &op = c.ops[i];
+    const GateDef *g = op.g;
+    src[i].assign(op.t.size(), 0xFFFFFFFFu);
+    if (g->kind == K_TICK) {
+      ++tick;
+      continue;
+    }
+    switch (g->kind) {
+      case K_N2:
+        chan[i] = 2;
+        for (size_t k = 0; k < op.t.size(); ++k) src[i][k] = tick * 4 + 0;
+        break;
+      case K_N1:
+        if (g->a == N1_DEP1) {
+          chan[i] = 1;
+          for (size_t k = 0; k < op.t.size(); ++k) src[i][k] = tick * 4 + 1;
+        } else if (g->a != N1_PC1) {
+          chan[i] = 0;
+          for (size_t k = 0; k < op.t.size(); ++k) src[i][k] = tick * 4 + (afterReset[op.t[k]] ? 3 : 2);
+        }
+        break;
+      case K_MEAS:
+      case K_MR:
+        chan[i] = 0;
+        for (size_t k = 0; k < op.t.size(); ++k) {
+          src[i][k] = tick * 4 + 2;
+          afterReset[op.t[k]] = g->kind == K_MR;
+        }
+        break;
+      case K_RESET:
+        for (uint32_t q : op.t) afterReset[q] = true;
+        break;
+      case K_C1:
+      case K_C2:
+        for (uint32_t q : op.t) afterReset[q] = false;
+        break;
+      default:
+        break;
+    }
+  }
+  r.numTicks = tick + 1;
+  const size_t raw = origin.size();
+  r.rawProb = probs;
+  r.rawSrc.resize(raw);
+  r.rawChan.resize(raw);
+  r.rawArg.resize(raw);
+  for (size_t i = 0; i < raw; ++i) {
+    const uint32_t oi = (uint32_t)(origin[i] >> 32), ti = (uint32_t)origin[i];
+    const Op &op = c.ops[oi];
+    r.rawSrc[i] = ti < src[oi].size() ? src[oi][ti] : 0xFFFFFFFFu;
+    r.rawChan[i] = chan[oi];
+    r.rawArg[i] = op.args.empty() ? 0.0 : op.args[0];
+  }
+}
+
 Result compile(const char *text, size_t len, int level, int threads) {
   Circuit c;
   Parser ps{text, text + len};
@@ -694,10 +775,12 @@ Result compile(const char *text, size_t len, int level, int threads) {
 
   // pass 0: enumerate components and their probabilities (word-independent)
   std::vector<double> probs;
+  std::vector<uint64_t> origin;
   {
     Walker wk(c, level, 0, 0, w);
     wk.counting = true;
     wk.probs = &probs;
+    wk.origin = &origin;
     wk.dense = nullptr;
     wk.run();
   }
@@ -752,6 +835,8 @@ Result compile(const char *text, size_t len, int level, int threads) {
   r.numQubits = c.nq;
   r.numRaw = raw;
   r.offsets.push_back(0);
+  provenance(c, origin, probs, r);
+  r.rawGroup.assign(raw, -1);
   size_t i = 0;
   while (i < idx.size()) {
     size_t j = i + 1;
@@ -762,6 +847,7 @@ Result compile(const char *text, size_t len, int level, int threads) {
     for (size_t k = i; k < j; ++k) {
       double q = probs[idx[k]];
       p = p * (1 - q) + q * (1 - p);
+      r.rawGroup[idx[k]] = (int32_t)r.probs.size();
     }
     const uint64_t *row = &dense[(size_t)idx[i] * w];
     for (uint32_t wd = 0; wd < w; ++wd) {
@@ -820,6 +906,19 @@ void oracle_arrays(const oracle_result *h, double *probs, uint32_t *offsets, uin
 }
 
 void oracle_free(oracle_result *h) { delete reinterpret_cast<Result *>(h); }
+
+uint32_t oracle_num_ticks(const oracle_result *h) { return reinterpret_cast<const Result *>(h)->numTicks; }
+
+// Provenance of the raw components (num_raw entries each, see oracle_info).
+void oracle_raw(const oracle_result *h, int32_t *group, double *prob, uint32_t *src, uint8_t *chan, double *arg) {
+  const Result *r = reinterpret_cast<const Result *>(h);
+  const size_t n = r->rawGroup.size();
+  memcpy(group, r->rawGroup.data(), n * sizeof(int32_t));
+  memcpy(prob, r->rawProb.data(), n * sizeof(double));
+  memcpy(src, r->rawSrc.data(), n * sizeof(uint32_t));
+  memcpy(chan, r->rawChan.data(), n * sizeof(uint8_t));
+  memcpy(arg, r->rawArg.data(), n * sizeof(double));
+}
 
 double oracle_split_dep1(double p) { return splitDep1(p); }
 double oracle_split_dep2(double p) { return splitDep2(p); }
