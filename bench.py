@@ -251,6 +251,96 @@ def batched_leg(gp, torch, local: int, flush, steps: int, warmup: int) -> dict:
     }
 
 
+def serving_leg(gp, requests: int, cap_requests: int, slots: int, max_batch: int, plain_sample: int) -> dict:
+    """Continuous batching: capacity (every request queued at once), then a Poisson trace at 80% of it.
+
+    Mix (seed 2): half rotated surface-code memory with d uniform in {5..25},
+    half bivariate-bicycle memory drawn from [[72,12,6]], [[144,12,12]],
+    [[288,12,18]], rounds = d, uniform noise with p log-uniform in [1e-4,
+    1e-2]; 120 GiB device-memory admission budget.  Latency is submit ->
+    result, host text to host DEM arrays."""
+    from greenpeas_gb300.serving import Server, replay
+    from greenpeas_gb300.workloads import ServingMix
+    mix = ServingMix(seed=2)
+    with Server(slots=slots, max_batch=max_batch, hbm_budget=120 << 30) as srv:
+        replay(srv, mix.requests(2 * slots * max_batch, 0.0))  # warm every worker
+        cap = replay(srv, mix.requests(cap_requests, 0.0))
+        rate = 0.8 * cap["dems_per_s"]
+        tr = replay(srv, mix.requests(requests, rate))
+    # the plain per-circuit path on the same mix: one driver, one circuit per compile
+    sample = mix.requests(plain_sample, 0.0)
+    drv = gp.get_driver(sample[0][1]())
+    texts = [f() for _, f in sample]
+    drv.compile(texts[0])
+    t0 = time.perf_counter()
+    for t in texts:
+        drv.compile(t)
+    plain = len(texts) / (time.perf_counter() - t0)
+    return {
+        "workload": "serving_mix_seed2_surface5-25_bb72-288_logp1e-4..1e-2", "slots": slots, "max_batch": max_batch,
+        "hbm_budget_bytes": 120 << 30,
+        "capacity": {"requests": cap["requests"], "dems_per_s": cap["dems_per_s"]},
+        "trace": {"requests": tr["requests"], "offered_per_s": rate, "dems_per_s": tr["dems_per_s"],
+                  "p50_ms": tr["p50_ms"], "p99_ms": tr["p99_ms"], "mean_ms": tr["mean_ms"], "max_ms": tr["max_ms"],
+                  "batches": tr["stats"]["batches"], "budget_peak_bytes": tr["stats"]["budget_peak"]},
+        "plain_e2e_dems_per_s": plain, "plain_sample": len(texts),
+        "speedup_capacity_vs_plain_e2e": cap["dems_per_s"] / plain,
+    }
+
+
+def grad_leg(gp, torch, reps: int = 20, fd_entries: int = 16) -> dict:
+    """Noise-rate gradients of the [[144,12,12]] memory (12 rounds): rates [num_ticks, 4] log-uniform in
+    [5e-4, 2e-3] (seed 1), loss sum_k w_k log p_k with w_k ~ N(0,1) keyed by the canonical symptom."""
+    import math
+    import numpy as np
+    from greenpeas_gb300 import noise as N
+    from greenpeas_gb300.autograd import NoiseRateDEM
+    tmpl = gp.BBCode(12).get_memory(12, 1e-3, noise="uniform")
+    model = NoiseRateDEM(tmpl)
+    rates = N.sample_rates(model.num_ticks, 5e-4, 2e-3, 1)
+    noise = torch.tensor(rates, dtype=torch.float64, device="cuda", requires_grad=True)
+    p = model(noise)
+    dem = model.last_dem()
+    w_np = N.symptom_weights(dem.offsets, dem.targets, seed=1)
+    w = torch.tensor(w_np, device="cuda")
+    fwd, bwd = [], []
+    for _ in range(reps):
+        noise.grad = None
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        p = model(noise)
+        loss = (w * torch.log(p)).sum()
+        torch.cuda.synchronize()
+        t1 = time.perf_counter()
+        loss.backward()
+        torch.cuda.synchronize()
+        fwd.append(t1 - t0)
+        bwd.append(time.perf_counter() - t1)
+    g = noise.grad.detach().cpu().numpy()
+
+    def L(r):
+        with torch.no_grad():
+            q = model(torch.tensor(r, dtype=torch.float64, device="cuda")).cpu().numpy()
+        return math.fsum(w_np * np.log(q))
+
+    rng = np.random.default_rng(1)
+    live = np.argwhere(g != 0)
+    worst = 0.0
+    h = 1e-7
+    for i, j in live[rng.choice(len(live), min(fd_entries, len(live)), replace=False)]:
+        rp, rm = rates.copy(), rates.copy()
+        rp[i, j] += h
+        rm[i, j] -= h
+        fd = (L(rp) - L(rm)) / (2 * h)
+        worst = max(worst, abs(fd - g[i, j]) / abs(g[i, j]))
+    fwd.sort()
+    bwd.sort()
+    return {"workload": "bb_144_12_12_r12_rates_seed1_logp5e-4..2e-3", "num_ticks": model.num_ticks,
+            "merged_mechanisms": int(dem.num_errors), "forward_ms": 1e3 * fwd[len(fwd) // 2],
+            "backward_ms": 1e3 * bwd[len(bwd) // 2], "fd_entries": int(min(fd_entries, len(live))), "fd_h": h,
+            "fd_max_rel_err": worst, "dtype": "f64"}
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -259,6 +349,11 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the mixed-size batch leg")
+    ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
+    ap.add_argument("--no-grad", action="store_true", help="skip the noise-rate gradient leg")
+    ap.add_argument("--serve-requests", type=int, default=10000)
+    ap.add_argument("--serve-slots", type=int, default=4)
+    ap.add_argument("--serve-batch", type=int, default=16)
     args = ap.parse_args()
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -372,6 +467,11 @@ def main() -> None:
     if not args.no_batch:
         line["batch"] = batched_leg(gp, torch, local, flush, steps=max(3, min(args.steps, 10)),
                                     warmup=args.warmup)
+    if not args.no_grad:
+        line["grad"] = grad_leg(gp, torch)
+    if not args.no_serve:
+        line["serve"] = serving_leg(gp, args.serve_requests, max(200, args.serve_requests // 10), args.serve_slots,
+                                    args.serve_batch, plain_sample=100)
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(text)
     print(json.dumps(line), flush=True)

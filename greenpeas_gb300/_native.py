@@ -27,6 +27,7 @@ EXPORTS = [
     "gpc_tape_lower", "gpc_tape_get_view", "gpc_tape_free", "gpc_tape_last_error", "gpc_last_traffic",
     "gpc_last_io_bytes", "gpc_merge_mechanisms_static", "gpc_prepare_batch", "gpc_fetch_batch",
     "gpc_param_prepare", "gpc_param_forward", "gpc_param_probs", "gpc_param_backward",
+    "gpc_server_create", "gpc_server_submit", "gpc_server_wait", "gpc_server_stats", "gpc_server_destroy",
 ]
 
 
@@ -36,6 +37,11 @@ class GpcError(RuntimeError):
     def __init__(self, status: int, message: str):
         self.status = status
         super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+
+
+class ServerOptions(ctypes.Structure):
+    _fields_ = [("device", ctypes.c_int32), ("correlation_level", ctypes.c_int32), ("slots", ctypes.c_uint32),
+                ("max_batch", ctypes.c_uint32), ("hbm_budget", ctypes.c_uint64), ("reserved", ctypes.c_uint32 * 4)]
 
 
 class Options(ctypes.Structure):
@@ -102,11 +108,19 @@ def lib() -> ctypes.CDLL:
     L.gpc_tape_free.argtypes = [vp]
     L.gpc_tape_free.restype = None
     L.gpc_tape_last_error.restype = ctypes.c_char_p
+    L.gpc_server_create.argtypes = [ctypes.POINTER(ServerOptions), ctypes.POINTER(vp)]
+    L.gpc_server_submit.argtypes = [vp, ctypes.c_char_p, sz, u64p]
+    L.gpc_server_wait.argtypes = [vp, ctypes.c_uint64, ctypes.c_double, ctypes.POINTER(vp),
+                                  ctypes.POINTER(ctypes.c_double)]
+    L.gpc_server_stats.argtypes = [vp, u64p, u64p, u64p, u64p]
+    L.gpc_server_destroy.argtypes = [vp]
+    L.gpc_server_destroy.restype = None
     L.gpc_param_prepare.argtypes = [vp, ctypes.c_char_p, sz, u32p]
     L.gpc_param_forward.argtypes = [vp, vp, vp, u32p]
     L.gpc_param_probs.argtypes = [vp, vp, vp]
     L.gpc_param_backward.argtypes = [vp, vp, vp, vp]
     for f in ("gpc_param_prepare", "gpc_param_forward", "gpc_param_probs", "gpc_param_backward",
+              "gpc_server_create", "gpc_server_submit", "gpc_server_wait", "gpc_server_stats",
               "gpc_get_driver", "gpc_compile", "gpc_compile_batch", "gpc_dem_arrays", "gpc_dem_info",
               "gpc_dem_text", "gpc_prepare", "gpc_run_device", "gpc_fetch", "gpc_last_timings",
               "gpc_last_sizes", "gpc_tape_lower", "gpc_tape_get_view", "gpc_last_traffic", "gpc_last_io_bytes",

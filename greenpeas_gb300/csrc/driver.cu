@@ -8,9 +8,15 @@
 // mechanisms (the reference copies the whole node x 32 class matrix,
 // Driver.hpp:158-161).
 #include <algorithm>
+#include <chrono>
 #include <cmath>
 #include <atomic>
+#include <condition_variable>
+#include <deque>
 #include <exception>
+#include <functional>
+#include <mutex>
+#include <unordered_map>
 #include <thread>
 #include <cstdio>
 #include <cstring>
@@ -164,6 +170,22 @@ struct gpc_driver {
   uint64_t *sk_sorted = nullptr;
   uint64_t sort_mask = ~0ull;
   bool force_global = false;  // test option: skip the bucket path (single circuits)
+  // Serving: called by prepare() with the device bytes it must add to the
+  // resident buffers and the bytes of all its buffers, before allocating them
+  // (may release the buffers, block or throw).
+  std::function<void(size_t, size_t)> admit;
+  size_t resident_bytes() const { return arena.cap + tgbuf.cap; }
+  // Frees the device buffers (a later prepare allocates them again).
+  void release_device_memory() {
+    if (stream) cudaStreamSynchronize(stream);
+    drop_graph();
+    arena.release();
+    tgbuf.release();
+    tg_cap = 0;
+    prepared = false;
+    ran = false;
+    last_run_sig = 0;
+  }
   // noise-rate gradients: record probabilities come from a device noise tensor
   bool param = false;
   const double *noise_dev = nullptr;
@@ -489,8 +511,13 @@ struct gpc_driver {
     layout();
     // The stream may still be reading the old arena: finish before regrowing.
     CK(cudaStreamSynchronize(stream));
-    arena.ensure(L.total);
     uint32_t want_tg = std::max<uint32_t>(1024u, (uint32_t)std::min<uint64_t>(0xFFFFFFF0ull, (uint64_t)L.M * 16));
+    if (admit) {
+      const size_t tgb = (size_t)std::max(want_tg, tg_cap) * 4;
+      const size_t grow = (L.total > arena.cap ? L.total - arena.cap : 0) + (tgb > tgbuf.cap ? tgb - tgbuf.cap : 0);
+      if (grow) admit(grow, L.total + tgb);
+    }
+    arena.ensure(L.total);
     if (want_tg > tg_cap) {
       tgbuf.ensure((size_t)want_tg * 4);
       tg_cap = want_tg;
@@ -1044,6 +1071,165 @@ gpc_status guarded(F &&f) {
 
 }  // namespace
 
+// ---- serving: continuous batching of compile requests ----------------------
+//
+// Requests wait in one FIFO queue.  Each of `slots` workers owns a resident
+// driver (its own stream and device buffers, kept between requests) and loops:
+// take every queued request up to max_batch, lower them on the host, admit
+// the device bytes its buffers must grow by against the HBM budget (waiting
+// until enough is free; a request that alone exceeds the budget fails), run
+// the batched pipeline, deliver each DEM.  Workers run concurrently, so one
+// batch's kernels overlap another's host lowering and kernels; requests that
+// arrive while the GPU is busy join the next batch of the first free worker.
+// When a worker waits for budget, others give their buffers back as they
+// finish a batch.
+struct gpc_server {
+  struct Req {
+    std::string text;
+    std::chrono::steady_clock::time_point t0, t1;
+    bool done = false;
+    gpc_status status = GPC_OK;
+    std::string msg;
+    gpc_dem *dem = nullptr;
+  };
+  int device = 0, level = 2;
+  uint32_t max_batch = 16;
+  size_t budget = 0, used = 0, peak = 0;
+  uint32_t budget_waiters = 0;
+  uint64_t next_ticket = 1, completed = 0, batches = 0;
+  bool stop = false;
+  std::mutex mu;
+  std::condition_variable cv_work, cv_done, cv_budget;
+  std::deque<uint64_t> queue;
+  std::unordered_map<uint64_t, std::unique_ptr<Req>> reqs;
+  std::vector<std::unique_ptr<gpc_driver>> drivers;
+  std::vector<size_t> held;  // budget bytes held by each worker's buffers
+  std::vector<std::thread> workers;
+
+  // Admits `grow` more bytes for worker w (whose buffers will total `total`).
+  // A worker that must wait first gives its own buffers back, so waiting
+  // workers hold nothing and the running ones can always finish and free.
+  void acquire(uint32_t w, size_t grow, size_t total) {
+    std::unique_lock<std::mutex> lk(mu);
+    if (total > budget) throw gpc::Error(GPC_ERR_CAPACITY, "the request needs more device memory than the serving budget");
+    if (used + grow <= budget) {
+      used += grow;
+      held[w] += grow;
+      peak = std::max(peak, used);
+      return;
+    }
+    used -= held[w];
+    held[w] = 0;
+    lk.unlock();
+    drivers[w]->release_device_memory();
+    lk.lock();
+    cv_budget.notify_all();
+    ++budget_waiters;
+    cv_budget.wait(lk, [&] { return stop || used + total <= budget; });
+    --budget_waiters;
+    if (stop) throw gpc::Error(GPC_ERR_INVALID, "server stopped");
+    used += total;
+    held[w] = total;
+    peak = std::max(peak, used);
+  }
+
+  void give_back(uint32_t w) {
+    drivers[w]->release_device_memory();
+    std::lock_guard<std::mutex> lk(mu);
+    used -= held[w];
+    held[w] = 0;
+    cv_budget.notify_all();
+  }
+
+  void deliver(uint64_t t, gpc_status st, const std::string &msg, gpc_dem *dem) {
+    std::lock_guard<std::mutex> lk(mu);
+    Req &r = *reqs.at(t);
+    r.status = st;
+    r.msg = msg;
+    r.dem = dem;
+    r.t1 = std::chrono::steady_clock::now();
+    r.done = true;
+    ++completed;
+  }
+
+  // Compiles tickets ts on worker w's driver (one batched pipeline).
+  void compile(uint32_t w, const std::vector<uint64_t> &ts) {
+    gpc_driver &d = *drivers[w];
+    std::vector<const char *> texts;
+    std::vector<size_t> lens;
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      for (uint64_t t : ts) {
+        texts.push_back(reqs.at(t)->text.data());
+        lens.push_back(reqs.at(t)->text.size());
+      }
+    }
+    d.prepare(texts.data(), lens.data(), (uint32_t)ts.size());
+    d.run();
+    std::vector<gpc_dem *> outs;
+    d.fetch_all(outs);
+    for (size_t i = 0; i < ts.size(); ++i) deliver(ts[i], GPC_OK, "", outs[i]);
+  }
+
+  void worker(uint32_t w) {
+    cudaSetDevice(device);
+    while (true) {
+      std::vector<uint64_t> ts;
+      {
+        std::unique_lock<std::mutex> lk(mu);
+        cv_work.wait(lk, [&] { return stop || !queue.empty(); });
+        if (stop) return;
+        while (!queue.empty() && ts.size() < max_batch) {
+          ts.push_back(queue.front());
+          queue.pop_front();
+        }
+      }
+      auto run_one_by_one = [&](const std::vector<uint64_t> &list) {
+        for (uint64_t t : list) {
+          try {
+            compile(w, {t});
+          } catch (const gpc::Error &e) {
+            deliver(t, e.code, e.what(), nullptr);
+          } catch (const std::exception &e) {
+            deliver(t, GPC_ERR_CUDA, e.what(), nullptr);
+          }
+        }
+      };
+      try {
+        compile(w, ts);
+      } catch (const gpc::Error &e) {
+        // one request's failure must not fail the others: compile them singly
+        if (ts.size() > 1) run_one_by_one(ts);
+        else deliver(ts[0], e.code, e.what(), nullptr);
+      } catch (const std::exception &e) {
+        if (ts.size() > 1) run_one_by_one(ts);
+        else deliver(ts[0], GPC_ERR_CUDA, e.what(), nullptr);
+      }
+      bool waiting;
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        ++batches;
+        waiting = budget_waiters > 0;
+      }
+      cv_done.notify_all();
+      if (waiting) give_back(w);
+    }
+  }
+
+  ~gpc_server() {
+    {
+      std::lock_guard<std::mutex> lk(mu);
+      stop = true;
+    }
+    cv_work.notify_all();
+    cv_budget.notify_all();
+    for (auto &t : workers)
+      if (t.joinable()) t.join();
+    for (auto &kv : reqs)
+      if (kv.second->dem) delete kv.second->dem;
+  }
+};
+
 extern "C" {
 
 const char *gpc_last_error(void) { return g_last_error.c_str(); }
@@ -1213,6 +1399,98 @@ gpc_status gpc_dem_text(const gpc_dem *dem_c, const char **text, size_t *len) {
 }
 
 void gpc_dem_free(gpc_dem *dem) { delete dem; }
+
+gpc_status gpc_server_create(const gpc_server_options *options, gpc_server **out) {
+  if (!out) return fail(GPC_ERR_INVALID, "out is null");
+  *out = nullptr;
+  gpc_server_options o{};
+  o.slots = 4;
+  o.max_batch = 16;
+  o.hbm_budget = 120ull << 30;
+  o.correlation_level = 2;
+  if (options) o = *options;
+  if (o.slots == 0 || o.slots > 64 || o.max_batch == 0 || o.hbm_budget == 0)
+    return fail(GPC_ERR_INVALID, "bad server options");
+  if (o.correlation_level < 0 || o.correlation_level > 2) return fail(GPC_ERR_INVALID, "bad correlation level");
+  std::unique_ptr<gpc_server> sv(new (std::nothrow) gpc_server());
+  if (!sv) return fail(GPC_ERR_OOM, "host allocation failed");
+  sv->device = o.device;
+  sv->level = o.correlation_level;
+  sv->max_batch = o.max_batch;
+  sv->budget = o.hbm_budget;
+  gpc_status st = guarded([&] {
+    int n = 0;
+    CK(cudaGetDeviceCount(&n));
+    if (sv->device < 0 || sv->device >= n) throw gpc::Error(GPC_ERR_CUDA, "no such CUDA device");
+    CK(cudaSetDevice(sv->device));
+    CK(gpc::walk_set_smem_limit());
+    sv->held.assign(o.slots, 0);
+    gpc_server *raw = sv.get();
+    for (uint32_t w = 0; w < o.slots; ++w) {
+      std::unique_ptr<gpc_driver> d(new gpc_driver());
+      d->device = sv->device;
+      d->level = sv->level;
+      d->init_streams();
+      d->admit = [raw, w](size_t grow, size_t total) { raw->acquire(w, grow, total); };
+      sv->drivers.push_back(std::move(d));
+    }
+    for (uint32_t w = 0; w < o.slots; ++w) sv->workers.emplace_back([raw, w] { raw->worker(w); });
+  });
+  if (st != GPC_OK) return st;
+  *out = sv.release();
+  return GPC_OK;
+}
+
+gpc_status gpc_server_submit(gpc_server *server, const char *stim_text, size_t len, uint64_t *ticket) {
+  if (!server || !stim_text || !ticket) return fail(GPC_ERR_INVALID, "null argument");
+  return guarded([&] {
+    auto r = std::make_unique<gpc_server::Req>();
+    r->text.assign(stim_text, len);
+    r->t0 = std::chrono::steady_clock::now();
+    {
+      std::lock_guard<std::mutex> lk(server->mu);
+      const uint64_t t = server->next_ticket++;
+      server->reqs.emplace(t, std::move(r));
+      server->queue.push_back(t);
+      *ticket = t;
+    }
+    server->cv_work.notify_one();
+  });
+}
+
+gpc_status gpc_server_wait(gpc_server *server, uint64_t ticket, double timeout_s, gpc_dem **out, double *latency_s) {
+  if (!server || !out) return fail(GPC_ERR_INVALID, "null argument");
+  *out = nullptr;
+  std::unique_ptr<gpc_server::Req> r;
+  {
+    std::unique_lock<std::mutex> lk(server->mu);
+    auto it = server->reqs.find(ticket);
+    if (it == server->reqs.end()) return fail(GPC_ERR_INVALID, "unknown ticket");
+    gpc_server::Req *p = it->second.get();
+    const auto until = std::chrono::steady_clock::now() + std::chrono::duration<double>(std::max(0.0, timeout_s));
+    if (!server->cv_done.wait_until(lk, until, [&] { return p->done; }))
+      return fail(GPC_ERR_TIMEOUT, "request not finished");
+    r = std::move(it->second);
+    server->reqs.erase(it);
+  }
+  if (latency_s) *latency_s = std::chrono::duration<double>(r->t1 - r->t0).count();
+  if (r->status != GPC_OK) return fail(r->status, r->msg);
+  *out = r->dem;
+  return GPC_OK;
+}
+
+gpc_status gpc_server_stats(gpc_server *server, uint64_t *completed, uint64_t *batches, uint64_t *budget_used,
+                            uint64_t *budget_peak) {
+  if (!server) return fail(GPC_ERR_INVALID, "server is null");
+  std::lock_guard<std::mutex> lk(server->mu);
+  if (completed) *completed = server->completed;
+  if (batches) *batches = server->batches;
+  if (budget_used) *budget_used = server->used;
+  if (budget_peak) *budget_peak = server->peak;
+  return GPC_OK;
+}
+
+void gpc_server_destroy(gpc_server *server) { delete server; }
 
 void gpc_driver_destroy(gpc_driver *driver) { delete driver; }
 

@@ -52,6 +52,48 @@ def batch_surface(n: int = 256, seed: int = 0, switch_prob: float = 0.1, p_lo: f
     return out
 
 
+_SENTINEL = 0.000123456789
+
+
+class ServingMix:
+    """The serving mix as per-request closures over cached templates.
+
+    A template per (code, d) is generated once with a sentinel rate; a
+    request's text replaces the sentinel with its own rate, so generating
+    10,000 requests costs one string substitution each."""
+
+    def __init__(self, seed: int = 2, p_lo: float = 1e-4, p_hi: float = 1e-2):
+        self.rng = np.random.default_rng(seed)
+        self.lo, self.hi = np.log10(p_lo), np.log10(p_hi)
+        self._tmpl: dict = {}
+
+    def _template(self, kind, d):
+        key = (kind, d)
+        if key not in self._tmpl:
+            code = _surface(d) if kind == "surface" else _bb(d)
+            self._tmpl[key] = code.get_memory(d, _SENTINEL, noise="uniform")
+        return self._tmpl[key]
+
+    def draw(self):
+        """(kind, d, p) of the next request."""
+        p = float(10 ** self.rng.uniform(self.lo, self.hi))
+        if self.rng.random() < 0.5:
+            return "surface", int(self.rng.choice(np.arange(5, 26, 2))), p
+        return "bb", int(self.rng.choice([6, 12, 18])), p
+
+    def text(self, kind, d, p) -> str:
+        from .codes import fmt_float
+        return self._template(kind, d).replace(f"({fmt_float(_SENTINEL)})", f"({fmt_float(p)})")
+
+    def requests(self, n: int, rate_hz: float):
+        """n (arrival time, text factory) pairs with Poisson arrivals at rate_hz (rate 0: all at once)."""
+        draws = [self.draw() for _ in range(n)]
+        t = np.cumsum(self.rng.exponential(1.0 / rate_hz, size=n)) if rate_hz > 0 else np.zeros(n)
+        for kind, d, _ in draws:
+            self._template(kind, d)
+        return [(float(a), (lambda k=k, d=d, p=p: self.text(k, d, p))) for a, (k, d, p) in zip(t, draws)]
+
+
 def serving_mix(n: int, rate_hz: float, seed: int = 2, p_lo: float = 1e-4, p_hi: float = 1e-2):
     """n requests: (arrival time in s, circuit text) with Poisson arrivals at rate_hz."""
     rng = np.random.default_rng(seed)

@@ -140,6 +140,38 @@ gpc_status gpc_param_forward(gpc_driver *driver, const double *noise, void *stre
 gpc_status gpc_param_probs(gpc_driver *driver, double *probs, void *stream);
 gpc_status gpc_param_backward(gpc_driver *driver, const double *grad_probs, double *grad_noise, void *stream);
 
+/* ---- serving: continuous batching of compile requests --------------------
+ * No counterpart in the reference (its Driver compiles one circuit per call,
+ * Driver.hpp:199-211).  A server owns `slots` workers, each with a resident
+ * driver (stream + device buffers kept between requests).  A free worker
+ * takes every queued request up to max_batch, lowers them, admits the device
+ * bytes its buffers must grow by against hbm_budget (waiting, after giving
+ * back its own buffers, until enough is free; a request that alone exceeds
+ * the budget fails with GPC_ERR_CAPACITY), and compiles them in one batched
+ * pipeline.  Workers run concurrently, so batches overlap on the device.
+ * Each DEM equals the one gpc_compile gives for the same circuit alone.
+ *   gpc_server_submit  queue a circuit (thread-safe); returns a ticket
+ *   gpc_server_wait    wait up to timeout_s for a ticket (GPC_ERR_TIMEOUT if
+ *                      not done; the ticket stays valid); on completion the
+ *                      ticket is consumed and *latency_s is submit -> done
+ *   gpc_server_stats   requests completed, batches run, budget bytes held
+ *                      now and at peak */
+typedef struct gpc_server gpc_server;
+typedef struct gpc_server_options {
+  int32_t device;
+  int32_t correlation_level; /* 0, 1, 2 */
+  uint32_t slots;            /* workers (resident drivers), default 4 */
+  uint32_t max_batch;        /* circuits per batch, default 16 */
+  uint64_t hbm_budget;       /* device bytes all workers' buffers may hold, default 120 GiB */
+  uint32_t reserved[4];
+} gpc_server_options;
+gpc_status gpc_server_create(const gpc_server_options *options, gpc_server **out);
+gpc_status gpc_server_submit(gpc_server *server, const char *stim_text, size_t len, uint64_t *ticket);
+gpc_status gpc_server_wait(gpc_server *server, uint64_t ticket, double timeout_s, gpc_dem **out, double *latency_s);
+gpc_status gpc_server_stats(gpc_server *server, uint64_t *completed, uint64_t *batches, uint64_t *budget_used,
+                            uint64_t *budget_peak);
+void gpc_server_destroy(gpc_server *server);
+
 /* The driver's CUDA stream (a cudaStream_t), for callers that time it. */
 void *gpc_driver_stream(gpc_driver *driver);
 
