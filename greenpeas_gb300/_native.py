@@ -28,6 +28,7 @@ EXPORTS = [
     "gpc_last_io_bytes", "gpc_merge_mechanisms_static", "gpc_prepare_batch", "gpc_fetch_batch",
     "gpc_param_prepare", "gpc_param_forward", "gpc_param_probs", "gpc_param_backward",
     "gpc_server_create", "gpc_server_submit", "gpc_server_wait", "gpc_server_stats", "gpc_server_destroy",
+    "gpc_device_dem",
 ]
 
 
@@ -108,6 +109,7 @@ def lib() -> ctypes.CDLL:
     L.gpc_tape_free.argtypes = [vp]
     L.gpc_tape_free.restype = None
     L.gpc_tape_last_error.restype = ctypes.c_char_p
+    L.gpc_device_dem.argtypes = [vp, i32, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp), u32p, u32p]
     L.gpc_server_create.argtypes = [ctypes.POINTER(ServerOptions), ctypes.POINTER(vp)]
     L.gpc_server_submit.argtypes = [vp, ctypes.c_char_p, sz, u64p]
     L.gpc_server_wait.argtypes = [vp, ctypes.c_uint64, ctypes.c_double, ctypes.POINTER(vp),
@@ -120,7 +122,7 @@ def lib() -> ctypes.CDLL:
     L.gpc_param_probs.argtypes = [vp, vp, vp]
     L.gpc_param_backward.argtypes = [vp, vp, vp, vp]
     for f in ("gpc_param_prepare", "gpc_param_forward", "gpc_param_probs", "gpc_param_backward",
-              "gpc_server_create", "gpc_server_submit", "gpc_server_wait", "gpc_server_stats",
+              "gpc_server_create", "gpc_server_submit", "gpc_server_wait", "gpc_server_stats", "gpc_device_dem",
               "gpc_get_driver", "gpc_compile", "gpc_compile_batch", "gpc_dem_arrays", "gpc_dem_info",
               "gpc_dem_text", "gpc_prepare", "gpc_run_device", "gpc_fetch", "gpc_last_timings",
               "gpc_last_sizes", "gpc_tape_lower", "gpc_tape_get_view", "gpc_last_traffic", "gpc_last_io_bytes",

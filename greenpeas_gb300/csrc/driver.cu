@@ -817,6 +817,36 @@ struct gpc_driver {
     throw gpc::Error(GPC_ERR_CUDA, "merge did not converge");
   }
 
+  // Device pointers to circuit i's merged mechanisms of the last run (no copy).
+  void device_dem(uint32_t i, const double **probs, const uint32_t **offsets, const uint32_t **targets,
+                  uint32_t *num_errors, uint32_t *targets_end) {
+    if (!ran) throw gpc::Error(GPC_ERR_INVALID, "nothing has been run");
+    if (i >= ncirc()) throw gpc::Error(GPC_ERR_INVALID, "circuit index out of range");
+    CK(cudaSetDevice(device));
+    uint32_t C = 0, NT = 0;
+    if (finish(&C, &NT) != Finish::Ok)
+      throw gpc::Error(GPC_ERR_UNSUPPORTED, "this batch was compiled circuit by circuit: no device arrays");
+    uint2 first = make_uint2(0, 0), next = make_uint2(C, NT);
+    pin_out.ensure(64);
+    uint32_t *h = static_cast<uint32_t *>(pin_out.p);
+    if (ncirc() > 1) {
+      CK(cudaMemcpyAsync(h, dptr<char>(L.cout) + (size_t)i * 8, i + 1 < ncirc() ? 16 : 8, cudaMemcpyDeviceToHost,
+                         stream));
+      CK(cudaStreamSynchronize(stream));
+      first = make_uint2(h[0], h[1]);
+      if (i + 1 < ncirc()) next = make_uint2(h[2], h[3]);
+    }
+    // the closing offset of the whole run (offsets are positions in the run's target array)
+    h[8] = NT;
+    CK(cudaMemcpyAsync(dptr<char>(L.out_off) + (size_t)C * 4, h + 8, 4, cudaMemcpyHostToDevice, stream));
+    CK(cudaStreamSynchronize(stream));
+    *probs = dptr<double>(L.out_prob) + first.x;
+    *offsets = dptr<uint32_t>(L.out_off) + first.x;
+    *targets = static_cast<const uint32_t *>(tgbuf.p);
+    *num_errors = next.x - first.x;
+    *targets_end = next.y;
+  }
+
   // ---- noise-rate gradients (one circuit) --------------------------------
   uint32_t n_src() const { return tapes.empty() ? 0 : tapes[0].n_ticks * gpc::SRC_CLASSES; }
 
@@ -1287,6 +1317,13 @@ gpc_status gpc_fetch_batch(gpc_driver *driver, gpc_dem **outs, int32_t n) {
     driver->fetch_all(v);
     for (int32_t i = 0; i < n; ++i) outs[i] = v[i];
   });
+}
+
+gpc_status gpc_device_dem(gpc_driver *driver, int32_t circuit, const double **probs, const uint32_t **offsets,
+                          const uint32_t **targets, uint32_t *num_errors, uint32_t *targets_end) {
+  if (!driver || !probs || !offsets || !targets || !num_errors || !targets_end || circuit < 0)
+    return fail(GPC_ERR_INVALID, "bad arguments");
+  return guarded([&] { driver->device_dem((uint32_t)circuit, probs, offsets, targets, num_errors, targets_end); });
 }
 
 gpc_status gpc_param_prepare(gpc_driver *driver, const char *stim_text, size_t len, uint32_t *num_ticks) {

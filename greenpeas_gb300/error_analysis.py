@@ -75,6 +75,7 @@ class Driver:
         L = _native.lib()
         self._h = ctypes.c_void_p()
         self.correlation_level = CorrelationLevel(correlation_level)
+        self.device = device
         opts = _native.Options()
         opts.device = device
         opts.sort_bits = sort_bits
@@ -137,6 +138,32 @@ class Driver:
         outs = (ctypes.c_void_p * n)()
         _native.check(_native.lib().gpc_fetch_batch(self._h, outs, n))
         return [dem_from_handle(ctypes.c_void_p(outs[i])) for i in range(n)]
+
+    def device_dem(self, circuit: int = 0):
+        """Circuit ``circuit``'s merged mechanisms of the last run as device arrays, without a copy.
+
+        Returns (probs, offsets, targets) as torch CUDA tensors viewing the
+        driver's buffers (valid until its next prepare/run/compile; do not
+        write them): probs[E] float64, offsets[E + 1] int32 positions in
+        targets (the run's whole target array, so offsets need not start at
+        0)."""
+        import torch
+        L = _native.lib()
+        pp, po, pt = ctypes.c_void_p(), ctypes.c_void_p(), ctypes.c_void_p()
+        n, end = ctypes.c_uint32(), ctypes.c_uint32()
+        _native.check(L.gpc_device_dem(self._h, int(circuit), ctypes.byref(pp), ctypes.byref(po), ctypes.byref(pt),
+                                       ctypes.byref(n), ctypes.byref(end)))
+
+        class _View:
+            def __init__(self, ptr, count, typestr):
+                self.__cuda_array_interface__ = {"shape": (count,), "typestr": typestr,
+                                                 "data": (ptr or 0, False), "version": 3, "strides": None}
+
+        dev = torch.device("cuda", self.device)
+        probs = torch.as_tensor(_View(pp.value, n.value, "<f8"), device=dev)
+        offsets = torch.as_tensor(_View(po.value, n.value + 1, "<i4"), device=dev)
+        targets = torch.as_tensor(_View(pt.value, end.value, "<i4"), device=dev)
+        return probs, offsets, targets
 
     # device-resident stages
     def prepare(self, circuit=None) -> None:

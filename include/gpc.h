@@ -112,6 +112,20 @@ gpc_status gpc_fetch(gpc_driver *driver, gpc_dem **out);
 gpc_status gpc_prepare_batch(gpc_driver *driver, const char *const *texts, const size_t *lens, int32_t n);
 gpc_status gpc_fetch_batch(gpc_driver *driver, gpc_dem **outs, int32_t n);
 
+/* ---- device-resident DEM for GPU consumers --------------------------------
+ * Replaces the text round trip of Driver::getDetectorErrorModel
+ * (Driver.hpp:166-194) for decoders on the same GPU: device pointers to
+ * circuit `circuit`'s merged mechanisms of the last run (0 for a single
+ * circuit; a batch index after gpc_prepare_batch + gpc_run_device), no copy.
+ * probs[num_errors]; offsets[num_errors + 1] are positions in `targets` (the
+ * run's whole target array), so error e has targets
+ * targets[offsets[e] .. offsets[e+1]); *targets_end = offsets[num_errors].
+ * Valid until the driver's next prepare, run or compile.  A batch that fell
+ * back to circuit-by-circuit compiles has no device arrays
+ * (GPC_ERR_UNSUPPORTED). */
+gpc_status gpc_device_dem(gpc_driver *driver, int32_t circuit, const double **probs, const uint32_t **offsets,
+                          const uint32_t **targets, uint32_t *num_errors, uint32_t *targets_end);
+
 /* ---- noise-rate gradients (differentiation form) ------------------------
  * No counterpart in the reference (GreenPeas computes DEMs only).  A circuit
  * is prepared as a template: each noise instruction's rate is read from a

@@ -15,6 +15,10 @@ It writes:
   circuits are hashed with their OBSERVABLE_INCLUDE lines removed, because
   this project's BB logical basis is its own.
 * ``kats.json`` -- known-answer values from the reference's unit tests.
+* ``circuits/iceberg_*.stim.gz`` -- the reference's concatenated
+  (iceberg + surface) fixture circuits, static and adaptive outer-check
+  schedules, circuit-level and phenomenological (data/circuits/iceberg_*.stim,
+  produced by ConcatenatedSurfaceCode.hpp:737-868), gzip-compressed verbatim.
 
 The tests never read the reference checkout; they read only these files.
 """
@@ -22,6 +26,7 @@ The tests never read the reference checkout; they read only these files.
 from __future__ import annotations
 
 import argparse
+import gzip
 import hashlib
 import json
 import re
@@ -75,6 +80,10 @@ def main() -> None:
             circ[path.stem] = {"sha256": hashlib.sha256(strip_observables(text).encode()).hexdigest(),
                                "observables": False}
     (HERE / "circuits.json").write_text(json.dumps(circ, indent=1, sort_keys=True) + "\n")
+    (HERE / "circuits").mkdir(exist_ok=True)
+    for path in sorted((ref / "data" / "circuits").glob("iceberg_*.stim")):
+        with open(HERE / "circuits" / (path.name + ".gz"), "wb") as f:
+            f.write(gzip.compress(path.read_bytes(), mtime=0))
     kats = {
         "dep1_split_p1e-3": {"value": 0.00033344451858030588, "tol": 1e-15,
                              "source": "tests/QEC/ErrorAnalysis/MixerTest.cpp:112"},

@@ -6,6 +6,7 @@ relative, same detector / observable counts.
 
 from __future__ import annotations
 
+import numpy as np
 import pytest
 
 import greenpeas_gb300 as gp
@@ -137,3 +138,33 @@ def test_driver_reuse_from_large_to_small_circuits():
         drv.run_device()
         drv.run_device()  # the second run comes from a captured graph
         assert drv.fetch() == gp.get_driver(text).compile(text)
+
+
+@pytest.mark.parametrize("name", ["iceberg_surface_4_static_circl", "iceberg_surface_4_adaptive_circl",
+                                  "iceberg_surface_6_static_circl", "iceberg_surface_6_adaptive_circl",
+                                  "iceberg_surface_6_static_pheno", "iceberg_surface_6_adaptive_pheno"])
+def test_concatenated_fixture_circuits(name):
+    """The reference's iceberg + surface circuits, static and adaptive outer-check schedules."""
+    from test_iceberg import load, noisy
+    text = noisy(load(name))
+    _check(gp.get_driver(text).compile(text), text)
+
+
+def test_device_dem_arrays_without_copy():
+    torch = pytest.importorskip("torch")
+    circs = [gp.SurfaceCode(3).get_memory(3, 1e-3, noise="uniform"), gp.BBCode(6).get_memory(2, 2e-3, noise="uniform")]
+    drv = gp.get_driver(circs[0])
+    dem = drv.compile(circs[0])
+    p, off, tg = drv.device_dem()
+    assert p.is_cuda and np.array_equal(p.cpu().numpy(), dem.probs)
+    assert np.array_equal(off.cpu().numpy().astype(np.uint32), dem.offsets)
+    assert np.array_equal(tg.cpu().numpy().astype(np.uint32), dem.targets)
+    drv.prepare_batch(circs)
+    drv.run_device()
+    host = drv.fetch_batch()
+    for i, d in enumerate(host):
+        p, off, tg = drv.device_dem(i)
+        o = off.cpu().numpy().astype(np.int64)
+        assert np.array_equal(p.cpu().numpy(), d.probs)
+        assert np.array_equal(o - o[0], d.offsets.astype(np.int64))
+        assert np.array_equal(tg.cpu().numpy()[o[0]:o[-1]].astype(np.uint32), d.targets)
