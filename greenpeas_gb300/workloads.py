@@ -70,8 +70,11 @@ class ServingMix:
     def _template(self, kind, d):
         key = (kind, d)
         if key not in self._tmpl:
+            from .codes import fmt_float
             code = _surface(d) if kind == "surface" else _bb(d)
-            self._tmpl[key] = code.get_memory(d, _SENTINEL, noise="uniform")
+            text = code.get_memory(d, _SENTINEL, noise="uniform")
+            # the template's bytes split at the sentinel rate: a request is one join
+            self._tmpl[key] = text.encode().split(f"({fmt_float(_SENTINEL)})".encode())
         return self._tmpl[key]
 
     def draw(self):
@@ -81,9 +84,10 @@ class ServingMix:
             return "surface", int(self.rng.choice(np.arange(5, 26, 2))), p
         return "bb", int(self.rng.choice([6, 12, 18])), p
 
-    def text(self, kind, d, p) -> str:
+    def text(self, kind, d, p) -> bytes:
+        """The request's stim text (bytes)."""
         from .codes import fmt_float
-        return self._template(kind, d).replace(f"({fmt_float(_SENTINEL)})", f"({fmt_float(p)})")
+        return f"({fmt_float(p)})".encode().join(self._template(kind, d))
 
     def requests(self, n: int, rate_hz: float):
         """n (arrival time, text factory) pairs with Poisson arrivals at rate_hz (rate 0: all at once)."""
