@@ -40,6 +40,13 @@ METRIC = "DEM compiles/s (plain method, one circuit per compile)"
 UNIT = "DEM/s"
 WORKLOAD = "bb_144_12_12_r12_uniform_p1e-3"
 PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
+# kernels of one run of the pipeline on one circuit: key-block table, walk, keys,
+# warp grouping, large-bucket grouping, scan, emit
+KERNELS_PER_RUN = 7
+# DRAM bytes (read + write) of one walk launch on the headline workload, from the ncu capture
+# summarised in profiles/headline_bb12_kernels.txt (cold cache: the tape is read once from DRAM,
+# the 28 word walks re-read it from L2, the snapshots stay in L2).
+WALK_DRAM_BYTES_PER_LAUNCH = 1_245_440
 
 
 def workload_text() -> str:
@@ -169,16 +176,37 @@ def dem_arrays_equal(a, b) -> bool:
             and np.array_equal(a.targets, b.targets) and np.array_equal(a.probs, b.probs))
 
 
-def batched_leg(gp, torch, local: int, flush, steps: int, warmup: int) -> dict:
+def batched_leg(gp, torch, local: int, flush, steps: int, warmup: int, circuits: int = 256,
+                device_only: bool = False) -> dict:
     """Mixed-size batch: one batched pipeline vs the plain per-circuit path on the same circuits.
 
     Device rates time only the kernel pipelines (CUDA events on the driver's
     stream, L2 flushed before each); e2e rates run host text to host arrays.
+    ``device_only`` times the batched pipeline alone (for profiling);
+    ``circuits`` takes the first circuits of the batch.
     """
     from greenpeas_gb300.workloads import batch_surface
-    texts = batch_surface()
+    texts = batch_surface()[:circuits]
     n = len(texts)
     dev = torch.device("cuda", local)
+    if device_only:
+        bdrv = gp.get_driver(texts[0], device=local)
+        bext = torch.cuda.ExternalStream(bdrv.stream, device=dev)
+        bdrv.prepare_batch(texts)
+        for _ in range(warmup):
+            bdrv.run_device()
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        with torch.cuda.stream(bext):
+            for i in range(steps):
+                flush.fill_(float(i))
+                ev[i][0].record(bext)
+                bdrv.run_device()
+                ev[i][1].record(bext)
+        torch.cuda.synchronize()
+        ms = sum(a.elapsed_time(b) for a, b in ev) / steps
+        bdrv.fetch_batch()
+        return {"circuits": n, "ms_per_batch": ms, "value": n / (ms / 1e3), "unit": UNIT, "device_only": True}
     # plain: one circuit per compile, the same driver reused
     plain = gp.get_driver(texts[0], device=local)
     ext = torch.cuda.ExternalStream(plain.stream, device=dev)
@@ -233,6 +261,16 @@ def batched_leg(gp, torch, local: int, flush, steps: int, warmup: int) -> dict:
     batch_e2e_s = (time.perf_counter() - t0) / e2e_steps
     h2d_b, d2h_b = bdrv.last_io_bytes()
     bmean = sum(batch_ms) / len(batch_ms)
+    # stage times and algorithmic bytes of one batched run (L2 flushed first)
+    with torch.cuda.stream(bext):
+        flush.fill_(0.5)
+    bdrv.run_device()
+    st = bdrv.last_timings()
+    tr = bdrv.last_traffic()
+    peak, peak_kind = peaks()
+    stages = {"walk": "walk", "key": "key", "sort": "bucket", "merge": "merge"}
+    roof = {k: {"ms": st[k], "algorithmic_bytes": tr[v], "achieved": tr[v] / (st[k] / 1e3) / 1e9,
+                "frac": tr[v] / (st[k] / 1e3) / 1e9 / peak} for k, v in stages.items()}
     plain_rate = n / (plain_ms / 1e3)
     batch_rate = n / (bmean / 1e3)
     return {
@@ -245,6 +283,8 @@ def batched_leg(gp, torch, local: int, flush, steps: int, warmup: int) -> dict:
         "plain": {"value": plain_rate, "unit": UNIT, "ms_total": plain_ms,
                   "mechanisms_per_s": {"raw": plain_rate * raw / n, "merged": plain_rate * merged / n},
                   "e2e": {"value": n / plain_e2e_s, "unit": UNIT}},
+        "roofline": {"bound": "hbm", "unit": "GB/s", "peak": peak, "peak_source": peak_kind, "stages": roof,
+                     "note": "walk bytes: each word's band of the tape (re-read from L2 across words) + snapshots"},
         "speedup_device": batch_rate / plain_rate,
         "speedup_e2e": plain_e2e_s / batch_e2e_s,
         "bit_exact_vs_plain": ok,
@@ -353,6 +393,9 @@ def main() -> None:
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-batch", action="store_true", help="skip the mixed-size batch leg")
+    ap.add_argument("--no-plain", action="store_true", help="skip the headline single-circuit leg (profiling)")
+    ap.add_argument("--batch-device-only", action="store_true", help="batch leg: time the batched pipeline alone")
+    ap.add_argument("--batch-circuits", type=int, default=256)
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
     ap.add_argument("--no-grad", action="store_true", help="skip the noise-rate gradient leg")
     ap.add_argument("--serve-requests", type=int, default=10000)
@@ -377,10 +420,18 @@ def main() -> None:
         dist.init_process_group("nccl", device_id=torch.device("cuda", local))
     import greenpeas_gb300 as gp
 
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    if args.no_plain:  # profiling runs: the batch leg alone
+        out = {"profiling": True}
+        if not args.no_batch:
+            out["batch"] = batched_leg(gp, torch, local, flush, steps=max(3, min(args.steps, 10)), warmup=args.warmup,
+                                       circuits=args.batch_circuits, device_only=args.batch_device_only)
+        if rank == 0:
+            print(json.dumps(out), flush=True)
+        return
     text = workload_text()
     drv = gp.get_driver(text, device=local)
     ext = torch.cuda.ExternalStream(drv.stream, device=torch.device("cuda", local))
-    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
     ref_dem = drv.compile(text)  # also checks the run completes without fallbacks
     sizes = drv.last_sizes()
 
@@ -463,14 +514,16 @@ def main() -> None:
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
-                     "algorithmic_bytes": traffic[names[dom]], "traffic": None,
+                     "algorithmic_bytes": traffic[names[dom]],
+                     "traffic": WALK_DRAM_BYTES_PER_LAUNCH if dom == "walk" else None,
                      "note": "latency-bound: one CTA per 64-bit detector word walks the circuit"},
-        "gpu_launches": 5 * args.steps,
+        "gpu_launches": KERNELS_PER_RUN * args.steps,
         "clocks": clocks.summary(),
     }
     if not args.no_batch:
         line["batch"] = batched_leg(gp, torch, local, flush, steps=max(3, min(args.steps, 10)),
-                                    warmup=args.warmup)
+                                    warmup=args.warmup, circuits=args.batch_circuits,
+                                    device_only=args.batch_device_only)
     if not args.no_grad:
         line["grad"] = grad_leg(gp, torch)
     if not args.no_serve:
