@@ -1,0 +1,42 @@
+"""The C ABI library (no GPU): it loads, and exports every function include/gpc.h declares.
+
+The declarations are read from the header itself, so a function added to the
+header but not to the library (or misspelled) fails here.  Nothing is called
+that needs a GPU.
+"""
+
+from __future__ import annotations
+
+import ctypes
+import re
+
+from conftest import ROOT
+from greenpeas_gb300 import _native
+
+
+def _declared() -> set:
+    text = (ROOT / "include" / "gpc.h").read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return set(re.findall(r"\b(gpc_[a-z0-9_]+)\s*\(", text))
+
+
+def test_header_declares_the_binding_list():
+    assert _declared() == set(_native.EXPORTS)
+
+
+def test_library_exports_every_declared_function():
+    lib = ctypes.CDLL(str(_native.LIB_PATH))
+    missing = [f for f in sorted(_declared()) if not hasattr(lib, f)]
+    assert not missing, missing
+
+
+def test_error_reporting_without_a_gpu():
+    L = _native.lib()
+    h = ctypes.c_void_p()
+    # a null text is rejected before any CUDA call
+    assert L.gpc_get_driver(None, 0, 2, None, ctypes.byref(h)) == -1
+    assert b"null" in L.gpc_last_error()
+    assert L.gpc_get_driver(b"H 0\n", 4, 7, None, ctypes.byref(h)) == -1  # bad correlation level
+    # tape lowering is host-only
+    t = ctypes.c_void_p()
+    assert L.gpc_tape_lower(b"FOO 0\n", 6, 2, ctypes.byref(t)) == -3
