@@ -87,7 +87,10 @@ struct WalkLaunch {
 };
 cudaError_t launch_walk(const WalkLaunch &L, cudaStream_t s);
 cudaError_t walk_set_smem_limit();  // call once per device before launching walks
-size_t walk_smem_bytes(uint32_t qpad, uint32_t chunk_cap);
+// Staged epoch/chunk table bytes for a launch (0: the tables are read from global memory).
+uint32_t walk_table_bytes(uint32_t max_epochs, uint32_t max_chunks);
+size_t walk_smem_bytes(uint32_t qpad, uint32_t chunk_cap, uint32_t table_bytes);
+uint32_t walk_max_threads(uint32_t qpt);  // 0: no walk instance for this many qubits per thread
 
 // Key kernel: one thread per noise record; expands the record into its
 // mechanisms (mdesc, mp), computes each mechanism's 128-bit key, and counts

@@ -170,6 +170,17 @@ struct gpc_driver {
   uint64_t *sk_sorted = nullptr;
   uint64_t sort_mask = ~0ull;
   bool force_global = false;  // test option: skip the bucket path (single circuits)
+  uint32_t walk_qpt = 0;      // qubits per walk thread (0: chosen per circuit)
+
+  static bool walk_qpt_fits(uint32_t qpad, uint32_t q) {
+    const uint32_t mt = gpc::walk_max_threads(q);
+    return mt && qpad % (32u * q) == 0 && qpad / q <= mt;
+  }
+  // Qubits per walk thread for a tape of qpad qubit slots.
+  uint32_t walk_qpt_for(uint32_t qpad) const {
+    if (walk_qpt && walk_qpt_fits(qpad, walk_qpt)) return walk_qpt;
+    return qpad <= 1024 ? 1u : qpad <= 2048 ? 2u : 4u;
+  }
   // Serving: called by prepare() with the device bytes it must add to the
   // resident buffers and the bytes of all its buffers, before allocating them
   // (may release the buffers, block or throw).
@@ -464,6 +475,7 @@ struct gpc_driver {
     std::vector<Tape> T(n);
     gpc::LowerOptions lo;
     lo.level = level;
+    if (n > 1) lo.chunk_min = gpc::kWalkChunkMin;
     auto one = [&](uint32_t i) {
       P[i] = gpc::parse_stim(texts[i], lens[i]);
       T[i] = gpc::lower(P[i], lo);
@@ -591,7 +603,7 @@ struct gpc_driver {
       wl.circs = dptr<CircuitDev>(L.cdev);
       wl.items = dptr<uint2>(L.items) + wc.item0;
       wl.n_items = wc.n_items;
-      wl.qpt = wc.qpad <= 1024 ? 1 : wc.qpad <= 2048 ? 2 : 4;
+      wl.qpt = walk_qpt_for(wc.qpad);
       wl.threads = wc.qpad / wl.qpt;
       wl.qpad = wc.qpad;
       wl.chunk_cap = wc.chunk_cap;
@@ -1278,6 +1290,9 @@ gpc_status gpc_get_driver(const char *stim_text, size_t len, int32_t correlation
     if (options->sort_bits < 0 || options->sort_bits > 64) return fail(GPC_ERR_INVALID, "sort_bits must be in 0..64");
     if (options->sort_bits) d->sort_bits = (uint32_t)options->sort_bits;
     d->force_global = options->global_sort != 0;
+    if (options->walk_qpt < 0 || (options->walk_qpt && !gpc::walk_max_threads((uint32_t)options->walk_qpt)))
+      return fail(GPC_ERR_INVALID, "walk_qpt must be 0, 1, 2, 3, 4, 6, 8, 12 or 16");
+    d->walk_qpt = (uint32_t)options->walk_qpt;
   }
   gpc_status st = guarded([&] {
     int n = 0;

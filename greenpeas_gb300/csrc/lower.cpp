@@ -782,7 +782,14 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
   }
   T.ep_ptoff[nE] = next;
   T.npoints = next;
-  // copy chunks: runs of whole epochs of at most chunk_cap bytes
+  // copy chunks: runs of whole epochs of at most chunk_cap bytes, chunk_cap
+  // sized from the largest epoch (and at least opt.chunk_min)
+  {
+    uint64_t big = 0;
+    for (uint32_t e = 0; e < nE; ++e) big = std::max<uint64_t>(big, (uint64_t)T.ep_k[e] * T.qpad * 8);
+    const uint64_t want = std::max<uint64_t>((big + 255) & ~(uint64_t)255, opt.chunk_min);
+    T.chunk_cap = (uint32_t)std::min<uint64_t>(walk_chunk_cap(T.qpad), want);
+  }
   T.ep_chunk.assign(nE, 0);
   for (uint32_t e = 0; e < nE;) {
     const uint32_t c = (uint32_t)T.ch_off.size();

@@ -131,15 +131,22 @@ struct Tape {
 
 enum : uint32_t { SRC_DEP2 = 0, SRC_DEP1 = 1, SRC_MEAS_FLIP = 2, SRC_RESET_FLIP = 3, SRC_CLASSES = 4 };
 
+// Smallest tape chunk for circuits compiled in a batch: chunks hold whole
+// epochs, and small chunks (sized from the tape's largest epoch) let several
+// walk CTAs share an SM.  A single circuit takes the largest chunk its walk's
+// shared memory holds (fewer chunk switches on its latency-bound walk).
+constexpr uint32_t kWalkChunkMin = 16 * 1024;
+
 struct LowerOptions {
   int level = 2;     // correlation level 0/1/2
   uint32_t kcap = 8; // max slots per epoch
+  uint32_t chunk_min = 0xFFFFFFFFu;  // smallest tape chunk (bytes; capped by the walk's shared memory)
 };
 
 // Shared-memory plan of the walk kernel (bytes): double-buffered tape chunks,
 // the published rows, and the epoch/chunk tables when they fit.
 constexpr uint32_t kWalkSmemBudget = 224 * 1024;  // of 227 KiB per CTA, leaving room for static shared memory
-constexpr uint32_t kWalkTableBudget = 32 * 1024;
+constexpr uint32_t kWalkTableBudget = 32 * 1024;  // most epoch/chunk table bytes a walk CTA stages
 constexpr uint32_t kWalkChunkMax = 96 * 1024;
 inline uint32_t walk_chunk_cap(uint32_t qpad) {
   const uint32_t pub = 2 * qpad * 16 + 128;

@@ -109,9 +109,15 @@ __device__ __forceinline__ uint64_t sel4(uint32_t m, uint64_t a, uint64_t b, uin
   return sel2(m & 3u, a, b) ^ sel2((m >> 2) & 3u, c, d);
 }
 
+// Largest block of each qubits-per-thread instance (registers: 4 QPT u64 of state per thread).
 template <int QPT>
-__global__ void __launch_bounds__(1024) walk_kernel(const CircuitDev *__restrict__ circs,
-                                                    const uint2 *__restrict__ items, uint32_t chunk_cap,
+struct WalkBound {
+  static constexpr int value = QPT <= 2 || QPT == 4 ? 1024 : QPT == 3 ? 512 : QPT <= 8 ? 256 : 128;
+};
+
+template <int QPT>
+__global__ void __launch_bounds__(WalkBound<QPT>::value) walk_kernel(const CircuitDev *__restrict__ circs,
+                                                    const uint2 *__restrict__ items, uint32_t chunk_cap, uint32_t table_bytes,
                                                     uint32_t *__restrict__ err) {
   extern __shared__ __align__(128) unsigned char smem[];
   const uint2 item = items[blockIdx.x];
@@ -137,9 +143,9 @@ __global__ void __launch_bounds__(1024) walk_kernel(const CircuitDev *__restrict
   uint2 *etab = reinterpret_cast<uint2 *>(smem + off);  // epoch e0+i: (op offset, slots | chunk << 8)
   const uint32_t c0 = C.ep_chunk[e0];
   const uint32_t ne = nE - e0, nc = C.n_chunks - c0;
-  const bool staged = ((size_t)ne + nc) * sizeof(uint2) <= kWalkTableBudget;
+  const bool staged = ((size_t)ne + nc) * sizeof(uint2) <= table_bytes;
   uint2 *ctab = etab + ne;  // chunk c0+i: (op offset, bytes)
-  off += kWalkTableBudget;
+  off += table_bytes;
   unsigned char *buf = smem + off;  // two buffers of chunk_cap bytes
   __shared__ uint32_t s_abort;
 
@@ -300,8 +306,13 @@ __global__ void __launch_bounds__(1024) walk_kernel(const CircuitDev *__restrict
 
 }  // namespace
 
-size_t walk_smem_bytes(uint32_t qpad, uint32_t chunk_cap) {
-  return (size_t)2 * qpad * sizeof(ulonglong2) + 128 + kWalkTableBudget + (size_t)2 * chunk_cap;
+uint32_t walk_table_bytes(uint32_t max_epochs, uint32_t max_chunks) {
+  const uint64_t b = ((uint64_t)max_epochs + max_chunks) * sizeof(uint2);
+  return b <= kWalkTableBudget ? (uint32_t)((b + 127) & ~(uint64_t)127) : 0u;
+}
+
+size_t walk_smem_bytes(uint32_t qpad, uint32_t chunk_cap, uint32_t table_bytes) {
+  return (size_t)2 * qpad * sizeof(ulonglong2) + 128 + table_bytes + (size_t)2 * chunk_cap;
 }
 
 // Raises the dynamic shared-memory limit of the walk kernels once (not a
@@ -321,15 +332,36 @@ cudaError_t walk_set_smem_limit() {
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
   if (e == cudaSuccess) e = walk_set_limit_one<1>(optin);
   if (e == cudaSuccess) e = walk_set_limit_one<2>(optin);
+  if (e == cudaSuccess) e = walk_set_limit_one<3>(optin);
   if (e == cudaSuccess) e = walk_set_limit_one<4>(optin);
+  if (e == cudaSuccess) e = walk_set_limit_one<6>(optin);
+  if (e == cudaSuccess) e = walk_set_limit_one<8>(optin);
+  if (e == cudaSuccess) e = walk_set_limit_one<12>(optin);
+  if (e == cudaSuccess) e = walk_set_limit_one<16>(optin);
   return e;
+}
+
+uint32_t walk_max_threads(uint32_t qpt) {
+  switch (qpt) {
+    case 1: return WalkBound<1>::value;
+    case 2: return WalkBound<2>::value;
+    case 3: return WalkBound<3>::value;
+    case 4: return WalkBound<4>::value;
+    case 6: return WalkBound<6>::value;
+    case 8: return WalkBound<8>::value;
+    case 12: return WalkBound<12>::value;
+    case 16: return WalkBound<16>::value;
+    default: return 0;
+  }
 }
 
 cudaError_t launch_walk(const WalkLaunch &L, cudaStream_t s) {
   if (L.n_items == 0) return cudaSuccess;
-  const size_t smem = walk_smem_bytes(L.qpad, L.chunk_cap);
+  const uint32_t tb = walk_table_bytes(L.max_epochs, L.max_chunks);
+  const size_t smem = walk_smem_bytes(L.qpad, L.chunk_cap, tb);
   if (smem > 227 * 1024 - 1024) return cudaErrorInvalidValue;
-#define GPC_WALK(Q) walk_kernel<Q><<<L.n_items, L.threads, smem, s>>>(L.circs, L.items, L.chunk_cap, L.err)
+  if (L.threads * L.qpt != L.qpad || L.threads % 32 || L.threads > walk_max_threads(L.qpt)) return cudaErrorInvalidValue;
+#define GPC_WALK(Q) walk_kernel<Q><<<L.n_items, L.threads, smem, s>>>(L.circs, L.items, L.chunk_cap, tb, L.err)
   switch (L.qpt) {
     case 1:
       GPC_WALK(1);
@@ -337,8 +369,23 @@ cudaError_t launch_walk(const WalkLaunch &L, cudaStream_t s) {
     case 2:
       GPC_WALK(2);
       break;
+    case 3:
+      GPC_WALK(3);
+      break;
     case 4:
       GPC_WALK(4);
+      break;
+    case 6:
+      GPC_WALK(6);
+      break;
+    case 8:
+      GPC_WALK(8);
+      break;
+    case 12:
+      GPC_WALK(12);
+      break;
+    case 16:
+      GPC_WALK(16);
       break;
     default:
       return cudaErrorInvalidValue;
