@@ -116,6 +116,7 @@ struct KeyLaunch {
   SlotTail *stail;          // [buckets * SLOT_CAP] slot tails
   uint32_t *list_total;     // += targets written to the lists (for traffic accounting)
   uint32_t *err;
+  uint32_t write_all;       // also write key[], and descriptors/probabilities (global path, gradients)
 };
 constexpr uint32_t KEY_THREADS = 256;
 inline uint32_t key_blocks(uint32_t M) { return (M + KEY_THREADS - 1) / KEY_THREADS; }

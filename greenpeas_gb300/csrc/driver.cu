@@ -634,10 +634,7 @@ struct gpc_driver {
     }
   }
 
-  void enqueue() {
-    CK(cudaMemsetAsync(dptr<char>(L.zero), 0, L.zero_bytes, stream));
-    for (uint32_t i = 0; i < ncirc(); ++i)
-      if (tapes[i].n_epochs == 0) CK(cudaMemsetAsync(dptr<char>(L.c[i].band), 0, (size_t)tapes[i].w * 8, stream));
+  gpc::KeyLaunch key_launch(bool write_all) {
     gpc::KeyLaunch kl{};
     kl.circs = dptr<CircuitDev>(L.cdev);
     kl.mbase = dptr<uint32_t>(L.mbase);
@@ -650,6 +647,15 @@ struct gpc_driver {
     kl.stail = dptr<gpc::SlotTail>(L.stail);
     kl.list_total = dptr<uint32_t>(L.totals) + 2;
     kl.err = dptr<uint32_t>(L.err);
+    kl.write_all = write_all ? 1u : 0u;
+    return kl;
+  }
+
+  void enqueue() {
+    CK(cudaMemsetAsync(dptr<char>(L.zero), 0, L.zero_bytes, stream));
+    for (uint32_t i = 0; i < ncirc(); ++i)
+      if (tapes[i].n_epochs == 0) CK(cudaMemsetAsync(dptr<char>(L.c[i].band), 0, (size_t)tapes[i].w * 8, stream));
+    const gpc::KeyLaunch kl = key_launch(param || (ncirc() == 1 && (force_global || lists_off)));
     rec(0);
     launch_walks(kl);
     rec(1);
@@ -795,7 +801,10 @@ struct gpc_driver {
         continue;
       }
       if ((err & gpc::DEV_FLAG_BIG_BUCKET) && !used_global) {
-        // a symptom repeated more often than one CTA holds: sort globally
+        // a symptom repeated more often than a bucket holds: sort globally
+        // (the bucket pass skipped the keys and descriptors this path reads)
+        CK(cudaMemsetAsync(dptr<char>(L.err), 0, 4, stream));
+        CK(gpc::launch_keys(key_launch(true), stream));
         CK(cudaMemsetAsync(dptr<char>(L.err), 0, 4, stream));
         run_global(false);
         continue;
@@ -998,8 +1007,9 @@ struct gpc_driver {
     const double M = L.M, lists = tot[2], groups = tot[0], targets = tot[1], nb = L.nb;
     const double per_list = M > 0 ? lists / M : 0.0;
     out[0] = walk;
-    // records, snapshot words in the bands, descriptor/probability/key/count, lists, bucket slots
-    out[1] = R * 20 + 16.0 * pts + M * (16 + 8 + 8 + 4) + 4.0 * lists + (double)nonempty * 32;
+    // records, snapshot words read, count (+ key, descriptor, probability when kept), lists, bucket slots
+    const bool all = param || (ncirc() == 1 && (force_global || lists_off));
+    out[1] = R * 20 + 16.0 * pts + M * (all ? 36 : 4) + 4.0 * lists + (double)nonempty * 32;
     // slots read, lists compared for the non-head items, group records written, counts and aggregates
     out[2] = (double)nonempty * 32 + (double)(nonempty - std::min<double>(nonempty, groups)) * 8.0 * per_list +
              groups * 16 + nb * 12;

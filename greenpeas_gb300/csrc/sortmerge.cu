@@ -166,8 +166,10 @@ __global__ void __launch_bounds__(KEY_THREADS) key_kernel(KeyLaunch L) {
   }
   if (Pb == 0) pb = 0;
   const double prob = __ldg(C.rec_p + r);
-  C.mdesc[m] = mk_desc(pa, Pa, pb, Pb);
-  C.mp[m] = prob;
+  if (L.write_all) {  // descriptors and probabilities: global merge path, gradients
+    C.mdesc[m] = mk_desc(pa, Pa, pb, Pb);
+    C.mp[m] = prob;
+  }
 
   const uint32_t tcap = C.tcap;
   uint64_t hx = 0, hy = 0;
@@ -205,7 +207,7 @@ __global__ void __launch_bounds__(KEY_THREADS) key_kernel(KeyLaunch L) {
     }
   }
   const ulonglong2 key = make_ulonglong2(hx, hy);
-  L.key[mg] = key;
+  if (L.write_all) L.key[mg] = key;
   if (tcap) {
     C.tn[m] = cnt;
     if (cnt > tcap) atomicOr(L.err, DEV_FLAG_LONG);
@@ -876,6 +878,7 @@ __global__ void __launch_bounds__(GW_WARPS * 32) group_warp_kernel(GroupLaunch L
   // a few ulps; it is deterministic.
   const uint32_t tcap = L.tcap;
   uint32_t gcount = 0, tcount = 0;
+  uint32_t carry_head = 0;  // item of the run open at the end of the previous chunk
   double carry = 0.0;
   for (uint32_t s0 = 0; s0 < n; s0 += 32) {
     const uint32_t s = s0 + lane;
@@ -885,18 +888,17 @@ __global__ void __launch_bounds__(GW_WARPS * 32) group_warp_kernel(GroupLaunch L
     if (in) {
       i = O[s];
       nt = T[i];
-      head = true;
-      if (s > 0) {
-        const uint32_t ip = O[s - 1];
-        if (key_eq(K[ip], K[i])) {
-          head = false;
-          const uint32_t m = Mm[i], mq = Mm[ip];
-          if (T[ip] != nt || !lists_equal(L.tl + (size_t)m * tcap, L.tl + (size_t)mq * tcap, nt))
-            atomicOr(L.err, DEV_ERR_COLLISION);
-        }
-      }
+      head = s == 0 || !key_eq(K[O[s - 1]], K[i]);
     }
     const uint32_t hb = __ballot_sync(0xFFFFFFFFu, head);
+    {
+      // collision check: every item of a run against the run's head (full target lists)
+      const uint32_t le0 = hb & (0xFFFFFFFFu >> (31u - lane));
+      const uint32_t ih = le0 ? (uint32_t)O[s0 + 31 - __clz(le0)] : carry_head;
+      if (in && !head && (T[ih] != nt || !lists_equal(L.tl + (size_t)Mm[i] * tcap, L.tl + (size_t)Mm[ih] * tcap, nt)))
+        atomicOr(L.err, DEV_ERR_COLLISION);
+      carry_head = __shfl_sync(0xFFFFFFFFu, ih, 31);
+    }
     const uint32_t tv = head ? nt : 0u;
     uint32_t inc = tv;
 #pragma unroll
