@@ -176,6 +176,24 @@ __global__ void __launch_bounds__(KEY_THREADS) key_kernel(KeyLaunch L) {
   uint32_t cnt = 0;
   bool nonzero = false;
   uint32_t *out = C.tl + (size_t)m * tcap;
+  // the first eight targets stay in registers and leave as two 16-byte stores
+  // (a row per thread: one scattered store per target would cost an L2
+  // transaction each); later ones are stored as they come
+  uint32_t t0 = 0, t1 = 0, t2 = 0, t3 = 0, t4 = 0, t5 = 0, t6 = 0, t7 = 0;
+  auto put = [&](uint32_t c, uint32_t v) {
+    switch (c) {
+      case 0: t0 = v; break;
+      case 1: t1 = v; break;
+      case 2: t2 = v; break;
+      case 3: t3 = v; break;
+      case 4: t4 = v; break;
+      case 5: t5 = v; break;
+      case 6: t6 = v; break;
+      case 7: t7 = v; break;
+      default:
+        if (c < tcap) out[c] = v;
+    }
+  };
   const ulonglong2 *snap = C.snap;
   const uint32_t np = C.npoints, mw = C.mw;
   const unsigned long long *ma = C.nzm + (size_t)pa * mw, *mb = C.nzm + (size_t)pb * mw;
@@ -199,7 +217,7 @@ __global__ void __launch_bounds__(KEY_THREADS) key_kernel(KeyLaunch L) {
       if (tcap) {
         uint64_t x = v;
         while (x) {
-          if (cnt < tcap) out[cnt] = j * 64u + (uint32_t)(__ffsll((long long)x) - 1);
+          put(cnt, j * 64u + (uint32_t)(__ffsll((long long)x) - 1));
           ++cnt;
           x &= x - 1;
         }
@@ -209,6 +227,9 @@ __global__ void __launch_bounds__(KEY_THREADS) key_kernel(KeyLaunch L) {
   const ulonglong2 key = make_ulonglong2(hx, hy);
   if (L.write_all) L.key[mg] = key;
   if (tcap) {
+    // rows are 16-byte aligned (tcap is a multiple of 4, at least 32)
+    if (cnt) reinterpret_cast<uint4 *>(out)[0] = make_uint4(t0, t1, t2, t3);
+    if (cnt > 4) reinterpret_cast<uint4 *>(out)[1] = make_uint4(t4, t5, t6, t7);
     C.tn[m] = cnt;
     if (cnt > tcap) atomicOr(L.err, DEV_FLAG_LONG);
     const uint32_t am = __activemask();
