@@ -45,8 +45,22 @@ def _stim_available() -> bool:
         return False
 
 
+class _DemHandle:
+    """Owns a gpc_dem; frees it when the last array viewing it is collected."""
+
+    def __init__(self, h: ctypes.c_void_p):
+        self.h = h
+
+    def __del__(self):
+        try:
+            _native.lib().gpc_dem_free(self.h)
+        except Exception:
+            pass
+
+
 def dem_from_handle(h: ctypes.c_void_p) -> DetectorErrorModel:
-    """Copies a gpc_dem into a DetectorErrorModel and frees the handle."""
+    """Wraps a gpc_dem in a DetectorErrorModel without copying its arrays; the handle is
+    freed once the DEM and every array taken from it are gone."""
     L = _native.lib()
     try:
         offs = ctypes.POINTER(ctypes.c_uint32)()
@@ -57,14 +71,28 @@ def dem_from_handle(h: ctypes.c_void_p) -> DetectorErrorModel:
         nd, no = ctypes.c_uint32(), ctypes.c_uint32()
         raw = ctypes.c_uint64()
         _native.check(L.gpc_dem_info(h, ctypes.byref(nd), ctypes.byref(no), ctypes.byref(raw)))
-        ne = n.value
-        offsets = np.ctypeslib.as_array(offs, shape=(ne + 1,)).copy()
-        nt = int(offsets[-1])
-        targets = np.ctypeslib.as_array(tg, shape=(nt,)).copy() if nt else np.zeros(0, np.uint32)
-        probs = np.ctypeslib.as_array(pr, shape=(ne,)).copy() if ne else np.zeros(0)
-        return DetectorErrorModel(probs, offsets, targets, nd.value, no.value, raw.value)
-    finally:
+    except Exception:
         L.gpc_dem_free(h)
+        raise
+    owner = _DemHandle(h)
+    ne = n.value
+    offsets = _owned(offs, ne + 1, np.uint32, owner)
+    nt = int(offsets[-1])
+    targets = _owned(tg, nt, np.uint32, owner)
+    probs = _owned(pr, ne, np.float64, owner)
+    return DetectorErrorModel(probs, offsets, targets, nd.value, no.value, raw.value)
+
+
+def _owned(ptr, n: int, dtype, owner) -> np.ndarray:
+    """Read-only numpy view of n elements at ptr whose base keeps ``owner`` (the gpc_dem) alive."""
+    if n == 0:
+        return np.zeros(0, dtype=dtype)
+    size = n * np.dtype(dtype).itemsize
+    buf = (ctypes.c_char * size).from_address(ctypes.addressof(ptr.contents))
+    buf._owner = owner  # the ctypes buffer object carries the handle
+    a = np.frombuffer(buf, dtype=dtype, count=n)
+    a.flags.writeable = False
+    return a
 
 
 class Driver:
