@@ -14,7 +14,7 @@ Lines printed (one JSON line on rank 0):
             between steps (a 512 MiB write, outside the timed window).
   e2e    -- the same metric through the C ABI from host text to host DEM
             arrays (parse + lowering + H2D + kernels + D2H), wall clock.
-  roofline, cpu_baseline, clocks, gpu_launches -- see the design doc.
+  roofline, cpu_baseline, clocks, gpu_launches, batch, grad, serve -- see main().
 
 ``--impl reference`` times the CPU FP64 oracle (a restatement of the
 reference's algorithm; the reference itself has no CPU path) on all host

@@ -47,7 +47,7 @@ enum {
   GPC_ERR_OOM = -5,         /* device or host allocation failed */
   GPC_ERR_COLLISION = -6,   /* two different symptoms share a 128-bit key */
   GPC_ERR_TIMEOUT = -7,     /* a bounded device wait gave up */
-  GPC_ERR_CAPACITY = -8     /* a size limit of this build was exceeded */
+  GPC_ERR_CAPACITY = -8     /* a size limit of the library was exceeded */
 };
 
 /* Correlation levels, as greenpeas.CorrelationLevel (Mixer.hpp:13-20). */
