@@ -52,6 +52,34 @@ struct CudaError : std::runtime_error {
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// Runs fn(i) for i in [0, n) on up to `threads` host threads (the calling
+// thread is one of them); rethrows the first exception after all joined.
+template <typename F>
+void parallel_for(uint32_t n, uint32_t threads, F &&fn) {
+  const uint32_t nt = std::max(1u, std::min(n, threads));
+  if (nt <= 1) {
+    for (uint32_t i = 0; i < n; ++i) fn(i);
+    return;
+  }
+  std::atomic<uint32_t> next{0};
+  std::vector<std::exception_ptr> errs(nt);
+  auto body = [&](uint32_t t) {
+    try {
+      for (uint32_t i; (i = next.fetch_add(1)) < n;) fn(i);
+    } catch (...) {
+      errs[t] = std::current_exception();
+    }
+  };
+  std::vector<std::thread> th;
+  for (uint32_t t = 1; t < nt; ++t) th.emplace_back(body, t);
+  body(0);
+  for (auto &x : th) x.join();
+  for (auto &e : errs)
+    if (e) std::rethrow_exception(e);
+}
+
+uint32_t host_threads() { return std::max(1u, std::thread::hardware_concurrency()); }
+
 // Grow-only device allocation.
 struct DevBuf {
   void *p = nullptr;
@@ -389,7 +417,8 @@ struct gpc_driver {
     };
     std::vector<CircuitDev> cd(N);
     std::vector<uint32_t> mb(N + 1), cb(N);
-    for (uint32_t i = 0; i < N; ++i) {
+    // circuits fill disjoint regions of the staging buffer: a batch copies in parallel
+    parallel_for(N, N >= 8 ? host_threads() : 1u, [&](uint32_t i) {
       const Tape &T = tapes[i];
       const CircLayout &l = L.c[i];
       put(l.ops, T.ops.data(), T.ops.size() * 8);
@@ -442,7 +471,7 @@ struct gpc_driver {
       c.bbits = l.bbits;
       mb[i] = l.mbase;
       cb[i] = l.bbase;
-    }
+    });
     mb[N] = L.M;
     put(L.cdev, cd.data(), cd.size() * sizeof(CircuitDev));
     put(L.mbase, mb.data(), mb.size() * 4);
@@ -1045,7 +1074,7 @@ struct gpc_driver {
     const uint2 *CO = reinterpret_cast<const uint2 *>(hc);
     outs.assign(N, nullptr);
     try {
-      for (uint32_t i = 0; i < N; ++i) {
+      parallel_for(N, N >= 8 ? host_threads() : 1u, [&](uint32_t i) {
         const uint32_t c0 = N > 1 ? CO[i].x : 0, c1 = (N > 1 && i + 1 < N) ? CO[i + 1].x : C;
         const uint32_t t0 = N > 1 ? CO[i].y : 0, t1 = (N > 1 && i + 1 < N) ? CO[i + 1].y : NT;
         if (c1 < c0 || c1 > C || t1 < t0 || t1 > NT) throw gpc::Error(GPC_ERR_CUDA, "inconsistent batch ranges");
@@ -1059,7 +1088,7 @@ struct gpc_driver {
         dem->offsets[c1 - c0] = t1 - t0;
         dem->targets.assign(TG + t0, TG + t1);
         outs[i] = dem.release();
-      }
+      });
     } catch (...) {
       for (auto &d : outs) delete d;
       outs.assign(N, nullptr);

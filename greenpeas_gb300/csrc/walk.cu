@@ -360,7 +360,7 @@ cudaError_t launch_walk(const WalkLaunch &L, cudaStream_t s) {
   const uint32_t tb = walk_table_bytes(L.max_epochs, L.max_chunks);
   const size_t smem = walk_smem_bytes(L.qpad, L.chunk_cap, tb);
   if (smem > 227 * 1024 - 1024) return cudaErrorInvalidValue;
-  if (L.threads * L.qpt != L.qpad || L.threads % 32 || L.threads > walk_max_threads(L.qpt)) return cudaErrorInvalidValue;
+  if (L.threads * L.qpt != L.qpad || L.threads > walk_max_threads(L.qpt)) return cudaErrorInvalidValue;
 #define GPC_WALK(Q) walk_kernel<Q><<<L.n_items, L.threads, smem, s>>>(L.circs, L.items, L.chunk_cap, tb, L.err)
   switch (L.qpt) {
     case 1:

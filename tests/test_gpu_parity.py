@@ -168,3 +168,13 @@ def test_device_dem_arrays_without_copy():
         assert np.array_equal(p.cpu().numpy(), d.probs)
         assert np.array_equal(o - o[0], d.offsets.astype(np.int64))
         assert np.array_equal(tg.cpu().numpy()[o[0]:o[-1]].astype(np.uint32), d.targets)
+
+
+def test_more_than_1024_qubits():
+    """Two qubits per walk thread; the packed slot count need not split into whole warps."""
+    text = gp.SurfaceCode(23).get_memory(2, 1e-3, noise="uniform")
+    t = gp.Tape(text)
+    assert t.num_qubits > 1024 and (t.qpad // 2) % 32 != 0  # 1,184 slots: 592 threads
+    _check(gp.get_driver(text).compile(text), text)
+    out = gp.get_driver(text).compile_batch([text, gp.SurfaceCode(3).get_memory(3, 1e-3, noise="uniform")])
+    _check(out[0], text)
