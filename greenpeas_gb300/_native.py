@@ -47,7 +47,7 @@ class ServerOptions(ctypes.Structure):
 
 class Options(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("sort_bits", ctypes.c_int32), ("global_sort", ctypes.c_int32),
-                ("walk_qpt", ctypes.c_int32), ("reserved", ctypes.c_int32 * 4)]
+                ("walk_qpt", ctypes.c_int32), ("bucket_mean", ctypes.c_int32), ("reserved", ctypes.c_int32 * 3)]
 
 
 class TapeView(ctypes.Structure):

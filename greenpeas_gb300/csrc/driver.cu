@@ -199,6 +199,7 @@ struct gpc_driver {
   uint64_t sort_mask = ~0ull;
   bool force_global = false;  // test option: skip the bucket path (single circuits)
   uint32_t walk_qpt = 0;      // qubits per walk thread (0: chosen per circuit)
+  uint32_t bucket_mean = 0;   // target mechanisms per bucket (0: from the run's size; buckets are a power of two per circuit)
 
   static bool walk_qpt_fits(uint32_t qpad, uint32_t q) {
     const uint32_t mt = gpc::walk_max_threads(q);
@@ -297,6 +298,15 @@ struct gpc_driver {
     };
     L.c.assign(N, CircLayout{});
     uint64_t M = 0, nb = 0, items = 0;
+    // Bucket size, from each circuit's own mechanism count (so a circuit gets
+    // the same buckets, and bit for bit the same DEM, alone and in a batch):
+    // small circuits are latency-bound and want more buckets (more warps in
+    // the grouping, fewer oversized buckets), large ones fewer (less
+    // per-bucket work).  Measured on GB300: 16 mechanisms per bucket up to
+    // 16k mechanisms, 48 up to 256k, then 96.
+    auto bmean_of = [&](uint64_t m) -> uint64_t {
+      return bucket_mean ? bucket_mean : m <= (16u << 10) ? 16 : m <= (256u << 10) ? 48 : 96;
+    };
     for (uint32_t i = 0; i < N; ++i) {
       const Tape &T = tapes[i];
       CircLayout &c = L.c[i];
@@ -313,9 +323,9 @@ struct gpc_driver {
       c.rec_p = take(T.rec_p.size() * 8);
       c.rec_moff = take(T.rec_moff.size() * 4);
       c.rec_src = take(T.rec_src.size() * 4);
-      // buckets: about 96 mechanisms each, a power of two between 2^4 and 2^16
+      // buckets: about bucket_mean mechanisms each, a power of two between 2^4 and 2^18
       uint32_t bb = 4;
-      while (bb < 16 && ((uint64_t)96 << bb) < T.M) ++bb;
+      while (bb < 18 && (bmean_of(T.M) << bb) < T.M) ++bb;
       c.mbase = (uint32_t)M;
       c.bbase = (uint32_t)nb;
       c.bbits = bb;
@@ -1332,6 +1342,9 @@ gpc_status gpc_get_driver(const char *stim_text, size_t len, int32_t correlation
     if (options->walk_qpt < 0 || (options->walk_qpt && !gpc::walk_max_threads((uint32_t)options->walk_qpt)))
       return fail(GPC_ERR_INVALID, "walk_qpt must be 0, 1, 2, 3, 4, 6, 8, 12 or 16");
     d->walk_qpt = (uint32_t)options->walk_qpt;
+    if (options->bucket_mean < 0 || (options->bucket_mean && (options->bucket_mean < 8 || options->bucket_mean > 128)))
+      return fail(GPC_ERR_INVALID, "bucket_mean must be 0 or 8..128");
+    d->bucket_mean = (uint32_t)options->bucket_mean;
   }
   gpc_status st = guarded([&] {
     int n = 0;

@@ -99,7 +99,8 @@ class Driver:
     """Owns a libgpc driver: device buffers, a CUDA stream, the parsed circuit."""
 
     def __init__(self, circuit, correlation_level: CorrelationLevel = CorrelationLevel.L2, *,
-                 device: int = 0, sort_bits: int = 0, global_sort: bool = False, walk_qpt: int = 0):
+                 device: int = 0, sort_bits: int = 0, global_sort: bool = False, walk_qpt: int = 0,
+                 bucket_mean: int = 0):
         L = _native.lib()
         self._h = ctypes.c_void_p()
         self.correlation_level = CorrelationLevel(correlation_level)
@@ -109,6 +110,7 @@ class Driver:
         opts.sort_bits = sort_bits
         opts.global_sort = 1 if global_sort else 0
         opts.walk_qpt = walk_qpt
+        opts.bucket_mean = bucket_mean
         text = _text(circuit)
         _native.check(L.gpc_get_driver(text, len(text), int(self.correlation_level), ctypes.byref(opts),
                                        ctypes.byref(self._h)))
