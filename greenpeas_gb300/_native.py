@@ -42,7 +42,8 @@ class GpcError(RuntimeError):
 
 class ServerOptions(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("correlation_level", ctypes.c_int32), ("slots", ctypes.c_uint32),
-                ("max_batch", ctypes.c_uint32), ("hbm_budget", ctypes.c_uint64), ("reserved", ctypes.c_uint32 * 4)]
+                ("max_batch", ctypes.c_uint32), ("hbm_budget", ctypes.c_uint64), ("lower_threads", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32 * 3)]
 
 
 class Options(ctypes.Structure):

@@ -542,6 +542,18 @@ struct gpc_driver {
     tapes = std::move(T);
   }
 
+  // Prepares circuits already lowered on the host (serving lowers requests as they arrive).
+  void prepare_tapes(std::vector<Tape> &&T) {
+    if (T.empty()) throw gpc::Error(GPC_ERR_INVALID, "empty batch");
+    param = false;
+    tcap = 32;
+    lists_off = false;
+    parsed.clear();
+    tapes = std::move(T);
+    have_tape = true;
+    prepare(nullptr, nullptr, 0);
+  }
+
   void prepare(const char *const *texts, const size_t *lens, uint32_t n, bool param_mode = false) {
     CK(cudaSetDevice(device));
     if (texts) {
@@ -1182,7 +1194,11 @@ struct gpc_server {
     gpc_status status = GPC_OK;
     std::string msg;
     gpc_dem *dem = nullptr;
+    std::unique_ptr<Tape> tape;  // lowered, waiting for a worker
   };
+  std::deque<uint64_t> lower_queue;  // submitted, not yet lowered
+  std::condition_variable cv_lower;
+  std::vector<std::thread> lowerers;
   int device = 0, level = 2;
   uint32_t max_batch = 16;
   size_t budget = 0, used = 0, peak = 0;
@@ -1243,19 +1259,72 @@ struct gpc_server {
     ++completed;
   }
 
-  // Compiles tickets ts on worker w's driver (one batched pipeline).
-  void compile(uint32_t w, const std::vector<uint64_t> &ts) {
-    gpc_driver &d = *drivers[w];
-    std::vector<const char *> texts;
-    std::vector<size_t> lens;
-    {
-      std::lock_guard<std::mutex> lk(mu);
-      for (uint64_t t : ts) {
-        texts.push_back(reqs.at(t)->text.data());
-        lens.push_back(reqs.at(t)->text.size());
+  // Lowering threads: parse and lower each request as it arrives (in
+  // parallel across requests), then hand it to the GPU workers.
+  void lowerer() {
+    gpc::LowerOptions lo;
+    lo.level = level;
+    lo.chunk_min = gpc::kWalkChunkMin;  // requests are compiled in batches
+    while (true) {
+      uint64_t t;
+      const char *text;
+      size_t len;
+      {
+        std::unique_lock<std::mutex> lk(mu);
+        cv_lower.wait(lk, [&] { return stop || !lower_queue.empty(); });
+        if (stop) return;
+        t = lower_queue.front();
+        lower_queue.pop_front();
+        text = reqs.at(t)->text.data();
+        len = reqs.at(t)->text.size();
+      }
+      try {
+        auto tape = std::make_unique<Tape>(gpc::lower(gpc::parse_stim(text, len), lo));
+        {
+          std::lock_guard<std::mutex> lk(mu);
+          reqs.at(t)->tape = std::move(tape);
+          queue.push_back(t);
+        }
+        cv_work.notify_one();
+      } catch (const gpc::Error &e) {
+        deliver(t, e.code, e.what(), nullptr);
+        cv_done.notify_all();
+      } catch (const std::bad_alloc &) {
+        deliver(t, GPC_ERR_OOM, "host allocation failed", nullptr);
+        cv_done.notify_all();
+      } catch (const std::exception &e) {
+        deliver(t, GPC_ERR_INVALID, e.what(), nullptr);
+        cv_done.notify_all();
       }
     }
-    d.prepare(texts.data(), lens.data(), (uint32_t)ts.size());
+  }
+
+  // Compiles tickets ts on worker w's driver (one batched pipeline over their
+  // lowered tapes, or from their texts when `from_text`).
+  void compile(uint32_t w, const std::vector<uint64_t> &ts, bool from_text) {
+    gpc_driver &d = *drivers[w];
+    if (from_text) {
+      std::vector<const char *> texts;
+      std::vector<size_t> lens;
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        for (uint64_t t : ts) {
+          texts.push_back(reqs.at(t)->text.data());
+          lens.push_back(reqs.at(t)->text.size());
+        }
+      }
+      d.prepare(texts.data(), lens.data(), (uint32_t)ts.size());
+    } else {
+      std::vector<Tape> tapes;
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        for (uint64_t t : ts) {
+          tapes.push_back(std::move(*reqs.at(t)->tape));
+          reqs.at(t)->tape.reset();
+        }
+      }
+      d.prepare_tapes(std::move(tapes));
+    }
     d.run();
     std::vector<gpc_dem *> outs;
     d.fetch_all(outs);
@@ -1278,7 +1347,7 @@ struct gpc_server {
       auto run_one_by_one = [&](const std::vector<uint64_t> &list) {
         for (uint64_t t : list) {
           try {
-            compile(w, {t});
+            compile(w, {t}, true);
           } catch (const gpc::Error &e) {
             deliver(t, e.code, e.what(), nullptr);
           } catch (const std::exception &e) {
@@ -1287,7 +1356,7 @@ struct gpc_server {
         }
       };
       try {
-        compile(w, ts);
+        compile(w, ts, false);
       } catch (const gpc::Error &e) {
         // one request's failure must not fail the others: compile them singly
         if (ts.size() > 1) run_one_by_one(ts);
@@ -1314,7 +1383,10 @@ struct gpc_server {
     }
     cv_work.notify_all();
     cv_budget.notify_all();
+    cv_lower.notify_all();
     for (auto &t : workers)
+      if (t.joinable()) t.join();
+    for (auto &t : lowerers)
       if (t.joinable()) t.join();
     for (auto &kv : reqs)
       if (kv.second->dem) delete kv.second->dem;
@@ -1539,6 +1611,8 @@ gpc_status gpc_server_create(const gpc_server_options *options, gpc_server **out
       sv->drivers.push_back(std::move(d));
     }
     for (uint32_t w = 0; w < o.slots; ++w) sv->workers.emplace_back([raw, w] { raw->worker(w); });
+    const uint32_t nl = o.lower_threads ? o.lower_threads : std::max(1u, std::thread::hardware_concurrency());
+    for (uint32_t i = 0; i < nl; ++i) sv->lowerers.emplace_back([raw] { raw->lowerer(); });
   });
   if (st != GPC_OK) return st;
   *out = sv.release();
@@ -1555,10 +1629,10 @@ gpc_status gpc_server_submit(gpc_server *server, const char *stim_text, size_t l
       std::lock_guard<std::mutex> lk(server->mu);
       const uint64_t t = server->next_ticket++;
       server->reqs.emplace(t, std::move(r));
-      server->queue.push_back(t);
+      server->lower_queue.push_back(t);
       *ticket = t;
     }
-    server->cv_work.notify_one();
+    server->cv_lower.notify_one();
   });
 }
 

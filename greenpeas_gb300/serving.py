@@ -4,9 +4,10 @@
         t = srv.submit(circuit)           # returns at once
         dem = srv.result(t)               # blocks until compiled
 
-The loop itself is native (``gpc_server_*`` in include/gpc.h): resident
-drivers, FIFO queue, batches formed from whatever is queued when a worker
-frees up, admission by device-memory footprint.  ``replay`` drives a server
+The loop itself is native (``gpc_server_*`` in include/gpc.h): requests are
+lowered on host threads as they arrive; GPU workers with resident drivers
+form batches from whatever is lowered when they free up, admitted by
+device-memory footprint.  ``replay`` drives a server
 with timed arrivals and reports throughput and latency percentiles.
 """
 
@@ -26,9 +27,9 @@ __all__ = ["Server", "replay"]
 
 class Server:
     def __init__(self, slots: int = 4, max_batch: int = 16, hbm_budget: int = 120 << 30, correlation_level: int = 2,
-                 device: int = 0):
+                 device: int = 0, lower_threads: int = 0):
         o = _native.ServerOptions(device=device, correlation_level=int(correlation_level), slots=slots,
-                                  max_batch=max_batch, hbm_budget=int(hbm_budget))
+                                  max_batch=max_batch, hbm_budget=int(hbm_budget), lower_threads=lower_threads)
         h = ctypes.c_void_p()
         _native.check(_native.lib().gpc_server_create(ctypes.byref(o), ctypes.byref(h)))
         self._h = h

@@ -158,9 +158,11 @@ gpc_status gpc_param_backward(gpc_driver *driver, const double *grad_probs, doub
 
 /* ---- serving: continuous batching of compile requests --------------------
  * No counterpart in the reference (its Driver compiles one circuit per call,
- * Driver.hpp:199-211).  A server owns `slots` workers, each with a resident
- * driver (stream + device buffers kept between requests).  A free worker
- * takes every queued request up to max_batch, lowers them, admits the device
+ * Driver.hpp:199-211).  Requests are lowered (parsed and scheduled into a
+ * tape) on `lower_threads` host threads as they arrive.  A server owns
+ * `slots` workers, each with a resident driver (stream + device buffers kept
+ * between requests).  A free worker takes every lowered request up to
+ * max_batch, admits the device
  * bytes its buffers must grow by against hbm_budget (waiting, after giving
  * back its own buffers, until enough is free; a request that alone exceeds
  * the budget fails with GPC_ERR_CAPACITY), and compiles them in one batched
@@ -179,7 +181,8 @@ typedef struct gpc_server_options {
   uint32_t slots;            /* workers (resident drivers), default 4 */
   uint32_t max_batch;        /* circuits per batch, default 16 */
   uint64_t hbm_budget;       /* device bytes all workers' buffers may hold, default 120 GiB */
-  uint32_t reserved[4];
+  uint32_t lower_threads;    /* host threads lowering requests as they arrive (0 = one per core) */
+  uint32_t reserved[3];
 } gpc_server_options;
 gpc_status gpc_server_create(const gpc_server_options *options, gpc_server **out);
 gpc_status gpc_server_submit(gpc_server *server, const char *stim_text, size_t len, uint64_t *ticket);
