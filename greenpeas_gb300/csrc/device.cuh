@@ -78,18 +78,19 @@ inline uint32_t merge_tiles(uint32_t n) { return (n + MERGE_THREADS - 1) / MERGE
 // ---- launch wrappers (defined in the .cu files) ----------------------------
 struct WalkLaunch {
   const CircuitDev *circs;  // device array
-  const uint2 *items;       // device array of (circuit, word)
+  const uint2 *items;       // device array of (circuit, first word of the CTA)
   uint32_t n_items;
   uint32_t threads, qpt, qpad;
   uint32_t chunk_cap;       // bytes of each of the two chunk buffers
   uint32_t max_epochs, max_chunks;  // largest tables of the launch (staged in shared memory if they fit)
+  uint32_t words;           // detector words per CTA (1, or 2 with 1 or 2 qubits per thread)
   uint32_t *err;
 };
 cudaError_t launch_walk(const WalkLaunch &L, cudaStream_t s);
 cudaError_t walk_set_smem_limit();  // call once per device before launching walks
 // Staged epoch/chunk table bytes for a launch (0: the tables are read from global memory).
 uint32_t walk_table_bytes(uint32_t max_epochs, uint32_t max_chunks);
-size_t walk_smem_bytes(uint32_t qpad, uint32_t chunk_cap, uint32_t table_bytes);
+size_t walk_smem_bytes(uint32_t qpad, uint32_t chunk_cap, uint32_t table_bytes, uint32_t words);
 uint32_t walk_max_threads(uint32_t qpt);  // 0: no walk instance for this many qubits per thread
 
 // Key kernel: one thread per noise record; expands the record into its

@@ -141,7 +141,7 @@ struct CircLayout {
 
 // One walk launch: circuits with the same thread count.
 struct WalkClass {
-  uint32_t qpad, item0, n_items, chunk_cap, max_epochs, max_chunks;
+  uint32_t qpad, item0, n_items, chunk_cap, max_epochs, max_chunks, words;
 };
 
 // Byte offsets of every array inside the arena (inputs first, so the whole
@@ -199,6 +199,7 @@ struct gpc_driver {
   uint64_t sort_mask = ~0ull;
   bool force_global = false;  // test option: skip the bucket path (single circuits)
   uint32_t walk_qpt = 0;      // qubits per walk thread (0: chosen per circuit)
+  uint32_t walk_words = 0;    // detector words per walk CTA (0: two in batches, one for a single circuit)
   uint32_t bucket_mean = 0;   // target mechanisms per bucket (0: from the run's size; buckets are a power of two per circuit)
 
   static bool walk_qpt_fits(uint32_t qpad, uint32_t q) {
@@ -400,16 +401,29 @@ struct gpc_driver {
     L.classes.clear();
     item_order = order;
     uint32_t item = 0;
+    circ_words.assign(N, 1);
     for (uint32_t k = 0; k < N;) {
       uint32_t e = k;
-      WalkClass wc{tapes[order[k]].qpad, item, 0, 0, 0, 0};
+      WalkClass wc{tapes[order[k]].qpad, item, 0, 0, 0, 0, 1};
       while (e < N && tapes[order[e]].qpad == wc.qpad) {
         const Tape &T = tapes[order[e]];
-        wc.n_items += T.w;
         wc.chunk_cap = std::max(wc.chunk_cap, T.chunk_cap);
         wc.max_epochs = std::max(wc.max_epochs, T.n_epochs);
         wc.max_chunks = std::max(wc.max_chunks, (uint32_t)T.ch_off.size());
         ++e;
+      }
+      // words per CTA: two in batches (half the CTAs; the walk is a chain of
+      // latency-bound epochs) when the qubits-per-thread instance and shared
+      // memory allow; one for a single circuit (latency)
+      const uint32_t want = walk_words ? walk_words : (N > 1 ? 2u : 1u);
+      const uint32_t q = walk_qpt_for(wc.qpad);
+      if (want == 2 && (q == 1 || q == 2) &&
+          gpc::walk_smem_bytes(wc.qpad, wc.chunk_cap, gpc::walk_table_bytes(wc.max_epochs, wc.max_chunks), 2) <=
+              227 * 1024 - 1024)
+        wc.words = 2;
+      for (uint32_t x = k; x < e; ++x) {
+        circ_words[order[x]] = wc.words;
+        wc.n_items += (tapes[order[x]].w + wc.words - 1) / wc.words;
       }
       item += wc.n_items;
       L.classes.push_back(wc);
@@ -417,6 +431,7 @@ struct gpc_driver {
     }
   }
   std::vector<uint32_t> item_order;  // circuits in walk-class order
+  std::vector<uint32_t> circ_words;  // detector words per walk CTA of each circuit
 
   void stage_inputs() {
     const uint32_t N = ncirc();
@@ -489,7 +504,7 @@ struct gpc_driver {
     std::vector<uint2> items;
     items.reserve(L.n_items);
     for (uint32_t i : item_order)
-      for (uint32_t j = 0; j < tapes[i].w; ++j) items.push_back(make_uint2(i, j));
+      for (uint32_t j = 0; j < tapes[i].w; j += circ_words[i]) items.push_back(make_uint2(i, j));
     put(L.items, items.data(), items.size() * sizeof(uint2));
     if (param) {
       // records of each (tick, class) source, in record order
@@ -607,6 +622,7 @@ struct gpc_driver {
       mix(c.chunk_cap);
       mix(c.max_epochs);
       mix(c.max_chunks);
+      mix(c.words);
     }
     cfg_sig = h;
     prepared = true;
@@ -660,6 +676,7 @@ struct gpc_driver {
       wl.chunk_cap = wc.chunk_cap;
       wl.max_epochs = wc.max_epochs;
       wl.max_chunks = wc.max_chunks;
+      wl.words = wc.words;
       wl.err = dptr<uint32_t>(L.err);
       CK(gpc::launch_walk(wl, s));
     };
@@ -1044,14 +1061,22 @@ struct gpc_driver {
       const Tape &T = tapes[i];
       std::vector<uint2> band(T.w);
       CK(cudaMemcpy(band.data(), dptr<char>(L.c[i].band), (size_t)T.w * 8, cudaMemcpyDeviceToHost));
-      for (uint32_t j = 0; j < T.w; ++j) {
-        if (band[j].y <= band[j].x) continue;
-        const uint32_t e0 = T.inj_lo[j];
-        uint32_t e1 = (uint32_t)(std::lower_bound(T.ep_ptoff.begin(), T.ep_ptoff.end(), band[j].y) - T.ep_ptoff.begin());
+      // one walk CTA per group of circuit-words: it reads the tape of its
+      // epochs once and writes each word's snapshots
+      const uint32_t W = circ_words.size() > i ? circ_words[i] : 1u;
+      for (uint32_t j0 = 0; j0 < T.w; j0 += W) {
+        const uint32_t nw = std::min(W, T.w - j0);
+        if (band[j0].y <= band[j0].x) continue;
+        uint32_t e0 = 0xFFFFFFFFu;
+        for (uint32_t j = j0; j < j0 + nw; ++j)
+          if (T.inj_lo[j] != 0xFFFFFFFFu) e0 = std::min(e0, T.inj_lo[j]);
+        if (e0 >= T.n_epochs) continue;
+        uint32_t e1 = (uint32_t)(std::lower_bound(T.ep_ptoff.begin(), T.ep_ptoff.end(), band[j0].y) - T.ep_ptoff.begin());
         if (e1 > T.n_epochs) e1 = T.n_epochs;
         const uint64_t a = T.ep_opoff[e0], b = e1 < T.n_epochs ? T.ep_opoff[e1] : T.ops.size();
-        walk += (double)(b - a) * 8 + 16.0 * (band[j].y - band[j].x);
-        pts += band[j].y - band[j].x;
+        const double p = (double)(band[j0].y - band[j0].x) * nw;
+        walk += (double)(b - a) * 8 + 16.0 * p;
+        pts += p;
       }
       R += (double)T.rec.size();
     }
@@ -1417,6 +1442,8 @@ gpc_status gpc_get_driver(const char *stim_text, size_t len, int32_t correlation
     if (options->bucket_mean < 0 || (options->bucket_mean && (options->bucket_mean < 8 || options->bucket_mean > 128)))
       return fail(GPC_ERR_INVALID, "bucket_mean must be 0 or 8..128");
     d->bucket_mean = (uint32_t)options->bucket_mean;
+    if (options->walk_words < 0 || options->walk_words > 2) return fail(GPC_ERR_INVALID, "walk_words must be 0, 1 or 2");
+    d->walk_words = (uint32_t)options->walk_words;
   }
   gpc_status st = guarded([&] {
     int n = 0;

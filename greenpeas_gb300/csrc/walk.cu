@@ -115,29 +115,42 @@ struct WalkBound {
   static constexpr int value = QPT <= 2 || QPT == 4 ? 1024 : QPT == 3 ? 512 : QPT <= 8 ? 256 : 128;
 };
 
-template <int QPT>
+// W detector words per CTA: the words j0 .. j0+W-1 of one circuit walk
+// together (rows W x 64 bits per qubit); a batch halves its CTAs with W = 2
+// while each epoch's latency chain stays about the same.
+template <int QPT, int W>
 __global__ void __launch_bounds__(WalkBound<QPT>::value) walk_kernel(const CircuitDev *__restrict__ circs,
                                                     const uint2 *__restrict__ items, uint32_t chunk_cap, uint32_t table_bytes,
                                                     uint32_t *__restrict__ err) {
   extern __shared__ __align__(128) unsigned char smem[];
   const uint2 item = items[blockIdx.x];
   const CircuitDev C = circs[item.x];
-  const uint32_t j = item.y;
+  const uint32_t j0 = item.y;
+  const uint32_t nw = min((uint32_t)W, C.w - j0);  // words of this CTA (the circuit's last group may be short)
   const uint32_t T = blockDim.x;
   const uint32_t tid = threadIdx.x;
   const uint32_t qpad = C.qpad;
   const uint32_t nE = C.n_epochs;
 
-  const uint32_t e0 = C.inj_lo[j];
-  if (e0 == 0xFFFFFFFFu || e0 >= nE) {
-    if (tid == 0) C.band[j] = make_uint2(0u, 0u);
+  // the CTA walks from the earliest first injection of its words to the
+  // latest last injection (and on until every row is zero)
+  uint32_t e0 = 0xFFFFFFFFu, elast = 0;
+#pragma unroll
+  for (int wi = 0; wi < W; ++wi) {
+    if ((uint32_t)wi >= nw) break;
+    const uint32_t lo = C.inj_lo[j0 + wi];
+    if (lo == 0xFFFFFFFFu || lo >= nE) continue;
+    e0 = min(e0, lo);
+    elast = max(elast, C.inj_hi[j0 + wi]);
+  }
+  if (e0 == 0xFFFFFFFFu) {
+    if (tid < nw) C.band[j0 + tid] = make_uint2(0u, 0u);
     return;
   }
-  const uint32_t elast = C.inj_hi[j];
 
   // shared memory: [published rows x2][mbarriers][tables][chunk buffer x2]
   ulonglong2 *pub = reinterpret_cast<ulonglong2 *>(smem);
-  size_t off = (size_t)2 * qpad * sizeof(ulonglong2);
+  size_t off = (size_t)2 * qpad * W * sizeof(ulonglong2);
   uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + off);
   off += 128;
   uint2 *etab = reinterpret_cast<uint2 *>(smem + off);  // epoch e0+i: (op offset, slots | chunk << 8)
@@ -183,16 +196,20 @@ __global__ void __launch_bounds__(WalkBound<QPT>::value) walk_kernel(const Circu
     if (nc > 1) issue();
   }
 
-  uint64_t X[QPT], Z[QPT], acc[QPT], last_inj[QPT];
+  uint64_t X[QPT][W], Z[QPT][W], acc[QPT][W], last_inj[QPT][W];
 #pragma unroll
-  for (int u = 0; u < QPT; ++u) X[u] = Z[u] = acc[u] = last_inj[u] = 0;
+  for (int u = 0; u < QPT; ++u)
+#pragma unroll
+    for (int wi = 0; wi < W; ++wi) X[u][wi] = Z[u][wi] = acc[u][wi] = last_inj[u][wi] = 0;
 
-  ulonglong2 *snap_j = C.snap + (size_t)j * C.npoints;
-  const uint32_t jlo = j * 64u;
-  // non-zero mask of each point: this word's bit in mask word j / 64
-  unsigned long long *nzm_j = C.nzm + (j >> 6);
+  const uint32_t np = C.npoints;
+  ulonglong2 *snap0 = C.snap + (size_t)j0 * np;  // word j0 + wi at + wi * np
+  const uint32_t jlo = j0 * 64u;
+  // non-zero masks: W divides 64 and groups start at multiples of W, so the
+  // CTA's words share one 64-bit mask word
+  unsigned long long *nzm0 = C.nzm + (j0 >> 6);
   const uint32_t mw = C.mw;
-  const unsigned long long jbit = 1ull << (j & 63u);
+  const uint32_t jsh = j0 & 63u;
   bool timed_out = false;
   uint32_t e = e0;
   uint32_t seq = 0;
@@ -201,16 +218,31 @@ __global__ void __launch_bounds__(WalkBound<QPT>::value) walk_kernel(const Circu
   const unsigned char *cbase = nullptr;
   uint32_t cbase_off = 0;
   uint2 ek_next = epoch(e0);
+  // stores the W words' snapshots of one point and sets their mask bits
+  auto snapshot = [&](uint32_t arg, const uint64_t *xs, const uint64_t *zs) {
+    unsigned long long bits = 0;
+#pragma unroll
+    for (int wi = 0; wi < W; ++wi) {
+      if ((uint32_t)wi < nw) {
+        snap0[(size_t)wi * np + arg] = make_ulonglong2(xs[wi], zs[wi]);
+        if (xs[wi] | zs[wi]) bits |= 1ull << (jsh + wi);
+      }
+    }
+    if (bits) atomicOr(nzm0 + arg * mw, bits);
+  };
   for (;; ++e, ++seq) {
-    // (1) publish rows (the state after epoch e-1)
-    ulonglong2 *pb = pub + (size_t)(seq & 1u) * qpad;
+    // (1) publish rows (the state after epoch e-1): slot s holds its W words at [s * W, s * W + W)
+    ulonglong2 *pb = pub + (size_t)(seq & 1u) * qpad * W;
     bool nz = false;
 #pragma unroll
-    for (int u = 0; u < QPT; ++u) {
-      asm volatile("st.shared.v2.u64 [%0], {%1, %2};" ::"r"(smem_u32(pb + tid + u * T)), "l"(X[u]), "l"(Z[u])
-                   : "memory");
-      nz |= (X[u] | Z[u]) != 0;
-    }
+    for (int u = 0; u < QPT; ++u)
+#pragma unroll
+      for (int wi = 0; wi < W; ++wi) {
+        asm volatile("st.shared.v2.u64 [%0], {%1, %2};" ::"r"(smem_u32(pb + (tid + u * T) * W + wi)),
+                     "l"(X[u][wi]), "l"(Z[u][wi])
+                     : "memory");
+        nz |= (X[u][wi] | Z[u][wi]) != 0;
+      }
     if (timed_out) s_abort = 1;
     // (2) the epoch barrier
     const int any = __syncthreads_or(nz ? 1 : 0);
@@ -248,51 +280,72 @@ __global__ void __launch_bounds__(WalkBound<QPT>::value) walk_kernel(const Circu
         const uint32_t opc = (uint32_t)op & 0xFFu;
         if (opc == OP_NOP) continue;
         const uint32_t arg = (uint32_t)(op >> 32);
+        const uint32_t pa = pub_s + arg * W * 16u;  // the partner slot's published words
         if (opc == OP_XPX) {
-          X[u] ^= lds64(pub_s + arg * 16u);
+#pragma unroll
+          for (int wi = 0; wi < W; ++wi) X[u][wi] ^= lds64(pa + wi * 16u);
         } else if (opc == OP_ZPZ) {
-          Z[u] ^= lds64(pub_s + arg * 16u + 8u);
+#pragma unroll
+          for (int wi = 0; wi < W; ++wi) Z[u][wi] ^= lds64(pa + wi * 16u + 8u);
         } else if (opc == OP_SNAP) {
-          snap_j[arg] = make_ulonglong2(X[u], Z[u]);
-          if (X[u] | Z[u]) atomicOr(nzm_j + arg * mw, jbit);
+          snapshot(arg, X[u], Z[u]);
         } else if (opc == OP_XPZ) {
-          X[u] ^= lds64(pub_s + arg * 16u + 8u);
+#pragma unroll
+          for (int wi = 0; wi < W; ++wi) X[u][wi] ^= lds64(pa + wi * 16u + 8u);
         } else {
           const uint32_t sub = ((uint32_t)op >> 8) & 0xFFu;
           if (opc == OP_C2) {
-            const ulonglong2 p = lds128(pub_s + arg * 16u);
-            const uint64_t x = X[u], z = Z[u];
-            X[u] = sel4(sub & 15u, x, z, p.x, p.y);
-            Z[u] = sel4(sub >> 4, x, z, p.x, p.y);
+#pragma unroll
+            for (int wi = 0; wi < W; ++wi) {
+              const ulonglong2 p = lds128(pa + wi * 16u);
+              const uint64_t x = X[u][wi], z = Z[u][wi];
+              X[u][wi] = sel4(sub & 15u, x, z, p.x, p.y);
+              Z[u][wi] = sel4(sub >> 4, x, z, p.x, p.y);
+            }
           } else if (opc == OP_C1) {
-            const uint64_t x = X[u], z = Z[u];
-            X[u] = sel2(sub & 3u, x, z);
-            Z[u] = sel2(sub >> 2, x, z);
+#pragma unroll
+            for (int wi = 0; wi < W; ++wi) {
+              const uint64_t x = X[u][wi], z = Z[u][wi];
+              X[u][wi] = sel2(sub & 3u, x, z);
+              Z[u][wi] = sel2(sub >> 2, x, z);
+            }
           } else if (opc == OP_R) {
-            X[u] = Z[u] = 0;
+#pragma unroll
+            for (int wi = 0; wi < W; ++wi) X[u][wi] = Z[u][wi] = 0;
           } else if (opc == OP_INJ) {
+            // measurement bits (one or two) that fall in this CTA's words
             const uint32_t b2 = ((uint32_t)op >> 8) & 0xFFFFFFu;
-            if (arg - jlo < 64u) acc[u] |= 1ull << (arg - jlo);
-            if (b2 != 0xFFFFFFu && b2 - jlo < 64u) acc[u] |= 1ull << (b2 - jlo);
+            const uint32_t d1 = arg - jlo, d2 = b2 - jlo;
+#pragma unroll
+            for (int wi = 0; wi < W; ++wi) {
+              if (d1 - wi * 64u < 64u) acc[u][wi] |= 1ull << (d1 & 63u);
+              if (b2 != 0xFFFFFFu && d2 - wi * 64u < 64u) acc[u][wi] |= 1ull << (d2 & 63u);
+            }
           } else if (opc == OP_M) {
-            uint64_t inj = acc[u];
-            if (arg - jlo < 64u) inj |= 1ull << (arg - jlo);
-            acc[u] = 0;
-            if (sub & 4u) X[u] = Z[u] = 0;
+            const uint32_t d1 = arg - jlo;
             const uint32_t basis = sub & 3u;
-            if (basis != 1u) X[u] ^= inj;
-            if (basis != 0u) Z[u] ^= inj;
-            last_inj[u] = inj;
+#pragma unroll
+            for (int wi = 0; wi < W; ++wi) {
+              uint64_t inj = acc[u][wi];
+              if (d1 - wi * 64u < 64u) inj |= 1ull << (d1 & 63u);
+              acc[u][wi] = 0;
+              if (sub & 4u) X[u][wi] = Z[u][wi] = 0;
+              if (basis != 1u) X[u][wi] ^= inj;
+              if (basis != 0u) Z[u][wi] ^= inj;
+              last_inj[u][wi] = inj;
+            }
           } else if (opc == OP_SNAPD) {
-            snap_j[arg] = make_ulonglong2(last_inj[u], 0ull);
-            if (last_inj[u]) atomicOr(nzm_j + arg * mw, jbit);
+            uint64_t zero[W];
+#pragma unroll
+            for (int wi = 0; wi < W; ++wi) zero[wi] = 0;
+            snapshot(arg, last_inj[u], zero);
           }
         }
       }
     }
   }
+  if (tid < nw) C.band[j0 + tid] = make_uint2(C.ep_ptoff[e0], C.ep_ptoff[e < nE ? e : nE]);
   if (tid == 0) {
-    C.band[j] = make_uint2(C.ep_ptoff[e0], C.ep_ptoff[e < nE ? e : nE]);
     // Copies still in flight target this CTA's shared memory: wait for them
     // (bounded) before the CTA exits.
     for (uint32_t i = waited; i < issued; ++i) {
@@ -311,18 +364,18 @@ uint32_t walk_table_bytes(uint32_t max_epochs, uint32_t max_chunks) {
   return b <= kWalkTableBudget ? (uint32_t)((b + 127) & ~(uint64_t)127) : 0u;
 }
 
-size_t walk_smem_bytes(uint32_t qpad, uint32_t chunk_cap, uint32_t table_bytes) {
-  return (size_t)2 * qpad * sizeof(ulonglong2) + 128 + table_bytes + (size_t)2 * chunk_cap;
+size_t walk_smem_bytes(uint32_t qpad, uint32_t chunk_cap, uint32_t table_bytes, uint32_t words) {
+  return (size_t)2 * qpad * words * sizeof(ulonglong2) + 128 + table_bytes + (size_t)2 * chunk_cap;
 }
 
 // Raises the dynamic shared-memory limit of the walk kernels once (not a
 // stream operation, so it is done here rather than inside a graph capture).
-template <int QPT>
+template <int QPT, int W>
 cudaError_t walk_set_limit_one(int optin) {
   cudaFuncAttributes a{};
-  cudaError_t e = cudaFuncGetAttributes(&a, walk_kernel<QPT>);
+  cudaError_t e = cudaFuncGetAttributes(&a, walk_kernel<QPT, W>);
   if (e != cudaSuccess) return e;
-  return cudaFuncSetAttribute(walk_kernel<QPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+  return cudaFuncSetAttribute(walk_kernel<QPT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                               optin - (int)a.sharedSizeBytes);
 }
 
@@ -330,14 +383,16 @@ cudaError_t walk_set_smem_limit() {
   int dev = 0, optin = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  if (e == cudaSuccess) e = walk_set_limit_one<1>(optin);
-  if (e == cudaSuccess) e = walk_set_limit_one<2>(optin);
-  if (e == cudaSuccess) e = walk_set_limit_one<3>(optin);
-  if (e == cudaSuccess) e = walk_set_limit_one<4>(optin);
-  if (e == cudaSuccess) e = walk_set_limit_one<6>(optin);
-  if (e == cudaSuccess) e = walk_set_limit_one<8>(optin);
-  if (e == cudaSuccess) e = walk_set_limit_one<12>(optin);
-  if (e == cudaSuccess) e = walk_set_limit_one<16>(optin);
+  if (e == cudaSuccess) e = walk_set_limit_one<1, 1>(optin);
+  if (e == cudaSuccess) e = walk_set_limit_one<2, 1>(optin);
+  if (e == cudaSuccess) e = walk_set_limit_one<3, 1>(optin);
+  if (e == cudaSuccess) e = walk_set_limit_one<4, 1>(optin);
+  if (e == cudaSuccess) e = walk_set_limit_one<6, 1>(optin);
+  if (e == cudaSuccess) e = walk_set_limit_one<8, 1>(optin);
+  if (e == cudaSuccess) e = walk_set_limit_one<12, 1>(optin);
+  if (e == cudaSuccess) e = walk_set_limit_one<16, 1>(optin);
+  if (e == cudaSuccess) e = walk_set_limit_one<1, 2>(optin);
+  if (e == cudaSuccess) e = walk_set_limit_one<2, 2>(optin);
   return e;
 }
 
@@ -358,10 +413,17 @@ uint32_t walk_max_threads(uint32_t qpt) {
 cudaError_t launch_walk(const WalkLaunch &L, cudaStream_t s) {
   if (L.n_items == 0) return cudaSuccess;
   const uint32_t tb = walk_table_bytes(L.max_epochs, L.max_chunks);
-  const size_t smem = walk_smem_bytes(L.qpad, L.chunk_cap, tb);
+  const size_t smem = walk_smem_bytes(L.qpad, L.chunk_cap, tb, L.words);
   if (smem > 227 * 1024 - 1024) return cudaErrorInvalidValue;
+  if (L.words != 1 && !(L.words == 2 && (L.qpt == 1 || L.qpt == 2))) return cudaErrorInvalidValue;
   if (L.threads * L.qpt != L.qpad || L.threads > walk_max_threads(L.qpt)) return cudaErrorInvalidValue;
-#define GPC_WALK(Q) walk_kernel<Q><<<L.n_items, L.threads, smem, s>>>(L.circs, L.items, L.chunk_cap, tb, L.err)
+#define GPC_WALK(Q) walk_kernel<Q, 1><<<L.n_items, L.threads, smem, s>>>(L.circs, L.items, L.chunk_cap, tb, L.err)
+#define GPC_WALK2(Q) walk_kernel<Q, 2><<<L.n_items, L.threads, smem, s>>>(L.circs, L.items, L.chunk_cap, tb, L.err)
+  if (L.words == 2) {
+    if (L.qpt == 1) GPC_WALK2(1);
+    else GPC_WALK2(2);
+    return cudaGetLastError();
+  }
   switch (L.qpt) {
     case 1:
       GPC_WALK(1);
@@ -391,6 +453,7 @@ cudaError_t launch_walk(const WalkLaunch &L, cudaStream_t s) {
       return cudaErrorInvalidValue;
   }
 #undef GPC_WALK
+#undef GPC_WALK2
   return cudaGetLastError();
 }
 
