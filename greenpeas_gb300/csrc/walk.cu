@@ -220,15 +220,20 @@ __global__ void __launch_bounds__(WalkBound<QPT>::value) walk_kernel(const Circu
   uint2 ek_next = epoch(e0);
   // stores the W words' snapshots of one point and sets their mask bits
   auto snapshot = [&](uint32_t arg, const uint64_t *xs, const uint64_t *zs) {
-    unsigned long long bits = 0;
+    if constexpr (W == 1) {
+      snap0[arg] = make_ulonglong2(xs[0], zs[0]);
+      if (xs[0] | zs[0]) atomicOr(nzm0 + arg * mw, 1ull << jsh);
+    } else {
+      unsigned long long bits = 0;
 #pragma unroll
-    for (int wi = 0; wi < W; ++wi) {
-      if ((uint32_t)wi < nw) {
-        snap0[(size_t)wi * np + arg] = make_ulonglong2(xs[wi], zs[wi]);
-        if (xs[wi] | zs[wi]) bits |= 1ull << (jsh + wi);
+      for (int wi = 0; wi < W; ++wi) {
+        if ((uint32_t)wi < nw) {
+          snap0[(size_t)wi * np + arg] = make_ulonglong2(xs[wi], zs[wi]);
+          if (xs[wi] | zs[wi]) bits |= 1ull << (jsh + wi);
+        }
       }
+      if (bits) atomicOr(nzm0 + arg * mw, bits);
     }
-    if (bits) atomicOr(nzm0 + arg * mw, bits);
   };
   for (;; ++e, ++seq) {
     // (1) publish rows (the state after epoch e-1): slot s holds its W words at [s * W, s * W + W)
@@ -335,10 +340,15 @@ __global__ void __launch_bounds__(WalkBound<QPT>::value) walk_kernel(const Circu
               last_inj[u][wi] = inj;
             }
           } else if (opc == OP_SNAPD) {
-            uint64_t zero[W];
+            if constexpr (W == 1) {
+              snap0[arg] = make_ulonglong2(last_inj[u][0], 0ull);
+              if (last_inj[u][0]) atomicOr(nzm0 + arg * mw, 1ull << jsh);
+            } else {
+              uint64_t zero[W];
 #pragma unroll
-            for (int wi = 0; wi < W; ++wi) zero[wi] = 0;
-            snapshot(arg, last_inj[u], zero);
+              for (int wi = 0; wi < W; ++wi) zero[wi] = 0;
+              snapshot(arg, last_inj[u], zero);
+            }
           }
         }
       }
