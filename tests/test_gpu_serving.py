@@ -38,12 +38,23 @@ def test_results_are_the_same_alone_and_in_the_mix():
         rep = replay(srv, list(zip(arrivals, circs)), keep=set(range(len(circs))))
         st = srv.stats()
     assert rep["requests"] == len(circs) and st["completed"] == len(circs)
-    assert st["batches"] < len(circs)  # requests were batched
     for i, text in enumerate(circs):
         assert rep["dems"][i] == gp.get_driver(text).compile(text)
     for i in (0, 1, 7):
         ref = O.compile_text(circs[i], 2)
         compare_errors(dict(rep["dems"][i].errors()), dict(ref.errors()), rel=1e-12)
+
+
+def test_a_burst_is_batched():
+    """Requests that arrive together while the only worker is busy leave in shared batches."""
+    circs = _mix(24, seed=4)
+    with Server(slots=1, max_batch=8) as srv:
+        rep = replay(srv, [(0.0, c) for c in circs], keep=set(range(len(circs))))
+        st = srv.stats()
+    assert st["completed"] == len(circs)
+    assert st["batches"] < len(circs)
+    for i, text in enumerate(circs):
+        assert rep["dems"][i] == gp.get_driver(text).compile(text)
 
 
 def test_admission_by_device_memory():
