@@ -26,6 +26,7 @@
 
 #include "../../include/gpc.h"
 #include "device.cuh"
+#include "host_pool.hpp"
 #include "lower.hpp"
 
 using gpc::CircuitDev;
@@ -54,30 +55,6 @@ size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
 // Runs fn(i) for i in [0, n) on up to `threads` host threads (the calling
 // thread is one of them); rethrows the first exception after all joined.
-template <typename F>
-void parallel_for(uint32_t n, uint32_t threads, F &&fn) {
-  const uint32_t nt = std::max(1u, std::min(n, threads));
-  if (nt <= 1) {
-    for (uint32_t i = 0; i < n; ++i) fn(i);
-    return;
-  }
-  std::atomic<uint32_t> next{0};
-  std::vector<std::exception_ptr> errs(nt);
-  auto body = [&](uint32_t t) {
-    try {
-      for (uint32_t i; (i = next.fetch_add(1)) < n;) fn(i);
-    } catch (...) {
-      errs[t] = std::current_exception();
-    }
-  };
-  std::vector<std::thread> th;
-  for (uint32_t t = 1; t < nt; ++t) th.emplace_back(body, t);
-  body(0);
-  for (auto &x : th) x.join();
-  for (auto &e : errs)
-    if (e) std::rethrow_exception(e);
-}
-
 uint32_t host_threads() { return std::max(1u, std::thread::hardware_concurrency()); }
 
 // Grow-only device allocation.
@@ -165,10 +142,29 @@ struct Layout {
 
 }  // namespace
 
+// Allocator whose resize() leaves new elements of trivial types uninitialised
+// (the DEM arrays are written in full right after they are sized).
+template <typename T>
+struct UninitAlloc : std::allocator<T> {
+  template <typename U>
+  struct rebind {
+    using other = UninitAlloc<U>;
+  };
+  UninitAlloc() = default;
+  template <typename U>
+  UninitAlloc(const UninitAlloc<U> &) noexcept {}
+  template <typename U>
+  void construct(U *) noexcept {}
+  template <typename U, typename... A>
+  void construct(U *p, A &&...a) {
+    ::new ((void *)p) U(std::forward<A>(a)...);
+  }
+};
+
 struct gpc_dem {
-  std::vector<double> probs;
-  std::vector<uint32_t> offsets;
-  std::vector<uint32_t> targets;
+  std::vector<double, UninitAlloc<double>> probs;
+  std::vector<uint32_t, UninitAlloc<uint32_t>> offsets;
+  std::vector<uint32_t, UninitAlloc<uint32_t>> targets;
   uint32_t num_detectors = 0, num_observables = 0;
   uint64_t num_raw = 0;
   std::string text;
@@ -183,8 +179,21 @@ struct gpc_driver {
   static constexpr int kAux = 4;
   cudaStream_t aux[kAux] = {};
   cudaEvent_t fork_ev = nullptr, join_ev[kAux] = {};
-  std::vector<gpc::Parsed> parsed;
   std::vector<Tape> tapes;
+  std::vector<gpc::LowerScratch> lower_scratch;  // host memory of parse + lower, one per pool slot
+  std::unique_ptr<gpc::HostPool> pool;            // host threads of this driver (made on first use)
+  gpc::HostPool &host_pool() {
+    if (!pool) pool.reset(new gpc::HostPool(host_threads() - 1));
+    return *pool;
+  }
+  // fn(i, slot) for i < n, on the host pool when `parallel`.
+  void for_each(uint32_t n, bool parallel, const std::function<void(uint32_t, uint32_t)> &fn) {
+    if (!parallel || n < 2) {
+      for (uint32_t i = 0; i < n; ++i) fn(i, 0);
+      return;
+    }
+    host_pool().run(n, fn);
+  }
   bool have_tape = false;
   bool prepared = false;
   bool ran = false;
@@ -443,10 +452,19 @@ struct gpc_driver {
     std::vector<CircuitDev> cd(N);
     std::vector<uint32_t> mb(N + 1), cb(N);
     // circuits fill disjoint regions of the staging buffer: a batch copies in parallel
-    parallel_for(N, N >= 8 ? host_threads() : 1u, [&](uint32_t i) {
+    for_each(N, N >= 8, [&](uint32_t i, uint32_t) {
       const Tape &T = tapes[i];
       const CircLayout &l = L.c[i];
-      put(l.ops, T.ops.data(), T.ops.size() * 8);
+      const size_t ob = T.ops.size() * 8;
+      if (N == 1 && ob >= (1u << 20)) {  // one large tape: its copy in pieces on the host pool
+        const uint32_t np = 8;
+        for_each(np, true, [&](uint32_t q, uint32_t) {
+          const size_t b0 = ob * q / np & ~(size_t)7, b1 = q + 1 == np ? ob : ob * (q + 1) / np & ~(size_t)7;
+          put(l.ops + b0, reinterpret_cast<const char *>(T.ops.data()) + b0, b1 - b0);
+        });
+      } else {
+        put(l.ops, T.ops.data(), ob);
+      }
       put(l.ep_opoff, T.ep_opoff.data(), T.ep_opoff.size() * 4);
       put(l.ep_k, T.ep_k.data(), T.ep_k.size() * 4);
       put(l.ep_ptoff, T.ep_ptoff.data(), T.ep_ptoff.size() * 4);
@@ -524,47 +542,30 @@ struct gpc_driver {
   }
 
   // Parses and lowers circuits (in parallel on host threads for batches).
+  // The tapes and each thread's scratch memory are kept from one compile to
+  // the next, so a repeated compile reuses mapped host memory.
   void lower_all(const char *const *texts, const size_t *lens, uint32_t n) {
-    std::vector<gpc::Parsed> P(n);
-    std::vector<Tape> T(n);
+    have_tape = false;  // the tapes are rewritten in place
     gpc::LowerOptions lo;
     lo.level = level;
     if (n > 1) lo.chunk_min = gpc::kWalkChunkMin;
-    auto one = [&](uint32_t i) {
-      P[i] = gpc::parse_stim(texts[i], lens[i]);
-      T[i] = gpc::lower(P[i], lo);
-    };
-    if (n == 1) {
-      one(0);
-    } else {
-      const uint32_t nt = std::max(1u, std::min<uint32_t>(n, std::thread::hardware_concurrency()));
-      std::vector<std::thread> th;
-      std::vector<std::exception_ptr> errs(nt);
-      std::atomic<uint32_t> next{0};
-      for (uint32_t t = 0; t < nt; ++t)
-        th.emplace_back([&, t] {
-          try {
-            for (uint32_t i; (i = next.fetch_add(1)) < n;) one(i);
-          } catch (...) {
-            errs[t] = std::current_exception();
-          }
-        });
-      for (auto &x : th) x.join();
-      for (auto &e : errs)
-        if (e) std::rethrow_exception(e);
-    }
-    parsed = std::move(P);
-    tapes = std::move(T);
+    gpc::HostPool &hp = host_pool();
+    if (lower_scratch.size() < hp.workers() + 1) lower_scratch.resize(hp.workers() + 1);
+    tapes.resize(n);
+    if (n == 1)  // one circuit: a large text is parsed in pieces on the pool
+      gpc::lower_text(texts[0], lens[0], lo, tapes[0], lower_scratch[0], &hp);
+    else
+      hp.run(n, [&](uint32_t i, uint32_t slot) { gpc::lower_text(texts[i], lens[i], lo, tapes[i], lower_scratch[slot]); });
   }
 
   // Prepares circuits already lowered on the host (serving lowers requests as they arrive).
-  void prepare_tapes(std::vector<Tape> &&T) {
+  // The driver's previous tapes come back in T (their memory can be reused).
+  void prepare_tapes(std::vector<Tape> &T) {
     if (T.empty()) throw gpc::Error(GPC_ERR_INVALID, "empty batch");
     param = false;
     tcap = 32;
     lists_off = false;
-    parsed.clear();
-    tapes = std::move(T);
+    tapes.swap(T);
     have_tape = true;
     prepare(nullptr, nullptr, 0);
   }
@@ -1121,7 +1122,7 @@ struct gpc_driver {
     const uint2 *CO = reinterpret_cast<const uint2 *>(hc);
     outs.assign(N, nullptr);
     try {
-      parallel_for(N, N >= 8 ? host_threads() : 1u, [&](uint32_t i) {
+      for_each(N, N >= 8, [&](uint32_t i, uint32_t) {
         const uint32_t c0 = N > 1 ? CO[i].x : 0, c1 = (N > 1 && i + 1 < N) ? CO[i + 1].x : C;
         const uint32_t t0 = N > 1 ? CO[i].y : 0, t1 = (N > 1 && i + 1 < N) ? CO[i + 1].y : NT;
         if (c1 < c0 || c1 > C || t1 < t0 || t1 > NT) throw gpc::Error(GPC_ERR_CUDA, "inconsistent batch ranges");
@@ -1129,11 +1130,23 @@ struct gpc_driver {
         dem->num_detectors = tapes[i].ndet;
         dem->num_observables = tapes[i].nobs;
         dem->num_raw = tapes[i].M;
-        dem->probs.assign(P + c0, P + c1);
+        dem->probs.resize(c1 - c0);
         dem->offsets.resize((size_t)(c1 - c0) + 1);
-        for (uint32_t k = c0; k < c1; ++k) dem->offsets[k - c0] = O[k] - t0;
-        dem->offsets[c1 - c0] = t1 - t0;
-        dem->targets.assign(TG + t0, TG + t1);
+        dem->targets.resize(t1 - t0);
+        double *dp = dem->probs.data();
+        uint32_t *dof = dem->offsets.data(), *dt = dem->targets.data();
+        // one large result is copied in pieces on the host pool (a single
+        // thread's copy rate would dominate the fetch)
+        const uint32_t ne = c1 - c0, nt = t1 - t0;
+        const uint32_t np = N == 1 && (size_t)ne * 12 + (size_t)nt * 4 >= (1u << 20) ? 8u : 1u;
+        for_each(np, np > 1, [&](uint32_t q, uint32_t) {
+          const uint32_t e0 = (uint32_t)((uint64_t)ne * q / np), e1 = (uint32_t)((uint64_t)ne * (q + 1) / np);
+          const uint32_t g0 = (uint32_t)((uint64_t)nt * q / np), g1 = (uint32_t)((uint64_t)nt * (q + 1) / np);
+          if (e1 > e0) memcpy(dp + e0, P + c0 + e0, (size_t)(e1 - e0) * 8);
+          for (uint32_t k = e0; k < e1; ++k) dof[k] = O[c0 + k] - t0;
+          if (g1 > g0) memcpy(dt + g0, TG + t0 + g0, (size_t)(g1 - g0) * 4);
+        });
+        dof[ne] = nt;
         outs[i] = dem.release();
       });
     } catch (...) {
@@ -1147,13 +1160,11 @@ struct gpc_driver {
   // bucket holds, or a symptom longer than the target lists): compile its
   // circuits one at a time on the single-circuit path.
   void batch_fallback(std::vector<gpc_dem *> &outs) {
-    std::vector<gpc::Parsed> P = std::move(parsed);
     std::vector<Tape> T = std::move(tapes);
     const uint32_t N = (uint32_t)T.size();
     outs.assign(N, nullptr);
     try {
       for (uint32_t i = 0; i < N; ++i) {
-        parsed.assign(1, P[i]);
         tapes.assign(1, std::move(T[i]));
         tcap = 32;
         lists_off = false;
@@ -1224,6 +1235,8 @@ struct gpc_server {
   std::deque<uint64_t> lower_queue;  // submitted, not yet lowered
   std::condition_variable cv_lower;
   std::vector<std::thread> lowerers;
+  std::vector<Tape> spare;  // tapes of compiled batches, lowered into again (their memory kept)
+  static constexpr size_t kSpareTapes = 32;
   int device = 0, level = 2;
   uint32_t max_batch = 16;
   size_t budget = 0, used = 0, peak = 0;
@@ -1287,6 +1300,7 @@ struct gpc_server {
   // Lowering threads: parse and lower each request as it arrives (in
   // parallel across requests), then hand it to the GPU workers.
   void lowerer() {
+    gpc::LowerScratch scratch;
     gpc::LowerOptions lo;
     lo.level = level;
     lo.chunk_min = gpc::kWalkChunkMin;  // requests are compiled in batches
@@ -1304,7 +1318,15 @@ struct gpc_server {
         len = reqs.at(t)->text.size();
       }
       try {
-        auto tape = std::make_unique<Tape>(gpc::lower(gpc::parse_stim(text, len), lo));
+        auto tape = std::make_unique<Tape>();
+        {
+          std::lock_guard<std::mutex> lk(mu);
+          if (!spare.empty()) {
+            *tape = std::move(spare.back());
+            spare.pop_back();
+          }
+        }
+        gpc::lower_text(text, len, lo, *tape, scratch);
         {
           std::lock_guard<std::mutex> lk(mu);
           reqs.at(t)->tape = std::move(tape);
@@ -1348,7 +1370,12 @@ struct gpc_server {
           reqs.at(t)->tape.reset();
         }
       }
-      d.prepare_tapes(std::move(tapes));
+      d.prepare_tapes(tapes);
+      {
+        std::lock_guard<std::mutex> lk(mu);
+        for (auto &x : tapes)
+          if (spare.size() < kSpareTapes) spare.push_back(std::move(x));
+      }
     }
     d.run();
     std::vector<gpc_dem *> outs;

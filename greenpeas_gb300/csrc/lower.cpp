@@ -1,6 +1,8 @@
 // lower.cpp -- stim text parser and the tick-tape lowering (see lower.hpp).
 #include "lower.hpp"
 
+#include "host_pool.hpp"
+
 #include <algorithm>
 #include <cctype>
 #include <cmath>
@@ -293,8 +295,11 @@ uint64_t c2_op(uint32_t sub, uint32_t partner) {
 
 // One tape entry placed by the backward scheduler: qubit, epoch, slot, op.
 struct Entry {
-  uint32_t q, e, k;
+  uint32_t qk;  // qubit | slot << 24
+  uint32_t e;
   uint64_t op;
+  uint32_t q() const { return qk & 0xFFFFFFu; }
+  uint32_t k() const { return qk >> 24; }
 };
 
 struct QState {
@@ -327,25 +332,121 @@ struct SplitCache {
 double split_dep1(double p) { return 0.5 - 0.5 * std::sqrt(1.0 - (4.0 * p) / 3.0); }
 double split_dep2(double p) { return 0.5 - 0.5 * std::pow(1.0 - (16.0 * p) / 15.0, 0.125); }
 
-Parsed parse_stim(const char *text, size_t len) {
-  Parsed p;
+void parse_stim_into(const char *text, size_t len, Parsed &p) {
+  p.ins.clear();
+  p.pool.clear();
   if (!text && len) throw Error(GPC_ERR_INVALID, "null circuit text");
   p.pool.reserve(len / 3 + 16);
   p.ins.reserve(len / 64 + 16);
   TextParser tp{text, text + len, 1, &p};
   tp.block(p.ins, false, 0);
+}
+
+Parsed parse_stim(const char *text, size_t len) {
+  Parsed p;
+  parse_stim_into(text, len, p);
   return p;
 }
 
+void Tape::reset() {
+  nq = qpad = nmeas = ndet = nobs = nbits = w = 0;
+  n_epochs = kmax = 0;
+  for (auto *v : {&ep_opoff, &ep_k, &ep_ptoff, &ep_chunk, &ch_off, &ch_bytes, &inj_lo, &inj_hi, &rec_moff, &rec_src})
+    v->clear();
+  ops.clear();
+  rec.clear();
+  rec_p.clear();
+  chunk_cap = 0;
+  npoints = 0;
+  M = 0;
+  n_ticks = 1;
+}
+
+struct LowerScratch::Buffers {
+  std::vector<uint32_t> measBase, tsrc, moff, mbits, measLo, measHi, slotOf, order, remap;
+  std::vector<std::pair<uint32_t, uint32_t>> detPairs, obsPairs, mb, kept, groups;
+  std::vector<uint8_t> lastReset;
+  std::vector<Entry> ent;
+  std::vector<QState> st;
+  std::vector<uint64_t> fine, coarse;
+};
+
+LowerScratch::LowerScratch() : b(new Buffers) {}
+LowerScratch::~LowerScratch() = default;
+LowerScratch::LowerScratch(LowerScratch &&) noexcept = default;
+LowerScratch &LowerScratch::operator=(LowerScratch &&) noexcept = default;
+
+void parse_stim_pieces(const char *text, size_t len, Parsed &out, std::vector<Parsed> &pieces, HostPool &pool) {
+  constexpr size_t kPieceMin = 32 * 1024;
+  const size_t want = std::min<size_t>({(size_t)pool.workers() + 1, 8, len / kPieceMin});
+  // a REPEAT block may not be cut: such texts (short ones, usually) parse whole
+  if (want < 2 || !text || memchr(text, '{', len)) {
+    parse_stim_into(text, len, out);
+    return;
+  }
+  std::vector<size_t> cut{0};
+  for (size_t i = 1; i < want; ++i) {
+    size_t c = std::max(cut.back(), len * i / want);
+    const void *nl = memchr(text + c, '\n', len - c);
+    c = nl ? (size_t)(static_cast<const char *>(nl) - text) + 1 : len;
+    if (c > cut.back() && c < len) cut.push_back(c);
+  }
+  cut.push_back(len);
+  const uint32_t np = (uint32_t)cut.size() - 1;
+  if (pieces.size() < np) pieces.resize(np);
+  try {
+    pool.run(np, [&](uint32_t i, uint32_t) { parse_stim_into(text + cut[i], cut[i + 1] - cut[i], pieces[i]); });
+  } catch (const Error &) {
+    parse_stim_into(text, len, out);  // the error again, with its line number in the whole text
+    return;
+  }
+  size_t ni = 0, nt = 0;
+  for (uint32_t i = 0; i < np; ++i) {
+    ni += pieces[i].ins.size();
+    nt += pieces[i].pool.size();
+  }
+  out.ins.clear();
+  out.pool.clear();
+  out.ins.reserve(ni);
+  out.pool.reserve(nt);
+  for (uint32_t i = 0; i < np; ++i) {
+    const uint32_t off = (uint32_t)out.pool.size();
+    out.pool.insert(out.pool.end(), pieces[i].pool.begin(), pieces[i].pool.end());
+    for (Instr in : pieces[i].ins) {
+      in.t0 += off;
+      out.ins.push_back(in);
+    }
+  }
+}
+
+void lower_text(const char *text, size_t len, const LowerOptions &opt, Tape &T, LowerScratch &S, HostPool *pool) {
+  if (pool)
+    parse_stim_pieces(text, len, S.parsed, S.pieces, *pool);
+  else
+    parse_stim_into(text, len, S.parsed);
+  lower_into(S.parsed, opt, T, S);
+}
+
 Tape lower(const Parsed &P, const LowerOptions &opt) {
-  if (opt.level < 0 || opt.level > 2) throw Error(GPC_ERR_INVALID, "correlation level must be 0, 1 or 2");
   Tape T;
+  LowerScratch S;
+  lower_into(P, opt, T, S);
+  return T;
+}
+
+void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch &S) {
+  if (opt.level < 0 || opt.level > 2) throw Error(GPC_ERR_INVALID, "correlation level must be 0, 1 or 2");
+  T.reset();
+  LowerScratch::Buffers &B = *S.b;
   uint32_t kcap = std::max<uint32_t>(1, opt.kcap);
 
   // ---- forward pass: qubits, measurements, detectors, observables --------
-  std::vector<uint32_t> measBase(P.ins.size());
-  std::vector<std::pair<uint32_t, uint32_t>> detPairs;  // (measurement, detector)
-  std::vector<std::pair<uint32_t, uint32_t>> obsPairs;  // (measurement, observable)
+  std::vector<uint32_t> &measBase = B.measBase;
+  measBase.resize(P.ins.size());
+  std::vector<std::pair<uint32_t, uint32_t>> &detPairs = B.detPairs;  // (measurement, detector)
+  std::vector<std::pair<uint32_t, uint32_t>> &obsPairs = B.obsPairs;  // (measurement, observable)
+  detPairs.clear();
+  obsPairs.clear();
   uint32_t m = 0, ndet = 0, nobs = 0;
   uint32_t nq = 0;
   for (size_t i = 0; i < P.ins.size(); ++i) {
@@ -353,23 +454,29 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
     const Gate &g = kGates[in.gate];
     const uint32_t *t = P.pool.data() + in.t0;
     measBase[i] = m;
+    // target kinds, checked on the OR / AND of the instruction's targets
+    uint32_t orv = 0, andv = 0xFFFFFFFFu, maxq = 0;
     for (uint32_t k = 0; k < in.tn; ++k) {
-      uint32_t v = t[k];
-      if (v & kRec) {
-        if (g.kind != G_DET && g.kind != G_OBS)
-          throw Error(GPC_ERR_UNSUPPORTED, std::string("record targets are not supported on ") + g.name);
-        continue;
+      const uint32_t v = t[k];
+      orv |= v;
+      andv &= v;
+      maxq = std::max(maxq, v & 0xFFFFFFu);
+    }
+    if (in.tn) {
+      if (g.kind == G_DET || g.kind == G_OBS) {
+        if (!(andv & kRec)) throw Error(GPC_ERR_PARSE, std::string(g.name) + " takes record targets only");
+      } else if (orv & kRec) {
+        throw Error(GPC_ERR_UNSUPPORTED, std::string("record targets are not supported on ") + g.name);
+      } else if (g.kind == G_MPAD) {
+        if (maxq > 1 || (orv & kPau)) throw Error(GPC_ERR_PARSE, "MPAD targets must be 0 or 1");
+      } else {
+        if (g.kind == G_CORR) {
+          if (!(andv & kPau)) throw Error(GPC_ERR_PARSE, "E takes Pauli targets");
+        } else if (orv & kPau) {
+          throw Error(GPC_ERR_PARSE, std::string("Pauli targets are not allowed on ") + g.name);
+        }
+        nq = std::max(nq, maxq + 1);
       }
-      if (g.kind == G_DET || g.kind == G_OBS)
-        throw Error(GPC_ERR_PARSE, std::string(g.name) + " takes record targets only");
-      if (g.kind == G_MPAD) {
-        if (v > 1) throw Error(GPC_ERR_PARSE, "MPAD targets must be 0 or 1");
-        continue;
-      }
-      if ((v & kPau) && g.kind != G_CORR)
-        throw Error(GPC_ERR_PARSE, std::string("Pauli targets are not allowed on ") + g.name);
-      if (!(v & kPau) && g.kind == G_CORR) throw Error(GPC_ERR_PARSE, "E takes Pauli targets");
-      nq = std::max(nq, (v & 0xFFFFFFu) + 1);
     }
     switch (g.kind) {
       case G_M:
@@ -423,10 +530,12 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
       throw Error(GPC_ERR_UNSUPPORTED, "noisy MPAD is not supported");
   }
   // sources of the noise targets: tick and class (see Tape::rec_src)
-  std::vector<uint32_t> tsrc(P.pool.size(), kNone);
+  std::vector<uint32_t> &tsrc = B.tsrc;
+  tsrc.assign(P.pool.size(), kNone);
   {
     uint32_t tick = 0;
-    std::vector<uint8_t> lastReset(nq, 0);  // the qubit's last operation was a reset
+    std::vector<uint8_t> &lastReset = B.lastReset;  // the qubit's last operation was a reset
+    lastReset.assign(nq, 0);
     for (size_t i = 0; i < P.ins.size(); ++i) {
       const Instr &in = P.ins[i];
       const Gate &g = kGates[in.gate];
@@ -487,14 +596,17 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
   }
 
   // measurement -> bits (XOR: a measurement listed twice in one detector cancels)
-  std::vector<uint32_t> moff(m + 1, 0), mbits;
+  std::vector<uint32_t> &moff = B.moff, &mbits = B.mbits;
+  moff.assign(m + 1, 0);
   {
-    std::vector<std::pair<uint32_t, uint32_t>> mb;
+    std::vector<std::pair<uint32_t, uint32_t>> &mb = B.mb;
+    mb.clear();
     mb.reserve(detPairs.size() + obsPairs.size());
     for (auto &d : detPairs) mb.push_back(d);
     for (auto &o : obsPairs) mb.push_back({o.first, ndet + o.second});
     std::sort(mb.begin(), mb.end());
-    std::vector<std::pair<uint32_t, uint32_t>> kept;
+    std::vector<std::pair<uint32_t, uint32_t>> &kept = B.kept;
+    kept.clear();
     kept.reserve(mb.size());
     for (size_t i = 0; i < mb.size();) {
       size_t j = i;
@@ -509,15 +621,19 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
   }
 
   // ---- backward pass: epoch scheduling and noise records -----------------
-  std::vector<Entry> ent;
+  std::vector<Entry> &ent = B.ent;
+  ent.clear();
   ent.reserve(P.pool.size() * 2 + 16);
-  std::vector<QState> st(nq);
-  std::vector<uint32_t> measLo(m, kNone), measHi(m, kNone);
+  std::vector<QState> &st = B.st;
+  st.assign(nq, QState{});
+  std::vector<uint32_t> &measLo = B.measLo, &measHi = B.measHi;
+  measLo.assign(m, kNone);
+  measHi.assign(m, kNone);
   uint32_t nprov = 0;  // provisional point ids (creation order)
   T.rec.reserve(P.pool.size());
   T.rec_p.reserve(P.pool.size());
   T.rec_src.reserve(P.pool.size());
-  std::vector<uint32_t> ep_k;  // slots per epoch, grown on demand
+  std::vector<uint32_t> &ep_k = T.ep_k;  // slots per epoch, grown on demand
   SplitCache split;
 
   auto place1 = [&](uint32_t q, uint64_t op) -> uint32_t {
@@ -532,7 +648,7 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
     } else {
       e = (uint32_t)s.last;
     }
-    ent.push_back({q, e, s.cnt, op});
+    ent.push_back({q | (s.cnt << 24), e, op});
     if (e >= ep_k.size()) ep_k.resize((size_t)e + 1, 0);
     ep_k[e] = std::max(ep_k[e], s.cnt + 1);
     s.last = e;
@@ -573,8 +689,8 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
           uint32_t E = (uint32_t)(std::max(st[a].last, st[b].last) + 1);
           uint32_t subA = (uint32_t)g.img[0] | ((uint32_t)g.img[1] << 4);
           uint32_t subB = swap_halves(g.img[2]) | (swap_halves(g.img[3]) << 4);
-          ent.push_back({a, E, 0, c2_op(subA, b)});  // partner operands become slots below
-          ent.push_back({b, E, 0, c2_op(subB, a)});
+          ent.push_back({a, E, c2_op(subA, b)});  // partner operands become slots below
+          ent.push_back({b, E, c2_op(subB, a)});
           if (E >= ep_k.size()) ep_k.resize((size_t)E + 1, 0);
           ep_k[E] = std::max<uint32_t>(ep_k[E], 1);
           st[a].last = st[b].last = E;
@@ -687,15 +803,18 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
   // of a code) take the same branches in the walk.  Group them, and start
   // each group on a warp boundary when that costs at most half again as many
   // slots, so a warp does not mix roles.
-  std::vector<uint32_t> slotOf(nq);
+  std::vector<uint32_t> &slotOf = B.slotOf;
+  slotOf.assign(nq, 0);
   {
     // fine signature: op kinds with their epochs; coarse: op kinds only
-    std::vector<uint64_t> fine(nq, 0xcbf29ce484222325ull), coarse(nq, 0xcbf29ce484222325ull);
+    std::vector<uint64_t> &fine = B.fine, &coarse = B.coarse;
+    fine.assign(nq, 0xcbf29ce484222325ull);
+    coarse.assign(nq, 0xcbf29ce484222325ull);
     for (const Entry &x : ent) {
       const uint32_t opc = (uint32_t)(x.op & 0xFF);
       if (opc == OP_INJ || opc == OP_SNAPD) continue;  // vary with detector membership only
-      coarse[x.q] = (coarse[x.q] ^ opc) * 0x100000001b3ull;
-      fine[x.q] = (fine[x.q] ^ (opc | ((uint64_t)x.e << 8))) * 0x100000001b3ull;
+      coarse[x.q()] = (coarse[x.q()] ^ opc) * 0x100000001b3ull;
+      fine[x.q()] = (fine[x.q()] ^ (opc | ((uint64_t)x.e << 8))) * 0x100000001b3ull;
     }
     const uint32_t qptBase = T.qpad <= 1024 ? 1u : T.qpad <= 2048 ? 2u : 4u;
     // Orders qubits by group (groups in order of their first qubit); returns the
@@ -726,8 +845,8 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
                       (uint64_t)kcap * qpadP * 8 <= walk_chunk_cap(qpadP);
       return ok ? qpadP : 0u;
     };
-    std::vector<uint32_t> order;
-    std::vector<std::pair<uint32_t, uint32_t>> groups;
+    std::vector<uint32_t> &order = B.order;
+    std::vector<std::pair<uint32_t, uint32_t>> &groups = B.groups;
     uint32_t qpadP = plan(fine, order, groups);
     if (!qpadP) qpadP = plan(coarse, order, groups);
     uint32_t next = 0;
@@ -745,7 +864,6 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
   const uint32_t nE = (uint32_t)ep_k.size();
   T.n_epochs = nE;
   for (auto &k : ep_k) k = std::max<uint32_t>(k, 1);  // every epoch copies at least one slot
-  T.ep_k = std::move(ep_k);
   T.ep_opoff.assign(nE, 0);
   uint64_t total = 0;
   for (uint32_t e = 0; e < nE; ++e) {
@@ -760,10 +878,11 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
     const uint32_t opc = (uint32_t)(op & 0xFF);
     if (opc == OP_C2 || opc >= OP_XPX)  // partner qubit -> partner slot
       op = (op & 0xFFFFFFFFull) | ((uint64_t)slotOf[(uint32_t)(op >> 32)] << 32);
-    T.ops[(size_t)T.ep_opoff[x.e] + (size_t)x.k * T.qpad + slotOf[x.q]] = op;
+    T.ops[(size_t)T.ep_opoff[x.e] + (size_t)x.k() * T.qpad + slotOf[x.q()]] = op;
   }
   // points: renumber in walk order (epoch, slot, qubit) so each epoch owns a contiguous range
-  std::vector<uint32_t> remap(nprov, kNone);
+  std::vector<uint32_t> &remap = B.remap;
+  remap.assign(nprov, kNone);
   T.ep_ptoff.assign(nE + 1, 0);
   uint32_t next = 0;
   for (uint32_t e = 0; e < nE; ++e) {
@@ -832,7 +951,6 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
       if (T.inj_hi[j] == kNone || measHi[k] > T.inj_hi[j]) T.inj_hi[j] = measHi[k];
     }
   }
-  return T;
 }
 
 }  // namespace gpc

@@ -19,11 +19,14 @@
 #pragma once
 
 #include <cstdint>
+#include <memory>
 #include <stdexcept>
 #include <string>
 #include <vector>
 
 namespace gpc {
+
+class HostPool;
 
 // Errors thrown by the lowering carry a gpc_status code.
 struct Error : std::runtime_error {
@@ -99,6 +102,8 @@ struct Parsed {
 
 // Parses stim circuit text, flattening REPEAT blocks.  Throws gpc::Error.
 Parsed parse_stim(const char *text, size_t len);
+// The same into `out`, whose buffers are reused.
+void parse_stim_into(const char *text, size_t len, Parsed &out);
 
 // A lowered circuit: everything the device pipeline needs.
 struct Tape {
@@ -127,6 +132,9 @@ struct Tape {
   // a reset).  PAULI_CHANNEL_1 and E have no source.
   std::vector<uint32_t> rec_src;    // [R]
   uint32_t n_ticks = 1;             // TICK instructions + 1
+
+  // Empties the tape, keeping the capacity of its arrays.
+  void reset();
 };
 
 enum : uint32_t { SRC_DEP2 = 0, SRC_DEP1 = 1, SRC_MEAS_FLIP = 2, SRC_RESET_FLIP = 3, SRC_CLASSES = 4 };
@@ -157,6 +165,29 @@ inline uint32_t walk_chunk_cap(uint32_t qpad) {
 }
 
 Tape lower(const Parsed &p, const LowerOptions &opt);
+
+// Reusable host memory of parse + lower.  A caller that lowers circuit after
+// circuit keeps one (per thread) and lowers into a kept Tape, so later
+// circuits write memory that is already mapped instead of fresh pages.
+struct LowerScratch {
+  LowerScratch();
+  ~LowerScratch();
+  LowerScratch(LowerScratch &&) noexcept;
+  LowerScratch &operator=(LowerScratch &&) noexcept;
+  Parsed parsed;
+  std::vector<Parsed> pieces;  // a text parsed in pieces on several threads
+  struct Buffers;
+  std::unique_ptr<Buffers> b;
+};
+// lower() into T (reset first), with S's buffers.
+void lower_into(const Parsed &p, const LowerOptions &opt, Tape &T, LowerScratch &S);
+// parse_stim + lower_into, parsing into S.parsed (a large text in pieces on
+// `pool`'s threads when a pool is given).
+void lower_text(const char *text, size_t len, const LowerOptions &opt, Tape &T, LowerScratch &S,
+                HostPool *pool = nullptr);
+// parse_stim_into, cutting a large text without REPEAT blocks at line ends
+// into pieces parsed on `pool`'s threads; the same result as one parse.
+void parse_stim_pieces(const char *text, size_t len, Parsed &out, std::vector<Parsed> &pieces, HostPool &pool);
 
 // Independent-component probability of DEPOLARIZE1(p) and DEPOLARIZE2(p)
 // (Mixer.hpp:164,184): 0.5 - 0.5 sqrt(1 - 4p/3), 0.5 - 0.5 (1 - 16p/15)^(1/8).

@@ -4,6 +4,7 @@
 #include <string>
 
 #include "../../include/gpc.h"
+#include "host_pool.hpp"
 #include "lower.hpp"
 
 struct gpc_tape {
@@ -20,10 +21,16 @@ gpc_status gpc_tape_lower(const char *stim_text, size_t len, int32_t correlation
   if (!out || !stim_text) return GPC_ERR_INVALID;
   *out = nullptr;
   try {
-    gpc::Parsed p = gpc::parse_stim(stim_text, len);
     gpc::LowerOptions lo;
     lo.level = correlation_level;
-    std::unique_ptr<gpc_tape> t(new gpc_tape{gpc::lower(p, lo)});
+    std::unique_ptr<gpc_tape> t(new gpc_tape{});
+    gpc::LowerScratch scratch;
+    if (len >= 64 * 1024) {  // a large text is parsed in pieces, as the compile path does
+      gpc::HostPool pool(3);
+      gpc::lower_text(stim_text, len, lo, t->t, scratch, &pool);
+    } else {
+      gpc::lower_text(stim_text, len, lo, t->t, scratch);
+    }
     *out = t.release();
     return GPC_OK;
   } catch (const gpc::Error &e) {

@@ -47,6 +47,29 @@ def test_bb6_uniform_matches_oracle():
     compare_errors(compile_tape(Tape(text)), _oracle(text))
 
 
+def _tape_arrays(t):
+    return {k: v for k, v in vars(t).items()}
+
+
+def test_large_text_parsed_in_pieces_gives_the_same_tape():
+    """Texts of 64 KiB and more are cut at line ends and parsed on several threads; a '{'
+    anywhere (here in a comment) makes the parse take the text whole.  Same tape either way."""
+    text = BBCode(12).get_memory(12, 1e-3, noise="uniform")
+    assert len(text) > 200_000 and "{" not in text
+    a, b = _tape_arrays(Tape(text)), _tape_arrays(Tape("# {\n" + text))
+    assert a.keys() == b.keys()
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
+
+
+@pytest.mark.parametrize("bad,code", [("FOO 1\n", -3), ("CX 5\n", -2), ("CX rec[-1] 0\n", -3)])
+def test_large_text_error_in_a_late_piece(bad, code):
+    text = BBCode(12).get_memory(12, 1e-3, noise="uniform")
+    with pytest.raises(GpcError) as ei:
+        Tape(text + bad)
+    assert ei.value.status == code
+
+
 def test_tape_shapes():
     t = Tape(SurfaceCode(3).get_memory(3, 1e-3, noise="uniform"))
     assert t.num_mechanisms == 1227  # raw mechanisms of the surface d=3 r=3 config
