@@ -4,6 +4,7 @@
 #include "host_pool.hpp"
 
 #include <algorithm>
+#include <atomic>
 #include <cctype>
 #include <cmath>
 #include <cstdlib>
@@ -362,11 +363,25 @@ void Tape::reset() {
   n_ticks = 1;
 }
 
+// A grow-only array whose elements are left uninitialised (filled before use).
+template <typename T>
+struct RawArray {
+  std::unique_ptr<T[]> p;
+  size_t cap = 0;
+  T *get(size_t n) {
+    if (n > cap) {
+      p.reset(new T[n]);
+      cap = n;
+    }
+    return p.get();
+  }
+};
+
 struct LowerScratch::Buffers {
-  std::vector<uint32_t> measBase, tsrc, moff, mbits, measLo, measHi, slotOf, order, remap;
-  std::vector<std::pair<uint32_t, uint32_t>> detPairs, obsPairs, mb, kept, groups;
+  std::vector<uint32_t> measBase, occBase, tsrc, moff, mbits, measLo, measHi, slotOf, order, remap, ep_np;
+  std::vector<std::pair<uint32_t, uint32_t>> detPairs, obsPairs, groups;
   std::vector<uint8_t> lastReset;
-  std::vector<Entry> ent;
+  RawArray<Entry> ent;
   std::vector<QState> st;
   std::vector<uint64_t> fine, coarse;
 };
@@ -424,7 +439,7 @@ void lower_text(const char *text, size_t len, const LowerOptions &opt, Tape &T, 
     parse_stim_pieces(text, len, S.parsed, S.pieces, *pool);
   else
     parse_stim_into(text, len, S.parsed);
-  lower_into(S.parsed, opt, T, S);
+  lower_into(S.parsed, opt, T, S, pool);
 }
 
 Tape lower(const Parsed &P, const LowerOptions &opt) {
@@ -434,7 +449,7 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
   return T;
 }
 
-void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch &S) {
+void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch &S, HostPool *pool) {
   if (opt.level < 0 || opt.level > 2) throw Error(GPC_ERR_INVALID, "correlation level must be 0, 1 or 2");
   T.reset();
   LowerScratch::Buffers &B = *S.b;
@@ -443,6 +458,10 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
   // ---- forward pass: qubits, measurements, detectors, observables --------
   std::vector<uint32_t> &measBase = B.measBase;
   measBase.resize(P.ins.size());
+  // target occurrences: a REPEAT body's targets are stored once and occur once per repetition
+  std::vector<uint32_t> &occBase = B.occBase;
+  occBase.resize(P.ins.size());
+  size_t occ = 0;
   std::vector<std::pair<uint32_t, uint32_t>> &detPairs = B.detPairs;  // (measurement, detector)
   std::vector<std::pair<uint32_t, uint32_t>> &obsPairs = B.obsPairs;  // (measurement, observable)
   detPairs.clear();
@@ -454,6 +473,9 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
     const Gate &g = kGates[in.gate];
     const uint32_t *t = P.pool.data() + in.t0;
     measBase[i] = m;
+    occBase[i] = (uint32_t)occ;
+    occ += in.tn;
+    if (occ > 0xFFFFFFFFull / 4) throw Error(GPC_ERR_CAPACITY, "circuit too long");
     // target kinds, checked on the OR / AND of the instruction's targets
     uint32_t orv = 0, andv = 0xFFFFFFFFu, maxq = 0;
     for (uint32_t k = 0; k < in.tn; ++k) {
@@ -531,7 +553,7 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
   }
   // sources of the noise targets: tick and class (see Tape::rec_src)
   std::vector<uint32_t> &tsrc = B.tsrc;
-  tsrc.assign(P.pool.size(), kNone);
+  tsrc.assign(occ, kNone);  // by target occurrence
   {
     uint32_t tick = 0;
     std::vector<uint8_t> &lastReset = B.lastReset;  // the qubit's last operation was a reset
@@ -545,20 +567,20 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
           ++tick;
           break;
         case G_N2:
-          for (uint32_t k = 0; k < in.tn; ++k) tsrc[in.t0 + k] = tick * SRC_CLASSES + SRC_DEP2;
+          for (uint32_t k = 0; k < in.tn; ++k) tsrc[occBase[i] + k] = tick * SRC_CLASSES + SRC_DEP2;
           break;
         case G_N1:
           for (uint32_t k = 0; k < in.tn; ++k) {
             if (g.a == N1_DEP1)
-              tsrc[in.t0 + k] = tick * SRC_CLASSES + SRC_DEP1;
+              tsrc[occBase[i] + k] = tick * SRC_CLASSES + SRC_DEP1;
             else if (g.a != N1_PC1)
-              tsrc[in.t0 + k] = tick * SRC_CLASSES + (lastReset[t[k]] ? SRC_RESET_FLIP : SRC_MEAS_FLIP);
+              tsrc[occBase[i] + k] = tick * SRC_CLASSES + (lastReset[t[k]] ? SRC_RESET_FLIP : SRC_MEAS_FLIP);
           }
           break;
         case G_M:
         case G_MR:
           for (uint32_t k = 0; k < in.tn; ++k) {
-            tsrc[in.t0 + k] = tick * SRC_CLASSES + SRC_MEAS_FLIP;
+            tsrc[occBase[i] + k] = tick * SRC_CLASSES + SRC_MEAS_FLIP;
             lastReset[t[k]] = g.kind == G_MR;
           }
           break;
@@ -595,35 +617,42 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
     kcap = std::min<uint32_t>(kcap, T.chunk_cap / (T.qpad * 8u));
   }
 
-  // measurement -> bits (XOR: a measurement listed twice in one detector cancels)
+  // measurement -> bits (XOR: a measurement listed twice in one detector cancels),
+  // bits ascending per measurement: a counting sort by measurement, then a
+  // small sort of each measurement's bits
   std::vector<uint32_t> &moff = B.moff, &mbits = B.mbits;
   moff.assign(m + 1, 0);
   {
-    std::vector<std::pair<uint32_t, uint32_t>> &mb = B.mb;
-    mb.clear();
-    mb.reserve(detPairs.size() + obsPairs.size());
-    for (auto &d : detPairs) mb.push_back(d);
-    for (auto &o : obsPairs) mb.push_back({o.first, ndet + o.second});
-    std::sort(mb.begin(), mb.end());
-    std::vector<std::pair<uint32_t, uint32_t>> &kept = B.kept;
-    kept.clear();
-    kept.reserve(mb.size());
-    for (size_t i = 0; i < mb.size();) {
-      size_t j = i;
-      while (j < mb.size() && mb[j] == mb[i]) ++j;
-      if ((j - i) & 1) kept.push_back(mb[i]);
-      i = j;
-    }
-    for (auto &k : kept) moff[k.first + 1]++;
+    for (auto &d : detPairs) moff[d.first + 1]++;
+    for (auto &o : obsPairs) moff[o.first + 1]++;
     for (uint32_t i = 0; i < m; ++i) moff[i + 1] += moff[i];
-    mbits.resize(kept.size());
-    for (size_t i = 0; i < kept.size(); ++i) mbits[i] = kept[i].second;
+    std::vector<uint32_t> &cur = B.order;
+    cur.assign(moff.begin(), moff.end() - 1);
+    mbits.resize(moff[m]);
+    for (auto &d : detPairs) mbits[cur[d.first]++] = d.second;
+    for (auto &o : obsPairs) mbits[cur[o.first]++] = ndet + o.second;
+    uint32_t w = 0, lo = 0;
+    for (uint32_t i = 0; i < m; ++i) {
+      const uint32_t hi = moff[i + 1];
+      std::sort(mbits.begin() + lo, mbits.begin() + hi);
+      moff[i] = w;
+      for (uint32_t a = lo; a < hi;) {
+        uint32_t b = a;
+        while (b < hi && mbits[b] == mbits[a]) ++b;
+        if ((b - a) & 1) mbits[w++] = mbits[a];
+        a = b;
+      }
+      lo = hi;
+    }
+    moff[m] = w;
+    mbits.resize(w);
   }
 
   // ---- backward pass: epoch scheduling and noise records -----------------
-  std::vector<Entry> &ent = B.ent;
-  ent.clear();
-  ent.reserve(P.pool.size() * 2 + 16);
+  // tape entries: at most one per target occurrence, plus two per measurement
+  // and one per further bit of a measurement (its OP_M, OP_SNAPD, OP_INJ slots)
+  Entry *const ent0 = B.ent.get(occ * 3 + mbits.size() + 16);
+  Entry *ent1 = ent0;
   std::vector<QState> &st = B.st;
   st.assign(nq, QState{});
   std::vector<uint32_t> &measLo = B.measLo, &measHi = B.measHi;
@@ -634,6 +663,8 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
   T.rec_p.reserve(P.pool.size());
   T.rec_src.reserve(P.pool.size());
   std::vector<uint32_t> &ep_k = T.ep_k;  // slots per epoch, grown on demand
+  std::vector<uint32_t> &ep_np = B.ep_np;  // points per epoch
+  ep_np.clear();
   SplitCache split;
 
   auto place1 = [&](uint32_t q, uint64_t op) -> uint32_t {
@@ -648,8 +679,11 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
     } else {
       e = (uint32_t)s.last;
     }
-    ent.push_back({q | (s.cnt << 24), e, op});
-    if (e >= ep_k.size()) ep_k.resize((size_t)e + 1, 0);
+    *ent1++ = {q | (s.cnt << 24), e, op};
+    if (e >= ep_k.size()) {
+      ep_k.resize((size_t)e + 1, 0);
+      ep_np.resize((size_t)e + 1, 0);
+    }
     ep_k[e] = std::max(ep_k[e], s.cnt + 1);
     s.last = e;
     s.cnt++;
@@ -659,7 +693,7 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
     QState &s = st[q];
     if (s.open != kNone) return s.open;
     uint32_t id = nprov++;
-    place1(q, make_op(OP_SNAP, 0, id));
+    ++ep_np[place1(q, make_op(OP_SNAP, 0, id))];
     s.open = id;
     return id;
   };
@@ -689,9 +723,12 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
           uint32_t E = (uint32_t)(std::max(st[a].last, st[b].last) + 1);
           uint32_t subA = (uint32_t)g.img[0] | ((uint32_t)g.img[1] << 4);
           uint32_t subB = swap_halves(g.img[2]) | (swap_halves(g.img[3]) << 4);
-          ent.push_back({a, E, c2_op(subA, b)});  // partner operands become slots below
-          ent.push_back({b, E, c2_op(subB, a)});
-          if (E >= ep_k.size()) ep_k.resize((size_t)E + 1, 0);
+          *ent1++ = {a, E, c2_op(subA, b)};  // partner operands become slots below
+          *ent1++ = {b, E, c2_op(subB, a)};
+          if (E >= ep_k.size()) {
+            ep_k.resize((size_t)E + 1, 0);
+            ep_np.resize((size_t)E + 1, 0);
+          }
           ep_k[E] = std::max<uint32_t>(ep_k[E], 1);
           st[a].last = st[b].last = E;
           st[a].cnt = st[b].cnt = 1;
@@ -725,8 +762,8 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
           st[q].open = kNone;
           if (p > 0 && b1 > b0) {
             uint32_t id = nprov++;
-            place1(q, make_op(OP_SNAPD, 0, id));
-            record(id, 0, REC_PAULI, 1, 0, p, tsrc[in.t0 + k]);
+            ++ep_np[place1(q, make_op(OP_SNAPD, 0, id))];
+            record(id, 0, REC_PAULI, 1, 0, p, tsrc[occBase[ii] + k]);
           }
         }
         break;
@@ -739,10 +776,10 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
             case N1_Y:
             case N1_Z:
               if (in.args[0] > 0)
-                record(point(q), 0, REC_PAULI, g.a == N1_X ? 1 : g.a == N1_Z ? 2 : 3, 0, in.args[0], tsrc[in.t0 + k]);
+                record(point(q), 0, REC_PAULI, g.a == N1_X ? 1 : g.a == N1_Z ? 2 : 3, 0, in.args[0], tsrc[occBase[ii] + k]);
               break;
             case N1_DEP1:
-              if (in.args[0] > 0) record(point(q), 0, dep1Type, 0, 0, split.dep1(in.args[0]), tsrc[in.t0 + k]);
+              if (in.args[0] > 0) record(point(q), 0, dep1Type, 0, 0, split.dep1(in.args[0]), tsrc[occBase[ii] + k]);
               break;
             case N1_PC1: {
               double qq[3];
@@ -765,7 +802,7 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
         for (uint32_t k = in.tn; k >= 2; k -= 2) {
           uint32_t a = t[k - 2], b = t[k - 1];
           uint32_t pa = point(a), pb = point(b);
-          record(pa, pb, dep2Type, 0, 0, sp, tsrc[in.t0 + k - 2]);
+          record(pa, pb, dep2Type, 0, 0, sp, tsrc[occBase[ii] + k - 2]);
         }
         break;
       }
@@ -810,7 +847,8 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
     std::vector<uint64_t> &fine = B.fine, &coarse = B.coarse;
     fine.assign(nq, 0xcbf29ce484222325ull);
     coarse.assign(nq, 0xcbf29ce484222325ull);
-    for (const Entry &x : ent) {
+    for (const Entry *xp = ent0; xp != ent1; ++xp) {
+      const Entry &x = *xp;
       const uint32_t opc = (uint32_t)(x.op & 0xFF);
       if (opc == OP_INJ || opc == OP_SNAPD) continue;  // vary with detector membership only
       coarse[x.q()] = (coarse[x.q()] ^ opc) * 0x100000001b3ull;
@@ -873,33 +911,53 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
     if (total > 0xFFFFFFFFull) throw Error(GPC_ERR_CAPACITY, "tape too long");
   }
   T.ops.assign(total, 0);
-  for (const Entry &x : ent) {
-    uint64_t op = x.op;
-    const uint32_t opc = (uint32_t)(op & 0xFF);
-    if (opc == OP_C2 || opc >= OP_XPX)  // partner qubit -> partner slot
-      op = (op & 0xFFFFFFFFull) | ((uint64_t)slotOf[(uint32_t)(op >> 32)] << 32);
-    T.ops[(size_t)T.ep_opoff[x.e] + (size_t)x.k() * T.qpad + slotOf[x.q()]] = op;
-  }
-  // points: renumber in walk order (epoch, slot, qubit) so each epoch owns a contiguous range
+  // points are numbered in walk order (epoch, slot, qubit slot), so each
+  // epoch owns a contiguous range; a large tape is scattered and renumbered
+  // in pieces on the pool (disjoint ops and points per piece)
+  T.ep_ptoff.assign(nE + 1, 0);
+  for (uint32_t e = 0; e < nE; ++e) T.ep_ptoff[e + 1] = T.ep_ptoff[e] + ep_np[e];
   std::vector<uint32_t> &remap = B.remap;
   remap.assign(nprov, kNone);
-  T.ep_ptoff.assign(nE + 1, 0);
-  uint32_t next = 0;
-  for (uint32_t e = 0; e < nE; ++e) {
-    T.ep_ptoff[e] = next;
-    uint64_t *base = T.ops.data() + T.ep_opoff[e];
-    const size_t n = (size_t)T.ep_k[e] * T.qpad;
-    for (size_t i = 0; i < n; ++i) {
-      uint64_t &op = base[i];
-      uint32_t opc = (uint32_t)(op & 0xFF);
-      if (opc == OP_SNAP || opc == OP_SNAPD) {
-        remap[(uint32_t)(op >> 32)] = next;
-        op = (op & 0xFFFFFFFFull) | ((uint64_t)next << 32);
-        ++next;
-      }
+  const uint32_t pieces = pool && total >= (1u << 16) ? std::min(8u, pool->workers() + 1) : 1u;
+  const size_t nent = (size_t)(ent1 - ent0);
+  auto scatter = [&](uint32_t q, uint32_t) {
+    for (size_t i = nent * q / pieces, i1 = nent * (q + 1) / pieces; i < i1; ++i) {
+      const Entry &x = ent0[i];
+      uint64_t op = x.op;
+      const uint32_t opc = (uint32_t)(op & 0xFF);
+      if (opc == OP_C2 || opc >= OP_XPX)  // partner qubit -> partner slot
+        op = (op & 0xFFFFFFFFull) | ((uint64_t)slotOf[(uint32_t)(op >> 32)] << 32);
+      T.ops[(size_t)T.ep_opoff[x.e] + (size_t)x.k() * T.qpad + slotOf[x.q()]] = op;
     }
+  };
+  std::atomic<bool> miscount{false};
+  auto renumber = [&](uint32_t q, uint32_t) {
+    for (uint32_t e = (uint32_t)((uint64_t)nE * q / pieces), e1 = (uint32_t)((uint64_t)nE * (q + 1) / pieces); e < e1;
+         ++e) {
+      uint32_t next = T.ep_ptoff[e];
+      uint64_t *base = T.ops.data() + T.ep_opoff[e];
+      const size_t n = (size_t)T.ep_k[e] * T.qpad;
+      for (size_t i = 0; i < n; ++i) {
+        uint64_t &op = base[i];
+        const uint32_t opc = (uint32_t)(op & 0xFF);
+        if (opc == OP_SNAP || opc == OP_SNAPD) {
+          remap[(uint32_t)(op >> 32)] = next;
+          op = (op & 0xFFFFFFFFull) | ((uint64_t)next << 32);
+          ++next;
+        }
+      }
+      if (next != T.ep_ptoff[e + 1]) miscount = true;
+    }
+  };
+  if (pieces > 1) {
+    pool->run(pieces, scatter);
+    pool->run(pieces, renumber);
+  } else {
+    scatter(0, 0);
+    renumber(0, 0);
   }
-  T.ep_ptoff[nE] = next;
+  if (miscount) throw Error(GPC_ERR_INVALID, "internal: points per epoch miscounted");
+  const uint32_t next = T.ep_ptoff[nE];
   T.npoints = next;
   // copy chunks: runs of whole epochs of at most chunk_cap bytes, chunk_cap
   // sized from the largest epoch (and at least opt.chunk_min)

@@ -179,8 +179,9 @@ struct LowerScratch {
   struct Buffers;
   std::unique_ptr<Buffers> b;
 };
-// lower() into T (reset first), with S's buffers.
-void lower_into(const Parsed &p, const LowerOptions &opt, Tape &T, LowerScratch &S);
+// lower() into T (reset first), with S's buffers; a large tape is assembled
+// in pieces on `pool`'s threads when a pool is given.
+void lower_into(const Parsed &p, const LowerOptions &opt, Tape &T, LowerScratch &S, HostPool *pool = nullptr);
 // parse_stim + lower_into, parsing into S.parsed (a large text in pieces on
 // `pool`'s threads when a pool is given).
 void lower_text(const char *text, size_t len, const LowerOptions &opt, Tape &T, LowerScratch &S,

@@ -18,6 +18,34 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (run with -m gpu)")
 
 
+def repetition_with_repeat(rounds: int = 5, p: float = 1e-3) -> str:
+    """A distance-3 repetition-code memory whose later rounds sit in a REPEAT block
+    (the block's targets are stored once and occur once per repetition)."""
+    layer = (f"DEPOLARIZE1({p}) 0 2 4\nCX 0 1 2 3\nDEPOLARIZE2({p}) 0 1 2 3\nTICK\n"
+             f"CX 2 1 4 3\nDEPOLARIZE2({p}) 2 1 4 3\nTICK\nX_ERROR({p}) 1 3\nMR 1 3\n")
+    return ("R 0 1 2 3 4\nTICK\n" + layer + "DETECTOR rec[-2]\nDETECTOR rec[-1]\n"
+            f"REPEAT {rounds} {{\nTICK\n" + layer + "DETECTOR rec[-2] rec[-4]\nDETECTOR rec[-1] rec[-3]\n}\n"
+            f"X_ERROR({p}) 0 2 4\nM 0 2 4\nDETECTOR rec[-3] rec[-2] rec[-5]\nDETECTOR rec[-2] rec[-1] rec[-4]\n"
+            "OBSERVABLE_INCLUDE(0) rec[-1]\n")
+
+
+def flatten_repeats(text: str) -> str:
+    """The same circuit with its (non-nested) REPEAT blocks written out."""
+    out, body, reps = [], None, 0
+    for line in text.splitlines():
+        s = line.strip()
+        if s.startswith("REPEAT"):
+            reps, body = int(s.split()[1]), []
+        elif s == "}" and body is not None:
+            out += body * reps
+            body = None
+        elif body is not None:
+            body.append(line)
+        else:
+            out.append(line)
+    return "\n".join(out) + "\n"
+
+
 def load_canonical_dem(path: Path):
     """Parses a canonical fixture DEM into {targets tuple: p} (observable k -> 'L', k)."""
     out = {}

@@ -15,7 +15,7 @@ import numpy as np
 import pytest
 
 import greenpeas_gb300 as gp
-from conftest import compare_errors
+from conftest import compare_errors, repetition_with_repeat
 from greenpeas_gb300 import noise as N
 from greenpeas_gb300.autograd import NoiseRateDEM
 from oracle import oracle as O
@@ -36,6 +36,7 @@ CASES = {
     "surface3-L0": (lambda: gp.SurfaceCode(3).get_memory(3, 1e-3, noise="uniform"), 0),
     "surface5-reference-L1": (lambda: gp.SurfaceCode(5).get_memory(5, 1e-3, noise="reference"), 1),
     "bb72-L2": (lambda: gp.BBCode(6).get_memory(6, 1e-3, noise="uniform"), 2),
+    "repetition-repeat-L2": (lambda: repetition_with_repeat(6), 2),
 }
 
 

@@ -5,7 +5,7 @@ from __future__ import annotations
 import numpy as np
 import pytest
 
-from conftest import GOLDEN, compare_errors, load_canonical_dem, to_named
+from conftest import GOLDEN, compare_errors, flatten_repeats, load_canonical_dem, repetition_with_repeat, to_named
 from greenpeas_gb300 import BBCode, SurfaceCode, Tape
 from greenpeas_gb300._native import GpcError
 from oracle import oracle as O
@@ -62,12 +62,30 @@ def test_large_text_parsed_in_pieces_gives_the_same_tape():
         assert np.array_equal(a[k], b[k]), k
 
 
+def test_large_tape_matches_oracle():
+    """A text this large is parsed in pieces and its tape scattered and renumbered on several
+    threads; interpreted on the CPU, the tape gives the oracle's DEM."""
+    text = BBCode(12).get_memory(12, 1e-3, noise="uniform")
+    compare_errors(compile_tape(Tape(text)), _oracle(text))
+
+
 @pytest.mark.parametrize("bad,code", [("FOO 1\n", -3), ("CX 5\n", -2), ("CX rec[-1] 0\n", -3)])
 def test_large_text_error_in_a_late_piece(bad, code):
     text = BBCode(12).get_memory(12, 1e-3, noise="uniform")
     with pytest.raises(GpcError) as ei:
         Tape(text + bad)
     assert ei.value.status == code
+
+
+def test_repeat_block_gives_the_tape_of_its_flattened_circuit():
+    """Every array of the tape -- ops, records, and the records' (tick, class) sources --
+    equals that of the circuit with the REPEAT block written out (500 repetitions share
+    one stored copy of the block's targets)."""
+    text = repetition_with_repeat(500)
+    a, b = _tape_arrays(Tape(text)), _tape_arrays(Tape(flatten_repeats(text)))
+    assert a["num_ticks"] == 3 * 501 + 1  # 1503 TICKs
+    for k in a:
+        assert np.array_equal(a[k], b[k]), k
 
 
 def test_tape_shapes():

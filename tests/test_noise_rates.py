@@ -17,6 +17,7 @@ import pytest
 from greenpeas_gb300 import error_analysis as ea
 from greenpeas_gb300 import noise as N
 from greenpeas_gb300.codes import BBCode, SurfaceCode
+from conftest import repetition_with_repeat
 from oracle import oracle as O
 
 
@@ -32,7 +33,8 @@ def _tape_sources(text, level=2):
 
 @pytest.mark.parametrize("text", [SurfaceCode(3).get_memory(3, 1e-3, noise="uniform"),
                                   SurfaceCode(3).get_memory(2, 1e-3, noise="reference"),
-                                  BBCode(6).get_memory(2, 1e-3, noise="uniform")])
+                                  BBCode(6).get_memory(2, 1e-3, noise="uniform"),
+                                  repetition_with_repeat(4)])
 def test_sources_agree_between_lowering_oracle_and_text(text):
     t, tape = _tape_sources(text)
     assert t.num_ticks == N.num_ticks(text)
