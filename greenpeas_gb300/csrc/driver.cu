@@ -186,6 +186,14 @@ struct gpc_driver {
     if (!pool) pool.reset(new gpc::HostPool(host_threads() - 1));
     return *pool;
   }
+  // Circuit indices by decreasing size (the order batch work is handed out in).
+  std::vector<uint32_t> big_first;
+  template <typename F>
+  void order_by_size(uint32_t n, F &&size) {
+    big_first.resize(n);
+    for (uint32_t i = 0; i < n; ++i) big_first[i] = i;
+    std::stable_sort(big_first.begin(), big_first.end(), [&](uint32_t a, uint32_t b) { return size(a) > size(b); });
+  }
   // fn(i, slot) for i < n, on the host pool when `parallel`.
   void for_each(uint32_t n, bool parallel, const std::function<void(uint32_t, uint32_t)> &fn) {
     if (!parallel || n < 2) {
@@ -452,7 +460,9 @@ struct gpc_driver {
     std::vector<CircuitDev> cd(N);
     std::vector<uint32_t> mb(N + 1), cb(N);
     // circuits fill disjoint regions of the staging buffer: a batch copies in parallel
-    for_each(N, N >= 8, [&](uint32_t i, uint32_t) {
+    order_by_size(N, [&](uint32_t i) { return (uint64_t)tapes[i].ops.size() + tapes[i].rec.size(); });
+    for_each(N, N >= 8, [&](uint32_t x, uint32_t) {
+      const uint32_t i = big_first[x];
       const Tape &T = tapes[i];
       const CircLayout &l = L.c[i];
       const size_t ob = T.ops.size() * 8;
@@ -552,10 +562,15 @@ struct gpc_driver {
     gpc::HostPool &hp = host_pool();
     if (lower_scratch.size() < hp.workers() + 1) lower_scratch.resize(hp.workers() + 1);
     tapes.resize(n);
+    order_by_size(n, [&](uint32_t i) { return (uint64_t)lens[i]; });
     if (n == 1)  // one circuit: a large text is parsed in pieces on the pool
       gpc::lower_text(texts[0], lens[0], lo, tapes[0], lower_scratch[0], &hp);
     else
-      hp.run(n, [&](uint32_t i, uint32_t slot) { gpc::lower_text(texts[i], lens[i], lo, tapes[i], lower_scratch[slot]); });
+      // largest texts first, so no large circuit starts last and holds up the batch
+      hp.run(n, [&](uint32_t x, uint32_t slot) {
+        const uint32_t i = big_first[x];
+        gpc::lower_text(texts[i], lens[i], lo, tapes[i], lower_scratch[slot]);
+      });
   }
 
   // Prepares circuits already lowered on the host (serving lowers requests as they arrive).
@@ -1122,7 +1137,8 @@ struct gpc_driver {
     const uint2 *CO = reinterpret_cast<const uint2 *>(hc);
     outs.assign(N, nullptr);
     try {
-      for_each(N, N >= 8, [&](uint32_t i, uint32_t) {
+      for_each(N, N >= 8, [&](uint32_t x, uint32_t) {
+        const uint32_t i = big_first[x];
         const uint32_t c0 = N > 1 ? CO[i].x : 0, c1 = (N > 1 && i + 1 < N) ? CO[i + 1].x : C;
         const uint32_t t0 = N > 1 ? CO[i].y : 0, t1 = (N > 1 && i + 1 < N) ? CO[i + 1].y : NT;
         if (c1 < c0 || c1 > C || t1 < t0 || t1 > NT) throw gpc::Error(GPC_ERR_CUDA, "inconsistent batch ranges");

@@ -39,7 +39,8 @@ class HostPool {
   unsigned workers() const { return (unsigned)threads_.size(); }
 
   // Runs fn(i, slot) for every i in [0, n); rethrows the first exception.
-  // Calls from several threads take turns.
+  // Calls from several threads take turns; fn must not call run() on the
+  // same pool (the call would wait for its own turn).
   void run(uint32_t n, const std::function<void(uint32_t, uint32_t)> &fn) {
     if (n == 0) return;
     if (n == 1 || threads_.empty()) {
