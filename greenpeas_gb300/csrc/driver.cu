@@ -142,29 +142,10 @@ struct Layout {
 
 }  // namespace
 
-// Allocator whose resize() leaves new elements of trivial types uninitialised
-// (the DEM arrays are written in full right after they are sized).
-template <typename T>
-struct UninitAlloc : std::allocator<T> {
-  template <typename U>
-  struct rebind {
-    using other = UninitAlloc<U>;
-  };
-  UninitAlloc() = default;
-  template <typename U>
-  UninitAlloc(const UninitAlloc<U> &) noexcept {}
-  template <typename U>
-  void construct(U *) noexcept {}
-  template <typename U, typename... A>
-  void construct(U *p, A &&...a) {
-    ::new ((void *)p) U(std::forward<A>(a)...);
-  }
-};
-
-struct gpc_dem {
-  std::vector<double, UninitAlloc<double>> probs;
-  std::vector<uint32_t, UninitAlloc<uint32_t>> offsets;
-  std::vector<uint32_t, UninitAlloc<uint32_t>> targets;
+struct gpc_dem {  // arrays written in full right after they are sized
+  gpc::HostArray<double> probs;
+  gpc::HostArray<uint32_t> offsets;
+  gpc::HostArray<uint32_t> targets;
   uint32_t num_detectors = 0, num_observables = 0;
   uint64_t num_raw = 0;
   std::string text;

@@ -352,11 +352,12 @@ Parsed parse_stim(const char *text, size_t len) {
 void Tape::reset() {
   nq = qpad = nmeas = ndet = nobs = nbits = w = 0;
   n_epochs = kmax = 0;
-  for (auto *v : {&ep_opoff, &ep_k, &ep_ptoff, &ep_chunk, &ch_off, &ch_bytes, &inj_lo, &inj_hi, &rec_moff, &rec_src})
+  for (auto *v : {&ep_opoff, &ep_k, &ep_ptoff, &ep_chunk, &ch_off, &ch_bytes, &inj_lo, &inj_hi, &rec_moff})
     v->clear();
   ops.clear();
   rec.clear();
   rec_p.clear();
+  rec_src.clear();
   chunk_cap = 0;
   npoints = 0;
   M = 0;
@@ -659,9 +660,16 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
   measLo.assign(m, kNone);
   measHi.assign(m, kNone);
   uint32_t nprov = 0;  // provisional point ids (creation order)
-  T.rec.reserve(P.pool.size());
-  T.rec_p.reserve(P.pool.size());
-  T.rec_src.reserve(P.pool.size());
+  // records: at most three per target occurrence (PAULI_CHANNEL_1), written
+  // through pointers into arrays sized to that bound and cut to size after
+  const size_t rec_max = occ * 3 + 16;
+  T.rec.resize(rec_max);
+  T.rec_p.resize(rec_max);
+  T.rec_src.resize(rec_max);
+  uint64_t *const rec_d = T.rec.data();
+  double *const rec_pp = T.rec_p.data();
+  uint32_t *const rec_s = T.rec_src.data();
+  size_t nrec = 0;
   std::vector<uint32_t> &ep_k = T.ep_k;  // slots per epoch, grown on demand
   std::vector<uint32_t> &ep_np = B.ep_np;  // points per epoch
   ep_np.clear();
@@ -698,9 +706,10 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
     return id;
   };
   auto record = [&](uint32_t pa, uint32_t pb, uint32_t type, uint32_t Pa, uint32_t Pb, double p, uint32_t src) {
-    T.rec.push_back(make_rec(pa, pb, type, Pa, Pb));
-    T.rec_p.push_back(p);
-    T.rec_src.push_back(src);
+    rec_d[nrec] = make_rec(pa, pb, type, Pa, Pb);
+    rec_pp[nrec] = p;
+    rec_s[nrec] = src;
+    ++nrec;
   };
   const uint32_t dep1Type = opt.level == 0 ? REC_DEP1_L0 : REC_DEP1_L12;
   const uint32_t dep2Type = opt.level == 0 ? REC_DEP2_L0 : opt.level == 1 ? REC_DEP2_L1 : REC_DEP2_L2;
@@ -834,6 +843,10 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
         break;
     }
   }
+
+  T.rec.resize(nrec);
+  T.rec_p.resize(nrec);
+  T.rec_src.resize(nrec);
 
   // ---- warp-uniform qubit packing -------------------------------------
   // Qubits with the same sequence of op kinds (data, X-check, Z-check qubits

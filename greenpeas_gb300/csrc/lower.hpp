@@ -22,11 +22,33 @@
 #include <memory>
 #include <stdexcept>
 #include <string>
+#include <utility>
 #include <vector>
 
 namespace gpc {
 
 class HostPool;
+
+// Allocator whose resize() leaves new elements of trivial types uninitialised,
+// for host arrays that are written in full after they are sized.
+template <typename T>
+struct UninitAlloc : std::allocator<T> {
+  template <typename U>
+  struct rebind {
+    using other = UninitAlloc<U>;
+  };
+  UninitAlloc() = default;
+  template <typename U>
+  UninitAlloc(const UninitAlloc<U> &) noexcept {}
+  template <typename U>
+  void construct(U *) noexcept {}
+  template <typename U, typename... A>
+  void construct(U *p, A &&...a) {
+    ::new ((void *)p) U(std::forward<A>(a)...);
+  }
+};
+template <typename T>
+using HostArray = std::vector<T, UninitAlloc<T>>;
 
 // Errors thrown by the lowering carry a gpc_status code.
 struct Error : std::runtime_error {
@@ -120,8 +142,8 @@ struct Tape {
   std::vector<uint32_t> inj_lo;     // [w] first epoch (walk order) injecting into word j, kNone if none
   std::vector<uint32_t> inj_hi;     // [w] last such epoch
   uint32_t npoints = 0;
-  std::vector<uint64_t> rec;        // [R] noise records
-  std::vector<double> rec_p;        // [R] probability of each of the record's mechanisms
+  HostArray<uint64_t> rec;          // [R] noise records
+  HostArray<double> rec_p;          // [R] probability of each of the record's mechanisms
   std::vector<uint32_t> rec_moff;   // [R + 1] first mechanism of each record
   uint32_t M = 0;                   // mechanisms (components)
   // Source of each record for the noise-rate gradient: tick * 4 + class, or
@@ -130,7 +152,7 @@ struct Tape {
   // not directly after a reset of its qubit, or the flip argument of a
   // measurement), 3 reset flip (X/Y/Z_ERROR whose qubit's last operation was
   // a reset).  PAULI_CHANNEL_1 and E have no source.
-  std::vector<uint32_t> rec_src;    // [R]
+  HostArray<uint32_t> rec_src;      // [R]
   uint32_t n_ticks = 1;             // TICK instructions + 1
 
   // Empties the tape, keeping the capacity of its arrays.
