@@ -47,6 +47,12 @@ struct CircuitDev {
   uint32_t mw;                // 64-bit mask words per point: ceil(w / 64)
 };
 
+// *p += v as a reduction that returns nothing (the thread does not wait for
+// the L2 round trip of an atomic whose old value it would not use).
+__device__ __forceinline__ void red_add(uint32_t *p, uint32_t v) {
+  asm volatile("red.global.add.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 constexpr uint32_t kMaxCircuitsStaged = 2048;  // batch tables staged in shared memory up to this size
 
 // Index of the circuit holding item x: the last c with base[c] <= x (base has n+1 entries).

@@ -234,7 +234,7 @@ __global__ void __launch_bounds__(KEY_THREADS) key_kernel(KeyLaunch L) {
     if (cnt > tcap) atomicOr(L.err, DEV_FLAG_LONG);
     const uint32_t am = __activemask();
     const uint32_t tot = __reduce_add_sync(am, cnt);
-    if (lane == (uint32_t)(__ffs(am) - 1) && tot) atomicAdd(L.list_total, tot);
+    if (lane == (uint32_t)(__ffs(am) - 1) && tot) red_add(L.list_total, tot);
   }
   if ((hx | hy) == 0) {
     if (cnt || (!tcap && nonzero)) atomicOr(L.err, DEV_ERR_COLLISION);  // a non-empty symptom hashed to 0
@@ -956,9 +956,9 @@ __global__ void __launch_bounds__(GW_WARPS * 32) group_warp_kernel(GroupLaunch L
   }
   if (lane == 0) {
     L.bagg[b] = make_uint2(gcount, tcount);
-    atomicAdd(&L.tsum[b / SCAN_TILE].x, gcount);
-    atomicAdd(&L.tsum[b / SCAN_TILE].y, tcount);
-    atomicAdd(L.totals + 3, n);
+    red_add(&L.tsum[b / SCAN_TILE].x, gcount);
+    red_add(&L.tsum[b / SCAN_TILE].y, tcount);
+    red_add(L.totals + 3, n);
   }
 }
 
@@ -1080,9 +1080,9 @@ __global__ void __launch_bounds__(GB_THREADS) group_big_kernel(GroupLaunch L) {
         run = c_head[c] ? c_tail[c] : xor_merge(run, c_tail[c]);
       }
       L.bagg[b] = make_uint2(g, t);
-      atomicAdd(&L.tsum[b / SCAN_TILE].x, g);
-      atomicAdd(&L.tsum[b / SCAN_TILE].y, t);
-      atomicAdd(L.totals + 3, n);
+      red_add(&L.tsum[b / SCAN_TILE].x, g);
+      red_add(&L.tsum[b / SCAN_TILE].y, t);
+      red_add(L.totals + 3, n);
     }
     __syncthreads();
     if (seg < 0) x = xor_merge(c_carry[warp], x);

@@ -80,6 +80,12 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
   return true;
 }
 
+// *p |= v as a reduction that returns nothing: the thread does not wait for
+// the atomic's round trip through L2 (measured 8 us of an 82 us walk).
+__device__ __forceinline__ void red_or(unsigned long long *p, unsigned long long v) {
+  asm volatile("red.global.or.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+
 // 1D bulk copy global -> shared, completing `bytes` of transaction count on `bar`.
 __device__ __forceinline__ void bulk_g2s(void *dst, const void *src, uint32_t bytes, uint64_t *bar) {
   asm volatile(
@@ -222,7 +228,7 @@ __global__ void __launch_bounds__(WalkBound<QPT>::value) walk_kernel(const Circu
   auto snapshot = [&](uint32_t arg, const uint64_t *xs, const uint64_t *zs) {
     if constexpr (W == 1) {
       snap0[arg] = make_ulonglong2(xs[0], zs[0]);
-      if (xs[0] | zs[0]) atomicOr(nzm0 + arg * mw, 1ull << jsh);
+      if (xs[0] | zs[0]) red_or(nzm0 + arg * mw, 1ull << jsh);
     } else {
       unsigned long long bits = 0;
 #pragma unroll
@@ -232,7 +238,7 @@ __global__ void __launch_bounds__(WalkBound<QPT>::value) walk_kernel(const Circu
           if (xs[wi] | zs[wi]) bits |= 1ull << (jsh + wi);
         }
       }
-      if (bits) atomicOr(nzm0 + arg * mw, bits);
+      if (bits) red_or(nzm0 + arg * mw, bits);
     }
   };
   for (;; ++e, ++seq) {
@@ -342,7 +348,7 @@ __global__ void __launch_bounds__(WalkBound<QPT>::value) walk_kernel(const Circu
           } else if (opc == OP_SNAPD) {
             if constexpr (W == 1) {
               snap0[arg] = make_ulonglong2(last_inj[u][0], 0ull);
-              if (last_inj[u][0]) atomicOr(nzm0 + arg * mw, 1ull << jsh);
+              if (last_inj[u][0]) red_or(nzm0 + arg * mw, 1ull << jsh);
             } else {
               uint64_t zero[W];
 #pragma unroll
