@@ -166,8 +166,17 @@ def cpu_baseline(text: str, budget_s: float = 10.0) -> dict:
         el = time.perf_counter() - t0
         if el > budget_s or n >= 400:
             break
+    # the same on one thread (a per-circuit figure)
+    n1, t1 = 0, time.perf_counter()
+    while True:
+        O.time_compile(text, 2, 1)
+        n1 += 1
+        el1 = time.perf_counter() - t1
+        if el1 > budget_s / 3 or n1 >= 100:
+            break
     return {"value": n / el, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{n} compiles of the workload in {el:.1f} s (CPU FP64 oracle, all host threads)"}
+            "sample": f"{n} compiles of the workload in {el:.1f} s (CPU FP64 oracle, all host threads)",
+            "single_thread": {"value": n1 / el1, "unit": UNIT, "sample": f"{n1} compiles in {el1:.1f} s on one thread"}}
 
 
 def dem_arrays_equal(a, b) -> bool:
@@ -501,6 +510,18 @@ def main() -> None:
     dom = max(("walk", "key", "sort", "merge"), key=lambda k: stage[k])
     achieved = traffic[names[dom]] / (stage[dom] / 1e3) / 1e9
     peak, peak_kind = peaks()
+    # Whole pipeline, two byte counts: the bytes this design's kernels must move
+    # (sparse symptoms: snapshots and target lists), and the fixed formulas of a
+    # dense-symptom pipeline (8w bytes per raw mechanism written and re-read,
+    # 16-byte keys + 4-byte permutation through an 8-pass radix sort):
+    # B = 8wM + 24M + T  +  2*8*20*M  +  28M + 8wM + C(8w + 8), T = tape bytes (the H2D).
+    M, w, C = sizes["raw"], sizes["words"], ref_dem.num_errors
+    dense = (8 * w * M + 24 * M + h2d) + 2 * 8 * 20 * M + (28 * M + 8 * w * M + C * (8 * w + 8))
+    stored = sum(traffic.values())
+    pipe_s = stage["total"] / 1e3
+    pipeline = {"ms": stage["total"], "algorithmic_bytes_stored": stored, "achieved_stored": stored / pipe_s / 1e9,
+                "algorithmic_bytes_dense": dense, "achieved_dense": dense / pipe_s / 1e9,
+                "frac_dense": dense / pipe_s / 1e9 / peak}
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
@@ -516,7 +537,8 @@ def main() -> None:
                      "frac": achieved / peak, "peak_source": peak_kind,
                      "algorithmic_bytes": traffic[names[dom]],
                      "traffic": WALK_DRAM_BYTES_PER_LAUNCH if dom == "walk" else None,
-                     "note": "latency-bound: one CTA per 64-bit detector word walks the circuit"},
+                     "note": "latency-bound: one CTA per 64-bit detector word walks the circuit",
+                     "pipeline": pipeline},
         "gpu_launches": KERNELS_PER_RUN * args.steps,
         "clocks": clocks.summary(),
     }
