@@ -382,8 +382,20 @@ struct LowerScratch::Buffers {
   std::vector<uint32_t> measBase, occBase, tsrc, moff, mbits, measLo, measHi, slotOf, order, remap, ep_np;
   std::vector<std::pair<uint32_t, uint32_t>> detPairs, obsPairs, groups;
   std::vector<uint8_t> lastReset;
-  RawArray<Entry> ent;
-  std::vector<QState> st;
+  // one time segment of the backward pass (its entries, epochs, points and records)
+  struct Segment {
+    RawArray<Entry> ent;
+    size_t nent = 0;
+    std::vector<QState> st;
+    std::vector<uint32_t> ep_k, ep_np;
+    HostArray<uint64_t> rec;
+    HostArray<double> rec_p;
+    HostArray<uint32_t> rec_src;
+    size_t nrec = 0, roff = 0;
+    uint32_t nprov = 0, eoff = 0, poff = 0;
+  };
+  std::vector<Segment> segs;
+  std::vector<size_t> cut;
   std::vector<uint64_t> fine, coarse;
 };
 
@@ -650,203 +662,283 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
   }
 
   // ---- backward pass: epoch scheduling and noise records -----------------
-  // tape entries: at most one per target occurrence, plus two per measurement
-  // and one per further bit of a measurement (its OP_M, OP_SNAPD, OP_INJ slots)
-  Entry *const ent0 = B.ent.get(occ * 3 + mbits.size() + 16);
-  Entry *ent1 = ent0;
-  std::vector<QState> &st = B.st;
-  st.assign(nq, QState{});
+  // The circuit is cut into time segments of a fixed number of target
+  // occurrences (the cut depends on the circuit alone).  Each segment is
+  // scheduled backwards from a fresh qubit state -- its first epoch starts
+  // empty for every qubit -- and the segments are stitched in walk order:
+  // a segment's epochs, points and records follow those of the segments after
+  // it in time.  Every qubit keeps its op order and the records keep theirs,
+  // so the DEM is that of one uncut pass; the schedule gains at most about one
+  // epoch per cut.  Segments run on the pool when one is given.
+  std::vector<size_t> &cut = B.cut;  // segment s covers instructions [cut[s + 1], cut[s])
+  cut.clear();
+  cut.push_back(P.ins.size());
+  {
+    const size_t per = std::max<size_t>(16384, occ / 8);
+    size_t acc = 0;
+    for (size_t ii = P.ins.size(); ii-- > 1;) {
+      acc += P.ins[ii].tn;
+      if (acc >= per) {
+        cut.push_back(ii);
+        acc = 0;
+      }
+    }
+    cut.push_back(0);
+  }
+  const uint32_t nseg = (uint32_t)cut.size() - 1;
+  if (B.segs.size() < nseg) B.segs.resize(nseg);
   std::vector<uint32_t> &measLo = B.measLo, &measHi = B.measHi;
   measLo.assign(m, kNone);
   measHi.assign(m, kNone);
-  uint32_t nprov = 0;  // provisional point ids (creation order)
-  // records: at most three per target occurrence (PAULI_CHANNEL_1), written
-  // through pointers into arrays sized to that bound and cut to size after
-  const size_t rec_max = occ * 3 + 16;
-  T.rec.resize(rec_max);
-  T.rec_p.resize(rec_max);
-  T.rec_src.resize(rec_max);
-  uint64_t *const rec_d = T.rec.data();
-  double *const rec_pp = T.rec_p.data();
-  uint32_t *const rec_s = T.rec_src.data();
-  size_t nrec = 0;
-  std::vector<uint32_t> &ep_k = T.ep_k;  // slots per epoch, grown on demand
-  std::vector<uint32_t> &ep_np = B.ep_np;  // points per epoch
-  ep_np.clear();
-  SplitCache split;
-
-  auto place1 = [&](uint32_t q, uint64_t op) -> uint32_t {
-    QState &s = st[q];
-    uint32_t e;
-    if (s.last < 0) {
-      e = 0;
-      s.cnt = 0;
-    } else if (s.cnt >= kcap) {
-      e = (uint32_t)s.last + 1;
-      s.cnt = 0;
-    } else {
-      e = (uint32_t)s.last;
-    }
-    *ent1++ = {q | (s.cnt << 24), e, op};
-    if (e >= ep_k.size()) {
-      ep_k.resize((size_t)e + 1, 0);
-      ep_np.resize((size_t)e + 1, 0);
-    }
-    ep_k[e] = std::max(ep_k[e], s.cnt + 1);
-    s.last = e;
-    s.cnt++;
-    return e;
-  };
-  auto point = [&](uint32_t q) -> uint32_t {
-    QState &s = st[q];
-    if (s.open != kNone) return s.open;
-    uint32_t id = nprov++;
-    ++ep_np[place1(q, make_op(OP_SNAP, 0, id))];
-    s.open = id;
-    return id;
-  };
-  auto record = [&](uint32_t pa, uint32_t pb, uint32_t type, uint32_t Pa, uint32_t Pb, double p, uint32_t src) {
-    rec_d[nrec] = make_rec(pa, pb, type, Pa, Pb);
-    rec_pp[nrec] = p;
-    rec_s[nrec] = src;
-    ++nrec;
-  };
   const uint32_t dep1Type = opt.level == 0 ? REC_DEP1_L0 : REC_DEP1_L12;
   const uint32_t dep2Type = opt.level == 0 ? REC_DEP2_L0 : opt.level == 1 ? REC_DEP2_L1 : REC_DEP2_L2;
+  auto occ_at = [&](size_t i) -> size_t { return i < P.ins.size() ? occBase[i] : occ; };
+  auto meas_at = [&](size_t i) -> uint32_t { return i < P.ins.size() ? measBase[i] : m; };
 
-  for (size_t ii = P.ins.size(); ii-- > 0;) {
-    const Instr &in = P.ins[ii];
-    const Gate &g = kGates[in.gate];
-    const uint32_t *t = P.pool.data() + in.t0;
-    switch (g.kind) {
-      case G_C1:
-        for (uint32_t k = in.tn; k-- > 0;) {
-          uint32_t q = t[k];
-          place1(q, make_op(OP_C1, (uint32_t)g.a | ((uint32_t)g.b << 2), 0));
-          st[q].open = kNone;
-        }
-        break;
-      case G_C2:
-        for (uint32_t k = in.tn; k >= 2; k -= 2) {
-          uint32_t a = t[k - 2], b = t[k - 1];
-          uint32_t E = (uint32_t)(std::max(st[a].last, st[b].last) + 1);
-          uint32_t subA = (uint32_t)g.img[0] | ((uint32_t)g.img[1] << 4);
-          uint32_t subB = swap_halves(g.img[2]) | (swap_halves(g.img[3]) << 4);
-          *ent1++ = {a, E, c2_op(subA, b)};  // partner operands become slots below
-          *ent1++ = {b, E, c2_op(subB, a)};
-          if (E >= ep_k.size()) {
-            ep_k.resize((size_t)E + 1, 0);
-            ep_np.resize((size_t)E + 1, 0);
-          }
-          ep_k[E] = std::max<uint32_t>(ep_k[E], 1);
-          st[a].last = st[b].last = E;
-          st[a].cnt = st[b].cnt = 1;
-          st[a].open = st[b].open = kNone;
-        }
-        break;
-      case G_R:
-        for (uint32_t k = in.tn; k-- > 0;) {
-          place1(t[k], make_op(OP_R, 0, 0));
-          st[t[k]].open = kNone;
-        }
-        break;
-      case G_M:
-      case G_MR: {
-        double p = in.nargs ? in.args[0] : 0.0;
-        uint32_t sub = (uint32_t)g.a | (g.kind == G_MR ? 4u : 0u);
-        for (uint32_t k = in.tn; k-- > 0;) {
-          uint32_t q = t[k];
-          uint32_t meas = measBase[ii] + k;
-          const uint32_t b0 = moff[meas], b1 = moff[meas + 1];
-          // bits beyond the first ride on OP_INJ slots placed before the OP_M
-          uint32_t first = b0 < b1 ? mbits[b0] : kNone;
-          uint32_t lo = kNone;
-          for (uint32_t b = b0 + 1; b < b1; b += 2) {
-            uint32_t e = place1(q, make_inj(mbits[b], b + 1 < b1 ? mbits[b + 1] : 0xFFFFFFu));
-            if (lo == kNone) lo = e;
-          }
-          uint32_t e = place1(q, make_op(OP_M, sub, first));
-          measLo[meas] = lo == kNone ? e : lo;
-          measHi[meas] = e;
-          st[q].open = kNone;
-          if (p > 0 && b1 > b0) {
-            uint32_t id = nprov++;
-            ++ep_np[place1(q, make_op(OP_SNAPD, 0, id))];
-            record(id, 0, REC_PAULI, 1, 0, p, tsrc[occBase[ii] + k]);
-          }
-        }
-        break;
+  auto run_segment = [&](uint32_t sg) {
+    LowerScratch::Buffers::Segment &G = B.segs[sg];
+    const size_t i0 = cut[sg + 1], i1 = cut[sg];
+    const size_t socc = occ_at(i1) - occ_at(i0);
+    const size_t sbits = moff[meas_at(i1)] - moff[meas_at(i0)];
+    // tape entries: at most one per target occurrence, plus two per
+    // measurement and one per further bit of a measurement (OP_M, OP_SNAPD, OP_INJ)
+    Entry *const ent0 = G.ent.get(socc * 3 + sbits + 16);
+    Entry *ent1 = ent0;
+    std::vector<QState> &st = G.st;
+    st.assign(nq, QState{});
+    std::vector<uint32_t> &ep_k = G.ep_k, &ep_np = G.ep_np;  // slots and points per epoch, grown on demand
+    ep_k.clear();
+    ep_np.clear();
+    uint32_t nprov = 0;  // provisional point ids (creation order)
+    // records: at most three per target occurrence (PAULI_CHANNEL_1), written
+    // through pointers into arrays sized to that bound and cut to size after
+    const size_t rec_max = socc * 3 + 16;
+    HostArray<uint64_t> &RD = nseg == 1 ? T.rec : G.rec;
+    HostArray<double> &RP = nseg == 1 ? T.rec_p : G.rec_p;
+    HostArray<uint32_t> &RS = nseg == 1 ? T.rec_src : G.rec_src;
+    RD.resize(rec_max);
+    RP.resize(rec_max);
+    RS.resize(rec_max);
+    uint64_t *const rec_d = RD.data();
+    double *const rec_pp = RP.data();
+    uint32_t *const rec_s = RS.data();
+    size_t nrec = 0;
+    SplitCache split;
+
+    auto place1 = [&](uint32_t q, uint64_t op) -> uint32_t {
+      QState &s = st[q];
+      uint32_t e;
+      if (s.last < 0) {
+        e = 0;
+        s.cnt = 0;
+      } else if (s.cnt >= kcap) {
+        e = (uint32_t)s.last + 1;
+        s.cnt = 0;
+      } else {
+        e = (uint32_t)s.last;
       }
-      case G_N1: {
-        for (uint32_t k = in.tn; k-- > 0;) {
-          uint32_t q = t[k];
-          switch (g.a) {
-            case N1_X:
-            case N1_Y:
-            case N1_Z:
-              if (in.args[0] > 0)
-                record(point(q), 0, REC_PAULI, g.a == N1_X ? 1 : g.a == N1_Z ? 2 : 3, 0, in.args[0], tsrc[occBase[ii] + k]);
-              break;
-            case N1_DEP1:
-              if (in.args[0] > 0) record(point(q), 0, dep1Type, 0, 0, split.dep1(in.args[0]), tsrc[occBase[ii] + k]);
-              break;
-            case N1_PC1: {
-              double qq[3];
-              pc1_independent(in.args[0], in.args[1], in.args[2], qq);
-              if (qq[0] > 0 || qq[1] > 0 || qq[2] > 0) {
-                uint32_t pt = point(q);
-                if (qq[0] > 0) record(pt, 0, REC_PAULI, 1, 0, qq[0], kNone);
-                if (qq[1] > 0) record(pt, 0, REC_PAULI, 3, 0, qq[1], kNone);
-                if (qq[2] > 0) record(pt, 0, REC_PAULI, 2, 0, qq[2], kNone);
-              }
-              break;
+      *ent1++ = {q | (s.cnt << 24), e, op};
+      if (e >= ep_k.size()) {
+        ep_k.resize((size_t)e + 1, 0);
+        ep_np.resize((size_t)e + 1, 0);
+      }
+      ep_k[e] = std::max(ep_k[e], s.cnt + 1);
+      s.last = e;
+      s.cnt++;
+      return e;
+    };
+    auto point = [&](uint32_t q) -> uint32_t {
+      QState &s = st[q];
+      if (s.open != kNone) return s.open;
+      uint32_t id = nprov++;
+      ++ep_np[place1(q, make_op(OP_SNAP, 0, id))];
+      s.open = id;
+      return id;
+    };
+    auto record = [&](uint32_t pa, uint32_t pb, uint32_t type, uint32_t Pa, uint32_t Pb, double p, uint32_t src) {
+      rec_d[nrec] = make_rec(pa, pb, type, Pa, Pb);
+      rec_pp[nrec] = p;
+      rec_s[nrec] = src;
+      ++nrec;
+    };
+
+    for (size_t ii = i1; ii-- > i0;) {
+      const Instr &in = P.ins[ii];
+      const Gate &g = kGates[in.gate];
+      const uint32_t *t = P.pool.data() + in.t0;
+      switch (g.kind) {
+        case G_C1:
+          for (uint32_t k = in.tn; k-- > 0;) {
+            uint32_t q = t[k];
+            place1(q, make_op(OP_C1, (uint32_t)g.a | ((uint32_t)g.b << 2), 0));
+            st[q].open = kNone;
+          }
+          break;
+        case G_C2:
+          for (uint32_t k = in.tn; k >= 2; k -= 2) {
+            uint32_t a = t[k - 2], b = t[k - 1];
+            uint32_t E = (uint32_t)(std::max(st[a].last, st[b].last) + 1);
+            uint32_t subA = (uint32_t)g.img[0] | ((uint32_t)g.img[1] << 4);
+            uint32_t subB = swap_halves(g.img[2]) | (swap_halves(g.img[3]) << 4);
+            *ent1++ = {a, E, c2_op(subA, b)};  // partner operands become slots below
+            *ent1++ = {b, E, c2_op(subB, a)};
+            if (E >= ep_k.size()) {
+              ep_k.resize((size_t)E + 1, 0);
+              ep_np.resize((size_t)E + 1, 0);
+            }
+            ep_k[E] = std::max<uint32_t>(ep_k[E], 1);
+            st[a].last = st[b].last = E;
+            st[a].cnt = st[b].cnt = 1;
+            st[a].open = st[b].open = kNone;
+          }
+          break;
+        case G_R:
+          for (uint32_t k = in.tn; k-- > 0;) {
+            place1(t[k], make_op(OP_R, 0, 0));
+            st[t[k]].open = kNone;
+          }
+          break;
+        case G_M:
+        case G_MR: {
+          double p = in.nargs ? in.args[0] : 0.0;
+          uint32_t sub = (uint32_t)g.a | (g.kind == G_MR ? 4u : 0u);
+          for (uint32_t k = in.tn; k-- > 0;) {
+            uint32_t q = t[k];
+            uint32_t meas = measBase[ii] + k;
+            const uint32_t b0 = moff[meas], b1 = moff[meas + 1];
+            // bits beyond the first ride on OP_INJ slots placed before the OP_M
+            uint32_t first = b0 < b1 ? mbits[b0] : kNone;
+            uint32_t lo = kNone;
+            for (uint32_t b = b0 + 1; b < b1; b += 2) {
+              uint32_t e = place1(q, make_inj(mbits[b], b + 1 < b1 ? mbits[b + 1] : 0xFFFFFFu));
+              if (lo == kNone) lo = e;
+            }
+            uint32_t e = place1(q, make_op(OP_M, sub, first));
+            measLo[meas] = lo == kNone ? e : lo;
+            measHi[meas] = e;
+            st[q].open = kNone;
+            if (p > 0 && b1 > b0) {
+              uint32_t id = nprov++;
+              ++ep_np[place1(q, make_op(OP_SNAPD, 0, id))];
+              record(id, 0, REC_PAULI, 1, 0, p, tsrc[occBase[ii] + k]);
             }
           }
+          break;
         }
-        break;
-      }
-      case G_N2: {
-        if (!(in.args[0] > 0)) break;
-        const double sp = split.dep2(in.args[0]);
-        for (uint32_t k = in.tn; k >= 2; k -= 2) {
-          uint32_t a = t[k - 2], b = t[k - 1];
-          uint32_t pa = point(a), pb = point(b);
-          record(pa, pb, dep2Type, 0, 0, sp, tsrc[occBase[ii] + k - 2]);
-        }
-        break;
-      }
-      case G_CORR: {
-        double p = in.args[0];
-        if (!(p > 0)) break;
-        uint32_t q0 = kNone, q1 = kNone, P0 = 0, P1 = 0;
-        for (uint32_t k = 0; k < in.tn; ++k) {
-          uint32_t q = t[k] & 0xFFFFFFu, Pv = (t[k] >> 24) & 3u;
-          if (q0 == kNone || q0 == q) {
-            q0 = q;
-            P0 ^= Pv;
-          } else if (q1 == kNone || q1 == q) {
-            q1 = q;
-            P1 ^= Pv;
-          } else {
-            throw Error(GPC_ERR_UNSUPPORTED, "correlated errors on more than two qubits are not supported");
+        case G_N1: {
+          for (uint32_t k = in.tn; k-- > 0;) {
+            uint32_t q = t[k];
+            switch (g.a) {
+              case N1_X:
+              case N1_Y:
+              case N1_Z:
+                if (in.args[0] > 0)
+                  record(point(q), 0, REC_PAULI, g.a == N1_X ? 1 : g.a == N1_Z ? 2 : 3, 0, in.args[0], tsrc[occBase[ii] + k]);
+                break;
+              case N1_DEP1:
+                if (in.args[0] > 0) record(point(q), 0, dep1Type, 0, 0, split.dep1(in.args[0]), tsrc[occBase[ii] + k]);
+                break;
+              case N1_PC1: {
+                double qq[3];
+                pc1_independent(in.args[0], in.args[1], in.args[2], qq);
+                if (qq[0] > 0 || qq[1] > 0 || qq[2] > 0) {
+                  uint32_t pt = point(q);
+                  if (qq[0] > 0) record(pt, 0, REC_PAULI, 1, 0, qq[0], kNone);
+                  if (qq[1] > 0) record(pt, 0, REC_PAULI, 3, 0, qq[1], kNone);
+                  if (qq[2] > 0) record(pt, 0, REC_PAULI, 2, 0, qq[2], kNone);
+                }
+                break;
+              }
+            }
           }
+          break;
         }
-        if (P0 && P1)
-          record(point(q0), point(q1), REC_PAULI, P0, P1, p, kNone);
-        else if (P0)
-          record(point(q0), 0, REC_PAULI, P0, 0, p, kNone);
-        else if (P1)
-          record(point(q1), 0, REC_PAULI, P1, 0, p, kNone);
-        break;
+        case G_N2: {
+          if (!(in.args[0] > 0)) break;
+          const double sp = split.dep2(in.args[0]);
+          for (uint32_t k = in.tn; k >= 2; k -= 2) {
+            uint32_t a = t[k - 2], b = t[k - 1];
+            uint32_t pa = point(a), pb = point(b);
+            record(pa, pb, dep2Type, 0, 0, sp, tsrc[occBase[ii] + k - 2]);
+          }
+          break;
+        }
+        case G_CORR: {
+          double p = in.args[0];
+          if (!(p > 0)) break;
+          uint32_t q0 = kNone, q1 = kNone, P0 = 0, P1 = 0;
+          for (uint32_t k = 0; k < in.tn; ++k) {
+            uint32_t q = t[k] & 0xFFFFFFu, Pv = (t[k] >> 24) & 3u;
+            if (q0 == kNone || q0 == q) {
+              q0 = q;
+              P0 ^= Pv;
+            } else if (q1 == kNone || q1 == q) {
+              q1 = q;
+              P1 ^= Pv;
+            } else {
+              throw Error(GPC_ERR_UNSUPPORTED, "correlated errors on more than two qubits are not supported");
+            }
+          }
+          if (P0 && P1)
+            record(point(q0), point(q1), REC_PAULI, P0, P1, p, kNone);
+          else if (P0)
+            record(point(q0), 0, REC_PAULI, P0, 0, p, kNone);
+          else if (P1)
+            record(point(q1), 0, REC_PAULI, P1, 0, p, kNone);
+          break;
+        }
+        default:
+          break;
       }
-      default:
-        break;
+    }
+
+    RD.resize(nrec);
+    RP.resize(nrec);
+    RS.resize(nrec);
+    G.nent = (size_t)(ent1 - ent0);
+    G.nrec = nrec;
+    G.nprov = nprov;
+  };
+  if (pool && nseg > 1)
+    pool->run(nseg, [&](uint32_t sg, uint32_t) { run_segment(sg); });
+  else
+    for (uint32_t sg = 0; sg < nseg; ++sg) run_segment(sg);
+
+  // stitch: offsets of each segment's epochs, points and records in walk order
+  std::vector<uint32_t> &ep_k = T.ep_k;
+  std::vector<uint32_t> &ep_np = B.ep_np;
+  ep_k.clear();
+  ep_np.clear();
+  uint32_t nprov = 0;
+  size_t nrec_all = 0;
+  for (uint32_t sg = 0; sg < nseg; ++sg) {
+    LowerScratch::Buffers::Segment &G = B.segs[sg];
+    G.eoff = (uint32_t)ep_k.size();
+    G.poff = nprov;
+    G.roff = nrec_all;
+    ep_k.insert(ep_k.end(), G.ep_k.begin(), G.ep_k.end());
+    ep_np.insert(ep_np.end(), G.ep_np.begin(), G.ep_np.end());
+    nprov += G.nprov;
+    nrec_all += G.nrec;
+    if (G.eoff)
+      for (uint32_t k = meas_at(cut[sg + 1]); k < meas_at(cut[sg]); ++k)
+        if (measLo[k] != kNone) {
+          measLo[k] += G.eoff;
+          measHi[k] += G.eoff;
+        }
+  }
+  if (nseg > 1) {
+    T.rec.resize(nrec_all);
+    T.rec_p.resize(nrec_all);
+    T.rec_src.resize(nrec_all);
+    for (uint32_t sg = 0; sg < nseg; ++sg) {
+      const LowerScratch::Buffers::Segment &G = B.segs[sg];
+      if (!G.nrec) continue;
+      memcpy(T.rec.data() + G.roff, G.rec.data(), G.nrec * 8);
+      memcpy(T.rec_p.data() + G.roff, G.rec_p.data(), G.nrec * 8);
+      memcpy(T.rec_src.data() + G.roff, G.rec_src.data(), G.nrec * 4);
     }
   }
-
-  T.rec.resize(nrec);
-  T.rec_p.resize(nrec);
-  T.rec_src.resize(nrec);
 
   // ---- warp-uniform qubit packing -------------------------------------
   // Qubits with the same sequence of op kinds (data, X-check, Z-check qubits
@@ -860,12 +952,16 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
     std::vector<uint64_t> &fine = B.fine, &coarse = B.coarse;
     fine.assign(nq, 0xcbf29ce484222325ull);
     coarse.assign(nq, 0xcbf29ce484222325ull);
-    for (const Entry *xp = ent0; xp != ent1; ++xp) {
-      const Entry &x = *xp;
-      const uint32_t opc = (uint32_t)(x.op & 0xFF);
-      if (opc == OP_INJ || opc == OP_SNAPD) continue;  // vary with detector membership only
-      coarse[x.q()] = (coarse[x.q()] ^ opc) * 0x100000001b3ull;
-      fine[x.q()] = (fine[x.q()] ^ (opc | ((uint64_t)x.e << 8))) * 0x100000001b3ull;
+    for (uint32_t sg = 0; sg < nseg; ++sg) {
+      const LowerScratch::Buffers::Segment &G = B.segs[sg];
+      const Entry *const ent0 = G.ent.p.get();
+      for (size_t i = 0; i < G.nent; ++i) {
+        const Entry &x = ent0[i];
+        const uint32_t opc = (uint32_t)(x.op & 0xFF);
+        if (opc == OP_INJ || opc == OP_SNAPD) continue;  // vary with detector membership only
+        coarse[x.q()] = (coarse[x.q()] ^ opc) * 0x100000001b3ull;
+        fine[x.q()] = (fine[x.q()] ^ (opc | ((uint64_t)(x.e + G.eoff) << 8))) * 0x100000001b3ull;
+      }
     }
     const uint32_t qptBase = T.qpad <= 1024 ? 1u : T.qpad <= 2048 ? 2u : 4u;
     // Orders qubits by group (groups in order of their first qubit); returns the
@@ -932,15 +1028,20 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
   std::vector<uint32_t> &remap = B.remap;
   remap.assign(nprov, kNone);
   const uint32_t pieces = pool && total >= (1u << 16) ? std::min(8u, pool->workers() + 1) : 1u;
-  const size_t nent = (size_t)(ent1 - ent0);
   auto scatter = [&](uint32_t q, uint32_t) {
-    for (size_t i = nent * q / pieces, i1 = nent * (q + 1) / pieces; i < i1; ++i) {
-      const Entry &x = ent0[i];
-      uint64_t op = x.op;
-      const uint32_t opc = (uint32_t)(op & 0xFF);
-      if (opc == OP_C2 || opc >= OP_XPX)  // partner qubit -> partner slot
-        op = (op & 0xFFFFFFFFull) | ((uint64_t)slotOf[(uint32_t)(op >> 32)] << 32);
-      T.ops[(size_t)T.ep_opoff[x.e] + (size_t)x.k() * T.qpad + slotOf[x.q()]] = op;
+    for (uint32_t sg = 0; sg < nseg; ++sg) {
+      const LowerScratch::Buffers::Segment &G = B.segs[sg];
+      const Entry *const ent0 = G.ent.p.get();
+      for (size_t i = G.nent * q / pieces, i1 = G.nent * (q + 1) / pieces; i < i1; ++i) {
+        const Entry &x = ent0[i];
+        uint64_t op = x.op;
+        const uint32_t opc = (uint32_t)(op & 0xFF);
+        if (opc == OP_C2 || opc >= OP_XPX)  // partner qubit -> partner slot
+          op = (op & 0xFFFFFFFFull) | ((uint64_t)slotOf[(uint32_t)(op >> 32)] << 32);
+        else if (opc == OP_SNAP || opc == OP_SNAPD)  // segment-local point -> provisional point
+          op += (uint64_t)G.poff << 32;
+        T.ops[(size_t)T.ep_opoff[x.e + G.eoff] + (size_t)x.k() * T.qpad + slotOf[x.q()]] = op;
+      }
     }
   };
   std::atomic<bool> miscount{false};
@@ -998,9 +1099,11 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
   const size_t R = T.rec.size();
   T.rec_moff.resize(R + 1);
   uint64_t mm = 0;
+  uint32_t sg = 0, poff = 0;  // the segment holding record r, and its point offset
   for (size_t r = 0; r < R; ++r) {
+    while (sg + 1 < nseg && r >= B.segs[sg + 1].roff) poff = B.segs[++sg].poff;
     uint64_t &d = T.rec[r];
-    const uint32_t pa = (uint32_t)(d & kMaxPoint28), pb = (uint32_t)((d >> 28) & kMaxPoint28);
+    const uint32_t pa = (uint32_t)(d & kMaxPoint28) + poff, pb = (uint32_t)((d >> 28) & kMaxPoint28) + poff;
     const uint32_t type = (uint32_t)((d >> 56) & 15u), Pb = (uint32_t)(d >> 62);
     const bool hasB = type >= REC_DEP2_L0 || Pb != 0;
     d = (d & ~(((uint64_t)kMaxPoint28) | ((uint64_t)kMaxPoint28 << 28))) | (uint64_t)remap[pa] |

@@ -172,9 +172,11 @@ def test_device_dem_arrays_without_copy():
 
 def test_more_than_1024_qubits():
     """Two qubits per walk thread; the packed slot count need not split into whole warps."""
-    text = gp.SurfaceCode(23).get_memory(2, 1e-3, noise="uniform")
+    # the first round count whose packed slot count leaves a partial warp (1,184 slots: 592 threads)
+    text = next(c for c in (gp.SurfaceCode(23).get_memory(r, 1e-3, noise="uniform") for r in (3, 1, 2, 4))
+                if (gp.Tape(c).qpad // 2) % 32 != 0)
     t = gp.Tape(text)
-    assert t.num_qubits > 1024 and (t.qpad // 2) % 32 != 0  # 1,184 slots: 592 threads
+    assert t.num_qubits > 1024 and (t.qpad // 2) % 32 != 0
     _check(gp.get_driver(text).compile(text), text)
     out = gp.get_driver(text).compile_batch([text, gp.SurfaceCode(3).get_memory(3, 1e-3, noise="uniform")])
     _check(out[0], text)
