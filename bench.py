@@ -286,7 +286,10 @@ def batched_leg(gp, torch, local: int, flush, steps: int, warmup: int, circuits:
     ok = len(outs) == n and all(dem_arrays_equal(a, b) for a, b in zip(outs, singles))
     if not ok:
         raise SystemExit("bench: batched DEMs differ from the plain per-circuit DEMs")
-    bdrv.compile_batch(texts)  # warm the end-to-end path
+    e2e_outs = bdrv.compile_batch(texts)  # warm the end-to-end path
+    if not all(dem_arrays_equal(a, b) for a, b in zip(e2e_outs, singles)):
+        raise SystemExit("bench: end-to-end batched DEMs differ from the plain per-circuit DEMs")
+    del e2e_outs
     h2d_b = d2h_b = 0
     t0 = time.perf_counter()
     e2e_steps = max(1, min(steps, 3))

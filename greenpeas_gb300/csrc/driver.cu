@@ -1184,6 +1184,68 @@ struct gpc_driver {
     for (size_t i = 1; i < outs.size(); ++i) delete outs[i];
     return outs.empty() ? nullptr : outs[0];
   }
+
+  // A second pipeline (own stream and buffers, same settings) for compile_batch.
+  std::unique_ptr<gpc_driver> partner;
+  gpc_driver &twin() {
+    if (!partner) {
+      std::unique_ptr<gpc_driver> d(new gpc_driver());
+      d->device = device;
+      d->level = level;
+      d->sort_bits = sort_bits;
+      d->force_global = force_global;
+      d->walk_qpt = walk_qpt;
+      d->bucket_mean = bucket_mean;
+      d->walk_words = walk_words;
+      d->init_streams();
+      partner = std::move(d);
+    }
+    return *partner;
+  }
+
+  // Compiles n circuits to n DEMs (in order).  A large batch is cut into up to
+  // four chunks that alternate between this pipeline and its twin: chunk c is
+  // lowered on the host while chunk c-1 runs on the device, and chunk c-1's
+  // results are split on the host while chunk c runs.  A circuit's DEM does not
+  // depend on the circuits beside it, so the result equals one pipeline's.
+  void compile_batch(const char *const *texts, const size_t *lens, uint32_t n, std::vector<gpc_dem *> &outs) {
+    size_t bytes = 0;
+    for (uint32_t i = 0; i < n; ++i) bytes += lens[i];
+    const uint32_t K = n >= 32 && bytes >= (8u << 20) ? 4u : 1u;
+    if (K == 1) {
+      prepare(texts, lens, n);
+      run();
+      fetch_all(outs);
+      return;
+    }
+    std::vector<uint32_t> cut{0};  // chunk c: circuits [cut[c], cut[c + 1]), about bytes / K of text each
+    size_t acc = 0;
+    for (uint32_t i = 0; i < n && cut.size() < K; ++i) {
+      acc += lens[i];
+      if (acc * K >= bytes * cut.size() && i + 1 < n) cut.push_back(i + 1);
+    }
+    cut.push_back(n);
+    const uint32_t nc = (uint32_t)cut.size() - 1;
+    gpc_driver *D[2] = {this, &twin()};
+    outs.assign(n, nullptr);
+    auto collect = [&](uint32_t c) {
+      std::vector<gpc_dem *> v;
+      D[c & 1]->fetch_all(v);
+      for (uint32_t i = 0; i < (uint32_t)v.size(); ++i) outs[cut[c] + i] = v[i];
+    };
+    try {
+      for (uint32_t c = 0; c < nc; ++c) {
+        D[c & 1]->prepare(texts + cut[c], lens + cut[c], cut[c + 1] - cut[c]);
+        D[c & 1]->run();
+        if (c) collect(c - 1);
+      }
+      collect(nc - 1);
+    } catch (...) {
+      for (auto &d : outs) delete d;
+      outs.assign(n, nullptr);
+      throw;
+    }
+  }
 };
 
 namespace {
@@ -1571,10 +1633,8 @@ gpc_status gpc_compile_batch(gpc_driver *driver, const char *const *texts, const
   for (int32_t i = 0; i < n; ++i)
     if (!texts[i]) return fail(GPC_ERR_INVALID, "null circuit text in batch");
   return guarded([&] {
-    driver->prepare(texts, lens, (uint32_t)n);
-    driver->run();
     std::vector<gpc_dem *> v;
-    driver->fetch_all(v);
+    driver->compile_batch(texts, lens, (uint32_t)n, v);
     for (int32_t i = 0; i < n; ++i) outs[i] = v[i];
   });
 }

@@ -83,16 +83,24 @@ def dem_from_handle(h: ctypes.c_void_p) -> DetectorErrorModel:
     return DetectorErrorModel(probs, offsets, targets, nd.value, no.value, raw.value)
 
 
+class _View:
+    """Array-interface exporter of n elements at an address; it holds the gpc_dem's owner, so
+    the numpy array made from it (whose base it becomes) keeps the handle alive.  Cheaper than
+    a ctypes array type per array (a new type for every size)."""
+
+    __slots__ = ("__array_interface__", "owner")
+
+    def __init__(self, addr: int, n: int, typestr: str, owner):
+        self.__array_interface__ = {"data": (addr, True), "shape": (n,), "typestr": typestr, "version": 3}
+        self.owner = owner
+
+
 def _owned(ptr, n: int, dtype, owner) -> np.ndarray:
     """Read-only numpy view of n elements at ptr whose base keeps ``owner`` (the gpc_dem) alive."""
     if n == 0:
         return np.zeros(0, dtype=dtype)
-    size = n * np.dtype(dtype).itemsize
-    buf = (ctypes.c_char * size).from_address(ctypes.addressof(ptr.contents))
-    buf._owner = owner  # the ctypes buffer object carries the handle
-    a = np.frombuffer(buf, dtype=dtype, count=n)
-    a.flags.writeable = False
-    return a
+    addr = ctypes.cast(ptr, ctypes.c_void_p).value
+    return np.asarray(_View(addr, n, np.dtype(dtype).str, owner))
 
 
 class Driver:

@@ -81,7 +81,12 @@ gpc_status gpc_compile(gpc_driver *driver, const char *stim_text, size_t len, gp
  * class (classes run concurrently), keyed, bucketed and merged by single
  * launches over the whole batch (buckets are numbered circuit by circuit, so
  * each circuit's output is contiguous).  outs[i] receives circuit i's DEM.
- * Batches whose merge needs a fallback are compiled circuit by circuit. */
+ * Batches whose merge needs a fallback are compiled circuit by circuit.  A
+ * large batch (32 circuits and 8 MiB of text or more) runs as up to four
+ * chunks alternating between the driver and a second pipeline it owns, so
+ * one chunk's host work overlaps another's device work; the DEMs are the
+ * same, and the driver's device arrays (gpc_device_dem) then hold one chunk
+ * only -- gpc_prepare_batch + gpc_run_device give a whole batch's. */
 gpc_status gpc_compile_batch(gpc_driver *driver, const char *const *texts, const size_t *lens,
                              int32_t n, gpc_dem **outs);
 

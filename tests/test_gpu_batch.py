@@ -70,3 +70,19 @@ def test_time_varying_switched_batch_matches_oracle():
         ref = O.compile_text(text, 2)
         assert dem.num_detectors == ref.num_detectors
         compare_errors(dict(dem.errors()), dict(ref.errors()), rel=1e-12)
+
+
+def test_large_batch_in_chunks_matches_single_compiles():
+    """32 circuits with more than 8 MiB of text: compile_batch overlaps chunks on two pipelines;
+    every DEM equals the circuit's own compile, bit for bit."""
+    from greenpeas_gb300.workloads import batch_surface
+    circs = batch_surface()[:32]
+    assert sum(len(c) for c in circs) > 8 << 20
+    drv = gp.get_driver(circs[0])
+    out = drv.compile_batch(circs)
+    single = gp.get_driver(circs[0])
+    for text, dem in zip(circs, out):
+        assert dem == single.compile(text)
+    again = drv.compile_batch(circs[::-1])  # the pipelines are reused with other chunk sizes
+    for a, b in zip(again, out[::-1]):
+        assert a == b
