@@ -104,10 +104,21 @@ constexpr uint32_t kRec = 0x80000000u;
 constexpr uint32_t kPau = 0x40000000u;
 constexpr uint32_t kMaxQubit = 1u << 24;
 
+// ASCII character classes (the locale-aware <cctype> calls cost a call per byte).
+inline bool is_digit(char c) { return (unsigned)(c - '0') < 10u; }
+inline bool is_name_char(char c) {
+  return is_digit(c) || (unsigned)((c | 0x20) - 'a') < 26u || c == '_';
+}
+inline char to_upper(char c) { return (unsigned)(c - 'a') < 26u ? (char)(c - 32) : c; }
+
 struct TextParser {
   const char *s, *e;
   size_t line = 1;
   Parsed *out;
+  // the gate of the previous instruction line (consecutive lines repeat names, e.g. DETECTOR)
+  char last_name[40] = {0};
+  size_t last_len = 0;
+  int last_gate = -1;
 
   [[noreturn]] void fail(int code, const std::string &m) { throw Error(code, "line " + std::to_string(line) + ": " + m); }
   void sp() {
@@ -149,9 +160,9 @@ struct TextParser {
         return;
       }
       size_t n = 0;
-      while (s < e && (isalnum((unsigned char)*s) || *s == '_')) {
+      while (s < e && is_name_char(*s)) {
         if (n + 1 >= sizeof(name)) fail(GPC_ERR_PARSE, "instruction name too long");
-        name[n++] = (char)toupper((unsigned char)*s++);
+        name[n++] = to_upper(*s++);
       }
       name[n] = 0;
       if (n == 0) fail(GPC_ERR_PARSE, std::string("unexpected character '") + c + "'");
@@ -174,11 +185,20 @@ struct TextParser {
         for (uint32_t r = 0; r < reps; ++r) dst.insert(dst.end(), body.begin(), body.end());
         continue;
       }
-      auto it = gateIndex().find(nv);
-      if (it == gateIndex().end()) fail(GPC_ERR_UNSUPPORTED, "unsupported instruction " + std::string(nv));
-      const Gate &g = kGates[it->second];
+      int gi;
+      if (n == last_len && last_gate >= 0 && memcmp(name, last_name, n) == 0) {
+        gi = last_gate;
+      } else {
+        auto it = gateIndex().find(nv);
+        if (it == gateIndex().end()) fail(GPC_ERR_UNSUPPORTED, "unsupported instruction " + std::string(nv));
+        gi = it->second;
+        memcpy(last_name, name, n);
+        last_len = n;
+        last_gate = gi;
+      }
+      const Gate &g = kGates[gi];
       Instr in{};
-      in.gate = (uint16_t)it->second;
+      in.gate = (uint16_t)gi;
       double args[3];
       int na = 0;
       if (s < e && *s == '(') {
@@ -213,14 +233,13 @@ struct TextParser {
         while (s < e && (*s == ' ' || *s == '\t')) ++s;
         if (s >= e) break;
         const char c0 = *s;
-        if ((unsigned)(c0 - '0') < 10u) {  // fast path: a plain qubit index
-          uint32_t q = (uint32_t)(c0 - '0');
+        if (is_digit(c0)) {  // fast path: a plain qubit index
+          const char *d0 = s;
+          uint64_t q = (uint32_t)(c0 - '0');
           ++s;
-          while (s < e && (unsigned)(*s - '0') < 10u) {
-            q = q * 10u + (uint32_t)(*s++ - '0');
-            if (q >= kMaxQubit) fail(GPC_ERR_CAPACITY, "qubit index too large");
-          }
-          pool.push_back(q);
+          while (s < e && is_digit(*s)) q = q * 10u + (uint32_t)(*s++ - '0');
+          if (s - d0 > 9 || q >= kMaxQubit) fail(GPC_ERR_CAPACITY, "qubit index too large");
+          pool.push_back((uint32_t)q);
           continue;
         }
         if (c0 == '\n' || c0 == '#' || c0 == '\r') break;
@@ -236,7 +255,7 @@ struct TextParser {
           ++s;
           pool.push_back(kRec | k);
         } else if (*s == 'X' || *s == 'Y' || *s == 'Z' || *s == 'x' || *s == 'y' || *s == 'z') {
-          char p = (char)toupper((unsigned char)*s++);
+          char p = to_upper(*s++);
           uint32_t q = uint();
           if (q >= kMaxQubit) fail(GPC_ERR_CAPACITY, "qubit index too large");
           pool.push_back(kPau | ((uint32_t)(p == 'X' ? 1 : p == 'Z' ? 2 : 3) << 24) | q);
