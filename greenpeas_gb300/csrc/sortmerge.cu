@@ -119,6 +119,7 @@ __global__ void key_prep_kernel(KeyLaunch L) {
 // circuit finds its mechanisms' records in shared memory.
 __global__ void __launch_bounds__(KEY_THREADS) key_kernel(KeyLaunch L) {
   __shared__ uint32_t srm[KEY_THREADS + 1];  // rec_moff of the block's records
+  __shared__ uint8_t sown[KEY_THREADS];      // record (from r0) of each of the block's mechanisms
   const uint32_t tid = threadIdx.x, lane = tid & 31u;
   const uint32_t m0 = blockIdx.x * KEY_THREADS;
   const uint32_t mg = m0 + tid;
@@ -127,8 +128,17 @@ __global__ void __launch_bounds__(KEY_THREADS) key_kernel(KeyLaunch L) {
   const bool one = (info.y >> 31) == 0;
   // every record holds at least one mechanism, so the block's records are r0 .. r0 + KEY_THREADS - 1
   const uint32_t nr = one ? min(KEY_THREADS, L.circs[c0].R - r0) : 0;
-  if (one)
+  if (one) {
     for (uint32_t k = tid; k <= nr; k += KEY_THREADS) srm[k] = __ldg(L.circs[c0].rec_moff + r0 + k);
+    __syncthreads();
+    // each record marks its mechanisms inside the block (at most 15), so a
+    // mechanism finds its record with one shared load instead of a search
+    const uint32_t mb0 = m0 - __ldg(L.mbase + c0);  // the block's first mechanism within its circuit
+    for (uint32_t k = tid; k < nr; k += KEY_THREADS) {
+      const uint32_t a = max(srm[k], mb0), b = min(srm[k + 1], mb0 + KEY_THREADS);
+      for (uint32_t j = a; j < b; ++j) sown[j - mb0] = (uint8_t)k;
+    }
+  }
   __syncthreads();
   if (mg >= L.M) return;
 
@@ -137,13 +147,7 @@ __global__ void __launch_bounds__(KEY_THREADS) key_kernel(KeyLaunch L) {
   const uint32_t m = mg - __ldg(L.mbase + c);
   uint32_t r;
   if (one) {
-    uint32_t lo = 0, hi = nr;
-    while (hi - lo > 1) {
-      const uint32_t mid = (lo + hi) >> 1;
-      if (srm[mid] <= m) lo = mid;
-      else hi = mid;
-    }
-    r = r0 + lo;
+    r = r0 + sown[tid];
   } else {
     uint32_t lo = 0, hi = C.R;
     while (hi - lo > 1) {
