@@ -570,16 +570,18 @@ def main() -> None:
         "gpu_launches": KERNELS_PER_RUN * args.steps,
         "clocks": clocks.summary(),
     }
-    if not args.no_batch:
+    # the other forms and the CPU baseline are single-GPU measurements (a multi-GPU
+    # run reports the replicated headline only)
+    if not args.no_batch and world == 1:
         line["batch"] = batched_leg(gp, torch, local, flush, steps=max(3, min(args.steps, 10)),
                                     warmup=args.warmup, circuits=args.batch_circuits,
                                     device_only=args.batch_device_only)
-    if not args.no_grad:
+    if not args.no_grad and world == 1:
         line["grad"] = grad_leg(gp, torch)
-    if not args.no_serve:
+    if not args.no_serve and world == 1:
         line["serve"] = serving_leg(gp, args.serve_requests, max(200, args.serve_requests // 10), args.serve_slots,
                                     args.serve_batch, plain_sample=100)
-    if not args.no_cpu_baseline:
+    if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(text)
     print(json.dumps(line), flush=True)
     if dist is not None:
