@@ -288,17 +288,6 @@ bool pc1_independent(double px, double py, double pz, double q[3]) {
   return q[0] >= 0 && q[1] >= 0 && q[2] >= 0;
 }
 
-// Components of DEPOLARIZE2 kept at each correlation level (Mixer.hpp:13-20):
-// L0 drops every component with a Y or an X/Z mix; L1 adds IY, YI, XZ, ZX.
-bool dep2_kept(int level, int pa, int pb) {
-  if (level >= 2) return true;
-  bool y = pa == 3 || pb == 3;
-  bool mixXZ = (pa == 1 && pb == 2) || (pa == 2 && pb == 1);
-  if (level == 0) return !y && !mixXZ;
-  bool extra = (pa == 0 && pb == 3) || (pa == 3 && pb == 0) || mixXZ;
-  return (!y && !mixXZ) || extra;
-}
-
 // Swaps the qubit halves of a two-qubit mask (Xa,Za,Xb,Zb) -> (Xb,Zb,Xa,Za).
 uint32_t swap_halves(uint32_t m) { return ((m >> 2) & 3u) | ((m & 3u) << 2); }
 
