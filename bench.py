@@ -269,6 +269,7 @@ def batched_leg(gp, torch, local: int, flush, steps: int, warmup: int, circuits:
 
     bdrv = gp.get_driver(texts[0], device=local)
     bext = torch.cuda.ExternalStream(bdrv.stream, device=dev)
+    tuning = bdrv.autotune(texts, reps=2)  # walk configuration of this driver's batches (the DEMs do not depend on it)
     bdrv.prepare_batch(texts)
     for _ in range(warmup):
         bdrv.run_device()
@@ -324,6 +325,7 @@ def batched_leg(gp, torch, local: int, flush, steps: int, warmup: int, circuits:
                      "note": "walk bytes: each word's band of the tape (re-read from L2 across words) + snapshots"},
         "speedup_device": batch_rate / plain_rate,
         "speedup_e2e": plain_e2e_s / batch_e2e_s,
+        "tuning": tuning,
         "bit_exact_vs_plain": ok,
     }
 

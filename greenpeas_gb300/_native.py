@@ -28,7 +28,7 @@ EXPORTS = [
     "gpc_last_io_bytes", "gpc_merge_mechanisms_static", "gpc_prepare_batch", "gpc_fetch_batch",
     "gpc_param_prepare", "gpc_param_forward", "gpc_param_probs", "gpc_param_backward",
     "gpc_server_create", "gpc_server_submit", "gpc_server_wait", "gpc_server_stats", "gpc_server_destroy",
-    "gpc_device_dem",
+    "gpc_device_dem", "gpc_autotune",
 ]
 
 
@@ -50,6 +50,15 @@ class Options(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("sort_bits", ctypes.c_int32), ("global_sort", ctypes.c_int32),
                 ("walk_qpt", ctypes.c_int32), ("bucket_mean", ctypes.c_int32), ("walk_words", ctypes.c_int32),
                 ("reserved", ctypes.c_int32 * 2)]
+
+
+class TuningEntry(ctypes.Structure):
+    _fields_ = [("walk_words", ctypes.c_int32), ("walk_qpt", ctypes.c_int32), ("ms", ctypes.c_float)]
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [("walk_words", ctypes.c_int32), ("walk_qpt", ctypes.c_int32), ("ms", ctypes.c_float),
+                ("num_tried", ctypes.c_int32), ("tried", TuningEntry * 8)]
 
 
 class TapeView(ctypes.Structure):
@@ -106,6 +115,7 @@ def lib() -> ctypes.CDLL:
     L.gpc_merge_mechanisms_static.argtypes = [vp, vp, u32, vp, u32, vp, vp, vp, u32, vp, vp]
     L.gpc_prepare_batch.argtypes = [vp, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(sz), i32]
     L.gpc_fetch_batch.argtypes = [vp, ctypes.POINTER(vp), i32]
+    L.gpc_autotune.argtypes = [vp, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(sz), i32, i32, ctypes.POINTER(Tuning)]
     L.gpc_tape_lower.argtypes = [ctypes.c_char_p, sz, i32, ctypes.POINTER(vp)]
     L.gpc_tape_get_view.argtypes = [vp, ctypes.POINTER(TapeView)]
     L.gpc_tape_free.argtypes = [vp]

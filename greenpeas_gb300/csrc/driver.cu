@@ -20,6 +20,7 @@
 #include <thread>
 #include <cstdio>
 #include <cstring>
+#include <limits>
 #include <memory>
 #include <string>
 #include <vector>
@@ -118,7 +119,7 @@ struct CircLayout {
 
 // One walk launch: circuits with the same thread count.
 struct WalkClass {
-  uint32_t qpad, item0, n_items, chunk_cap, max_epochs, max_chunks, words;
+  uint32_t qpad, item0, n_items, chunk_cap, max_epochs, max_chunks, words, qpt;
 };
 
 // Byte offsets of every array inside the arena (inputs first, so the whole
@@ -199,14 +200,15 @@ struct gpc_driver {
   uint32_t walk_qpt = 0;      // qubits per walk thread (0: chosen per circuit)
   uint32_t walk_words = 0;    // detector words per walk CTA (0: two in batches, one for a single circuit)
   uint32_t bucket_mean = 0;   // target mechanisms per bucket (0: from the run's size; buckets are a power of two per circuit)
+  uint32_t batch_words = 0, batch_qpt = 0;  // walk configuration of batches chosen by autotune (0: defaults)
 
   static bool walk_qpt_fits(uint32_t qpad, uint32_t q) {
     const uint32_t mt = gpc::walk_max_threads(q);
     return mt && qpad % (32u * q) == 0 && qpad / q <= mt;
   }
-  // Qubits per walk thread for a tape of qpad qubit slots.
-  uint32_t walk_qpt_for(uint32_t qpad) const {
-    if (walk_qpt && walk_qpt_fits(qpad, walk_qpt)) return walk_qpt;
+  // Qubits per walk thread for a tape of qpad qubit slots (`pref` if it fits).
+  static uint32_t walk_qpt_for(uint32_t qpad, uint32_t pref) {
+    if (pref && walk_qpt_fits(qpad, pref)) return pref;
     return qpad <= 1024 ? 1u : qpad <= 2048 ? 2u : 4u;
   }
   // Serving: called by prepare() with the device bytes it must add to the
@@ -413,8 +415,9 @@ struct gpc_driver {
       // words per CTA: two in batches (half the CTAs; the walk is a chain of
       // latency-bound epochs) when the qubits-per-thread instance and shared
       // memory allow; one for a single circuit (latency)
-      const uint32_t want = walk_words ? walk_words : (N > 1 ? 2u : 1u);
-      const uint32_t q = walk_qpt_for(wc.qpad);
+      const uint32_t want = walk_words ? walk_words : (N > 1 ? (batch_words ? batch_words : 2u) : 1u);
+      const uint32_t q = walk_qpt_for(wc.qpad, walk_qpt ? walk_qpt : (N > 1 ? batch_qpt : 0u));
+      wc.qpt = q;
       if (want == 2 && (q == 1 || q == 2) &&
           gpc::walk_smem_bytes(wc.qpad, wc.chunk_cap, gpc::walk_table_bytes(wc.max_epochs, wc.max_chunks), 2) <=
               227 * 1024 - 1024)
@@ -620,6 +623,7 @@ struct gpc_driver {
       mix(c.max_epochs);
       mix(c.max_chunks);
       mix(c.words);
+      mix(c.qpt);
     }
     cfg_sig = h;
     prepared = true;
@@ -667,7 +671,7 @@ struct gpc_driver {
       wl.circs = dptr<CircuitDev>(L.cdev);
       wl.items = dptr<uint2>(L.items) + wc.item0;
       wl.n_items = wc.n_items;
-      wl.qpt = walk_qpt_for(wc.qpad);
+      wl.qpt = wc.qpt;
       wl.threads = wc.qpad / wl.qpt;
       wl.qpad = wc.qpad;
       wl.chunk_cap = wc.chunk_cap;
@@ -1185,6 +1189,48 @@ struct gpc_driver {
     return outs.empty() ? nullptr : outs[0];
   }
 
+  // Times the batched pipeline of these circuits in each walk configuration
+  // (words per CTA x qubits per thread) and keeps the fastest for batches.
+  void autotune(const char *const *texts, const size_t *lens, uint32_t n, uint32_t reps, gpc_tuning &out) {
+    static const uint32_t cand[][2] = {{2, 1}, {1, 1}, {2, 2}, {1, 2}, {1, 4}};
+    out = gpc_tuning{};
+    prepare(texts, lens, n);  // lowered once: each configuration lays out the same tapes again
+    float best = std::numeric_limits<float>::infinity();
+    uint32_t bw = batch_words, bq = batch_qpt;
+    try {
+      for (const auto &c : cand) {
+        batch_words = c[0];
+        batch_qpt = c[1];
+        prepare(nullptr, nullptr, 0);
+        run();  // first launches of this configuration
+        float t = std::numeric_limits<float>::infinity();
+        for (uint32_t r = 0; r < std::max(1u, reps); ++r) {
+          run();
+          CK(cudaEventSynchronize(ev[4]));
+          float ms = 0;
+          CK(cudaEventElapsedTime(&ms, ev[0], ev[4]));
+          t = std::min(t, ms);
+        }
+        if (out.num_tried < 8) out.tried[out.num_tried++] = gpc_tuning_entry{(int32_t)c[0], (int32_t)c[1], t};
+        if (t < best) {
+          best = t;
+          bw = c[0];
+          bq = c[1];
+        }
+      }
+    } catch (...) {
+      batch_words = 0;
+      batch_qpt = 0;
+      throw;
+    }
+    batch_words = bw;
+    batch_qpt = bq;
+    prepare(nullptr, nullptr, 0);
+    out.walk_words = (int32_t)bw;
+    out.walk_qpt = (int32_t)bq;
+    out.ms = best;
+  }
+
   // A second pipeline (own stream and buffers, same settings) for compile_batch.
   std::unique_ptr<gpc_driver> partner;
   gpc_driver &twin() {
@@ -1197,6 +1243,8 @@ struct gpc_driver {
       d->walk_qpt = walk_qpt;
       d->bucket_mean = bucket_mean;
       d->walk_words = walk_words;
+      d->batch_words = batch_words;
+      d->batch_qpt = batch_qpt;
       d->init_streams();
       partner = std::move(d);
     }
@@ -1636,6 +1684,20 @@ gpc_status gpc_compile_batch(gpc_driver *driver, const char *const *texts, const
     std::vector<gpc_dem *> v;
     driver->compile_batch(texts, lens, (uint32_t)n, v);
     for (int32_t i = 0; i < n; ++i) outs[i] = v[i];
+  });
+}
+
+gpc_status gpc_autotune(gpc_driver *driver, const char *const *texts, const size_t *lens, int32_t n, int32_t reps,
+                        gpc_tuning *out) {
+  if (!driver || !texts || !lens || !out || n < 2) return fail(GPC_ERR_INVALID, "autotune takes a batch of two or more circuits");
+  for (int32_t i = 0; i < n; ++i)
+    if (!texts[i]) return fail(GPC_ERR_INVALID, "null circuit text in batch");
+  return guarded([&] {
+    driver->autotune(texts, lens, (uint32_t)n, (uint32_t)std::max(1, reps), *out);
+    if (driver->partner) {  // the second pipeline of compile_batch follows the choice
+      driver->partner->batch_words = driver->batch_words;
+      driver->partner->batch_qpt = driver->batch_qpt;
+    }
   });
 }
 

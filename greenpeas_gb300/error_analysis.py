@@ -168,6 +168,18 @@ class Driver:
         _native.check(L.gpc_compile_batch(self._h, arr, lens, n, outs))
         return [dem_from_handle(ctypes.c_void_p(outs[i])) for i in range(n)]
 
+    def autotune(self, circuits, reps: int = 3) -> dict:
+        """Times the batched pipeline of ``circuits`` in each walk configuration (detector words per
+        walk CTA x qubits per walk thread) and keeps the fastest for this driver's batches; the DEMs
+        do not depend on it.  Returns the choice and every configuration's time (ms, best of reps)."""
+        n, arr, lens = self._batch_args(circuits)
+        t = _native.Tuning()
+        _native.check(_native.lib().gpc_autotune(self._h, arr, lens, n, int(reps), ctypes.byref(t)))
+        self._batch_n = n
+        tried = [{"walk_words": e.walk_words, "walk_qpt": e.walk_qpt, "ms": float(e.ms)}
+                 for e in t.tried[:t.num_tried]]
+        return {"walk_words": t.walk_words, "walk_qpt": t.walk_qpt, "ms": float(t.ms), "tried": tried}
+
     def prepare_batch(self, circuits) -> None:
         n, arr, lens = self._batch_args(circuits)
         self._batch_n = n

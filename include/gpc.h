@@ -90,6 +90,29 @@ gpc_status gpc_compile(gpc_driver *driver, const char *stim_text, size_t len, gp
 gpc_status gpc_compile_batch(gpc_driver *driver, const char *const *texts, const size_t *lens,
                              int32_t n, gpc_dem **outs);
 
+/* ---- autotuning (batched form) ------------------------------------------
+ * Times the batched pipeline of circuits texts[0..n) (n >= 2) under each walk
+ * configuration the kernels offer -- detector words per walk CTA (1, 2) x
+ * qubits per walk thread (1, 2, 4; a choice that does not fit a circuit's
+ * slot count falls back to the default for that circuit) -- best of `reps`
+ * runs each by CUDA events on the driver's stream, and keeps the fastest for
+ * the driver's later batches (single circuits keep their defaults; explicit
+ * walk_words / walk_qpt options take precedence).  The DEMs do not depend on
+ * the choice.  On return the circuits are prepared in the chosen
+ * configuration (gpc_run_device runs them). */
+typedef struct gpc_tuning_entry {
+  int32_t walk_words, walk_qpt;
+  float ms; /* pipeline time, best of the repetitions */
+} gpc_tuning_entry;
+typedef struct gpc_tuning {
+  int32_t walk_words, walk_qpt; /* the chosen configuration */
+  float ms;
+  int32_t num_tried;
+  gpc_tuning_entry tried[8];
+} gpc_tuning;
+gpc_status gpc_autotune(gpc_driver *driver, const char *const *texts, const size_t *lens, int32_t n,
+                        int32_t reps, gpc_tuning *out);
+
 /* Merged mechanisms as CSR arrays owned by the DEM: error i has targets
  * targets[offsets[i] .. offsets[i+1]) (ascending) and probability probs[i]. */
 gpc_status gpc_dem_arrays(const gpc_dem *dem, const uint32_t **offsets, const uint32_t **targets,

@@ -86,3 +86,17 @@ def test_large_batch_in_chunks_matches_single_compiles():
     again = drv.compile_batch(circs[::-1])  # the pipelines are reused with other chunk sizes
     for a, b in zip(again, out[::-1]):
         assert a == b
+
+
+def test_autotune_keeps_results_and_picks_a_configuration():
+    """The autotuner times each walk configuration on the batch and keeps the fastest; the DEMs
+    before and after are identical, and the prepared batch runs in the chosen configuration."""
+    circs = _mixed()
+    drv = gp.get_driver(circs[0])
+    before = drv.compile_batch(circs)
+    tune = drv.autotune(circs, reps=2)
+    assert (tune["walk_words"], tune["walk_qpt"]) in {(t["walk_words"], t["walk_qpt"]) for t in tune["tried"]}
+    assert len(tune["tried"]) == 5 and tune["ms"] == min(t["ms"] for t in tune["tried"])
+    drv.run_device()
+    assert [a == b for a, b in zip(drv.fetch_batch(), before)] == [True] * len(circs)
+    assert [a == b for a, b in zip(drv.compile_batch(circs), before)] == [True] * len(circs)
