@@ -124,12 +124,20 @@ struct KeyLaunch {
   uint32_t *list_total;     // += targets written to the lists (for traffic accounting)
   uint32_t *err;
   uint32_t write_all;       // also write key[], and descriptors/probabilities (global path, gradients)
+  // One circuit whose key pass is split (kNoSplit: one pass over every word):
+  // key_kernel covers the words below late_word and leaves each mechanism's
+  // descriptor, probability, targets and partial key; key_late_kernel adds
+  // the words from late_word on (the observables', whose walk is the longest)
+  // and files the mechanism in its bucket.
+  uint32_t late_word;
 };
+constexpr uint32_t kNoSplit = 0xFFFFFFFFu;
 constexpr uint32_t KEY_THREADS = 256;
 inline uint32_t key_blocks(uint32_t M) { return (M + KEY_THREADS - 1) / KEY_THREADS; }
 // Finds each key block's first record (one thread per block).
 cudaError_t launch_key_prep(const KeyLaunch &L, cudaStream_t s);
 cudaError_t launch_keys(const KeyLaunch &L, cudaStream_t s);
+cudaError_t launch_keys_late(const KeyLaunch &L, cudaStream_t s);  // second pass of a split key pass
 
 // Exclusive scan of the bucket counts into bucket offsets (+ total at [nb]).
 cudaError_t launch_bucket_scan(const uint32_t *count, uint32_t *offset, uint32_t nb, cudaStream_t s);

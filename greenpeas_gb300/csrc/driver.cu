@@ -625,6 +625,7 @@ struct gpc_driver {
       mix(c.words);
       mix(c.qpt);
     }
+    mix(split_word());
     cfg_sig = h;
     prepared = true;
   }
@@ -664,23 +665,25 @@ struct gpc_driver {
 
   // The walks (one launch per class; several classes run on the auxiliary
   // streams), and meanwhile the key-block table on the main stream.
+  void walk_one(const WalkClass &wc, cudaStream_t s) {
+    gpc::WalkLaunch wl{};
+    wl.circs = dptr<CircuitDev>(L.cdev);
+    wl.items = dptr<uint2>(L.items) + wc.item0;
+    wl.n_items = wc.n_items;
+    wl.qpt = wc.qpt;
+    wl.threads = wc.qpad / wl.qpt;
+    wl.qpad = wc.qpad;
+    wl.chunk_cap = wc.chunk_cap;
+    wl.max_epochs = wc.max_epochs;
+    wl.max_chunks = wc.max_chunks;
+    wl.words = wc.words;
+    wl.err = dptr<uint32_t>(L.err);
+    CK(gpc::launch_walk(wl, s));
+  }
+
   void launch_walks(const gpc::KeyLaunch &kl) {
     const uint32_t nc = (uint32_t)L.classes.size();
-    auto one = [&](const WalkClass &wc, cudaStream_t s) {
-      gpc::WalkLaunch wl{};
-      wl.circs = dptr<CircuitDev>(L.cdev);
-      wl.items = dptr<uint2>(L.items) + wc.item0;
-      wl.n_items = wc.n_items;
-      wl.qpt = wc.qpt;
-      wl.threads = wc.qpad / wl.qpt;
-      wl.qpad = wc.qpad;
-      wl.chunk_cap = wc.chunk_cap;
-      wl.max_epochs = wc.max_epochs;
-      wl.max_chunks = wc.max_chunks;
-      wl.words = wc.words;
-      wl.err = dptr<uint32_t>(L.err);
-      CK(gpc::launch_walk(wl, s));
-    };
+    auto one = [&](const WalkClass &wc, cudaStream_t s) { walk_one(wc, s); };
     if (nc <= 1) {
       // the key-block table on an auxiliary stream beside the walk
       CK(cudaEventRecord(fork_ev, stream));
@@ -703,6 +706,41 @@ struct gpc_driver {
     }
   }
 
+  // First word of a split key pass, or kNoSplit.  One circuit with target
+  // lists whose observables sit in words after some detector-only words: the
+  // observables never vanish, so their walk covers every epoch, while the
+  // detector words stop early; their keys are computed beside that walk.
+  uint32_t split_word() const {
+    if (ncirc() != 1 || force_global || lists_off || tcap == 0 || L.classes.size() != 1) return gpc::kNoSplit;
+    const Tape &T = tapes[0];
+    if (T.nobs == 0 || T.n_epochs == 0) return gpc::kNoSplit;
+    const uint32_t W = std::max(1u, L.classes[0].words);
+    const uint32_t late = T.ndet / 64u / W * W;  // whole walk items before the first observable's word
+    return late >= 1 && late < T.w ? late : gpc::kNoSplit;
+  }
+
+  // The walks of a split key pass: the detector words on the main stream, the
+  // late words (from `late`) and the key-block table on auxiliary streams; the
+  // end of the late walk is timing event 1 and join_ev[1].
+  void launch_walks_split(const gpc::KeyLaunch &kl, uint32_t late) {
+    const WalkClass &wc = L.classes[0];
+    WalkClass a = wc, b = wc;
+    a.n_items = late / std::max(1u, wc.words);
+    b.item0 = wc.item0 + a.n_items;
+    b.n_items = wc.n_items - a.n_items;
+    CK(cudaEventRecord(fork_ev, stream));
+    CK(cudaStreamWaitEvent(aux[0], fork_ev, 0));
+    CK(cudaStreamWaitEvent(aux[1], fork_ev, 0));
+    CK(gpc::launch_key_prep(kl, aux[0]));
+    CK(cudaEventRecord(join_ev[0], aux[0]));
+    walk_one(b, aux[1]);
+    if (capturing) CK(cudaEventRecordWithFlags(ev[1], aux[1], cudaEventRecordExternal));
+    else CK(cudaEventRecord(ev[1], aux[1]));
+    CK(cudaEventRecord(join_ev[1], aux[1]));
+    walk_one(a, stream);
+    CK(cudaStreamWaitEvent(stream, join_ev[0], 0));
+  }
+
   gpc::KeyLaunch key_launch(bool write_all) {
     gpc::KeyLaunch kl{};
     kl.circs = dptr<CircuitDev>(L.cdev);
@@ -717,6 +755,7 @@ struct gpc_driver {
     kl.list_total = dptr<uint32_t>(L.totals) + 2;
     kl.err = dptr<uint32_t>(L.err);
     kl.write_all = write_all ? 1u : 0u;
+    kl.late_word = gpc::kNoSplit;
     return kl;
   }
 
@@ -724,11 +763,20 @@ struct gpc_driver {
     CK(cudaMemsetAsync(dptr<char>(L.zero), 0, L.zero_bytes, stream));
     for (uint32_t i = 0; i < ncirc(); ++i)
       if (tapes[i].n_epochs == 0) CK(cudaMemsetAsync(dptr<char>(L.c[i].band), 0, (size_t)tapes[i].w * 8, stream));
-    const gpc::KeyLaunch kl = key_launch(param || (ncirc() == 1 && (force_global || lists_off)));
+    gpc::KeyLaunch kl = key_launch(param || (ncirc() == 1 && (force_global || lists_off)));
+    const uint32_t late = split_word();
     rec(0);
-    launch_walks(kl);
-    rec(1);
-    CK(gpc::launch_keys(kl, stream));
+    if (late == gpc::kNoSplit) {
+      launch_walks(kl);
+      rec(1);
+      CK(gpc::launch_keys(kl, stream));
+    } else {
+      launch_walks_split(kl, late);
+      kl.late_word = late;
+      CK(gpc::launch_keys(kl, stream));  // the detector words, beside the late walk
+      CK(cudaStreamWaitEvent(stream, join_ev[1], 0));
+      CK(gpc::launch_keys_late(kl, stream));
+    }
     rec(2);
     if (ncirc() == 1 && (force_global || lists_off)) {
       run_global(false);

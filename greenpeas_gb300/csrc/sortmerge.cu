@@ -170,7 +170,8 @@ __global__ void __launch_bounds__(KEY_THREADS) key_kernel(KeyLaunch L) {
   }
   if (Pb == 0) pb = 0;
   const double prob = __ldg(C.rec_p + r);
-  if (L.write_all) {  // descriptors and probabilities: global merge path, gradients
+  const bool split = L.late_word != kNoSplit;
+  if (L.write_all || split) {  // descriptors and probabilities: global merge path, gradients, second pass
     C.mdesc[m] = mk_desc(pa, Pa, pb, Pb);
     C.mp[m] = prob;
   }
@@ -201,10 +202,12 @@ __global__ void __launch_bounds__(KEY_THREADS) key_kernel(KeyLaunch L) {
   const ulonglong2 *snap = C.snap;
   const uint32_t np = C.npoints, mw = C.mw;
   const unsigned long long *ma = C.nzm + (size_t)pa * mw, *mb = C.nzm + (size_t)pb * mw;
-  for (uint32_t i = 0; i < mw; ++i) {
+  const uint32_t jend = split ? L.late_word : mw * 64u;  // words of this pass: j < jend
+  for (uint32_t i = 0; i < mw && i * 64u < jend; ++i) {
     // a point's snapshot of word j exists only where its own bit is set
     const uint64_t ba = __ldg(ma + i), bb = Pb ? __ldg(mb + i) : 0ull;
     uint64_t bits = ba | bb;
+    if (jend - i * 64u < 64u) bits &= (1ull << (jend - i * 64u)) - 1ull;
     while (bits) {
       const uint32_t bit = (uint32_t)(__ffsll((long long)bits) - 1);
       const uint32_t j = i * 64u + bit;
@@ -229,7 +232,7 @@ __global__ void __launch_bounds__(KEY_THREADS) key_kernel(KeyLaunch L) {
     }
   }
   const ulonglong2 key = make_ulonglong2(hx, hy);
-  if (L.write_all) L.key[mg] = key;
+  if (L.write_all || split) L.key[mg] = key;  // a split pass leaves the partial key
   if (tcap) {
     // rows are 16-byte aligned (tcap is a multiple of 4, at least 32)
     if (cnt) reinterpret_cast<uint4 *>(out)[0] = make_uint4(t0, t1, t2, t3);
@@ -240,6 +243,7 @@ __global__ void __launch_bounds__(KEY_THREADS) key_kernel(KeyLaunch L) {
     const uint32_t tot = __reduce_add_sync(am, cnt);
     if (lane == (uint32_t)(__ffs(am) - 1) && tot) red_add(L.list_total, tot);
   }
+  if (split) return;  // filed in its bucket by the second pass
   if ((hx | hy) == 0) {
     if (cnt || (!tcap && nonzero)) atomicOr(L.err, DEV_ERR_COLLISION);  // a non-empty symptom hashed to 0
   } else {
@@ -249,6 +253,70 @@ __global__ void __launch_bounds__(KEY_THREADS) key_kernel(KeyLaunch L) {
       const size_t pos = (size_t)b * SLOT_CAP + slot;
       L.skey[pos] = key;
       L.stail[pos] = SlotTail{mg, cnt, prob};
+    } else {
+      atomicOr(L.err, DEV_FLAG_BIG_BUCKET);
+    }
+  }
+}
+
+// Second pass of a split key pass (one circuit, target lists on): adds the
+// words from late_word on to each mechanism's partial key, appends their
+// targets after the first pass's (they are the larger indices, so the list
+// stays ascending), and files the mechanism in its bucket.
+__global__ void __launch_bounds__(KEY_THREADS) key_late_kernel(KeyLaunch L) {
+  const uint32_t lane = threadIdx.x & 31u;
+  const uint32_t m = blockIdx.x * KEY_THREADS + threadIdx.x;
+  if (m >= L.M) return;
+  const CircuitDev &C = L.circs[0];
+  const uint64_t d = C.mdesc[m];
+  const uint32_t pa = (uint32_t)(d & 0x3FFFFFFFu), Pa = (uint32_t)((d >> 30) & 3u);
+  const uint32_t pb = (uint32_t)((d >> 32) & 0x3FFFFFFFu), Pb = (uint32_t)(d >> 62);
+  const double prob = C.mp[m];
+  ulonglong2 key = L.key[m];
+  const uint32_t tcap = C.tcap;
+  uint32_t *out = C.tl + (size_t)m * tcap;
+  const uint32_t cnt1 = C.tn[m];
+  uint32_t cnt = cnt1;
+  const ulonglong2 *snap = C.snap;
+  const uint32_t np = C.npoints, mw = C.mw, jbeg = L.late_word;
+  const unsigned long long *ma = C.nzm + (size_t)pa * mw, *mb = C.nzm + (size_t)pb * mw;
+  for (uint32_t i = jbeg / 64u; i < mw; ++i) {
+    const uint64_t ba = __ldg(ma + i), bb = Pb ? __ldg(mb + i) : 0ull;
+    uint64_t bits = ba | bb;
+    if (jbeg > i * 64u) bits &= ~((1ull << (jbeg - i * 64u)) - 1ull);
+    while (bits) {
+      const uint32_t bit = (uint32_t)(__ffsll((long long)bits) - 1);
+      const uint32_t j = i * 64u + bit;
+      bits &= bits - 1;
+      const ulonglong2 *sj = snap + (size_t)j * np;
+      uint64_t v = 0;
+      if ((ba >> bit) & 1ull) v = pauli_sel(sj[pa], Pa);
+      if ((bb >> bit) & 1ull) v ^= pauli_sel(sj[pb], Pb);
+      if (!v) continue;
+      const ulonglong2 h = word_hash(j, v);
+      key.x ^= h.x;
+      key.y ^= h.y;
+      for (uint64_t x = v; x; x &= x - 1) {
+        if (cnt < tcap) out[cnt] = j * 64u + (uint32_t)(__ffsll((long long)x) - 1);
+        ++cnt;
+      }
+    }
+  }
+  if (L.write_all) L.key[m] = key;
+  if (cnt != cnt1) C.tn[m] = cnt;
+  if (cnt > tcap) atomicOr(L.err, DEV_FLAG_LONG);
+  const uint32_t am = __activemask();
+  const uint32_t tot = __reduce_add_sync(am, cnt - cnt1);
+  if (lane == (uint32_t)(__ffs(am) - 1) && tot) red_add(L.list_total, tot);
+  if ((key.x | key.y) == 0) {
+    if (cnt) atomicOr(L.err, DEV_ERR_COLLISION);  // a non-empty symptom hashed to 0
+  } else {
+    const uint32_t b = C.bbase + (uint32_t)(key.x >> (64u - C.bbits));
+    const uint32_t slot = atomicAdd(L.bucket_count + b, 1u);
+    if (slot < SLOT_CAP) {
+      const size_t pos = (size_t)b * SLOT_CAP + slot;
+      L.skey[pos] = key;
+      L.stail[pos] = SlotTail{m, cnt, prob};
     } else {
       atomicOr(L.err, DEV_FLAG_BIG_BUCKET);
     }
@@ -1309,6 +1377,13 @@ cudaError_t launch_key_prep(const KeyLaunch &L, cudaStream_t s) {
 cudaError_t launch_keys(const KeyLaunch &L, cudaStream_t s) {
   if (L.M == 0) return cudaSuccess;
   key_kernel<<<key_blocks(L.M), KEY_THREADS, 0, s>>>(L);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_keys_late(const KeyLaunch &L, cudaStream_t s) {
+  if (L.M == 0) return cudaSuccess;
+  if (L.late_word == kNoSplit || L.n_circ != 1) return cudaErrorInvalidValue;
+  key_late_kernel<<<key_blocks(L.M), KEY_THREADS, 0, s>>>(L);
   return cudaGetLastError();
 }
 
