@@ -49,7 +49,7 @@ class ServerOptions(ctypes.Structure):
 class Options(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("sort_bits", ctypes.c_int32), ("global_sort", ctypes.c_int32),
                 ("walk_qpt", ctypes.c_int32), ("bucket_mean", ctypes.c_int32), ("walk_words", ctypes.c_int32),
-                ("reserved", ctypes.c_int32 * 2)]
+                ("key_split", ctypes.c_int32), ("reserved", ctypes.c_int32 * 1)]
 
 
 class TuningEntry(ctypes.Structure):

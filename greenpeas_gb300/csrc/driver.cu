@@ -201,6 +201,7 @@ struct gpc_driver {
   uint32_t walk_words = 0;    // detector words per walk CTA (0: two in batches, one for a single circuit)
   uint32_t bucket_mean = 0;   // target mechanisms per bucket (0: from the run's size; buckets are a power of two per circuit)
   uint32_t batch_words = 0, batch_qpt = 0;  // walk configuration of batches chosen by autotune (0: defaults)
+  bool key_split = true;                     // split key pass for one circuit when it pays (option key_split)
 
   static bool walk_qpt_fits(uint32_t qpad, uint32_t q) {
     const uint32_t mt = gpc::walk_max_threads(q);
@@ -239,6 +240,7 @@ struct gpc_driver {
   uint32_t tcap = 32;      // target-list stride (grows when a symptom is longer)
   bool lists_off = false;  // symptoms too long for target lists: merge from snapshots
   uint64_t last_d2h = 0;   // bytes copied device -> host by the last fetch
+  uint64_t last_h2d = 0;   // bytes copied host -> device by the last prepare (a chunked batch: all of its chunks)
   bool used_global = false;
   bool capturing = false;
   uint32_t ncirc() const { return (uint32_t)tapes.size(); }
@@ -602,6 +604,7 @@ struct gpc_driver {
     }
     stage_inputs();
     CK(cudaMemcpyAsync(arena.p, pin_in.p, L.in_bytes, cudaMemcpyHostToDevice, stream));
+    last_h2d = L.in_bytes;
     // what a captured graph depends on: buffer addresses and launch sizes
     uint64_t h = 0xcbf29ce484222325ull;
     auto mix = [&](uint64_t v) { h = (h ^ v) * 0x100000001b3ull; };
@@ -711,12 +714,16 @@ struct gpc_driver {
   // observables never vanish, so their walk covers every epoch, while the
   // detector words stop early; their keys are computed beside that walk.
   uint32_t split_word() const {
-    if (ncirc() != 1 || force_global || lists_off || tcap == 0 || L.classes.size() != 1) return gpc::kNoSplit;
+    if (!key_split || ncirc() != 1 || force_global || lists_off || tcap == 0 || L.classes.size() != 1)
+      return gpc::kNoSplit;
     const Tape &T = tapes[0];
     if (T.nobs == 0 || T.n_epochs == 0) return gpc::kNoSplit;
     const uint32_t W = std::max(1u, L.classes[0].words);
     const uint32_t late = T.ndet / 64u / W * W;  // whole walk items before the first observable's word
-    return late >= 1 && late < T.w ? late : gpc::kNoSplit;
+    // worth a second launch only when the detector words' keys are a real
+    // kernel and the observables' walk is long (measured: a loss for d = 5-9
+    // surface circuits, a gain for [[144,12,12]] with 27 detector words)
+    return late >= 8 && late < T.w && T.n_epochs >= 64 ? late : gpc::kNoSplit;
   }
 
   // The walks of a split key pass: the detector words on the main stream, the
@@ -1291,6 +1298,7 @@ struct gpc_driver {
       d->walk_qpt = walk_qpt;
       d->bucket_mean = bucket_mean;
       d->walk_words = walk_words;
+      d->key_split = key_split;
       d->batch_words = batch_words;
       d->batch_qpt = batch_qpt;
       d->init_streams();
@@ -1324,18 +1332,23 @@ struct gpc_driver {
     const uint32_t nc = (uint32_t)cut.size() - 1;
     gpc_driver *D[2] = {this, &twin()};
     outs.assign(n, nullptr);
+    uint64_t h2d = 0, d2h = 0;
     auto collect = [&](uint32_t c) {
       std::vector<gpc_dem *> v;
       D[c & 1]->fetch_all(v);
+      d2h += D[c & 1]->last_d2h;
       for (uint32_t i = 0; i < (uint32_t)v.size(); ++i) outs[cut[c] + i] = v[i];
     };
     try {
       for (uint32_t c = 0; c < nc; ++c) {
         D[c & 1]->prepare(texts + cut[c], lens + cut[c], cut[c + 1] - cut[c]);
+        h2d += D[c & 1]->last_h2d;
         D[c & 1]->run();
         if (c) collect(c - 1);
       }
       collect(nc - 1);
+      last_h2d = h2d;
+      last_d2h = d2h;
     } catch (...) {
       for (auto &d : outs) delete d;
       outs.assign(n, nullptr);
@@ -1626,6 +1639,8 @@ gpc_status gpc_get_driver(const char *stim_text, size_t len, int32_t correlation
     d->bucket_mean = (uint32_t)options->bucket_mean;
     if (options->walk_words < 0 || options->walk_words > 2) return fail(GPC_ERR_INVALID, "walk_words must be 0, 1 or 2");
     d->walk_words = (uint32_t)options->walk_words;
+    if (options->key_split != 0 && options->key_split != -1) return fail(GPC_ERR_INVALID, "key_split must be 0 or -1");
+    d->key_split = options->key_split == 0;
   }
   gpc_status st = guarded([&] {
     int n = 0;
@@ -1913,7 +1928,7 @@ gpc_status gpc_last_traffic(gpc_driver *driver, double *bytes4) {
 
 gpc_status gpc_last_io_bytes(gpc_driver *driver, uint64_t *h2d, uint64_t *d2h) {
   if (!driver) return fail(GPC_ERR_INVALID, "driver is null");
-  if (h2d) *h2d = driver->L.in_bytes;
+  if (h2d) *h2d = driver->last_h2d;
   if (d2h) *d2h = driver->last_d2h;
   return GPC_OK;
 }

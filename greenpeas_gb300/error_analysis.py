@@ -108,7 +108,7 @@ class Driver:
 
     def __init__(self, circuit, correlation_level: CorrelationLevel = CorrelationLevel.L2, *,
                  device: int = 0, sort_bits: int = 0, global_sort: bool = False, walk_qpt: int = 0,
-                 bucket_mean: int = 0, walk_words: int = 0):
+                 bucket_mean: int = 0, walk_words: int = 0, key_split: int = 0):
         L = _native.lib()
         self._h = ctypes.c_void_p()
         self.correlation_level = CorrelationLevel(correlation_level)
@@ -120,6 +120,7 @@ class Driver:
         opts.walk_qpt = walk_qpt
         opts.bucket_mean = bucket_mean
         opts.walk_words = walk_words
+        opts.key_split = key_split
         text = _text(circuit)
         _native.check(L.gpc_get_driver(text, len(text), int(self.correlation_level), ctypes.byref(opts),
                                        ctypes.byref(self._h)))

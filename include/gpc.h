@@ -63,7 +63,8 @@ typedef struct gpc_options {
   int32_t walk_qpt;    /* qubits per thread of the walk (1,2,3,4,6,8,12,16; 0 = chosen per circuit) */
   int32_t bucket_mean; /* target mechanisms per merge bucket (8..128; 0 = default) */
   int32_t walk_words;  /* detector words per walk CTA (1, 2; 0 = two in batches, one for a single circuit) */
-  int32_t reserved[2];
+  int32_t key_split;   /* one circuit: key the detector words beside the observables' walk (0 = when it pays, -1 = never) */
+  int32_t reserved[1];
 } gpc_options;
 
 /* Parses `stim_text` (length `len`), sizes device buffers for it and returns
