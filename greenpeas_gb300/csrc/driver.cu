@@ -164,8 +164,9 @@ struct gpc_driver {
   std::vector<Tape> tapes;
   std::vector<gpc::LowerScratch> lower_scratch;  // host memory of parse + lower, one per pool slot
   std::unique_ptr<gpc::HostPool> pool;            // host threads of this driver (made on first use)
+  uint32_t pool_threads = 0;  // threads of the host pool, the caller included (0: every host thread)
   gpc::HostPool &host_pool() {
-    if (!pool) pool.reset(new gpc::HostPool(host_threads() - 1));
+    if (!pool) pool.reset(new gpc::HostPool((pool_threads ? pool_threads : host_threads()) - 1));
     return *pool;
   }
   // Circuit indices by decreasing size (the order batch work is handed out in).
@@ -1838,16 +1839,21 @@ gpc_status gpc_server_create(const gpc_server_options *options, gpc_server **out
     CK(gpc::walk_set_smem_limit());
     sv->held.assign(o.slots, 0);
     gpc_server *raw = sv.get();
+    // host threads: one core per GPU worker, the rest lowering requests (more
+    // threads than cores measured 27% less capacity); a worker's own pool for
+    // staging and splitting its batches gets its share of the cores
+    const uint32_t hw = host_threads();
     for (uint32_t w = 0; w < o.slots; ++w) {
       std::unique_ptr<gpc_driver> d(new gpc_driver());
       d->device = sv->device;
       d->level = sv->level;
+      d->pool_threads = std::max(1u, hw / o.slots);
       d->init_streams();
       d->admit = [raw, w](size_t grow, size_t total) { raw->acquire(w, grow, total); };
       sv->drivers.push_back(std::move(d));
     }
     for (uint32_t w = 0; w < o.slots; ++w) sv->workers.emplace_back([raw, w] { raw->worker(w); });
-    const uint32_t nl = o.lower_threads ? o.lower_threads : std::max(1u, std::thread::hardware_concurrency());
+    const uint32_t nl = o.lower_threads ? o.lower_threads : std::max(1u, hw > o.slots ? hw - o.slots : 1u);
     for (uint32_t i = 0; i < nl; ++i) sv->lowerers.emplace_back([raw] { raw->lowerer(); });
   });
   if (st != GPC_OK) return st;
