@@ -49,16 +49,17 @@ class ServerOptions(ctypes.Structure):
 class Options(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("sort_bits", ctypes.c_int32), ("global_sort", ctypes.c_int32),
                 ("walk_qpt", ctypes.c_int32), ("bucket_mean", ctypes.c_int32), ("walk_words", ctypes.c_int32),
-                ("key_split", ctypes.c_int32), ("reserved", ctypes.c_int32 * 1)]
+                ("key_split", ctypes.c_int32), ("walk_queue", ctypes.c_int32)]
 
 
 class TuningEntry(ctypes.Structure):
-    _fields_ = [("walk_words", ctypes.c_int32), ("walk_qpt", ctypes.c_int32), ("ms", ctypes.c_float)]
+    _fields_ = [("walk_words", ctypes.c_int32), ("walk_qpt", ctypes.c_int32), ("walk_queue", ctypes.c_int32),
+                ("ms", ctypes.c_float)]
 
 
 class Tuning(ctypes.Structure):
-    _fields_ = [("walk_words", ctypes.c_int32), ("walk_qpt", ctypes.c_int32), ("ms", ctypes.c_float),
-                ("num_tried", ctypes.c_int32), ("tried", TuningEntry * 8)]
+    _fields_ = [("walk_words", ctypes.c_int32), ("walk_qpt", ctypes.c_int32), ("walk_queue", ctypes.c_int32),
+                ("ms", ctypes.c_float), ("num_tried", ctypes.c_int32), ("tried", TuningEntry * 12)]
 
 
 class TapeView(ctypes.Structure):

@@ -91,6 +91,10 @@ struct WalkLaunch {
   uint32_t max_epochs, max_chunks;  // largest tables of the launch (staged in shared memory if they fit)
   uint32_t words;           // detector words per CTA (1, or 2 with 1 or 2 qubits per thread)
   uint32_t *err;
+  // Persistent launch (null: one CTA per item): a zeroed counter from which
+  // resident CTAs take items until none are left.  Circuits of any slot count
+  // up to qpad share the launch; the items should come longest first.
+  uint32_t *queue;
 };
 cudaError_t launch_walk(const WalkLaunch &L, cudaStream_t s);
 cudaError_t walk_set_smem_limit();  // call once per device before launching walks
@@ -98,6 +102,7 @@ cudaError_t walk_set_smem_limit();  // call once per device before launching wal
 uint32_t walk_table_bytes(uint32_t max_epochs, uint32_t max_chunks);
 size_t walk_smem_bytes(uint32_t qpad, uint32_t chunk_cap, uint32_t table_bytes, uint32_t words);
 uint32_t walk_max_threads(uint32_t qpt);  // 0: no walk instance for this many qubits per thread
+bool walk_queue_supported(uint32_t qpt, uint32_t words);  // a persistent walk instance exists
 
 // Key kernel: one thread per noise record; expands the record into its
 // mechanisms (mdesc, mp), computes each mechanism's 128-bit key, and counts

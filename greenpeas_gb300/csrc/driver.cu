@@ -117,9 +117,10 @@ struct CircLayout {
   uint32_t mbase, bbase, bbits;
 };
 
-// One walk launch: circuits with the same thread count.
+// One walk launch: circuits with the same thread count, or (queue) every
+// circuit of a batch in one persistent launch sized for the largest.
 struct WalkClass {
-  uint32_t qpad, item0, n_items, chunk_cap, max_epochs, max_chunks, words, qpt;
+  uint32_t qpad, item0, n_items, chunk_cap, max_epochs, max_chunks, words, qpt, queue;
 };
 
 // Byte offsets of every array inside the arena (inputs first, so the whole
@@ -129,7 +130,7 @@ struct Layout {
   size_t cdev, items, mbase, cbbase;
   size_t in_bytes;
   size_t mdesc, mp, tl, tn, key, blk_r0, skey, stail, bagg, bout, cout, big_list;
-  size_t zero, err, totals, bcount, tsum, big_n, zero_bytes;
+  size_t zero, err, totals, bcount, tsum, big_n, wq, zero_bytes;
   size_t sk0, sk1, pm0, pm1, hik;  // global path (single circuit)
   size_t src_off, src_rec, gq, grad_rec, ptab;  // noise-rate gradients (single circuit)
   size_t gzero, sort_scr, merge_status, merge_ctr, gzero_bytes;
@@ -202,6 +203,8 @@ struct gpc_driver {
   uint32_t walk_words = 0;    // detector words per walk CTA (0: two in batches, one for a single circuit)
   uint32_t bucket_mean = 0;   // target mechanisms per bucket (0: from the run's size; buckets are a power of two per circuit)
   uint32_t batch_words = 0, batch_qpt = 0;  // walk configuration of batches chosen by autotune (0: defaults)
+  uint32_t batch_queue = 0;                  // 1: batches walk in one persistent launch (autotune's choice)
+  int walk_queue = 0;                        // option walk_queue: 1 always, -1 never, 0 batch_queue
   bool key_split = true;                     // split key pass for one circuit when it pays (option key_split)
 
   static bool walk_qpt_fits(uint32_t qpad, uint32_t q) {
@@ -371,6 +374,7 @@ struct gpc_driver {
     L.err = take(4);
     L.totals = take(16);
     L.big_n = take(4);
+    L.wq = take(4);
     L.bcount = take((size_t)nb * 4);
     L.tsum = take(((size_t)nb + gpc::SCAN_TILE - 1) / gpc::SCAN_TILE * 8);
     for (uint32_t i = 0; i < N; ++i)
@@ -402,12 +406,13 @@ struct gpc_driver {
     for (uint32_t i = 0; i < N; ++i) order[i] = i;
     std::stable_sort(order.begin(), order.end(), [&](uint32_t a, uint32_t b) { return tapes[a].qpad < tapes[b].qpad; });
     L.classes.clear();
-    item_order = order;
-    uint32_t item = 0;
     circ_words.assign(N, 1);
+    walk_items.clear();
+    if (N > 1 && build_queue_class()) return;
+    uint32_t item = 0;
     for (uint32_t k = 0; k < N;) {
       uint32_t e = k;
-      WalkClass wc{tapes[order[k]].qpad, item, 0, 0, 0, 0, 1};
+      WalkClass wc{tapes[order[k]].qpad, item, 0, 0, 0, 0, 1, 1, 0};
       while (e < N && tapes[order[e]].qpad == wc.qpad) {
         const Tape &T = tapes[order[e]];
         wc.chunk_cap = std::max(wc.chunk_cap, T.chunk_cap);
@@ -426,15 +431,68 @@ struct gpc_driver {
               227 * 1024 - 1024)
         wc.words = 2;
       for (uint32_t x = k; x < e; ++x) {
-        circ_words[order[x]] = wc.words;
-        wc.n_items += (tapes[order[x]].w + wc.words - 1) / wc.words;
+        const uint32_t i = order[x];
+        circ_words[i] = wc.words;
+        for (uint32_t j = 0; j < tapes[i].w; j += wc.words) walk_items.push_back(make_uint2(i, j));
+        wc.n_items += (tapes[i].w + wc.words - 1) / wc.words;
       }
       item += wc.n_items;
       L.classes.push_back(wc);
       k = e;
     }
   }
-  std::vector<uint32_t> item_order;  // circuits in walk-class order
+
+  // One persistent walk launch over every circuit of a batch (option
+  // walk_queue, or the autotuner's choice): block size and shared memory of
+  // the largest circuit, items ordered by estimated walk length, longest
+  // first.  False (classes instead) when not chosen or when it does not fit.
+  bool build_queue_class() {
+    const uint32_t N = ncirc();
+    if (walk_queue < 0 || (walk_queue == 0 && !batch_queue)) return false;
+    WalkClass wc{0, 0, 0, 0, 0, 0, 1, 1, 1};
+    for (uint32_t i = 0; i < N; ++i) {
+      const Tape &T = tapes[i];
+      wc.qpad = std::max(wc.qpad, T.qpad);
+      wc.chunk_cap = std::max(wc.chunk_cap, T.chunk_cap);
+      wc.max_epochs = std::max(wc.max_epochs, T.n_epochs);
+      wc.max_chunks = std::max(wc.max_chunks, (uint32_t)T.ch_off.size());
+    }
+    const uint32_t want = walk_words ? walk_words : (batch_words ? batch_words : 2u);
+    const uint32_t q = walk_qpt ? walk_qpt : (batch_qpt ? batch_qpt : 1u);
+    wc.qpad = (wc.qpad + 32 * q - 1) / (32 * q) * (32 * q);  // q slots per thread, whole warps
+    if (!gpc::walk_queue_supported(q, want) || wc.qpad / q > gpc::walk_max_threads(q)) return false;
+    if (gpc::walk_smem_bytes(wc.qpad, wc.chunk_cap, gpc::walk_table_bytes(wc.max_epochs, wc.max_chunks), want) >
+        227 * 1024 - 1024)
+      return false;
+    wc.qpt = q;
+    wc.words = want;
+    // estimated walk length of an item: its epochs (words holding observables
+    // walk to the end; detector words stop a little after their last
+    // injection) times the CTA's active warps plus a fixed cost per epoch
+    std::vector<std::pair<uint64_t, uint2>> est;
+    for (uint32_t i = 0; i < N; ++i) {
+      const Tape &T = tapes[i];
+      circ_words[i] = want;
+      for (uint32_t j0 = 0; j0 < T.w; j0 += want) {
+        uint32_t e0 = 0xFFFFFFFFu, e1 = 0;
+        bool obs = false;
+        for (uint32_t j = j0; j < std::min(T.w, j0 + want); ++j) {
+          if ((uint64_t)(j + 1) * 64 > T.ndet) obs = true;
+          if (T.inj_lo[j] == 0xFFFFFFFFu || T.inj_lo[j] >= T.n_epochs) continue;
+          e0 = std::min(e0, T.inj_lo[j]);
+          e1 = std::max(e1, T.inj_hi[j]);
+        }
+        const uint64_t ep = e0 == 0xFFFFFFFFu ? 0 : (obs ? T.n_epochs : std::min(T.n_epochs, e1 + 16)) - e0;
+        est.push_back({ep * (T.qpad / 32 + 8), make_uint2(i, j0)});
+      }
+    }
+    std::stable_sort(est.begin(), est.end(), [](const auto &a, const auto &b) { return a.first > b.first; });
+    for (const auto &x : est) walk_items.push_back(x.second);
+    wc.n_items = (uint32_t)walk_items.size();
+    L.classes.push_back(wc);
+    return true;
+  }
+  std::vector<uint2> walk_items;     // (circuit, first word) of each walk CTA, in launch order
   std::vector<uint32_t> circ_words;  // detector words per walk CTA of each circuit
 
   void stage_inputs() {
@@ -516,11 +574,7 @@ struct gpc_driver {
     put(L.cdev, cd.data(), cd.size() * sizeof(CircuitDev));
     put(L.mbase, mb.data(), mb.size() * 4);
     put(L.cbbase, cb.data(), cb.size() * 4);
-    std::vector<uint2> items;
-    items.reserve(L.n_items);
-    for (uint32_t i : item_order)
-      for (uint32_t j = 0; j < tapes[i].w; j += circ_words[i]) items.push_back(make_uint2(i, j));
-    put(L.items, items.data(), items.size() * sizeof(uint2));
+    put(L.items, walk_items.data(), walk_items.size() * sizeof(uint2));
     if (param) {
       // records of each (tick, class) source, in record order
       const Tape &T = tapes[0];
@@ -628,6 +682,7 @@ struct gpc_driver {
       mix(c.max_chunks);
       mix(c.words);
       mix(c.qpt);
+      mix(c.queue);
     }
     mix(split_word());
     cfg_sig = h;
@@ -682,6 +737,7 @@ struct gpc_driver {
     wl.max_chunks = wc.max_chunks;
     wl.words = wc.words;
     wl.err = dptr<uint32_t>(L.err);
+    wl.queue = wc.queue ? dptr<uint32_t>(L.wq) : nullptr;
     CK(gpc::launch_walk(wl, s));
   }
 
@@ -1246,18 +1302,24 @@ struct gpc_driver {
   }
 
   // Times the batched pipeline of these circuits in each walk configuration
-  // (words per CTA x qubits per thread) and keeps the fastest for batches.
+  // (words per CTA x qubits per thread, one launch per thread-count class or
+  // one persistent launch) and keeps the fastest for batches.
   void autotune(const char *const *texts, const size_t *lens, uint32_t n, uint32_t reps, gpc_tuning &out) {
-    static const uint32_t cand[][2] = {{2, 1}, {1, 1}, {2, 2}, {1, 2}, {1, 4}};
+    static const uint32_t cand[][3] = {{2, 1, 0}, {1, 1, 0}, {2, 2, 0}, {1, 2, 0}, {1, 4, 0},
+                                       {2, 1, 1}, {1, 1, 1}, {2, 2, 1}, {1, 2, 1}};
     out = gpc_tuning{};
     prepare(texts, lens, n);  // lowered once: each configuration lays out the same tapes again
     float best = std::numeric_limits<float>::infinity();
-    uint32_t bw = batch_words, bq = batch_qpt;
+    uint32_t bw = batch_words, bq = batch_qpt, bz = batch_queue;
     try {
       for (const auto &c : cand) {
         batch_words = c[0];
         batch_qpt = c[1];
+        batch_queue = c[2];
         prepare(nullptr, nullptr, 0);
+        // a persistent configuration that does not fit these circuits runs as classes: skip it
+        const bool queued = L.classes.size() == 1 && L.classes[0].queue;
+        if (c[2] && !queued) continue;
         run();  // first launches of this configuration
         float t = std::numeric_limits<float>::infinity();
         for (uint32_t r = 0; r < std::max(1u, reps); ++r) {
@@ -1267,23 +1329,28 @@ struct gpc_driver {
           CK(cudaEventElapsedTime(&ms, ev[0], ev[4]));
           t = std::min(t, ms);
         }
-        if (out.num_tried < 8) out.tried[out.num_tried++] = gpc_tuning_entry{(int32_t)c[0], (int32_t)c[1], t};
+        if (out.num_tried < 12)
+          out.tried[out.num_tried++] = gpc_tuning_entry{(int32_t)c[0], (int32_t)c[1], (int32_t)c[2], t};
         if (t < best) {
           best = t;
           bw = c[0];
           bq = c[1];
+          bz = c[2];
         }
       }
     } catch (...) {
       batch_words = 0;
       batch_qpt = 0;
+      batch_queue = 0;
       throw;
     }
     batch_words = bw;
     batch_qpt = bq;
+    batch_queue = bz;
     prepare(nullptr, nullptr, 0);
     out.walk_words = (int32_t)bw;
     out.walk_qpt = (int32_t)bq;
+    out.walk_queue = (int32_t)bz;
     out.ms = best;
   }
 
@@ -1302,6 +1369,8 @@ struct gpc_driver {
       d->key_split = key_split;
       d->batch_words = batch_words;
       d->batch_qpt = batch_qpt;
+      d->batch_queue = batch_queue;
+      d->walk_queue = walk_queue;
       d->init_streams();
       partner = std::move(d);
     }
@@ -1642,6 +1711,8 @@ gpc_status gpc_get_driver(const char *stim_text, size_t len, int32_t correlation
     d->walk_words = (uint32_t)options->walk_words;
     if (options->key_split != 0 && options->key_split != -1) return fail(GPC_ERR_INVALID, "key_split must be 0 or -1");
     d->key_split = options->key_split == 0;
+    if (options->walk_queue < -1 || options->walk_queue > 1) return fail(GPC_ERR_INVALID, "walk_queue must be -1, 0 or 1");
+    d->walk_queue = options->walk_queue;
   }
   gpc_status st = guarded([&] {
     int n = 0;
@@ -1761,6 +1832,7 @@ gpc_status gpc_autotune(gpc_driver *driver, const char *const *texts, const size
     if (driver->partner) {  // the second pipeline of compile_batch follows the choice
       driver->partner->batch_words = driver->batch_words;
       driver->partner->batch_qpt = driver->batch_qpt;
+      driver->partner->batch_queue = driver->batch_queue;
     }
   });
 }

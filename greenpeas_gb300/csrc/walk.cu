@@ -29,6 +29,13 @@
 //      non-zero words of a point.
 // The epoch and chunk tables are staged in shared memory at start, so no
 // global load sits on the per-epoch critical path.
+//
+// Two launch forms share that body (walk_item): one CTA per item for the
+// circuits of one thread-count class (walk_kernel), or one persistent launch
+// over a whole batch (walk_queue_kernel) whose resident CTAs, sized for the
+// largest circuit, take (circuit, word group) items from a queue counter,
+// longest first, until it runs dry.
+#include <algorithm>
 #include <cstdint>
 
 #include "device.cuh"
@@ -121,22 +128,35 @@ struct WalkBound {
   static constexpr int value = QPT <= 2 || QPT == 4 ? 1024 : QPT == 3 ? 512 : QPT <= 8 ? 256 : 128;
 };
 
-// W detector words per CTA: the words j0 .. j0+W-1 of one circuit walk
-// together (rows W x 64 bits per qubit); a batch halves its CTAs with W = 2
-// while each epoch's latency chain stays about the same.
-template <int QPT, int W>
-__global__ void __launch_bounds__(WalkBound<QPT>::value) walk_kernel(const CircuitDev *__restrict__ circs,
-                                                    const uint2 *__restrict__ items, uint32_t chunk_cap, uint32_t table_bytes,
-                                                    uint32_t *__restrict__ err) {
-  extern __shared__ __align__(128) unsigned char smem[];
-  const uint2 item = items[blockIdx.x];
-  const CircuitDev C = circs[item.x];
-  const uint32_t j0 = item.y;
+__device__ __forceinline__ void mbar_inval(uint64_t *bar) {
+  asm volatile("mbarrier.inval.shared::cta.b64 [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+enum : uint32_t { ITEM_DONE = 0, ITEM_EMPTY = 1, ITEM_ABORTED = 2 };
+
+// One walk item: the words j0 .. j0+W-1 of circuit C (rows W x 64 bits per
+// qubit; a batch halves its CTAs with W = 2 while each epoch's latency chain
+// stays about the same), walked by the whole CTA.  `pub_slots` lays out the
+// shared memory (the circuit's slot count, or the largest of a persistent
+// launch).  QUEUE: the CTA may have more threads than the circuit has qubit
+// slots (a persistent launch sized for its largest circuit); thread slots at
+// or past C.qpad hold nothing, publish nothing and skip the ops (qpad is a
+// multiple of 32, so whole warps idle).  Returns ITEM_EMPTY when the words
+// inject nothing (the mbarriers were not initialised), ITEM_ABORTED after a
+// bounded wait gave up, else ITEM_DONE.  CTA-uniform.
+template <int QPT, int W, bool QUEUE>
+__device__ __forceinline__ uint32_t walk_item(const CircuitDev &C, const uint32_t j0, unsigned char *smem,
+                                              const uint32_t pub_slots, const uint32_t chunk_cap,
+                                              const uint32_t table_bytes, uint32_t *__restrict__ err,
+                                              uint32_t &s_abort) {
   const uint32_t nw = min((uint32_t)W, C.w - j0);  // words of this CTA (the circuit's last group may be short)
   const uint32_t T = blockDim.x;
   const uint32_t tid = threadIdx.x;
   const uint32_t qpad = C.qpad;
   const uint32_t nE = C.n_epochs;
+  bool act[QPT];  // thread slot tid + u * T holds a qubit slot of the circuit
+#pragma unroll
+  for (int u = 0; u < QPT; ++u) act[u] = !QUEUE || tid + (uint32_t)u * T < qpad;
 
   // the CTA walks from the earliest first injection of its words to the
   // latest last injection (and on until every row is zero)
@@ -151,12 +171,12 @@ __global__ void __launch_bounds__(WalkBound<QPT>::value) walk_kernel(const Circu
   }
   if (e0 == 0xFFFFFFFFu) {
     if (tid < nw) C.band[j0 + tid] = make_uint2(0u, 0u);
-    return;
+    return ITEM_EMPTY;
   }
 
   // shared memory: [published rows x2][mbarriers][tables][chunk buffer x2]
   ulonglong2 *pub = reinterpret_cast<ulonglong2 *>(smem);
-  size_t off = (size_t)2 * qpad * W * sizeof(ulonglong2);
+  size_t off = (size_t)2 * pub_slots * W * sizeof(ulonglong2);
   uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + off);
   off += 128;
   uint2 *etab = reinterpret_cast<uint2 *>(smem + off);  // epoch e0+i: (op offset, slots | chunk << 8)
@@ -166,7 +186,6 @@ __global__ void __launch_bounds__(WalkBound<QPT>::value) walk_kernel(const Circu
   uint2 *ctab = etab + ne;  // chunk c0+i: (op offset, bytes)
   off += table_bytes;
   unsigned char *buf = smem + off;  // two buffers of chunk_cap bytes
-  __shared__ uint32_t s_abort;
 
   if (staged) {
     for (uint32_t i = tid; i < ne; i += T)
@@ -216,7 +235,7 @@ __global__ void __launch_bounds__(WalkBound<QPT>::value) walk_kernel(const Circu
   unsigned long long *nzm0 = C.nzm + (j0 >> 6);
   const uint32_t mw = C.mw;
   const uint32_t jsh = j0 & 63u;
-  bool timed_out = false;
+  bool timed_out = false, aborted = false;
   uint32_t e = e0;
   uint32_t seq = 0;
   uint32_t cur = 0xFFFFFFFFu;  // chunk whose data this thread has waited for
@@ -249,6 +268,7 @@ __global__ void __launch_bounds__(WalkBound<QPT>::value) walk_kernel(const Circu
     for (int u = 0; u < QPT; ++u)
 #pragma unroll
       for (int wi = 0; wi < W; ++wi) {
+        if (!act[u]) continue;
         asm volatile("st.shared.v2.u64 [%0], {%1, %2};" ::"r"(smem_u32(pb + (tid + u * T) * W + wi)),
                      "l"(X[u][wi]), "l"(Z[u][wi])
                      : "memory");
@@ -259,6 +279,7 @@ __global__ void __launch_bounds__(WalkBound<QPT>::value) walk_kernel(const Circu
     const int any = __syncthreads_or(nz ? 1 : 0);
     if (s_abort) {
       if (tid == 0) atomicOr(err, DEV_ERR_TIMEOUT);
+      aborted = true;
       break;
     }
     if ((!any && e > elast) || e >= nE) break;
@@ -287,6 +308,7 @@ __global__ void __launch_bounds__(WalkBound<QPT>::value) walk_kernel(const Circu
     for (uint32_t k = 0; k < K; ++k) {
 #pragma unroll
       for (int u = 0; u < QPT; ++u) {
+        if (!act[u]) continue;
         const uint64_t op = lds64(ops_s + (k * qpad + (uint32_t)u * T) * 8u);
         const uint32_t opc = (uint32_t)op & 0xFFu;
         if (opc == OP_NOP) continue;
@@ -363,12 +385,60 @@ __global__ void __launch_bounds__(WalkBound<QPT>::value) walk_kernel(const Circu
   if (tid < nw) C.band[j0 + tid] = make_uint2(C.ep_ptoff[e0], C.ep_ptoff[e < nE ? e : nE]);
   if (tid == 0) {
     // Copies still in flight target this CTA's shared memory: wait for them
-    // (bounded) before the CTA exits.
+    // (bounded) before the CTA exits or takes another item.
     for (uint32_t i = waited; i < issued; ++i) {
       if (!mbar_wait_bounded(&mbar[i & 1u], (i >> 1) & 1u)) {
         atomicOr(err, DEV_ERR_TIMEOUT);
+        s_abort = 1;
         break;
       }
+    }
+  }
+  return aborted ? ITEM_ABORTED : ITEM_DONE;
+}
+
+// One CTA per item (circuit, first word), all circuits of the launch with
+// the same slot count.
+template <int QPT, int W>
+__global__ void __launch_bounds__(WalkBound<QPT>::value) walk_kernel(const CircuitDev *__restrict__ circs,
+                                                    const uint2 *__restrict__ items, uint32_t chunk_cap, uint32_t table_bytes,
+                                                    uint32_t *__restrict__ err) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ uint32_t s_abort;
+  const uint2 item = items[blockIdx.x];
+  const CircuitDev C = circs[item.x];
+  walk_item<QPT, W, false>(C, item.y, smem, C.qpad, chunk_cap, table_bytes, err, s_abort);
+}
+
+// Persistent walk: one launch over the items of circuits of every size, at
+// most as many CTAs as fit on the GPU at once.  Each CTA takes the next item
+// from the queue counter (items are ordered longest first, so the longest
+// walks start first and the short ones fill in behind them) until the queue
+// is empty.  A CTA stops taking items after a wait gave up.
+template <int QPT, int W>
+__global__ void __launch_bounds__(WalkBound<QPT>::value) walk_queue_kernel(const CircuitDev *__restrict__ circs,
+                                                          const uint2 *__restrict__ items, uint32_t n_items,
+                                                          uint32_t *__restrict__ next, uint32_t pub_slots,
+                                                          uint32_t chunk_cap, uint32_t table_bytes,
+                                                          uint32_t *__restrict__ err) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ uint32_t s_item, s_abort;
+  uint64_t *mbar = reinterpret_cast<uint64_t *>(smem + (size_t)2 * pub_slots * W * sizeof(ulonglong2));
+  for (;;) {
+    if (threadIdx.x == 0) s_item = atomicAdd(next, 1u);
+    __syncthreads();
+    const uint32_t it = s_item;
+    if (it >= n_items) return;
+    const uint2 item = items[it];
+    const CircuitDev C = circs[item.x];
+    const uint32_t st = walk_item<QPT, W, true>(C, item.y, smem, pub_slots, chunk_cap, table_bytes, err, s_abort);
+    // every thread is done with the item's shared memory and mbarriers (and
+    // thread 0 has seen every copy of the item complete)
+    __syncthreads();
+    if (st == ITEM_ABORTED || s_abort) return;
+    if (st == ITEM_DONE && threadIdx.x == 0) {
+      mbar_inval(&mbar[0]);
+      mbar_inval(&mbar[1]);
     }
   }
 }
@@ -395,6 +465,15 @@ cudaError_t walk_set_limit_one(int optin) {
                               optin - (int)a.sharedSizeBytes);
 }
 
+template <int QPT, int W>
+cudaError_t walk_queue_set_limit_one(int optin) {
+  cudaFuncAttributes a{};
+  cudaError_t e = cudaFuncGetAttributes(&a, walk_queue_kernel<QPT, W>);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(walk_queue_kernel<QPT, W>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              optin - (int)a.sharedSizeBytes);
+}
+
 cudaError_t walk_set_smem_limit() {
   int dev = 0, optin = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -409,6 +488,10 @@ cudaError_t walk_set_smem_limit() {
   if (e == cudaSuccess) e = walk_set_limit_one<16, 1>(optin);
   if (e == cudaSuccess) e = walk_set_limit_one<1, 2>(optin);
   if (e == cudaSuccess) e = walk_set_limit_one<2, 2>(optin);
+  if (e == cudaSuccess) e = walk_queue_set_limit_one<1, 1>(optin);
+  if (e == cudaSuccess) e = walk_queue_set_limit_one<2, 1>(optin);
+  if (e == cudaSuccess) e = walk_queue_set_limit_one<1, 2>(optin);
+  if (e == cudaSuccess) e = walk_queue_set_limit_one<2, 2>(optin);
   return e;
 }
 
@@ -426,6 +509,29 @@ uint32_t walk_max_threads(uint32_t qpt) {
   }
 }
 
+bool walk_queue_supported(uint32_t qpt, uint32_t words) {
+  return (qpt == 1 || qpt == 2) && (words == 1 || words == 2);
+}
+
+namespace {
+// As many CTAs as can be resident at once (occupancy of this block size and
+// shared memory), at most one per item.
+template <int QPT, int W>
+cudaError_t launch_walk_queue_one(const WalkLaunch &L, uint32_t tb, size_t smem, cudaStream_t s) {
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, walk_queue_kernel<QPT, W>, (int)L.threads, smem);
+  if (e != cudaSuccess) return e;
+  if (per_sm < 1) return cudaErrorInvalidConfiguration;
+  const uint32_t grid = (uint32_t)std::min<uint64_t>((uint64_t)sms * (uint64_t)per_sm, L.n_items);
+  walk_queue_kernel<QPT, W><<<grid, L.threads, smem, s>>>(L.circs, L.items, L.n_items, L.queue, L.qpad, L.chunk_cap,
+                                                         tb, L.err);
+  return cudaGetLastError();
+}
+}  // namespace
+
 cudaError_t launch_walk(const WalkLaunch &L, cudaStream_t s) {
   if (L.n_items == 0) return cudaSuccess;
   const uint32_t tb = walk_table_bytes(L.max_epochs, L.max_chunks);
@@ -433,6 +539,12 @@ cudaError_t launch_walk(const WalkLaunch &L, cudaStream_t s) {
   if (smem > 227 * 1024 - 1024) return cudaErrorInvalidValue;
   if (L.words != 1 && !(L.words == 2 && (L.qpt == 1 || L.qpt == 2))) return cudaErrorInvalidValue;
   if (L.threads * L.qpt != L.qpad || L.threads > walk_max_threads(L.qpt)) return cudaErrorInvalidValue;
+  if (L.queue) {
+    // every circuit of the launch has at most L.qpad slots (checked by the caller)
+    if (!walk_queue_supported(L.qpt, L.words)) return cudaErrorInvalidValue;
+    if (L.words == 2) return L.qpt == 1 ? launch_walk_queue_one<1, 2>(L, tb, smem, s) : launch_walk_queue_one<2, 2>(L, tb, smem, s);
+    return L.qpt == 1 ? launch_walk_queue_one<1, 1>(L, tb, smem, s) : launch_walk_queue_one<2, 1>(L, tb, smem, s);
+  }
 #define GPC_WALK(Q) walk_kernel<Q, 1><<<L.n_items, L.threads, smem, s>>>(L.circs, L.items, L.chunk_cap, tb, L.err)
 #define GPC_WALK2(Q) walk_kernel<Q, 2><<<L.n_items, L.threads, smem, s>>>(L.circs, L.items, L.chunk_cap, tb, L.err)
   if (L.words == 2) {

@@ -108,7 +108,7 @@ class Driver:
 
     def __init__(self, circuit, correlation_level: CorrelationLevel = CorrelationLevel.L2, *,
                  device: int = 0, sort_bits: int = 0, global_sort: bool = False, walk_qpt: int = 0,
-                 bucket_mean: int = 0, walk_words: int = 0, key_split: int = 0):
+                 bucket_mean: int = 0, walk_words: int = 0, key_split: int = 0, walk_queue: int = 0):
         L = _native.lib()
         self._h = ctypes.c_void_p()
         self.correlation_level = CorrelationLevel(correlation_level)
@@ -121,6 +121,7 @@ class Driver:
         opts.bucket_mean = bucket_mean
         opts.walk_words = walk_words
         opts.key_split = key_split
+        opts.walk_queue = walk_queue
         text = _text(circuit)
         _native.check(L.gpc_get_driver(text, len(text), int(self.correlation_level), ctypes.byref(opts),
                                        ctypes.byref(self._h)))
@@ -171,15 +172,17 @@ class Driver:
 
     def autotune(self, circuits, reps: int = 3) -> dict:
         """Times the batched pipeline of ``circuits`` in each walk configuration (detector words per
-        walk CTA x qubits per walk thread) and keeps the fastest for this driver's batches; the DEMs
-        do not depend on it.  Returns the choice and every configuration's time (ms, best of reps)."""
+        walk CTA x qubits per walk thread x per-class launches or one persistent launch) and keeps the
+        fastest for this driver's batches; the DEMs do not depend on it.  Returns the choice and every
+        configuration's time (ms, best of reps)."""
         n, arr, lens = self._batch_args(circuits)
         t = _native.Tuning()
         _native.check(_native.lib().gpc_autotune(self._h, arr, lens, n, int(reps), ctypes.byref(t)))
         self._batch_n = n
-        tried = [{"walk_words": e.walk_words, "walk_qpt": e.walk_qpt, "ms": float(e.ms)}
-                 for e in t.tried[:t.num_tried]]
-        return {"walk_words": t.walk_words, "walk_qpt": t.walk_qpt, "ms": float(t.ms), "tried": tried}
+        tried = [{"walk_words": e.walk_words, "walk_qpt": e.walk_qpt, "walk_queue": e.walk_queue,
+                  "ms": float(e.ms)} for e in t.tried[:t.num_tried]]
+        return {"walk_words": t.walk_words, "walk_qpt": t.walk_qpt, "walk_queue": t.walk_queue,
+                "ms": float(t.ms), "tried": tried}
 
     def prepare_batch(self, circuits) -> None:
         n, arr, lens = self._batch_args(circuits)

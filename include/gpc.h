@@ -64,7 +64,9 @@ typedef struct gpc_options {
   int32_t bucket_mean; /* target mechanisms per merge bucket (8..128; 0 = default) */
   int32_t walk_words;  /* detector words per walk CTA (1, 2; 0 = two in batches, one for a single circuit) */
   int32_t key_split;   /* one circuit: key the detector words beside the observables' walk (0 = when it pays, -1 = never) */
-  int32_t reserved[1];
+  int32_t walk_queue;  /* batches: 1 = one persistent walk launch (resident CTAs take (circuit, word group) items
+                          from a queue, longest first), -1 = one launch per thread-count class,
+                          0 = classes unless gpc_autotune chose the persistent launch */
 } gpc_options;
 
 /* Parses `stim_text` (length `len`), sizes device buffers for it and returns
@@ -95,21 +97,23 @@ gpc_status gpc_compile_batch(gpc_driver *driver, const char *const *texts, const
  * Times the batched pipeline of circuits texts[0..n) (n >= 2) under each walk
  * configuration the kernels offer -- detector words per walk CTA (1, 2) x
  * qubits per walk thread (1, 2, 4; a choice that does not fit a circuit's
- * slot count falls back to the default for that circuit) -- best of `reps`
- * runs each by CUDA events on the driver's stream, and keeps the fastest for
- * the driver's later batches (single circuits keep their defaults; explicit
- * walk_words / walk_qpt options take precedence).  The DEMs do not depend on
- * the choice.  On return the circuits are prepared in the chosen
- * configuration (gpc_run_device runs them). */
+ * slot count falls back to the default for that circuit) x one launch per
+ * thread-count class or one persistent launch (queue; only where the
+ * largest circuit fits its block and shared memory) -- best of `reps` runs
+ * each by CUDA events on the driver's stream, and keeps the fastest for the
+ * driver's later batches (single circuits keep their defaults; explicit
+ * walk_words / walk_qpt / walk_queue options take precedence).  The DEMs do
+ * not depend on the choice.  On return the circuits are prepared in the
+ * chosen configuration (gpc_run_device runs them). */
 typedef struct gpc_tuning_entry {
-  int32_t walk_words, walk_qpt;
+  int32_t walk_words, walk_qpt, walk_queue;
   float ms; /* pipeline time, best of the repetitions */
 } gpc_tuning_entry;
 typedef struct gpc_tuning {
-  int32_t walk_words, walk_qpt; /* the chosen configuration */
+  int32_t walk_words, walk_qpt, walk_queue; /* the chosen configuration */
   float ms;
   int32_t num_tried;
-  gpc_tuning_entry tried[8];
+  gpc_tuning_entry tried[12];
 } gpc_tuning;
 gpc_status gpc_autotune(gpc_driver *driver, const char *const *texts, const size_t *lens, int32_t n,
                         int32_t reps, gpc_tuning *out);

@@ -95,8 +95,40 @@ def test_autotune_keeps_results_and_picks_a_configuration():
     drv = gp.get_driver(circs[0])
     before = drv.compile_batch(circs)
     tune = drv.autotune(circs, reps=2)
-    assert (tune["walk_words"], tune["walk_qpt"]) in {(t["walk_words"], t["walk_qpt"]) for t in tune["tried"]}
-    assert len(tune["tried"]) == 5 and tune["ms"] == min(t["ms"] for t in tune["tried"])
+    key = ("walk_words", "walk_qpt", "walk_queue")
+    assert tuple(tune[k] for k in key) in {tuple(t[k] for k in key) for t in tune["tried"]}
+    # five per-class configurations, and the four persistent ones (these circuits fit them)
+    assert len(tune["tried"]) == 9 and sum(t["walk_queue"] for t in tune["tried"]) == 4
+    assert tune["ms"] == min(t["ms"] for t in tune["tried"])
     drv.run_device()
     assert [a == b for a, b in zip(drv.fetch_batch(), before)] == [True] * len(circs)
     assert [a == b for a, b in zip(drv.compile_batch(circs), before)] == [True] * len(circs)
+
+
+@pytest.mark.parametrize("words,qpt", [(2, 1), (1, 1), (2, 2), (1, 2)])
+def test_persistent_walk_matches_class_launches(words, qpt):
+    """One persistent walk launch over circuits of every size (CTAs sized for the largest take
+    (circuit, word group) items from a queue, longest first) gives the DEMs of the per-class
+    launches, bit for bit, and the oracle's."""
+    from greenpeas_gb300.workloads import batch_surface
+    circs = _mixed() + batch_surface(n=6, seed=3, distances=(3, 9, 15))
+    ref = gp.get_driver(circs[0], walk_queue=-1, walk_words=words, walk_qpt=qpt).compile_batch(circs)
+    drv = gp.get_driver(circs[0], walk_queue=1, walk_words=words, walk_qpt=qpt)
+    out = drv.compile_batch(circs)
+    assert [a == b for a, b in zip(out, ref)] == [True] * len(circs)
+    drv.prepare_batch(circs)
+    for _ in range(3):  # later runs come from a captured graph (the queue counter is reset in it)
+        drv.run_device()
+    assert [a == b for a, b in zip(drv.fetch_batch(), ref)] == [True] * len(circs)
+    for text, dem in list(zip(circs, out))[:len(_mixed())]:
+        compare_errors(dict(dem.errors()), dict(O.compile_text(text, 2).errors()), rel=1e-12)
+
+
+def test_persistent_walk_with_the_largest_batch_circuit():
+    """The persistent launch sized for a d = 21 surface circuit (881 qubits, 896 threads) walks
+    d = 3 circuits with most of its warps idle; DEMs equal the per-class launches'."""
+    from greenpeas_gb300.workloads import batch_surface
+    circs = batch_surface(n=1, seed=7, distances=(21,)) + batch_surface(n=3, seed=8, distances=(3,))
+    ref = gp.get_driver(circs[0], walk_queue=-1).compile_batch(circs)
+    out = gp.get_driver(circs[0], walk_queue=1).compile_batch(circs)
+    assert [a == b for a, b in zip(out, ref)] == [True] * len(circs)
