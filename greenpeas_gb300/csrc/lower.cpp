@@ -401,6 +401,7 @@ struct LowerScratch::Buffers {
     HostArray<uint32_t> rec_src;
     size_t nrec = 0, roff = 0;
     uint32_t nprov = 0, eoff = 0, poff = 0;
+    std::vector<uint64_t> fine, coarse;  // per-qubit op signatures of the segment (qubit packing)
   };
   std::vector<Segment> segs;
   std::vector<size_t> cut;
@@ -469,6 +470,8 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
   lower_into(P, opt, T, S);
   return T;
 }
+
+constexpr uint64_t kFnvBasis = 0xcbf29ce484222325ull, kFnvPrime = 0x100000001b3ull;  // FNV-1a 64
 
 void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch &S, HostPool *pool) {
   if (opt.level < 0 || opt.level > 2) throw Error(GPC_ERR_INVALID, "correlation level must be 0, 1 or 2");
@@ -906,6 +909,17 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
     G.nent = (size_t)(ent1 - ent0);
     G.nrec = nrec;
     G.nprov = nprov;
+    // the segment's share of each qubit's signatures (see the qubit packing):
+    // op kinds, and op kinds with their (segment-local) epochs
+    G.fine.assign(nq, kFnvBasis);
+    G.coarse.assign(nq, kFnvBasis);
+    for (const Entry *x = ent0; x < ent1; ++x) {
+      const uint32_t opc = (uint32_t)(x->op & 0xFF);
+      if (opc == OP_INJ || opc == OP_SNAPD) continue;  // vary with detector membership only
+      const uint32_t q = x->q();
+      G.coarse[q] = (G.coarse[q] ^ opc) * kFnvPrime;
+      G.fine[q] = (G.fine[q] ^ (opc | ((uint64_t)x->e << 8))) * kFnvPrime;
+    }
   };
   if (pool && nseg > 1)
     pool->run(nseg, [&](uint32_t sg, uint32_t) { run_segment(sg); });
@@ -956,19 +970,18 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
   std::vector<uint32_t> &slotOf = B.slotOf;
   slotOf.assign(nq, 0);
   {
-    // fine signature: op kinds with their epochs; coarse: op kinds only
+    // fine signature: op kinds with their epochs; coarse: op kinds only.
+    // Each segment hashed its own ops; the segments' hashes are chained in
+    // segment order (segments are time ranges common to every qubit, so equal
+    // fine signatures still mean equal op kinds at equal epochs)
     std::vector<uint64_t> &fine = B.fine, &coarse = B.coarse;
-    fine.assign(nq, 0xcbf29ce484222325ull);
-    coarse.assign(nq, 0xcbf29ce484222325ull);
+    fine.assign(nq, kFnvBasis);
+    coarse.assign(nq, kFnvBasis);
     for (uint32_t sg = 0; sg < nseg; ++sg) {
       const LowerScratch::Buffers::Segment &G = B.segs[sg];
-      const Entry *const ent0 = G.ent.p.get();
-      for (size_t i = 0; i < G.nent; ++i) {
-        const Entry &x = ent0[i];
-        const uint32_t opc = (uint32_t)(x.op & 0xFF);
-        if (opc == OP_INJ || opc == OP_SNAPD) continue;  // vary with detector membership only
-        coarse[x.q()] = (coarse[x.q()] ^ opc) * 0x100000001b3ull;
-        fine[x.q()] = (fine[x.q()] ^ (opc | ((uint64_t)(x.e + G.eoff) << 8))) * 0x100000001b3ull;
+      for (uint32_t q = 0; q < nq; ++q) {
+        coarse[q] = (coarse[q] ^ G.coarse[q]) * kFnvPrime;
+        fine[q] = (fine[q] ^ G.fine[q]) * kFnvPrime;
       }
     }
     const uint32_t qptBase = T.qpad <= 1024 ? 1u : T.qpad <= 2048 ? 2u : 4u;
@@ -1027,35 +1040,33 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
     T.kmax = std::max(T.kmax, T.ep_k[e]);
     if (total > 0xFFFFFFFFull) throw Error(GPC_ERR_CAPACITY, "tape too long");
   }
-  T.ops.assign(total, 0);
   // points are numbered in walk order (epoch, slot, qubit slot), so each
-  // epoch owns a contiguous range; a large tape is scattered and renumbered
-  // in pieces on the pool (disjoint ops and points per piece)
+  // epoch owns a contiguous range.  Segments own disjoint epoch ranges (so
+  // disjoint ops and points): a large tape is zeroed, scattered and
+  // renumbered segment by segment on the pool.
+  T.ops.resize(total);
   T.ep_ptoff.assign(nE + 1, 0);
   for (uint32_t e = 0; e < nE; ++e) T.ep_ptoff[e + 1] = T.ep_ptoff[e] + ep_np[e];
   std::vector<uint32_t> &remap = B.remap;
   remap.assign(nprov, kNone);
-  const uint32_t pieces = pool && total >= (1u << 16) ? std::min(8u, pool->workers() + 1) : 1u;
-  auto scatter = [&](uint32_t q, uint32_t) {
-    for (uint32_t sg = 0; sg < nseg; ++sg) {
-      const LowerScratch::Buffers::Segment &G = B.segs[sg];
-      const Entry *const ent0 = G.ent.p.get();
-      for (size_t i = G.nent * q / pieces, i1 = G.nent * (q + 1) / pieces; i < i1; ++i) {
-        const Entry &x = ent0[i];
-        uint64_t op = x.op;
-        const uint32_t opc = (uint32_t)(op & 0xFF);
-        if (opc == OP_C2 || opc >= OP_XPX)  // partner qubit -> partner slot
-          op = (op & 0xFFFFFFFFull) | ((uint64_t)slotOf[(uint32_t)(op >> 32)] << 32);
-        else if (opc == OP_SNAP || opc == OP_SNAPD)  // segment-local point -> provisional point
-          op += (uint64_t)G.poff << 32;
-        T.ops[(size_t)T.ep_opoff[x.e + G.eoff] + (size_t)x.k() * T.qpad + slotOf[x.q()]] = op;
-      }
-    }
-  };
   std::atomic<bool> miscount{false};
-  auto renumber = [&](uint32_t q, uint32_t) {
-    for (uint32_t e = (uint32_t)((uint64_t)nE * q / pieces), e1 = (uint32_t)((uint64_t)nE * (q + 1) / pieces); e < e1;
-         ++e) {
+  auto assemble = [&](uint32_t sg, uint32_t) {
+    const LowerScratch::Buffers::Segment &G = B.segs[sg];
+    const uint32_t ea = G.eoff, eb = G.eoff + (uint32_t)G.ep_k.size();
+    const size_t oa = ea < nE ? T.ep_opoff[ea] : total, ob = eb < nE ? T.ep_opoff[eb] : total;
+    if (ob > oa) memset(T.ops.data() + oa, 0, (ob - oa) * 8);
+    const Entry *const ent0 = G.ent.p.get();
+    for (size_t i = 0; i < G.nent; ++i) {
+      const Entry &x = ent0[i];
+      uint64_t op = x.op;
+      const uint32_t opc = (uint32_t)(op & 0xFF);
+      if (opc == OP_C2 || opc >= OP_XPX)  // partner qubit -> partner slot
+        op = (op & 0xFFFFFFFFull) | ((uint64_t)slotOf[(uint32_t)(op >> 32)] << 32);
+      else if (opc == OP_SNAP || opc == OP_SNAPD)  // segment-local point -> provisional point
+        op += (uint64_t)G.poff << 32;
+      T.ops[(size_t)T.ep_opoff[x.e + G.eoff] + (size_t)x.k() * T.qpad + slotOf[x.q()]] = op;
+    }
+    for (uint32_t e = ea; e < eb; ++e) {
       uint32_t next = T.ep_ptoff[e];
       uint64_t *base = T.ops.data() + T.ep_opoff[e];
       const size_t n = (size_t)T.ep_k[e] * T.qpad;
@@ -1071,13 +1082,10 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
       if (next != T.ep_ptoff[e + 1]) miscount = true;
     }
   };
-  if (pieces > 1) {
-    pool->run(pieces, scatter);
-    pool->run(pieces, renumber);
-  } else {
-    scatter(0, 0);
-    renumber(0, 0);
-  }
+  if (pool && nseg > 1 && total >= (1u << 16))
+    pool->run(nseg, assemble);
+  else
+    for (uint32_t sg = 0; sg < nseg; ++sg) assemble(sg, 0);
   if (miscount) throw Error(GPC_ERR_INVALID, "internal: points per epoch miscounted");
   const uint32_t next = T.ep_ptoff[nE];
   T.npoints = next;

@@ -131,7 +131,7 @@ void parse_stim_into(const char *text, size_t len, Parsed &out);
 struct Tape {
   uint32_t nq = 0, qpad = 0, nmeas = 0, ndet = 0, nobs = 0, nbits = 0, w = 0;
   uint32_t n_epochs = 0, kmax = 0;
-  std::vector<uint64_t> ops;        // sum_e K_e * qpad
+  HostArray<uint64_t> ops;          // sum_e K_e * qpad (every op written by the lowering)
   std::vector<uint32_t> ep_opoff;   // [n_epochs]     first op of epoch e
   std::vector<uint32_t> ep_k;       // [n_epochs]     slots in epoch e
   std::vector<uint32_t> ep_ptoff;   // [n_epochs + 1] first point of epoch e
