@@ -28,7 +28,7 @@ EXPORTS = [
     "gpc_last_io_bytes", "gpc_merge_mechanisms_static", "gpc_prepare_batch", "gpc_fetch_batch",
     "gpc_param_prepare", "gpc_param_forward", "gpc_param_probs", "gpc_param_backward",
     "gpc_server_create", "gpc_server_submit", "gpc_server_wait", "gpc_server_stats", "gpc_server_destroy",
-    "gpc_device_dem", "gpc_autotune",
+    "gpc_device_dem", "gpc_autotune", "gpc_last_host_timings",
 ]
 
 
@@ -93,8 +93,8 @@ def lib() -> ctypes.CDLL:
     vp, sz, i32, u32 = ctypes.c_void_p, ctypes.c_size_t, ctypes.c_int32, ctypes.c_uint32
     u32p, u64p = ctypes.POINTER(ctypes.c_uint32), ctypes.POINTER(ctypes.c_uint64)
     L.gpc_get_driver.argtypes = [ctypes.c_char_p, sz, i32, ctypes.POINTER(Options), ctypes.POINTER(vp)]
-    L.gpc_compile.argtypes = [vp, ctypes.c_char_p, sz, ctypes.POINTER(vp)]
-    L.gpc_compile_batch.argtypes = [vp, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(sz), i32, ctypes.POINTER(vp)]
+    L.gpc_compile.argtypes = [vp, vp, sz, ctypes.POINTER(vp)]  # text: bytes or an address
+    L.gpc_compile_batch.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(sz), i32, ctypes.POINTER(vp)]
     L.gpc_dem_arrays.argtypes = [vp, ctypes.POINTER(u32p), ctypes.POINTER(u32p),
                                  ctypes.POINTER(ctypes.POINTER(ctypes.c_double)), u32p]
     L.gpc_dem_info.argtypes = [vp, u32p, u32p, u64p]
@@ -104,19 +104,20 @@ def lib() -> ctypes.CDLL:
     L.gpc_driver_destroy.argtypes = [vp]
     L.gpc_driver_destroy.restype = None
     L.gpc_last_error.restype = ctypes.c_char_p
-    L.gpc_prepare.argtypes = [vp, ctypes.c_char_p, sz]
+    L.gpc_prepare.argtypes = [vp, vp, sz]
     L.gpc_run_device.argtypes = [vp]
     L.gpc_fetch.argtypes = [vp, ctypes.POINTER(vp)]
     L.gpc_driver_stream.argtypes = [vp]
     L.gpc_driver_stream.restype = vp
     L.gpc_last_timings.argtypes = [vp, ctypes.POINTER(ctypes.c_float)]
+    L.gpc_last_host_timings.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
     L.gpc_last_sizes.argtypes = [vp, u64p, u64p, u32p, u32p, u32p]
     L.gpc_last_traffic.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
     L.gpc_last_io_bytes.argtypes = [vp, u64p, u64p]
     L.gpc_merge_mechanisms_static.argtypes = [vp, vp, u32, vp, u32, vp, vp, vp, u32, vp, vp]
-    L.gpc_prepare_batch.argtypes = [vp, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(sz), i32]
+    L.gpc_prepare_batch.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(sz), i32]
     L.gpc_fetch_batch.argtypes = [vp, ctypes.POINTER(vp), i32]
-    L.gpc_autotune.argtypes = [vp, ctypes.POINTER(ctypes.c_char_p), ctypes.POINTER(sz), i32, i32, ctypes.POINTER(Tuning)]
+    L.gpc_autotune.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(sz), i32, i32, ctypes.POINTER(Tuning)]
     L.gpc_tape_lower.argtypes = [ctypes.c_char_p, sz, i32, ctypes.POINTER(vp)]
     L.gpc_tape_get_view.argtypes = [vp, ctypes.POINTER(TapeView)]
     L.gpc_tape_free.argtypes = [vp]
@@ -124,7 +125,7 @@ def lib() -> ctypes.CDLL:
     L.gpc_tape_last_error.restype = ctypes.c_char_p
     L.gpc_device_dem.argtypes = [vp, i32, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp), u32p, u32p]
     L.gpc_server_create.argtypes = [ctypes.POINTER(ServerOptions), ctypes.POINTER(vp)]
-    L.gpc_server_submit.argtypes = [vp, ctypes.c_char_p, sz, u64p]
+    L.gpc_server_submit.argtypes = [vp, vp, sz, u64p]
     L.gpc_server_wait.argtypes = [vp, ctypes.c_uint64, ctypes.c_double, ctypes.POINTER(vp),
                                   ctypes.POINTER(ctypes.c_double)]
     L.gpc_server_stats.argtypes = [vp, u64p, u64p, u64p, u64p]
@@ -139,7 +140,7 @@ def lib() -> ctypes.CDLL:
               "gpc_get_driver", "gpc_compile", "gpc_compile_batch", "gpc_dem_arrays", "gpc_dem_info",
               "gpc_dem_text", "gpc_prepare", "gpc_run_device", "gpc_fetch", "gpc_last_timings",
               "gpc_last_sizes", "gpc_tape_lower", "gpc_tape_get_view", "gpc_last_traffic", "gpc_last_io_bytes",
-              "gpc_merge_mechanisms_static", "gpc_prepare_batch", "gpc_fetch_batch"):
+              "gpc_merge_mechanisms_static", "gpc_prepare_batch", "gpc_fetch_batch", "gpc_last_host_timings"):
         getattr(L, f).restype = i32
     _lib = L
     return L

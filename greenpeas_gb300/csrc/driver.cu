@@ -166,8 +166,9 @@ struct gpc_driver {
   std::vector<gpc::LowerScratch> lower_scratch;  // host memory of parse + lower, one per pool slot
   std::unique_ptr<gpc::HostPool> pool;            // host threads of this driver (made on first use)
   uint32_t pool_threads = 0;  // threads of the host pool, the caller included (0: every host thread)
+  uint32_t pool_spin_us = 200;  // how long an idle pool thread polls for the next hand-off before parking
   gpc::HostPool &host_pool() {
-    if (!pool) pool.reset(new gpc::HostPool((pool_threads ? pool_threads : host_threads()) - 1));
+    if (!pool) pool.reset(new gpc::HostPool((pool_threads ? pool_threads : host_threads()) - 1, pool_spin_us));
     return *pool;
   }
   // Circuit indices by decreasing size (the order batch work is handed out in).
@@ -206,6 +207,13 @@ struct gpc_driver {
   uint32_t batch_queue = 0;                  // 1: batches walk in one persistent launch (autotune's choice)
   int walk_queue = 0;                        // option walk_queue: 1 always, -1 never, 0 batch_queue
   bool key_split = true;                     // split key pass for one circuit when it pays (option key_split)
+  // host phases of the last prepare / fetch (ms): lower, layout, staging,
+  // wait for the pipeline + result sizes, D2H copies, DEM split
+  double host_ms[6] = {};
+  using HostClock = std::chrono::steady_clock;
+  static double ms_since(HostClock::time_point t) {
+    return std::chrono::duration<double, std::milli>(HostClock::now() - t).count();
+  }
 
   static bool walk_qpt_fits(uint32_t qpad, uint32_t q) {
     const uint32_t mt = gpc::walk_max_threads(q);
@@ -275,6 +283,7 @@ struct gpc_driver {
     if (fork_ev) cudaEventDestroy(fork_ev);
     if (caller_ev) cudaEventDestroy(caller_ev);
     if (done_ev) cudaEventDestroy(done_ev);
+    if (wait_ev) cudaEventDestroy(wait_ev);
     for (auto &e : join_ev)
       if (e) cudaEventDestroy(e);
     for (auto &a : aux)
@@ -282,8 +291,24 @@ struct gpc_driver {
     if (stream) cudaStreamDestroy(stream);
   }
 
+  // Waits for the driver's stream.  A server worker sleeps in the wait (an
+  // event with blocking sync) so the lowering threads get its core while the
+  // GPU runs its batch; otherwise the CUDA default (a spinning wait, lowest
+  // latency) applies.
+  bool blocking_wait = false;
+  cudaEvent_t wait_ev = nullptr;
+  void wait() {
+    if (blocking_wait) {
+      CK(cudaEventRecord(wait_ev, stream));
+      CK(cudaEventSynchronize(wait_ev));
+    } else {
+      CK(cudaStreamSynchronize(stream));
+    }
+  }
+
   void init_streams() {
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&wait_ev, cudaEventBlockingSync | cudaEventDisableTiming));
     for (auto &a : aux) CK(cudaStreamCreateWithFlags(&a, cudaStreamNonBlocking));
     for (auto &e : ev) CK(cudaEventCreate(&e));
     CK(cudaEventCreateWithFlags(&fork_ev, cudaEventDisableTiming));
@@ -638,14 +663,19 @@ struct gpc_driver {
       if (n == 0) throw gpc::Error(GPC_ERR_INVALID, "empty batch");
       tcap = 32;
       lists_off = false;
+      const auto t0 = HostClock::now();
       lower_all(texts, lens, n);
+      host_ms[0] = ms_since(t0);
       have_tape = true;
     } else if (!have_tape) {
       throw gpc::Error(GPC_ERR_INVALID, "no circuit to compile");
+    } else {
+      host_ms[0] = 0;
     }
+    const auto t1 = HostClock::now();
     layout();
     // The stream may still be reading the old arena: finish before regrowing.
-    CK(cudaStreamSynchronize(stream));
+    wait();
     uint32_t want_tg = std::max<uint32_t>(1024u, (uint32_t)std::min<uint64_t>(0xFFFFFFF0ull, (uint64_t)L.M * 16));
     if (admit) {
       const size_t tgb = (size_t)std::max(want_tg, tg_cap) * 4;
@@ -657,7 +687,10 @@ struct gpc_driver {
       tgbuf.ensure((size_t)want_tg * 4);
       tg_cap = want_tg;
     }
+    host_ms[1] = ms_since(t1);
+    const auto t2 = HostClock::now();
     stage_inputs();
+    host_ms[2] = ms_since(t2);
     CK(cudaMemcpyAsync(arena.p, pin_in.p, L.in_bytes, cudaMemcpyHostToDevice, stream));
     last_h2d = L.in_bytes;
     // what a captured graph depends on: buffer addresses and launch sizes
@@ -960,7 +993,7 @@ struct gpc_driver {
     for (int attempt = 0; attempt < 8; ++attempt) {
       CK(cudaMemcpyAsync(h, dptr<char>(L.err), 4, cudaMemcpyDeviceToHost, stream));
       CK(cudaMemcpyAsync(h + 1, dptr<char>(L.totals), 8, cudaMemcpyDeviceToHost, stream));
-      CK(cudaStreamSynchronize(stream));
+      wait();
       const uint32_t err = h[0];
       if (err & gpc::DEV_ERR_TIMEOUT) throw gpc::Error(GPC_ERR_TIMEOUT, "a bounded device wait timed out");
       if (err & gpc::DEV_ERR_COLLISION)
@@ -1034,14 +1067,14 @@ struct gpc_driver {
     if (ncirc() > 1) {
       CK(cudaMemcpyAsync(h, dptr<char>(L.cout) + (size_t)i * 8, i + 1 < ncirc() ? 16 : 8, cudaMemcpyDeviceToHost,
                          stream));
-      CK(cudaStreamSynchronize(stream));
+      wait();
       first = make_uint2(h[0], h[1]);
       if (i + 1 < ncirc()) next = make_uint2(h[2], h[3]);
     }
     // the closing offset of the whole run (offsets are positions in the run's target array)
     h[8] = NT;
     CK(cudaMemcpyAsync(dptr<char>(L.out_off) + (size_t)C * 4, h + 8, 4, cudaMemcpyHostToDevice, stream));
-    CK(cudaStreamSynchronize(stream));
+    wait();
     *probs = dptr<double>(L.out_prob) + first.x;
     *offsets = dptr<uint32_t>(L.out_off) + first.x;
     *targets = static_cast<const uint32_t *>(tgbuf.p);
@@ -1093,7 +1126,7 @@ struct gpc_driver {
     pin_out.ensure((size_t)ns * 8 * 7);
     double *h = static_cast<double *>(pin_out.p);
     CK(cudaMemcpyAsync(h, noise, (size_t)ns * 8, cudaMemcpyDeviceToHost, stream));
-    CK(cudaStreamSynchronize(stream));
+    wait();
     double *qt = h + ns, *st = h + 4 * (size_t)ns;
     for (uint32_t e = 0; e < ns; ++e) {
       const double p = h[e];
@@ -1158,13 +1191,13 @@ struct gpc_driver {
     A.grad_noise = grad_noise;
     CK(gpc::launch_adjoint(A, stream));
     signal_caller(caller);
-    CK(cudaStreamSynchronize(stream));
+    wait();
   }
 
   // Algorithmic bytes of each stage of the last run (walk, keys, bucket groups,
   // scan + emit): what the design must move, counted from the run's own sizes.
   void traffic(double out[4]) {
-    CK(cudaStreamSynchronize(stream));
+    wait();
     uint32_t tot[4] = {0, 0, 0, 0};
     uint32_t nonempty = 0;
     CK(cudaMemcpy(tot, dptr<char>(L.totals), 16, cudaMemcpyDeviceToHost));
@@ -1211,10 +1244,13 @@ struct gpc_driver {
     if (!ran) throw gpc::Error(GPC_ERR_INVALID, "nothing has been run");
     CK(cudaSetDevice(device));
     uint32_t C = 0, NT = 0;
+    const auto t3 = HostClock::now();
     if (finish(&C, &NT) == Finish::BatchFallback) {
       batch_fallback(outs);
       return;
     }
+    host_ms[3] = ms_since(t3);
+    const auto t4 = HostClock::now();
     const uint32_t N = ncirc();
     const size_t bytes = (size_t)C * 8 + (size_t)C * 4 + (size_t)NT * 4 + (size_t)N * 8 + 64;
     pin_out.ensure(bytes);
@@ -1226,7 +1262,9 @@ struct gpc_driver {
     }
     if (NT) CK(cudaMemcpyAsync(ht, tgbuf.p, (size_t)NT * 4, cudaMemcpyDeviceToHost, stream));
     if (N > 1) CK(cudaMemcpyAsync(hc, dptr<char>(L.cout), (size_t)N * 8, cudaMemcpyDeviceToHost, stream));
-    CK(cudaStreamSynchronize(stream));
+    wait();
+    host_ms[4] = ms_since(t4);
+    const auto t5 = HostClock::now();
     last_d2h = (uint64_t)C * 12 + (uint64_t)NT * 4 + 12 + (N > 1 ? (uint64_t)N * 8 : 0);
     const double *P = reinterpret_cast<const double *>(hp);
     const uint32_t *O = reinterpret_cast<const uint32_t *>(ho);
@@ -1267,6 +1305,7 @@ struct gpc_driver {
       outs.assign(N, nullptr);
       throw;
     }
+    host_ms[5] = ms_since(t5);
   }
 
   // A batch whose merge needs a fallback (a symptom repeated more than a
@@ -1920,6 +1959,8 @@ gpc_status gpc_server_create(const gpc_server_options *options, gpc_server **out
       d->device = sv->device;
       d->level = sv->level;
       d->pool_threads = std::max(1u, hw / o.slots);
+      d->pool_spin_us = 0;  // the lowering threads need the cores between a worker's hand-offs
+      d->blocking_wait = true;  // and while the GPU runs the worker's batch
       d->init_streams();
       d->admit = [raw, w](size_t grow, size_t total) { raw->acquire(w, grow, total); };
       sv->drivers.push_back(std::move(d));
@@ -1987,6 +2028,12 @@ void gpc_server_destroy(gpc_server *server) { delete server; }
 void gpc_driver_destroy(gpc_driver *driver) { delete driver; }
 
 void *gpc_driver_stream(gpc_driver *driver) { return driver ? (void *)driver->stream : nullptr; }
+
+gpc_status gpc_last_host_timings(gpc_driver *driver, double *ms6) {
+  if (!driver || !ms6) return fail(GPC_ERR_INVALID, "null argument");
+  for (int k = 0; k < 6; ++k) ms6[k] = driver->host_ms[k];
+  return GPC_OK;
+}
 
 gpc_status gpc_last_timings(gpc_driver *driver, float *ms5) {
   if (!driver || !ms5) return fail(GPC_ERR_INVALID, "null argument");

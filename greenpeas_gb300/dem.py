@@ -16,12 +16,42 @@ class DetectorErrorModel:
 
     def __init__(self, probs, offsets, targets, num_detectors: int, num_observables: int,
                  num_raw_mechanisms: int = 0):
-        self.probs = np.asarray(probs, dtype=np.float64)
-        self.offsets = np.asarray(offsets, dtype=np.uint32)
-        self.targets = np.asarray(targets, dtype=np.uint32)
+        self._arrays = (np.asarray(probs, dtype=np.float64), np.asarray(offsets, dtype=np.uint32),
+                        np.asarray(targets, dtype=np.uint32))
+        self._loader = None
         self._num_detectors = int(num_detectors)
         self._num_observables = int(num_observables)
         self.num_raw_mechanisms = int(num_raw_mechanisms)
+
+    @classmethod
+    def _deferred(cls, loader, num_detectors: int, num_observables: int, num_raw_mechanisms: int):
+        """A DEM whose arrays ``loader()`` returns as (probs, offsets, targets) views on first use
+        (the data already sits in host memory; only the views are deferred)."""
+        self = cls.__new__(cls)
+        self._arrays = None
+        self._loader = loader
+        self._num_detectors = int(num_detectors)
+        self._num_observables = int(num_observables)
+        self.num_raw_mechanisms = int(num_raw_mechanisms)
+        return self
+
+    def _views(self):
+        if self._arrays is None:
+            self._arrays = self._loader()
+            self._loader = None
+        return self._arrays
+
+    @property
+    def probs(self) -> np.ndarray:
+        return self._views()[0]
+
+    @property
+    def offsets(self) -> np.ndarray:
+        return self._views()[1]
+
+    @property
+    def targets(self) -> np.ndarray:
+        return self._views()[2]
 
     @property
     def num_errors(self) -> int:

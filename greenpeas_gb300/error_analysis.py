@@ -37,6 +37,30 @@ def _text(circuit) -> bytes:
     return str(circuit).encode()
 
 
+_as_utf8 = None
+
+
+def _text_ref(circuit):
+    """(address, length, keep-alive) of the circuit text's UTF-8 bytes, without a copy: bytes as
+    they are, a str through the UTF-8 buffer CPython keeps for it (for ASCII text, the str's own
+    storage).  The address is valid while the keep-alive object lives; the library only reads it.
+    None gives (None, 0, None)."""
+    global _as_utf8
+    if circuit is None:
+        return None, 0, None
+    if isinstance(circuit, bytes):
+        return ctypes.cast(ctypes.c_char_p(circuit), ctypes.c_void_p).value, len(circuit), circuit
+    text = circuit if isinstance(circuit, str) else str(circuit)
+    if _as_utf8 is None:
+        f = ctypes.pythonapi.PyUnicode_AsUTF8AndSize
+        f.restype = ctypes.c_void_p
+        f.argtypes = [ctypes.py_object, ctypes.POINTER(ctypes.c_ssize_t)]
+        _as_utf8 = f
+    n = ctypes.c_ssize_t()
+    addr = _as_utf8(text, ctypes.byref(n))
+    return addr, n.value, text
+
+
 def _stim_available() -> bool:
     try:
         import stim  # noqa: F401
@@ -59,15 +83,11 @@ class _DemHandle:
 
 
 def dem_from_handle(h: ctypes.c_void_p) -> DetectorErrorModel:
-    """Wraps a gpc_dem in a DetectorErrorModel without copying its arrays; the handle is
-    freed once the DEM and every array taken from it are gone."""
+    """Wraps a gpc_dem in a DetectorErrorModel without copying its arrays (numpy views over the
+    library's host arrays, made on first use); the handle is freed once the DEM and every array
+    taken from it are gone."""
     L = _native.lib()
     try:
-        offs = ctypes.POINTER(ctypes.c_uint32)()
-        tg = ctypes.POINTER(ctypes.c_uint32)()
-        pr = ctypes.POINTER(ctypes.c_double)()
-        n = ctypes.c_uint32()
-        _native.check(L.gpc_dem_arrays(h, ctypes.byref(offs), ctypes.byref(tg), ctypes.byref(pr), ctypes.byref(n)))
         nd, no = ctypes.c_uint32(), ctypes.c_uint32()
         raw = ctypes.c_uint64()
         _native.check(L.gpc_dem_info(h, ctypes.byref(nd), ctypes.byref(no), ctypes.byref(raw)))
@@ -75,12 +95,21 @@ def dem_from_handle(h: ctypes.c_void_p) -> DetectorErrorModel:
         L.gpc_dem_free(h)
         raise
     owner = _DemHandle(h)
-    ne = n.value
-    offsets = _owned(offs, ne + 1, np.uint32, owner)
-    nt = int(offsets[-1])
-    targets = _owned(tg, nt, np.uint32, owner)
-    probs = _owned(pr, ne, np.float64, owner)
-    return DetectorErrorModel(probs, offsets, targets, nd.value, no.value, raw.value)
+
+    def views():
+        offs = ctypes.POINTER(ctypes.c_uint32)()
+        tg = ctypes.POINTER(ctypes.c_uint32)()
+        pr = ctypes.POINTER(ctypes.c_double)()
+        n = ctypes.c_uint32()
+        _native.check(L.gpc_dem_arrays(owner.h, ctypes.byref(offs), ctypes.byref(tg), ctypes.byref(pr),
+                                       ctypes.byref(n)))
+        ne = n.value
+        offsets = _owned(offs, ne + 1, np.uint32, owner)
+        targets = _owned(tg, int(offsets[-1]), np.uint32, owner)
+        probs = _owned(pr, ne, np.float64, owner)
+        return probs, offsets, targets
+
+    return DetectorErrorModel._deferred(views, nd.value, no.value, raw.value)
 
 
 class _View:
@@ -145,8 +174,9 @@ class Driver:
         """Compiles ``circuit`` (or the driver's current circuit) to this package's DEM type."""
         L = _native.lib()
         out = ctypes.c_void_p()
-        text = _text(circuit)
-        _native.check(L.gpc_compile(self._h, text, len(text) if text else 0, ctypes.byref(out)))
+        addr, n, keep = _text_ref(circuit)
+        _native.check(L.gpc_compile(self._h, addr, n, ctypes.byref(out)))
+        del keep
         return dem_from_handle(out)
 
     def compile_detector_error_model(self, circuit=None):
@@ -156,10 +186,11 @@ class Driver:
 
     @staticmethod
     def _batch_args(circuits):
-        texts = [_text(c) for c in circuits]
-        n = len(texts)
-        arr = (ctypes.c_char_p * n)(*texts)
-        lens = (ctypes.c_size_t * n)(*[len(t) for t in texts])
+        refs = [_text_ref(c) for c in circuits]
+        n = len(refs)
+        arr = (ctypes.c_void_p * n)(*[r[0] for r in refs])
+        lens = (ctypes.c_size_t * n)(*[r[1] for r in refs])
+        arr._keep = refs  # the texts outlive the call that reads them
         return n, arr, lens
 
     def compile_batch(self, circuits) -> list:
@@ -223,8 +254,9 @@ class Driver:
 
     # device-resident stages
     def prepare(self, circuit=None) -> None:
-        text = _text(circuit)
-        _native.check(_native.lib().gpc_prepare(self._h, text, len(text) if text else 0))
+        addr, n, keep = _text_ref(circuit)
+        _native.check(_native.lib().gpc_prepare(self._h, addr, n))
+        del keep
 
     def run_device(self) -> None:
         _native.check(_native.lib().gpc_run_device(self._h))
@@ -238,6 +270,12 @@ class Driver:
         ms = (ctypes.c_float * 5)()
         _native.check(_native.lib().gpc_last_timings(self._h, ms))
         return dict(zip(("walk", "key", "sort", "merge", "total"), [float(x) for x in ms]))
+
+    def last_host_timings(self) -> dict:
+        """Host wall-clock phases (ms) of the last prepare and fetch."""
+        ms = (ctypes.c_double * 6)()
+        _native.check(_native.lib().gpc_last_host_timings(self._h, ms))
+        return dict(zip(("lower", "layout", "stage", "wait", "d2h", "split"), [float(x) for x in ms]))
 
     def last_sizes(self) -> dict:
         raw, pts = ctypes.c_uint64(), ctypes.c_uint64()

@@ -20,7 +20,7 @@ import time
 import numpy as np
 
 from . import _native
-from .error_analysis import _text, dem_from_handle
+from .error_analysis import _text_ref, dem_from_handle
 
 __all__ = ["Server", "replay"]
 
@@ -52,9 +52,10 @@ class Server:
             pass
 
     def submit(self, circuit) -> int:
-        text = _text(circuit)
+        addr, n, keep = _text_ref(circuit)
         t = ctypes.c_uint64()
-        _native.check(_native.lib().gpc_server_submit(self._h, text, len(text), ctypes.byref(t)))
+        _native.check(_native.lib().gpc_server_submit(self._h, addr, n, ctypes.byref(t)))  # copies the text
+        del keep
         return int(t.value)
 
     def result(self, ticket: int, timeout: float = 600.0, with_latency: bool = False):

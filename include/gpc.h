@@ -232,6 +232,14 @@ void *gpc_driver_stream(gpc_driver *driver);
  * the driver's stream): [0] walk, [1] key, [2] sort, [3] merge, [4] total. */
 gpc_status gpc_last_timings(gpc_driver *driver, float *ms5);
 
+/* Host wall-clock phases of the driver's last prepare and fetch, in
+ * milliseconds (no counterpart in the reference): [0] parse + lower (0 when
+ * the prepared tapes were reused), [1] layout and device buffer growth, [2]
+ * staging of the inputs into pinned memory, [3] waiting for the pipeline and
+ * its result sizes, [4] device-to-host copies of the DEM arrays, [5] splitting
+ * them into per-circuit DEMs. */
+gpc_status gpc_last_host_timings(gpc_driver *driver, double *ms6);
+
 /* Algorithmic bytes moved by each stage of the last run, counted from its
  * sizes: [0] walk (tape read + snapshots written), [1] key (records + snapshot
  * reads + keys, descriptors, target lists and bucket slots written), [2]

@@ -132,3 +132,12 @@ def test_persistent_walk_with_the_largest_batch_circuit():
     ref = gp.get_driver(circs[0], walk_queue=-1).compile_batch(circs)
     out = gp.get_driver(circs[0], walk_queue=1).compile_batch(circs)
     assert [a == b for a, b in zip(out, ref)] == [True] * len(circs)
+
+
+def test_host_timings_cover_prepare_and_fetch():
+    circs = _mixed()[:5]
+    drv = gp.get_driver(circs[0])
+    drv.compile_batch(circs)
+    t = drv.last_host_timings()
+    assert set(t) == {"lower", "layout", "stage", "wait", "d2h", "split"}
+    assert all(v >= 0 for v in t.values()) and t["lower"] > 0
