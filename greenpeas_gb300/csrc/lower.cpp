@@ -115,6 +115,10 @@ struct TextParser {
   const char *s, *e;
   size_t line = 1;
   Parsed *out;
+  // targets are written through this cursor into out->pool, sized up front:
+  // targets are separated by whitespace, so a text of n bytes holds at most
+  // n / 2 + 1 of them (a REPEAT body's are stored once)
+  uint32_t *tw = nullptr;
   // the gate of the previous instruction line (consecutive lines repeat names, e.g. DETECTOR)
   char last_name[40] = {0};
   size_t last_len = 0;
@@ -227,8 +231,8 @@ struct TextParser {
         fail(GPC_ERR_PARSE, std::string(g.name) + ": wrong number of arguments");
       in.nargs = (uint8_t)std::min(na, 3);
       for (int i = 0; i < in.nargs; ++i) in.args[i] = args[i];
-      in.t0 = (uint32_t)out->pool.size();
-      std::vector<uint32_t> &pool = out->pool;
+      uint32_t *const t0 = tw;
+      in.t0 = (uint32_t)(t0 - out->pool.data());
       while (true) {
         while (s < e && (*s == ' ' || *s == '\t')) ++s;
         if (s >= e) break;
@@ -239,7 +243,7 @@ struct TextParser {
           ++s;
           while (s < e && is_digit(*s)) q = q * 10u + (uint32_t)(*s++ - '0');
           if (s - d0 > 9 || q >= kMaxQubit) fail(GPC_ERR_CAPACITY, "qubit index too large");
-          pool.push_back((uint32_t)q);
+          *tw++ = (uint32_t)q;
           continue;
         }
         if (c0 == '\n' || c0 == '#' || c0 == '\r') break;
@@ -253,23 +257,23 @@ struct TextParser {
           uint32_t k = uint();
           if (s >= e || *s != ']' || k == 0) fail(GPC_ERR_PARSE, "bad record target");
           ++s;
-          pool.push_back(kRec | k);
+          *tw++ = kRec | k;
         } else if (*s == 'X' || *s == 'Y' || *s == 'Z' || *s == 'x' || *s == 'y' || *s == 'z') {
           char p = to_upper(*s++);
           uint32_t q = uint();
           if (q >= kMaxQubit) fail(GPC_ERR_CAPACITY, "qubit index too large");
-          pool.push_back(kPau | ((uint32_t)(p == 'X' ? 1 : p == 'Z' ? 2 : 3) << 24) | q);
+          *tw++ = kPau | ((uint32_t)(p == 'X' ? 1 : p == 'Z' ? 2 : 3) << 24) | q;
         } else if ((unsigned)(*s - '0') < 10u) {
           uint32_t q = uint();
           if (q >= kMaxQubit) fail(GPC_ERR_CAPACITY, "qubit index too large");
-          pool.push_back(q);
+          *tw++ = q;
         } else if (e - s >= 6 && memcmp(s, "sweep[", 6) == 0) {
           fail(GPC_ERR_UNSUPPORTED, "sweep targets are not supported");
         } else {
           fail(GPC_ERR_PARSE, "bad target");
         }
       }
-      in.tn = (uint32_t)out->pool.size() - in.t0;
+      in.tn = (uint32_t)(tw - t0);
       dst.push_back(in);
     }
   }
@@ -343,12 +347,18 @@ double split_dep2(double p) { return 0.5 - 0.5 * std::pow(1.0 - (16.0 * p) / 15.
 
 void parse_stim_into(const char *text, size_t len, Parsed &p) {
   p.ins.clear();
-  p.pool.clear();
   if (!text && len) throw Error(GPC_ERR_INVALID, "null circuit text");
-  p.pool.reserve(len / 3 + 16);
+  p.pool.resize(len / 2 + 16);  // the most targets a text of len bytes holds (not initialised)
   p.ins.reserve(len / 64 + 16);
   TextParser tp{text, text + len, 1, &p};
-  tp.block(p.ins, false, 0);
+  tp.tw = p.pool.data();
+  try {
+    tp.block(p.ins, false, 0);
+  } catch (...) {
+    p.pool.clear();
+    throw;
+  }
+  p.pool.resize((size_t)(tp.tw - p.pool.data()));
 }
 
 Parsed parse_stim(const char *text, size_t len) {

@@ -119,7 +119,7 @@ struct Instr {
 
 struct Parsed {
   std::vector<Instr> ins;
-  std::vector<uint32_t> pool;
+  HostArray<uint32_t> pool;  // targets of every instruction (a REPEAT body's once)
 };
 
 // Parses stim circuit text, flattening REPEAT blocks.  Throws gpc::Error.
