@@ -412,6 +412,7 @@ struct LowerScratch::Buffers {
     size_t nrec = 0, roff = 0;
     uint32_t nprov = 0, eoff = 0, poff = 0;
     std::vector<uint64_t> fine, coarse;  // per-qubit op signatures of the segment (qubit packing)
+    std::vector<uint64_t> snapbits;      // bit i: op oa + i of the segment's tape range is a snapshot
   };
   std::vector<Segment> segs;
   std::vector<size_t> cut;
@@ -1061,36 +1062,39 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
   remap.assign(nprov, kNone);
   std::atomic<bool> miscount{false};
   auto assemble = [&](uint32_t sg, uint32_t) {
-    const LowerScratch::Buffers::Segment &G = B.segs[sg];
+    LowerScratch::Buffers::Segment &G = B.segs[sg];
     const uint32_t ea = G.eoff, eb = G.eoff + (uint32_t)G.ep_k.size();
     const size_t oa = ea < nE ? T.ep_opoff[ea] : total, ob = eb < nE ? T.ep_opoff[eb] : total;
     if (ob > oa) memset(T.ops.data() + oa, 0, (ob - oa) * 8);
+    std::vector<uint64_t> &bits = G.snapbits;
+    bits.assign((ob - oa + 63) / 64, 0);
     const Entry *const ent0 = G.ent.p.get();
     for (size_t i = 0; i < G.nent; ++i) {
       const Entry &x = ent0[i];
       uint64_t op = x.op;
       const uint32_t opc = (uint32_t)(op & 0xFF);
-      if (opc == OP_C2 || opc >= OP_XPX)  // partner qubit -> partner slot
+      const size_t at = (size_t)T.ep_opoff[x.e + G.eoff] + (size_t)x.k() * T.qpad + slotOf[x.q()];
+      if (opc == OP_C2 || opc >= OP_XPX) {  // partner qubit -> partner slot
         op = (op & 0xFFFFFFFFull) | ((uint64_t)slotOf[(uint32_t)(op >> 32)] << 32);
-      else if (opc == OP_SNAP || opc == OP_SNAPD)  // segment-local point -> provisional point
+      } else if (opc == OP_SNAP || opc == OP_SNAPD) {  // segment-local point -> provisional point
         op += (uint64_t)G.poff << 32;
-      T.ops[(size_t)T.ep_opoff[x.e + G.eoff] + (size_t)x.k() * T.qpad + slotOf[x.q()]] = op;
-    }
-    for (uint32_t e = ea; e < eb; ++e) {
-      uint32_t next = T.ep_ptoff[e];
-      uint64_t *base = T.ops.data() + T.ep_opoff[e];
-      const size_t n = (size_t)T.ep_k[e] * T.qpad;
-      for (size_t i = 0; i < n; ++i) {
-        uint64_t &op = base[i];
-        const uint32_t opc = (uint32_t)(op & 0xFF);
-        if (opc == OP_SNAP || opc == OP_SNAPD) {
-          remap[(uint32_t)(op >> 32)] = next;
-          op = (op & 0xFFFFFFFFull) | ((uint64_t)next << 32);
-          ++next;
-        }
+        bits[(at - oa) >> 6] |= 1ull << ((at - oa) & 63);
       }
-      if (next != T.ep_ptoff[e + 1]) miscount = true;
+      T.ops[at] = op;
     }
+    // points in walk order = snapshot ops in tape order: number them by
+    // walking the set bits (the segment's epochs are consecutive in the tape)
+    uint32_t next = T.ep_ptoff[ea];
+    uint64_t *const base = T.ops.data() + oa;
+    for (size_t w = 0; w < bits.size(); ++w) {
+      for (uint64_t m = bits[w]; m; m &= m - 1) {
+        uint64_t &op = base[w * 64 + (size_t)__builtin_ctzll(m)];
+        remap[(uint32_t)(op >> 32)] = next;
+        op = (op & 0xFFFFFFFFull) | ((uint64_t)next << 32);
+        ++next;
+      }
+    }
+    if (next != T.ep_ptoff[eb]) miscount = true;
   };
   if (pool && nseg > 1 && total >= (1u << 16))
     pool->run(nseg, assemble);

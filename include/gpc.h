@@ -215,7 +215,8 @@ typedef struct gpc_server_options {
   uint32_t slots;            /* workers (resident drivers), default 4 */
   uint32_t max_batch;        /* circuits per batch, default 16 */
   uint64_t hbm_budget;       /* device bytes all workers' buffers may hold, default 120 GiB */
-  uint32_t lower_threads;    /* host threads lowering requests as they arrive (0 = one per core left after one per slot) */
+  uint32_t lower_threads;    /* host threads lowering requests as they arrive (0 = the cores left after one per
+                                slot, plus one: workers sleep while their batch runs) */
   uint32_t reserved[3];
 } gpc_server_options;
 gpc_status gpc_server_create(const gpc_server_options *options, gpc_server **out);
