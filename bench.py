@@ -331,7 +331,13 @@ def batched_leg(gp, torch, local: int, flush, steps: int, warmup: int, circuits:
     }
 
 
-def serving_leg(gp, requests: int, cap_requests: int, slots: int, max_batch: int, plain_sample: int) -> dict:
+def batch_workload_texts(circuits: int) -> list:
+    from greenpeas_gb300.workloads import batch_surface
+    return batch_surface()[:circuits]
+
+
+def serving_leg(gp, requests: int, cap_requests: int, slots: int, max_batch: int, plain_every: int = 10,
+                batch_texts=None, batch_plain_e2e=None) -> dict:
     """Continuous batching: capacity (a burst of requests queued at once), then a Poisson trace at 80% of it.
 
     Mix (seed 2): half rotated surface-code memory with d uniform in {5..25},
@@ -346,15 +352,26 @@ def serving_leg(gp, requests: int, cap_requests: int, slots: int, max_batch: int
     def materialise(reqs):  # request texts built before the timed replay (the harness is not measured)
         return [(t, f()) for t, f in reqs]
 
+    cap_reqs = materialise(mix.requests(cap_requests, 0.0))
+    on_batch = None
     with Server(slots=slots, max_batch=max_batch, hbm_budget=120 << 30) as srv:
         replay(srv, materialise(mix.requests(2 * slots * max_batch, 0.0)))  # warm every worker
-        cap = replay(srv, materialise(mix.requests(cap_requests, 0.0)))
+        cap = replay(srv, cap_reqs)
         rate = 0.8 * cap["dems_per_s"]
         tr = replay(srv, materialise(mix.requests(requests, rate)))
-    # the plain per-circuit path on the same mix: one driver, one circuit per compile
-    sample = mix.requests(plain_sample, 0.0)
-    drv = gp.get_driver(sample[0][1]())
-    texts = [f() for _, f in sample]
+        if batch_texts:
+            # the mixed-size batch workload served as requests (repeated to a
+            # burst of >= 1,024), against the plain path on the same circuits
+            reps = max(1, -(-1024 // len(batch_texts)))
+            bc = replay(srv, [(0.0, t) for _ in range(reps) for t in batch_texts])
+            on_batch = {"requests": bc["requests"], "dems_per_s": bc["dems_per_s"],
+                        "plain_e2e_dems_per_s": batch_plain_e2e,
+                        "speedup_vs_plain_e2e": bc["dems_per_s"] / batch_plain_e2e if batch_plain_e2e else None}
+    # the plain per-circuit path on the same mix: one driver, one circuit per
+    # compile, over every `plain_every`-th request of the capacity burst (a
+    # sample of the same size distribution)
+    texts = [t for _, t in cap_reqs[::plain_every]]
+    drv = gp.get_driver(texts[0])
     drv.compile(texts[0])
     t0 = time.perf_counter()
     for t in texts:
@@ -367,8 +384,10 @@ def serving_leg(gp, requests: int, cap_requests: int, slots: int, max_batch: int
         "trace": {"requests": tr["requests"], "offered_per_s": rate, "dems_per_s": tr["dems_per_s"],
                   "p50_ms": tr["p50_ms"], "p99_ms": tr["p99_ms"], "mean_ms": tr["mean_ms"], "max_ms": tr["max_ms"],
                   "batches": tr["stats"]["batches"], "budget_peak_bytes": tr["stats"]["budget_peak"]},
-        "plain_e2e_dems_per_s": plain, "plain_sample": len(texts),
+        "plain_e2e_dems_per_s": plain, "plain_sample": f"every {plain_every}th request of the capacity burst "
+                                                          f"({len(texts)})",
         "speedup_capacity_vs_plain_e2e": cap["dems_per_s"] / plain,
+        "on_batch_workload": on_batch,
     }
 
 
@@ -584,8 +603,11 @@ def main() -> None:
     if not args.no_serve and world == 1:
         # capacity from a burst long enough that filling and draining the
         # pipeline is a small part of it (1,000 requests: ~0.2 s, 5-15% low)
+        bl = line.get("batch") or {}
         line["serve"] = serving_leg(gp, args.serve_requests, max(200, min(3000, args.serve_requests // 3)),
-                                    args.serve_slots, args.serve_batch, plain_sample=100)
+                                    args.serve_slots, args.serve_batch,
+                                    batch_texts=batch_workload_texts(args.batch_circuits) if bl.get("plain") else None,
+                                    batch_plain_e2e=bl.get("plain", {}).get("e2e", {}).get("value"))
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(text)
     print(json.dumps(line), flush=True)
