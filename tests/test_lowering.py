@@ -102,3 +102,15 @@ def test_rejects_bad_input(bad, code):
     with pytest.raises(GpcError) as ei:
         Tape(bad)
     assert ei.value.status == code
+
+
+def test_text_reference_passes_utf8_without_copy():
+    """The Python layer hands text to the library as (address, length) of its UTF-8 bytes: a str
+    through CPython's UTF-8 buffer (non-ASCII text included), bytes as they are."""
+    import ctypes
+    from greenpeas_gb300.error_analysis import _text_ref
+    for text in ["H 0\nM 0\n", "# qubit é中\nH 0\n", b"CX 0 1\n", ""]:
+        addr, n, keep = _text_ref(text)
+        want = text if isinstance(text, bytes) else text.encode()
+        assert n == len(want) and ctypes.string_at(addr, n) == want
+    assert _text_ref(None) == (None, 0, None)
