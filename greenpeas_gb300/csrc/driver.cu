@@ -354,7 +354,7 @@ struct gpc_driver {
       c.rec = take(T.rec.size() * 8);
       c.rec_p = take(T.rec_p.size() * 8);
       c.rec_moff = take(T.rec_moff.size() * 4);
-      c.rec_src = take(T.rec_src.size() * 4);
+      c.rec_src = take(param ? T.rec_src.size() * 4 : 0);  // record sources: read by the gradient kernels only
       // buckets: about bucket_mean mechanisms each, a power of two between 2^4 and 2^18
       uint32_t bb = 4;
       while (bb < 18 && (bmean_of(T.M) << bb) < T.M) ++bb;
@@ -556,7 +556,7 @@ struct gpc_driver {
       put(l.rec, T.rec.data(), T.rec.size() * 8);
       put(l.rec_p, T.rec_p.data(), T.rec_p.size() * 8);
       put(l.rec_moff, T.rec_moff.data(), T.rec_moff.size() * 4);
-      put(l.rec_src, T.rec_src.data(), T.rec_src.size() * 4);
+      if (param) put(l.rec_src, T.rec_src.data(), T.rec_src.size() * 4);
       CircuitDev &c = cd[i];
       c = CircuitDev{};
       c.ops = dptr<uint64_t>(l.ops);
