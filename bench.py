@@ -210,7 +210,7 @@ def dem_arrays_equal(a, b) -> bool:
             and np.array_equal(a.targets, b.targets) and np.array_equal(a.probs, b.probs))
 
 
-def batched_leg(gp, torch, local: int, flush, steps: int, warmup: int, circuits: int = 256,
+def batched_leg(gp, torch, local: int, flush, steps: int, warmup: int, circuits: int = 256, walk_queue: int = 0,
                 device_only: bool = False) -> dict:
     """Mixed-size batch: one batched pipeline vs the plain per-circuit path on the same circuits.
 
@@ -224,7 +224,8 @@ def batched_leg(gp, torch, local: int, flush, steps: int, warmup: int, circuits:
     n = len(texts)
     dev = torch.device("cuda", local)
     if device_only:
-        bdrv = gp.get_driver(texts[0], device=local)
+        # walk_queue: 1 persistent walk launch, -1 per-class launches, 0 the default
+        bdrv = gp.get_driver(texts[0], device=local, walk_queue=walk_queue)
         bext = torch.cuda.ExternalStream(bdrv.stream, device=dev)
         bdrv.prepare_batch(texts)
         for _ in range(warmup):
@@ -455,6 +456,8 @@ def main() -> None:
     ap.add_argument("--no-plain", action="store_true", help="skip the headline single-circuit leg (profiling)")
     ap.add_argument("--batch-device-only", action="store_true", help="batch leg: time the batched pipeline alone")
     ap.add_argument("--batch-circuits", type=int, default=256)
+    ap.add_argument("--walk-queue", type=int, default=0, choices=(-1, 0, 1),
+                    help="batch leg with --batch-device-only: 1 one persistent walk launch, -1 per-class launches")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
     ap.add_argument("--no-grad", action="store_true", help="skip the noise-rate gradient leg")
     ap.add_argument("--serve-requests", type=int, default=10000)
@@ -484,7 +487,8 @@ def main() -> None:
         out = {"profiling": True}
         if not args.no_batch:
             out["batch"] = batched_leg(gp, torch, local, flush, steps=max(3, min(args.steps, 10)), warmup=args.warmup,
-                                       circuits=args.batch_circuits, device_only=args.batch_device_only)
+                                       circuits=args.batch_circuits, walk_queue=args.walk_queue,
+                                       device_only=args.batch_device_only)
         if rank == 0:
             print(json.dumps(out), flush=True)
         return
@@ -596,7 +600,7 @@ def main() -> None:
     # run reports the replicated headline only)
     if not args.no_batch and world == 1:
         line["batch"] = batched_leg(gp, torch, local, flush, steps=max(3, min(args.steps, 10)),
-                                    warmup=args.warmup, circuits=args.batch_circuits,
+                                    warmup=args.warmup, circuits=args.batch_circuits, walk_queue=args.walk_queue,
                                     device_only=args.batch_device_only)
     if not args.no_grad and world == 1:
         line["grad"] = grad_leg(gp, torch)
