@@ -28,7 +28,7 @@ EXPORTS = [
     "gpc_last_io_bytes", "gpc_merge_mechanisms_static", "gpc_prepare_batch", "gpc_fetch_batch",
     "gpc_param_prepare", "gpc_param_forward", "gpc_param_probs", "gpc_param_backward",
     "gpc_server_create", "gpc_server_submit", "gpc_server_wait", "gpc_server_stats", "gpc_server_destroy",
-    "gpc_device_dem", "gpc_autotune", "gpc_last_host_timings",
+    "gpc_device_dem", "gpc_autotune", "gpc_last_host_timings", "gpc_walk_form",
 ]
 
 
@@ -111,6 +111,7 @@ def lib() -> ctypes.CDLL:
     L.gpc_driver_stream.restype = vp
     L.gpc_last_timings.argtypes = [vp, ctypes.POINTER(ctypes.c_float)]
     L.gpc_last_host_timings.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
+    L.gpc_walk_form.argtypes = [vp, ctypes.POINTER(i32), ctypes.POINTER(i32)]
     L.gpc_last_sizes.argtypes = [vp, u64p, u64p, u32p, u32p, u32p]
     L.gpc_last_traffic.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
     L.gpc_last_io_bytes.argtypes = [vp, u64p, u64p]
@@ -140,7 +141,7 @@ def lib() -> ctypes.CDLL:
               "gpc_get_driver", "gpc_compile", "gpc_compile_batch", "gpc_dem_arrays", "gpc_dem_info",
               "gpc_dem_text", "gpc_prepare", "gpc_run_device", "gpc_fetch", "gpc_last_timings",
               "gpc_last_sizes", "gpc_tape_lower", "gpc_tape_get_view", "gpc_last_traffic", "gpc_last_io_bytes",
-              "gpc_merge_mechanisms_static", "gpc_prepare_batch", "gpc_fetch_batch", "gpc_last_host_timings"):
+              "gpc_merge_mechanisms_static", "gpc_prepare_batch", "gpc_fetch_batch", "gpc_last_host_timings", "gpc_walk_form"):
         getattr(L, f).restype = i32
     _lib = L
     return L

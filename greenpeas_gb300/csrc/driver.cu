@@ -2032,6 +2032,14 @@ void gpc_driver_destroy(gpc_driver *driver) { delete driver; }
 
 void *gpc_driver_stream(gpc_driver *driver) { return driver ? (void *)driver->stream : nullptr; }
 
+gpc_status gpc_walk_form(gpc_driver *driver, int32_t *launches, int32_t *persistent) {
+  if (!driver || !launches || !persistent) return fail(GPC_ERR_INVALID, "null argument");
+  if (!driver->prepared) return fail(GPC_ERR_INVALID, "no circuit prepared");
+  *launches = (int32_t)driver->L.classes.size();
+  *persistent = driver->L.classes.size() == 1 && driver->L.classes[0].queue ? 1 : 0;
+  return GPC_OK;
+}
+
 gpc_status gpc_last_host_timings(gpc_driver *driver, double *ms6) {
   if (!driver || !ms6) return fail(GPC_ERR_INVALID, "null argument");
   for (int k = 0; k < 6; ++k) ms6[k] = driver->host_ms[k];

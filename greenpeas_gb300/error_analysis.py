@@ -271,6 +271,12 @@ class Driver:
         _native.check(_native.lib().gpc_last_timings(self._h, ms))
         return dict(zip(("walk", "key", "sort", "merge", "total"), [float(x) for x in ms]))
 
+    def walk_form(self) -> dict:
+        """Walk launches per run of the prepared circuits and whether they form one persistent launch."""
+        n, q = ctypes.c_int32(), ctypes.c_int32()
+        _native.check(_native.lib().gpc_walk_form(self._h, ctypes.byref(n), ctypes.byref(q)))
+        return {"launches": n.value, "persistent": bool(q.value)}
+
     def last_host_timings(self) -> dict:
         """Host wall-clock phases (ms) of the last prepare and fetch."""
         ms = (ctypes.c_double * 6)()

@@ -241,6 +241,11 @@ gpc_status gpc_last_timings(gpc_driver *driver, float *ms5);
  * them into per-circuit DEMs. */
 gpc_status gpc_last_host_timings(gpc_driver *driver, double *ms6);
 
+/* Walk launches of the prepared circuits (no counterpart in the reference):
+ * `launches` per run (one per thread-count class, or 1), `persistent` 1 when
+ * the batch walks in one persistent launch off its work queue. */
+gpc_status gpc_walk_form(gpc_driver *driver, int32_t *launches, int32_t *persistent);
+
 /* Algorithmic bytes moved by each stage of the last run, counted from its
  * sizes: [0] walk (tape read + snapshots written), [1] key (records + snapshot
  * reads + keys, descriptors, target lists and bucket slots written), [2]

@@ -141,3 +141,22 @@ def test_host_timings_cover_prepare_and_fetch():
     t = drv.last_host_timings()
     assert set(t) == {"lower", "layout", "stage", "wait", "d2h", "split"}
     assert all(v >= 0 for v in t.values()) and t["lower"] > 0
+
+
+
+def test_walk_queue_option_selects_the_launch_form():
+    """walk_queue=1 prepares the persistent walk (one launch), walk_queue=-1 one launch per
+    thread-count class; the autotuner's choice is what the driver then prepares."""
+    from greenpeas_gb300.workloads import batch_surface
+    circs = batch_surface(n=6, seed=3, distances=(3, 9, 15))
+    forms = {}
+    for q in (1, -1):
+        drv = gp.get_driver(circs[0], walk_queue=q)
+        drv.prepare_batch(circs)
+        forms[q] = drv.walk_form()
+    assert forms[1] == {"launches": 1, "persistent": True}, forms
+    classes = len({gp.Tape(c).qpad for c in circs})  # one launch per distinct qubit-slot count
+    assert forms[-1] == {"launches": classes, "persistent": False}, forms
+    drv = gp.get_driver(circs[0])
+    tune = drv.autotune(circs, reps=1)
+    assert drv.walk_form()["persistent"] == bool(tune["walk_queue"])
