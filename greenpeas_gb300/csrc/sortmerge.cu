@@ -649,7 +649,7 @@ __global__ void __launch_bounds__(MERGE_THREADS) merge_kernel(MergeLaunch L) {
   }
   L.out_prob[slot] = p;
   L.out_off[slot] = toff;
-  if (toff + ntg <= L.tg_cap) {
+  if ((uint64_t)toff + ntg <= L.tg_cap) {
     const uint64_t d = __ldg(C.mdesc + m);
     uint32_t o = toff;
     for (uint32_t j = 0; j < w; ++j) {
@@ -775,18 +775,21 @@ __global__ void __launch_bounds__(BUCKET_THREADS) bucket_merge_kernel(BucketMerg
   }
   __syncthreads();
   // group heads, collision checks (full target lists), target counts
+  // A caller's list longer than the stride was reported (and cut to the
+  // stride) by the key pass; every read of a count here is cut the same way,
+  // so no list is read past its row.
   const uint32_t tcap = C.tcap;
   for (uint32_t s = threadIdx.x; s < n; s += NT) {
     const uint32_t i = ord[s];
     const uint32_t m = sm[i];
-    const uint32_t nt = __ldg(C.tn + m);
+    const uint32_t nt = min(__ldg(C.tn + m), tcap);
     bool head = true;
     if (s > 0) {
       const uint32_t ip = ord[s - 1];
       if (sk[ip].x == sk[i].x && sk[ip].y == sk[i].y) {
         head = false;
         const uint32_t mq = sm[ip];
-        if (__ldg(C.tn + mq) != nt ||
+        if (min(__ldg(C.tn + mq), tcap) != nt ||
             !lists_equal(C.tl + (size_t)m * tcap, C.tl + (size_t)mq * tcap, nt))
           atomicOr(L.err, DEV_ERR_COLLISION);
       }
@@ -835,7 +838,7 @@ __global__ void __launch_bounds__(BUCKET_THREADS) bucket_merge_kernel(BucketMerg
       if (b == L.nb - 1) {
         L.totals[0] = pc + carry_c;
         L.totals[1] = pt + carry_t;
-        if (pt + carry_t > L.tg_cap) atomicOr(L.err, DEV_FLAG_TG_OVF);
+        if ((uint64_t)pt + carry_t > L.tg_cap) atomicOr(L.err, DEV_FLAG_TG_OVF);
       }
     }
   }
@@ -856,7 +859,7 @@ __global__ void __launch_bounds__(BUCKET_THREADS) bucket_merge_kernel(BucketMerg
     }
     L.out_prob[slot] = p;
     L.out_off[slot] = toff;
-    if (toff + ntg <= L.tg_cap) {
+    if ((uint64_t)toff + ntg <= L.tg_cap) {
       const uint4 *src = reinterpret_cast<const uint4 *>(C.tl + (size_t)m * tcap);
       for (uint32_t k = 0; k * 4 < ntg; ++k) {
         const uint4 x = __ldg(src + k);
@@ -1276,7 +1279,7 @@ __global__ void __launch_bounds__(GW_WARPS * 32) emit_kernel(GroupLaunch L) {
     L.out_prob[slot] = t.p;
     L.out_off[slot] = toff;
     const uint32_t ntg = __ldg(L.tn + m);
-    if (toff + ntg <= L.tg_cap) {
+    if ((uint64_t)toff + ntg <= L.tg_cap) {
       const uint4 *src = reinterpret_cast<const uint4 *>(L.tl + (size_t)m * tcap);
       for (uint32_t k = 0; k * 4 < ntg; ++k) {
         const uint4 x = __ldg(src + k);

@@ -154,6 +154,9 @@ extern "C" gpc_status gpc_merge_mechanisms_static(const uint32_t *num_targets, c
     return GPC_ERR_INVALID;
   // target lists are read as 16-byte vectors
   if (stride % 4 != 0 || (reinterpret_cast<uintptr_t>(targets) & 15u) != 0) return GPC_ERR_INVALID;
+  // list lengths are cut to the stride, so n * stride bounds every target
+  // count and offset the kernels form in 32 bits
+  if ((uint64_t)n * stride > 0xFFFFFFFFull) return GPC_ERR_CAPACITY;
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || (uint32_t)dev >= kMaxDevices) return GPC_ERR_CUDA;
   char *base;

@@ -278,15 +278,19 @@ gpc_status gpc_last_sizes(gpc_driver *driver, uint64_t *raw, uint64_t *points, u
  *   out_probs[n], out_offsets[n + 1], out_targets[out_target_cap]  -- the
  *   merged DEM, as gpc_dem_arrays; result[4] = {errors, targets, flags, 0},
  *   flags != 0 means the output is not valid (1 timeout, 2 hash collision,
- *   8 out_target_cap too small, 16 one symptom repeated over 1024 times,
- *   64 a target list is longer than stride or not ascending).
+ *   8 out_target_cap too small: nothing is written past it, 16 more than
+ *   1024 mechanisms fell into one of the 1024 key buckets (for example one
+ *   symptom repeated over 1024 times; that bucket's errors are missing),
+ *   64 a target list is longer than stride (it is read cut to stride) or
+ *   not ascending).
  * Empty symptoms are dropped; equal symptoms are merged with
  * p <- p1(1-p2) + p2(1-p1).
  *
  * It calls no allocator: all scratch lives in a static device array of about
  * 2.3 MiB that every GPU loading the library keeps until exit, which limits n
- * to 65,536 (GPC_ERR_CAPACITY above that).  Every call on a device shares
- * that array, so calls that overlap on the GPU race: serialise them.  The
+ * to 65,536 and n * stride to 2^32 - 1 (GPC_ERR_CAPACITY above either).
+ * Every call on a device shares that array, so calls that overlap on the GPU
+ * race: serialise them.  The
  * first call on each device looks up the array's device address (make it
  * before any stream capture).  Returns once the work is queued. */
 gpc_status gpc_merge_mechanisms_static(const uint32_t *num_targets, const uint32_t *targets, uint32_t stride,

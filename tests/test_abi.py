@@ -40,3 +40,16 @@ def test_error_reporting_without_a_gpu():
     # tape lowering is host-only
     t = ctypes.c_void_p()
     assert L.gpc_tape_lower(b"FOO 0\n", 6, 2, ctypes.byref(t)) == -3
+
+
+def test_static_merge_rejects_a_stride_too_large_for_32_bit_counts():
+    import pytest
+
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("argument checks only: stand-in addresses must never reach a device")
+    L = _native.lib()
+    fake = ctypes.c_void_p(0x1000)  # non-null, 16-byte aligned, never dereferenced
+    # 8,192 mechanisms x stride 2^20 = 2^33 targets: more than 32-bit counts hold
+    st = L.gpc_merge_mechanisms_static(fake, fake, 1 << 20, fake, 1 << 13, fake, fake, fake, 0, fake, None)
+    assert st == -8  # GPC_ERR_CAPACITY, before any CUDA call

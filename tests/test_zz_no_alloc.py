@@ -87,3 +87,57 @@ def test_static_merge_rejects_too_many_mechanisms():
     null = ctypes.c_void_p(0)
     st = L.gpc_merge_mechanisms_static(null, null, 1, null, (1 << 16) + 1, null, null, null, 0, null, null)
     assert st == -8  # GPC_ERR_CAPACITY, checked before any device work
+
+
+def _static_call(tn, tl_rows, p, stride, cap, pad=16):
+    """Runs the allocation-free merge on small hand-made lists.
+
+    The target buffer carries `pad` sentinel entries past `cap`, and the row
+    buffer one spare row past the last mechanism, so a write past the
+    capacity or a read past a row shows up as a changed sentinel or a fault
+    the bounds of the buffers would not hide.  Returns (result, targets).
+    """
+    import torch
+
+    dev = torch.device("cuda", 0)
+    n = len(tn)
+    rows = np.zeros((n + 1, stride), dtype=np.uint32)
+    for m, r in enumerate(tl_rows):
+        rows[m, : min(len(r), stride)] = r[:stride]
+    d_tn = torch.from_numpy(np.asarray(tn, dtype=np.uint32).view(np.int32)).to(dev)
+    d_tl = torch.from_numpy(rows.reshape(-1).view(np.int32)).to(dev)
+    d_p = torch.tensor(p, dtype=torch.float64, device=dev)
+    out_p = torch.zeros(n, dtype=torch.float64, device=dev)
+    out_off = torch.zeros(n + 1, dtype=torch.int32, device=dev)
+    out_tg = torch.full((cap + pad,), -7, dtype=torch.int32, device=dev)
+    result = torch.zeros(4, dtype=torch.int32, device=dev)
+    st = _native.lib().gpc_merge_mechanisms_static(
+        ctypes.c_void_p(d_tn.data_ptr()), ctypes.c_void_p(d_tl.data_ptr()), stride,
+        ctypes.c_void_p(d_p.data_ptr()), n, ctypes.c_void_p(out_p.data_ptr()),
+        ctypes.c_void_p(out_off.data_ptr()), ctypes.c_void_p(out_tg.data_ptr()), cap,
+        ctypes.c_void_p(result.data_ptr()), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream))
+    assert st == 0
+    torch.cuda.synchronize()
+    return [int(x) for x in result.cpu()], out_tg.cpu().numpy()
+
+
+def test_static_merge_reports_a_small_target_buffer():
+    # 6 mechanisms, 5 distinct symptoms with 14 targets in all; room for 9
+    lists = [[1, 2, 3], [4, 5], [1, 2, 3], [6, 7, 8, 9], [10, 11], [12, 13, 14]]
+    tn = [len(r) for r in lists]
+    res, tg = _static_call(tn, lists, [1e-3] * 6, 4, cap=9)
+    assert res[2] & 8
+    assert res[1] == 14  # the count the caller would need
+    assert (tg[9:] == -7).all(), "written past out_target_cap"
+
+
+def test_static_merge_reports_a_list_longer_than_the_stride():
+    # mechanism 0 claims stride + 1 targets (not the last row); mechanism 2 is
+    # not ascending
+    lists = [[1, 2, 3, 4], [5, 6], [9, 7], [8]]
+    tn = [5, 2, 2, 1]
+    res, tg = _static_call(tn, lists, [1e-3] * 4, 4, cap=16)
+    assert res[2] & 64
+    assert (tg[16:] == -7).all(), "written past out_target_cap"
+    assert res[1] <= 16
+
