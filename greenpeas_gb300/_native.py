@@ -24,11 +24,12 @@ EXPORTS = [
     "gpc_get_driver", "gpc_compile", "gpc_compile_batch", "gpc_dem_arrays", "gpc_dem_info",
     "gpc_dem_text", "gpc_dem_free", "gpc_driver_destroy", "gpc_last_error", "gpc_prepare",
     "gpc_run_device", "gpc_fetch", "gpc_driver_stream", "gpc_last_timings", "gpc_last_sizes",
-    "gpc_tape_lower", "gpc_tape_get_view", "gpc_tape_free", "gpc_tape_last_error", "gpc_last_traffic",
+    "gpc_tape_lower", "gpc_tape_get_view", "gpc_tape_free", "gpc_tape_last_error", "gpc_tape_walk_segments",
+    "gpc_last_traffic",
     "gpc_last_io_bytes", "gpc_merge_mechanisms_static", "gpc_prepare_batch", "gpc_fetch_batch",
     "gpc_param_prepare", "gpc_param_forward", "gpc_param_probs", "gpc_param_backward",
     "gpc_server_create", "gpc_server_submit", "gpc_server_wait", "gpc_server_stats", "gpc_server_destroy",
-    "gpc_device_dem", "gpc_autotune", "gpc_last_host_timings", "gpc_walk_form",
+    "gpc_device_dem", "gpc_autotune", "gpc_last_host_timings", "gpc_walk_form", "gpc_walk_segments",
 ]
 
 
@@ -49,7 +50,7 @@ class ServerOptions(ctypes.Structure):
 class Options(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("sort_bits", ctypes.c_int32), ("global_sort", ctypes.c_int32),
                 ("walk_qpt", ctypes.c_int32), ("bucket_mean", ctypes.c_int32), ("walk_words", ctypes.c_int32),
-                ("key_split", ctypes.c_int32), ("walk_queue", ctypes.c_int32)]
+                ("key_split", ctypes.c_int32), ("walk_queue", ctypes.c_int32), ("walk_segment", ctypes.c_int32)]
 
 
 class TuningEntry(ctypes.Structure):
@@ -121,6 +122,8 @@ def lib() -> ctypes.CDLL:
     L.gpc_autotune.argtypes = [vp, ctypes.POINTER(vp), ctypes.POINTER(sz), i32, i32, ctypes.POINTER(Tuning)]
     L.gpc_tape_lower.argtypes = [ctypes.c_char_p, sz, i32, ctypes.POINTER(vp)]
     L.gpc_tape_get_view.argtypes = [vp, ctypes.POINTER(TapeView)]
+    L.gpc_tape_walk_segments.argtypes = [vp, u32, u32p, u32, u32p]
+    L.gpc_walk_segments.argtypes = [vp, u32p, u32p, u32p]
     L.gpc_tape_free.argtypes = [vp]
     L.gpc_tape_free.restype = None
     L.gpc_tape_last_error.restype = ctypes.c_char_p
@@ -141,7 +144,8 @@ def lib() -> ctypes.CDLL:
               "gpc_get_driver", "gpc_compile", "gpc_compile_batch", "gpc_dem_arrays", "gpc_dem_info",
               "gpc_dem_text", "gpc_prepare", "gpc_run_device", "gpc_fetch", "gpc_last_timings",
               "gpc_last_sizes", "gpc_tape_lower", "gpc_tape_get_view", "gpc_last_traffic", "gpc_last_io_bytes",
-              "gpc_merge_mechanisms_static", "gpc_prepare_batch", "gpc_fetch_batch", "gpc_last_host_timings", "gpc_walk_form"):
+              "gpc_merge_mechanisms_static", "gpc_prepare_batch", "gpc_fetch_batch", "gpc_last_host_timings", "gpc_walk_form",
+              "gpc_tape_walk_segments", "gpc_walk_segments"):
         getattr(L, f).restype = i32
     _lib = L
     return L

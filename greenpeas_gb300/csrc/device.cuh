@@ -98,6 +98,60 @@ struct WalkLaunch {
 };
 cudaError_t launch_walk(const WalkLaunch &L, cudaStream_t s);
 cudaError_t walk_set_smem_limit();  // call once per device before launching walks
+
+// ---- segmented walk (one circuit) -------------------------------------------
+// The epochs are cut into time segments s = [b_s, b_{s+1}) at clean cuts
+// (walk_segment_bounds, lower.hpp).  A word whose walk spans segments s0..K
+// (K: the last segment for words holding observables, else the one holding
+// the word's last measurement) runs as
+//   launch A: SEG_FIRST  -- [e0, b_{s0+1}) from zero rows, with snapshots; exit rows -> a state;
+//             SEG_AFF    -- each segment s in (s0, K) holding measurements of the word,
+//                           from zero rows, no snapshots; exit rows -> a state (c_s);
+//             SEG_XFER   -- per segment s and 64-row column c, the walk of unit rows
+//                           without measurement bits: column c of the transfer matrix A_s;
+//   launch B: SEG_REST   -- segment s in (s0, K]: entry rows composed from the
+//                           first part's exit through A and c of segments
+//                           (s0, s), then the segment walked with snapshots
+//                           (the last one on to the end, or until the rows vanish).
+// A word that spans one segment is a single SEG_FIRST item walking to the end.
+// States are [2 qpad] u64 rows: X of slots 0..qpad-1, then Z of the same slots.
+enum : uint32_t { SEG_FIRST = 0, SEG_AFF = 1, SEG_XFER = 2, SEG_REST = 3 };
+// Entries of a transfer row kept as a sparse list (rows with more are read
+// from the dense transfer columns): measured on code circuits, rows hold 1-3
+// entries on average and up to 12 where a cut falls inside a round.
+constexpr uint32_t kSegRowCap = 16;
+// Most compose steps a REST item keeps in flight (shared-memory ring).
+constexpr uint32_t kSegRingMax = 4;
+struct SegItem {
+  uint32_t kind;
+  uint32_t idx;             // word (SEG_XFER: transfer column)
+  uint32_t e_begin, e_end;  // epochs walked
+  uint32_t state;           // FIRST/AFF/XFER: state written at exit (0xFFFFFFFF: none); REST: entry state
+  uint32_t s_from, s_to;    // REST: compose through segments [s_from, s_to) before walking; XFER: s_from
+                            // is the segment
+  uint32_t pad;
+};
+static_assert(sizeof(SegItem) == 32, "segment item is 32 bytes");
+struct SegLaunch {
+  const CircuitDev *circ;   // the circuit
+  const SegItem *items;
+  uint32_t n_items;
+  uint32_t threads, qpt, qpad;
+  uint32_t chunk_cap, max_epochs, max_chunks;
+  uint64_t *state;          // [states][2 qpad]
+  uint32_t xfer0;           // state of segment s's transfer column c: xfer0 + s * ncol + c
+  uint32_t ncol;            // 64-row columns of a transfer matrix: ceil(2 qpad / 64)
+  const uint32_t *aff;      // [w][S] state of word j's SEG_AFF walk of segment s (0xFFFFFFFF: no measurements)
+  uint32_t S;
+  uint32_t *xcnt;           // [S][2 qpad] (zeroed) entries of each transfer row
+  uint16_t *xlst;           // [S][2 qpad][kSegRowCap] the entries
+  uint32_t ring_nb;         // compose step buffers of a REST CTA (launch B; 0 in launch A)
+  uint32_t *err;
+};
+// Dynamic shared memory of a segment launch (0: it does not fit a CTA).
+size_t walk_seg_smem_bytes(const SegLaunch &L);
+cudaError_t launch_walk_seg(const SegLaunch &L, cudaStream_t s);
+bool walk_seg_supported(uint32_t qpt);
 // Staged epoch/chunk table bytes for a launch (0: the tables are read from global memory).
 uint32_t walk_table_bytes(uint32_t max_epochs, uint32_t max_chunks);
 size_t walk_smem_bytes(uint32_t qpad, uint32_t chunk_cap, uint32_t table_bytes, uint32_t words);

@@ -135,6 +135,7 @@ struct Layout {
   size_t src_off, src_rec, gq, grad_rec, ptab;  // noise-rate gradients (single circuit)
   size_t gzero, sort_scr, merge_status, merge_ctr, gzero_bytes;
   size_t out_prob, out_off;
+  size_t seg_items, seg_aff, seg_state, seg_xcnt, seg_xlst;  // segmented walk (single circuit)
   size_t total;
   uint32_t M, nb, n_items;
   uint32_t sort_tiles, merge_tiles;
@@ -207,6 +208,17 @@ struct gpc_driver {
   uint32_t batch_queue = 0;                  // 1: batches walk in one persistent launch (autotune's choice)
   int walk_queue = 0;                        // option walk_queue: 1 always, -1 never, 0 batch_queue
   bool key_split = true;                     // split key pass for one circuit when it pays (option key_split)
+  int walk_segment = 0;                      // option walk_segment: 0 when it pays, -1 never, > 0 target cost
+  // Segmented walk of the current circuit (single circuits; plan_segments):
+  // the cut epochs, launch A's items then launch B's, each word's AFF state
+  // per segment, and the state buffer's size.
+  bool seg_on = false;
+  std::vector<uint32_t> seg_bounds;
+  std::vector<gpc::SegItem> seg_items;
+  uint32_t seg_na = 0, seg_nb = 0;
+  std::vector<uint32_t> seg_aff;  // [w][S]
+  uint32_t seg_states = 0, seg_xfer0 = 0, seg_ncol = 0, seg_qpt = 1, seg_ring = 1;
+  bool seg_band_reset = false;    // a word without measurements: its band is zeroed before the walk
   // host phases of the last prepare / fetch (ms): lower, layout, staging,
   // wait for the pipeline + result sizes, D2H copies, DEM split
   double host_ms[6] = {};
@@ -373,6 +385,8 @@ struct gpc_driver {
     L.items = take((size_t)items * sizeof(uint2));
     L.mbase = take((size_t)(N + 1) * 4);
     L.cbbase = take((size_t)N * 4);
+    L.seg_items = take(seg_on ? seg_items.size() * sizeof(gpc::SegItem) : 0);
+    L.seg_aff = take(seg_on ? seg_aff.size() * 4 : 0);
     if (param) {
       L.src_off = take(((size_t)tapes[0].n_ticks * gpc::SRC_CLASSES + 1) * 4);
       L.src_rec = take(tapes[0].rec.size() * 4);
@@ -404,9 +418,13 @@ struct gpc_driver {
     L.tsum = take(((size_t)nb + gpc::SCAN_TILE - 1) / gpc::SCAN_TILE * 8);
     for (uint32_t i = 0; i < N; ++i)
       L.c[i].nzm = take((size_t)tapes[i].npoints * ((tapes[i].w + 63) / 64) * 8);
+    const size_t seg_rows = seg_on ? (seg_bounds.size() - 1) * (size_t)2 * tapes[0].qpad : 0;
+    L.seg_xcnt = take(seg_rows * 4);
     L.zero_bytes = o - L.zero;
     L.out_prob = take((size_t)M * 8);
     L.out_off = take((size_t)(M + 1) * 4);
+    L.seg_state = take(seg_on ? (size_t)seg_states * 2 * tapes[0].qpad * 8 : 0);
+    L.seg_xlst = take(seg_rows * gpc::kSegRowCap * 2);
     // global path (single circuit only)
     const uint32_t Mg = N == 1 ? (uint32_t)M : 0;
     L.sk0 = take((size_t)Mg * 8);
@@ -600,6 +618,10 @@ struct gpc_driver {
     put(L.mbase, mb.data(), mb.size() * 4);
     put(L.cbbase, cb.data(), cb.size() * 4);
     put(L.items, walk_items.data(), walk_items.size() * sizeof(uint2));
+    if (seg_on) {
+      put(L.seg_items, seg_items.data(), seg_items.size() * sizeof(gpc::SegItem));
+      put(L.seg_aff, seg_aff.data(), seg_aff.size() * 4);
+    }
     if (param) {
       // records of each (tick, class) source, in record order
       const Tape &T = tapes[0];
@@ -673,6 +695,7 @@ struct gpc_driver {
       host_ms[0] = 0;
     }
     const auto t1 = HostClock::now();
+    plan_segments();
     layout();
     // The stream may still be reading the old arena: finish before regrowing.
     wait();
@@ -718,6 +741,15 @@ struct gpc_driver {
       mix(c.queue);
     }
     mix(split_word());
+    mix((uint64_t)seg_on);
+    if (seg_on) {
+      mix(seg_na);
+      mix(seg_nb);
+      mix(seg_states);
+      mix(seg_qpt);
+      mix(seg_ring);
+      for (uint32_t b : seg_bounds) mix(b);
+    }
     cfg_sig = h;
     prepared = true;
   }
@@ -799,12 +831,200 @@ struct gpc_driver {
     }
   }
 
+  // ---- segmented walk (one circuit) ----------------------------------------
+  // Auto policy: segments of about kSegTarget cost units (an epoch costs its
+  // slots + 2), taken when the longest word walk is at least kSegMinSpan
+  // segments long.  Measured on GB300 (walk stage, L2 flushed between runs):
+  // [[144,12,12]] r12 77 -> 41 us at 32 (16: 53, 48: 42), surface d = 7 61 ->
+  // 34, d = 11 86 -> 41, [[72,12,6]] 42 -> 30, [[288,12,18]] 129 -> 77 (48:
+  // 69); surface d = 3 walks 17 epochs and stays whole (segmenting it costs
+  // 2-5 us).  A compose step costs about 1 us (instruction latency of one CTA
+  // over a sparse transfer matrix), a segment epoch about 0.8 us.  Segment
+  // walks copy the tape in chunks of at most kSegChunk bytes that never cross
+  // a cut, so several segment CTAs share an SM and a segment's first copy is
+  // short.
+  static constexpr uint32_t kSegTarget = 32;
+  static constexpr uint32_t kSegMinSpan = 3;
+  static constexpr uint32_t kSegChunk = 24 * 1024;
+  // A detector word's rows vanish some epochs after its last measurement
+  // (the walk reaches the resets of the qubits they sit on); its segments
+  // reach this many epochs past that measurement, the last one walking on.
+  static constexpr uint32_t kSegTail = 12;
+
+  // Chunks of whole epochs of at most the chunk capacity, cut at every bound.
+  static void rechunk_at(Tape &T, const std::vector<uint32_t> &bounds, uint32_t cap_want) {
+    const uint32_t nE = T.n_epochs;
+    uint64_t big = 0;
+    for (uint32_t e = 0; e < nE; ++e) big = std::max<uint64_t>(big, (uint64_t)T.ep_k[e] * T.qpad * 8);
+    const uint64_t want = std::max<uint64_t>((big + 255) & ~(uint64_t)255, cap_want);
+    T.chunk_cap = (uint32_t)std::min<uint64_t>(gpc::walk_chunk_cap(T.qpad), want);
+    T.ep_chunk.assign(nE, 0);
+    T.ch_off.clear();
+    T.ch_bytes.clear();
+    for (size_t s = 0; s + 1 < bounds.size(); ++s) {
+      for (uint32_t e = bounds[s]; e < bounds[s + 1];) {
+        const uint32_t c = (uint32_t)T.ch_off.size();
+        uint64_t bytes = 0;
+        uint32_t f = e;
+        while (f < bounds[s + 1] && bytes + (uint64_t)T.ep_k[f] * T.qpad * 8 <= T.chunk_cap) {
+          bytes += (uint64_t)T.ep_k[f] * T.qpad * 8;
+          T.ep_chunk[f] = c;
+          ++f;
+        }
+        T.ch_off.push_back(T.ep_opoff[e]);
+        T.ch_bytes.push_back((uint32_t)bytes);
+        e = f;
+      }
+    }
+  }
+
+  // Decides whether the single circuit's walk runs in segments and builds
+  // the items of the two launches (device.cuh, SEG_*).
+  void plan_segments() {
+    seg_on = false;
+    seg_band_reset = false;
+    if (ncirc() != 1 || walk_segment < 0) return;
+    Tape &T = tapes[0];
+    const uint32_t nE = T.n_epochs;
+    if (nE < 2 || T.w == 0) return;
+    const uint32_t q = walk_qpt_for(T.qpad, walk_qpt);
+    if (!gpc::walk_seg_supported(q) || !walk_qpt_fits(T.qpad, q)) return;
+    std::vector<uint64_t> cum(nE + 1, 0);  // cost of epochs [0, e)
+    for (uint32_t e = 0; e < nE; ++e) cum[e + 1] = cum[e] + gpc::walk_epoch_cost(T.ep_k[e]);
+    auto holds_obs = [&](uint32_t j) { return (uint64_t)(j + 1) * 64 > T.ndet; };
+    uint64_t longest = 0;
+    for (uint32_t j = 0; j < T.w; ++j) {
+      const uint32_t lo = T.inj_lo[j];
+      if (lo == gpc::kNone || lo >= nE) continue;
+      const uint32_t hi = holds_obs(j) ? nE : std::min(nE, T.inj_hi[j] + 1);
+      longest = std::max<uint64_t>(longest, cum[hi] - cum[lo]);
+    }
+    const uint32_t target = walk_segment > 0 ? (uint32_t)walk_segment : kSegTarget;
+    if (walk_segment == 0 && longest < (uint64_t)kSegMinSpan * target) return;
+    gpc::walk_segment_bounds(T, target, seg_bounds);
+    const uint32_t S = (uint32_t)seg_bounds.size() - 1;
+    if (S < 2) return;
+    const std::vector<uint32_t> &b = seg_bounds;
+    auto seg_of = [&](uint32_t e) {
+      return (uint32_t)(std::upper_bound(b.begin(), b.end(), e) - b.begin()) - 1;
+    };
+    seg_qpt = q;
+    seg_ncol = (2 * T.qpad + 63) / 64;
+    seg_aff.assign((size_t)T.w * S, gpc::kNone);
+    std::vector<gpc::SegItem> A, B;
+    std::vector<char> need_xfer(S, 0);
+    uint32_t states = 0;
+    for (uint32_t j = 0; j < T.w; ++j) {
+      const uint32_t e0 = T.inj_lo[j];
+      if (e0 == gpc::kNone || e0 >= nE) {
+        seg_band_reset = true;  // no item writes this word's band
+        continue;
+      }
+      const uint32_t elast = T.inj_hi[j];
+      const uint32_t s0 = seg_of(e0);
+      const uint32_t K = holds_obs(j) ? S - 1 : std::max(s0, seg_of(std::min(nE - 1, elast + kSegTail)));
+      if (K == s0) {
+        A.push_back(gpc::SegItem{gpc::SEG_FIRST, j, e0, nE, gpc::kNone, 0, 0, 0});
+        continue;
+      }
+      const uint32_t ent = states++;
+      A.push_back(gpc::SegItem{gpc::SEG_FIRST, j, e0, b[s0 + 1], ent, 0, 0, 0});
+      for (uint32_t s = s0 + 1; s < K; ++s) {
+        need_xfer[s] = 1;
+        if (b[s] <= elast) {
+          seg_aff[(size_t)j * S + s] = states;
+          A.push_back(gpc::SegItem{gpc::SEG_AFF, j, b[s], b[s + 1], states++, 0, 0, 0});
+        }
+      }
+      for (uint32_t s = s0 + 1; s <= K; ++s)
+        B.push_back(gpc::SegItem{gpc::SEG_REST, j, b[s], s == K ? nE : b[s + 1], ent, s0 + 1, s, 0});
+    }
+    seg_xfer0 = states;
+    for (uint32_t s = 0; s < S; ++s)
+      if (need_xfer[s])
+        for (uint32_t c = 0; c < seg_ncol; ++c)
+          A.push_back(gpc::SegItem{gpc::SEG_XFER, c, b[s], b[s + 1], seg_xfer0 + s * seg_ncol + c, s, 0, 0});
+    seg_states = seg_xfer0 + S * seg_ncol;
+    rechunk_at(T, seg_bounds, kSegChunk);
+    // compose ring: as many step buffers (2 to kSegRingMax: step k + 1 is copied while step k is
+    // composed) as the REST CTA's shared memory holds
+    uint32_t max_steps = 0;
+    for (const auto &it : B) max_steps = std::max(max_steps, it.s_to - it.s_from);
+    seg_ring = 0;
+    for (uint32_t nb = std::min(gpc::kSegRingMax, std::max(2u, max_steps)); nb >= 2; --nb) {
+      gpc::SegLaunch probe{};
+      probe.qpad = T.qpad;
+      probe.chunk_cap = T.chunk_cap;
+      probe.max_epochs = nE;
+      probe.max_chunks = (uint32_t)T.ch_off.size();
+      probe.S = S;
+      probe.ring_nb = nb;
+      if (gpc::walk_seg_smem_bytes(probe)) {
+        seg_ring = nb;
+        break;
+      }
+    }
+    if (seg_ring == 0) {  // no room for a compose step: the plain walk, with the tape's usual chunks
+      rechunk_at(T, {0u, nE}, 0xFFFFFFFFu);
+      return;
+    }
+    // longest items first (launch order is the order CTAs start in)
+    auto span = [&](const gpc::SegItem &it) {
+      return cum[it.e_end] - cum[it.e_begin] + (it.kind == gpc::SEG_REST ? 8ull * (it.s_to - it.s_from) : 0ull);
+    };
+    auto longer = [&](const gpc::SegItem &x, const gpc::SegItem &y) { return span(x) > span(y); };
+    std::stable_sort(A.begin(), A.end(), longer);
+    std::stable_sort(B.begin(), B.end(), longer);
+    seg_na = (uint32_t)A.size();
+    seg_nb = (uint32_t)B.size();
+    seg_items = std::move(A);
+    seg_items.insert(seg_items.end(), B.begin(), B.end());
+    seg_on = true;
+  }
+
+  // Launch A (first parts, AFF and transfer walks) then launch B (the rest
+  // of every segmented word) on the main stream; the key-block table beside
+  // them on an auxiliary stream.
+  void launch_walks_seg(const gpc::KeyLaunch &kl) {
+    const Tape &T = tapes[0];
+    CK(cudaEventRecord(fork_ev, stream));
+    CK(cudaStreamWaitEvent(aux[0], fork_ev, 0));
+    CK(gpc::launch_key_prep(kl, aux[0]));
+    CK(cudaEventRecord(join_ev[0], aux[0]));
+    if (seg_band_reset) CK(cudaMemsetAsync(dptr<char>(L.c[0].band), 0, (size_t)T.w * 8, stream));
+    gpc::SegLaunch sl{};
+    sl.circ = dptr<CircuitDev>(L.cdev);
+    sl.items = dptr<gpc::SegItem>(L.seg_items);
+    sl.n_items = seg_na;
+    sl.qpt = seg_qpt;
+    sl.qpad = T.qpad;
+    sl.threads = T.qpad / seg_qpt;
+    sl.chunk_cap = T.chunk_cap;
+    sl.max_epochs = T.n_epochs;
+    sl.max_chunks = (uint32_t)T.ch_off.size();
+    sl.state = dptr<uint64_t>(L.seg_state);
+    sl.xfer0 = seg_xfer0;
+    sl.ncol = seg_ncol;
+    sl.aff = dptr<uint32_t>(L.seg_aff);
+    sl.S = (uint32_t)seg_bounds.size() - 1;
+    sl.xcnt = dptr<uint32_t>(L.seg_xcnt);
+    sl.xlst = dptr<uint16_t>(L.seg_xlst);
+    sl.err = dptr<uint32_t>(L.err);
+    sl.ring_nb = 0;
+    CK(gpc::launch_walk_seg(sl, stream));
+    sl.items += seg_na;
+    sl.n_items = seg_nb;
+    sl.ring_nb = seg_ring;
+    CK(gpc::launch_walk_seg(sl, stream));
+    CK(cudaStreamWaitEvent(stream, join_ev[0], 0));
+  }
+
   // First word of a split key pass, or kNoSplit.  One circuit with target
   // lists whose observables sit in words after some detector-only words: the
   // observables never vanish, so their walk covers every epoch, while the
   // detector words stop early; their keys are computed beside that walk.
   uint32_t split_word() const {
-    if (!key_split || ncirc() != 1 || force_global || lists_off || tcap == 0 || L.classes.size() != 1)
+    if (!key_split || seg_on || ncirc() != 1 || force_global || lists_off || tcap == 0 || L.classes.size() != 1)
       return gpc::kNoSplit;
     const Tape &T = tapes[0];
     if (T.nobs == 0 || T.n_epochs == 0) return gpc::kNoSplit;
@@ -863,7 +1083,11 @@ struct gpc_driver {
     gpc::KeyLaunch kl = key_launch(param || (ncirc() == 1 && (force_global || lists_off)));
     const uint32_t late = split_word();
     rec(0);
-    if (late == gpc::kNoSplit) {
+    if (seg_on) {
+      launch_walks_seg(kl);
+      rec(1);
+      CK(gpc::launch_keys(kl, stream));
+    } else if (late == gpc::kNoSplit) {
       launch_walks(kl);
       rec(1);
       CK(gpc::launch_keys(kl, stream));
@@ -1410,6 +1634,7 @@ struct gpc_driver {
       d->batch_qpt = batch_qpt;
       d->batch_queue = batch_queue;
       d->walk_queue = walk_queue;
+      d->walk_segment = walk_segment;
       d->init_streams();
       partner = std::move(d);
     }
@@ -1752,6 +1977,8 @@ gpc_status gpc_get_driver(const char *stim_text, size_t len, int32_t correlation
     d->key_split = options->key_split == 0;
     if (options->walk_queue < -1 || options->walk_queue > 1) return fail(GPC_ERR_INVALID, "walk_queue must be -1, 0 or 1");
     d->walk_queue = options->walk_queue;
+    if (options->walk_segment < -1) return fail(GPC_ERR_INVALID, "walk_segment must be -1, 0 or positive");
+    d->walk_segment = options->walk_segment;
   }
   gpc_status st = guarded([&] {
     int n = 0;
@@ -2037,6 +2264,15 @@ gpc_status gpc_walk_form(gpc_driver *driver, int32_t *launches, int32_t *persist
   if (!driver->prepared) return fail(GPC_ERR_INVALID, "no circuit prepared");
   *launches = (int32_t)driver->L.classes.size();
   *persistent = driver->L.classes.size() == 1 && driver->L.classes[0].queue ? 1 : 0;
+  return GPC_OK;
+}
+
+gpc_status gpc_walk_segments(gpc_driver *driver, uint32_t *segments, uint32_t *items_first, uint32_t *items_rest) {
+  if (!driver || !segments || !items_first || !items_rest) return fail(GPC_ERR_INVALID, "null argument");
+  if (!driver->prepared) return fail(GPC_ERR_INVALID, "no circuit prepared");
+  *segments = driver->seg_on ? (uint32_t)driver->seg_bounds.size() - 1 : 0u;
+  *items_first = driver->seg_on ? driver->seg_na : 0u;
+  *items_rest = driver->seg_on ? driver->seg_nb : 0u;
   return GPC_OK;
 }
 

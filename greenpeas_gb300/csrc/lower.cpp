@@ -342,6 +342,34 @@ struct SplitCache {
 
 }  // namespace
 
+bool walk_clean_cut(const Tape &T, uint32_t e) {
+  if (e == 0 || e >= T.n_epochs) return false;
+  const uint64_t *op = T.ops.data() + T.ep_opoff[e];  // slot 0 of epoch e
+  for (uint32_t s = 0; s < T.qpad; ++s) {
+    const uint32_t opc = (uint32_t)op[s] & 0xFFu;
+    if (opc == OP_INJ || opc == OP_M || opc == OP_SNAPD) return false;
+  }
+  return true;
+}
+
+void walk_segment_bounds(const Tape &T, uint32_t target, std::vector<uint32_t> &bounds) {
+  const uint32_t nE = T.n_epochs;
+  bounds.clear();
+  bounds.push_back(0);
+  if (nE == 0) return;
+  target = std::max(1u, target);
+  uint64_t acc = 0;
+  for (uint32_t e = 0; e < nE; ++e) {
+    if (acc >= target && walk_clean_cut(T, e)) {
+      bounds.push_back(e);
+      acc = 0;
+    }
+    acc += walk_epoch_cost(T.ep_k[e]);
+  }
+  if (bounds.size() > 1 && acc * 2 < target) bounds.pop_back();
+  bounds.push_back(nE);
+}
+
 double split_dep1(double p) { return 0.5 - 0.5 * std::sqrt(1.0 - (4.0 * p) / 3.0); }
 double split_dep2(double p) { return 0.5 - 0.5 * std::pow(1.0 - (16.0 * p) / 15.0, 0.125); }
 

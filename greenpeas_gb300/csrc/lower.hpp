@@ -212,6 +212,29 @@ void lower_text(const char *text, size_t len, const LowerOptions &opt, Tape &T, 
 // into pieces parsed on `pool`'s threads; the same result as one parse.
 void parse_stim_pieces(const char *text, size_t len, Parsed &out, std::vector<Parsed> &pieces, HostPool &pool);
 
+// ---- time segments of one circuit's walk ---------------------------------
+// The walk of a word is affine over GF(2) in the rows it starts from: across
+// epochs [a, b) the rows at b are A_ab * (rows at a) ^ c_ab, where A_ab (the
+// Cliffords and resets, the same for every word) is a (2 qpad x 2 qpad) bit
+// matrix and c_ab comes from the measurements in [a, b).  So a long walk can
+// be cut at epoch boundaries into segments walked side by side, once each
+// segment's entry rows are known (A and c of the segments before it, composed
+// in walk order).  A cut must not split a measurement: its OP_INJ ops carry
+// bits into the OP_M, and its OP_SNAPD reads the OP_M's bits, through
+// per-slot registers.  Such a pair straddles an epoch boundary only when the
+// later op was pushed into slot 0 of the next epoch, so an epoch whose slot 0
+// holds no OP_INJ, OP_M or OP_SNAPD is a clean cut.
+//
+// Epoch cost in the walk's units: its slots plus two (a barrier and the
+// publish of the rows cost about two slots' work).
+inline uint32_t walk_epoch_cost(uint32_t slots) { return slots + 2u; }
+// True if a segment may start at epoch e (0 < e < n_epochs).
+bool walk_clean_cut(const Tape &T, uint32_t e);
+// Cuts [0, n_epochs) into segments of about `target` cost units at clean
+// cuts: bounds = {0 = b_0 < b_1 < ... < b_S = n_epochs}.  The last segment is
+// merged into the one before when it would cost less than target / 2.
+void walk_segment_bounds(const Tape &T, uint32_t target, std::vector<uint32_t> &bounds);
+
 // Independent-component probability of DEPOLARIZE1(p) and DEPOLARIZE2(p)
 // (Mixer.hpp:164,184): 0.5 - 0.5 sqrt(1 - 4p/3), 0.5 - 0.5 (1 - 16p/15)^(1/8).
 double split_dep1(double p);

@@ -2,6 +2,7 @@
 #include <memory>
 #include <new>
 #include <string>
+#include <vector>
 
 #include "../../include/gpc.h"
 #include "host_pool.hpp"
@@ -72,6 +73,17 @@ gpc_status gpc_tape_get_view(const gpc_tape *tape, gpc_tape_view *v) {
   v->rec_moff = T.rec_moff.data();
   v->rec_src = T.rec_src.data();
   v->num_ticks = T.n_ticks;
+  return GPC_OK;
+}
+
+gpc_status gpc_tape_walk_segments(const gpc_tape *tape, uint32_t target, uint32_t *bounds, uint32_t cap,
+                                  uint32_t *n) {
+  if (!tape || !n || (cap && !bounds)) return GPC_ERR_INVALID;
+  std::vector<uint32_t> b;
+  gpc::walk_segment_bounds(tape->t, target, b);
+  *n = (uint32_t)b.size();
+  if (b.size() > cap) return GPC_ERR_CAPACITY;
+  for (size_t i = 0; i < b.size(); ++i) bounds[i] = b[i];
   return GPC_OK;
 }
 

@@ -134,6 +134,194 @@ __device__ __forceinline__ void mbar_inval(uint64_t *bar) {
 
 enum : uint32_t { ITEM_DONE = 0, ITEM_EMPTY = 1, ITEM_ABORTED = 2 };
 
+// What walk_item runs: the plain walk of words j0 .. j0+W-1, or one item of
+// the segmented walk (device.cuh: SEG_*; one word per CTA).
+enum : int { MODE_PLAIN = 0, MODE_FIRST = 1, MODE_AFF = 2, MODE_XFER = 3, MODE_REST = 4 };
+
+// One segment item as walk_item sees it.
+struct SegCtx {
+  uint32_t e_begin, e_end;  // epochs walked
+  uint64_t *out;            // FIRST / AFF / XFER: exit rows ([2 qpad]; null: none)
+  const uint64_t *in;       // REST: entry rows of segment s_from
+  const uint64_t *state;    // all states (transfer columns, AFF exits)
+  const uint32_t *aff_row;  // REST: [S] AFF state of this word in each segment (kNoState: none)
+  uint32_t *xcnt;           // [S][2 qpad] entries of each transfer row (XFER adds, REST reads)
+  uint16_t *xlst;           // [S][2 qpad][kSegRowCap] entries (the rows at the segment's start)
+  uint32_t xfer0, ncol, s_from, s_to;
+  uint32_t col, seg;        // XFER: the unit column walked, its segment
+  uint32_t ring_nb;         // REST: step buffers of the compose ring
+  uint32_t S;               // segments of the plan (sizes the staged AFF table)
+};
+constexpr uint32_t kNoState = 0xFFFFFFFFu;
+
+// Bytes of one compose step in shared memory: entry counts (u32), entries
+// (kSegRowCap u16) and the segment's AFF rows (u64) of every row.
+__host__ __device__ constexpr size_t seg_step_bytes(uint32_t qpad) {
+  return (size_t)2 * qpad * (4 + 2 * kSegRowCap + 8);
+}
+
+// XFER exit: the set bits of row r's word of column col, as entries of the
+// row's sparse list (order is free: the compose XORs them).
+__device__ __forceinline__ void seg_list_add(const SegCtx &sc, uint32_t n2, uint32_t r, uint64_t w) {
+  const size_t row = (size_t)sc.seg * n2 + r;
+  for (; w; w &= w - 1) {
+    const uint32_t j = sc.col * 64u + (uint32_t)(__ffsll((long long)w) - 1);
+    const uint32_t pos = atomicAdd(sc.xcnt + row, 1u);
+    if (pos < kSegRowCap) sc.xlst[row * kSegRowCap + pos] = (uint16_t)j;
+  }
+}
+
+// One transfer row of one compose step, held in registers: its entry count,
+// its first eight entries (u16 pairs) and its AFF row.
+struct SegRow {
+  uint32_t n;
+  uint32_t e[4];
+  uint64_t c;
+};
+
+// REST: composes the entry rows of segment s_to from those of s_from, one
+// segment at a time: rows <- A_s rows ^ c_s.  Row r of A_s is the sparse list
+// of the rows at the segment's start that feed it (XFER built it; a row
+// with more than kSegRowCap entries is read from the dense transfer columns
+// instead: bit r' mod 64 of word r of column r' / 64).  The current rows sit
+// in the published buffer, so a thread reads the rows its entries name from
+// shared memory.  Each step's lists and AFF rows are copied into a ring of
+// ring_nb shared-memory buffers by cp.async.bulk, issued ring_nb - 1 steps
+// ahead by lane 0 of the last warp on one mbarrier per buffer (mbar[2 + b]);
+// thread 0 issues the walk's first tape copies (issue_walk_copies).  A thread keeps the
+// next step's row lists in registers (loaded while the current step runs: they
+// do not depend on its result), so a step's chain is: publish the rows, one
+// barrier, the entries' loads from the published rows, XOR.  Waits are
+// bounded and a timeout aborts the item.  CTA-wide (barriers); one word per
+// CTA.  Returns false after a wait gave up (in-flight ring copies have been
+// waited for).
+template <int QPT, typename F>
+__device__ __forceinline__ bool seg_compose(uint64_t (&X)[QPT][1], uint64_t (&Z)[QPT][1], const SegCtx &sc,
+                                            ulonglong2 *pub, const uint32_t qpad, uint64_t *mbar,
+                                            unsigned char *ring, const uint32_t *s_aff, uint32_t *err,
+                                            F &&issue_walk_copies) {
+  const uint32_t T = blockDim.x, tid = threadIdx.x;
+  const uint32_t n2 = 2 * qpad;
+  const uint32_t steps = sc.s_to - sc.s_from, NB = sc.ring_nb;
+  const size_t step_bytes = seg_step_bytes(qpad);
+  const uint32_t cnt_b = n2 * 4u, lst_b = n2 * 2u * kSegRowCap, c_b = n2 * 8u;
+  // the ring's copies are issued by lane 0 of the last warp (whose slots are
+  // the packing's padding when there is any), so the first warp is not held up
+  const uint32_t issuer = T - 32u;
+  uint32_t issued = 0, waited = 0;  // steps issued (issuer) / seen complete (this thread)
+  auto issue = [&]() {  // issuer: the next step into its ring buffer
+    const uint32_t k = issued++;
+    const uint32_t s = sc.s_from + k;
+    unsigned char *dst = ring + (size_t)(k % NB) * step_bytes;
+    uint64_t *bar = &mbar[2 + k % NB];
+    const uint32_t ai = s_aff[s];
+    mbar_expect_tx(bar, cnt_b + lst_b + (ai == kNoState ? 0u : c_b));
+    bulk_g2s(dst, sc.xcnt + (size_t)s * n2, cnt_b, bar);
+    bulk_g2s(dst + cnt_b, sc.xlst + (size_t)s * n2 * kSegRowCap, lst_b, bar);
+    if (ai != kNoState) bulk_g2s(dst + cnt_b + lst_b, sc.state + (size_t)ai * n2, c_b, bar);
+  };
+  if (tid == issuer) {
+    while (issued < min(NB, steps)) issue();
+  }
+  if (tid == 0) issue_walk_copies();  // the walk's first tape chunks (thread 0 owns them), needed after the compose
+  bool bad = false;
+  auto wait_step = [&](uint32_t k) {
+    if (!mbar_wait_bounded(&mbar[2 + k % NB], (k / NB) & 1u)) bad = true;
+    else waited = k + 1;
+  };
+  const unsigned char *const ring_c = ring;
+  auto load_row = [&](uint32_t k, uint32_t r, SegRow &m) {
+    const unsigned char *buf = ring_c + (size_t)(k % NB) * step_bytes;
+    m.n = reinterpret_cast<const uint32_t *>(buf)[r];
+    const uint4 e = reinterpret_cast<const uint4 *>(buf + cnt_b)[r * (kSegRowCap / 8)];
+    m.e[0] = e.x;
+    m.e[1] = e.y;
+    m.e[2] = e.z;
+    m.e[3] = e.w;
+    m.c = s_aff[sc.s_from + k] != kNoState ? reinterpret_cast<const uint64_t *>(buf + cnt_b + lst_b)[r] : 0ull;
+  };
+  // the published rows as words: word 2 j of a buffer is X of slot j, word 2 j + 1 its Z
+  const uint32_t pub_s0 = smem_u32(pub);
+  auto word_addr = [&](uint32_t pbuf, uint32_t j) -> uint32_t {
+    return pbuf + (j < qpad ? j * 16u : (j - qpad) * 16u + 8u);
+  };
+  // row r of step k: its AFF row XOR the published rows its entries name; the
+  // row's own previous value comes from registers (`self`, most rows keep
+  // themselves), the others from shared memory, so a step loads only the
+  // entries that move sensitivity between rows
+  auto apply = [&](uint32_t k, uint32_t r, const SegRow &m, uint64_t self, uint32_t pbuf) -> uint64_t {
+    uint64_t v = m.c;
+    if (m.n <= kSegRowCap) {
+      const uint32_t n8 = min(m.n, 8u);
+      for (uint32_t i = 0; i < n8; ++i) {
+        const uint32_t j = (m.e[i >> 1] >> ((i & 1u) * 16u)) & 0xFFFFu;
+        v ^= j == r ? self : j < n2 ? lds64(word_addr(pbuf, j)) : 0ull;
+      }
+      if (m.n > 8) {  // entries 8..15 from the step's buffer (not refilled before the next barrier)
+        const uint16_t *l =
+            reinterpret_cast<const uint16_t *>(ring_c + (size_t)(k % NB) * step_bytes + cnt_b) + (size_t)r * kSegRowCap;
+        for (uint32_t i = 8; i < m.n; ++i) {
+          const uint32_t j = l[i];
+          v ^= j == r ? self : j < n2 ? lds64(word_addr(pbuf, j)) : 0ull;
+        }
+      }
+    } else {  // a long row: its words from the dense transfer columns
+      const uint64_t *tm = sc.state + (size_t)(sc.xfer0 + (sc.s_from + k) * sc.ncol) * n2;
+      for (uint32_t c = 0; c < sc.ncol; ++c)
+        for (uint64_t w = __ldg(tm + (size_t)c * n2 + r); w; w &= w - 1) {
+          const uint32_t j = c * 64u + (uint32_t)(__ffsll((long long)w) - 1);
+          v ^= j == r ? self : j < n2 ? lds64(word_addr(pbuf, j)) : 0ull;
+        }
+    }
+    return v;
+  };
+  SegRow mx[QPT], mz[QPT];
+  if (steps) {
+    wait_step(0);
+#pragma unroll
+    for (int u = 0; u < QPT; ++u) {
+      load_row(0, tid + (uint32_t)u * T, mx[u]);
+      load_row(0, qpad + tid + (uint32_t)u * T, mz[u]);
+    }
+  }
+  for (uint32_t k = 0; k < steps; ++k) {
+    ulonglong2 *pb = pub + (size_t)(k & 1u) * qpad;
+#pragma unroll
+    for (int u = 0; u < QPT; ++u) pb[tid + u * T] = make_ulonglong2(X[u][0], Z[u][0]);
+    if (__syncthreads_or(bad ? 1 : 0)) {
+      bad = true;
+      break;
+    }
+    // every thread is done with step k - 1's buffer
+    if (tid == issuer && k >= 1 && issued < steps) issue();
+    const uint32_t pbuf = pub_s0 + (k & 1u) * qpad * 16u;
+#pragma unroll
+    for (int u = 0; u < QPT; ++u) {
+      const uint32_t slot = tid + (uint32_t)u * T;
+      const uint64_t nx = apply(k, slot, mx[u], X[u][0], pbuf);
+      const uint64_t nz = apply(k, qpad + slot, mz[u], Z[u][0], pbuf);
+      X[u][0] = nx;
+      Z[u][0] = nz;
+    }
+    if (k + 1 < steps) {
+      wait_step(k + 1);
+#pragma unroll
+      for (int u = 0; u < QPT; ++u) {
+        load_row(k + 1, tid + (uint32_t)u * T, mx[u]);
+        load_row(k + 1, qpad + tid + (uint32_t)u * T, mz[u]);
+      }
+    }
+  }
+  if (bad && tid == issuer) {
+    atomicOr(err, DEV_ERR_TIMEOUT);
+    // copies still in flight target this CTA's shared memory
+    for (uint32_t k = waited; k < issued; ++k)
+      if (!mbar_wait_bounded(&mbar[2 + k % NB], (k / NB) & 1u)) break;
+  }
+  __syncthreads();  // the walk publishes into buffer 0 next, which may have been read last
+  return !bad;
+}
+
 // One walk item: the words j0 .. j0+W-1 of circuit C (rows W x 64 bits per
 // qubit; a batch halves its CTAs with W = 2 while each epoch's latency chain
 // stays about the same), walked by the whole CTA.  `pub_slots` lays out the
@@ -144,12 +332,21 @@ enum : uint32_t { ITEM_DONE = 0, ITEM_EMPTY = 1, ITEM_ABORTED = 2 };
 // multiple of 32, so whole warps idle).  Returns ITEM_EMPTY when the words
 // inject nothing (the mbarriers were not initialised), ITEM_ABORTED after a
 // bounded wait gave up, else ITEM_DONE.  CTA-uniform.
-template <int QPT, int W, bool QUEUE>
+//
+// Segment items (MODE != MODE_PLAIN, W = 1, `sc` given) walk [e_begin, e_end)
+// only: FIRST from zero rows with snapshots (and the word's band), AFF from
+// zero rows without snapshots, XFER from unit rows without measurement bits
+// or snapshots (stopping once the rows vanish), REST from composed entry rows
+// with snapshots (a REST that stops early lowers the band's end).
+template <int QPT, int W, bool QUEUE, int MODE = MODE_PLAIN>
 __device__ __forceinline__ uint32_t walk_item(const CircuitDev &C, const uint32_t j0, unsigned char *smem,
                                               const uint32_t pub_slots, const uint32_t chunk_cap,
                                               const uint32_t table_bytes, uint32_t *__restrict__ err,
-                                              uint32_t &s_abort) {
-  const uint32_t nw = min((uint32_t)W, C.w - j0);  // words of this CTA (the circuit's last group may be short)
+                                              uint32_t &s_abort, const SegCtx *sc = nullptr) {
+  constexpr bool SEG = MODE != MODE_PLAIN;
+  constexpr bool SNAPS = MODE == MODE_PLAIN || MODE == MODE_FIRST || MODE == MODE_REST;
+  static_assert(!SEG || (W == 1 && !QUEUE), "segment items walk one word per CTA");
+  const uint32_t nw = SEG ? 1u : min((uint32_t)W, C.w - j0);  // words of this CTA (the circuit's last group may be short)
   const uint32_t T = blockDim.x;
   const uint32_t tid = threadIdx.x;
   const uint32_t qpad = C.qpad;
@@ -160,18 +357,24 @@ __device__ __forceinline__ uint32_t walk_item(const CircuitDev &C, const uint32_
 
   // the CTA walks from the earliest first injection of its words to the
   // latest last injection (and on until every row is zero)
-  uint32_t e0 = 0xFFFFFFFFu, elast = 0;
+  uint32_t e0 = 0xFFFFFFFFu, elast = 0, e_end = nE;
+  if constexpr (SEG) {
+    e0 = sc->e_begin;
+    e_end = sc->e_end;
+    if constexpr (MODE != MODE_XFER) elast = C.inj_hi[j0];
+  } else {
 #pragma unroll
-  for (int wi = 0; wi < W; ++wi) {
-    if ((uint32_t)wi >= nw) break;
-    const uint32_t lo = C.inj_lo[j0 + wi];
-    if (lo == 0xFFFFFFFFu || lo >= nE) continue;
-    e0 = min(e0, lo);
-    elast = max(elast, C.inj_hi[j0 + wi]);
-  }
-  if (e0 == 0xFFFFFFFFu) {
-    if (tid < nw) C.band[j0 + tid] = make_uint2(0u, 0u);
-    return ITEM_EMPTY;
+    for (int wi = 0; wi < W; ++wi) {
+      if ((uint32_t)wi >= nw) break;
+      const uint32_t lo = C.inj_lo[j0 + wi];
+      if (lo == 0xFFFFFFFFu || lo >= nE) continue;
+      e0 = min(e0, lo);
+      elast = max(elast, C.inj_hi[j0 + wi]);
+    }
+    if (e0 == 0xFFFFFFFFu) {
+      if (tid < nw) C.band[j0 + tid] = make_uint2(0u, 0u);
+      return ITEM_EMPTY;
+    }
   }
 
   // shared memory: [published rows x2][mbarriers][tables][chunk buffer x2]
@@ -181,11 +384,22 @@ __device__ __forceinline__ uint32_t walk_item(const CircuitDev &C, const uint32_
   off += 128;
   uint2 *etab = reinterpret_cast<uint2 *>(smem + off);  // epoch e0+i: (op offset, slots | chunk << 8)
   const uint32_t c0 = C.ep_chunk[e0];
-  const uint32_t ne = nE - e0, nc = C.n_chunks - c0;
+  const uint32_t c_end = SEG ? C.ep_chunk[e_end - 1] + 1 : C.n_chunks;  // chunks past the last one walked
+  const uint32_t ne = e_end - e0, nc = c_end - c0;
   const bool staged = ((size_t)ne + nc) * sizeof(uint2) <= table_bytes;
   uint2 *ctab = etab + ne;  // chunk c0+i: (op offset, bytes)
   off += table_bytes;
   unsigned char *buf = smem + off;  // two buffers of chunk_cap bytes
+  // REST: [S aff states (u32, 16-byte rounded)][ring_nb compose step buffers]
+  uint32_t *s_aff = nullptr;
+  unsigned char *ring = nullptr;
+  if constexpr (MODE == MODE_REST) {
+    off += (size_t)2 * chunk_cap;
+    s_aff = reinterpret_cast<uint32_t *>(smem + off);
+    off += ((size_t)sc->S * 4 + 15) & ~(size_t)15;
+    ring = smem + ((off + 127) & ~(size_t)127);
+    for (uint32_t i = tid; i < sc->s_to; i += T) s_aff[i] = sc->aff_row[i];
+  }
 
   if (staged) {
     for (uint32_t i = tid; i < ne; i += T)
@@ -196,6 +410,8 @@ __device__ __forceinline__ uint32_t walk_item(const CircuitDev &C, const uint32_
     s_abort = 0;
     mbar_init(&mbar[0], 1);
     mbar_init(&mbar[1], 1);
+    if constexpr (MODE == MODE_REST)
+      for (uint32_t b = 0; b < sc->ring_nb; ++b) mbar_init(&mbar[2 + b], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   __syncthreads();
@@ -216,16 +432,41 @@ __device__ __forceinline__ uint32_t walk_item(const CircuitDev &C, const uint32_
     bulk_g2s(buf + (size_t)(issued & 1u) * chunk_cap, C.ops + ck.x, ck.y, bar);
     ++issued;
   };
-  if (tid == 0) {
+  auto issue_first_chunks = [&]() {
     issue();
     if (nc > 1) issue();
-  }
+  };
+  // (REST: after the compose ring's first copies, which are needed first)
+  if (MODE != MODE_REST && tid == 0) issue_first_chunks();
 
   uint64_t X[QPT][W], Z[QPT][W], acc[QPT][W], last_inj[QPT][W];
+  bool compose_bad = false;
 #pragma unroll
   for (int u = 0; u < QPT; ++u)
 #pragma unroll
     for (int wi = 0; wi < W; ++wi) X[u][wi] = Z[u][wi] = acc[u][wi] = last_inj[u][wi] = 0;
+  if constexpr (MODE == MODE_XFER) {
+    // unit rows of column col: row r (X of slot r, or Z of slot r - qpad) holds bit r - 64 col
+#pragma unroll
+    for (int u = 0; u < QPT; ++u) {
+      const uint32_t xr = tid + (uint32_t)u * T, zr = qpad + xr;
+      if constexpr (W == 1) {
+        X[u][0] = (xr >> 6) == sc->col ? 1ull << (xr & 63u) : 0ull;
+        Z[u][0] = (zr >> 6) == sc->col ? 1ull << (zr & 63u) : 0ull;
+      }
+    }
+  } else if constexpr (MODE == MODE_REST) {
+    if constexpr (W == 1) {
+#pragma unroll
+      for (int u = 0; u < QPT; ++u) {
+        const uint32_t slot = tid + (uint32_t)u * T;
+        X[u][0] = __ldg(sc->in + slot);
+        Z[u][0] = __ldg(sc->in + qpad + slot);
+      }
+      compose_bad = !seg_compose<QPT>(X, Z, *sc, reinterpret_cast<ulonglong2 *>(smem), qpad, mbar, ring, s_aff,
+                                      err, issue_first_chunks);
+    }
+  }
 
   const uint32_t np = C.npoints;
   ulonglong2 *snap0 = C.snap + (size_t)j0 * np;  // word j0 + wi at + wi * np
@@ -235,7 +476,7 @@ __device__ __forceinline__ uint32_t walk_item(const CircuitDev &C, const uint32_
   unsigned long long *nzm0 = C.nzm + (j0 >> 6);
   const uint32_t mw = C.mw;
   const uint32_t jsh = j0 & 63u;
-  bool timed_out = false, aborted = false;
+  bool timed_out = compose_bad, aborted = false;  // (the walk's first barrier aborts after a failed compose)
   uint32_t e = e0;
   uint32_t seq = 0;
   uint32_t cur = 0xFFFFFFFFu;  // chunk whose data this thread has waited for
@@ -282,15 +523,16 @@ __device__ __forceinline__ uint32_t walk_item(const CircuitDev &C, const uint32_
       aborted = true;
       break;
     }
-    if ((!any && e > elast) || e >= nE) break;
+    // (XFER has no measurement bits: its rows stay zero once they vanish)
+    if ((!any && (MODE == MODE_XFER || e > elast)) || e >= e_end) break;
     const uint2 ek = ek_next;
-    if (e + 1 < nE) ek_next = epoch(e + 1);  // used next epoch: its latency hides behind this one
+    if (e + 1 < e_end) ek_next = epoch(e + 1);  // used next epoch: its latency hides behind this one
     const uint32_t K = ek.y & 0xFFu;
     const uint32_t ch = ek.y >> 8;
     if (ch != cur) {
       // (3) first epoch of a chunk: every thread has finished the previous
       //     chunk (barrier above), so its buffer can take the chunk after this one
-      if (tid == 0 && ch + 1 < C.n_chunks && c0 + issued == ch + 1) issue();
+      if (tid == 0 && ch + 1 < c_end && c0 + issued == ch + 1) issue();
       const uint32_t i = ch - c0;
       if (!mbar_wait_bounded(&mbar[i & 1u], (i >> 1) & 1u)) {
         timed_out = true;
@@ -321,7 +563,7 @@ __device__ __forceinline__ uint32_t walk_item(const CircuitDev &C, const uint32_
 #pragma unroll
           for (int wi = 0; wi < W; ++wi) Z[u][wi] ^= lds64(pa + wi * 16u + 8u);
         } else if (opc == OP_SNAP) {
-          snapshot(arg, X[u], Z[u]);
+          if constexpr (SNAPS) snapshot(arg, X[u], Z[u]);
         } else if (opc == OP_XPZ) {
 #pragma unroll
           for (int wi = 0; wi < W; ++wi) X[u][wi] ^= lds64(pa + wi * 16u + 8u);
@@ -346,6 +588,7 @@ __device__ __forceinline__ uint32_t walk_item(const CircuitDev &C, const uint32_
 #pragma unroll
             for (int wi = 0; wi < W; ++wi) X[u][wi] = Z[u][wi] = 0;
           } else if (opc == OP_INJ) {
+            if constexpr (MODE == MODE_XFER) continue;  // the linear part only
             // measurement bits (one or two) that fall in this CTA's words
             const uint32_t b2 = ((uint32_t)op >> 8) & 0xFFFFFFu;
             const uint32_t d1 = arg - jlo, d2 = b2 - jlo;
@@ -361,6 +604,7 @@ __device__ __forceinline__ uint32_t walk_item(const CircuitDev &C, const uint32_
             for (int wi = 0; wi < W; ++wi) {
               uint64_t inj = acc[u][wi];
               if (d1 - wi * 64u < 64u) inj |= 1ull << (d1 & 63u);
+              if constexpr (MODE == MODE_XFER) inj = 0;
               acc[u][wi] = 0;
               if (sub & 4u) X[u][wi] = Z[u][wi] = 0;
               if (basis != 1u) X[u][wi] ^= inj;
@@ -368,6 +612,7 @@ __device__ __forceinline__ uint32_t walk_item(const CircuitDev &C, const uint32_
               last_inj[u][wi] = inj;
             }
           } else if (opc == OP_SNAPD) {
+            if constexpr (!SNAPS) continue;
             if constexpr (W == 1) {
               snap0[arg] = make_ulonglong2(last_inj[u][0], 0ull);
               if (last_inj[u][0]) red_or(nzm0 + arg * mw, 1ull << jsh);
@@ -382,7 +627,32 @@ __device__ __forceinline__ uint32_t walk_item(const CircuitDev &C, const uint32_
       }
     }
   }
-  if (tid < nw) C.band[j0 + tid] = make_uint2(C.ep_ptoff[e0], C.ep_ptoff[e < nE ? e : nE]);
+  if constexpr (MODE == MODE_PLAIN) {
+    if (tid < nw) C.band[j0 + tid] = make_uint2(C.ep_ptoff[e0], C.ep_ptoff[e < nE ? e : nE]);
+  } else if constexpr (MODE == MODE_FIRST) {
+    // later segments (if any) cover up to the end unless they stop early
+    if (tid == 0) C.band[j0] = make_uint2(C.ep_ptoff[e0], C.ep_ptoff[e < e_end ? e : nE]);
+  } else if constexpr (MODE == MODE_REST) {
+    if (tid == 0 && e < e_end) atomicMin(&C.band[j0].y, C.ep_ptoff[e]);
+  }
+  if constexpr (MODE == MODE_XFER) {
+#pragma unroll
+    for (int u = 0; u < QPT; ++u) {
+      const uint32_t slot = tid + (uint32_t)u * T;
+      seg_list_add(*sc, 2 * qpad, slot, X[u][0]);
+      seg_list_add(*sc, 2 * qpad, qpad + slot, Z[u][0]);
+    }
+  }
+  if constexpr (MODE == MODE_FIRST || MODE == MODE_AFF || MODE == MODE_XFER) {
+    if (sc->out) {
+#pragma unroll
+      for (int u = 0; u < QPT; ++u) {
+        const uint32_t slot = tid + (uint32_t)u * T;
+        sc->out[slot] = X[u][0];
+        sc->out[qpad + slot] = Z[u][0];
+      }
+    }
+  }
   if (tid == 0) {
     // Copies still in flight target this CTA's shared memory: wait for them
     // (bounded) before the CTA exits or takes another item.
@@ -443,6 +713,51 @@ __global__ void __launch_bounds__(WalkBound<QPT>::value) walk_queue_kernel(const
   }
 }
 
+// Segmented walk of one circuit: one CTA per segment item (SEG_*).
+template <int QPT>
+__global__ void __launch_bounds__(WalkBound<QPT>::value) walk_seg_kernel(const SegLaunch L, uint32_t table_bytes) {
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ uint32_t s_abort;
+  const SegItem it = L.items[blockIdx.x];
+  if (it.kind == SEG_REST && L.ring_nb < 2) {  // no compose ring in this launch
+    if (threadIdx.x == 0) atomicOr(L.err, DEV_ERR_TIMEOUT);
+    return;
+  }
+  const CircuitDev C = *L.circ;
+  const size_t n2 = (size_t)2 * C.qpad;
+  SegCtx sc;
+  sc.e_begin = it.e_begin;
+  sc.e_end = it.e_end;
+  sc.out = it.kind != SEG_REST && it.state != kNoState ? L.state + (size_t)it.state * n2 : nullptr;
+  sc.in = it.kind == SEG_REST ? L.state + (size_t)it.state * n2 : nullptr;
+  sc.state = L.state;
+  sc.aff_row = L.aff + (size_t)(it.kind == SEG_XFER ? 0u : it.idx) * L.S;
+  sc.xfer0 = L.xfer0;
+  sc.ncol = L.ncol;
+  sc.s_from = it.s_from;
+  sc.s_to = it.s_to;
+  sc.col = it.idx;
+  sc.seg = it.s_from;
+  sc.xcnt = L.xcnt;
+  sc.xlst = L.xlst;
+  sc.ring_nb = L.ring_nb;
+  sc.S = L.S;
+  switch (it.kind) {
+    case SEG_FIRST:
+      walk_item<QPT, 1, false, MODE_FIRST>(C, it.idx, smem, C.qpad, L.chunk_cap, table_bytes, L.err, s_abort, &sc);
+      break;
+    case SEG_AFF:
+      walk_item<QPT, 1, false, MODE_AFF>(C, it.idx, smem, C.qpad, L.chunk_cap, table_bytes, L.err, s_abort, &sc);
+      break;
+    case SEG_XFER:
+      walk_item<QPT, 1, false, MODE_XFER>(C, 0, smem, C.qpad, L.chunk_cap, table_bytes, L.err, s_abort, &sc);
+      break;
+    default:
+      walk_item<QPT, 1, false, MODE_REST>(C, it.idx, smem, C.qpad, L.chunk_cap, table_bytes, L.err, s_abort, &sc);
+      break;
+  }
+}
+
 }  // namespace
 
 uint32_t walk_table_bytes(uint32_t max_epochs, uint32_t max_chunks) {
@@ -474,6 +789,15 @@ cudaError_t walk_queue_set_limit_one(int optin) {
                               optin - (int)a.sharedSizeBytes);
 }
 
+template <int QPT>
+cudaError_t walk_seg_set_limit_one(int optin) {
+  cudaFuncAttributes a{};
+  cudaError_t e = cudaFuncGetAttributes(&a, walk_seg_kernel<QPT>);
+  if (e != cudaSuccess) return e;
+  return cudaFuncSetAttribute(walk_seg_kernel<QPT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              optin - (int)a.sharedSizeBytes);
+}
+
 cudaError_t walk_set_smem_limit() {
   int dev = 0, optin = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -492,6 +816,8 @@ cudaError_t walk_set_smem_limit() {
   if (e == cudaSuccess) e = walk_queue_set_limit_one<2, 1>(optin);
   if (e == cudaSuccess) e = walk_queue_set_limit_one<1, 2>(optin);
   if (e == cudaSuccess) e = walk_queue_set_limit_one<2, 2>(optin);
+  if (e == cudaSuccess) e = walk_seg_set_limit_one<1>(optin);
+  if (e == cudaSuccess) e = walk_seg_set_limit_one<2>(optin);
   return e;
 }
 
@@ -582,6 +908,29 @@ cudaError_t launch_walk(const WalkLaunch &L, cudaStream_t s) {
   }
 #undef GPC_WALK
 #undef GPC_WALK2
+  return cudaGetLastError();
+}
+
+bool walk_seg_supported(uint32_t qpt) { return qpt == 1 || qpt == 2; }
+
+size_t walk_seg_smem_bytes(const SegLaunch &L) {
+  const uint32_t tb = walk_table_bytes(L.max_epochs, L.max_chunks);
+  size_t b = walk_smem_bytes(L.qpad, L.chunk_cap, tb, 1);
+  if (L.ring_nb) b = ((b + ((size_t)L.S * 4 + 15) / 16 * 16 + 127) & ~(size_t)127) + L.ring_nb * seg_step_bytes(L.qpad);
+  return b <= 227 * 1024 - 1024 ? b : 0;
+}
+
+cudaError_t launch_walk_seg(const SegLaunch &L, cudaStream_t s) {
+  if (L.n_items == 0) return cudaSuccess;
+  const uint32_t tb = walk_table_bytes(L.max_epochs, L.max_chunks);
+  const size_t smem = walk_seg_smem_bytes(L);
+  // a compose ring needs two buffers at least: step k + 1's copy is issued
+  // only once every thread is done with step k - 1's buffer
+  if (smem == 0 || L.ring_nb > kSegRingMax || L.ring_nb == 1) return cudaErrorInvalidValue;
+  if (!walk_seg_supported(L.qpt) || L.threads * L.qpt != L.qpad || L.threads > walk_max_threads(L.qpt))
+    return cudaErrorInvalidValue;
+  if (L.qpt == 1) walk_seg_kernel<1><<<L.n_items, L.threads, smem, s>>>(L, tb);
+  else walk_seg_kernel<2><<<L.n_items, L.threads, smem, s>>>(L, tb);
   return cudaGetLastError();
 }
 

@@ -137,7 +137,8 @@ class Driver:
 
     def __init__(self, circuit, correlation_level: CorrelationLevel = CorrelationLevel.L2, *,
                  device: int = 0, sort_bits: int = 0, global_sort: bool = False, walk_qpt: int = 0,
-                 bucket_mean: int = 0, walk_words: int = 0, key_split: int = 0, walk_queue: int = 0):
+                 bucket_mean: int = 0, walk_words: int = 0, key_split: int = 0, walk_queue: int = 0,
+                 walk_segment: int = 0):
         L = _native.lib()
         self._h = ctypes.c_void_p()
         self.correlation_level = CorrelationLevel(correlation_level)
@@ -151,6 +152,7 @@ class Driver:
         opts.walk_words = walk_words
         opts.key_split = key_split
         opts.walk_queue = walk_queue
+        opts.walk_segment = walk_segment
         text = _text(circuit)
         _native.check(L.gpc_get_driver(text, len(text), int(self.correlation_level), ctypes.byref(opts),
                                        ctypes.byref(self._h)))
@@ -169,6 +171,14 @@ class Driver:
     @property
     def handle(self) -> ctypes.c_void_p:
         return self._h
+
+    def walk_segments(self) -> dict:
+        """The segmented walk of the prepared single circuit: segments (0: not segmented) and the
+        CTAs of its two launches."""
+        L = _native.lib()
+        a, b, c = ctypes.c_uint32(), ctypes.c_uint32(), ctypes.c_uint32()
+        _native.check(L.gpc_walk_segments(self._h, ctypes.byref(a), ctypes.byref(b), ctypes.byref(c)))
+        return {"segments": a.value, "items_first": b.value, "items_rest": c.value}
 
     def compile(self, circuit=None) -> DetectorErrorModel:
         """Compiles ``circuit`` (or the driver's current circuit) to this package's DEM type."""
@@ -314,7 +324,9 @@ def get_driver(circuit, correlation_level: CorrelationLevel = CorrelationLevel.L
 class Tape:
     """The lowered device tape of a circuit, as numpy arrays (host only, no GPU)."""
 
-    def __init__(self, circuit, correlation_level: int = 2):
+    def __init__(self, circuit, correlation_level: int = 2, segment_target: int | None = None):
+        """``segment_target``: also set ``walk_bounds``, the epoch boundaries a single-circuit
+        compile cuts the walk at for that segment cost (slots + 2 per epoch)."""
         L = _native.lib()
         h = ctypes.c_void_p()
         text = _text(circuit)
@@ -340,5 +352,11 @@ class Tape:
             self.rec_moff = arr(v.rec_moff, v.num_records + 1)
             self.rec_src = arr(v.rec_src, v.num_records)
             self.num_ticks = int(v.num_ticks)
+            if segment_target is not None:
+                n = ctypes.c_uint32()
+                cap = int(v.num_epochs) + 2
+                buf = (ctypes.c_uint32 * cap)()
+                _native.check(L.gpc_tape_walk_segments(h, int(segment_target), buf, cap, ctypes.byref(n)), tape=True)
+                self.walk_bounds = np.array(buf[: n.value], dtype=np.int64)
         finally:
             L.gpc_tape_free(h)

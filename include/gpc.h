@@ -67,6 +67,9 @@ typedef struct gpc_options {
   int32_t walk_queue;  /* batches: 1 = one persistent walk launch (resident CTAs take (circuit, word group) items
                           from a queue, longest first), -1 = one launch per thread-count class,
                           0 = classes unless gpc_autotune chose the persistent launch */
+  int32_t walk_segment; /* one circuit: cut the walk into time segments walked side by side, composed
+                           through their GF(2) transfer maps (0 = when it pays, -1 = never, > 0 = always,
+                           about this many cost units per segment: an epoch costs its slots + 2) */
 } gpc_options;
 
 /* Parses `stim_text` (length `len`), sizes device buffers for it and returns
@@ -246,6 +249,15 @@ gpc_status gpc_last_host_timings(gpc_driver *driver, double *ms6);
  * the batch walks in one persistent launch off its work queue. */
 gpc_status gpc_walk_form(gpc_driver *driver, int32_t *launches, int32_t *persistent);
 
+/* Segmented walk of the prepared single circuit (no counterpart in the
+ * reference): `segments` the time segments its walk is cut into (0: not
+ * segmented), `items_first` the CTAs of the first launch (first parts of the
+ * words, their walks of later segments from zero rows, the transfer-matrix
+ * columns) and `items_rest` those of the second (each later segment of a
+ * word, from its composed entry rows). */
+gpc_status gpc_walk_segments(gpc_driver *driver, uint32_t *segments, uint32_t *items_first,
+                             uint32_t *items_rest);
+
 /* Algorithmic bytes moved by each stage of the last run, counted from its
  * sizes: [0] walk (tape read + snapshots written), [1] key (records + snapshot
  * reads + keys, descriptors, target lists and bucket slots written), [2]
@@ -321,6 +333,12 @@ typedef struct gpc_tape_view {
 
 gpc_status gpc_tape_lower(const char *stim_text, size_t len, int32_t correlation_level, gpc_tape **out);
 gpc_status gpc_tape_get_view(const gpc_tape *tape, gpc_tape_view *view);
+/* The epoch boundaries a single-circuit compile cuts its walk at, for a
+ * segment cost of `target` (slots + 2 per epoch): bounds[0] = 0 < ... <
+ * bounds[n-1] = num_epochs, written when n <= cap (GPC_ERR_CAPACITY
+ * otherwise; n is always set). */
+gpc_status gpc_tape_walk_segments(const gpc_tape *tape, uint32_t target, uint32_t *bounds, uint32_t cap,
+                                  uint32_t *n);
 void gpc_tape_free(gpc_tape *tape);
 /* Thread-local message of the last gpc_tape_lower failure. */
 const char *gpc_tape_last_error(void);

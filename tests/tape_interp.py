@@ -30,85 +30,173 @@ def _sel2(m, x, z):
     return (x & (U64(0) - (m & U64(1)))) ^ (z & (U64(0) - ((m >> U64(1)) & U64(1))))
 
 
+def _decoded(t):
+    if not hasattr(t, "_dec"):
+        t._dec = ((t.ops & U64(0xFF)).astype(np.uint32), ((t.ops >> U64(8)) & U64(0xFF)).astype(np.uint32),
+                  (t.ops >> U64(32)).astype(np.int64))
+    return t._dec
+
+
 def walk(t):
     """Returns (snap [w, npoints, 2] uint64, band [w, 2])."""
     w, qpad, nE = t.words, t.qpad, t.num_epochs
     snap = np.zeros((w, max(1, t.num_points), 2), dtype=np.uint64)
     band = np.zeros((w, 2), dtype=np.int64)
-    opc_all = (t.ops & U64(0xFF)).astype(np.uint32)
-    sub_all = ((t.ops >> U64(8)) & U64(0xFF)).astype(np.uint32)
-    arg_all = (t.ops >> U64(32)).astype(np.int64)
+    for j in range(w):
+        e0 = int(t.inj_lo[j])
+        if e0 == NONE or e0 >= nE:
+            continue
+        X = np.zeros(qpad, dtype=np.uint64)
+        Z = np.zeros(qpad, dtype=np.uint64)
+        e = walk_range(t, j, e0, nE, int(t.inj_hi[j]), X, Z, snap)
+        band[j] = (int(t.ep_ptoff[e0]), int(t.ep_ptoff[min(e, nE)]))
+    return snap, band
+
+
+def walk_range(t, j, e_begin, e_end, elast, X, Z, snap=None, inject=True):
+    """Walks epochs [e_begin, e_end) of word j from rows X, Z (updated in place), the way the
+    walk kernel does; stops early, before an epoch e > elast, once every row is zero.  With
+    ``snap`` given, snapshots are stored in it; ``inject=False`` leaves out the measurements'
+    bits (the linear part of the walk).  Returns the epoch it stopped before."""
+    qpad = t.qpad
+    opc_all, sub_all, arg_all = _decoded(t)
+    last = np.zeros(qpad, dtype=np.uint64)
+    acc = np.zeros(qpad, dtype=np.uint64)
+    e = e_begin
+    while True:
+        pX, pZ = X.copy(), Z.copy()
+        anynz = bool(np.any(X | Z))
+        if (not anynz and e > elast) or e >= e_end:
+            break
+        off = int(t.ep_opoff[e])
+        for k in range(int(t.ep_k[e])):
+            sl = slice(off + k * qpad, off + (k + 1) * qpad)
+            opc, sub, arg = opc_all[sl], sub_all[sl], arg_all[sl]
+            m = opc == OP_C1
+            if m.any():
+                x, z = X[m], Z[m]
+                X[m] = _sel2(sub[m] & 3, x, z)
+                Z[m] = _sel2(sub[m] >> 2, x, z)
+            m = opc == OP_C2
+            if m.any():
+                x, z = X[m], Z[m]
+                px, pz = pX[arg[m]], pZ[arg[m]]
+                s = sub[m]
+                X[m] = _sel2(s & 3, x, z) ^ _sel2((s >> 2) & 3, px, pz)
+                Z[m] = _sel2((s >> 4) & 3, x, z) ^ _sel2((s >> 6) & 3, px, pz)
+            m = opc == OP_XPX
+            X[m] ^= pX[arg[m]]
+            m = opc == OP_ZPZ
+            Z[m] ^= pZ[arg[m]]
+            m = opc == OP_XPZ
+            X[m] ^= pZ[arg[m]]
+            m = opc == OP_R
+            X[m] = 0
+            Z[m] = 0
+            jlo = 64 * j if inject else -(1 << 40)
+            for q in np.nonzero(opc == OP_INJ)[0]:
+                b1, b2 = int(arg[q]), (int(t.ops[off + k * qpad + q]) >> 8) & 0xFFFFFF
+                for b in (b1, b2):
+                    if b != 0xFFFFFF and 0 <= b - jlo < 64:
+                        acc[q] |= U64(1 << (b - jlo))
+            for q in np.nonzero(opc == OP_M)[0]:
+                inj = int(acc[q])
+                b1 = int(arg[q])
+                if 0 <= b1 - jlo < 64:
+                    inj |= 1 << (b1 - jlo)
+                acc[q] = 0
+                inj = U64(inj)
+                if sub[q] & 4:
+                    X[q] = 0
+                    Z[q] = 0
+                if (sub[q] & 3) != 1:
+                    X[q] ^= inj
+                if (sub[q] & 3) != 0:
+                    Z[q] ^= inj
+                last[q] = inj
+            if snap is None:
+                continue
+            m = opc == OP_SNAP
+            if m.any():
+                snap[j, arg[m], 0] = X[m]
+                snap[j, arg[m], 1] = Z[m]
+            m = opc == OP_SNAPD
+            if m.any():
+                snap[j, arg[m], 0] = last[m]
+                snap[j, arg[m], 1] = 0
+        e += 1
+    return e
+
+
+def _unpack(X, Z):
+    """Rows (X of slots 0..qpad-1, then Z) as a (2 qpad, 64) 0/1 matrix."""
+    v = np.concatenate([X, Z])
+    return ((v[:, None] >> np.arange(64, dtype=np.uint64)[None, :]) & U64(1)).astype(np.int64)
+
+
+def _pack(bits):
+    return (bits.astype(np.uint64) << np.arange(64, dtype=np.uint64)[None, :]).sum(axis=1, dtype=np.uint64)
+
+
+def transfer_matrix(t, a, b):
+    """The (2 qpad x 2 qpad) 0/1 matrix A with rows at epoch b = A rows at epoch a over GF(2),
+    for the walk of [a, b) without the measurements' bits: column by column, as the transfer
+    walk kernel finds it, walking 64 unit rows at a time."""
+    n = 2 * t.qpad
+    A = np.zeros((n, n), dtype=np.int64)
+    for c in range(0, n, 64):
+        idx = np.arange(n)
+        unit = np.where((idx >= c) & (idx < c + 64), U64(1) << (idx - c).clip(0, 63).astype(np.uint64), U64(0))
+        X, Z = unit[: t.qpad].copy(), unit[t.qpad:].copy()
+        walk_range(t, 0, a, b, -1, X, Z, inject=False)
+        A[:, c: c + 64] = _unpack(X, Z)[:, : min(64, n - c)]
+    return A
+
+
+def walk_segmented(t, bounds):
+    """The walk cut into time segments at ``bounds`` (0 = b_0 < ... < b_S = num_epochs), as
+    the segmented walk kernels run it: a word whose walk spans segments s0 .. K walks its first
+    part [e0, b_{s0+1}) from zero; each later segment s is walked from its entry rows, composed
+    from the first part's exit rows through the segments between as rows_{s+1} = A_s rows_s ^
+    c_s, where A_s is the segment's transfer matrix and c_s its walk from zero rows.  A word
+    holding observables walks to the end; a detector word's last segment is the one holding its
+    last measurement, walked on until its rows vanish.  Same (snap, band) contract as walk()."""
+    w, qpad, nE = t.words, t.qpad, t.num_epochs
+    bounds = [int(b) for b in bounds]
+    S = len(bounds) - 1
+    seg_of = lambda e: int(np.searchsorted(bounds, e, side="right")) - 1  # noqa: E731
+    snap = np.zeros((w, max(1, t.num_points), 2), dtype=np.uint64)
+    band = np.zeros((w, 2), dtype=np.int64)
+    A = {}
     for j in range(w):
         e0 = int(t.inj_lo[j])
         if e0 == NONE or e0 >= nE:
             continue
         elast = int(t.inj_hi[j])
+        s0 = seg_of(e0)
+        K = S - 1 if (j + 1) * 64 > t.num_detectors else seg_of(elast)
         X = np.zeros(qpad, dtype=np.uint64)
         Z = np.zeros(qpad, dtype=np.uint64)
-        last = np.zeros(qpad, dtype=np.uint64)
-        acc = np.zeros(qpad, dtype=np.uint64)
-        e = e0
-        while True:
-            pX, pZ = X.copy(), Z.copy()
-            anynz = bool(np.any(X | Z))
-            if (not anynz and e > elast) or e >= nE:
-                break
-            off = int(t.ep_opoff[e])
-            for k in range(int(t.ep_k[e])):
-                sl = slice(off + k * qpad, off + (k + 1) * qpad)
-                opc, sub, arg = opc_all[sl], sub_all[sl], arg_all[sl]
-                m = opc == OP_C1
-                if m.any():
-                    x, z = X[m], Z[m]
-                    X[m] = _sel2(sub[m] & 3, x, z)
-                    Z[m] = _sel2(sub[m] >> 2, x, z)
-                m = opc == OP_C2
-                if m.any():
-                    x, z = X[m], Z[m]
-                    px, pz = pX[arg[m]], pZ[arg[m]]
-                    s = sub[m]
-                    X[m] = _sel2(s & 3, x, z) ^ _sel2((s >> 2) & 3, px, pz)
-                    Z[m] = _sel2((s >> 4) & 3, x, z) ^ _sel2((s >> 6) & 3, px, pz)
-                m = opc == OP_XPX
-                X[m] ^= pX[arg[m]]
-                m = opc == OP_ZPZ
-                Z[m] ^= pZ[arg[m]]
-                m = opc == OP_XPZ
-                X[m] ^= pZ[arg[m]]
-                m = opc == OP_R
-                X[m] = 0
-                Z[m] = 0
-                jlo = 64 * j
-                for q in np.nonzero(opc == OP_INJ)[0]:
-                    b1, b2 = int(arg[q]), (int(t.ops[off + k * qpad + q]) >> 8) & 0xFFFFFF
-                    for b in (b1, b2):
-                        if b != 0xFFFFFF and 0 <= b - jlo < 64:
-                            acc[q] |= U64(1 << (b - jlo))
-                for q in np.nonzero(opc == OP_M)[0]:
-                    inj = int(acc[q])
-                    b1 = int(arg[q])
-                    if 0 <= b1 - jlo < 64:
-                        inj |= 1 << (b1 - jlo)
-                    acc[q] = 0
-                    inj = U64(inj)
-                    if sub[q] & 4:
-                        X[q] = 0
-                        Z[q] = 0
-                    if (sub[q] & 3) != 1:
-                        X[q] ^= inj
-                    if (sub[q] & 3) != 0:
-                        Z[q] ^= inj
-                    last[q] = inj
-                m = opc == OP_SNAP
-                if m.any():
-                    snap[j, arg[m], 0] = X[m]
-                    snap[j, arg[m], 1] = Z[m]
-                m = opc == OP_SNAPD
-                if m.any():
-                    snap[j, arg[m], 0] = last[m]
-                    snap[j, arg[m], 1] = 0
-            e += 1
-        band[j] = (int(t.ep_ptoff[e0]), int(t.ep_ptoff[min(e, nE)]))
+        end0 = nE if K == s0 else bounds[s0 + 1]
+        e = walk_range(t, j, e0, end0, elast, X, Z, snap)
+        band[j] = (int(t.ep_ptoff[e0]), int(t.ep_ptoff[e if e < end0 else nE]))
+        rows = _unpack(X, Z)
+        for s in range(s0 + 1, K + 1):
+            if s > s0 + 1:  # compose through segment s - 1
+                p = s - 1
+                if p not in A:
+                    A[p] = transfer_matrix(t, bounds[p], bounds[p + 1])
+                cX = np.zeros(qpad, dtype=np.uint64)
+                cZ = np.zeros(qpad, dtype=np.uint64)
+                if bounds[p] <= elast:
+                    walk_range(t, j, bounds[p], bounds[p + 1], elast, cX, cZ)
+                rows = (A[p] @ rows + _unpack(cX, cZ)) & 1
+            v = _pack(rows)
+            X, Z = v[:qpad].copy(), v[qpad:].copy()
+            end = nE if s == K else bounds[s + 1]
+            e = walk_range(t, j, bounds[s], end, elast, X, Z, snap)
+            if e < end:
+                band[j, 1] = min(band[j, 1], int(t.ep_ptoff[e]))
     return snap, band
 
 

@@ -114,3 +114,37 @@ def test_text_reference_passes_utf8_without_copy():
         want = text if isinstance(text, bytes) else text.encode()
         assert n == len(want) and ctypes.string_at(addr, n) == want
     assert _text_ref(None) == (None, 0, None)
+
+
+@pytest.mark.parametrize("name", ["surface3", "surface5_golden", "bb6"])
+@pytest.mark.parametrize("target", [8, 24])
+def test_segmented_walk_matches_the_plain_walk(name, target):
+    """The walk cut into time segments (the segmented walk kernels' algorithm: first parts walked
+    from zero, later segments from entry rows composed through each segment's GF(2) transfer
+    matrix and its walk from zero) gives every mechanism the symptom of the uncut walk, at the
+    cuts the library plans."""
+    from tape_interp import expand, symptoms, walk, walk_segmented
+
+    text = {"surface3": SurfaceCode(3).get_memory(3, 1e-3, noise="uniform"),
+            "surface5_golden": SurfaceCode(5).get_memory(5, 1e-3),
+            "bb6": BBCode(6).get_memory(6, 1e-3, noise="uniform")}[name]
+    t = Tape(text, segment_target=target)
+    assert len(t.walk_bounds) > 2, "the plan should cut this walk"
+    mech = expand(t)
+    a = symptoms(t, *walk(t), mech)
+    b = symptoms(t, *walk_segmented(t, t.walk_bounds), mech)
+    assert (a == b).all()
+
+
+def test_walk_segments_cut_only_between_measurements():
+    """No planned cut splits a measurement: the first slot of a cut epoch holds no OP_INJ, OP_M or
+    OP_SNAPD (the ops that carry bits from the previous op of their slot)."""
+    from tape_interp import OP_INJ, OP_M, OP_SNAPD
+
+    t = Tape(BBCode(12).get_memory(12, 1e-3, noise="uniform"), segment_target=12)
+    b = t.walk_bounds
+    assert b[0] == 0 and b[-1] == t.num_epochs and (np.diff(b) > 0).all()
+    assert len(b) > 10
+    for e in b[1:-1]:
+        first = t.ops[int(t.ep_opoff[e]): int(t.ep_opoff[e]) + t.qpad] & np.uint64(0xFF)
+        assert not np.isin(first, [OP_INJ, OP_M, OP_SNAPD]).any()
