@@ -348,5 +348,9 @@ class BBCode(Code):
             hx[r, s] = 1
         for r, s in enumerate(zsup):
             hz[r, s] = 1
+        # the reference's logical basis for its own codes (bb_logicals); a basis
+        # computed from the check matrices for other parameters
+        from .bb_logicals import BB_LOGICAL_Z
+        lz = BB_LOGICAL_Z[d] if params == BB_PARAMS.get(d) and d in BB_LOGICAL_Z else _logicals(hx, hz)
         super().__init__(num_data=n, x_support=xsup, x_layers=xlay, z_support=zsup, z_layers=zlay,
-                         logical_z=_logicals(hx, hz))
+                         logical_z=lz)

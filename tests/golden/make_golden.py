@@ -11,9 +11,13 @@ It writes:
   rewritten in canonical form: targets sorted within an error, errors sorted
   by target list, probabilities printed with ``repr`` (exact round trip).
 * ``circuits.json`` -- SHA-256 digests of the reference's fixture circuits
-  (data/circuits/*.stim).  Surface-code circuits are hashed whole; BB-code
-  circuits are hashed with their OBSERVABLE_INCLUDE lines removed, because
-  this project's BB logical basis is its own.
+  (data/circuits/*.stim), hashed whole (BB-code circuits also without their
+  OBSERVABLE_INCLUDE lines, which a generator with another logical basis
+  would differ in).
+* ``codes.json`` -- SHA-256 digests of the reference's check matrices for
+  the BB codes without a fixture circuit (data/codes/bb/d18/H{x,z}.mtx, as
+  sorted (row, column, CNOT layer) triples, 0-based), so the generator's
+  [[288,12,18]] code is checked against the reference's definition.
 * ``kats.json`` -- known-answer values from the reference's unit tests.
 * ``circuits/iceberg_*.stim.gz`` -- the reference's concatenated
   (iceberg + surface) fixture circuits, static and adaptive outer-check
@@ -57,6 +61,24 @@ def canonical_dem(text: str) -> str:
     return "\n".join(out) + "\n"
 
 
+def triples_digest(triples) -> str:
+    """SHA-256 of sorted 0-based (row, column, value) triples, one 'r c v' line each."""
+    return hashlib.sha256("".join(f"{r} {c} {v}\n" for r, c, v in sorted(triples)).encode()).hexdigest()
+
+
+def mtx_digest(path: Path) -> str:
+    triples, header = [], False
+    for line in path.read_text().splitlines():
+        if line.startswith("%") or not line.strip():
+            continue
+        if not header:
+            header = True
+            continue
+        r, c, v = (int(x) for x in line.split())
+        triples.append((r - 1, c - 1, v))
+    return triples_digest(triples)
+
+
 def strip_observables(text: str) -> str:
     return "\n".join(l for l in text.splitlines() if not l.startswith("OBSERVABLE_INCLUDE")) + "\n"
 
@@ -78,8 +100,14 @@ def main() -> None:
             circ[path.stem] = {"sha256": hashlib.sha256(text.encode()).hexdigest(), "observables": True}
         elif path.stem.startswith("bb"):
             circ[path.stem] = {"sha256": hashlib.sha256(strip_observables(text).encode()).hexdigest(),
-                               "observables": False}
+                               "observables": False,
+                               "sha256_full": hashlib.sha256(text.encode()).hexdigest()}
     (HERE / "circuits.json").write_text(json.dumps(circ, indent=1, sort_keys=True) + "\n")
+    codes = {}
+    for d in (18,):
+        for m in ("Hx", "Hz"):
+            codes[f"bb{d}_{m}"] = mtx_digest(ref / "data" / "codes" / "bb" / f"d{d}" / f"{m}.mtx")
+    (HERE / "codes.json").write_text(json.dumps(codes, indent=1, sort_keys=True) + "\n")
     (HERE / "circuits").mkdir(exist_ok=True)
     for path in sorted((ref / "data" / "circuits").glob("iceberg_*.stim")):
         with open(HERE / "circuits" / (path.name + ".gz"), "wb") as f:

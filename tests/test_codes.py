@@ -1,7 +1,8 @@
 """Circuit generators against the reference's fixture circuits (data/circuits/*.stim).
 
-Surface-code circuits must match byte for byte; BB-code circuits must match on
-every line except OBSERVABLE_INCLUDE (this project computes its own logical basis).
+Surface- and BB-code circuits must match byte for byte (the BB codes take the
+reference's logical basis, greenpeas_gb300/bb_logicals.py); the [[288,12,18]]
+code, which has no fixture circuit, must have the reference's check matrices.
 """
 
 from __future__ import annotations
@@ -29,9 +30,26 @@ def test_surface_matches_reference(d):
 
 
 @pytest.mark.parametrize("d", [6, 10, 12])
-def test_bb_matches_reference_except_observables(d):
+def test_bb_matches_reference(d):
     text = BBCode(d).get_memory(rounds=d, p=0.001)
     assert hashlib.sha256(_strip_obs(text).encode()).hexdigest() == CIRC[f"bb{d}"]["sha256"]
+    assert hashlib.sha256(text.encode()).hexdigest() == CIRC[f"bb{d}"]["sha256_full"]
+
+
+def test_bb18_check_matrices_match_reference():
+    """[[288,12,18]] (l = m = 12): the X and Z checks, their data qubits and CNOT layers equal the
+    reference's data/codes/bb/d18/H{x,z}.mtx (digests in tests/golden/codes.json)."""
+    import importlib.util
+
+    spec = importlib.util.spec_from_file_location("make_golden", GOLDEN / "make_golden.py")
+    mg = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(mg)
+    triples_digest = mg.triples_digest
+    codes = json.loads((GOLDEN / "codes.json").read_text())
+    c = BBCode(18)
+    for name, sup, lay in (("Hx", c.x_support, c.x_layers), ("Hz", c.z_support, c.z_layers)):
+        triples = [(r, q, l) for r, (qs, ls) in enumerate(zip(sup, lay)) for q, l in zip(qs, ls)]
+        assert triples_digest(triples) == codes[f"bb18_{name}"], name
 
 
 @pytest.mark.parametrize("d,k", [(6, 12), (10, 8), (12, 12), (18, 12)])
