@@ -17,8 +17,9 @@ Lines printed (one JSON line on rank 0):
   roofline, cpu_baseline, clocks, gpu_launches, batch, grad, serve -- see main().
 
 ``--impl reference`` times the CPU FP64 oracle (a restatement of the
-reference's algorithm; the reference itself has no CPU path) on all host
-threads for the same workload.
+reference's algorithm; the reference itself has no CPU path) for the same
+workload in its fastest CPU configuration: one single-threaded process per
+host core, each compiling the workload.
 """
 
 from __future__ import annotations
@@ -41,12 +42,14 @@ UNIT = "DEM/s"
 WORKLOAD = "bb_144_12_12_r12_uniform_p1e-3"
 PEAKS_FILE = ROOT / "MEASURED_PEAKS.json"
 # kernels of one run of the pipeline on one circuit: key-block table, walk, keys,
-# warp grouping, large-bucket grouping, scan, emit
+# warp grouping, large-bucket grouping, scan, emit (the segmented walk is two launches)
 KERNELS_PER_RUN = 7
-# DRAM bytes (read + write) of one walk launch on the headline workload, from the ncu capture
-# summarised in profiles/headline_bb12_kernels.txt (cold cache: the tape is read once from DRAM,
-# the 28 word walks re-read it from L2, the snapshots stay in L2).
-WALK_DRAM_BYTES_PER_LAUNCH = 1_245_440
+# DRAM bytes (read + write) of the walk on the headline workload, from ncu captures (cold cache:
+# the tape is read once from DRAM, the word walks re-read it from L2): the plain walk launch
+# (profiles/headline_bb12_kernels.txt) and the two launches of the segmented walk
+# (profiles/headline_bb12_segmented_walk.txt).
+WALK_DRAM_BYTES_PLAIN = 1_245_440
+WALK_DRAM_BYTES_PER_RUN = None
 
 
 def workload_text() -> str:
@@ -128,80 +131,101 @@ def peaks() -> tuple:
         return 6800.0, "fallback"
 
 
-def run_reference(args, rank: int, world: int) -> None:
-    if rank != 0:
-        return
-    from oracle import oracle as O
-    text = workload_text()
-    threads = os.cpu_count() or 1
-    O.lib()
-    for _ in range(max(1, args.warmup)):
-        O.time_compile(text, 2, threads)
-    t = []
-    for _ in range(args.steps):
-        t0 = time.perf_counter()
-        O.time_compile(text, 2, threads)
-        t.append(time.perf_counter() - t0)
-    total = sum(t)
-    v = args.steps / total
-    sample = f"{args.steps} compiles of the workload after {max(1, args.warmup)} warm-up"
-    line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": world,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 bitsets, f64 probabilities",
-            "data": "synthetic (generated circuit)", "config": config(),
-            "cpu_baseline": {"value": v, "unit": UNIT, "cores": threads, "kind": "port",
-                             "sample": sample + "; the CPU FP64 oracle (the reference has no CPU implementation of this path)"},
-            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
-    print(json.dumps(line), flush=True)
+_worker_text = None
 
 
-def _oracle_rate(args) -> tuple:
-    """One process of the per-core CPU figure: single-threaded oracle compiles for a time budget."""
-    text, budget = args
+def _oracle_init(text: str) -> None:
+    global _worker_text
+    _worker_text = text
     if str(ROOT) not in sys.path:
         sys.path.insert(0, str(ROOT))
     from oracle import oracle as O
-    O.time_compile(text, 2, 1)
+    O.lib()
+
+
+def _oracle_one(_=None) -> int:
+    """One single-threaded oracle compile of the worker's workload."""
+    from oracle import oracle as O
+    O.time_compile(_worker_text, 2, 1)
+    return 1
+
+
+def _oracle_rate(args) -> tuple:
+    """Single-threaded oracle compiles for a time budget (one process of the per-core figure)."""
+    text, budget = args
+    _oracle_init(text)
+    _oracle_one()
     n, t0 = 0, time.perf_counter()
     while True:
-        O.time_compile(text, 2, 1)
+        _oracle_one()
         n += 1
         el = time.perf_counter() - t0
         if el > budget:
             return n, el
 
 
+def run_reference(args, rank: int, world: int) -> None:
+    """The CPU arm: the CPU FP64 oracle (the reference has no CPU implementation of this path) as
+    the fastest CPU configuration measured -- one single-threaded process per host core, each
+    compiling the workload (independent circuits, as a request stream gives them).  One step is
+    one compile on every core; W warm-up steps, then K timed."""
+    if rank != 0:
+        return
+    import multiprocessing as mp
+    text = workload_text()
+    cores = os.cpu_count() or 1
+    with mp.get_context("spawn").Pool(cores, initializer=_oracle_init, initargs=(text,)) as pool:
+        for _ in range(max(1, args.warmup)):
+            pool.map(_oracle_one, range(cores), chunksize=1)
+        t = []
+        for _ in range(args.steps):
+            t0 = time.perf_counter()
+            pool.map(_oracle_one, range(cores), chunksize=1)
+            t.append(time.perf_counter() - t0)
+    total = sum(t)
+    v = cores * args.steps / total
+    sample = (f"{args.steps} steps of one compile of the workload on each of {cores} single-threaded processes "
+              f"(one per host core) after {max(1, args.warmup)} warm-up steps; the CPU FP64 oracle")
+    line = {"metric": METRIC, "value": v, "unit": UNIT, "impl": "reference", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * total / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 bitsets, f64 probabilities",
+            "data": "synthetic (generated circuit)", "config": config(),
+            "cpu_baseline": {"value": v, "unit": UNIT, "cores": cores, "kind": "port", "sample": sample},
+            "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
 def cpu_baseline(text: str, budget_s: float = 10.0) -> dict:
+    """The oracle on the host cores: one single-threaded process per core (the headline figure:
+    the fastest CPU configuration), all threads on one compile, and one thread."""
+    import multiprocessing as mp
     from oracle import oracle as O
     threads = os.cpu_count() or 1
+    # processes are spawned, never forked after CUDA use
+    with mp.get_context("spawn").Pool(threads) as pool:
+        res = pool.map(_oracle_rate, [(text, budget_s / 2)] * threads)
+    per_core = sum(k / t for k, t in res)
     O.time_compile(text, 2, threads)
     n, t0 = 0, time.perf_counter()
     while True:
         O.time_compile(text, 2, threads)
         n += 1
         el = time.perf_counter() - t0
-        if el > budget_s or n >= 400:
+        if el > budget_s / 4 or n >= 400:
             break
-    # the same on one thread (a per-circuit figure)
     n1, t1 = 0, time.perf_counter()
     while True:
         O.time_compile(text, 2, 1)
         n1 += 1
         el1 = time.perf_counter() - t1
-        if el1 > budget_s / 3 or n1 >= 100:
+        if el1 > budget_s / 4 or n1 >= 100:
             break
-    # throughput with one single-threaded process per core (independent circuits, as a batch or a
-    # request stream would give them); processes are spawned, never forked after CUDA use
-    import multiprocessing as mp
-    with mp.get_context("spawn").Pool(threads) as pool:
-        res = pool.map(_oracle_rate, [(text, budget_s / 3)] * threads)
-    per_core = sum(k / t for k, t in res)
-    return {"value": n / el, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": f"{n} compiles of the workload in {el:.1f} s (CPU FP64 oracle, all host threads)",
-            "single_thread": {"value": n1 / el1, "unit": UNIT, "sample": f"{n1} compiles in {el1:.1f} s on one thread"},
-            "process_per_core": {"value": per_core, "unit": UNIT, "processes": threads,
-                                 "sample": f"{sum(k for k, _ in res)} compiles, one single-threaded process per core, "
-                                           f"{budget_s / 3:.1f} s each"}}
+    return {"value": per_core, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{sum(k for k, _ in res)} compiles of the workload, one single-threaded CPU FP64 oracle "
+                      f"process per host core, {budget_s / 2:.1f} s each",
+            "all_threads_one_compile": {"value": n / el, "unit": UNIT, "threads": threads,
+                                        "sample": f"{n} compiles in {el:.1f} s"},
+            "single_thread": {"value": n1 / el1, "unit": UNIT, "sample": f"{n1} compiles in {el1:.1f} s on one thread"}}
 
 
 def dem_arrays_equal(a, b) -> bool:
@@ -267,6 +291,7 @@ def batched_leg(gp, torch, local: int, flush, steps: int, warmup: int, circuits:
     plain_e2e_s = time.perf_counter() - t0
     raw = sum(d.num_raw_mechanisms for d in singles)
     merged = sum(d.num_errors for d in singles)
+    plain_fallbacks = plain.fallback_counts()
     del plain
 
     bdrv = gp.get_driver(texts[0], device=local)
@@ -325,11 +350,86 @@ def batched_leg(gp, torch, local: int, flush, steps: int, warmup: int, circuits:
                   "e2e": {"value": n / plain_e2e_s, "unit": UNIT}},
         "roofline": {"bound": "hbm", "unit": "GB/s", "peak": peak, "peak_source": peak_kind, "stages": roof,
                      "note": "walk bytes: each word's band of the tape (re-read from L2 across words) + snapshots"},
+        "fallbacks": {"batched": bdrv.fallback_counts(), "plain": plain_fallbacks},
         "speedup_device": batch_rate / plain_rate,
         "speedup_e2e": plain_e2e_s / batch_e2e_s,
         "tuning": tuning,
         "bit_exact_vs_plain": ok,
     }
+
+
+def plain_leg(gp, torch, local: int, flush, text: str, steps: int, warmup: int, e2e_steps: int) -> dict:
+    """One circuit per compile.  Device rate: CUDA events around each run of the kernel pipeline
+    on the driver's stream (tape resident in HBM, L2 flushed before each run, outside the
+    events); e2e: host text to host DEM arrays through the C ABI, wall clock."""
+    drv = gp.get_driver(text, device=local)
+    ext = torch.cuda.ExternalStream(drv.stream, device=torch.device("cuda", local))
+    ref_dem = drv.compile(text)  # also checks the run completes
+    sizes = drv.last_sizes()
+    drv.prepare(text)
+    for _ in range(warmup):
+        drv.run_device()
+    torch.cuda.synchronize()
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+    with torch.cuda.stream(ext):
+        for i in range(steps):
+            flush.fill_(float(i))  # evict the tape and scratch from L2 (not timed)
+            ev[i][0].record(ext)
+            drv.run_device()
+            ev[i][1].record(ext)
+    torch.cuda.synchronize()
+    step_ms = [a.elapsed_time(b) for a, b in ev]
+    stage = {"walk": 0.0, "key": 0.0, "sort": 0.0, "merge": 0.0, "total": 0.0}
+    nstage = min(20, steps)
+    for i in range(nstage):  # per-stage times (events inside the pipeline)
+        with torch.cuda.stream(ext):
+            flush.fill_(float(i))
+        drv.run_device()
+        t = drv.last_timings()
+        for k in stage:
+            stage[k] += t[k] / nstage
+    dem_dev = drv.fetch()
+    traffic = drv.last_traffic()
+    for _ in range(warmup):
+        drv.compile(text)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        dem = drv.compile(text)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    h2d, d2h = drv.last_io_bytes()
+    if dem_dev.canonical() != ref_dem.canonical() or dem.canonical() != ref_dem.canonical():
+        raise SystemExit("bench: results changed between runs")
+    return {"drv": drv, "step_ms": step_ms, "dev_ms": sum(step_ms), "stage": stage, "traffic": traffic,
+            "sizes": sizes, "merged": ref_dem.num_errors, "e2e_s": e2e_s, "e2e_steps": e2e_steps, "h2d": h2d,
+            "d2h": d2h, "walk_plan": drv.walk_segments(), "fallbacks": drv.fallback_counts()}
+
+
+# The plain-method configurations beside the headline: surface d = 3 (3 rounds), [[72,12,6]]
+# (6 rounds), [[288,12,18]] (18 rounds), uniform circuit-level noise p = 1e-3.
+SWEEP = (("surface_d3_r3_uniform_p1e-3", lambda gp: gp.SurfaceCode(3).get_memory(3, 1e-3, noise="uniform")),
+         ("bb_72_12_6_r6_uniform_p1e-3", lambda gp: gp.BBCode(6).get_memory(6, 1e-3, noise="uniform")),
+         ("bb_288_12_18_r18_uniform_p1e-3", lambda gp: gp.BBCode(18).get_memory(18, 1e-3, noise="uniform")))
+NOMINAL_HBM_GBS = 8000.0
+
+
+def sweep_entry(r: dict) -> dict:
+    peak, kind = peaks()
+    n = len(r["step_ms"])
+    v = n / (r["dev_ms"] / 1e3)
+    walk_gbs = r["traffic"]["walk"] / (r["stage"]["walk"] / 1e3) / 1e9
+    return {"value": v, "unit": UNIT, "ms_per_step": r["dev_ms"] / n,
+            "e2e": {"value": r["e2e_steps"] / r["e2e_s"], "unit": UNIT, "h2d_bytes_per_step": r["h2d"],
+                    "d2h_bytes_per_step": r["d2h"]},
+            "mechanisms_per_s": {"raw": v * r["sizes"]["raw"], "merged": v * r["merged"]},
+            "raw_mechanisms": r["sizes"]["raw"], "merged_mechanisms": r["merged"], "words": r["sizes"]["words"],
+            "epochs": r["sizes"]["epochs"], "stage_ms": r["stage"], "walk_segments": r["walk_plan"],
+            "walk_roofline": {"algorithmic_bytes": r["traffic"]["walk"], "ms": r["stage"]["walk"],
+                              "achieved": walk_gbs, "unit": "GB/s", "frac_of_measured": walk_gbs / peak,
+                              "peak_measured": peak, "peak_source": kind,
+                              "frac_of_nominal_8tbs": walk_gbs / NOMINAL_HBM_GBS},
+            "fallbacks": r["fallbacks"]}
 
 
 def batch_workload_texts(circuits: int) -> list:
@@ -368,6 +468,7 @@ def serving_leg(gp, requests: int, cap_requests: int, slots: int, max_batch: int
             on_batch = {"requests": bc["requests"], "dems_per_s": bc["dems_per_s"],
                         "plain_e2e_dems_per_s": batch_plain_e2e,
                         "speedup_vs_plain_e2e": bc["dems_per_s"] / batch_plain_e2e if batch_plain_e2e else None}
+        fallbacks = srv.fallback_counts()
     # the plain per-circuit path on the same mix: one driver, one circuit per
     # compile, over every `plain_every`-th request of the capacity burst (a
     # sample of the same size distribution)
@@ -389,6 +490,7 @@ def serving_leg(gp, requests: int, cap_requests: int, slots: int, max_batch: int
                                                           f"({len(texts)})",
         "speedup_capacity_vs_plain_e2e": cap["dems_per_s"] / plain,
         "on_batch_workload": on_batch,
+        "fallbacks": fallbacks,
     }
 
 
@@ -460,6 +562,7 @@ def main() -> None:
                     help="batch leg with --batch-device-only: 1 one persistent walk launch, -1 per-class launches")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
     ap.add_argument("--no-grad", action="store_true", help="skip the noise-rate gradient leg")
+    ap.add_argument("--no-sweep", action="store_true", help="skip the plain-method configuration sweep")
     ap.add_argument("--serve-requests", type=int, default=10000)
     ap.add_argument("--serve-slots", type=int, default=4)
     ap.add_argument("--serve-batch", type=int, default=16)
@@ -493,57 +596,17 @@ def main() -> None:
             print(json.dumps(out), flush=True)
         return
     text = workload_text()
-    drv = gp.get_driver(text, device=local)
-    ext = torch.cuda.ExternalStream(drv.stream, device=torch.device("cuda", local))
-    ref_dem = drv.compile(text)  # also checks the run completes without fallbacks
-    sizes = drv.last_sizes()
 
     def barrier():
         if dist is not None:
             dist.barrier()
         torch.cuda.synchronize()
 
+    barrier()
     with ClockSampler(local) as clocks:
-        # ---- device-resident steps -----------------------------------------
-        drv.prepare(text)
-        for _ in range(args.warmup):
-            drv.run_device()
-        torch.cuda.synchronize()
-        stage = {"walk": 0.0, "key": 0.0, "sort": 0.0, "merge": 0.0, "total": 0.0}
-        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
-        barrier()
-        with torch.cuda.stream(ext):
-            for i in range(args.steps):
-                flush.fill_(float(i))  # evict the tape and scratch from L2 (not timed)
-                ev[i][0].record(ext)
-                drv.run_device()
-                ev[i][1].record(ext)
-        torch.cuda.synchronize()
-        step_ms = [a.elapsed_time(b) for a, b in ev]
-        dev_ms = sum(step_ms)
-        # per-stage times on a few steps (events inside the pipeline)
-        nstage = min(20, args.steps)
-        for i in range(nstage):
-            with torch.cuda.stream(ext):
-                flush.fill_(float(i))
-            drv.run_device()
-            t = drv.last_timings()
-            for k in stage:
-                stage[k] += t[k] / nstage
-        dem_dev = drv.fetch()
-        traffic = drv.last_traffic()
-        barrier()
-        # ---- end to end through the C ABI ---------------------------------
-        for _ in range(args.warmup):
-            drv.compile(text)
-        barrier()
-        t0 = time.perf_counter()
-        for _ in range(args.steps):
-            dem = drv.compile(text)
-        torch.cuda.synchronize()
-        e2e_s = time.perf_counter() - t0
-        h2d, d2h = drv.last_io_bytes()
-
+        r = plain_leg(gp, torch, local, flush, text, args.steps, args.warmup, args.steps)
+    barrier()
+    dev_ms, e2e_s = r["dev_ms"], r["e2e_s"]
     if dist is not None:
         tt = torch.tensor([dev_ms, e2e_s], device=f"cuda:{local}", dtype=torch.float64)
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
@@ -551,15 +614,13 @@ def main() -> None:
     if rank != 0:
         dist.destroy_process_group()
         return
-    if dem_dev.canonical() != ref_dem.canonical() or dem.canonical() != ref_dem.canonical():
-        raise SystemExit("bench: results changed between runs")
-
+    stage, traffic, sizes = r["stage"], r["traffic"], r["sizes"]
     value = world * args.steps / (dev_ms / 1e3)
     e2e = world * args.steps / e2e_s
-    ms_sorted = sorted(step_ms)
+    ms_sorted = sorted(r["step_ms"])
     p50 = ms_sorted[len(ms_sorted) // 2]
     p99 = ms_sorted[min(len(ms_sorted) - 1, int(0.99 * len(ms_sorted)))]
-    # roofline of the dominant kernel (HBM-bound integer/bitset work)
+    # roofline of the dominant stage (HBM-bound integer/bitset work)
     names = {"walk": "walk", "key": "key", "sort": "bucket", "merge": "merge"}
     dom = max(("walk", "key", "sort", "merge"), key=lambda k: stage[k])
     achieved = traffic[names[dom]] / (stage[dom] / 1e3) / 1e9
@@ -569,33 +630,49 @@ def main() -> None:
     # dense-symptom pipeline (8w bytes per raw mechanism written and re-read,
     # 16-byte keys + 4-byte permutation through an 8-pass radix sort):
     # B = 8wM + 24M + T  +  2*8*20*M  +  28M + 8wM + C(8w + 8), T = tape bytes (the H2D).
-    M, w, C = sizes["raw"], sizes["words"], ref_dem.num_errors
-    dense = (8 * w * M + 24 * M + h2d) + 2 * 8 * 20 * M + (28 * M + 8 * w * M + C * (8 * w + 8))
+    M, w, C = sizes["raw"], sizes["words"], r["merged"]
+    dense = (8 * w * M + 24 * M + r["h2d"]) + 2 * 8 * 20 * M + (28 * M + 8 * w * M + C * (8 * w + 8))
     stored = sum(traffic.values())
     pipe_s = stage["total"] / 1e3
     pipeline = {"ms": stage["total"], "algorithmic_bytes_stored": stored, "achieved_stored": stored / pipe_s / 1e9,
                 "algorithmic_bytes_dense": dense, "achieved_dense": dense / pipe_s / 1e9,
                 "frac_dense": dense / pipe_s / 1e9 / peak}
+    plan = r["walk_plan"]
+    walk_launches = 2 if plan["segments"] else 1
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": dev_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "u64 bitsets, f64 probabilities", "data": "synthetic (generated circuit)",
-        "config": config({"raw_mechanisms": sizes["raw"], "merged_mechanisms": ref_dem.num_errors,
+        "config": config({"raw_mechanisms": sizes["raw"], "merged_mechanisms": C,
                           "qubits": sizes["qubits"], "words": sizes["words"], "epochs": sizes["epochs"],
                           "snapshot_points": sizes["points"]}),
-        "mechanisms_per_s": {"raw": value * sizes["raw"], "merged": value * ref_dem.num_errors},
+        "mechanisms_per_s": {"raw": value * sizes["raw"], "merged": value * C},
         "latency_ms": {"p50": p50, "p99": p99, "e2e_mean": 1e3 * e2e_s / args.steps},
         "stage_ms": stage,
-        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "walk_segments": plan,
+        "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"]},
         "roofline": {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_kind,
+                     "frac_of_nominal_8tbs": achieved / NOMINAL_HBM_GBS,
                      "algorithmic_bytes": traffic[names[dom]],
-                     "traffic": WALK_DRAM_BYTES_PER_LAUNCH if dom == "walk" else None,
-                     "note": "latency-bound: one CTA per 64-bit detector word walks the circuit",
+                     "traffic": (WALK_DRAM_BYTES_PER_RUN if plan["segments"] else WALK_DRAM_BYTES_PLAIN)
+                     if dom == "walk" else None,
+                     "note": "latency-bound: word walks cut into time segments walked side by side",
                      "pipeline": pipeline},
-        "gpu_launches": KERNELS_PER_RUN * args.steps,
+        "fallbacks": r["fallbacks"],
+        # key-block table, walk launch(es), keys, warp grouping, large-bucket grouping, scan, emit
+        "gpu_launches": (KERNELS_PER_RUN - 1 + walk_launches) * args.steps,
         "clocks": clocks.summary(),
     }
+    del r
+    if world == 1 and not args.no_sweep:
+        sweep = {}
+        for name, make in SWEEP:
+            sweep[name] = sweep_entry(plain_leg(gp, torch, local, flush, make(gp), min(args.steps, 30),
+                                                args.warmup, min(args.steps, 20)))
+        sweep["bb_144_12_12_r12_uniform_p1e-3"] = {"value": value, "e2e": line["e2e"],
+                                                   "note": "the headline line above"}
+        line["plain_sweep"] = sweep
     # the other forms and the CPU baseline are single-GPU measurements (a multi-GPU
     # run reports the replicated headline only)
     if not args.no_batch and world == 1:
@@ -603,7 +680,7 @@ def main() -> None:
                                     warmup=args.warmup, circuits=args.batch_circuits, walk_queue=args.walk_queue,
                                     device_only=args.batch_device_only)
     if not args.no_grad and world == 1:
-        line["grad"] = grad_leg(gp, torch)
+        line["grad"] = grad_leg(gp, torch, fd_entries=64)
     if not args.no_serve and world == 1:
         # capacity from a burst long enough that filling and draining the
         # pipeline is a small part of it (1,000 requests: ~0.2 s, 5-15% low)

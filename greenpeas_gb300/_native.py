@@ -30,6 +30,7 @@ EXPORTS = [
     "gpc_param_prepare", "gpc_param_forward", "gpc_param_probs", "gpc_param_backward",
     "gpc_server_create", "gpc_server_submit", "gpc_server_wait", "gpc_server_stats", "gpc_server_destroy",
     "gpc_device_dem", "gpc_autotune", "gpc_last_host_timings", "gpc_walk_form", "gpc_walk_segments",
+    "gpc_fallback_counts", "gpc_server_fallback_counts",
 ]
 
 
@@ -124,6 +125,8 @@ def lib() -> ctypes.CDLL:
     L.gpc_tape_get_view.argtypes = [vp, ctypes.POINTER(TapeView)]
     L.gpc_tape_walk_segments.argtypes = [vp, u32, u32p, u32, u32p]
     L.gpc_walk_segments.argtypes = [vp, u32p, u32p, u32p]
+    L.gpc_fallback_counts.argtypes = [vp, u64p]
+    L.gpc_server_fallback_counts.argtypes = [vp, u64p]
     L.gpc_tape_free.argtypes = [vp]
     L.gpc_tape_free.restype = None
     L.gpc_tape_last_error.restype = ctypes.c_char_p
@@ -145,7 +148,8 @@ def lib() -> ctypes.CDLL:
               "gpc_dem_text", "gpc_prepare", "gpc_run_device", "gpc_fetch", "gpc_last_timings",
               "gpc_last_sizes", "gpc_tape_lower", "gpc_tape_get_view", "gpc_last_traffic", "gpc_last_io_bytes",
               "gpc_merge_mechanisms_static", "gpc_prepare_batch", "gpc_fetch_batch", "gpc_last_host_timings", "gpc_walk_form",
-              "gpc_tape_walk_segments", "gpc_walk_segments"):
+              "gpc_tape_walk_segments", "gpc_walk_segments", "gpc_fallback_counts",
+              "gpc_server_fallback_counts"):
         getattr(L, f).restype = i32
     _lib = L
     return L

@@ -838,13 +838,14 @@ struct gpc_driver {
   // [[144,12,12]] r12 77 -> 41 us at 32 (16: 53, 48: 42), surface d = 7 61 ->
   // 34, d = 11 86 -> 41, [[72,12,6]] 42 -> 30, [[288,12,18]] 129 -> 77 (48:
   // 69); surface d = 3 walks 17 epochs and stays whole (segmenting it costs
-  // 2-5 us).  A compose step costs about 1 us (instruction latency of one CTA
+  // 2-5 us; its longest walk costs 123 units, under kSegMinSpan segments).
+  // A compose step costs about 1 us (instruction latency of one CTA
   // over a sparse transfer matrix), a segment epoch about 0.8 us.  Segment
   // walks copy the tape in chunks of at most kSegChunk bytes that never cross
   // a cut, so several segment CTAs share an SM and a segment's first copy is
   // short.
   static constexpr uint32_t kSegTarget = 32;
-  static constexpr uint32_t kSegMinSpan = 3;
+  static constexpr uint32_t kSegMinSpan = 4;
   static constexpr uint32_t kSegChunk = 24 * 1024;
   // A detector word's rows vanish some epochs after its last measurement
   // (the walk reaches the resets of the qubits they sit on); its segments
@@ -1208,6 +1209,12 @@ struct gpc_driver {
 
   enum class Finish { Ok, BatchFallback };
 
+  // How often a run left the fast path (gpc_fallback_counts): [0] batches
+  // compiled circuit by circuit, [1] runs through the global sort (a bucket
+  // overflowed), [2] reruns with wider target lists (a long symptom), [3]
+  // full 128-bit re-sorts, [4] target-buffer regrowths.
+  std::atomic<uint64_t> fallbacks[5] = {};
+
   // Reads flags and totals; handles the rare fallbacks (bucket overflow,
   // long symptoms, short sort keys, target-buffer growth).
   Finish finish(uint32_t *groups, uint32_t *targets) {
@@ -1222,9 +1229,12 @@ struct gpc_driver {
       if (err & gpc::DEV_ERR_TIMEOUT) throw gpc::Error(GPC_ERR_TIMEOUT, "a bounded device wait timed out");
       if (err & gpc::DEV_ERR_COLLISION)
         throw gpc::Error(GPC_ERR_COLLISION, "two different symptoms share a 128-bit key");
-      if ((err & (gpc::DEV_FLAG_LONG | gpc::DEV_FLAG_BIG_BUCKET)) && !used_global && ncirc() > 1)
+      if ((err & (gpc::DEV_FLAG_LONG | gpc::DEV_FLAG_BIG_BUCKET)) && !used_global && ncirc() > 1) {
+        ++fallbacks[0];
         return Finish::BatchFallback;  // compile the batch's circuits one by one
+      }
       if ((err & gpc::DEV_FLAG_LONG) && !used_global) {
+        ++fallbacks[2];
         // a symptom longer than the target-list stride: widen it (or merge from
         // the snapshots) and run again
         if (tcap < 256) {
@@ -1239,6 +1249,7 @@ struct gpc_driver {
         continue;
       }
       if ((err & gpc::DEV_FLAG_BIG_BUCKET) && !used_global) {
+        ++fallbacks[1];
         // a symptom repeated more often than a bucket holds: sort globally
         // (the bucket pass skipped the keys and descriptors this path reads)
         CK(cudaMemsetAsync(dptr<char>(L.err), 0, 4, stream));
@@ -1248,6 +1259,7 @@ struct gpc_driver {
         continue;
       }
       if (used_global && (err & gpc::DEV_FLAG_MIXED) && !did_full) {
+        ++fallbacks[3];
         // equal sort keys with different full keys: sort on all 128 bits
         CK(cudaMemsetAsync(dptr<char>(L.err), 0, 4, stream));
         run_global(true);
@@ -1255,6 +1267,7 @@ struct gpc_driver {
         continue;
       }
       if (err & gpc::DEV_FLAG_TG_OVF) {
+        ++fallbacks[4];
         const uint32_t need = h[2];
         tgbuf.ensure((size_t)need * 4 + 1024);
         tg_cap = (uint32_t)std::min<size_t>(0xFFFFFFF0ull, tgbuf.cap / 4);
@@ -2239,6 +2252,28 @@ gpc_status gpc_server_wait(gpc_server *server, uint64_t ticket, double timeout_s
   if (latency_s) *latency_s = std::chrono::duration<double>(r->t1 - r->t0).count();
   if (r->status != GPC_OK) return fail(r->status, r->msg);
   *out = r->dem;
+  return GPC_OK;
+}
+
+gpc_status gpc_fallback_counts(gpc_driver *driver, uint64_t *counts5) {
+  if (!driver || !counts5) return fail(GPC_ERR_INVALID, "null argument");
+  for (int i = 0; i < 5; ++i) {
+    counts5[i] = driver->fallbacks[i].load();
+    if (driver->partner) counts5[i] += driver->partner->fallbacks[i].load();
+  }
+  return GPC_OK;
+}
+
+gpc_status gpc_server_fallback_counts(gpc_server *server, uint64_t *counts5) {
+  if (!server || !counts5) return fail(GPC_ERR_INVALID, "null argument");
+  for (int i = 0; i < 5; ++i) counts5[i] = 0;
+  std::lock_guard<std::mutex> lk(server->mu);
+  for (const auto &d : server->drivers) {
+    if (!d) continue;
+    uint64_t c[5];
+    gpc_fallback_counts(d.get(), c);
+    for (int i = 0; i < 5; ++i) counts5[i] += c[i];
+  }
   return GPC_OK;
 }
 

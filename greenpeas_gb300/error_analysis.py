@@ -21,6 +21,9 @@ from . import _native
 from .dem import DetectorErrorModel
 
 
+FALLBACK_NAMES = ("batch_per_circuit", "global_sort", "wider_lists", "full_key_resort", "target_regrowth")
+
+
 class CorrelationLevel(enum.IntEnum):
     """Pauli components kept per depolarizing channel (Mixer.hpp:13-20)."""
 
@@ -171,6 +174,12 @@ class Driver:
     @property
     def handle(self) -> ctypes.c_void_p:
         return self._h
+
+    def fallback_counts(self) -> dict:
+        """How often this driver left the fast path (gpc_fallback_counts)."""
+        c = (ctypes.c_uint64 * 5)()
+        _native.check(_native.lib().gpc_fallback_counts(self._h, c))
+        return dict(zip(FALLBACK_NAMES, (int(x) for x in c)))
 
     def walk_segments(self) -> dict:
         """The segmented walk of the prepared single circuit: segments (0: not segmented) and the

@@ -72,6 +72,13 @@ class Server:
         _native.check(_native.lib().gpc_server_stats(self._h, *(ctypes.byref(x) for x in v)))
         return dict(zip(("completed", "batches", "budget_used", "budget_peak"), (int(x.value) for x in v)))
 
+    def fallback_counts(self) -> dict:
+        """Fallbacks taken by the workers' drivers, summed (Driver.fallback_counts)."""
+        from .error_analysis import FALLBACK_NAMES
+        c = (ctypes.c_uint64 * 5)()
+        _native.check(_native.lib().gpc_server_fallback_counts(self._h, c))
+        return dict(zip(FALLBACK_NAMES, (int(x) for x in c)))
+
 
 def replay(server: Server, requests, keep=None) -> dict:
     """Submits ``requests`` -- (arrival time in s, circuit text or a callable returning it) -- at their

@@ -227,6 +227,8 @@ gpc_status gpc_server_submit(gpc_server *server, const char *stim_text, size_t l
 gpc_status gpc_server_wait(gpc_server *server, uint64_t ticket, double timeout_s, gpc_dem **out, double *latency_s);
 gpc_status gpc_server_stats(gpc_server *server, uint64_t *completed, uint64_t *batches, uint64_t *budget_used,
                             uint64_t *budget_peak);
+/* Fallbacks taken by a server's workers, summed (as gpc_fallback_counts). */
+gpc_status gpc_server_fallback_counts(gpc_server *server, uint64_t *counts5);
 void gpc_server_destroy(gpc_server *server);
 
 /* The driver's CUDA stream (a cudaStream_t), for callers that time it. */
@@ -248,6 +250,16 @@ gpc_status gpc_last_host_timings(gpc_driver *driver, double *ms6);
  * `launches` per run (one per thread-count class, or 1), `persistent` 1 when
  * the batch walks in one persistent launch off its work queue. */
 gpc_status gpc_walk_form(gpc_driver *driver, int32_t *launches, int32_t *persistent);
+
+/* How often this driver (and the second pipeline of its chunked batches)
+ * left the fast path since it was created (no counterpart in the reference):
+ * counts5[0] batches compiled circuit by circuit instead (a circuit needed
+ * one of the fallbacks below), [1] runs merged through the global radix sort
+ * (a symptom repeated more often than a bucket's 256 slots), [2] reruns with
+ * wider target lists (a symptom longer than the list stride), [3] full
+ * 128-bit re-sorts on the global path, [4] reruns of scan + emit after the
+ * target buffer grew. */
+gpc_status gpc_fallback_counts(gpc_driver *driver, uint64_t *counts5);
 
 /* Segmented walk of the prepared single circuit (no counterpart in the
  * reference): `segments` the time segments its walk is cut into (0: not
