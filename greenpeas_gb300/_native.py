@@ -30,7 +30,7 @@ EXPORTS = [
     "gpc_param_prepare", "gpc_param_forward", "gpc_param_probs", "gpc_param_backward",
     "gpc_server_create", "gpc_server_submit", "gpc_server_wait", "gpc_server_stats", "gpc_server_destroy",
     "gpc_device_dem", "gpc_autotune", "gpc_last_host_timings", "gpc_walk_form", "gpc_walk_segments",
-    "gpc_fallback_counts", "gpc_server_fallback_counts",
+    "gpc_fallback_counts", "gpc_server_fallback_counts", "gpc_alloc_counts",
 ]
 
 
@@ -51,7 +51,9 @@ class ServerOptions(ctypes.Structure):
 class Options(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("sort_bits", ctypes.c_int32), ("global_sort", ctypes.c_int32),
                 ("walk_qpt", ctypes.c_int32), ("bucket_mean", ctypes.c_int32), ("walk_words", ctypes.c_int32),
-                ("key_split", ctypes.c_int32), ("walk_queue", ctypes.c_int32), ("walk_segment", ctypes.c_int32)]
+                ("key_split", ctypes.c_int32), ("walk_queue", ctypes.c_int32), ("walk_segment", ctypes.c_int32),
+                ("wait_limit_us", ctypes.c_int32), ("test_hold_tile", ctypes.c_int32),
+                ("test_fail_alloc", ctypes.c_int32)]
 
 
 class TuningEntry(ctypes.Structure):
@@ -126,6 +128,7 @@ def lib() -> ctypes.CDLL:
     L.gpc_tape_walk_segments.argtypes = [vp, u32, u32p, u32, u32p]
     L.gpc_walk_segments.argtypes = [vp, u32p, u32p, u32p]
     L.gpc_fallback_counts.argtypes = [vp, u64p]
+    L.gpc_alloc_counts.argtypes = [vp, u64p, u64p]
     L.gpc_server_fallback_counts.argtypes = [vp, u64p]
     L.gpc_tape_free.argtypes = [vp]
     L.gpc_tape_free.restype = None
@@ -149,7 +152,7 @@ def lib() -> ctypes.CDLL:
               "gpc_last_sizes", "gpc_tape_lower", "gpc_tape_get_view", "gpc_last_traffic", "gpc_last_io_bytes",
               "gpc_merge_mechanisms_static", "gpc_prepare_batch", "gpc_fetch_batch", "gpc_last_host_timings", "gpc_walk_form",
               "gpc_tape_walk_segments", "gpc_walk_segments", "gpc_fallback_counts",
-              "gpc_server_fallback_counts"):
+              "gpc_server_fallback_counts", "gpc_alloc_counts"):
         getattr(L, f).restype = i32
     _lib = L
     return L

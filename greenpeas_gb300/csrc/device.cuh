@@ -170,6 +170,21 @@ struct SlotTail {
   double p;
 };
 static_assert(sizeof(SlotTail) == 16, "slot tail is 16 bytes");
+// A slot: key and tail side by side, so a mechanism's item is one 32-byte
+// sector written once and read once.  After grouping, the key half of slot s
+// holds the saved permutation as two 32-bit words: [0] the mechanism at
+// sorted position s, [1] (for s < groups) the first sorted position of group s.
+struct Slot {
+  ulonglong2 key;
+  SlotTail tail;
+};
+static_assert(sizeof(Slot) == 32, "a slot is one 32-byte sector");
+__host__ __device__ __forceinline__ uint32_t *slot_perm(Slot *bucket, uint32_t s) {
+  return reinterpret_cast<uint32_t *>(&bucket[s].key);
+}
+__host__ __device__ __forceinline__ const uint32_t *slot_perm(const Slot *bucket, uint32_t s) {
+  return reinterpret_cast<const uint32_t *>(&bucket[s].key);
+}
 
 struct KeyLaunch {
   const CircuitDev *circs;  // [n_circ]
@@ -178,8 +193,7 @@ struct KeyLaunch {
   uint2 *blk_info;          // [key blocks] (record of the block's first mechanism, its circuit | spans << 31)
   ulonglong2 *key;          // [M]
   uint32_t *bucket_count;   // [buckets of the batch] (zeroed)
-  ulonglong2 *skey;         // [buckets * SLOT_CAP] slot keys
-  SlotTail *stail;          // [buckets * SLOT_CAP] slot tails
+  Slot *slot;               // [buckets * SLOT_CAP] bucket slots
   uint32_t *list_total;     // += targets written to the lists (for traffic accounting)
   uint32_t *err;
   uint32_t write_all;       // also write key[], and descriptors/probabilities (global path, gradients)
@@ -242,10 +256,8 @@ struct GroupLaunch {
   const uint32_t *tl;       // [M][tcap] batch-wide target lists
   const uint32_t *tn;       // [M]
   uint32_t tcap;
-  ulonglong2 *skey;         // [nb * SLOT_CAP] keys; afterwards, as 32-bit pairs, the saved
-                            // permutation: [2s] mechanism at sorted position s, [2g+1] first
-                            // sorted position of group g
-  SlotTail *stail;          // [nb * SLOT_CAP] items, then group records
+  Slot *slot;               // [nb * SLOT_CAP] items; afterwards the saved permutation in the
+                            // key halves (slot_perm) and one group record per group in the tails
   const uint32_t *count;    // [nb]
   uint32_t nb;
   uint2 *bagg;              // [nb] (groups, targets) of each bucket
@@ -288,11 +300,12 @@ cudaError_t launch_param_rec(const ParamLaunch &L, cudaStream_t s);
 //          slope at the source's rate (stab[src][kind], filled by the host);
 //  source: dL/dnoise[e] = sum over the records of source e, in record order.
 struct AdjointLaunch {
-  const ulonglong2 *skey;  // saved permutation (see GroupLaunch)
+  const Slot *slot;        // saved permutation (see GroupLaunch)
   const uint32_t *count;
   const uint2 *bagg, *bout;
   uint32_t nb;
-  const double *mp;        // [M] mechanism probabilities of the forward
+  const uint2 *blk_info;   // [key blocks] record of each key block's first mechanism (the forward's key pass)
+  const double *rec_p;     // [R] each record's component probability of the forward (from the noise tensor)
   const double *grad_out;  // [groups] dL/dp of each merged mechanism
   double *gq;              // [M] (zeroed) dL/dq of each mechanism
   const uint64_t *rec;
@@ -314,6 +327,10 @@ struct SortScratch {
   uint32_t *status;    // [passes][tiles][RADIX]
   uint32_t *tile_ctr;  // [passes]
   uint32_t *err;
+  unsigned long long spin_ns;  // a look-back wait gives up (DEV_ERR_TIMEOUT) after this long
+  // Test of the bounded look-back: tile 0 of the first pass keeps its digit
+  // counts to itself, so the waits of the tiles after it run out.
+  uint32_t hold_first;
 };
 size_t sort_scratch_words(uint32_t n, uint32_t bits);
 cudaError_t launch_sort(uint64_t *keys, uint64_t *keys_alt, uint32_t *vals, uint32_t *vals_alt, uint32_t n,
@@ -341,6 +358,7 @@ struct MergeLaunch {
   uint32_t *tile_ctr;
   uint32_t *totals;  // [0] groups, [1] targets
   uint32_t *err;
+  unsigned long long spin_ns;  // a look-back wait gives up (DEV_ERR_TIMEOUT) after this long
 };
 cudaError_t launch_merge(const MergeLaunch &L, cudaStream_t s);
 

@@ -58,15 +58,31 @@ size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 // thread is one of them); rethrows the first exception after all joined.
 uint32_t host_threads() { return std::max(1u, std::thread::hardware_concurrency()); }
 
+// Device allocations of one driver: counted, and (a test of the failure
+// path) the allocation numbered fail_at fails once as if the device were out
+// of memory.
+struct AllocCounter {
+  uint64_t allocs = 0, frees = 0;
+  int64_t fail_at = -1;  // -1: never
+};
+
 // Grow-only device allocation.
 struct DevBuf {
   void *p = nullptr;
   size_t cap = 0;
+  AllocCounter *ctr = nullptr;
   void ensure(size_t bytes) {
     if (bytes <= cap) return;
-    if (p) CK(cudaFree(p));
+    if (p) {
+      CK(cudaFree(p));
+      if (ctr) ++ctr->frees;
+    }
     p = nullptr;
     cap = 0;
+    if (ctr && ctr->fail_at >= 0 && ctr->allocs == (uint64_t)ctr->fail_at) {
+      ctr->fail_at = -1;
+      throw gpc::Error(GPC_ERR_OOM, "device allocation of " + std::to_string(bytes) + " bytes failed (injected)");
+    }
     size_t want = std::max(bytes, cap + cap / 2);
     cudaError_t e = cudaMalloc(&p, want);
     if (e != cudaSuccess) {
@@ -79,9 +95,13 @@ struct DevBuf {
       want = bytes;
     }
     cap = want;
+    if (ctr) ++ctr->allocs;
   }
   void release() {
-    if (p) cudaFree(p);
+    if (p) {
+      cudaFree(p);
+      if (ctr) ++ctr->frees;
+    }
     p = nullptr;
     cap = 0;
   }
@@ -129,7 +149,7 @@ struct Layout {
   std::vector<CircLayout> c;
   size_t cdev, items, mbase, cbbase;
   size_t in_bytes;
-  size_t mdesc, mp, tl, tn, key, blk_r0, skey, stail, bagg, bout, cout, big_list;
+  size_t mdesc, mp, tl, tn, key, blk_r0, slot, bagg, bout, cout, big_list;
   size_t zero, err, totals, bcount, tsum, big_n, wq, zero_bytes;
   size_t sk0, sk1, pm0, pm1, hik;  // global path (single circuit)
   size_t src_off, src_rec, gq, grad_rec, ptab;  // noise-rate gradients (single circuit)
@@ -192,7 +212,8 @@ struct gpc_driver {
   bool prepared = false;
   bool ran = false;
   Layout L{};
-  DevBuf arena, tgbuf;
+  AllocCounter alloc_ctr;
+  DevBuf arena{nullptr, 0, &alloc_ctr}, tgbuf{nullptr, 0, &alloc_ctr};
   HostBuf pin_in, pin_out;
   uint32_t tg_cap = 0;
   cudaEvent_t ev[5] = {};
@@ -209,6 +230,8 @@ struct gpc_driver {
   int walk_queue = 0;                        // option walk_queue: 1 always, -1 never, 0 batch_queue
   bool key_split = true;                     // split key pass for one circuit when it pays (option key_split)
   int walk_segment = 0;                      // option walk_segment: 0 when it pays, -1 never, > 0 target cost
+  unsigned long long spin_ns = 200ull * 1000 * 1000;  // option wait_limit_us: global-path look-back waits
+  uint32_t hold_runs = 0;  // option test_hold_tile: global-path runs left whose first sort tile stays unpublished
   // Segmented walk of the current circuit (single circuits; plan_segments):
   // the cut epochs, launch A's items then launch B's, each word's AFF state
   // per segment, and the state buffer's size.
@@ -403,8 +426,7 @@ struct gpc_driver {
     L.key = take((size_t)M * 16);
     L.blk_r0 = take((size_t)gpc::key_blocks((uint32_t)M) * 8);
     const size_t slots = (size_t)nb * gpc::SLOT_CAP;
-    L.skey = take(slots * 16);
-    L.stail = take(slots * sizeof(gpc::SlotTail));
+    L.slot = take(slots * sizeof(gpc::Slot));
     L.bagg = take((size_t)nb * 8);
     L.bout = take((size_t)nb * 8);
     L.cout = take((size_t)N * 8);
@@ -1068,8 +1090,7 @@ struct gpc_driver {
     kl.key = dptr<ulonglong2>(L.key);
     kl.bucket_count = dptr<uint32_t>(L.bcount);
     kl.blk_info = dptr<uint2>(L.blk_r0);
-    kl.skey = dptr<ulonglong2>(L.skey);
-    kl.stail = dptr<gpc::SlotTail>(L.stail);
+    kl.slot = dptr<gpc::Slot>(L.slot);
     kl.list_total = dptr<uint32_t>(L.totals) + 2;
     kl.err = dptr<uint32_t>(L.err);
     kl.write_all = write_all ? 1u : 0u;
@@ -1115,8 +1136,7 @@ struct gpc_driver {
     gl.tl = dptr<uint32_t>(L.tl);
     gl.tn = dptr<uint32_t>(L.tn);
     gl.tcap = tcap;
-    gl.skey = dptr<ulonglong2>(L.skey);
-    gl.stail = dptr<gpc::SlotTail>(L.stail);
+    gl.slot = dptr<gpc::Slot>(L.slot);
     gl.count = dptr<uint32_t>(L.bcount);
     gl.nb = L.nb;
     gl.bagg = dptr<uint2>(L.bagg);
@@ -1151,10 +1171,13 @@ struct gpc_driver {
     uint32_t *sw = dptr<uint32_t>(L.sort_scr);
     const uint32_t passes = 8;
     const size_t one = (size_t)passes * gpc::RADIX + (size_t)passes * L.sort_tiles * gpc::RADIX + passes;
+    const uint32_t hold = hold_runs ? 1u : 0u;
+    if (hold_runs) --hold_runs;
     gpc::SortScratch s1{sw, sw + passes * gpc::RADIX, sw + passes * gpc::RADIX + (size_t)passes * L.sort_tiles * gpc::RADIX,
-                        dptr<uint32_t>(L.err)};
+                        dptr<uint32_t>(L.err), spin_ns, hold};
     gpc::SortScratch s2{sw + one, sw + one + passes * gpc::RADIX,
-                        sw + one + passes * gpc::RADIX + (size_t)passes * L.sort_tiles * gpc::RADIX, dptr<uint32_t>(L.err)};
+                        sw + one + passes * gpc::RADIX + (size_t)passes * L.sort_tiles * gpc::RADIX, dptr<uint32_t>(L.err),
+                        spin_ns, 0u};
     uint64_t *k0 = dptr<uint64_t>(L.sk0), *k1 = dptr<uint64_t>(L.sk1);
     uint32_t *p0 = dptr<uint32_t>(L.pm0), *p1 = dptr<uint32_t>(L.pm1);
     bool alt = false;
@@ -1198,6 +1221,7 @@ struct gpc_driver {
     ml.tile_ctr = dptr<uint32_t>(L.merge_ctr);
     ml.totals = dptr<uint32_t>(L.totals);
     ml.err = dptr<uint32_t>(L.err);
+    ml.spin_ns = spin_ns;
     CK(gpc::launch_merge(ml, stream));
   }
 
@@ -1408,12 +1432,13 @@ struct gpc_driver {
     const Tape &T = tapes[0];
     CK(cudaMemsetAsync(dptr<char>(L.gq), 0, (size_t)L.M * 8, stream));
     gpc::AdjointLaunch A{};
-    A.skey = dptr<ulonglong2>(L.skey);
+    A.slot = dptr<gpc::Slot>(L.slot);
     A.count = dptr<uint32_t>(L.bcount);
     A.bagg = dptr<uint2>(L.bagg);
     A.bout = dptr<uint2>(L.bout);
     A.nb = L.nb;
-    A.mp = dptr<double>(L.mp);
+    A.blk_info = dptr<uint2>(L.blk_r0);
+    A.rec_p = dptr<double>(L.c[0].rec_p);
     A.grad_out = grad_out;
     A.gq = dptr<double>(L.gq);
     A.rec = dptr<uint64_t>(L.c[0].rec);
@@ -1648,6 +1673,7 @@ struct gpc_driver {
       d->batch_queue = batch_queue;
       d->walk_queue = walk_queue;
       d->walk_segment = walk_segment;
+      d->spin_ns = spin_ns;
       d->init_streams();
       partner = std::move(d);
     }
@@ -1992,6 +2018,12 @@ gpc_status gpc_get_driver(const char *stim_text, size_t len, int32_t correlation
     d->walk_queue = options->walk_queue;
     if (options->walk_segment < -1) return fail(GPC_ERR_INVALID, "walk_segment must be -1, 0 or positive");
     d->walk_segment = options->walk_segment;
+    if (options->wait_limit_us < 0 || options->test_hold_tile < 0)
+      return fail(GPC_ERR_INVALID, "wait_limit_us and test_hold_tile must be >= 0");
+    if (options->wait_limit_us) d->spin_ns = (unsigned long long)options->wait_limit_us * 1000ull;
+    d->hold_runs = (uint32_t)options->test_hold_tile;
+    if (options->test_fail_alloc < 0) return fail(GPC_ERR_INVALID, "test_fail_alloc must be >= 0");
+    if (options->test_fail_alloc) d->alloc_ctr.fail_at = options->test_fail_alloc - 1;
   }
   gpc_status st = guarded([&] {
     int n = 0;
@@ -2299,6 +2331,13 @@ gpc_status gpc_walk_form(gpc_driver *driver, int32_t *launches, int32_t *persist
   if (!driver->prepared) return fail(GPC_ERR_INVALID, "no circuit prepared");
   *launches = (int32_t)driver->L.classes.size();
   *persistent = driver->L.classes.size() == 1 && driver->L.classes[0].queue ? 1 : 0;
+  return GPC_OK;
+}
+
+gpc_status gpc_alloc_counts(gpc_driver *driver, uint64_t *device_allocs, uint64_t *device_frees) {
+  if (!driver || !device_allocs || !device_frees) return fail(GPC_ERR_INVALID, "null argument");
+  *device_allocs = driver->alloc_ctr.allocs;
+  *device_frees = driver->alloc_ctr.frees;
   return GPC_OK;
 }
 

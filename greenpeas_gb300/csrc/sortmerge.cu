@@ -17,7 +17,7 @@
 //    by (K, mechanism), so a group (run of equal K) keeps ascending mechanism
 //    order; every item checks its full symptom against its predecessor
 //    (collision check); group heads fold their run's probabilities left to
-//    right with p <- p(1-q) + q(1-p) (CUDAHandlers.hpp:635-640) in FP64,
+//    right with p <- p(1-q) + q(1-p) (CUDAHandlers.hpp:124-139) in FP64,
 //    extract their targets and get an output slot from a block scan plus a
 //    warp-wide decoupled look-back over the preceding buckets.  The empty
 //    symptom is dropped (Driver.hpp:185).
@@ -117,9 +117,10 @@ __global__ void key_prep_kernel(KeyLaunch L) {
 // into a slot of its bucket.  The symptom's words are the words set in the
 // non-zero masks of the mechanism's points (ascending); a block inside one
 // circuit finds its mechanisms' records in shared memory.
-__global__ void __launch_bounds__(KEY_THREADS) key_kernel(KeyLaunch L) {
+__global__ void __launch_bounds__(KEY_THREADS, 5) key_kernel(KeyLaunch L) {
   __shared__ uint32_t srm[KEY_THREADS + 1];  // rec_moff of the block's records
   __shared__ uint8_t sown[KEY_THREADS];      // record (from r0) of each of the block's mechanisms
+  __shared__ uint32_t stg[8][KEY_THREADS];   // each thread's first eight targets ([slot][thread]: no bank conflicts)
   const uint32_t tid = threadIdx.x, lane = tid & 31u;
   const uint32_t m0 = blockIdx.x * KEY_THREADS;
   const uint32_t mg = m0 + tid;
@@ -181,23 +182,12 @@ __global__ void __launch_bounds__(KEY_THREADS) key_kernel(KeyLaunch L) {
   uint32_t cnt = 0;
   bool nonzero = false;
   uint32_t *out = C.tl + (size_t)m * tcap;
-  // the first eight targets stay in registers and leave as two 16-byte stores
-  // (a row per thread: one scattered store per target would cost an L2
-  // transaction each); later ones are stored as they come
-  uint32_t t0 = 0, t1 = 0, t2 = 0, t3 = 0, t4 = 0, t5 = 0, t6 = 0, t7 = 0;
+  // the first eight targets are staged in shared memory and leave as two
+  // 16-byte stores (a row per thread: one scattered store per target would
+  // cost an L2 transaction each); later ones are stored as they come
   auto put = [&](uint32_t c, uint32_t v) {
-    switch (c) {
-      case 0: t0 = v; break;
-      case 1: t1 = v; break;
-      case 2: t2 = v; break;
-      case 3: t3 = v; break;
-      case 4: t4 = v; break;
-      case 5: t5 = v; break;
-      case 6: t6 = v; break;
-      case 7: t7 = v; break;
-      default:
-        if (c < tcap) out[c] = v;
-    }
+    if (c < 8) stg[c][tid] = v;
+    else if (c < tcap) out[c] = v;
   };
   const ulonglong2 *snap = C.snap;
   const uint32_t np = C.npoints, mw = C.mw;
@@ -235,8 +225,8 @@ __global__ void __launch_bounds__(KEY_THREADS) key_kernel(KeyLaunch L) {
   if (L.write_all || split) L.key[mg] = key;  // a split pass leaves the partial key
   if (tcap) {
     // rows are 16-byte aligned (tcap is a multiple of 4, at least 32)
-    if (cnt) reinterpret_cast<uint4 *>(out)[0] = make_uint4(t0, t1, t2, t3);
-    if (cnt > 4) reinterpret_cast<uint4 *>(out)[1] = make_uint4(t4, t5, t6, t7);
+    if (cnt) reinterpret_cast<uint4 *>(out)[0] = make_uint4(stg[0][tid], stg[1][tid], stg[2][tid], stg[3][tid]);
+    if (cnt > 4) reinterpret_cast<uint4 *>(out)[1] = make_uint4(stg[4][tid], stg[5][tid], stg[6][tid], stg[7][tid]);
     C.tn[m] = cnt;
     if (cnt > tcap) atomicOr(L.err, DEV_FLAG_LONG);
     const uint32_t am = __activemask();
@@ -251,8 +241,7 @@ __global__ void __launch_bounds__(KEY_THREADS) key_kernel(KeyLaunch L) {
     const uint32_t slot = atomicAdd(L.bucket_count + b, 1u);
     if (slot < SLOT_CAP) {
       const size_t pos = (size_t)b * SLOT_CAP + slot;
-      L.skey[pos] = key;
-      L.stail[pos] = SlotTail{mg, cnt, prob};
+      L.slot[pos] = Slot{key, SlotTail{mg, cnt, prob}};
     } else {
       atomicOr(L.err, DEV_FLAG_BIG_BUCKET);
     }
@@ -315,8 +304,7 @@ __global__ void __launch_bounds__(KEY_THREADS) key_late_kernel(KeyLaunch L) {
     const uint32_t slot = atomicAdd(L.bucket_count + b, 1u);
     if (slot < SLOT_CAP) {
       const size_t pos = (size_t)b * SLOT_CAP + slot;
-      L.skey[pos] = key;
-      L.stail[pos] = SlotTail{m, cnt, prob};
+      L.slot[pos] = Slot{key, SlotTail{m, cnt, prob}};
     } else {
       atomicOr(L.err, DEV_FLAG_BIG_BUCKET);
     }
@@ -411,7 +399,8 @@ constexpr uint32_t ST_MASK = (1u << 30) - 1;
 __global__ void __launch_bounds__(SORT_THREADS) sort_pass_kernel(
     const uint64_t *__restrict__ kin, const uint32_t *__restrict__ vin, uint64_t *__restrict__ kout,
     uint32_t *__restrict__ vout, uint32_t n, uint32_t shift, const uint32_t *__restrict__ gofs,
-    uint32_t *__restrict__ status, uint32_t *__restrict__ tile_ctr, uint32_t *__restrict__ err) {
+    uint32_t *__restrict__ status, uint32_t *__restrict__ tile_ctr, uint32_t *__restrict__ err,
+    unsigned long long spin_ns, uint32_t hold_tile0) {
   constexpr int WARPS = SORT_THREADS / 32;
   __shared__ uint32_t wcount[WARPS][RADIX];
   __shared__ uint32_t dbase[RADIX];
@@ -465,7 +454,7 @@ __global__ void __launch_bounds__(SORT_THREADS) sort_pass_kernel(
     }
     volatile uint32_t *st = status;
     if (tile == 0) {
-      st[d] = ST_PREFIX | sum;
+      if (!hold_tile0) st[d] = ST_PREFIX | sum;  // (held: a test of the waits below)
       dbase[d] = gofs[d];
     } else {
       st[(size_t)tile * RADIX + d] = ST_AGG | sum;
@@ -476,7 +465,7 @@ __global__ void __launch_bounds__(SORT_THREADS) sort_pass_kernel(
         const uint32_t s = st[(size_t)t * RADIX + d];
         if ((s & ~ST_MASK) == 0) {
           if (t0 == 0) t0 = globaltimer();
-          else if (globaltimer() - t0 > kSpinLimitNs) {
+          else if (globaltimer() - t0 > spin_ns) {
             atomicOr(err, DEV_ERR_TIMEOUT);
             break;
           }
@@ -508,7 +497,7 @@ __global__ void __launch_bounds__(SORT_THREADS) sort_pass_kernel(
 __global__ void gather_hi_kernel(const ulonglong2 *__restrict__ key, const uint32_t *__restrict__ perm,
                                  uint64_t *__restrict__ out, uint32_t n) {
   for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
-    out[i] = key[perm[i]].y;
+    out[i] = perm[i] < n ? key[perm[i]].y : 0ull;  // (an index past n: a sort pass timed out)
 }
 
 // ---- merge ------------------------------------------------------------------
@@ -538,13 +527,18 @@ __global__ void __launch_bounds__(MERGE_THREADS) merge_kernel(MergeLaunch L) {
   bool head = false;
   uint32_t ntg = 0, m = 0;
   ulonglong2 k = make_ulonglong2(0, 0);
-  if (i < n) {
-    m = L.perm[i];
+  // After a sort pass timed out (DEV_ERR_TIMEOUT, the compile fails) the
+  // permutation may hold stale entries: an index past n is never followed.
+  m = i < n ? L.perm[i] : 0u;
+  if (i < n && m >= n) {
+    atomicOr(L.err, DEV_ERR_TIMEOUT);
+    m = 0;
+  } else if (i < n) {
     k = L.key[m];
     const uint64_t d = __ldg(C.mdesc + m);
     bool newgroup = true;
-    if (i > 0) {
-      const uint32_t mp = L.perm[i - 1];
+    const uint32_t mp = i > 0 ? L.perm[i - 1] : 0u;
+    if (i > 0 && mp < n) {
       const ulonglong2 kp = L.key[mp];
       if (kp.x == k.x && kp.y == k.y) {
         newgroup = false;
@@ -610,7 +604,7 @@ __global__ void __launch_bounds__(MERGE_THREADS) merge_kernel(MergeLaunch L) {
         const unsigned long long s = st[t];
         if ((s >> 62) == 0) {
           if (t0 == 0) t0 = globaltimer();
-          else if (globaltimer() - t0 > kSpinLimitNs) {
+          else if (globaltimer() - t0 > L.spin_ns) {
             atomicOr(L.err, DEV_ERR_TIMEOUT);
             break;
           }
@@ -642,6 +636,7 @@ __global__ void __launch_bounds__(MERGE_THREADS) merge_kernel(MergeLaunch L) {
   double p = __ldg(C.mp + m);
   for (uint32_t i2 = i + 1; i2 < n; ++i2) {
     const uint32_t m2 = L.perm[i2];
+    if (m2 >= n) break;  // stale entry after a timed-out sort pass
     const ulonglong2 k2 = L.key[m2];
     if (k2.x != k.x || k2.y != k.y) break;
     const double q = __ldg(C.mp + m2);
@@ -924,8 +919,9 @@ __global__ void __launch_bounds__(GW_WARPS * 32) group_warp_kernel(GroupLaunch L
   H[lane + 32] = 0;
   __syncwarp();
   for (uint32_t i = lane; i < n; i += 32) {
-    const ulonglong2 k = L.skey[base + i];
-    const SlotTail t = L.stail[base + i];
+    const Slot sl = L.slot[base + i];
+    const ulonglong2 k = sl.key;
+    const SlotTail t = sl.tail;
     K[i] = k;
     Mm[i] = t.m;
     T[i] = t.t;
@@ -964,8 +960,8 @@ __global__ void __launch_bounds__(GW_WARPS * 32) group_warp_kernel(GroupLaunch L
   __syncwarp();
   // the saved permutation for the adjoint: mechanism at each sorted position
   // (every key of this bucket is in shared memory already)
-  uint32_t *perm = reinterpret_cast<uint32_t *>(L.skey + base);
-  for (uint32_t s = lane; s < n; s += 32) perm[2 * s] = Mm[O[s]];
+  Slot *const bslot = L.slot + base;
+  for (uint32_t s = lane; s < n; s += 32) slot_perm(bslot, s)[0] = Mm[O[s]];
   // Groups, 32 sorted positions at a time.  Each group's probability is a
   // segmented inclusive scan of the XOR-merge over its run: log2(longest run
   // in the chunk) shuffle steps with every lane busy (FP64 throughput is
@@ -991,7 +987,10 @@ __global__ void __launch_bounds__(GW_WARPS * 32) group_warp_kernel(GroupLaunch L
       // collision check: every item of a run against the run's head (full target lists)
       const uint32_t le0 = hb & (0xFFFFFFFFu >> (31u - lane));
       const uint32_t ih = le0 ? (uint32_t)O[s0 + 31 - __clz(le0)] : carry_head;
-      if (in && !head && (T[ih] != nt || !lists_equal(L.tl + (size_t)Mm[i] * tcap, L.tl + (size_t)Mm[ih] * tcap, nt)))
+      // (a list longer than the stride holds only its first tcap targets; the
+      // key pass flagged it and the run is redone with wider lists)
+      if (in && !head && nt <= tcap &&
+          (T[ih] != nt || !lists_equal(L.tl + (size_t)Mm[i] * tcap, L.tl + (size_t)Mm[ih] * tcap, nt)))
         atomicOr(L.err, DEV_ERR_COLLISION);
       carry_head = __shfl_sync(0xFFFFFFFFu, ih, 31);
     }
@@ -1017,13 +1016,13 @@ __global__ void __launch_bounds__(GW_WARPS * 32) group_warp_kernel(GroupLaunch L
     const uint32_t gh = gcount + __popc(hb & ((1u << lane) - 1u));  // group of a head at this lane
     // every slot of this bucket was read into shared memory above
     if (head) {
-      L.stail[base + gh].m = Mm[i];
-      L.stail[base + gh].t = tcount + inc - tv;
-      perm[2 * gh + 1] = s;
+      bslot[gh].tail.m = Mm[i];
+      bslot[gh].tail.t = tcount + inc - tv;
+      slot_perm(bslot, gh)[1] = s;
     }
     if (in && (s + 1 >= n || !key_eq(K[O[s + 1]], K[i]))) {  // the run's last item holds its value
       const uint32_t g = seg < 0 ? gcount - 1u : gcount + __popc(hb & ((1u << seg0) - 1u));
-      L.stail[base + g].p = x;
+      bslot[g].tail.p = x;
     }
     carry = __shfl_sync(0xFFFFFFFFu, x, 31);
     gcount += __popc(hb);
@@ -1063,8 +1062,9 @@ __global__ void __launch_bounds__(GB_THREADS) group_big_kernel(GroupLaunch L) {
     if (tid < NBIN) sh[tid] = 0;
     __syncthreads();
     if (tid < n) {
-      const ulonglong2 k = L.skey[base + tid];
-      const SlotTail t = L.stail[base + tid];
+      const Slot sl = L.slot[base + tid];
+      const ulonglong2 k = sl.key;
+      const SlotTail t = sl.tail;
       sk[tid] = k;
       sm[tid] = t.m;
       st[tid] = t.t;
@@ -1114,7 +1114,8 @@ __global__ void __launch_bounds__(GB_THREADS) group_big_kernel(GroupLaunch L) {
         const uint32_t ip = ord[s - 1];
         if (key_eq(sk[ip], sk[i])) {
           head = false;
-          if (st[ip] != nt || !lists_equal(L.tl + (size_t)sm[i] * tcap, L.tl + (size_t)sm[ip] * tcap, nt))
+          // (lists longer than the stride: flagged by the key pass, redone wider)
+          if (nt <= tcap && (st[ip] != nt || !lists_equal(L.tl + (size_t)sm[i] * tcap, L.tl + (size_t)sm[ip] * tcap, nt)))
             atomicOr(L.err, DEV_ERR_COLLISION);
         }
       }
@@ -1162,17 +1163,17 @@ __global__ void __launch_bounds__(GB_THREADS) group_big_kernel(GroupLaunch L) {
     __syncthreads();
     if (seg < 0) x = xor_merge(c_carry[warp], x);
     const uint32_t gb = c_gbase[warp];
-    uint32_t *perm = reinterpret_cast<uint32_t *>(L.skey + base);
-    if (in) perm[2 * s] = sm[i];
+    Slot *const bslot = L.slot + base;
+    if (in) slot_perm(bslot, s)[0] = sm[i];
     if (head) {
       const uint32_t g = gb + __popc(hb & ((1u << lane) - 1u));
-      L.stail[base + g].m = sm[i];
-      L.stail[base + g].t = c_tbase[warp] + inc - tv;
-      perm[2 * g + 1] = s;
+      bslot[g].tail.m = sm[i];
+      bslot[g].tail.t = c_tbase[warp] + inc - tv;
+      slot_perm(bslot, g)[1] = s;
     }
     if (in && (s + 1 >= n || !key_eq(sk[ord[s + 1]], sk[i]))) {
       const uint32_t g = seg < 0 ? gb - 1u : gb + __popc(hb & ((1u << seg0) - 1u));
-      L.stail[base + g].p = x;
+      bslot[g].tail.p = x;
     }
     __syncthreads();
   }
@@ -1273,12 +1274,14 @@ __global__ void __launch_bounds__(GW_WARPS * 32) emit_kernel(GroupLaunch L) {
   const uint32_t tcap = L.tcap;
   for (uint32_t g = lane; g < agg.x; g += 32) {
     const uint32_t slot = out.x + g;
-    const SlotTail t = L.stail[base + g];
+    const SlotTail t = L.slot[base + g].tail;
     const uint32_t toff = out.y + t.t;
     const uint32_t m = t.m;
     L.out_prob[slot] = t.p;
     L.out_off[slot] = toff;
-    const uint32_t ntg = __ldg(L.tn + m);
+    // (a list longer than the stride was flagged by the key pass; the run is
+    // redone with wider lists, so only the stride's targets are copied here)
+    const uint32_t ntg = min(__ldg(L.tn + m), tcap);
     if ((uint64_t)toff + ntg <= L.tg_cap) {
       const uint4 *src = reinterpret_cast<const uint4 *>(L.tl + (size_t)m * tcap);
       for (uint32_t k = 0; k * 4 < ntg; ++k) {
@@ -1308,28 +1311,47 @@ __global__ void param_rec_kernel(ParamLaunch L) {
   L.rec_p[r] = L.qtab[(size_t)src * 3 + channel_kind((uint32_t)((L.rec[r] >> 56) & 15u))];
 }
 
+// Record of mechanism m (one circuit): a search of rec_moff between the
+// record of m's key block's first mechanism and KEY_THREADS + 15 records
+// after it (each record holds 1 to 15 mechanisms, so m's record lies there).
+__device__ __forceinline__ uint32_t record_of(const AdjointLaunch &A, uint32_t m) {
+  uint32_t lo = A.blk_info[m / KEY_THREADS].x;
+  uint32_t hi = min(A.R, lo + KEY_THREADS + 15u);
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(A.rec_moff + mid) <= m) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
 __global__ void __launch_bounds__(GW_WARPS * 32) adjoint_group_kernel(AdjointLaunch A) {
-  const uint32_t lane = threadIdx.x & 31u;
-  const uint32_t b = blockIdx.x * GW_WARPS + (threadIdx.x >> 5);
+  __shared__ double s_q[GW_WARPS][SLOT_CAP];  // probability of the mechanism at each sorted position
+  const uint32_t lane = threadIdx.x & 31u, wi = threadIdx.x >> 5;
+  const uint32_t b = blockIdx.x * GW_WARPS + wi;
   if (b >= A.nb) return;
   const uint32_t n = A.count[b];
   if (n == 0 || n > SLOT_CAP) return;
   const uint32_t groups = A.bagg[b].x, out0 = A.bout[b].x;
-  const uint32_t *perm = reinterpret_cast<const uint32_t *>(A.skey + (size_t)b * SLOT_CAP);
+  const Slot *const bslot = A.slot + (size_t)b * SLOT_CAP;
+  double *q = s_q[wi];
+  // the forward's mechanism probabilities, recomputed from the records (every
+  // component of a record carries the record's probability)
+  for (uint32_t s = lane; s < n; s += 32) q[s] = __ldg(A.rec_p + record_of(A, slot_perm(bslot, s)[0]));
+  __syncwarp();
   for (uint32_t g = lane; g < groups; g += 32) {
-    const uint32_t s0 = perm[2 * g + 1], s1 = g + 1 < groups ? perm[2 * (g + 1) + 1] : n;
+    const uint32_t s0 = slot_perm(bslot, g)[1], s1 = g + 1 < groups ? slot_perm(bslot, g + 1)[1] : n;
     const double dl = A.grad_out[out0 + g];
     double pre = 1.0;
     for (uint32_t s = s0; s < s1; ++s) {
-      const uint32_t m = perm[2 * s];
-      A.gq[m] = pre;
-      pre *= 1.0 - 2.0 * A.mp[m];
+      A.gq[slot_perm(bslot, s)[0]] = pre;
+      pre *= 1.0 - 2.0 * q[s];
     }
     double suf = 1.0;
     for (uint32_t s = s1; s-- > s0;) {
-      const uint32_t m = perm[2 * s];
+      const uint32_t m = slot_perm(bslot, s)[0];
       A.gq[m] = dl * A.gq[m] * suf;
-      suf *= 1.0 - 2.0 * A.mp[m];
+      suf *= 1.0 - 2.0 * q[s];
     }
   }
 }
@@ -1454,7 +1476,7 @@ cudaError_t launch_sort(uint64_t *keys, uint64_t *keys_alt, uint32_t *vals, uint
   for (uint32_t p = 0; p < passes; ++p) {
     sort_pass_kernel<<<tiles, SORT_THREADS, 0, s>>>(ki, vi, ko, vo, n, p * RADIX_BITS, scr.hist + p * RADIX,
                                                     scr.status + (size_t)p * tiles * RADIX, scr.tile_ctr + p,
-                                                    scr.err);
+                                                    scr.err, scr.spin_ns, p == 0 ? scr.hold_first : 0u);
     uint64_t *tk = ki;
     ki = ko;
     ko = tk;

@@ -141,7 +141,8 @@ class Driver:
     def __init__(self, circuit, correlation_level: CorrelationLevel = CorrelationLevel.L2, *,
                  device: int = 0, sort_bits: int = 0, global_sort: bool = False, walk_qpt: int = 0,
                  bucket_mean: int = 0, walk_words: int = 0, key_split: int = 0, walk_queue: int = 0,
-                 walk_segment: int = 0):
+                 walk_segment: int = 0, wait_limit_us: int = 0, test_hold_tile: int = 0,
+                 test_fail_alloc: int = 0):
         L = _native.lib()
         self._h = ctypes.c_void_p()
         self.correlation_level = CorrelationLevel(correlation_level)
@@ -156,6 +157,9 @@ class Driver:
         opts.key_split = key_split
         opts.walk_queue = walk_queue
         opts.walk_segment = walk_segment
+        opts.wait_limit_us = wait_limit_us
+        opts.test_hold_tile = test_hold_tile
+        opts.test_fail_alloc = test_fail_alloc
         text = _text(circuit)
         _native.check(L.gpc_get_driver(text, len(text), int(self.correlation_level), ctypes.byref(opts),
                                        ctypes.byref(self._h)))
@@ -174,6 +178,12 @@ class Driver:
     @property
     def handle(self) -> ctypes.c_void_p:
         return self._h
+
+    def alloc_counts(self) -> dict:
+        """Device allocations and frees of this driver's buffers since its creation."""
+        a, f = ctypes.c_uint64(), ctypes.c_uint64()
+        _native.check(_native.lib().gpc_alloc_counts(self._h, ctypes.byref(a), ctypes.byref(f)))
+        return {"allocs": a.value, "frees": f.value}
 
     def fallback_counts(self) -> dict:
         """How often this driver left the fast path (gpc_fallback_counts)."""

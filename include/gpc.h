@@ -70,6 +70,13 @@ typedef struct gpc_options {
   int32_t walk_segment; /* one circuit: cut the walk into time segments walked side by side, composed
                            through their GF(2) transfer maps (0 = when it pays, -1 = never, > 0 = always,
                            about this many cost units per segment: an epoch costs its slots + 2) */
+  int32_t wait_limit_us; /* global path: a decoupled look-back wait gives up after this many microseconds
+                            and the compile fails with GPC_ERR_TIMEOUT (0 = 200,000) */
+  int32_t test_hold_tile; /* tests of the bounded waits: the next this-many global-path runs keep the
+                             first radix tile's counts unpublished, so the waits after it run out
+                             (0 = never) */
+  int32_t test_fail_alloc; /* tests of the allocation failure path: the driver's k-th device allocation
+                              (counting from its creation) fails once with GPC_ERR_OOM (0 = never) */
 } gpc_options;
 
 /* Parses `stim_text` (length `len`), sizes device buffers for it and returns
@@ -260,6 +267,13 @@ gpc_status gpc_walk_form(gpc_driver *driver, int32_t *launches, int32_t *persist
  * 128-bit re-sorts on the global path, [4] reruns of scan + emit after the
  * target buffer grew. */
 gpc_status gpc_fallback_counts(gpc_driver *driver, uint64_t *counts5);
+
+/* Device allocations and frees of this driver's own buffers since its
+ * creation (no counterpart in the reference's API; its tests count the
+ * allocations of a host storage policy, tests/Helpers/CountingStorage.hpp:9-51).
+ * A driver compiling circuits no larger than the largest it has seen
+ * allocates nothing. */
+gpc_status gpc_alloc_counts(gpc_driver *driver, uint64_t *device_allocs, uint64_t *device_frees);
 
 /* Segmented walk of the prepared single circuit (no counterpart in the
  * reference): `segments` the time segments its walk is cut into (0: not

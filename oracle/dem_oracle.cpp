@@ -24,7 +24,7 @@
 //     rows its Pauli touches; a measurement flip M(p) has the constant
 //     symptom of its measurement;
 //   * components with equal symptoms are merged with the XOR-merge
-//     p <- p1(1-p2) + p2(1-p1) (STEPG.hpp:128-131, CUDAHandlers.hpp:635-640),
+//     p <- p1(1-p2) + p2(1-p1) (STEPG.hpp:128-131, CUDAHandlers.hpp:124-139),
 //     folded in emission order; empty symptoms and p == 0 are dropped
 //     (Driver.hpp:185).
 //   * CorrelationLevel L0/L1/L2 keep the Pauli component sets listed at

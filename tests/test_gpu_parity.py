@@ -116,14 +116,20 @@ def test_device_stages_and_timings():
     _check(dem, text)
 
 
-def test_long_symptoms_widen_target_lists():
-    """A symptom with more targets than the default target-list stride (32): the key kernel flags it,
-    the driver widens the stride and runs again."""
-    n = 80
-    text = "R " + " ".join(map(str, range(n))) + "\nX_ERROR(0.01) 0\n"
+@pytest.mark.parametrize("n", [80, 300])
+def test_long_symptoms(n):
+    """Symptoms of 80 and 300 targets spread over several 64-bit words, one of them repeated (merged
+    after the full-symptom check): past the default target-list stride (32) the driver widens the
+    lists and runs again, past 256 targets it merges from the snapshots (the global path; a batch
+    holding such a circuit compiles circuit by circuit); alone and in a batch."""
+    text = "R " + " ".join(map(str, range(n))) + "\nX_ERROR(0.01) 0\nX_ERROR(0.02) 0\nTICK\n"
     text += "".join(f"CX 0 {q}\n" for q in range(1, n))
+    text += "DEPOLARIZE1(0.001) " + " ".join(map(str, range(n))) + "\n"
     text += "M " + " ".join(map(str, range(n))) + "\n" + "".join(f"DETECTOR rec[-{k}]\n" for k in range(1, n + 1))
     _check(gp.get_driver(text).compile(text), text)
+    small = gp.SurfaceCode(3).get_memory(3, 1e-3, noise="uniform")
+    for dem, t in zip(gp.get_driver(text).compile_batch([small, text, small]), [small, text, small]):
+        _check(dem, t)
 
 
 def test_driver_reuse_from_large_to_small_circuits():
