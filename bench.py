@@ -399,11 +399,16 @@ def plain_leg(gp, torch, local: int, flush, text: str, steps: int, warmup: int, 
     torch.cuda.synchronize()
     e2e_s = time.perf_counter() - t0
     h2d, d2h = drv.last_io_bytes()
+    host, nhost = {}, min(10, e2e_steps)
+    for _ in range(nhost):  # host phases of a compile, after the timed loop
+        drv.compile(text)
+        for k, v in drv.last_host_timings().items():
+            host[k] = host.get(k, 0.0) + v / nhost
     if dem_dev.canonical() != ref_dem.canonical() or dem.canonical() != ref_dem.canonical():
         raise SystemExit("bench: results changed between runs")
     return {"drv": drv, "step_ms": step_ms, "dev_ms": sum(step_ms), "stage": stage, "traffic": traffic,
             "sizes": sizes, "merged": ref_dem.num_errors, "e2e_s": e2e_s, "e2e_steps": e2e_steps, "h2d": h2d,
-            "d2h": d2h, "walk_plan": drv.walk_segments(), "fallbacks": drv.fallback_counts()}
+            "d2h": d2h, "walk_plan": drv.walk_segments(), "fallbacks": drv.fallback_counts(), "host_ms": host}
 
 
 # The plain-method configurations beside the headline: surface d = 3 (3 rounds), [[72,12,6]]
@@ -647,7 +652,8 @@ def main() -> None:
                           "qubits": sizes["qubits"], "words": sizes["words"], "epochs": sizes["epochs"],
                           "snapshot_points": sizes["points"]}),
         "mechanisms_per_s": {"raw": value * sizes["raw"], "merged": value * C},
-        "latency_ms": {"p50": p50, "p99": p99, "e2e_mean": 1e3 * e2e_s / args.steps},
+        "latency_ms": {"p50": p50, "p99": p99, "e2e_mean": 1e3 * e2e_s / args.steps,
+                       "e2e_host_phases": {k: round(v, 4) for k, v in r["host_ms"].items()}},
         "stage_ms": stage,
         "walk_segments": plan,
         "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"]},

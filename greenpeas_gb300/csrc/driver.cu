@@ -175,6 +175,61 @@ struct gpc_dem {  // arrays written in full right after they are sized
   bool text_ready = false;
 };
 
+namespace {
+// DEMs freed by the caller keep their host arrays for the next fetch, up to a
+// bound: a repeated compile then writes its result into memory that is
+// already mapped instead of faulting in fresh pages (a [[144,12,12]] DEM is
+// ~3 MB).  The cache is never destroyed (DEMs may be freed during process
+// exit); what it holds at exit is returned with the process.
+class DemCache {
+ public:
+  gpc_dem *take() {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      if (!free_.empty()) {
+        gpc_dem *d = free_.back();
+        free_.pop_back();
+        bytes_ -= size_of(d);
+        return d;
+      }
+    }
+    return new gpc_dem;
+  }
+  void give(gpc_dem *d) {
+    d->probs.clear();  // sizes 0: a later resize past the capacity copies nothing
+    d->offsets.clear();
+    d->targets.clear();
+    std::string().swap(d->text);
+    d->text_ready = false;
+    d->num_detectors = d->num_observables = 0;
+    d->num_raw = 0;
+    const size_t b = size_of(d);
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      if (free_.size() < kMaxDems && bytes_ + b <= kMaxBytes) {
+        free_.push_back(d);
+        bytes_ += b;
+        return;
+      }
+    }
+    delete d;
+  }
+
+ private:
+  static size_t size_of(const gpc_dem *d) {
+    return d->probs.capacity() * 8 + (d->offsets.capacity() + d->targets.capacity()) * 4;
+  }
+  static constexpr size_t kMaxDems = 8, kMaxBytes = (size_t)64 << 20;
+  std::mutex mu_;
+  std::vector<gpc_dem *> free_;
+  size_t bytes_ = 0;
+};
+DemCache &dem_cache() {
+  static DemCache *c = new DemCache;
+  return *c;
+}
+}  // namespace
+
 struct gpc_driver {
   int device = 0;
   int level = 2;
@@ -200,6 +255,8 @@ struct gpc_driver {
     for (uint32_t i = 0; i < n; ++i) big_first[i] = i;
     std::stable_sort(big_first.begin(), big_first.end(), [&](uint32_t a, uint32_t b) { return size(a) > size(b); });
   }
+  // Pieces of a large host copy: one per pool thread, at most 16.
+  uint32_t copy_pieces() { return std::min<uint32_t>(16u, host_pool().workers() + 1); }
   // fn(i, slot) for i < n, on the host pool when `parallel`.
   void for_each(uint32_t n, bool parallel, const std::function<void(uint32_t, uint32_t)> &fn) {
     if (!parallel || n < 2) {
@@ -575,28 +632,38 @@ struct gpc_driver {
       const uint32_t i = big_first[x];
       const Tape &T = tapes[i];
       const CircLayout &l = L.c[i];
-      const size_t ob = T.ops.size() * 8;
-      if (N == 1 && ob >= (1u << 20)) {  // one large tape: its copy in pieces on the host pool
-        const uint32_t np = 8;
-        for_each(np, true, [&](uint32_t q, uint32_t) {
-          const size_t b0 = ob * q / np & ~(size_t)7, b1 = q + 1 == np ? ob : ob * (q + 1) / np & ~(size_t)7;
-          put(l.ops + b0, reinterpret_cast<const char *>(T.ops.data()) + b0, b1 - b0);
-        });
-      } else {
-        put(l.ops, T.ops.data(), ob);
-      }
-      put(l.ep_opoff, T.ep_opoff.data(), T.ep_opoff.size() * 4);
-      put(l.ep_k, T.ep_k.data(), T.ep_k.size() * 4);
-      put(l.ep_ptoff, T.ep_ptoff.data(), T.ep_ptoff.size() * 4);
-      put(l.ep_chunk, T.ep_chunk.data(), T.ep_chunk.size() * 4);
-      put(l.ch_off, T.ch_off.data(), T.ch_off.size() * 4);
-      put(l.ch_bytes, T.ch_bytes.data(), T.ch_bytes.size() * 4);
-      put(l.inj_lo, T.inj_lo.data(), T.inj_lo.size() * 4);
-      put(l.inj_hi, T.inj_hi.data(), T.inj_hi.size() * 4);
-      put(l.rec, T.rec.data(), T.rec.size() * 8);
-      put(l.rec_p, T.rec_p.data(), T.rec_p.size() * 8);
-      put(l.rec_moff, T.rec_moff.data(), T.rec_moff.size() * 4);
-      if (param) put(l.rec_src, T.rec_src.data(), T.rec_src.size() * 4);
+      struct Copy {
+        size_t off;
+        const void *src;
+        size_t bytes;
+      };
+      const Copy cs[] = {{l.ops, T.ops.data(), T.ops.size() * 8},
+                         {l.ep_opoff, T.ep_opoff.data(), T.ep_opoff.size() * 4},
+                         {l.ep_k, T.ep_k.data(), T.ep_k.size() * 4},
+                         {l.ep_ptoff, T.ep_ptoff.data(), T.ep_ptoff.size() * 4},
+                         {l.ep_chunk, T.ep_chunk.data(), T.ep_chunk.size() * 4},
+                         {l.ch_off, T.ch_off.data(), T.ch_off.size() * 4},
+                         {l.ch_bytes, T.ch_bytes.data(), T.ch_bytes.size() * 4},
+                         {l.inj_lo, T.inj_lo.data(), T.inj_lo.size() * 4},
+                         {l.inj_hi, T.inj_hi.data(), T.inj_hi.size() * 4},
+                         {l.rec, T.rec.data(), T.rec.size() * 8},
+                         {l.rec_p, T.rec_p.data(), T.rec_p.size() * 8},
+                         {l.rec_moff, T.rec_moff.data(), T.rec_moff.size() * 4},
+                         {l.rec_src, T.rec_src.data(), param ? T.rec_src.size() * 4 : 0}};
+      size_t total = 0;
+      for (const Copy &c : cs) total += c.bytes;
+      // one large circuit: its arrays are copied as pieces of equal size on the host pool
+      // (one thread's copy rate into pinned memory would dominate the staging)
+      const uint32_t np = N == 1 && total >= (256u << 10) ? copy_pieces() : 1u;
+      for_each(np, np > 1, [&](uint32_t q, uint32_t) {
+        const size_t b0 = total * q / np, b1 = total * (q + 1) / np;
+        size_t at = 0;
+        for (const Copy &c : cs) {
+          const size_t lo = std::max(b0, at), hi = std::min(b1, at + c.bytes);
+          if (hi > lo) put(c.off + (lo - at), static_cast<const char *>(c.src) + (lo - at), hi - lo);
+          at += c.bytes;
+        }
+      });
       CircuitDev &c = cd[i];
       c = CircuitDev{};
       c.ops = dptr<uint64_t>(l.ops);
@@ -668,6 +735,7 @@ struct gpc_driver {
     have_tape = false;  // the tapes are rewritten in place
     gpc::LowerOptions lo;
     lo.level = level;
+    lo.sources = param;  // record sources feed the gradient kernels only
     if (n > 1) lo.chunk_min = gpc::kWalkChunkMin;
     gpc::HostPool &hp = host_pool();
     if (lower_scratch.size() < hp.workers() + 1) lower_scratch.resize(hp.workers() + 1);
@@ -1539,7 +1607,7 @@ struct gpc_driver {
         const uint32_t c0 = N > 1 ? CO[i].x : 0, c1 = (N > 1 && i + 1 < N) ? CO[i + 1].x : C;
         const uint32_t t0 = N > 1 ? CO[i].y : 0, t1 = (N > 1 && i + 1 < N) ? CO[i + 1].y : NT;
         if (c1 < c0 || c1 > C || t1 < t0 || t1 > NT) throw gpc::Error(GPC_ERR_CUDA, "inconsistent batch ranges");
-        auto dem = std::make_unique<gpc_dem>();
+        std::unique_ptr<gpc_dem> dem(dem_cache().take());
         dem->num_detectors = tapes[i].ndet;
         dem->num_observables = tapes[i].nobs;
         dem->num_raw = tapes[i].M;
@@ -1551,7 +1619,7 @@ struct gpc_driver {
         // one large result is copied in pieces on the host pool (a single
         // thread's copy rate would dominate the fetch)
         const uint32_t ne = c1 - c0, nt = t1 - t0;
-        const uint32_t np = N == 1 && (size_t)ne * 12 + (size_t)nt * 4 >= (1u << 20) ? 8u : 1u;
+        const uint32_t np = N == 1 && (size_t)ne * 12 + (size_t)nt * 4 >= (256u << 10) ? copy_pieces() : 1u;
         for_each(np, np > 1, [&](uint32_t q, uint32_t) {
           const uint32_t e0 = (uint32_t)((uint64_t)ne * q / np), e1 = (uint32_t)((uint64_t)ne * (q + 1) / np);
           const uint32_t g0 = (uint32_t)((uint64_t)nt * q / np), g1 = (uint32_t)((uint64_t)nt * (q + 1) / np);
@@ -1845,6 +1913,7 @@ struct gpc_server {
     gpc::LowerOptions lo;
     lo.level = level;
     lo.chunk_min = gpc::kWalkChunkMin;  // requests are compiled in batches
+    lo.sources = false;
     while (true) {
       uint64_t t;
       const char *text;
@@ -2194,7 +2263,9 @@ gpc_status gpc_dem_text(const gpc_dem *dem_c, const char **text, size_t *len) {
   });
 }
 
-void gpc_dem_free(gpc_dem *dem) { delete dem; }
+void gpc_dem_free(gpc_dem *dem) {
+  if (dem) dem_cache().give(dem);
+}
 
 gpc_status gpc_server_create(const gpc_server_options *options, gpc_server **out) {
   if (!out) return fail(GPC_ERR_INVALID, "out is null");

@@ -274,6 +274,19 @@ struct TextParser {
         }
       }
       in.tn = (uint32_t)(tw - t0);
+      // the target checks of the lowering, made here while the targets are in cache
+      uint32_t orv = 0, andv = 0xFFFFFFFFu, maxq = 0;
+      for (const uint32_t *p = t0; p < tw; ++p) {
+        orv |= *p;
+        andv &= *p;
+        maxq = std::max(maxq, *p & 0xFFFFFFu);
+      }
+      in.maxq = maxq;
+      in.kinds = (uint8_t)((orv & kRec ? kAnyRec : 0) | (in.tn && (andv & kRec) ? kAllRec : 0) |
+                           (orv & kPau ? kAnyPau : 0) | (in.tn && (andv & kPau) ? kAllPau : 0));
+      if ((g.kind == G_C2 || g.kind == G_N2) && in.tn % 2 == 0)
+        for (uint32_t k = 0; k < in.tn; k += 2)
+          if (t0[k] == t0[k + 1]) fail(GPC_ERR_PARSE, std::string(g.name) + " on a single qubit");
       dst.push_back(in);
     }
   }
@@ -438,6 +451,7 @@ struct LowerScratch::Buffers {
     HostArray<double> rec_p;
     HostArray<uint32_t> rec_src;
     size_t nrec = 0, roff = 0;
+    uint64_t ncomp = 0, moff0 = 0;  // the segment's mechanisms, and those of the records before it
     uint32_t nprov = 0, eoff = 0, poff = 0;
     std::vector<uint64_t> fine, coarse;  // per-qubit op signatures of the segment (qubit packing)
     std::vector<uint64_t> snapbits;      // bit i: op oa + i of the segment's tape range is a snapshot
@@ -453,8 +467,8 @@ LowerScratch::LowerScratch(LowerScratch &&) noexcept = default;
 LowerScratch &LowerScratch::operator=(LowerScratch &&) noexcept = default;
 
 void parse_stim_pieces(const char *text, size_t len, Parsed &out, std::vector<Parsed> &pieces, HostPool &pool) {
-  constexpr size_t kPieceMin = 32 * 1024;
-  const size_t want = std::min<size_t>({(size_t)pool.workers() + 1, 8, len / kPieceMin});
+  constexpr size_t kPieceMin = 16 * 1024;
+  const size_t want = std::min<size_t>({(size_t)pool.workers() + 1, 16, len / kPieceMin});
   // a REPEAT block may not be cut: such texts (short ones, usually) parse whole
   if (want < 2 || !text || memchr(text, '{', len)) {
     parse_stim_into(text, len, out);
@@ -476,23 +490,25 @@ void parse_stim_pieces(const char *text, size_t len, Parsed &out, std::vector<Pa
     parse_stim_into(text, len, out);  // the error again, with its line number in the whole text
     return;
   }
-  size_t ni = 0, nt = 0;
+  // the pieces' instructions and targets, concatenated (each piece on the pool)
+  std::vector<size_t> ioff(np + 1, 0), toff(np + 1, 0);
   for (uint32_t i = 0; i < np; ++i) {
-    ni += pieces[i].ins.size();
-    nt += pieces[i].pool.size();
+    ioff[i + 1] = ioff[i] + pieces[i].ins.size();
+    toff[i + 1] = toff[i] + pieces[i].pool.size();
   }
-  out.ins.clear();
-  out.pool.clear();
-  out.ins.reserve(ni);
-  out.pool.reserve(nt);
-  for (uint32_t i = 0; i < np; ++i) {
-    const uint32_t off = (uint32_t)out.pool.size();
-    out.pool.insert(out.pool.end(), pieces[i].pool.begin(), pieces[i].pool.end());
-    for (Instr in : pieces[i].ins) {
-      in.t0 += off;
-      out.ins.push_back(in);
+  if (toff[np] > 0xFFFFFFFFull) throw Error(GPC_ERR_CAPACITY, "circuit too long");
+  out.ins.resize(ioff[np]);
+  out.pool.resize(toff[np]);
+  pool.run(np, [&](uint32_t i, uint32_t) {
+    const Parsed &pc = pieces[i];
+    if (!pc.pool.empty()) memcpy(out.pool.data() + toff[i], pc.pool.data(), pc.pool.size() * 4);
+    Instr *dst = out.ins.data() + ioff[i];
+    for (const Instr &in : pc.ins) {
+      *dst = in;
+      dst->t0 += (uint32_t)toff[i];
+      ++dst;
     }
-  }
+  });
 }
 
 void lower_text(const char *text, size_t len, const LowerOptions &opt, Tape &T, LowerScratch &S, HostPool *pool) {
@@ -539,28 +555,21 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
     occBase[i] = (uint32_t)occ;
     occ += in.tn;
     if (occ > 0xFFFFFFFFull / 4) throw Error(GPC_ERR_CAPACITY, "circuit too long");
-    // target kinds, checked on the OR / AND of the instruction's targets
-    uint32_t orv = 0, andv = 0xFFFFFFFFu, maxq = 0;
-    for (uint32_t k = 0; k < in.tn; ++k) {
-      const uint32_t v = t[k];
-      orv |= v;
-      andv &= v;
-      maxq = std::max(maxq, v & 0xFFFFFFu);
-    }
+    // target kinds (summarised by the parser)
     if (in.tn) {
       if (g.kind == G_DET || g.kind == G_OBS) {
-        if (!(andv & kRec)) throw Error(GPC_ERR_PARSE, std::string(g.name) + " takes record targets only");
-      } else if (orv & kRec) {
+        if (!(in.kinds & kAllRec)) throw Error(GPC_ERR_PARSE, std::string(g.name) + " takes record targets only");
+      } else if (in.kinds & kAnyRec) {
         throw Error(GPC_ERR_UNSUPPORTED, std::string("record targets are not supported on ") + g.name);
       } else if (g.kind == G_MPAD) {
-        if (maxq > 1 || (orv & kPau)) throw Error(GPC_ERR_PARSE, "MPAD targets must be 0 or 1");
+        if (in.maxq > 1 || (in.kinds & kAnyPau)) throw Error(GPC_ERR_PARSE, "MPAD targets must be 0 or 1");
       } else {
         if (g.kind == G_CORR) {
-          if (!(andv & kPau)) throw Error(GPC_ERR_PARSE, "E takes Pauli targets");
-        } else if (orv & kPau) {
+          if (!(in.kinds & kAllPau)) throw Error(GPC_ERR_PARSE, "E takes Pauli targets");
+        } else if (in.kinds & kAnyPau) {
           throw Error(GPC_ERR_PARSE, std::string("Pauli targets are not allowed on ") + g.name);
         }
-        nq = std::max(nq, maxq + 1);
+        nq = std::max(nq, in.maxq + 1);
       }
     }
     switch (g.kind) {
@@ -590,10 +599,8 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
         break;
       }
       case G_C2:
-      case G_N2:
+      case G_N2:  // (the parser checked that no pair names one qubit twice)
         if (in.tn % 2) throw Error(GPC_ERR_PARSE, std::string(g.name) + " needs an even number of targets");
-        for (uint32_t k = 0; k < in.tn; k += 2)
-          if (t[k] == t[k + 1]) throw Error(GPC_ERR_PARSE, std::string(g.name) + " on a single qubit");
         break;
       default:
         break;
@@ -616,8 +623,8 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
   }
   // sources of the noise targets: tick and class (see Tape::rec_src)
   std::vector<uint32_t> &tsrc = B.tsrc;
-  tsrc.assign(occ, kNone);  // by target occurrence
-  {
+  if (opt.sources) {
+    tsrc.assign(occ, kNone);  // by target occurrence
     uint32_t tick = 0;
     std::vector<uint8_t> &lastReset = B.lastReset;  // the qubit's last operation was a reset
     lastReset.assign(nq, 0);
@@ -660,6 +667,10 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
       }
     }
     T.n_ticks = tick + 1;
+  } else {
+    tsrc.clear();
+    T.n_ticks = 1;
+    for (const Instr &in : P.ins) T.n_ticks += kGates[in.gate].kind == G_TICK;
   }
   T.nq = nq;
   T.nmeas = m;
@@ -697,8 +708,15 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
     uint32_t w = 0, lo = 0;
     for (uint32_t i = 0; i < m; ++i) {
       const uint32_t hi = moff[i + 1];
-      std::sort(mbits.begin() + lo, mbits.begin() + hi);
       moff[i] = w;
+      if (hi - lo == 1) {
+        mbits[w++] = mbits[lo];
+        lo = hi;
+        continue;
+      }
+      // detector bits arrive in ascending order (detectors are numbered as they
+      // appear); only observable bits can be out of order
+      if (!std::is_sorted(mbits.begin() + lo, mbits.begin() + hi)) std::sort(mbits.begin() + lo, mbits.begin() + hi);
       for (uint32_t a = lo; a < hi;) {
         uint32_t b = a;
         while (b < hi && mbits[b] == mbits[a]) ++b;
@@ -724,7 +742,9 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
   cut.clear();
   cut.push_back(P.ins.size());
   {
-    const size_t per = std::max<size_t>(16384, occ / 8);
+    // at most 8 segments of equal size, about 16,384 occurrences or fewer each
+    const size_t nsegw = std::max<size_t>(1, std::min<size_t>(8, (occ + 16383) / 16384));
+    const size_t per = (occ + nsegw - 1) / nsegw;
     size_t acc = 0;
     for (size_t ii = P.ins.size(); ii-- > 1;) {
       acc += P.ins[ii].tn;
@@ -768,11 +788,12 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
     HostArray<uint32_t> &RS = nseg == 1 ? T.rec_src : G.rec_src;
     RD.resize(rec_max);
     RP.resize(rec_max);
-    RS.resize(rec_max);
+    RS.resize(opt.sources ? rec_max : 0);
     uint64_t *const rec_d = RD.data();
     double *const rec_pp = RP.data();
-    uint32_t *const rec_s = RS.data();
+    uint32_t *const rec_s = opt.sources ? RS.data() : nullptr;
     size_t nrec = 0;
+    uint64_t ncomp = 0;
     SplitCache split;
 
     auto place1 = [&](uint32_t q, uint64_t op) -> uint32_t {
@@ -805,10 +826,12 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
       s.open = id;
       return id;
     };
-    auto record = [&](uint32_t pa, uint32_t pb, uint32_t type, uint32_t Pa, uint32_t Pb, double p, uint32_t src) {
+    // `at`: the target occurrence whose (tick, class) source the record takes, or kNone
+    auto record = [&](uint32_t pa, uint32_t pb, uint32_t type, uint32_t Pa, uint32_t Pb, double p, uint32_t at) {
       rec_d[nrec] = make_rec(pa, pb, type, Pa, Pb);
       rec_pp[nrec] = p;
-      rec_s[nrec] = src;
+      if (rec_s) rec_s[nrec] = at == kNone ? kNone : tsrc[at];
+      ncomp += kRecComps[type];
       ++nrec;
     };
 
@@ -870,7 +893,7 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
             if (p > 0 && b1 > b0) {
               uint32_t id = nprov++;
               ++ep_np[place1(q, make_op(OP_SNAPD, 0, id))];
-              record(id, 0, REC_PAULI, 1, 0, p, tsrc[occBase[ii] + k]);
+              record(id, 0, REC_PAULI, 1, 0, p, occBase[ii] + k);
             }
           }
           break;
@@ -883,10 +906,10 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
               case N1_Y:
               case N1_Z:
                 if (in.args[0] > 0)
-                  record(point(q), 0, REC_PAULI, g.a == N1_X ? 1 : g.a == N1_Z ? 2 : 3, 0, in.args[0], tsrc[occBase[ii] + k]);
+                  record(point(q), 0, REC_PAULI, g.a == N1_X ? 1 : g.a == N1_Z ? 2 : 3, 0, in.args[0], occBase[ii] + k);
                 break;
               case N1_DEP1:
-                if (in.args[0] > 0) record(point(q), 0, dep1Type, 0, 0, split.dep1(in.args[0]), tsrc[occBase[ii] + k]);
+                if (in.args[0] > 0) record(point(q), 0, dep1Type, 0, 0, split.dep1(in.args[0]), occBase[ii] + k);
                 break;
               case N1_PC1: {
                 double qq[3];
@@ -909,7 +932,7 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
           for (uint32_t k = in.tn; k >= 2; k -= 2) {
             uint32_t a = t[k - 2], b = t[k - 1];
             uint32_t pa = point(a), pb = point(b);
-            record(pa, pb, dep2Type, 0, 0, sp, tsrc[occBase[ii] + k - 2]);
+            record(pa, pb, dep2Type, 0, 0, sp, occBase[ii] + k - 2);
           }
           break;
         }
@@ -944,9 +967,10 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
 
     RD.resize(nrec);
     RP.resize(nrec);
-    RS.resize(nrec);
+    RS.resize(opt.sources ? nrec : 0);
     G.nent = (size_t)(ent1 - ent0);
     G.nrec = nrec;
+    G.ncomp = ncomp;
     G.nprov = nprov;
     // the segment's share of each qubit's signatures (see the qubit packing):
     // op kinds, and op kinds with their (segment-local) epochs
@@ -987,18 +1011,6 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
           measLo[k] += G.eoff;
           measHi[k] += G.eoff;
         }
-  }
-  if (nseg > 1) {
-    T.rec.resize(nrec_all);
-    T.rec_p.resize(nrec_all);
-    T.rec_src.resize(nrec_all);
-    for (uint32_t sg = 0; sg < nseg; ++sg) {
-      const LowerScratch::Buffers::Segment &G = B.segs[sg];
-      if (!G.nrec) continue;
-      memcpy(T.rec.data() + G.roff, G.rec.data(), G.nrec * 8);
-      memcpy(T.rec_p.data() + G.roff, G.rec_p.data(), G.nrec * 8);
-      memcpy(T.rec_src.data() + G.roff, G.rec_src.data(), G.nrec * 4);
-    }
   }
 
   // ---- warp-uniform qubit packing -------------------------------------
@@ -1154,22 +1166,48 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
     e = f;
   }
   if (next > kMaxPoint28) throw Error(GPC_ERR_CAPACITY, "too many snapshot points");
-  const size_t R = T.rec.size();
-  T.rec_moff.resize(R + 1);
+  // records in walk order: each segment's records go to their place with their
+  // points renumbered, beside the first mechanism of each record (segments on
+  // the pool)
+  const size_t R = nrec_all;
   uint64_t mm = 0;
-  uint32_t sg = 0, poff = 0;  // the segment holding record r, and its point offset
-  for (size_t r = 0; r < R; ++r) {
-    while (sg + 1 < nseg && r >= B.segs[sg + 1].roff) poff = B.segs[++sg].poff;
-    uint64_t &d = T.rec[r];
-    const uint32_t pa = (uint32_t)(d & kMaxPoint28) + poff, pb = (uint32_t)((d >> 28) & kMaxPoint28) + poff;
-    const uint32_t type = (uint32_t)((d >> 56) & 15u), Pb = (uint32_t)(d >> 62);
-    const bool hasB = type >= REC_DEP2_L0 || Pb != 0;
-    d = (d & ~(((uint64_t)kMaxPoint28) | ((uint64_t)kMaxPoint28 << 28))) | (uint64_t)remap[pa] |
-        ((uint64_t)(hasB ? remap[pb] : 0) << 28);
-    T.rec_moff[r] = (uint32_t)mm;
-    mm += kRecComps[type];
+  for (uint32_t s = 0; s < nseg; ++s) {
+    B.segs[s].moff0 = mm;
+    mm += B.segs[s].ncomp;
   }
   if (mm >= 0xFFFFFFFFull) throw Error(GPC_ERR_CAPACITY, "too many error mechanisms");
+  if (nseg > 1) {  // one segment wrote its records in place
+    T.rec.resize(R);
+    T.rec_p.resize(R);
+    T.rec_src.resize(opt.sources ? R : 0);
+  }
+  T.rec_moff.resize(R + 1);
+  auto place_records = [&](uint32_t sg, uint32_t) {
+    const LowerScratch::Buffers::Segment &G = B.segs[sg];
+    const uint64_t *const src = nseg == 1 ? T.rec.data() : G.rec.data();
+    uint64_t *const dst = T.rec.data() + G.roff;
+    uint32_t *const mo = T.rec_moff.data() + G.roff;
+    uint64_t m0 = G.moff0;
+    for (size_t i = 0; i < G.nrec; ++i) {
+      uint64_t d = src[i];
+      const uint32_t pa = (uint32_t)(d & kMaxPoint28) + G.poff, pb = (uint32_t)((d >> 28) & kMaxPoint28) + G.poff;
+      const uint32_t type = (uint32_t)((d >> 56) & 15u), Pb = (uint32_t)(d >> 62);
+      const bool hasB = type >= REC_DEP2_L0 || Pb != 0;
+      d = (d & ~(((uint64_t)kMaxPoint28) | ((uint64_t)kMaxPoint28 << 28))) | (uint64_t)remap[pa] |
+          ((uint64_t)(hasB ? remap[pb] : 0) << 28);
+      dst[i] = d;
+      mo[i] = (uint32_t)m0;
+      m0 += kRecComps[type];
+    }
+    if (nseg > 1 && G.nrec) {
+      memcpy(T.rec_p.data() + G.roff, G.rec_p.data(), G.nrec * 8);
+      if (opt.sources) memcpy(T.rec_src.data() + G.roff, G.rec_src.data(), G.nrec * 4);
+    }
+  };
+  if (pool && nseg > 1)
+    pool->run(nseg, place_records);
+  else
+    for (uint32_t s = 0; s < nseg; ++s) place_records(s, 0);
   T.rec_moff[R] = (uint32_t)mm;
   T.M = (uint32_t)mm;
   // injection range of each word

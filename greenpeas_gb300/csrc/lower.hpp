@@ -113,9 +113,12 @@ constexpr uint32_t kNone = 0xFFFFFFFFu;
 struct Instr {
   uint16_t gate;
   uint8_t nargs;
+  uint8_t kinds;  // its targets: bit 0 some record target, 1 all records, 2 some Pauli target, 3 all Pauli
+  uint32_t maxq;  // the largest qubit index (low 24 bits) among its targets
   double args[3];
   uint32_t t0, tn;
 };
+constexpr uint8_t kAnyRec = 1, kAllRec = 2, kAnyPau = 4, kAllPau = 8;
 
 struct Parsed {
   std::vector<Instr> ins;
@@ -171,6 +174,7 @@ struct LowerOptions {
   int level = 2;     // correlation level 0/1/2
   uint32_t kcap = 8; // max slots per epoch
   uint32_t chunk_min = 0xFFFFFFFFu;  // smallest tape chunk (bytes; capped by the walk's shared memory)
+  bool sources = true;  // fill Tape::rec_src (read by the noise-rate gradient only)
 };
 
 // Shared-memory plan of the walk kernel (bytes): double-buffered tape chunks,
