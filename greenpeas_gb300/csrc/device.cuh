@@ -120,6 +120,9 @@ enum : uint32_t { SEG_FIRST = 0, SEG_AFF = 1, SEG_XFER = 2, SEG_REST = 3 };
 // from the dense transfer columns): measured on code circuits, rows hold 1-3
 // entries on average and up to 12 where a cut falls inside a round.
 constexpr uint32_t kSegRowCap = 16;
+// Entries of a row that the compose ring copies into shared memory (entries
+// kSegRingCap .. kSegRowCap - 1, rare, are read from global memory).
+constexpr uint32_t kSegRingCap = 8;
 // Most compose steps a REST item keeps in flight (shared-memory ring).
 constexpr uint32_t kSegRingMax = 4;
 struct SegItem {
@@ -144,7 +147,7 @@ struct SegLaunch {
   const uint32_t *aff;      // [w][S] state of word j's SEG_AFF walk of segment s (0xFFFFFFFF: no measurements)
   uint32_t S;
   uint32_t *xcnt;           // [S][2 qpad] (zeroed) entries of each transfer row
-  uint16_t *xlst;           // [S][2 qpad][kSegRowCap] the entries
+  uint16_t *xlst;           // entries 0..7 [S][2 qpad][kSegRingCap], then entries 8..15 [S][2 qpad][8]
   uint32_t ring_nb;         // compose step buffers of a REST CTA (launch B; 0 in launch A)
   uint32_t *err;
 };

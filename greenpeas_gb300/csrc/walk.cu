@@ -146,7 +146,9 @@ struct SegCtx {
   const uint64_t *state;    // all states (transfer columns, AFF exits)
   const uint32_t *aff_row;  // REST: [S] AFF state of this word in each segment (kNoState: none)
   uint32_t *xcnt;           // [S][2 qpad] entries of each transfer row (XFER adds, REST reads)
-  uint16_t *xlst;           // [S][2 qpad][kSegRowCap] entries (the rows at the segment's start)
+  uint16_t *xlst;           // entries (the rows at the segment's start, as word offsets in a published
+                            // buffer: 2 slot for X, 2 slot + 1 for Z): [S][2 qpad][kSegRingCap] entries
+                            // 0..7, then [S][2 qpad][kSegRowCap - kSegRingCap] entries 8..15
   uint32_t xfer0, ncol, s_from, s_to;
   uint32_t col, seg;        // XFER: the unit column walked, its segment
   uint32_t ring_nb;         // REST: step buffers of the compose ring
@@ -155,19 +157,27 @@ struct SegCtx {
 constexpr uint32_t kNoState = 0xFFFFFFFFu;
 
 // Bytes of one compose step in shared memory: entry counts (u32), entries
-// (kSegRowCap u16) and the segment's AFF rows (u64) of every row.
+// 0..7 (kSegRingCap u16) and the segment's AFF rows (u64) of every row.
 __host__ __device__ constexpr size_t seg_step_bytes(uint32_t qpad) {
-  return (size_t)2 * qpad * (4 + 2 * kSegRowCap + 8);
+  return (size_t)2 * qpad * (4 + 2 * kSegRingCap + 8);
 }
 
 // XFER exit: the set bits of row r's word of column col, as entries of the
-// row's sparse list (order is free: the compose XORs them).
+// row's sparse list (order is free: the compose XORs them).  An entry is the
+// row's word offset in a published buffer, so the compose adds it to the
+// buffer's address as it is.
 __device__ __forceinline__ void seg_list_add(const SegCtx &sc, uint32_t n2, uint32_t r, uint64_t w) {
   const size_t row = (size_t)sc.seg * n2 + r;
+  const uint32_t qpad = n2 / 2u;
+  uint16_t *const hi = sc.xlst + (size_t)sc.S * n2 * kSegRingCap;
   for (; w; w &= w - 1) {
     const uint32_t j = sc.col * 64u + (uint32_t)(__ffsll((long long)w) - 1);
+    const uint16_t wj = (uint16_t)(j < qpad ? 2u * j : 2u * (j - qpad) + 1u);
     const uint32_t pos = atomicAdd(sc.xcnt + row, 1u);
-    if (pos < kSegRowCap) sc.xlst[row * kSegRowCap + pos] = (uint16_t)j;
+    if (pos < kSegRingCap)
+      sc.xlst[row * kSegRingCap + pos] = wj;
+    else if (pos < kSegRowCap)
+      hi[row * (kSegRowCap - kSegRingCap) + pos - kSegRingCap] = wj;
   }
 }
 
@@ -204,7 +214,8 @@ __device__ __forceinline__ bool seg_compose(uint64_t (&X)[QPT][1], uint64_t (&Z)
   const uint32_t n2 = 2 * qpad;
   const uint32_t steps = sc.s_to - sc.s_from, NB = sc.ring_nb;
   const size_t step_bytes = seg_step_bytes(qpad);
-  const uint32_t cnt_b = n2 * 4u, lst_b = n2 * 2u * kSegRowCap, c_b = n2 * 8u;
+  const uint32_t cnt_b = n2 * 4u, lst_b = n2 * 2u * kSegRingCap, c_b = n2 * 8u;
+  const uint16_t *const xhi = sc.xlst + (size_t)sc.S * n2 * kSegRingCap;  // entries 8..15
   // the ring's copies are issued by lane 0 of the last warp (whose slots are
   // the packing's padding when there is any), so the first warp is not held up
   const uint32_t issuer = T - 32u;
@@ -217,7 +228,7 @@ __device__ __forceinline__ bool seg_compose(uint64_t (&X)[QPT][1], uint64_t (&Z)
     const uint32_t ai = s_aff[s];
     mbar_expect_tx(bar, cnt_b + lst_b + (ai == kNoState ? 0u : c_b));
     bulk_g2s(dst, sc.xcnt + (size_t)s * n2, cnt_b, bar);
-    bulk_g2s(dst + cnt_b, sc.xlst + (size_t)s * n2 * kSegRowCap, lst_b, bar);
+    bulk_g2s(dst + cnt_b, sc.xlst + (size_t)s * n2 * kSegRingCap, lst_b, bar);
     if (ai != kNoState) bulk_g2s(dst + cnt_b + lst_b, sc.state + (size_t)ai * n2, c_b, bar);
   };
   if (tid == issuer) {
@@ -233,7 +244,7 @@ __device__ __forceinline__ bool seg_compose(uint64_t (&X)[QPT][1], uint64_t (&Z)
   auto load_row = [&](uint32_t k, uint32_t r, SegRow &m) {
     const unsigned char *buf = ring_c + (size_t)(k % NB) * step_bytes;
     m.n = reinterpret_cast<const uint32_t *>(buf)[r];
-    const uint4 e = reinterpret_cast<const uint4 *>(buf + cnt_b)[r * (kSegRowCap / 8)];
+    const uint4 e = reinterpret_cast<const uint4 *>(buf + cnt_b)[r];  // entries 0..7
     m.e[0] = e.x;
     m.e[1] = e.y;
     m.e[2] = e.z;
@@ -245,24 +256,38 @@ __device__ __forceinline__ bool seg_compose(uint64_t (&X)[QPT][1], uint64_t (&Z)
   auto word_addr = [&](uint32_t pbuf, uint32_t j) -> uint32_t {
     return pbuf + (j < qpad ? j * 16u : (j - qpad) * 16u + 8u);
   };
-  // row r of step k: its AFF row XOR the published rows its entries name; the
-  // row's own previous value comes from registers (`self`, most rows keep
-  // themselves), the others from shared memory, so a step loads only the
-  // entries that move sensitivity between rows
+  // row r of step k: its AFF row XOR the published rows its entries name.
+  // The loads of a row issue together, without branches: entries past the
+  // row's count read a shared word that is always zero (four loads always,
+  // four more for a row of five to eight entries: rows of one role share a
+  // warp).  A step takes as long as its slowest row's chain, since a barrier
+  // follows.
+  __shared__ uint64_t s_zero;
+  if (tid == 0) s_zero = 0;  // read after the first step's barrier
+  const uint32_t zaddr = smem_u32(&s_zero);
   auto apply = [&](uint32_t k, uint32_t r, const SegRow &m, uint64_t self, uint32_t pbuf) -> uint64_t {
     uint64_t v = m.c;
     if (m.n <= kSegRowCap) {
-      const uint32_t n8 = min(m.n, 8u);
-      for (uint32_t i = 0; i < n8; ++i) {
-        const uint32_t j = (m.e[i >> 1] >> ((i & 1u) * 16u)) & 0xFFFFu;
-        v ^= j == r ? self : j < n2 ? lds64(word_addr(pbuf, j)) : 0ull;
+#pragma unroll
+      for (uint32_t i = 0; i < 4; ++i) {
+        const uint32_t wj = (m.e[i >> 1] >> ((i & 1u) * 16u)) & 0xFFFFu;
+        v ^= lds64(i < m.n ? pbuf + wj * 8u : zaddr);
       }
-      if (m.n > 8) {  // entries 8..15 from the step's buffer (not refilled before the next barrier)
-        const uint16_t *l =
-            reinterpret_cast<const uint16_t *>(ring_c + (size_t)(k % NB) * step_bytes + cnt_b) + (size_t)r * kSegRowCap;
-        for (uint32_t i = 8; i < m.n; ++i) {
-          const uint32_t j = l[i];
-          v ^= j == r ? self : j < n2 ? lds64(word_addr(pbuf, j)) : 0ull;
+      if (m.n > 4) {
+#pragma unroll
+        for (uint32_t i = 4; i < kSegRingCap; ++i) {
+          const uint32_t wj = (m.e[i >> 1] >> ((i & 1u) * 16u)) & 0xFFFFu;
+          v ^= lds64(i < m.n ? pbuf + wj * 8u : zaddr);
+        }
+      }
+      if (m.n > kSegRingCap) {  // entries 8..15 (rare): from global memory
+        const uint4 t = __ldg(reinterpret_cast<const uint4 *>(
+            xhi + ((size_t)(sc.s_from + k) * n2 + r) * (kSegRowCap - kSegRingCap)));
+        const uint32_t e2[4] = {t.x, t.y, t.z, t.w};
+#pragma unroll
+        for (uint32_t i = 0; i < kSegRowCap - kSegRingCap; ++i) {
+          const uint32_t wj = (e2[i >> 1] >> ((i & 1u) * 16u)) & 0xFFFFu;
+          v ^= lds64(i + kSegRingCap < m.n ? pbuf + wj * 8u : zaddr);
         }
       }
     } else {  // a long row: its words from the dense transfer columns
