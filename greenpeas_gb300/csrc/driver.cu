@@ -165,10 +165,67 @@ struct Layout {
 
 }  // namespace
 
+namespace {
+// A DEM's host array: heap memory, or pinned memory that the device copies a
+// single-circuit result into directly.  resize() keeps no contents (the array
+// is written in full right after it is sized); pinned capacity grows with a
+// quarter of slack, since cudaHostAlloc is slow.
+template <typename T>
+class DemArray {
+ public:
+  explicit DemArray(bool pinned = false) : pinned_(pinned) {}
+  DemArray(const DemArray &) = delete;
+  DemArray &operator=(const DemArray &) = delete;
+  ~DemArray() { release(); }
+  void resize(size_t m) {
+    if (m > cap_) {
+      release();
+      const size_t want = pinned_ ? m + m / 4 : m;
+      if (pinned_) {
+        void *q = nullptr;
+        if (cudaHostAlloc(&q, want * sizeof(T), cudaHostAllocDefault) != cudaSuccess) {
+          cudaGetLastError();
+          throw gpc::Error(GPC_ERR_CUDA, "pinned DEM array allocation failed");
+        }
+        p_ = static_cast<T *>(q);
+      } else {
+        p_ = static_cast<T *>(::operator new(want * sizeof(T)));
+      }
+      cap_ = want;
+    }
+    n_ = m;
+  }
+  void clear() { n_ = 0; }
+  T *data() { return p_; }
+  const T *data() const { return p_; }
+  size_t size() const { return n_; }
+  size_t capacity() const { return cap_; }
+  T &operator[](size_t i) { return p_[i]; }
+  const T &operator[](size_t i) const { return p_[i]; }
+
+ private:
+  void release() {
+    if (p_) {
+      if (pinned_)
+        cudaFreeHost(p_);  // (fails harmlessly once the runtime has shut down at exit)
+      else
+        ::operator delete(p_);
+    }
+    p_ = nullptr;
+    n_ = cap_ = 0;
+  }
+  T *p_ = nullptr;
+  size_t n_ = 0, cap_ = 0;
+  bool pinned_;
+};
+}  // namespace
+
 struct gpc_dem {  // arrays written in full right after they are sized
-  gpc::HostArray<double> probs;
-  gpc::HostArray<uint32_t> offsets;
-  gpc::HostArray<uint32_t> targets;
+  explicit gpc_dem(bool pin = false) : probs(pin), offsets(pin), targets(pin), pinned(pin) {}
+  DemArray<double> probs;
+  DemArray<uint32_t> offsets;
+  DemArray<uint32_t> targets;
+  const bool pinned;
   uint32_t num_detectors = 0, num_observables = 0;
   uint64_t num_raw = 0;
   std::string text;
@@ -195,6 +252,22 @@ class DemCache {
     }
     return new gpc_dem;
   }
+  // A DEM with pinned arrays (a single-circuit fetch copies into it), or null
+  // when kMaxPinned of them exist already (the caller holds them): pinned
+  // memory stays bounded, and such a caller gets heap DEMs.
+  gpc_dem *take_pinned() {
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      if (!free_pinned_.empty()) {
+        gpc_dem *d = free_pinned_.back();
+        free_pinned_.pop_back();
+        return d;
+      }
+      if (live_pinned_ >= kMaxPinned) return nullptr;
+      ++live_pinned_;
+    }
+    return new gpc_dem(true);
+  }
   void give(gpc_dem *d) {
     d->probs.clear();  // sizes 0: a later resize past the capacity copies nothing
     d->offsets.clear();
@@ -203,6 +276,11 @@ class DemCache {
     d->text_ready = false;
     d->num_detectors = d->num_observables = 0;
     d->num_raw = 0;
+    if (d->pinned) {  // kept: at most kMaxPinned exist
+      std::lock_guard<std::mutex> lk(mu_);
+      free_pinned_.push_back(d);
+      return;
+    }
     const size_t b = size_of(d);
     {
       std::lock_guard<std::mutex> lk(mu_);
@@ -214,15 +292,21 @@ class DemCache {
     }
     delete d;
   }
+  // A pinned DEM that failed to fill (its arrays could not grow): freed, not kept.
+  void drop_pinned(gpc_dem *d) {
+    delete d;
+    std::lock_guard<std::mutex> lk(mu_);
+    --live_pinned_;
+  }
 
  private:
   static size_t size_of(const gpc_dem *d) {
     return d->probs.capacity() * 8 + (d->offsets.capacity() + d->targets.capacity()) * 4;
   }
-  static constexpr size_t kMaxDems = 8, kMaxBytes = (size_t)64 << 20;
+  static constexpr size_t kMaxDems = 8, kMaxBytes = (size_t)64 << 20, kMaxPinned = 4;
   std::mutex mu_;
-  std::vector<gpc_dem *> free_;
-  size_t bytes_ = 0;
+  std::vector<gpc_dem *> free_, free_pinned_;
+  size_t bytes_ = 0, live_pinned_ = 0;
 };
 DemCache &dem_cache() {
   static DemCache *c = new DemCache;
@@ -1582,6 +1666,43 @@ struct gpc_driver {
     host_ms[3] = ms_since(t3);
     const auto t4 = HostClock::now();
     const uint32_t N = ncirc();
+    if (N == 1) {  // one circuit: copied straight into a pinned DEM's arrays when one is to be had
+      gpc_dem *d = dem_cache().take_pinned();
+      if (d) {
+        try {
+          d->probs.resize(C);
+          d->offsets.resize((size_t)C + 1);
+          d->targets.resize(NT);
+        } catch (const gpc::Error &) {  // no pinned memory: the staged copy below
+          dem_cache().drop_pinned(d);
+          d = nullptr;
+        }
+      }
+      if (d) {
+        try {
+          if (C) {
+            CK(cudaMemcpyAsync(d->probs.data(), dptr<char>(L.out_prob), (size_t)C * 8, cudaMemcpyDeviceToHost,
+                               stream));
+            CK(cudaMemcpyAsync(d->offsets.data(), dptr<char>(L.out_off), (size_t)C * 4, cudaMemcpyDeviceToHost,
+                               stream));
+          }
+          if (NT) CK(cudaMemcpyAsync(d->targets.data(), tgbuf.p, (size_t)NT * 4, cudaMemcpyDeviceToHost, stream));
+          wait();
+        } catch (...) {
+          dem_cache().give(d);
+          throw;
+        }
+        d->offsets[C] = NT;
+        d->num_detectors = tapes[0].ndet;
+        d->num_observables = tapes[0].nobs;
+        d->num_raw = tapes[0].M;
+        last_d2h = (uint64_t)C * 12 + (uint64_t)NT * 4 + 12;
+        outs.assign(1, d);
+        host_ms[4] = ms_since(t4);
+        host_ms[5] = 0;
+        return;
+      }
+    }
     const size_t bytes = (size_t)C * 8 + (size_t)C * 4 + (size_t)NT * 4 + (size_t)N * 8 + 64;
     pin_out.ensure(bytes);
     char *h = static_cast<char *>(pin_out.p);
@@ -1631,7 +1752,8 @@ struct gpc_driver {
         outs[i] = dem.release();
       });
     } catch (...) {
-      for (auto &d : outs) delete d;
+      for (auto &d : outs)
+        if (d) dem_cache().give(d);
       outs.assign(N, nullptr);
       throw;
     }
@@ -1657,7 +1779,8 @@ struct gpc_driver {
         outs[i] = one[0];
       }
     } catch (...) {
-      for (auto &d : outs) delete d;
+      for (auto &d : outs)
+        if (d) dem_cache().give(d);
       outs.assign(N, nullptr);
       throw;
     }
@@ -1666,7 +1789,8 @@ struct gpc_driver {
   gpc_dem *fetch() {
     std::vector<gpc_dem *> outs;
     fetch_all(outs);
-    for (size_t i = 1; i < outs.size(); ++i) delete outs[i];
+    for (size_t i = 1; i < outs.size(); ++i)
+      if (outs[i]) dem_cache().give(outs[i]);
     return outs.empty() ? nullptr : outs[0];
   }
 
@@ -1791,7 +1915,8 @@ struct gpc_driver {
       last_h2d = h2d;
       last_d2h = d2h;
     } catch (...) {
-      for (auto &d : outs) delete d;
+      for (auto &d : outs)
+        if (d) dem_cache().give(d);
       outs.assign(n, nullptr);
       throw;
     }

@@ -328,10 +328,21 @@ struct Entry {
   uint32_t k() const { return qk >> 24; }
 };
 
+constexpr uint64_t kFnvBasis = 0xcbf29ce484222325ull, kFnvPrime = 0x100000001b3ull;  // FNV-1a 64
+
 struct QState {
   int64_t last = -1;      // epoch of the latest entry
   uint32_t cnt = 0;       // entries in that epoch
   uint32_t open = kNone;  // point holding the current rows (until a row-changing op)
+  // the qubit's op signatures in this segment (see the qubit packing), hashed
+  // as its entries are placed: op kinds, and op kinds with their epochs
+  uint64_t coarse = kFnvBasis, fine = kFnvBasis;
+  void sign(uint64_t op, uint32_t e) {
+    const uint32_t opc = (uint32_t)(op & 0xFF);
+    if (opc == OP_INJ || opc == OP_SNAPD) return;  // vary with detector membership only
+    coarse = (coarse ^ opc) * kFnvPrime;
+    fine = (fine ^ (opc | ((uint64_t)e << 8))) * kFnvPrime;
+  }
 };
 
 // Memoises the last split so uniform noise costs one sqrt/pow per distinct p.
@@ -525,8 +536,6 @@ Tape lower(const Parsed &P, const LowerOptions &opt) {
   lower_into(P, opt, T, S);
   return T;
 }
-
-constexpr uint64_t kFnvBasis = 0xcbf29ce484222325ull, kFnvPrime = 0x100000001b3ull;  // FNV-1a 64
 
 void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch &S, HostPool *pool) {
   if (opt.level < 0 || opt.level > 2) throw Error(GPC_ERR_INVALID, "correlation level must be 0, 1 or 2");
@@ -809,6 +818,7 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
         e = (uint32_t)s.last;
       }
       *ent1++ = {q | (s.cnt << 24), e, op};
+      s.sign(op, e);
       if (e >= ep_k.size()) {
         ep_k.resize((size_t)e + 1, 0);
         ep_np.resize((size_t)e + 1, 0);
@@ -853,8 +863,11 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
             uint32_t E = (uint32_t)(std::max(st[a].last, st[b].last) + 1);
             uint32_t subA = (uint32_t)g.img[0] | ((uint32_t)g.img[1] << 4);
             uint32_t subB = swap_halves(g.img[2]) | (swap_halves(g.img[3]) << 4);
-            *ent1++ = {a, E, c2_op(subA, b)};  // partner operands become slots below
-            *ent1++ = {b, E, c2_op(subB, a)};
+            const uint64_t opA = c2_op(subA, b), opB = c2_op(subB, a);
+            *ent1++ = {a, E, opA};  // partner operands become slots below
+            *ent1++ = {b, E, opB};
+            st[a].sign(opA, E);
+            st[b].sign(opB, E);
             if (E >= ep_k.size()) {
               ep_k.resize((size_t)E + 1, 0);
               ep_np.resize((size_t)E + 1, 0);
@@ -974,14 +987,11 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
     G.nprov = nprov;
     // the segment's share of each qubit's signatures (see the qubit packing):
     // op kinds, and op kinds with their (segment-local) epochs
-    G.fine.assign(nq, kFnvBasis);
-    G.coarse.assign(nq, kFnvBasis);
-    for (const Entry *x = ent0; x < ent1; ++x) {
-      const uint32_t opc = (uint32_t)(x->op & 0xFF);
-      if (opc == OP_INJ || opc == OP_SNAPD) continue;  // vary with detector membership only
-      const uint32_t q = x->q();
-      G.coarse[q] = (G.coarse[q] ^ opc) * kFnvPrime;
-      G.fine[q] = (G.fine[q] ^ (opc | ((uint64_t)x->e << 8))) * kFnvPrime;
+    G.fine.resize(nq);
+    G.coarse.resize(nq);
+    for (uint32_t q = 0; q < nq; ++q) {
+      G.fine[q] = st[q].fine;
+      G.coarse[q] = st[q].coarse;
     }
   };
   if (pool && nseg > 1)

@@ -132,6 +132,25 @@ def test_long_symptoms(n):
         _check(dem, t)
 
 
+def test_many_live_dems():
+    """A single compile copies its result straight into a pinned DEM while at most four of those
+    are alive; a caller holding more gets DEMs filled through the staging buffer.  Every DEM stays
+    intact while others are made and freed."""
+    texts = [gp.BBCode(6).get_memory(6, 1e-3, noise="uniform"), gp.SurfaceCode(5).get_memory(5, 1e-3, noise="uniform")]
+    drv = gp.get_driver(texts[0])
+    refs = [drv.compile(t).canonical() for t in texts]
+    held = [drv.compile(texts[i % 2]) for i in range(9)]
+    for i, dem in enumerate(held):
+        assert dem.canonical() == refs[i % 2]
+    del held[::2]  # freed DEMs return to the cache, are reused by the next compiles
+    more = [drv.compile(texts[i % 2]) for i in range(6)]
+    for i, dem in enumerate(held):
+        assert dem.canonical() == refs[(2 * i + 1) % 2]
+    for i, dem in enumerate(more):
+        assert dem.canonical() == refs[i % 2]
+    _check(more[0], texts[0])
+
+
 def test_driver_reuse_from_large_to_small_circuits():
     """One driver compiling circuits of falling size (its arena holds the previous circuit's data)
     gives exactly what fresh drivers give."""
