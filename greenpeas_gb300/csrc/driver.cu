@@ -195,7 +195,18 @@ class DemArray {
     }
     n_ = m;
   }
-  void clear() { n_ = 0; }
+  // Views n elements at p (memory owned elsewhere: a batch's result block);
+  // the array's own buffer is released.
+  void view(T *p, size_t n) {
+    release();
+    p_ = p;
+    n_ = n;
+    view_ = true;
+  }
+  void clear() {
+    if (view_) release();
+    n_ = 0;
+  }
   T *data() { return p_; }
   const T *data() const { return p_; }
   size_t size() const { return n_; }
@@ -205,7 +216,7 @@ class DemArray {
 
  private:
   void release() {
-    if (p_) {
+    if (p_ && !view_) {
       if (pinned_)
         cudaFreeHost(p_);  // (fails harmlessly once the runtime has shut down at exit)
       else
@@ -213,11 +224,80 @@ class DemArray {
     }
     p_ = nullptr;
     n_ = cap_ = 0;
+    view_ = false;
   }
   T *p_ = nullptr;
   size_t n_ = 0, cap_ = 0;
   bool pinned_;
+  bool view_ = false;
 };
+
+// Page-locked memory that one batch's DEM arrays are copied back into.  The
+// batch's DEMs view their probabilities and targets in it and share it; the
+// last one freed returns it to the pool.  At most kMaxLive blocks exist, so
+// page-locked memory stays bounded: a caller holding more batches gets DEMs
+// that own copies of their arrays.
+struct ResultBlock {
+  void *p = nullptr;
+  size_t cap = 0;
+  ~ResultBlock() {
+    if (p) cudaFreeHost(p);
+  }
+};
+class BlockPool {
+ public:
+  // A block of at least `bytes`, or null (none free and kMaxLive alive, or no page-locked memory).
+  std::shared_ptr<ResultBlock> take(size_t bytes) {
+    ResultBlock *b = nullptr;
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      if (!free_.empty()) {  // the largest free block
+        auto it = std::max_element(free_.begin(), free_.end(),
+                                   [](const ResultBlock *x, const ResultBlock *y) { return x->cap < y->cap; });
+        b = *it;
+        free_.erase(it);
+      } else if (live_ < kMaxLive) {
+        b = new ResultBlock;
+        ++live_;
+      } else {
+        return nullptr;
+      }
+    }
+    if (b->cap < bytes) {  // grow, with slack (page-locked allocations are slow)
+      if (b->p) cudaFreeHost(b->p);
+      b->p = nullptr;
+      b->cap = 0;
+      const size_t want = bytes + bytes / 4;
+      if (cudaHostAlloc(&b->p, want, cudaHostAllocPortable) != cudaSuccess) {
+        cudaGetLastError();
+        b->p = nullptr;
+        drop(b);
+        return nullptr;
+      }
+      b->cap = want;
+    }
+    return std::shared_ptr<ResultBlock>(b, [this](ResultBlock *x) { give(x); });
+  }
+
+ private:
+  void give(ResultBlock *b) {
+    std::lock_guard<std::mutex> lk(mu_);
+    free_.push_back(b);
+  }
+  void drop(ResultBlock *b) {
+    delete b;
+    std::lock_guard<std::mutex> lk(mu_);
+    --live_;
+  }
+  static constexpr size_t kMaxLive = 4;
+  std::mutex mu_;
+  std::vector<ResultBlock *> free_;
+  size_t live_ = 0;
+};
+BlockPool &block_pool() {
+  static BlockPool *p = new BlockPool;  // never destroyed (blocks may be freed during process exit)
+  return *p;
+}
 }  // namespace
 
 struct gpc_dem {  // arrays written in full right after they are sized
@@ -226,6 +306,7 @@ struct gpc_dem {  // arrays written in full right after they are sized
   DemArray<uint32_t> offsets;
   DemArray<uint32_t> targets;
   const bool pinned;
+  std::shared_ptr<ResultBlock> block;  // the batch result block its probabilities and targets view
   uint32_t num_detectors = 0, num_observables = 0;
   uint64_t num_raw = 0;
   std::string text;
@@ -269,9 +350,10 @@ class DemCache {
     return new gpc_dem(true);
   }
   void give(gpc_dem *d) {
-    d->probs.clear();  // sizes 0: a later resize past the capacity copies nothing
+    d->probs.clear();  // sizes 0: a later resize past the capacity copies nothing (views dropped)
     d->offsets.clear();
     d->targets.clear();
+    d->block.reset();
     std::string().swap(d->text);
     d->text_ready = false;
     d->num_detectors = d->num_observables = 0;
@@ -303,7 +385,8 @@ class DemCache {
   static size_t size_of(const gpc_dem *d) {
     return d->probs.capacity() * 8 + (d->offsets.capacity() + d->targets.capacity()) * 4;
   }
-  static constexpr size_t kMaxDems = 8, kMaxBytes = (size_t)64 << 20, kMaxPinned = 4;
+  // (a batch's DEMs come back together: enough for one batch's offsets arrays)
+  static constexpr size_t kMaxDems = 1024, kMaxBytes = (size_t)128 << 20, kMaxPinned = 4;
   std::mutex mu_;
   std::vector<gpc_dem *> free_, free_pinned_;
   size_t bytes_ = 0, live_pinned_ = 0;
@@ -460,6 +543,7 @@ struct gpc_driver {
     if (caller_ev) cudaEventDestroy(caller_ev);
     if (done_ev) cudaEventDestroy(done_ev);
     if (wait_ev) cudaEventDestroy(wait_ev);
+    if (fetch_ev) cudaEventDestroy(fetch_ev);
     for (auto &e : join_ev)
       if (e) cudaEventDestroy(e);
     for (auto &a : aux)
@@ -1653,14 +1737,30 @@ struct gpc_driver {
     out[3] = nb * 24 + groups * (16 + 4) + 8.0 * targets + groups * 12;
   }
 
-  // Copies the merged arrays of the last run to the host and splits them per circuit.
-  void fetch_all(std::vector<gpc_dem *> &outs) {
+  // A fetch whose copies are issued and whose DEMs are not built yet, with
+  // what building them needs after the driver has moved on to other circuits.
+  struct PendingFetch {
+    bool active = false;
+    std::vector<gpc_dem *> done;  // DEMs built already (single-circuit pinned path, fallback)
+    std::shared_ptr<ResultBlock> blk;
+    const char *h = nullptr;  // where the copies land (the block, else the staging buffer)
+    uint32_t C = 0, NT = 0, N = 0;
+    std::vector<uint32_t> ndet, nobs, order;
+    std::vector<uint64_t> M;
+  };
+  cudaEvent_t fetch_ev = nullptr;  // the last begin_fetch's copies
+
+  // Waits for the pipeline and issues the copies of its result on the driver's
+  // stream; end_fetch builds the DEMs.  A single circuit copied into a pinned
+  // DEM, and a batch that falls back to circuit-by-circuit compiles, finish here.
+  void begin_fetch(PendingFetch &pf) {
     if (!ran) throw gpc::Error(GPC_ERR_INVALID, "nothing has been run");
     CK(cudaSetDevice(device));
+    pf = PendingFetch{};
     uint32_t C = 0, NT = 0;
     const auto t3 = HostClock::now();
     if (finish(&C, &NT) == Finish::BatchFallback) {
-      batch_fallback(outs);
+      batch_fallback(pf.done);
       return;
     }
     host_ms[3] = ms_since(t3);
@@ -1697,15 +1797,23 @@ struct gpc_driver {
         d->num_observables = tapes[0].nobs;
         d->num_raw = tapes[0].M;
         last_d2h = (uint64_t)C * 12 + (uint64_t)NT * 4 + 12;
-        outs.assign(1, d);
+        pf.done.assign(1, d);
         host_ms[4] = ms_since(t4);
         host_ms[5] = 0;
         return;
       }
     }
     const size_t bytes = (size_t)C * 8 + (size_t)C * 4 + (size_t)NT * 4 + (size_t)N * 8 + 64;
-    pin_out.ensure(bytes);
-    char *h = static_cast<char *>(pin_out.p);
+    // into a result block that the DEMs keep (they view their probabilities and targets in
+    // it), else into the staging buffer, split into DEMs that own copies
+    pf.blk = block_pool().take(bytes);
+    char *h;
+    if (pf.blk) {
+      h = static_cast<char *>(pf.blk->p);
+    } else {
+      pin_out.ensure(bytes);
+      h = static_cast<char *>(pin_out.p);
+    }
     char *hp = h, *ho = h + (size_t)C * 8, *ht = ho + (size_t)C * 4, *hc = ht + (size_t)NT * 4;
     if (C) {
       CK(cudaMemcpyAsync(hp, dptr<char>(L.out_prob), (size_t)C * 8, cudaMemcpyDeviceToHost, stream));
@@ -1713,33 +1821,79 @@ struct gpc_driver {
     }
     if (NT) CK(cudaMemcpyAsync(ht, tgbuf.p, (size_t)NT * 4, cudaMemcpyDeviceToHost, stream));
     if (N > 1) CK(cudaMemcpyAsync(hc, dptr<char>(L.cout), (size_t)N * 8, cudaMemcpyDeviceToHost, stream));
-    wait();
-    host_ms[4] = ms_since(t4);
-    const auto t5 = HostClock::now();
+    if (!fetch_ev) CK(cudaEventCreateWithFlags(&fetch_ev, cudaEventDisableTiming));
+    CK(cudaEventRecord(fetch_ev, stream));
     last_d2h = (uint64_t)C * 12 + (uint64_t)NT * 4 + 12 + (N > 1 ? (uint64_t)N * 8 : 0);
-    const double *P = reinterpret_cast<const double *>(hp);
-    const uint32_t *O = reinterpret_cast<const uint32_t *>(ho);
-    const uint32_t *TG = reinterpret_cast<const uint32_t *>(ht);
-    const uint2 *CO = reinterpret_cast<const uint2 *>(hc);
+    pf.active = true;
+    pf.h = h;
+    pf.C = C;
+    pf.NT = NT;
+    pf.N = N;
+    pf.ndet.resize(N);
+    pf.nobs.resize(N);
+    pf.M.resize(N);
+    for (uint32_t i = 0; i < N; ++i) {
+      pf.ndet[i] = tapes[i].ndet;
+      pf.nobs[i] = tapes[i].nobs;
+      pf.M[i] = tapes[i].M;
+    }
+    pf.order = big_first;
+    if (pf.order.size() != N) {
+      pf.order.resize(N);
+      for (uint32_t i = 0; i < N; ++i) pf.order[i] = i;
+    }
+    host_ms[4] = ms_since(t4);
+  }
+
+  // Waits for begin_fetch's copies and builds the DEMs: views into the result
+  // block, or copies out of the staging buffer.
+  void end_fetch(PendingFetch &pf, std::vector<gpc_dem *> &outs) {
+    if (!pf.active) {
+      outs.swap(pf.done);
+      return;
+    }
+    const auto t4 = HostClock::now();
+    CK(cudaEventSynchronize(fetch_ev));
+    host_ms[4] += ms_since(t4);
+    const auto t5 = HostClock::now();
+    const uint32_t C = pf.C, NT = pf.NT, N = pf.N;
+    const char *h = pf.h;
+    const double *P = reinterpret_cast<const double *>(h);
+    const uint32_t *O = reinterpret_cast<const uint32_t *>(h + (size_t)C * 8);
+    const uint32_t *TG = reinterpret_cast<const uint32_t *>(h + (size_t)C * 12);
+    const uint2 *CO = reinterpret_cast<const uint2 *>(h + (size_t)C * 12 + (size_t)NT * 4);
+    const std::shared_ptr<ResultBlock> blk = std::move(pf.blk);
+    pf.active = false;
     outs.assign(N, nullptr);
     try {
       for_each(N, N >= 8, [&](uint32_t x, uint32_t) {
-        const uint32_t i = big_first[x];
+        const uint32_t i = pf.order[x];
         const uint32_t c0 = N > 1 ? CO[i].x : 0, c1 = (N > 1 && i + 1 < N) ? CO[i + 1].x : C;
         const uint32_t t0 = N > 1 ? CO[i].y : 0, t1 = (N > 1 && i + 1 < N) ? CO[i + 1].y : NT;
         if (c1 < c0 || c1 > C || t1 < t0 || t1 > NT) throw gpc::Error(GPC_ERR_CUDA, "inconsistent batch ranges");
         std::unique_ptr<gpc_dem> dem(dem_cache().take());
-        dem->num_detectors = tapes[i].ndet;
-        dem->num_observables = tapes[i].nobs;
-        dem->num_raw = tapes[i].M;
-        dem->probs.resize(c1 - c0);
-        dem->offsets.resize((size_t)(c1 - c0) + 1);
-        dem->targets.resize(t1 - t0);
+        dem->num_detectors = pf.ndet[i];
+        dem->num_observables = pf.nobs[i];
+        dem->num_raw = pf.M[i];
+        const uint32_t ne = c1 - c0, nt = t1 - t0;
+        if (blk) {  // views into the block; the offsets rebased to the DEM's first target
+          dem->block = blk;
+          dem->probs.view(const_cast<double *>(P) + c0, ne);
+          dem->targets.view(const_cast<uint32_t *>(TG) + t0, nt);
+          dem->offsets.resize((size_t)ne + 1);
+          uint32_t *dof = dem->offsets.data();
+          for (uint32_t k = 0; k < ne; ++k) dof[k] = O[c0 + k] - t0;
+          dof[ne] = nt;
+          outs[i] = dem.release();
+          return;
+        }
+        dem->probs.resize(ne);
+        dem->offsets.resize((size_t)ne + 1);
+        dem->targets.resize(nt);
         double *dp = dem->probs.data();
         uint32_t *dof = dem->offsets.data(), *dt = dem->targets.data();
         // one large result is copied in pieces on the host pool (a single
         // thread's copy rate would dominate the fetch)
-        const uint32_t ne = c1 - c0, nt = t1 - t0;
         const uint32_t np = N == 1 && (size_t)ne * 12 + (size_t)nt * 4 >= (256u << 10) ? copy_pieces() : 1u;
         for_each(np, np > 1, [&](uint32_t q, uint32_t) {
           const uint32_t e0 = (uint32_t)((uint64_t)ne * q / np), e1 = (uint32_t)((uint64_t)ne * (q + 1) / np);
@@ -1760,6 +1914,13 @@ struct gpc_driver {
     host_ms[5] = ms_since(t5);
   }
 
+  // Copies the merged arrays of the last run to the host and splits them per circuit.
+  void fetch_all(std::vector<gpc_dem *> &outs) {
+    PendingFetch pf;
+    begin_fetch(pf);
+    end_fetch(pf, outs);
+  }
+
   // A batch whose merge needs a fallback (a symptom repeated more than a
   // bucket holds, or a symptom longer than the target lists): compile its
   // circuits one at a time on the single-circuit path.
@@ -1769,7 +1930,8 @@ struct gpc_driver {
     outs.assign(N, nullptr);
     try {
       for (uint32_t i = 0; i < N; ++i) {
-        tapes.assign(1, std::move(T[i]));
+        tapes.clear();
+        tapes.push_back(std::move(T[i]));
         tcap = 32;
         lists_off = false;
         prepare(nullptr, nullptr, 0);
@@ -1898,25 +2060,48 @@ struct gpc_driver {
     gpc_driver *D[2] = {this, &twin()};
     outs.assign(n, nullptr);
     uint64_t h2d = 0, d2h = 0;
-    auto collect = [&](uint32_t c) {
-      std::vector<gpc_dem *> v;
-      D[c & 1]->fetch_all(v);
+    double ms[6] = {};  // host phases summed over the chunks of both pipelines
+    auto add_ms = [&](const gpc_driver *d, int k0, int k1) {
+      for (int k = k0; k < k1; ++k) ms[k] += d->host_ms[k];
+    };
+    // Chunk c - 1's copies back are issued once chunk c is running, and its
+    // DEMs built after chunk c + 1 is prepared on the same pipeline (whose
+    // stream has drained them meanwhile): the host lowers while they copy.
+    std::vector<PendingFetch> pend(nc);
+    auto begin = [&](uint32_t c) {
+      D[c & 1]->begin_fetch(pend[c]);
+      add_ms(D[c & 1], 3, 5);
       d2h += D[c & 1]->last_d2h;
+    };
+    auto end = [&](uint32_t c) {
+      std::vector<gpc_dem *> v;
+      const double issued = D[c & 1]->host_ms[4];
+      D[c & 1]->end_fetch(pend[c], v);
+      ms[4] += D[c & 1]->host_ms[4] - issued;  // the wait for the copies
+      add_ms(D[c & 1], 5, 6);
       for (uint32_t i = 0; i < (uint32_t)v.size(); ++i) outs[cut[c] + i] = v[i];
     };
     try {
       for (uint32_t c = 0; c < nc; ++c) {
         D[c & 1]->prepare(texts + cut[c], lens + cut[c], cut[c + 1] - cut[c]);
+        add_ms(D[c & 1], 0, 3);
         h2d += D[c & 1]->last_h2d;
+        if (c >= 2) end(c - 2);
         D[c & 1]->run();
-        if (c) collect(c - 1);
+        if (c >= 1) begin(c - 1);
       }
-      collect(nc - 1);
+      begin(nc - 1);
+      if (nc >= 2) end(nc - 2);
+      end(nc - 1);
       last_h2d = h2d;
       last_d2h = d2h;
+      for (int k = 0; k < 6; ++k) host_ms[k] = ms[k];
     } catch (...) {
       for (auto &d : outs)
         if (d) dem_cache().give(d);
+      for (auto &pf : pend)
+        for (auto &d : pf.done)
+          if (d) dem_cache().give(d);
       outs.assign(n, nullptr);
       throw;
     }

@@ -250,7 +250,8 @@ gpc_status gpc_last_timings(gpc_driver *driver, float *ms5);
  * the prepared tapes were reused), [1] layout and device buffer growth, [2]
  * staging of the inputs into pinned memory, [3] waiting for the pipeline and
  * its result sizes, [4] device-to-host copies of the DEM arrays, [5] splitting
- * them into per-circuit DEMs. */
+ * them into per-circuit DEMs.  After a gpc_compile_batch that ran in chunks,
+ * each phase summed over the chunks. */
 gpc_status gpc_last_host_timings(gpc_driver *driver, double *ms6);
 
 /* Walk launches of the prepared circuits (no counterpart in the reference):
