@@ -143,12 +143,14 @@ struct WalkClass {
   uint32_t qpad, item0, n_items, chunk_cap, max_epochs, max_chunks, words, qpt, queue;
 };
 
-// Byte offsets of every array inside the arena (inputs first, so the whole
-// input region is one contiguous H2D copy).
+// Byte offsets of every array inside the arena (staged inputs first, so they
+// are one contiguous H2D copy; then the ops of tapes in page-locked memory,
+// one copy each).
 struct Layout {
   std::vector<CircLayout> c;
   size_t cdev, items, mbase, cbbase;
   size_t in_bytes;
+  size_t ext_ops;  // bytes of page-locked tape ops
   size_t mdesc, mp, tl, tn, key, blk_r0, slot, bagg, bout, cout, big_list;
   size_t zero, err, totals, bcount, tsum, big_n, wq, zero_bytes;
   size_t sk0, sk1, pm0, pm1, hik;  // global path (single circuit)
@@ -166,6 +168,21 @@ struct Layout {
 }  // namespace
 
 namespace {
+// Page-locked memory for the op arrays of the tapes a driver owns (null when
+// there is none: the tape then uses the heap and its ops are staged).  A
+// driver keeps its tapes (and their buffers) from one compile to the next,
+// since freeing page-locked memory is slow and may wait for the device.
+void *pinned_alloc(size_t bytes) {
+  void *p = nullptr;
+  if (cudaHostAlloc(&p, bytes, cudaHostAllocPortable) != cudaSuccess) {
+    cudaGetLastError();
+    return nullptr;
+  }
+  return p;
+}
+void pinned_free(void *p) { cudaFreeHost(p); }
+void pin_ops(Tape &T) { T.ops.set_allocator(pinned_alloc, pinned_free); }
+
 // A DEM's host array: heap memory, or pinned memory that the device copies a
 // single-circuit result into directly.  resize() keeps no contents (the array
 // is written in full right after it is sized); pinned capacity grows with a
@@ -564,7 +581,12 @@ struct gpc_driver {
     } else {
       CK(cudaStreamSynchronize(stream));
     }
+    ops_in_flight = false;
   }
+  // A copy of page-locked tape ops to the device may still be reading them
+  // (set by prepare, cleared by wait): the tapes are not rewritten or handed
+  // back before the stream has caught up.
+  bool ops_in_flight = false;
 
   void init_streams() {
     CK(cudaStreamCreateWithFlags(&stream, cudaStreamNonBlocking));
@@ -602,7 +624,7 @@ struct gpc_driver {
     for (uint32_t i = 0; i < N; ++i) {
       const Tape &T = tapes[i];
       CircLayout &c = L.c[i];
-      c.ops = take(T.ops.size() * 8);
+      c.ops = T.ops.external() ? 0 : take(T.ops.size() * 8);  // page-locked ops: placed below
       c.ep_opoff = take(T.ep_opoff.size() * 4);
       c.ep_k = take(T.ep_k.size() * 4);
       c.ep_ptoff = take(T.ep_ptoff.size() * 4);
@@ -639,7 +661,14 @@ struct gpc_driver {
       L.src_off = take(((size_t)tapes[0].n_ticks * gpc::SRC_CLASSES + 1) * 4);
       L.src_rec = take(tapes[0].rec.size() * 4);
     }
-    L.in_bytes = o;
+    L.in_bytes = o;  // the staged inputs (one copy from pinned memory)
+    // ops in page-locked tape memory: copied to the device straight from it, one copy per tape
+    L.ext_ops = 0;
+    for (uint32_t i = 0; i < N; ++i)
+      if (tapes[i].ops.external()) {
+        L.c[i].ops = take(tapes[i].ops.size() * 8);
+        L.ext_ops += tapes[i].ops.size() * 8;
+      }
     for (uint32_t i = 0; i < N; ++i) {
       L.c[i].snap = take((size_t)tapes[i].w * tapes[i].npoints * 16);
       L.c[i].band = take((size_t)tapes[i].w * 8);
@@ -805,7 +834,7 @@ struct gpc_driver {
         const void *src;
         size_t bytes;
       };
-      const Copy cs[] = {{l.ops, T.ops.data(), T.ops.size() * 8},
+      const Copy cs[] = {{l.ops, T.ops.data(), T.ops.external() ? 0 : T.ops.size() * 8},
                          {l.ep_opoff, T.ep_opoff.data(), T.ep_opoff.size() * 4},
                          {l.ep_k, T.ep_k.data(), T.ep_k.size() * 4},
                          {l.ep_ptoff, T.ep_ptoff.data(), T.ep_ptoff.size() * 4},
@@ -899,7 +928,27 @@ struct gpc_driver {
   // Parses and lowers circuits (in parallel on host threads for batches).
   // The tapes and each thread's scratch memory are kept from one compile to
   // the next, so a repeated compile reuses mapped host memory.
+  // n tapes, taken from and given back to the spares (tapes are not freed:
+  // their op buffers are page-locked)
+  std::vector<Tape> spare_tapes;
+  void resize_tapes(uint32_t n) {
+    while (tapes.size() > n) {
+      spare_tapes.push_back(std::move(tapes.back()));
+      tapes.pop_back();
+    }
+    while (tapes.size() < n) {
+      if (spare_tapes.empty()) {
+        tapes.emplace_back();
+      } else {
+        tapes.push_back(std::move(spare_tapes.back()));
+        spare_tapes.pop_back();
+      }
+      pin_ops(tapes.back());
+    }
+  }
+
   void lower_all(const char *const *texts, const size_t *lens, uint32_t n) {
+    if (ops_in_flight) wait();
     have_tape = false;  // the tapes are rewritten in place
     gpc::LowerOptions lo;
     lo.level = level;
@@ -907,7 +956,7 @@ struct gpc_driver {
     if (n > 1) lo.chunk_min = gpc::kWalkChunkMin;
     gpc::HostPool &hp = host_pool();
     if (lower_scratch.size() < hp.workers() + 1) lower_scratch.resize(hp.workers() + 1);
-    tapes.resize(n);
+    resize_tapes(n);
     order_by_size(n, [&](uint32_t i) { return (uint64_t)lens[i]; });
     if (n == 1)  // one circuit: a large text is parsed in pieces on the pool
       gpc::lower_text(texts[0], lens[0], lo, tapes[0], lower_scratch[0], &hp);
@@ -926,6 +975,7 @@ struct gpc_driver {
     param = false;
     tcap = 32;
     lists_off = false;
+    if (ops_in_flight) wait();
     tapes.swap(T);
     have_tape = true;
     prepare(nullptr, nullptr, 0);
@@ -973,7 +1023,13 @@ struct gpc_driver {
     stage_inputs();
     host_ms[2] = ms_since(t2);
     CK(cudaMemcpyAsync(arena.p, pin_in.p, L.in_bytes, cudaMemcpyHostToDevice, stream));
-    last_h2d = L.in_bytes;
+    for (uint32_t i = 0; i < ncirc(); ++i)
+      if (tapes[i].ops.external() && tapes[i].ops.size()) {
+        CK(cudaMemcpyAsync(dptr<char>(L.c[i].ops), tapes[i].ops.data(), tapes[i].ops.size() * 8,
+                           cudaMemcpyHostToDevice, stream));
+        ops_in_flight = true;
+      }
+    last_h2d = L.in_bytes + L.ext_ops;
     // what a captured graph depends on: buffer addresses and launch sizes
     uint64_t h = 0xcbf29ce484222325ull;
     auto mix = [&](uint64_t v) { h = (h ^ v) * 0x100000001b3ull; };
@@ -1930,6 +1986,7 @@ struct gpc_driver {
     outs.assign(N, nullptr);
     try {
       for (uint32_t i = 0; i < N; ++i) {
+        for (Tape &x : tapes) spare_tapes.push_back(std::move(x));  // kept (page-locked ops)
         tapes.clear();
         tapes.push_back(std::move(T[i]));
         tcap = 32;
@@ -2246,6 +2303,7 @@ struct gpc_server {
             spare.pop_back();
           }
         }
+        pin_ops(*tape);
         gpc::lower_text(text, len, lo, *tape, scratch);
         {
           std::lock_guard<std::mutex> lk(mu);

@@ -19,6 +19,8 @@
 #pragma once
 
 #include <cstdint>
+#include <cstdlib>
+#include <new>
 #include <memory>
 #include <stdexcept>
 #include <string>
@@ -131,10 +133,90 @@ Parsed parse_stim(const char *text, size_t len);
 void parse_stim_into(const char *text, size_t len, Parsed &out);
 
 // A lowered circuit: everything the device pipeline needs.
+// A tape's op array.  Its memory comes from the allocator its owner set
+// (page-locked memory for the tapes a driver owns: the device copy of the ops
+// is made straight from it) or, without one or when that allocator has none
+// to give, from the heap.  resize() keeps no contents: the lowering writes
+// every op after sizing the array.
+class OpArray {
+ public:
+  using AllocFn = void *(*)(size_t bytes);
+  using FreeFn = void (*)(void *);
+  OpArray() = default;
+  OpArray(OpArray &&o) noexcept { take(o); }
+  OpArray &operator=(OpArray &&o) noexcept {
+    if (this != &o) {
+      release();
+      take(o);
+    }
+    return *this;
+  }
+  OpArray(const OpArray &) = delete;
+  OpArray &operator=(const OpArray &) = delete;
+  ~OpArray() { release(); }
+  // Takes effect from the next allocation (a held buffer is released now).
+  void set_allocator(AllocFn a, FreeFn f) {
+    if (a == alloc_ && f == free_) return;
+    release();
+    alloc_ = a;
+    free_ = f;
+  }
+  void resize(size_t n) {
+    if (n > cap_) {
+      release();
+      const size_t want = n + n / 4;  // slack: page-locked allocations are slow
+      void *q = alloc_ ? alloc_(want * sizeof(uint64_t)) : nullptr;
+      ext_ = q != nullptr;
+      if (!q) q = std::malloc(want * sizeof(uint64_t));
+      if (!q) throw std::bad_alloc();
+      p_ = static_cast<uint64_t *>(q);
+      cap_ = want;
+    }
+    n_ = n;
+  }
+  void clear() { n_ = 0; }
+  uint64_t *data() { return p_; }
+  const uint64_t *data() const { return p_; }
+  size_t size() const { return n_; }
+  uint64_t &operator[](size_t i) { return p_[i]; }
+  const uint64_t &operator[](size_t i) const { return p_[i]; }
+  // The buffer came from the owner's allocator.
+  bool external() const { return ext_; }
+
+ private:
+  void release() {
+    if (p_) {
+      if (ext_)
+        free_(p_);
+      else
+        std::free(p_);
+    }
+    p_ = nullptr;
+    n_ = cap_ = 0;
+    ext_ = false;
+  }
+  void take(OpArray &o) {
+    p_ = o.p_;
+    n_ = o.n_;
+    cap_ = o.cap_;
+    ext_ = o.ext_;
+    alloc_ = o.alloc_;
+    free_ = o.free_;
+    o.p_ = nullptr;
+    o.n_ = o.cap_ = 0;
+    o.ext_ = false;
+  }
+  uint64_t *p_ = nullptr;
+  size_t n_ = 0, cap_ = 0;
+  bool ext_ = false;
+  AllocFn alloc_ = nullptr;
+  FreeFn free_ = nullptr;
+};
+
 struct Tape {
   uint32_t nq = 0, qpad = 0, nmeas = 0, ndet = 0, nobs = 0, nbits = 0, w = 0;
   uint32_t n_epochs = 0, kmax = 0;
-  HostArray<uint64_t> ops;          // sum_e K_e * qpad (every op written by the lowering)
+  OpArray ops;                      // sum_e K_e * qpad (every op written by the lowering)
   std::vector<uint32_t> ep_opoff;   // [n_epochs]     first op of epoch e
   std::vector<uint32_t> ep_k;       // [n_epochs]     slots in epoch e
   std::vector<uint32_t> ep_ptoff;   // [n_epochs + 1] first point of epoch e
