@@ -326,7 +326,7 @@ def batched_leg(gp, torch, local: int, flush, steps: int, warmup: int, circuits:
     del e2e_outs
     h2d_b = d2h_b = 0
     t0 = time.perf_counter()
-    e2e_steps = max(1, min(steps, 3))
+    e2e_steps = max(3, min(steps, 10))
     for _ in range(e2e_steps):
         bdrv.compile_batch(texts)
     batch_e2e_s = (time.perf_counter() - t0) / e2e_steps

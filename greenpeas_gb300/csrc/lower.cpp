@@ -751,10 +751,9 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
   cut.clear();
   cut.push_back(P.ins.size());
   {
-    // at most 8 segments of equal size, about 8,192 occurrences or fewer each
-    // (each cut adds at most about one epoch to the walk, and splits the
-    // scheduling and assembly across one more pool thread)
-    const size_t nsegw = std::max<size_t>(1, std::min<size_t>(8, (occ + 8191) / 8192));
+    // at most 8 segments of equal size, about opt.segment_occ occurrences or fewer each
+    const size_t so = std::max<uint32_t>(1024, opt.segment_occ);
+    const size_t nsegw = std::max<size_t>(1, std::min<size_t>(8, (occ + so - 1) / so));
     const size_t per = (occ + nsegw - 1) / nsegw;
     size_t acc = 0;
     for (size_t ii = P.ins.size(); ii-- > 1;) {

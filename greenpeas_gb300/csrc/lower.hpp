@@ -257,6 +257,11 @@ struct LowerOptions {
   uint32_t kcap = 8; // max slots per epoch
   uint32_t chunk_min = 0xFFFFFFFFu;  // smallest tape chunk (bytes; capped by the walk's shared memory)
   bool sources = true;  // fill Tape::rec_src (read by the noise-rate gradient only)
+  // Target occurrences per time segment of the backward pass (at most 8
+  // segments, of equal size).  Segments are scheduled on the host pool when
+  // one is given; each cut adds at most about one epoch to the walk.  The
+  // DEM does not depend on it.
+  uint32_t segment_occ = 16384;
 };
 
 // Shared-memory plan of the walk kernel (bytes): double-buffered tape chunks,

@@ -24,6 +24,7 @@ gpc_status gpc_tape_lower(const char *stim_text, size_t len, int32_t correlation
   try {
     gpc::LowerOptions lo;
     lo.level = correlation_level;
+    lo.segment_occ = 8192;  // as a compile lowers it
     std::unique_ptr<gpc_tape> t(new gpc_tape{});
     gpc::LowerScratch scratch;
     if (len >= 64 * 1024) {  // a large text is parsed in pieces, as the compile path does

@@ -358,6 +358,7 @@ typedef struct gpc_tape_view {
   uint32_t num_ticks;         /* TICK instructions + 1 */
 } gpc_tape_view;
 
+/* The tape a compile lowers the circuit to. */
 gpc_status gpc_tape_lower(const char *stim_text, size_t len, int32_t correlation_level, gpc_tape **out);
 gpc_status gpc_tape_get_view(const gpc_tape *tape, gpc_tape_view *view);
 /* The epoch boundaries a single-circuit compile cuts its walk at, for a

@@ -199,7 +199,7 @@ def test_more_than_1024_qubits():
     """Two qubits per walk thread; the packed slot count need not split into whole warps."""
     # the first round count whose packed slot count leaves a partial warp (1,184 slots: 592 threads;
     # the packing follows the circuit's op sequences, so which round counts qualify can change)
-    text = next(c for c in (gp.SurfaceCode(23).get_memory(r, 1e-3, noise="uniform") for r in (3, 1, 2, 4, 8, 5, 6, 7))
+    text = next(c for c in (gp.SurfaceCode(23).get_memory(r, 1e-3, noise="uniform") for r in (8, 3, 1, 2, 4, 5, 6, 7))
                 if (gp.Tape(c).qpad // 2) % 32 != 0)
     t = gp.Tape(text)
     assert t.num_qubits > 1024 and (t.qpad // 2) % 32 != 0
