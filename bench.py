@@ -461,7 +461,8 @@ def serving_leg(gp, requests: int, cap_requests: int, slots: int, max_batch: int
     cap_reqs = materialise(mix.requests(cap_requests, 0.0))
     on_batch = None
     with Server(slots=slots, max_batch=max_batch, hbm_budget=120 << 30) as srv:
-        replay(srv, materialise(mix.requests(2 * slots * max_batch, 0.0)))  # warm every worker
+        # warm every worker and the page-locked pool its tapes and results come from (not timed)
+        replay(srv, materialise(mix.requests(8 * slots * max_batch, 0.0)))
         cap = replay(srv, cap_reqs)
         rate = 0.8 * cap["dems_per_s"]
         tr = replay(srv, materialise(mix.requests(requests, rate)))

@@ -53,7 +53,7 @@ class Options(ctypes.Structure):
                 ("walk_qpt", ctypes.c_int32), ("bucket_mean", ctypes.c_int32), ("walk_words", ctypes.c_int32),
                 ("key_split", ctypes.c_int32), ("walk_queue", ctypes.c_int32), ("walk_segment", ctypes.c_int32),
                 ("wait_limit_us", ctypes.c_int32), ("test_hold_tile", ctypes.c_int32),
-                ("test_fail_alloc", ctypes.c_int32)]
+                ("test_fail_alloc", ctypes.c_int32), ("heap_results", ctypes.c_int32)]
 
 
 class TuningEntry(ctypes.Structure):

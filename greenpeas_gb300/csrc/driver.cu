@@ -168,19 +168,65 @@ struct Layout {
 }  // namespace
 
 namespace {
-// Page-locked memory for the op arrays of the tapes a driver owns (null when
-// there is none: the tape then uses the heap and its ops are staged).  A
-// driver keeps its tapes (and their buffers) from one compile to the next,
-// since freeing page-locked memory is slow and may wait for the device.
-void *pinned_alloc(size_t bytes) {
-  void *p = nullptr;
-  if (cudaHostAlloc(&p, bytes, cudaHostAllocPortable) != cudaSuccess) {
-    cudaGetLastError();
-    return nullptr;
+// Page-locked host memory, recycled by size class.  Freeing page-locked
+// memory is slow and may wait for the device, so a freed buffer goes back to
+// the free list of its class (two classes per power of two, from 64 KiB) and
+// is handed out again.  At most kCapBytes are allocated; past that take()
+// returns null and the caller uses the heap (staged copies).  Never destroyed
+// (buffers may come back during process exit).
+class PinnedPool {
+ public:
+  static size_t class_of(size_t bytes) {
+    size_t c = (size_t)64 << 10;
+    while (c < bytes) {
+      const size_t mid = c + c / 2;  // between c and 2c
+      if (mid >= bytes) return mid;
+      c *= 2;
+    }
+    return c;
   }
-  return p;
+  void *take(size_t bytes) {
+    const size_t c = class_of(bytes);
+    {
+      std::lock_guard<std::mutex> lk(mu_);
+      auto &f = free_[c];
+      if (!f.empty()) {
+        void *p = f.back();
+        f.pop_back();
+        return p;
+      }
+      if (total_ + c > kCapBytes) return nullptr;
+      total_ += c;
+    }
+    void *p = nullptr;
+    if (cudaHostAlloc(&p, c, cudaHostAllocPortable) != cudaSuccess) {
+      cudaGetLastError();
+      std::lock_guard<std::mutex> lk(mu_);
+      total_ -= c;
+      return nullptr;
+    }
+    return p;
+  }
+  void give(void *p, size_t bytes) {
+    if (!p) return;
+    std::lock_guard<std::mutex> lk(mu_);
+    free_[class_of(bytes)].push_back(p);
+  }
+
+ private:
+  static constexpr size_t kCapBytes = (size_t)4 << 30;
+  std::mutex mu_;
+  std::unordered_map<size_t, std::vector<void *>> free_;
+  size_t total_ = 0;
+};
+PinnedPool &pinned_pool() {
+  static PinnedPool *p = new PinnedPool;
+  return *p;
 }
-void pinned_free(void *p) { cudaFreeHost(p); }
+
+// Tape ops in page-locked memory (the device copy is made straight from them).
+void *pinned_alloc(size_t bytes) { return pinned_pool().take(bytes); }
+void pinned_free(void *p, size_t bytes) { pinned_pool().give(p, bytes); }
 void pin_ops(Tape &T) { T.ops.set_allocator(pinned_alloc, pinned_free); }
 
 // A DEM's host array: heap memory, or pinned memory that the device copies a
@@ -199,11 +245,8 @@ class DemArray {
       release();
       const size_t want = pinned_ ? m + m / 4 : m;
       if (pinned_) {
-        void *q = nullptr;
-        if (cudaHostAlloc(&q, want * sizeof(T), cudaHostAllocDefault) != cudaSuccess) {
-          cudaGetLastError();
-          throw gpc::Error(GPC_ERR_CUDA, "pinned DEM array allocation failed");
-        }
+        void *q = pinned_pool().take(want * sizeof(T));
+        if (!q) throw gpc::Error(GPC_ERR_CUDA, "no page-locked memory for a DEM array");
         p_ = static_cast<T *>(q);
       } else {
         p_ = static_cast<T *>(::operator new(want * sizeof(T)));
@@ -235,7 +278,7 @@ class DemArray {
   void release() {
     if (p_ && !view_) {
       if (pinned_)
-        cudaFreeHost(p_);  // (fails harmlessly once the runtime has shut down at exit)
+        pinned_pool().give(p_, cap_ * sizeof(T));
       else
         ::operator delete(p_);
     }
@@ -251,77 +294,20 @@ class DemArray {
 
 // Page-locked memory that one batch's DEM arrays are copied back into.  The
 // batch's DEMs view their probabilities and targets in it and share it; the
-// last one freed returns it to the pool.  At most kMaxLive blocks exist, so
-// page-locked memory stays bounded: a caller holding more batches gets DEMs
-// that own copies of their arrays.  Single circuits use pinned DEMs instead.
+// last one freed gives it back to the page-locked pool.  When the pool has
+// none to give (a caller holding many results), the DEMs own heap copies.
+// Single circuits use pinned DEMs instead.
 struct ResultBlock {
   void *p = nullptr;
   size_t cap = 0;
-  ~ResultBlock() {
-    if (p) cudaFreeHost(p);
-  }
 };
-class BlockPool {
- public:
-  // A block of at least `bytes`, or null (none free and kMaxLive alive, or no page-locked memory).
-  std::shared_ptr<ResultBlock> take(size_t bytes) {
-    ResultBlock *b = nullptr;
-    {
-      // the smallest free block that holds `bytes`; else a new one; else the largest free
-      // block, grown (growing frees page-locked memory, which may wait for the device)
-      std::lock_guard<std::mutex> lk(mu_);
-      auto fit = free_.end(), big = free_.end();
-      for (auto it = free_.begin(); it != free_.end(); ++it) {
-        if ((*it)->cap >= bytes && (fit == free_.end() || (*it)->cap < (*fit)->cap)) fit = it;
-        if (big == free_.end() || (*it)->cap > (*big)->cap) big = it;
-      }
-      if (fit != free_.end()) {
-        b = *fit;
-        free_.erase(fit);
-      } else if (live_ < kMaxLive) {
-        b = new ResultBlock;
-        ++live_;
-      } else if (big != free_.end()) {
-        b = *big;
-        free_.erase(big);
-      } else {
-        return nullptr;
-      }
-    }
-    if (b->cap < bytes) {  // grow, with slack (page-locked allocations are slow)
-      if (b->p) cudaFreeHost(b->p);
-      b->p = nullptr;
-      b->cap = 0;
-      const size_t want = bytes + bytes / 4;
-      if (cudaHostAlloc(&b->p, want, cudaHostAllocPortable) != cudaSuccess) {
-        cudaGetLastError();
-        b->p = nullptr;
-        drop(b);
-        return nullptr;
-      }
-      b->cap = want;
-    }
-    return std::shared_ptr<ResultBlock>(b, [this](ResultBlock *x) { give(x); });
-  }
-
- private:
-  void give(ResultBlock *b) {
-    std::lock_guard<std::mutex> lk(mu_);
-    free_.push_back(b);
-  }
-  void drop(ResultBlock *b) {
+std::shared_ptr<ResultBlock> take_block(size_t bytes) {
+  void *p = pinned_pool().take(bytes);
+  if (!p) return nullptr;
+  return std::shared_ptr<ResultBlock>(new ResultBlock{p, bytes}, [](ResultBlock *b) {
+    pinned_pool().give(b->p, b->cap);
     delete b;
-    std::lock_guard<std::mutex> lk(mu_);
-    --live_;
-  }
-  static constexpr size_t kMaxLive = 8;  // two batches of four chunks alive
-  std::mutex mu_;
-  std::vector<ResultBlock *> free_;
-  size_t live_ = 0;
-};
-BlockPool &block_pool() {
-  static BlockPool *p = new BlockPool;  // never destroyed (blocks may be freed during process exit)
-  return *p;
+  });
 }
 }  // namespace
 
@@ -1818,8 +1804,7 @@ struct gpc_driver {
   };
   cudaEvent_t fetch_ev = nullptr;  // the last begin_fetch's copies
   // Results copied into page-locked memory that the DEMs keep (pinned DEMs,
-  // batch result blocks).  Off for the serving workers, whose callers hold
-  // DEMs for as long as they like: their DEMs own heap copies.
+  // batch result blocks), as far as the page-locked pool reaches.
   bool pinned_results = true;
 
   // Waits for the pipeline and issues the copies of its result on the driver's
@@ -1878,7 +1863,7 @@ struct gpc_driver {
     const size_t bytes = (size_t)C * 8 + (size_t)C * 4 + (size_t)NT * 4 + (size_t)N * 8 + 64;
     // into a result block that the DEMs keep (they view their probabilities and targets in
     // it), else into the staging buffer, split into DEMs that own copies
-    if (N > 1 && pinned_results) pf.blk = block_pool().take(bytes);
+    if (N > 1 && pinned_results) pf.blk = take_block(bytes);
     char *h;
     if (pf.blk) {
       h = static_cast<char *>(pf.blk->p);
@@ -2101,6 +2086,7 @@ struct gpc_driver {
       d->batch_queue = batch_queue;
       d->walk_queue = walk_queue;
       d->walk_segment = walk_segment;
+      d->pinned_results = pinned_results;
       d->spin_ns = spin_ns;
       d->init_streams();
       partner = std::move(d);
@@ -2242,6 +2228,7 @@ struct gpc_server {
   std::unordered_map<uint64_t, std::unique_ptr<Req>> reqs;
   std::vector<std::unique_ptr<gpc_driver>> drivers;
   std::vector<size_t> held;  // budget bytes held by each worker's buffers
+  size_t max_ahead() const { return (size_t)2 * drivers.size() * max_batch; }  // lowered, waiting for a worker
   std::vector<std::thread> workers;
 
   // Admits `grow` more bytes for worker w (whose buffers will total `total`).
@@ -2304,8 +2291,10 @@ struct gpc_server {
       const char *text;
       size_t len;
       {
+        // back-pressure: at most two rounds of full batches lowered ahead of the workers (bounded
+        // host memory; their tapes stay within the page-locked pool)
         std::unique_lock<std::mutex> lk(mu);
-        cv_lower.wait(lk, [&] { return stop || !lower_queue.empty(); });
+        cv_lower.wait(lk, [&] { return stop || (!lower_queue.empty() && queue.size() < max_ahead()); });
         if (stop) return;
         t = lower_queue.front();
         lower_queue.pop_front();
@@ -2321,6 +2310,7 @@ struct gpc_server {
             spare.pop_back();
           }
         }
+        pin_ops(*tape);
         gpc::lower_text(text, len, lo, *tape, scratch);
         {
           std::lock_guard<std::mutex> lk(mu);
@@ -2391,6 +2381,7 @@ struct gpc_server {
           queue.pop_front();
         }
       }
+      cv_lower.notify_all();  // room below the back-pressure bound
       auto run_one_by_one = [&](const std::vector<uint64_t> &list) {
         for (uint64_t t : list) {
           try {
@@ -2478,6 +2469,8 @@ gpc_status gpc_get_driver(const char *stim_text, size_t len, int32_t correlation
     d->hold_runs = (uint32_t)options->test_hold_tile;
     if (options->test_fail_alloc < 0) return fail(GPC_ERR_INVALID, "test_fail_alloc must be >= 0");
     if (options->test_fail_alloc) d->alloc_ctr.fail_at = options->test_fail_alloc - 1;
+    if (options->heap_results != 0 && options->heap_results != 1) return fail(GPC_ERR_INVALID, "heap_results must be 0 or 1");
+    d->pinned_results = options->heap_results == 0;
   }
   gpc_status st = guarded([&] {
     int n = 0;
@@ -2692,9 +2685,6 @@ gpc_status gpc_server_create(const gpc_server_options *options, gpc_server **out
       d->pool_threads = std::max(1u, hw / o.slots);
       d->pool_spin_us = 0;  // the lowering threads need the cores between a worker's hand-offs
       d->blocking_wait = true;  // and while the GPU runs the worker's batch
-      // requests of every size pass through a worker, held by callers for as long as they
-      // like: heap tapes (staged) and heap DEMs, no page-locked memory regrown on the way
-      d->pinned_results = false;
       d->init_streams();
       d->admit = [raw, w](size_t grow, size_t total) { raw->acquire(w, grow, total); };
       sv->drivers.push_back(std::move(d));

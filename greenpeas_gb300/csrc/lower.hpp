@@ -141,7 +141,7 @@ void parse_stim_into(const char *text, size_t len, Parsed &out);
 class OpArray {
  public:
   using AllocFn = void *(*)(size_t bytes);
-  using FreeFn = void (*)(void *);
+  using FreeFn = void (*)(void *, size_t bytes);  // bytes: as allocated
   OpArray() = default;
   OpArray(OpArray &&o) noexcept { take(o); }
   OpArray &operator=(OpArray &&o) noexcept {
@@ -187,7 +187,7 @@ class OpArray {
   void release() {
     if (p_) {
       if (ext_)
-        free_(p_);
+        free_(p_, cap_ * sizeof(uint64_t));
       else
         std::free(p_);
     }

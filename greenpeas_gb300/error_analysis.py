@@ -142,7 +142,7 @@ class Driver:
                  device: int = 0, sort_bits: int = 0, global_sort: bool = False, walk_qpt: int = 0,
                  bucket_mean: int = 0, walk_words: int = 0, key_split: int = 0, walk_queue: int = 0,
                  walk_segment: int = 0, wait_limit_us: int = 0, test_hold_tile: int = 0,
-                 test_fail_alloc: int = 0):
+                 test_fail_alloc: int = 0, heap_results: bool = False):
         L = _native.lib()
         self._h = ctypes.c_void_p()
         self.correlation_level = CorrelationLevel(correlation_level)
@@ -160,6 +160,7 @@ class Driver:
         opts.wait_limit_us = wait_limit_us
         opts.test_hold_tile = test_hold_tile
         opts.test_fail_alloc = test_fail_alloc
+        opts.heap_results = 1 if heap_results else 0
         text = _text(circuit)
         _native.check(L.gpc_get_driver(text, len(text), int(self.correlation_level), ctypes.byref(opts),
                                        ctypes.byref(self._h)))

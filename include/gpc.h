@@ -77,6 +77,9 @@ typedef struct gpc_options {
                              (0 = never) */
   int32_t test_fail_alloc; /* tests of the allocation failure path: the driver's k-th device allocation
                               (counting from its creation) fails once with GPC_ERR_OOM (0 = never) */
+  int32_t heap_results;    /* 1: DEM arrays are heap copies out of a staging buffer; 0: the device copies
+                              them into page-locked memory the DEM keeps (a single circuit's own arrays, a
+                              batch's shared result block), while a 4 GiB page-locked pool reaches */
 } gpc_options;
 
 /* Parses `stim_text` (length `len`), sizes device buffers for it and returns

@@ -134,12 +134,14 @@ def test_persistent_walk_with_the_largest_batch_circuit():
     assert [a == b for a, b in zip(out, ref)] == [True] * len(circs)
 
 
-def test_held_batches_keep_their_dems():
-    """A batch's DEMs view their arrays in a shared page-locked result block (at most eight blocks
-    exist); a caller holding more batches gets DEMs that own copies.  Every held DEM stays equal to
-    its circuit's own compile while later batches are compiled and earlier ones freed."""
+@pytest.mark.parametrize("heap_results", [False, True])
+def test_held_batches_keep_their_dems(heap_results):
+    """A batch's DEMs view their arrays in a shared page-locked result block, which goes back to the
+    page-locked pool when the last of them is freed (heap_results: the DEMs own heap copies
+    instead).  Every held DEM stays equal to its circuit's own compile while later batches are
+    compiled and earlier ones freed."""
     circs = _mixed()
-    drv = gp.get_driver(circs[0])
+    drv = gp.get_driver(circs[0], heap_results=heap_results)
     single = [gp.get_driver(t).compile(t) for t in circs]
     held = [drv.compile_batch(circs[k % 3:] + circs[:k % 3]) for k in range(10)]
     for k, out in enumerate(held):

@@ -132,12 +132,13 @@ def test_long_symptoms(n):
         _check(dem, t)
 
 
-def test_many_live_dems():
+@pytest.mark.parametrize("heap_results", [False, True])
+def test_many_live_dems(heap_results):
     """A single compile copies its result straight into a pinned DEM while at most four of those
-    are alive; a caller holding more gets DEMs filled through the staging buffer.  Every DEM stays
-    intact while others are made and freed."""
+    are alive; a caller holding more (or a driver with heap_results) gets DEMs filled through the
+    staging buffer.  Every DEM stays intact while others are made and freed."""
     texts = [gp.BBCode(6).get_memory(6, 1e-3, noise="uniform"), gp.SurfaceCode(5).get_memory(5, 1e-3, noise="uniform")]
-    drv = gp.get_driver(texts[0])
+    drv = gp.get_driver(texts[0], heap_results=heap_results)
     refs = [drv.compile(t).canonical() for t in texts]
     held = [drv.compile(texts[i % 2]) for i in range(9)]
     for i, dem in enumerate(held):
