@@ -49,7 +49,7 @@ KERNELS_PER_RUN = 7
 # (profiles/headline_bb12_kernels.txt) and the two launches of the segmented walk
 # (profiles/headline_bb12_segmented_walk.txt).
 WALK_DRAM_BYTES_PLAIN = 1_245_440
-WALK_DRAM_BYTES_PER_RUN = 1_144_576 + 2_091_776
+WALK_DRAM_BYTES_PER_RUN = 1_147_904 + 1_919_488
 
 
 def workload_text() -> str:
