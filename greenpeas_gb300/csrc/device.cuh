@@ -76,7 +76,8 @@ constexpr int BUCKET_THREADS = 128;
 constexpr int BUCKET_CAP = 1024;  // items one CTA sorts in shared memory (allocation-free merge)
 constexpr uint32_t SLOT_CAP = 256;  // slots of one bucket in the compile pipeline
 constexpr uint32_t WARP_CAP = 128;  // bucket items one warp merges; larger buckets take a CTA
-constexpr uint32_t SCAN_TILE = 4096;  // bucket aggregates one scan block covers
+constexpr uint32_t SCAN_TILE = 1024;    // bucket aggregates one scan block covers
+constexpr uint32_t SCAN_THREADS = 256;  // threads of a scan block (4 aggregates each)
 
 inline uint32_t sort_tiles(uint32_t n) { return (n + SORT_TILE - 1) / SORT_TILE; }
 inline uint32_t merge_tiles(uint32_t n) { return (n + MERGE_THREADS - 1) / MERGE_THREADS; }

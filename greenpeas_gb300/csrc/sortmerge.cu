@@ -1195,26 +1195,42 @@ __device__ __forceinline__ uint2 block_sum1024(uint2 v, uint2 *scratch) {
 
 // Exclusive scan of the bucket aggregates: block t covers buckets
 // [t * SCAN_TILE, (t + 1) * SCAN_TILE) and starts from the sum of the tile
-// sums before it.  The last block writes the totals.
-__global__ void __launch_bounds__(1024) group_scan_kernel(GroupLaunch L) {
-  __shared__ uint2 red[32];
-  __shared__ uint2 wsum[32];
+// sums before it.  The aggregates go through shared memory both ways, so the
+// block's global loads and stores are coalesced while each thread scans
+// SCAN_TILE / SCAN_THREADS consecutive ones.  The last block writes the totals.
+__global__ void __launch_bounds__(SCAN_THREADS) group_scan_kernel(GroupLaunch L) {
+  constexpr uint32_t PER = SCAN_TILE / SCAN_THREADS, NW = SCAN_THREADS / 32;
+  __shared__ uint2 stage[SCAN_TILE];
+  __shared__ uint2 red[NW], wsum[NW];
   const uint32_t t = threadIdx.x, lane = t & 31u, warp = t >> 5;
   const uint32_t tile = blockIdx.x;
+  const size_t b0 = (size_t)tile * SCAN_TILE;
+#pragma unroll
+  for (uint32_t k = 0; k < PER; ++k) {
+    const size_t i = b0 + (size_t)k * SCAN_THREADS + t;
+    stage[k * SCAN_THREADS + t] = i < L.nb ? L.bagg[i] : make_uint2(0, 0);
+  }
   uint2 pre = make_uint2(0, 0);
-  for (uint32_t k = t; k < tile; k += 1024) {
+  for (uint32_t k = t; k < tile; k += SCAN_THREADS) {
     const uint2 a = L.tsum[k];
     pre.x += a.x;
     pre.y += a.y;
   }
-  pre = block_sum1024(pre, red);
-  constexpr uint32_t PER = SCAN_TILE / 1024;
-  const uint32_t i0 = tile * SCAN_TILE + t * PER;
+  pre.x = __reduce_add_sync(0xFFFFFFFFu, pre.x);
+  pre.y = __reduce_add_sync(0xFFFFFFFFu, pre.y);
+  if (lane == 0) red[warp] = pre;
+  __syncthreads();  // (also: the staged aggregates are visible)
+  pre = make_uint2(0, 0);
+#pragma unroll
+  for (uint32_t w = 0; w < NW; ++w) {
+    pre.x += red[w].x;
+    pre.y += red[w].y;
+  }
   uint2 v[PER];
   uint2 loc = make_uint2(0, 0);
 #pragma unroll
   for (uint32_t k = 0; k < PER; ++k) {
-    v[k] = i0 + k < L.nb ? L.bagg[i0 + k] : make_uint2(0, 0);
+    v[k] = stage[t * PER + k];
     loc.x += v[k].x;
     loc.y += v[k].y;
   }
@@ -1230,31 +1246,24 @@ __global__ void __launch_bounds__(1024) group_scan_kernel(GroupLaunch L) {
   }
   if (lane == 31) wsum[warp] = inc;
   __syncthreads();
-  if (warp == 0) {
-    uint2 x = wsum[lane];
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const uint32_t ax = __shfl_up_sync(0xFFFFFFFFu, x.x, o), ay = __shfl_up_sync(0xFFFFFFFFu, x.y, o);
-      if (lane >= (uint32_t)o) {
-        x.x += ax;
-        x.y += ay;
-      }
-    }
-    wsum[lane] = x;  // inclusive prefix over warps
-  }
-  __syncthreads();
   uint2 run = make_uint2(pre.x + inc.x - loc.x, pre.y + inc.y - loc.y);
-  if (warp > 0) {
-    run.x += wsum[warp - 1].x;
-    run.y += wsum[warp - 1].y;
+  for (uint32_t w = 0; w < warp; ++w) {
+    run.x += wsum[w].x;
+    run.y += wsum[w].y;
   }
 #pragma unroll
   for (uint32_t k = 0; k < PER; ++k) {
-    if (i0 + k < L.nb) L.bout[i0 + k] = run;
+    stage[t * PER + k] = run;  // (each thread rewrites only the entries it read)
     run.x += v[k].x;
     run.y += v[k].y;
   }
-  if (tile == gridDim.x - 1 && t == 1023) {
+  __syncthreads();
+#pragma unroll
+  for (uint32_t k = 0; k < PER; ++k) {
+    const size_t i = b0 + (size_t)k * SCAN_THREADS + t;
+    if (i < L.nb) L.bout[i] = stage[k * SCAN_THREADS + t];
+  }
+  if (tile == gridDim.x - 1 && t == SCAN_THREADS - 1) {
     L.totals[0] = run.x;
     L.totals[1] = run.y;
     if (run.y > L.tg_cap) atomicOr(L.err, DEV_FLAG_TG_OVF);
@@ -1269,19 +1278,27 @@ __global__ void __launch_bounds__(GW_WARPS * 32) emit_kernel(GroupLaunch L) {
   const uint32_t lane = threadIdx.x & 31u;
   const uint32_t b = blockIdx.x * GW_WARPS + (threadIdx.x >> 5);
   if (b >= L.nb) return;
-  const uint2 agg = L.bagg[b], out = L.bout[b];
   const size_t base = (size_t)b * SLOT_CAP;
+  // the first records load beside the bucket's aggregate and offset (a slot
+  // past the groups holds whatever it held: only the ones below agg.x are used)
+  SlotTail t = L.slot[base + lane].tail, tn1 = L.slot[base + lane + 1].tail;
+  const uint2 agg = L.bagg[b], out = L.bout[b];
   const uint32_t tcap = L.tcap;
   for (uint32_t g = lane; g < agg.x; g += 32) {
+    if (g != lane) {
+      t = L.slot[base + g].tail;
+      if (g + 1 < agg.x) tn1 = L.slot[base + g + 1].tail;  // (slot g + 1 <= SLOT_CAP - 1)
+    }
     const uint32_t slot = out.x + g;
-    const SlotTail t = L.slot[base + g].tail;
     const uint32_t toff = out.y + t.t;
     const uint32_t m = t.m;
     L.out_prob[slot] = t.p;
     L.out_off[slot] = toff;
-    // (a list longer than the stride was flagged by the key pass; the run is
-    // redone with wider lists, so only the stride's targets are copied here)
-    const uint32_t ntg = min(__ldg(L.tn + m), tcap);
+    // the group's targets run to the next group's (the bucket's total after
+    // the last); a list longer than the stride was flagged by the key pass
+    // and the run is redone with wider lists, so only the stride's targets
+    // are copied here
+    const uint32_t ntg = min((g + 1 < agg.x ? tn1.t : agg.y) - t.t, tcap);
     if ((uint64_t)toff + ntg <= L.tg_cap) {
       const uint4 *src = reinterpret_cast<const uint4 *>(L.tl + (size_t)m * tcap);
       for (uint32_t k = 0; k * 4 < ntg; ++k) {
@@ -1435,7 +1452,7 @@ cudaError_t launch_group(const GroupLaunch &L, cudaStream_t s) {
 
 cudaError_t launch_scan_emit(const GroupLaunch &L, cudaStream_t s) {
   if (L.nb == 0) return cudaSuccess;
-  group_scan_kernel<<<(L.nb + SCAN_TILE - 1) / SCAN_TILE, 1024, 0, s>>>(L);
+  group_scan_kernel<<<(L.nb + SCAN_TILE - 1) / SCAN_TILE, SCAN_THREADS, 0, s>>>(L);
   emit_kernel<<<(L.nb + GW_WARPS - 1) / GW_WARPS, GW_WARPS * 32, 0, s>>>(L);
   return cudaGetLastError();
 }
