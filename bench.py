@@ -311,10 +311,12 @@ def batched_leg(gp, torch, local: int, flush, steps: int, warmup: int, circuits:
     torch.cuda.synchronize()
     batch_ms = [a.elapsed_time(b) for a, b in ev]
     # stage times and algorithmic bytes of one batched run of the whole batch (L2 flushed first)
+    bdrv.set_stage_timing(True)  # (events between the stages: in this run only)
     with torch.cuda.stream(bext):
         flush.fill_(0.5)
     bdrv.run_device()
     st = bdrv.last_timings()
+    bdrv.set_stage_timing(False)
     tr = bdrv.last_traffic()
     outs = bdrv.fetch_batch()
     ok = len(outs) == n and all(dem_arrays_equal(a, b) for a, b in zip(outs, singles))
@@ -379,15 +381,20 @@ def plain_leg(gp, torch, local: int, flush, text: str, steps: int, warmup: int, 
             ev[i][1].record(ext)
     torch.cuda.synchronize()
     step_ms = [a.elapsed_time(b) for a, b in ev]
+    # per-stage times: events between the stages, in runs of their own (the timed runs above
+    # have none: an event node between two kernels of the captured graph costs microseconds)
     stage = {"walk": 0.0, "key": 0.0, "sort": 0.0, "merge": 0.0, "total": 0.0}
     nstage = min(20, steps)
-    for i in range(nstage):  # per-stage times (events inside the pipeline)
+    drv.set_stage_timing(True)
+    drv.run_device()
+    for i in range(nstage):
         with torch.cuda.stream(ext):
             flush.fill_(float(i))
         drv.run_device()
         t = drv.last_timings()
         for k in stage:
             stage[k] += t[k] / nstage
+    drv.set_stage_timing(False)
     dem_dev = drv.fetch()
     traffic = drv.last_traffic()
     for _ in range(warmup):

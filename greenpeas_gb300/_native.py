@@ -23,7 +23,7 @@ STATUS_NAMES = {
 EXPORTS = [
     "gpc_get_driver", "gpc_compile", "gpc_compile_batch", "gpc_dem_arrays", "gpc_dem_info",
     "gpc_dem_text", "gpc_dem_free", "gpc_driver_destroy", "gpc_last_error", "gpc_prepare",
-    "gpc_run_device", "gpc_fetch", "gpc_driver_stream", "gpc_last_timings", "gpc_last_sizes",
+    "gpc_run_device", "gpc_fetch", "gpc_driver_stream", "gpc_last_timings", "gpc_set_stage_timing", "gpc_last_sizes",
     "gpc_tape_lower", "gpc_tape_get_view", "gpc_tape_free", "gpc_tape_last_error", "gpc_tape_walk_segments",
     "gpc_last_traffic",
     "gpc_last_io_bytes", "gpc_merge_mechanisms_static", "gpc_prepare_batch", "gpc_fetch_batch",
@@ -114,6 +114,7 @@ def lib() -> ctypes.CDLL:
     L.gpc_driver_stream.argtypes = [vp]
     L.gpc_driver_stream.restype = vp
     L.gpc_last_timings.argtypes = [vp, ctypes.POINTER(ctypes.c_float)]
+    L.gpc_set_stage_timing.argtypes = [vp, i32]
     L.gpc_last_host_timings.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
     L.gpc_walk_form.argtypes = [vp, ctypes.POINTER(i32), ctypes.POINTER(i32)]
     L.gpc_last_sizes.argtypes = [vp, u64p, u64p, u32p, u32p, u32p]
@@ -148,7 +149,7 @@ def lib() -> ctypes.CDLL:
     for f in ("gpc_param_prepare", "gpc_param_forward", "gpc_param_probs", "gpc_param_backward",
               "gpc_server_create", "gpc_server_submit", "gpc_server_wait", "gpc_server_stats", "gpc_device_dem",
               "gpc_get_driver", "gpc_compile", "gpc_compile_batch", "gpc_dem_arrays", "gpc_dem_info",
-              "gpc_dem_text", "gpc_prepare", "gpc_run_device", "gpc_fetch", "gpc_last_timings",
+              "gpc_dem_text", "gpc_prepare", "gpc_run_device", "gpc_fetch", "gpc_last_timings", "gpc_set_stage_timing",
               "gpc_last_sizes", "gpc_tape_lower", "gpc_tape_get_view", "gpc_last_traffic", "gpc_last_io_bytes",
               "gpc_merge_mechanisms_static", "gpc_prepare_batch", "gpc_fetch_batch", "gpc_last_host_timings", "gpc_walk_form",
               "gpc_tape_walk_segments", "gpc_walk_segments", "gpc_fallback_counts",

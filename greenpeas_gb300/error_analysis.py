@@ -296,7 +296,13 @@ class Driver:
         _native.check(_native.lib().gpc_fetch(self._h, ctypes.byref(out)))
         return dem_from_handle(out)
 
+    def set_stage_timing(self, on: bool = True) -> None:
+        """Records CUDA events between the pipeline's stages from the next run on (off by default:
+        the event nodes of a captured graph cost a few microseconds each)."""
+        _native.check(_native.lib().gpc_set_stage_timing(self._h, 1 if on else 0))
+
     def last_timings(self) -> dict:
+        """Stage times (ms) of the last run; stage timing must have been on for it."""
         ms = (ctypes.c_float * 5)()
         _native.check(_native.lib().gpc_last_timings(self._h, ms))
         return dict(zip(("walk", "key", "sort", "merge", "total"), [float(x) for x in ms]))

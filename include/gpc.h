@@ -244,8 +244,15 @@ void gpc_server_destroy(gpc_server *server);
 /* The driver's CUDA stream (a cudaStream_t), for callers that time it. */
 void *gpc_driver_stream(gpc_driver *driver);
 
+/* Stage timing (no counterpart in the reference): with `on` != 0 the
+ * pipeline records CUDA events between its stages on the driver's stream
+ * (off by default: in a captured graph each event node between two kernels
+ * adds a few microseconds to the run). */
+gpc_status gpc_set_stage_timing(gpc_driver *driver, int32_t on);
+
 /* Kernel timing of the last gpc_run_device, in milliseconds (CUDA events on
- * the driver's stream): [0] walk, [1] key, [2] sort, [3] merge, [4] total. */
+ * the driver's stream): [0] walk, [1] key, [2] sort, [3] merge, [4] total.
+ * GPC_ERR_INVALID unless stage timing was on for that run. */
 gpc_status gpc_last_timings(gpc_driver *driver, float *ms5);
 
 /* Host wall-clock phases of the driver's last prepare and fetch, in

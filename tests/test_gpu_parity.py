@@ -106,14 +106,25 @@ def test_empty_and_noiseless():
 
 
 def test_device_stages_and_timings():
+    """Stage times need stage timing on for the run (its events live in another captured graph);
+    the DEM does not depend on it."""
     text = gp.BBCode(6).get_memory(6, 1e-3, noise="uniform")
     drv = gp.get_driver(text)
     drv.prepare(text)
     drv.run_device()
+    with pytest.raises(gp.GpcError):
+        drv.last_timings()
+    drv.set_stage_timing(True)
+    for _ in range(3):  # the third run replays the captured graph with the events
+        drv.run_device()
+        t = drv.last_timings()
+        assert t["total"] > 0 and all(v >= 0 for v in t.values())
     dem = drv.fetch()
-    t = drv.last_timings()
-    assert t["total"] > 0 and all(v >= 0 for v in t.values())
     _check(dem, text)
+    drv.set_stage_timing(False)
+    for _ in range(3):
+        drv.run_device()
+    assert drv.fetch() == dem
 
 
 @pytest.mark.parametrize("n", [80, 300])
