@@ -560,6 +560,41 @@ def grad_leg(gp, torch, reps: int = 20, fd_entries: int = 16) -> dict:
             "fd_max_rel_err": worst, "dtype": "f64"}
 
 
+def global_sort_leg(gp, torch, local: int, flush, args) -> dict:
+    """One circuit compiled on the global merge path (every mechanism's key through the onesweep
+    radix sort, merged from the snapshots: the path a bucket overflow or a symptom over 256
+    targets takes), device-resident runs timed by CUDA events, L2 flushed before each."""
+    make = {"bb18": lambda: gp.BBCode(18).get_memory(18, 1e-3, noise="uniform"),
+            "s21": lambda: gp.SurfaceCode(21).get_memory(21, 1e-3, noise="uniform"),
+            "s25": lambda: gp.SurfaceCode(25).get_memory(25, 1e-3, noise="uniform")}[args.global_sort]
+    text = make()
+    drv = gp.get_driver(text, device=local, global_sort=True)
+    ref = drv.compile(text)
+    ext = torch.cuda.ExternalStream(drv.stream, device=torch.device("cuda", local))
+    drv.prepare(text)
+    for _ in range(max(1, args.warmup)):
+        drv.run_device()
+    torch.cuda.synchronize()
+    ms = []
+    for i in range(max(1, args.steps)):
+        with torch.cuda.stream(ext):
+            flush.fill_(float(i))
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(ext)
+            drv.run_device()
+            e1.record(ext)
+        torch.cuda.synchronize()
+        ms.append(e0.elapsed_time(e1))
+    drv.set_stage_timing(True)
+    drv.run_device()
+    st = drv.last_timings()
+    if drv.fetch() != ref:
+        raise SystemExit("bench: global-path runs changed the DEM")
+    sizes = drv.last_sizes()
+    return {"circuit": args.global_sort, "raw_mechanisms": sizes["raw"], "merged": ref.num_errors,
+            "ms_median": sorted(ms)[len(ms) // 2], "stage_ms": st}
+
+
 def main() -> None:
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -573,6 +608,8 @@ def main() -> None:
     ap.add_argument("--batch-circuits", type=int, default=256)
     ap.add_argument("--walk-queue", type=int, default=0, choices=(-1, 0, 1),
                     help="batch leg with --batch-device-only: 1 one persistent walk launch, -1 per-class launches")
+    ap.add_argument("--global-sort", choices=("bb18", "s21", "s25"), default=None,
+                    help="profiling: one circuit on the global (onesweep sort) merge path, timed alone")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
     ap.add_argument("--no-grad", action="store_true", help="skip the noise-rate gradient leg")
     ap.add_argument("--no-sweep", action="store_true", help="skip the plain-method configuration sweep")
@@ -599,6 +636,10 @@ def main() -> None:
     import greenpeas_gb300 as gp
 
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=f"cuda:{local}")
+    if args.global_sort:  # profiling runs: the global merge path (sort kernels) on one circuit
+        if rank == 0:
+            print(json.dumps({"profiling": True, "global_sort": global_sort_leg(gp, torch, local, flush, args)}), flush=True)
+        return
     if args.no_plain:  # profiling runs: the batch leg alone
         out = {"profiling": True}
         if not args.no_batch:

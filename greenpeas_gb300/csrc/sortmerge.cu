@@ -509,6 +509,18 @@ __device__ __forceinline__ unsigned long long ms_pack(uint32_t cnt, uint32_t tg)
   return ((unsigned long long)(cnt & 0x3FFFFFFFu) << 32) | tg;
 }
 
+// Mask word i of the words where mechanism d's symptom can be non-zero: the
+// union of its points' non-zero masks (a word whose mask bit is clear has a
+// zero snapshot at that point, so it adds nothing to the symptom).
+__device__ __forceinline__ uint64_t symptom_mask(const CircuitDev &C, uint64_t d, uint32_t i) {
+  const uint32_t pa = (uint32_t)(d & 0x3FFFFFFFu), Pa = (uint32_t)((d >> 30) & 3u);
+  const uint32_t pb = (uint32_t)((d >> 32) & 0x3FFFFFFFu), Pb = (uint32_t)(d >> 62);
+  uint64_t b = 0;
+  if (Pa) b |= __ldg(C.nzm + (size_t)pa * C.mw + i);
+  if (Pb) b |= __ldg(C.nzm + (size_t)pb * C.mw + i);
+  return b;
+}
+
 __global__ void __launch_bounds__(MERGE_THREADS) merge_kernel(MergeLaunch L) {
   const CircuitDev C = *L.c_dev;
   extern __shared__ uint2 sband[];  // [w]
@@ -543,27 +555,33 @@ __global__ void __launch_bounds__(MERGE_THREADS) merge_kernel(MergeLaunch L) {
       if (kp.x == k.x && kp.y == k.y) {
         newgroup = false;
         const uint64_t dp = __ldg(C.mdesc + mp);
-        for (uint32_t j = 0; j < w; ++j) {
-          if (symptom_word(C, d, j, sband[j]) != symptom_word(C, dp, j, sband[j])) {
-            atomicOr(L.err, DEV_ERR_COLLISION);
-            break;
+        // the full symptoms, compared on the words either can be non-zero in
+        bool diff = false;
+        for (uint32_t mi = 0; mi < C.mw && !diff; ++mi)
+          for (uint64_t bits = symptom_mask(C, d, mi) | symptom_mask(C, dp, mi); bits && !diff; bits &= bits - 1) {
+            const uint32_t j = mi * 64u + (uint32_t)(__ffsll((long long)bits) - 1);
+            diff = j < w && symptom_word(C, d, j, sband[j]) != symptom_word(C, dp, j, sband[j]);
           }
-        }
+        if (diff) atomicOr(L.err, DEV_ERR_COLLISION);
       } else if (((L.sortkey[i] ^ L.sortkey[i - 1]) & L.sort_mask) == 0 && L.sort_mask) {
         atomicOr(L.err, DEV_FLAG_MIXED);
       }
     }
     const bool empty = (k.x | k.y) == 0;
-    if (newgroup && empty) {
-      for (uint32_t j = 0; j < w; ++j)
-        if (symptom_word(C, d, j, sband[j])) {
-          atomicOr(L.err, DEV_ERR_COLLISION);
-          break;
+    if (newgroup) {
+      // a non-empty symptom hashed to zero is a collision; a head counts its targets
+      bool nonzero = false;
+      for (uint32_t mi = 0; mi < C.mw; ++mi)
+        for (uint64_t bits = symptom_mask(C, d, mi); bits; bits &= bits - 1) {
+          const uint32_t j = mi * 64u + (uint32_t)(__ffsll((long long)bits) - 1);
+          const uint32_t c = j < w ? __popcll(symptom_word(C, d, j, sband[j])) : 0u;
+          nonzero |= c != 0;
+          ntg += c;
         }
+      if (empty && nonzero) atomicOr(L.err, DEV_ERR_COLLISION);
     }
     head = newgroup && !empty;
-    if (head)
-      for (uint32_t j = 0; j < w; ++j) ntg += __popcll(symptom_word(C, d, j, sband[j]));
+    if (!head) ntg = 0;
   }
   // block-wide exclusive scan of (head, ntg)
   const uint32_t lane = threadIdx.x & 31u, warp = threadIdx.x >> 5;
@@ -647,13 +665,15 @@ __global__ void __launch_bounds__(MERGE_THREADS) merge_kernel(MergeLaunch L) {
   if ((uint64_t)toff + ntg <= L.tg_cap) {
     const uint64_t d = __ldg(C.mdesc + m);
     uint32_t o = toff;
-    for (uint32_t j = 0; j < w; ++j) {
-      uint64_t v = symptom_word(C, d, j, sband[j]);
-      while (v) {
-        L.out_tg[o++] = j * 64u + (uint32_t)(__ffsll((long long)v) - 1);
-        v &= v - 1;
+    for (uint32_t mi = 0; mi < C.mw; ++mi)  // the masked words, ascending: the targets stay ascending
+      for (uint64_t bits = symptom_mask(C, d, mi); bits; bits &= bits - 1) {
+        const uint32_t j = mi * 64u + (uint32_t)(__ffsll((long long)bits) - 1);
+        uint64_t v = j < w ? symptom_word(C, d, j, sband[j]) : 0ull;
+        while (v) {
+          L.out_tg[o++] = j * 64u + (uint32_t)(__ffsll((long long)v) - 1);
+          v &= v - 1;
+        }
       }
-    }
   }
 }
 
