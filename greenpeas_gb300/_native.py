@@ -30,6 +30,7 @@ EXPORTS = [
     "gpc_param_prepare", "gpc_param_forward", "gpc_param_probs", "gpc_param_backward",
     "gpc_server_create", "gpc_server_submit", "gpc_server_wait", "gpc_server_stats", "gpc_server_destroy",
     "gpc_device_dem", "gpc_autotune", "gpc_last_host_timings", "gpc_walk_form", "gpc_walk_segments",
+    "gpc_walk_config", "gpc_tune_cache_clear",
     "gpc_fallback_counts", "gpc_server_fallback_counts", "gpc_alloc_counts",
 ]
 
@@ -117,6 +118,9 @@ def lib() -> ctypes.CDLL:
     L.gpc_set_stage_timing.argtypes = [vp, i32]
     L.gpc_last_host_timings.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
     L.gpc_walk_form.argtypes = [vp, ctypes.POINTER(i32), ctypes.POINTER(i32)]
+    L.gpc_walk_config.argtypes = [vp, ctypes.POINTER(i32), ctypes.POINTER(i32), ctypes.POINTER(i32)]
+    L.gpc_tune_cache_clear.argtypes = []
+    L.gpc_tune_cache_clear.restype = None
     L.gpc_last_sizes.argtypes = [vp, u64p, u64p, u32p, u32p, u32p]
     L.gpc_last_traffic.argtypes = [vp, ctypes.POINTER(ctypes.c_double)]
     L.gpc_last_io_bytes.argtypes = [vp, u64p, u64p]
@@ -152,7 +156,7 @@ def lib() -> ctypes.CDLL:
               "gpc_dem_text", "gpc_prepare", "gpc_run_device", "gpc_fetch", "gpc_last_timings", "gpc_set_stage_timing",
               "gpc_last_sizes", "gpc_tape_lower", "gpc_tape_get_view", "gpc_last_traffic", "gpc_last_io_bytes",
               "gpc_merge_mechanisms_static", "gpc_prepare_batch", "gpc_fetch_batch", "gpc_last_host_timings", "gpc_walk_form",
-              "gpc_tape_walk_segments", "gpc_walk_segments", "gpc_fallback_counts",
+              "gpc_tape_walk_segments", "gpc_walk_segments", "gpc_fallback_counts", "gpc_walk_config",
               "gpc_server_fallback_counts", "gpc_alloc_counts"):
         getattr(L, f).restype = i32
     _lib = L

@@ -8,6 +8,7 @@
 // mechanisms (the reference copies the whole node x 32 class matrix,
 // Driver.hpp:158-161).
 #include <algorithm>
+#include <array>
 #include <chrono>
 #include <cmath>
 #include <atomic>
@@ -404,6 +405,42 @@ class DemCache {
 };
 DemCache &dem_cache() {
   static DemCache *c = new DemCache;
+  return *c;
+}
+}  // namespace
+
+namespace {
+// Walk configurations chosen by gpc_autotune, kept for the process and keyed
+// by the bitset widths of the batch they were tuned on: the set of its
+// circuits' (walk slot count, detector words rounded up to a power of two)
+// classes.  A coarse key on purpose: the chunks of a large batch, and other
+// batches of the same workload, hold the same classes.  A batch prepared
+// without explicit walk options on a driver that has not tuned itself takes
+// the configuration cached for its key (the DEMs do not depend on it).
+class TuneCache {
+ public:
+  bool get(uint64_t key, uint32_t cfg[3]) {
+    std::lock_guard<std::mutex> lk(mu_);
+    auto it = map_.find(key);
+    if (it == map_.end()) return false;
+    for (int k = 0; k < 3; ++k) cfg[k] = it->second[k];
+    return true;
+  }
+  void put(uint64_t key, const uint32_t cfg[3]) {
+    std::lock_guard<std::mutex> lk(mu_);
+    map_[key] = {cfg[0], cfg[1], cfg[2]};
+  }
+  void clear() {
+    std::lock_guard<std::mutex> lk(mu_);
+    map_.clear();
+  }
+
+ private:
+  std::mutex mu_;
+  std::unordered_map<uint64_t, std::array<uint32_t, 3>> map_;
+};
+TuneCache &tune_cache() {
+  static TuneCache *c = new TuneCache;
   return *c;
 }
 }  // namespace
@@ -1011,6 +1048,14 @@ struct gpc_driver {
       host_ms[0] = 0;
     }
     const auto t1 = HostClock::now();
+    if (!tuned && walk_words == 0 && walk_qpt == 0 && walk_queue == 0) {
+      // a batch takes the walk configuration tuned for its widths, if any (else the defaults)
+      uint32_t cfg[3] = {0, 0, 0};
+      if (ncirc() > 1) tune_cache().get(width_key(), cfg);
+      batch_words = cfg[0];
+      batch_qpt = cfg[1];
+      batch_queue = cfg[2];
+    }
     plan_segments();
     layout();
     // The stream may still be reading the old arena: finish before regrowing.
@@ -2032,10 +2077,27 @@ struct gpc_driver {
   // Times the batched pipeline of these circuits in each walk configuration
   // (words per CTA x qubits per thread, one launch per thread-count class or
   // one persistent launch) and keeps the fastest for batches.
+  // The tuning key of the prepared circuits (see TuneCache).
+  uint64_t width_key() const {
+    std::vector<uint64_t> cls;
+    for (const Tape &T : tapes) {
+      uint64_t w = 1;
+      while (w < T.w) w <<= 1;
+      cls.push_back(((uint64_t)T.qpad << 32) | w);
+    }
+    std::sort(cls.begin(), cls.end());
+    cls.erase(std::unique(cls.begin(), cls.end()), cls.end());
+    uint64_t h = 0xcbf29ce484222325ull;
+    for (uint64_t v : cls) h = (h ^ v) * 0x100000001b3ull;
+    return h;
+  }
+  bool tuned = false;  // this driver chose its batches' walk configuration itself
+
   void autotune(const char *const *texts, const size_t *lens, uint32_t n, uint32_t reps, gpc_tuning &out) {
     static const uint32_t cand[][3] = {{2, 1, 0}, {1, 1, 0}, {2, 2, 0}, {1, 2, 0}, {1, 4, 0},
                                        {2, 1, 1}, {1, 1, 1}, {2, 2, 1}, {1, 2, 1}};
     out = gpc_tuning{};
+    tuned = true;
     prepare(texts, lens, n);  // lowered once: each configuration lays out the same tapes again
     float best = std::numeric_limits<float>::infinity();
     uint32_t bw = batch_words, bq = batch_qpt, bz = batch_queue;
@@ -2077,6 +2139,8 @@ struct gpc_driver {
     batch_words = bw;
     batch_qpt = bq;
     batch_queue = bz;
+    const uint32_t cfg[3] = {bw, bq, bz};
+    tune_cache().put(width_key(), cfg);  // for other drivers' batches of these widths
     prepare(nullptr, nullptr, 0);
     out.walk_words = (int32_t)bw;
     out.walk_qpt = (int32_t)bq;
@@ -2159,6 +2223,12 @@ struct gpc_driver {
     };
     try {
       for (uint32_t c = 0; c < nc; ++c) {
+        if (c == 1) {  // the second pipeline walks as the first one settled (tuned or cached)
+          D[1]->batch_words = D[0]->batch_words;
+          D[1]->batch_qpt = D[0]->batch_qpt;
+          D[1]->batch_queue = D[0]->batch_queue;
+          D[1]->tuned = true;
+        }
         D[c & 1]->prepare(texts + cut[c], lens + cut[c], cut[c + 1] - cut[c]);
         add_ms(D[c & 1], 0, 3);
         h2d += D[c & 1]->last_h2d;
@@ -2790,6 +2860,16 @@ void gpc_server_destroy(gpc_server *server) { delete server; }
 void gpc_driver_destroy(gpc_driver *driver) { delete driver; }
 
 void *gpc_driver_stream(gpc_driver *driver) { return driver ? (void *)driver->stream : nullptr; }
+
+gpc_status gpc_walk_config(gpc_driver *driver, int32_t *words, int32_t *qpt, int32_t *queue) {
+  if (!driver || !words || !qpt || !queue) return fail(GPC_ERR_INVALID, "null argument");
+  *words = (int32_t)driver->batch_words;
+  *qpt = (int32_t)driver->batch_qpt;
+  *queue = (int32_t)driver->batch_queue;
+  return GPC_OK;
+}
+
+void gpc_tune_cache_clear(void) { tune_cache().clear(); }
 
 gpc_status gpc_walk_form(gpc_driver *driver, int32_t *launches, int32_t *persistent) {
   if (!driver || !launches || !persistent) return fail(GPC_ERR_INVALID, "null argument");

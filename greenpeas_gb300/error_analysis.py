@@ -307,6 +307,14 @@ class Driver:
         _native.check(_native.lib().gpc_last_timings(self._h, ms))
         return dict(zip(("walk", "key", "sort", "merge", "total"), [float(x) for x in ms]))
 
+    def walk_config(self) -> dict:
+        """Walk configuration of this driver's batches: detector words per walk CTA, qubits per
+        walk thread, persistent launch (0: defaults); set by autotune, or taken from the
+        configurations autotune kept for batches of the same bitset widths."""
+        w, q, z = ctypes.c_int32(), ctypes.c_int32(), ctypes.c_int32()
+        _native.check(_native.lib().gpc_walk_config(self._h, ctypes.byref(w), ctypes.byref(q), ctypes.byref(z)))
+        return {"walk_words": w.value, "walk_qpt": q.value, "walk_queue": z.value}
+
     def walk_form(self) -> dict:
         """Walk launches per run of the prepared circuits and whether they form one persistent launch."""
         n, q = ctypes.c_int32(), ctypes.c_int32()
@@ -340,6 +348,11 @@ class Driver:
     @property
     def stream(self) -> int:
         return _native.lib().gpc_driver_stream(self._h) or 0
+
+
+def tune_cache_clear() -> None:
+    """Forgets the walk configurations autotune kept for the process (gpc_tune_cache_clear)."""
+    _native.lib().gpc_tune_cache_clear()
 
 
 def get_driver(circuit, correlation_level: CorrelationLevel = CorrelationLevel.L2, **kw) -> Driver:

@@ -264,6 +264,17 @@ gpc_status gpc_last_timings(gpc_driver *driver, float *ms5);
  * each phase summed over the chunks. */
 gpc_status gpc_last_host_timings(gpc_driver *driver, double *ms6);
 
+/* Walk configuration of the driver's batches (no counterpart in the
+ * reference): detector words per walk CTA, qubits per walk thread and the
+ * persistent launch (0: the defaults).  gpc_autotune sets it and also keeps
+ * it for the process, keyed by the bitset widths of the batch it tuned (the
+ * set of its circuits' walk slot counts and word counts rounded up to a
+ * power of two); a batch prepared on a driver without explicit walk options
+ * that has not tuned itself takes the configuration kept for its widths. */
+gpc_status gpc_walk_config(gpc_driver *driver, int32_t *words, int32_t *qpt, int32_t *queue);
+/* Forgets every kept walk configuration. */
+void gpc_tune_cache_clear(void);
+
 /* Walk launches of the prepared circuits (no counterpart in the reference):
  * `launches` per run (one per thread-count class, or 1), `persistent` 1 when
  * the batch walks in one persistent launch off its work queue. */

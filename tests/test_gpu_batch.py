@@ -103,6 +103,32 @@ def test_autotune_keeps_results_and_picks_a_configuration():
     drv.run_device()
     assert [a == b for a, b in zip(drv.fetch_batch(), before)] == [True] * len(circs)
     assert [a == b for a, b in zip(drv.compile_batch(circs), before)] == [True] * len(circs)
+    gp.tune_cache_clear()  # (the choice is kept for the process: later tests start from the defaults)
+
+
+def test_autotune_choice_is_kept_for_batches_of_the_same_widths():
+    """Autotune keeps its choice for the process, keyed by the batch's bitset widths: a fresh driver
+    preparing a batch of the same widths walks in that configuration, a driver with explicit walk
+    options keeps its own, and the DEMs do not depend on either."""
+    gp.tune_cache_clear()
+    circs = _mixed()
+    fresh = gp.get_driver(circs[0])
+    fresh.prepare_batch(circs)
+    assert fresh.walk_config() == {"walk_words": 0, "walk_qpt": 0, "walk_queue": 0}
+    ref = fresh.compile_batch(circs)
+    tune = gp.get_driver(circs[0]).autotune(circs, reps=1)
+    chosen = {k: tune[k] for k in ("walk_words", "walk_qpt", "walk_queue")}
+    other = gp.get_driver(circs[0])
+    other.prepare_batch(circs[::-1])  # the same widths in another order
+    assert other.walk_config() == chosen
+    assert [a == b for a, b in zip(other.compile_batch(circs), ref)] == [True] * len(circs)
+    explicit = gp.get_driver(circs[0], walk_words=1)
+    explicit.prepare_batch(circs)
+    assert explicit.walk_config() == {"walk_words": 0, "walk_qpt": 0, "walk_queue": 0}
+    narrower = gp.get_driver(circs[0])
+    narrower.prepare_batch(circs[:3])  # other widths: nothing kept for them
+    assert narrower.walk_config() == {"walk_words": 0, "walk_qpt": 0, "walk_queue": 0}
+    gp.tune_cache_clear()
 
 
 @pytest.mark.parametrize("words,qpt", [(2, 1), (1, 1), (2, 2), (1, 2)])
@@ -182,3 +208,4 @@ def test_walk_queue_option_selects_the_launch_form():
     drv = gp.get_driver(circs[0])
     tune = drv.autotune(circs, reps=1)
     assert drv.walk_form()["persistent"] == bool(tune["walk_queue"])
+    gp.tune_cache_clear()
