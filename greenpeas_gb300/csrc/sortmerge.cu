@@ -225,8 +225,12 @@ __global__ void __launch_bounds__(KEY_THREADS, 5) key_kernel(KeyLaunch L) {
   if (L.write_all || split) L.key[mg] = key;  // a split pass leaves the partial key
   if (tcap) {
     // rows are 16-byte aligned (tcap is a multiple of 4, at least 32)
-    if (cnt) reinterpret_cast<uint4 *>(out)[0] = make_uint4(stg[0][tid], stg[1][tid], stg[2][tid], stg[3][tid]);
-    if (cnt > 4) reinterpret_cast<uint4 *>(out)[1] = make_uint4(stg[4][tid], stg[5][tid], stg[6][tid], stg[7][tid]);
+    // (both halves even for four targets or fewer: a whole 32-byte sector per row; entries past
+    // the count are never read)
+    if (cnt) {
+      reinterpret_cast<uint4 *>(out)[0] = make_uint4(stg[0][tid], stg[1][tid], stg[2][tid], stg[3][tid]);
+      reinterpret_cast<uint4 *>(out)[1] = make_uint4(stg[4][tid], stg[5][tid], stg[6][tid], stg[7][tid]);
+    }
     C.tn[m] = cnt;
     if (cnt > tcap) atomicOr(L.err, DEV_FLAG_LONG);
     const uint32_t am = __activemask();
