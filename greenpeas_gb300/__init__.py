@@ -14,7 +14,7 @@ from ._native import GpcError
 from .autograd import NoiseRateDEM
 from .codes import BBCode, SurfaceCode
 from .dem import DetectorErrorModel
-from .error_analysis import CorrelationLevel, Driver, Tape, get_driver, tune_cache_clear
+from .error_analysis import CorrelationLevel, Driver, Lowerer, Tape, get_driver, tune_cache_clear
 
-__all__ = ["BBCode", "CorrelationLevel", "DetectorErrorModel", "Driver", "GpcError", "NoiseRateDEM", "SurfaceCode",
+__all__ = ["BBCode", "CorrelationLevel", "DetectorErrorModel", "Driver", "GpcError", "Lowerer", "NoiseRateDEM", "SurfaceCode",
            "Tape", "get_driver", "tune_cache_clear"]

@@ -32,6 +32,7 @@ EXPORTS = [
     "gpc_device_dem", "gpc_autotune", "gpc_last_host_timings", "gpc_walk_form", "gpc_walk_segments",
     "gpc_walk_config", "gpc_tune_cache_clear",
     "gpc_fallback_counts", "gpc_server_fallback_counts", "gpc_alloc_counts",
+    "gpc_tape_lower_cuts", "gpc_lowerer_create", "gpc_lowerer_lower", "gpc_lowerer_stats", "gpc_lowerer_free",
 ]
 
 
@@ -46,7 +47,7 @@ class GpcError(RuntimeError):
 class ServerOptions(ctypes.Structure):
     _fields_ = [("device", ctypes.c_int32), ("correlation_level", ctypes.c_int32), ("slots", ctypes.c_uint32),
                 ("max_batch", ctypes.c_uint32), ("hbm_budget", ctypes.c_uint64), ("lower_threads", ctypes.c_uint32),
-                ("reserved", ctypes.c_uint32 * 3)]
+                ("incremental", ctypes.c_uint32), ("reserved", ctypes.c_uint32 * 2)]
 
 
 class Options(ctypes.Structure):
@@ -54,7 +55,12 @@ class Options(ctypes.Structure):
                 ("walk_qpt", ctypes.c_int32), ("bucket_mean", ctypes.c_int32), ("walk_words", ctypes.c_int32),
                 ("key_split", ctypes.c_int32), ("walk_queue", ctypes.c_int32), ("walk_segment", ctypes.c_int32),
                 ("wait_limit_us", ctypes.c_int32), ("test_hold_tile", ctypes.c_int32),
-                ("test_fail_alloc", ctypes.c_int32), ("heap_results", ctypes.c_int32)]
+                ("test_fail_alloc", ctypes.c_int32), ("heap_results", ctypes.c_int32), ("incremental", ctypes.c_int32)]
+
+
+class LowerStats(ctypes.Structure):
+    _fields_ = [("incremental", ctypes.c_uint32), ("segments", ctypes.c_uint32), ("reused", ctypes.c_uint32),
+                ("reserved", ctypes.c_uint32), ("parsed_bytes", ctypes.c_uint64)]
 
 
 class TuningEntry(ctypes.Structure):
@@ -137,6 +143,12 @@ def lib() -> ctypes.CDLL:
     L.gpc_server_fallback_counts.argtypes = [vp, u64p]
     L.gpc_tape_free.argtypes = [vp]
     L.gpc_tape_free.restype = None
+    L.gpc_tape_lower_cuts.argtypes = [ctypes.c_char_p, sz, i32, u64p, u32, ctypes.POINTER(vp)]
+    L.gpc_lowerer_create.argtypes = [i32, i32, ctypes.POINTER(vp)]
+    L.gpc_lowerer_lower.argtypes = [vp, ctypes.c_char_p, sz, ctypes.POINTER(vp)]
+    L.gpc_lowerer_stats.argtypes = [vp, ctypes.POINTER(LowerStats), u64p, u32, u32p]
+    L.gpc_lowerer_free.argtypes = [vp]
+    L.gpc_lowerer_free.restype = None
     L.gpc_tape_last_error.restype = ctypes.c_char_p
     L.gpc_device_dem.argtypes = [vp, i32, ctypes.POINTER(vp), ctypes.POINTER(vp), ctypes.POINTER(vp), u32p, u32p]
     L.gpc_server_create.argtypes = [ctypes.POINTER(ServerOptions), ctypes.POINTER(vp)]
@@ -157,7 +169,8 @@ def lib() -> ctypes.CDLL:
               "gpc_last_sizes", "gpc_tape_lower", "gpc_tape_get_view", "gpc_last_traffic", "gpc_last_io_bytes",
               "gpc_merge_mechanisms_static", "gpc_prepare_batch", "gpc_fetch_batch", "gpc_last_host_timings", "gpc_walk_form",
               "gpc_tape_walk_segments", "gpc_walk_segments", "gpc_fallback_counts", "gpc_walk_config",
-              "gpc_server_fallback_counts", "gpc_alloc_counts"):
+              "gpc_server_fallback_counts", "gpc_alloc_counts", "gpc_tape_lower_cuts", "gpc_lowerer_create",
+              "gpc_lowerer_lower", "gpc_lowerer_stats"):
         getattr(L, f).restype = i32
     _lib = L
     return L

@@ -999,6 +999,7 @@ struct gpc_driver {
     // (measured on GB300 + Grace: bb12 end to end 0.41 -> 0.36 ms; a batch's lowering, one
     // circuit per thread, 17.3 -> 16.8 ms)
     lo.segment_occ = 8192;
+    lo.incremental = incremental;
     gpc::HostPool &hp = host_pool();
     if (lower_scratch.size() < hp.workers() + 1) lower_scratch.resize(hp.workers() + 1);
     resize_tapes(n);
@@ -1865,6 +1866,7 @@ struct gpc_driver {
   // Results copied into page-locked memory that the DEMs keep (pinned DEMs,
   // batch result blocks), as far as the page-locked pool reaches.
   bool pinned_results = true;
+  bool incremental = false;  // lower each circuit against the previous one of its lowering slot
 
   // Waits for the pipeline and issues the copies of its result on the driver's
   // stream; end_fetch builds the DEMs.  A single circuit copied into a pinned
@@ -2304,6 +2306,7 @@ struct gpc_server {
   static constexpr size_t kSpareTapes = 32;
   int device = 0, level = 2;
   uint32_t max_batch = 16;
+  bool incremental = false;  // each lowering thread lowers a request against its previous one
   size_t budget = 0, used = 0, peak = 0;
   uint32_t budget_waiters = 0;
   uint64_t next_ticket = 1, completed = 0, batches = 0;
@@ -2372,6 +2375,7 @@ struct gpc_server {
     lo.chunk_min = gpc::kWalkChunkMin;  // requests are compiled in batches
     lo.sources = false;
     lo.segment_occ = 8192;  // as the driver lowers
+    lo.incremental = incremental;
     while (true) {
       uint64_t t;
       const char *text;
@@ -2557,6 +2561,8 @@ gpc_status gpc_get_driver(const char *stim_text, size_t len, int32_t correlation
     if (options->test_fail_alloc) d->alloc_ctr.fail_at = options->test_fail_alloc - 1;
     if (options->heap_results != 0 && options->heap_results != 1) return fail(GPC_ERR_INVALID, "heap_results must be 0 or 1");
     d->pinned_results = options->heap_results == 0;
+    if (options->incremental != 0 && options->incremental != 1) return fail(GPC_ERR_INVALID, "incremental must be 0 or 1");
+    d->incremental = options->incremental == 1;
   }
   gpc_status st = guarded([&] {
     int n = 0;
@@ -2749,6 +2755,8 @@ gpc_status gpc_server_create(const gpc_server_options *options, gpc_server **out
   sv->level = o.correlation_level;
   sv->max_batch = o.max_batch;
   sv->budget = o.hbm_budget;
+  if (o.incremental > 1) return fail(GPC_ERR_INVALID, "incremental must be 0 or 1");
+  sv->incremental = o.incremental == 1;
   gpc_status st = guarded([&] {
     int n = 0;
     CK(cudaGetDeviceCount(&n));

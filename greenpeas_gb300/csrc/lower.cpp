@@ -9,6 +9,7 @@
 #include <cmath>
 #include <cstdlib>
 #include <cstring>
+#include <string>
 #include <string_view>
 #include <unordered_map>
 
@@ -115,6 +116,8 @@ struct TextParser {
   const char *s, *e;
   size_t line = 1;
   Parsed *out;
+  const char *s0 = nullptr;  // start of the text (offsets of the marks)
+  const char *ls = nullptr;  // start of the current line
   // targets are written through this cursor into out->pool, sized up front:
   // targets are separated by whitespace, so a text of n bytes holds at most
   // n / 2 + 1 of them (a REPEAT body's are stored once)
@@ -152,6 +155,7 @@ struct TextParser {
       if (c == '\n') {
         ++s;
         ++line;
+        ls = s;
         continue;
       }
       if (c == '#') {
@@ -162,6 +166,14 @@ struct TextParser {
         if (!inner) fail(GPC_ERR_PARSE, "unmatched '}'");
         ++s;
         return;
+      }
+      if (depth == 0 && out->want_marks) {
+        // a top-level statement that opens its line: a place where the text
+        // may be re-parsed from (the incremental lowering)
+        const char *q = ls;
+        while (q < s && (*q == ' ' || *q == '\t' || *q == '\r')) ++q;
+        if (q == s)
+          out->marks.push_back({(size_t)(ls - s0), line, dst.size(), (size_t)(tw - out->pool.data())});
       }
       size_t n = 0;
       while (s < e && is_name_char(*s)) {
@@ -399,10 +411,12 @@ double split_dep2(double p) { return 0.5 - 0.5 * std::pow(1.0 - (16.0 * p) / 15.
 
 void parse_stim_into(const char *text, size_t len, Parsed &p) {
   p.ins.clear();
+  p.marks.clear();
   if (!text && len) throw Error(GPC_ERR_INVALID, "null circuit text");
   p.pool.resize(len / 2 + 16);  // the most targets a text of len bytes holds (not initialised)
   p.ins.reserve(len / 64 + 16);
   TextParser tp{text, text + len, 1, &p};
+  tp.s0 = tp.ls = text;
   tp.tw = p.pool.data();
   try {
     tp.block(p.ins, false, 0);
@@ -411,6 +425,7 @@ void parse_stim_into(const char *text, size_t len, Parsed &p) {
     throw;
   }
   p.pool.resize((size_t)(tp.tw - p.pool.data()));
+  p.end_line = tp.line;
 }
 
 Parsed parse_stim(const char *text, size_t len) {
@@ -466,16 +481,48 @@ struct LowerScratch::Buffers {
     uint32_t nprov = 0, eoff = 0, poff = 0;
     std::vector<uint64_t> fine, coarse;  // per-qubit op signatures of the segment (qubit packing)
     std::vector<uint64_t> snapbits;      // bit i: op oa + i of the segment's tape range is a snapshot
+    std::vector<uint32_t> mlo, mhi;      // its measurements' first/last epochs (segment-local; incremental)
   };
   std::vector<Segment> segs;
   std::vector<size_t> cut;
   std::vector<uint64_t> fine, coarse;
+
+  // ---- incremental lowering ----
+  // The previous circuit of this scratch: its text, and (swapped out of the
+  // arrays above when the next circuit is lowered against it) its forward-pass
+  // arrays, cuts and segments.
+  struct Prev {
+    bool valid = false;
+    std::string text;
+    std::vector<uint32_t> measBase, occBase, tsrc, moff, mbits;
+    std::vector<size_t> cut;
+    std::vector<Segment> segs;
+    size_t n_ins = 0, nocc = 0;
+    uint32_t nmeas = 0, nq = 0, kcap = 0;
+    int level = -1;
+    bool sources = false;
+  } prev;
+  // Set by the planner for the next lower_into: the cuts, and for each new
+  // segment the previous segment over the same statements (or -1).
+  struct Plan {
+    bool active = false;
+    std::vector<size_t> cut;
+    std::vector<int32_t> from;
+  } plan;
+  Parsed mid;  // the statements parsed again
+  std::vector<uint32_t> runs;  // segments scheduled by this lowering
+  std::vector<int64_t> dbits, dsrc;  // per reused segment: shift of its detector bits and sources
 };
 
 LowerScratch::LowerScratch() : b(new Buffers) {}
 LowerScratch::~LowerScratch() = default;
 LowerScratch::LowerScratch(LowerScratch &&) noexcept = default;
 LowerScratch &LowerScratch::operator=(LowerScratch &&) noexcept = default;
+const std::vector<size_t> &LowerScratch::last_cuts() const { return b->cut; }
+void LowerScratch::forget() {
+  b->prev.valid = false;
+  b->plan.active = false;
+}
 
 void parse_stim_pieces(const char *text, size_t len, Parsed &out, std::vector<Parsed> &pieces, HostPool &pool) {
   constexpr size_t kPieceMin = 16 * 1024;
@@ -495,6 +542,7 @@ void parse_stim_pieces(const char *text, size_t len, Parsed &out, std::vector<Pa
   cut.push_back(len);
   const uint32_t np = (uint32_t)cut.size() - 1;
   if (pieces.size() < np) pieces.resize(np);
+  for (uint32_t i = 0; i < np; ++i) pieces[i].want_marks = out.want_marks;
   try {
     pool.run(np, [&](uint32_t i, uint32_t) { parse_stim_into(text + cut[i], cut[i + 1] - cut[i], pieces[i]); });
   } catch (const Error &) {
@@ -510,6 +558,14 @@ void parse_stim_pieces(const char *text, size_t len, Parsed &out, std::vector<Pa
   if (toff[np] > 0xFFFFFFFFull) throw Error(GPC_ERR_CAPACITY, "circuit too long");
   out.ins.resize(ioff[np]);
   out.pool.resize(toff[np]);
+  out.marks.clear();
+  size_t line0 = 0;
+  for (uint32_t i = 0; i < np; ++i) {
+    for (const ParseMark &k : pieces[i].marks)
+      out.marks.push_back({k.off + cut[i], k.line + line0, k.ins + ioff[i], k.tpos + toff[i]});
+    line0 += pieces[i].end_line - 1;
+  }
+  out.end_line = line0 + 1;
   pool.run(np, [&](uint32_t i, uint32_t) {
     const Parsed &pc = pieces[i];
     if (!pc.pool.empty()) memcpy(out.pool.data() + toff[i], pc.pool.data(), pc.pool.size() * 4);
@@ -522,12 +578,149 @@ void parse_stim_pieces(const char *text, size_t len, Parsed &out, std::vector<Pa
   });
 }
 
+namespace {
+
+// Lowers `text` against the previous circuit of S (incremental lowering):
+// re-parses the statements between the longest common prefix and suffix of
+// the two texts into S.parsed, and plans the backward pass's cuts so that
+// the previous segments over unchanged statements can be taken over.
+// Returns false (S.parsed untouched) when a full lowering is the better way.
+bool plan_incremental(const char *text, size_t len, const LowerOptions &opt, LowerScratch &S) {
+  LowerScratch::Buffers &B = *S.b;
+  const LowerScratch::Buffers::Prev &V = B.prev;
+  Parsed &P = S.parsed;
+  if (!V.valid || opt.cuts || !text || P.marks.empty() || B.cut.size() < 2 || B.cut.front() != P.ins.size())
+    return false;
+  const char *o = V.text.data();
+  const size_t on = V.text.size(), mn = std::min(on, len);
+  size_t lp = 0;
+  while (lp < mn && o[lp] == text[lp]) ++lp;
+  size_t ls = 0;
+  while (ls < mn - lp && o[on - 1 - ls] == text[len - 1 - ls]) ++ls;
+  const std::vector<ParseMark> &mk = P.marks;
+  // the statement holding the first changed byte: the last mark at or before it
+  size_t k = (size_t)(std::upper_bound(mk.begin(), mk.end(), lp,
+                                       [](size_t v, const ParseMark &x) { return v < x.off; }) - mk.begin());
+  const ParseMark a = k ? mk[k - 1] : ParseMark{0, 1, 0, 0};
+  const size_t ka = k ? k - 1 : 0;  // marks kept before the changed span
+  // the first statement after the last changed byte whose line starts inside
+  // the common suffix (so the byte before it, a newline, is common too)
+  const size_t need = on - ls + 1;
+  const size_t kb = (size_t)(std::lower_bound(mk.begin(), mk.end(), need,
+                                              [](const ParseMark &x, size_t v) { return x.off < v; }) - mk.begin());
+  const ParseMark b = kb < mk.size() ? mk[kb] : ParseMark{on, P.end_line, P.ins.size(), P.pool.size()};
+  if (b.off < a.off || b.ins < a.ins || b.tpos < a.tpos) return false;
+  const size_t bn = b.off + len - on;  // where that statement starts in the new text
+  if (bn < a.off || bn > len || (bn > 0 && bn < len && text[bn - 1] != '\n')) return false;
+  // a changed span of more than half the text: parse and lower it whole
+  if (2 * (bn - a.off) > len) return false;
+  Parsed &M = B.mid;
+  M.want_marks = true;
+  try {
+    parse_stim_into(text + a.off, bn - a.off, M);
+  } catch (const Error &) {
+    return false;  // (a full parse reports the error with its line in the whole text)
+  }
+  // splice: instructions, targets and marks of [0, a) + the new span + [b, end)
+  const size_t nI0 = P.ins.size(), nT0 = P.pool.size();
+  const size_t nI = a.ins + M.ins.size() + (nI0 - b.ins), nT = a.tpos + M.pool.size() + (nT0 - b.tpos);
+  if (nT > 0xFFFFFFFFull) return false;
+  const size_t sufI = nI0 - b.ins, sufT = nT0 - b.tpos;
+  const size_t newB_I = a.ins + M.ins.size(), newB_T = a.tpos + M.pool.size();
+  if (nI > nI0) P.ins.resize(nI);
+  if (sufI) memmove(P.ins.data() + newB_I, P.ins.data() + b.ins, sufI * sizeof(Instr));
+  if (nI < nI0) P.ins.resize(nI);
+  if (nT > nT0) P.pool.resize(nT);
+  if (sufT) memmove(P.pool.data() + newB_T, P.pool.data() + b.tpos, sufT * sizeof(uint32_t));
+  if (nT < nT0) P.pool.resize(nT);
+  if (!M.pool.empty()) memcpy(P.pool.data() + a.tpos, M.pool.data(), M.pool.size() * sizeof(uint32_t));
+  for (size_t i = 0; i < M.ins.size(); ++i) {
+    P.ins[a.ins + i] = M.ins[i];
+    P.ins[a.ins + i].t0 += (uint32_t)a.tpos;
+  }
+  const int64_t dT = (int64_t)newB_T - (int64_t)b.tpos;
+  if (dT)
+    for (size_t i = newB_I; i < nI; ++i) P.ins[i].t0 = (uint32_t)((int64_t)P.ins[i].t0 + dT);
+  const size_t line_b = a.line + M.end_line - 1;  // line of the suffix's first statement in the new text
+  std::vector<ParseMark> &tail = B.mid.marks;     // (M's marks, rebased, then the suffix's)
+  for (ParseMark &x : tail) {
+    x.off += a.off;
+    x.line += a.line - 1;
+    x.ins += a.ins;
+    x.tpos += a.tpos;
+  }
+  for (size_t i = kb; i < mk.size(); ++i)
+    tail.push_back({mk[i].off + len - on, mk[i].line + line_b - b.line, mk[i].ins + newB_I - b.ins,
+                    mk[i].tpos + newB_T - b.tpos});
+  P.marks.resize(ka);
+  P.marks.insert(P.marks.end(), tail.begin(), tail.end());
+  P.end_line = P.end_line + line_b - b.line;
+  S.stats.parsed_bytes = bn - a.off;
+
+  // cuts: the previous segments wholly after the changed span (shifted by
+  // the change in instruction count) and wholly before it; the span between
+  // them is cut afresh into pieces of about segment_occ occurrences
+  const std::vector<size_t> &oc = B.cut;
+  const int64_t dI = (int64_t)nI - (int64_t)nI0;
+  std::vector<size_t> &nc = B.plan.cut;
+  std::vector<int32_t> &from = B.plan.from;
+  nc.clear();
+  from.clear();
+  nc.push_back(nI);
+  const size_t nseg0 = oc.size() - 1;
+  size_t s = 0;
+  for (; s < nseg0 && oc[s + 1] >= b.ins; ++s) {
+    nc.push_back((size_t)((int64_t)oc[s + 1] + dI));
+    from.push_back((int32_t)s);
+  }
+  size_t t = s;  // first segment wholly before the changed span
+  while (t < nseg0 && oc[t] > a.ins) ++t;
+  const size_t hi = nc.back(), lo = t < nseg0 ? oc[t] : 0;
+  if (hi > lo) {
+    const size_t so = std::max<uint32_t>(1024, opt.segment_occ);
+    size_t acc = 0;
+    for (size_t ii = hi; ii-- > lo + 1;) {
+      acc += P.ins[ii].tn;
+      if (acc >= so) {
+        nc.push_back(ii);
+        from.push_back(-1);
+        acc = 0;
+      }
+    }
+    nc.push_back(lo);
+    from.push_back(-1);
+  }
+  for (; t < nseg0; ++t) {
+    nc.push_back(oc[t + 1]);
+    from.push_back((int32_t)t);
+  }
+  if (nc.back() != 0 || from.size() + 1 != nc.size()) return false;
+  B.plan.active = true;
+  return true;
+}
+
+}  // namespace
+
 void lower_text(const char *text, size_t len, const LowerOptions &opt, Tape &T, LowerScratch &S, HostPool *pool) {
-  if (pool)
-    parse_stim_pieces(text, len, S.parsed, S.pieces, *pool);
-  else
-    parse_stim_into(text, len, S.parsed);
+  LowerScratch::Buffers &B = *S.b;
+  S.stats = LowerScratch::Stats{};
+  S.parsed.want_marks = opt.incremental;
+  B.plan.active = false;
+  if (!opt.incremental || !plan_incremental(text, len, opt, S)) {
+    B.prev.valid = false;  // (a parse that fails leaves S.parsed half written)
+    if (pool)
+      parse_stim_pieces(text, len, S.parsed, S.pieces, *pool);
+    else
+      parse_stim_into(text, len, S.parsed);
+  }
+  const size_t parsed = B.plan.active ? S.stats.parsed_bytes : len;
+  B.prev.valid = false;
   lower_into(S.parsed, opt, T, S, pool);
+  S.stats.parsed_bytes = parsed;
+  if (opt.incremental) {
+    B.prev.text.assign(text, len);
+    B.prev.valid = true;
+  }
 }
 
 Tape lower(const Parsed &P, const LowerOptions &opt) {
@@ -542,6 +735,23 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
   T.reset();
   LowerScratch::Buffers &B = *S.b;
   uint32_t kcap = std::max<uint32_t>(1, opt.kcap);
+  // Lowered against the previous circuit (a plan from lower_text): its arrays
+  // move aside, readable while this circuit's are built, and its segments
+  // are taken over where they still apply.
+  const bool reuse = opt.incremental && B.plan.active;
+  B.plan.active = false;
+  B.prev.valid = false;  // lower_text marks the state valid once this lowering is done
+  if (reuse) {
+    std::swap(B.measBase, B.prev.measBase);
+    std::swap(B.occBase, B.prev.occBase);
+    std::swap(B.tsrc, B.prev.tsrc);
+    std::swap(B.moff, B.prev.moff);
+    std::swap(B.mbits, B.prev.mbits);
+    std::swap(B.cut, B.prev.cut);
+    std::swap(B.segs, B.prev.segs);
+  }
+  S.stats = LowerScratch::Stats{};
+  S.stats.incremental = reuse;
 
   // ---- forward pass: qubits, measurements, detectors, observables --------
   std::vector<uint32_t> &measBase = B.measBase;
@@ -748,9 +958,16 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
   // so the DEM is that of one uncut pass; the schedule gains at most about one
   // epoch per cut.  Segments run on the pool when one is given.
   std::vector<size_t> &cut = B.cut;  // segment s covers instructions [cut[s + 1], cut[s])
-  cut.clear();
-  cut.push_back(P.ins.size());
-  {
+  if (reuse) {
+    cut.swap(B.plan.cut);
+  } else if (opt.cuts) {
+    cut = *opt.cuts;
+    bool ok = cut.size() >= 2 && cut.front() == P.ins.size() && cut.back() == 0;
+    for (size_t i = 0; ok && i + 1 < cut.size(); ++i) ok = cut[i] > cut[i + 1] || (P.ins.empty() && cut.size() == 2);
+    if (!ok) throw Error(GPC_ERR_INVALID, "segment cuts must descend from the instruction count to 0");
+  } else {
+    cut.clear();
+    cut.push_back(P.ins.size());
     // at most 8 segments of equal size, about opt.segment_occ occurrences or fewer each
     const size_t so = std::max<uint32_t>(1024, opt.segment_occ);
     const size_t nsegw = std::max<size_t>(1, std::min<size_t>(8, (occ + so - 1) / so));
@@ -767,6 +984,9 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
   }
   const uint32_t nseg = (uint32_t)cut.size() - 1;
   if (B.segs.size() < nseg) B.segs.resize(nseg);
+  // one segment writes its records in place (unless the segment is kept for
+  // the next circuit of an incremental lowering)
+  const bool direct = nseg == 1 && !opt.incremental;
   std::vector<uint32_t> &measLo = B.measLo, &measHi = B.measHi;
   measLo.assign(m, kNone);
   measHi.assign(m, kNone);
@@ -774,6 +994,79 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
   const uint32_t dep2Type = opt.level == 0 ? REC_DEP2_L0 : opt.level == 1 ? REC_DEP2_L1 : REC_DEP2_L2;
   auto occ_at = [&](size_t i) -> size_t { return i < P.ins.size() ? occBase[i] : occ; };
   auto meas_at = [&](size_t i) -> uint32_t { return i < P.ins.size() ? measBase[i] : m; };
+
+  // Segments taken over from the previous circuit.  A previous segment over
+  // the same statements scheduled exactly these ops, except that its
+  // measurements' detector bits and its noise targets' sources came from the
+  // rest of that circuit: it is taken over when both differ from this
+  // circuit's by one shift each (detectors numbered after a changed span,
+  // ticks counted after it), and its bits and sources are shifted.
+  std::vector<uint32_t> &runs = B.runs;  // 1: schedule the segment, 0: take it over
+  runs.assign(nseg, 1);
+  B.dbits.assign(nseg, 0);
+  B.dsrc.assign(nseg, 0);
+  if (reuse && B.prev.nq == nq && B.prev.kcap == kcap && B.prev.level == opt.level &&
+      B.prev.sources == opt.sources && B.plan.from.size() == nseg) {
+    const LowerScratch::Buffers::Prev &V = B.prev;
+    auto pocc_at = [&](size_t i) -> size_t { return i < V.n_ins ? V.occBase[i] : V.nocc; };
+    auto pmeas_at = [&](size_t i) -> uint32_t { return i < V.n_ins ? V.measBase[i] : V.nmeas; };
+    for (uint32_t sg = 0; sg < nseg; ++sg) {
+      const int32_t f = B.plan.from[sg];
+      if (f < 0 || (size_t)f + 1 >= V.cut.size()) continue;
+      const size_t i0 = cut[sg + 1], i1 = cut[sg], j0 = V.cut[f + 1], j1 = V.cut[f];
+      if (i1 - i0 != j1 - j0) continue;
+      const uint32_t m0 = meas_at(i0), m1 = meas_at(i1), pm0 = pmeas_at(j0), pm1 = pmeas_at(j1);
+      if (m1 - m0 != pm1 - pm0) continue;
+      bool ok = true;
+      int64_t db = 0;
+      bool have = false;
+      for (uint32_t k = 0; ok && k < m1 - m0; ++k) {
+        const uint32_t a0 = moff[m0 + k], a1 = moff[m0 + k + 1];
+        const uint32_t b0 = V.moff[pm0 + k], b1 = V.moff[pm0 + k + 1];
+        if (a1 - a0 != b1 - b0) {
+          ok = false;
+          break;
+        }
+        for (uint32_t i = 0; i < a1 - a0; ++i) {
+          const int64_t d = (int64_t)mbits[a0 + i] - (int64_t)V.mbits[b0 + i];
+          if (!have) {
+            db = d;
+            have = true;
+          } else if (d != db) {
+            ok = false;
+            break;
+          }
+        }
+      }
+      int64_t ds = 0;
+      if (ok && opt.sources) {
+        const size_t o0 = occ_at(i0), o1 = occ_at(i1), po0 = pocc_at(j0);
+        if (o1 - o0 != pocc_at(j1) - po0) ok = false;
+        bool hs = false;
+        for (size_t o = 0; ok && o < o1 - o0; ++o) {
+          const uint32_t x = tsrc[o0 + o], y = V.tsrc[po0 + o];
+          if ((x == kNone) != (y == kNone)) {
+            ok = false;
+          } else if (x != kNone) {
+            const int64_t d = (int64_t)x - (int64_t)y;
+            if (!hs) {
+              ds = d;
+              hs = true;
+            } else if (d != ds) {
+              ok = false;
+            }
+          }
+        }
+      }
+      if (!ok) continue;
+      std::swap(B.segs[sg], B.prev.segs[f]);
+      runs[sg] = 0;
+      B.dbits[sg] = db;
+      B.dsrc[sg] = ds;
+      ++S.stats.reused;
+    }
+  }
+  S.stats.segments = nseg;
 
   auto run_segment = [&](uint32_t sg) {
     LowerScratch::Buffers::Segment &G = B.segs[sg];
@@ -793,9 +1086,9 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
     // records: at most three per target occurrence (PAULI_CHANNEL_1), written
     // through pointers into arrays sized to that bound and cut to size after
     const size_t rec_max = socc * 3 + 16;
-    HostArray<uint64_t> &RD = nseg == 1 ? T.rec : G.rec;
-    HostArray<double> &RP = nseg == 1 ? T.rec_p : G.rec_p;
-    HostArray<uint32_t> &RS = nseg == 1 ? T.rec_src : G.rec_src;
+    HostArray<uint64_t> &RD = direct ? T.rec : G.rec;
+    HostArray<double> &RP = direct ? T.rec_p : G.rec_p;
+    HostArray<uint32_t> &RS = direct ? T.rec_src : G.rec_src;
     RD.resize(rec_max);
     RP.resize(rec_max);
     RS.resize(opt.sources ? rec_max : 0);
@@ -994,11 +1287,47 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
       G.fine[q] = st[q].fine;
       G.coarse[q] = st[q].coarse;
     }
+    if (opt.incremental) {  // kept for a later circuit that takes this segment over
+      G.mlo.assign(measLo.begin() + meas_at(i0), measLo.begin() + meas_at(i1));
+      G.mhi.assign(measHi.begin() + meas_at(i0), measHi.begin() + meas_at(i1));
+    }
+  };
+  // A segment taken over: shift its detector bits (the OP_M operand and the
+  // OP_INJ bits) and its sources, and place its measurements' epochs.
+  auto take_segment = [&](uint32_t sg) {
+    LowerScratch::Buffers::Segment &G = B.segs[sg];
+    const int64_t db = B.dbits[sg], ds = B.dsrc[sg];
+    if (db) {
+      Entry *const ent0 = G.ent.p.get();
+      for (size_t i = 0; i < G.nent; ++i) {
+        uint64_t &op = ent0[i].op;
+        const uint32_t opc = (uint32_t)(op & 0xFF);
+        if (opc == OP_M) {
+          const uint32_t b = (uint32_t)(op >> 32);
+          if (b != kNone) op = (op & 0xFFFFFFFFull) | ((uint64_t)(uint32_t)((int64_t)b + db) << 32);
+        } else if (opc == OP_INJ) {
+          const uint32_t b1 = (uint32_t)(op >> 32), b2 = (uint32_t)(op >> 8) & 0xFFFFFFu;
+          op = make_inj((uint32_t)((int64_t)b1 + db), b2 == 0xFFFFFFu ? b2 : (uint32_t)((int64_t)b2 + db));
+        }
+      }
+    }
+    if (ds && opt.sources)
+      for (size_t i = 0; i < G.nrec; ++i)
+        if (G.rec_src[i] != kNone) G.rec_src[i] = (uint32_t)((int64_t)G.rec_src[i] + ds);
+    const uint32_t a = meas_at(cut[sg + 1]);
+    std::copy(G.mlo.begin(), G.mlo.end(), measLo.begin() + a);
+    std::copy(G.mhi.begin(), G.mhi.end(), measHi.begin() + a);
+  };
+  auto segment_job = [&](uint32_t sg) {
+    if (runs[sg])
+      run_segment(sg);
+    else
+      take_segment(sg);
   };
   if (pool && nseg > 1)
-    pool->run(nseg, [&](uint32_t sg, uint32_t) { run_segment(sg); });
+    pool->run(nseg, [&](uint32_t sg, uint32_t) { segment_job(sg); });
   else
-    for (uint32_t sg = 0; sg < nseg; ++sg) run_segment(sg);
+    for (uint32_t sg = 0; sg < nseg; ++sg) segment_job(sg);
 
   // stitch: offsets of each segment's epochs, points and records in walk order
   std::vector<uint32_t> &ep_k = T.ep_k;
@@ -1187,7 +1516,7 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
     mm += B.segs[s].ncomp;
   }
   if (mm >= 0xFFFFFFFFull) throw Error(GPC_ERR_CAPACITY, "too many error mechanisms");
-  if (nseg > 1) {  // one segment wrote its records in place
+  if (!direct) {  // (one segment wrote its records in place)
     T.rec.resize(R);
     T.rec_p.resize(R);
     T.rec_src.resize(opt.sources ? R : 0);
@@ -1195,7 +1524,7 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
   T.rec_moff.resize(R + 1);
   auto place_records = [&](uint32_t sg, uint32_t) {
     const LowerScratch::Buffers::Segment &G = B.segs[sg];
-    const uint64_t *const src = nseg == 1 ? T.rec.data() : G.rec.data();
+    const uint64_t *const src = direct ? T.rec.data() : G.rec.data();
     uint64_t *const dst = T.rec.data() + G.roff;
     uint32_t *const mo = T.rec_moff.data() + G.roff;
     uint64_t m0 = G.moff0;
@@ -1210,7 +1539,7 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
       mo[i] = (uint32_t)m0;
       m0 += kRecComps[type];
     }
-    if (nseg > 1 && G.nrec) {
+    if (!direct && G.nrec) {
       memcpy(T.rec_p.data() + G.roff, G.rec_p.data(), G.nrec * 8);
       if (opt.sources) memcpy(T.rec_src.data() + G.roff, G.rec_src.data(), G.nrec * 4);
     }
@@ -1231,6 +1560,16 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
       if (T.inj_lo[j] == kNone || measLo[k] < T.inj_lo[j]) T.inj_lo[j] = measLo[k];
       if (T.inj_hi[j] == kNone || measHi[k] > T.inj_hi[j]) T.inj_hi[j] = measHi[k];
     }
+  }
+  if (opt.incremental) {
+    LowerScratch::Buffers::Prev &V = B.prev;
+    V.n_ins = P.ins.size();
+    V.nocc = occ;
+    V.nmeas = m;
+    V.nq = nq;
+    V.kcap = kcap;
+    V.level = opt.level;
+    V.sources = opt.sources;
   }
 }
 

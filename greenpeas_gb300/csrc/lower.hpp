@@ -122,9 +122,18 @@ struct Instr {
 };
 constexpr uint8_t kAnyRec = 1, kAllRec = 2, kAnyPau = 4, kAllPau = 8;
 
+// A top-level statement that opens its line: the text offset of the line,
+// its line number, and the instructions and targets parsed before it.
+struct ParseMark {
+  size_t off, line, ins, tpos;
+};
+
 struct Parsed {
   std::vector<Instr> ins;
   HostArray<uint32_t> pool;  // targets of every instruction (a REPEAT body's once)
+  bool want_marks = false;   // record `marks` (the incremental lowering reads them)
+  std::vector<ParseMark> marks;
+  size_t end_line = 1;       // line number at the end of the text
 };
 
 // Parses stim circuit text, flattening REPEAT blocks.  Throws gpc::Error.
@@ -262,6 +271,16 @@ struct LowerOptions {
   // one is given; each cut adds at most about one epoch to the walk.  The
   // DEM does not depend on it.
   uint32_t segment_occ = 16384;
+  // Keep this circuit's parse and time segments in the scratch, and lower the
+  // next circuit of the same scratch against them: only the statements that
+  // differ are parsed again, and a time segment whose instructions are
+  // unchanged is scheduled again only if its measurements' detector bits or
+  // its noise sources changed other than by one common shift (see
+  // lower_text).  The tape equals a full lowering with the same segment cuts.
+  bool incremental = false;
+  // Cut the backward pass at these instruction indices (descending, from the
+  // instruction count to 0) instead of by segment_occ.
+  const std::vector<size_t> *cuts = nullptr;
 };
 
 // Shared-memory plan of the walk kernel (bytes): double-buffered tape chunks,
@@ -291,6 +310,17 @@ struct LowerScratch {
   std::vector<Parsed> pieces;  // a text parsed in pieces on several threads
   struct Buffers;
   std::unique_ptr<Buffers> b;
+  // The last lowering: its time segments (the backward pass's cuts,
+  // descending instruction indices), how many were taken over from the
+  // lowering before it, and how many text bytes were parsed.
+  struct Stats {
+    bool incremental = false;  // lowered against the scratch's previous circuit
+    uint32_t segments = 0, reused = 0;
+    size_t parsed_bytes = 0;
+  } stats;
+  const std::vector<size_t> &last_cuts() const;
+  // Forget the previous circuit (the next incremental lowering is a full one).
+  void forget();
 };
 // lower() into T (reset first), with S's buffers; a large tape is assembled
 // in pieces on `pool`'s threads when a pool is given.

@@ -12,39 +12,121 @@ struct gpc_tape {
   gpc::Tape t;
 };
 
+struct gpc_lowerer {
+  gpc::LowerOptions lo;
+  gpc::LowerScratch scratch;
+};
+
 namespace {
 thread_local std::string g_tape_error;
-}
 
-extern "C" {
-
-gpc_status gpc_tape_lower(const char *stim_text, size_t len, int32_t correlation_level, gpc_tape **out) {
-  if (!out || !stim_text) return GPC_ERR_INVALID;
-  *out = nullptr;
+template <typename F>
+gpc_status tape_guarded(F &&f) {
   try {
-    gpc::LowerOptions lo;
-    lo.level = correlation_level;
-    lo.segment_occ = 8192;  // as a compile lowers it
-    std::unique_ptr<gpc_tape> t(new gpc_tape{});
-    gpc::LowerScratch scratch;
-    if (len >= 64 * 1024) {  // a large text is parsed in pieces, as the compile path does
-      gpc::HostPool pool(3);
-      gpc::lower_text(stim_text, len, lo, t->t, scratch, &pool);
-    } else {
-      gpc::lower_text(stim_text, len, lo, t->t, scratch);
-    }
-    *out = t.release();
+    f();
     return GPC_OK;
   } catch (const gpc::Error &e) {
     g_tape_error = e.what();
     return e.code;
   } catch (const std::bad_alloc &) {
+    g_tape_error = "host allocation failed";
     return GPC_ERR_OOM;
   } catch (const std::exception &e) {
     g_tape_error = e.what();
     return GPC_ERR_INVALID;
   }
 }
+
+// A lowering as a compile does it: a large text is parsed in pieces on a pool.
+void lower_like_compile(const char *text, size_t len, const gpc::LowerOptions &lo, gpc::Tape &T,
+                        gpc::LowerScratch &scratch) {
+  if (len >= 64 * 1024) {
+    gpc::HostPool pool(3);
+    gpc::lower_text(text, len, lo, T, scratch, &pool);
+  } else {
+    gpc::lower_text(text, len, lo, T, scratch);
+  }
+}
+}  // namespace
+
+extern "C" {
+
+gpc_status gpc_tape_lower(const char *stim_text, size_t len, int32_t correlation_level, gpc_tape **out) {
+  if (!out || !stim_text) return GPC_ERR_INVALID;
+  *out = nullptr;
+  return tape_guarded([&] {
+    gpc::LowerOptions lo;
+    lo.level = correlation_level;
+    lo.segment_occ = 8192;  // as a compile lowers it
+    std::unique_ptr<gpc_tape> t(new gpc_tape{});
+    gpc::LowerScratch scratch;
+    lower_like_compile(stim_text, len, lo, t->t, scratch);
+    *out = t.release();
+  });
+}
+
+gpc_status gpc_tape_lower_cuts(const char *stim_text, size_t len, int32_t correlation_level, const uint64_t *cuts,
+                               uint32_t ncuts, gpc_tape **out) {
+  if (!out || !stim_text || (ncuts && !cuts)) return GPC_ERR_INVALID;
+  *out = nullptr;
+  return tape_guarded([&] {
+    std::vector<size_t> c(cuts, cuts + ncuts);
+    gpc::LowerOptions lo;
+    lo.level = correlation_level;
+    lo.segment_occ = 8192;
+    lo.cuts = &c;
+    std::unique_ptr<gpc_tape> t(new gpc_tape{});
+    gpc::LowerScratch scratch;
+    gpc::lower_text(stim_text, len, lo, t->t, scratch);
+    *out = t.release();
+  });
+}
+
+gpc_status gpc_lowerer_create(int32_t correlation_level, int32_t incremental, gpc_lowerer **out) {
+  if (!out) return GPC_ERR_INVALID;
+  *out = nullptr;
+  if (correlation_level < 0 || correlation_level > 2) {
+    g_tape_error = "correlation level must be 0, 1 or 2";
+    return GPC_ERR_INVALID;
+  }
+  return tape_guarded([&] {
+    std::unique_ptr<gpc_lowerer> lw(new gpc_lowerer{});
+    lw->lo.level = correlation_level;
+    lw->lo.segment_occ = 8192;  // as a compile lowers it
+    lw->lo.incremental = incremental != 0;
+    *out = lw.release();
+  });
+}
+
+gpc_status gpc_lowerer_lower(gpc_lowerer *lowerer, const char *stim_text, size_t len, gpc_tape **out) {
+  if (!lowerer || !out || !stim_text) return GPC_ERR_INVALID;
+  *out = nullptr;
+  return tape_guarded([&] {
+    std::unique_ptr<gpc_tape> t(new gpc_tape{});
+    lower_like_compile(stim_text, len, lowerer->lo, t->t, lowerer->scratch);
+    *out = t.release();
+  });
+}
+
+gpc_status gpc_lowerer_stats(const gpc_lowerer *lowerer, gpc_lower_stats *stats, uint64_t *cuts, uint32_t cap,
+                             uint32_t *ncuts) {
+  if (!lowerer || (cap && !cuts)) return GPC_ERR_INVALID;
+  const gpc::LowerScratch &S = lowerer->scratch;
+  if (stats) {
+    stats->incremental = S.stats.incremental ? 1u : 0u;
+    stats->segments = S.stats.segments;
+    stats->reused = S.stats.reused;
+    stats->reserved = 0;
+    stats->parsed_bytes = S.stats.parsed_bytes;
+  }
+  const std::vector<size_t> &c = S.last_cuts();
+  if (ncuts) *ncuts = (uint32_t)c.size();
+  if (c.size() > cap) return cap ? GPC_ERR_CAPACITY : GPC_OK;
+  for (size_t i = 0; i < c.size(); ++i) cuts[i] = c[i];
+  return GPC_OK;
+}
+
+void gpc_lowerer_free(gpc_lowerer *lowerer) { delete lowerer; }
 
 const char *gpc_tape_last_error(void) { return g_tape_error.c_str(); }
 

@@ -142,7 +142,10 @@ class Driver:
                  device: int = 0, sort_bits: int = 0, global_sort: bool = False, walk_qpt: int = 0,
                  bucket_mean: int = 0, walk_words: int = 0, key_split: int = 0, walk_queue: int = 0,
                  walk_segment: int = 0, wait_limit_us: int = 0, test_hold_tile: int = 0,
-                 test_fail_alloc: int = 0, heap_results: bool = False):
+                 test_fail_alloc: int = 0, heap_results: bool = False, incremental: bool = False):
+        """``incremental``: lower each circuit against the previous one of its lowering thread
+        (branches of one circuit re-parse only the statements that differ and reschedule only the
+        time segments those change; see ``Lowerer``).  The DEMs are the same."""
         L = _native.lib()
         self._h = ctypes.c_void_p()
         self.correlation_level = CorrelationLevel(correlation_level)
@@ -161,6 +164,7 @@ class Driver:
         opts.test_hold_tile = test_hold_tile
         opts.test_fail_alloc = test_fail_alloc
         opts.heap_results = 1 if heap_results else 0
+        opts.incremental = 1 if incremental else 0
         text = _text(circuit)
         _native.check(L.gpc_get_driver(text, len(text), int(self.correlation_level), ctypes.byref(opts),
                                        ctypes.byref(self._h)))
@@ -363,13 +367,30 @@ def get_driver(circuit, correlation_level: CorrelationLevel = CorrelationLevel.L
 class Tape:
     """The lowered device tape of a circuit, as numpy arrays (host only, no GPU)."""
 
-    def __init__(self, circuit, correlation_level: int = 2, segment_target: int | None = None):
+    def __init__(self, circuit, correlation_level: int = 2, segment_target: int | None = None, cuts=None):
         """``segment_target``: also set ``walk_bounds``, the epoch boundaries a single-circuit
-        compile cuts the walk at for that segment cost (slots + 2 per epoch)."""
+        compile cuts the walk at for that segment cost (slots + 2 per epoch).  ``cuts``: cut the
+        backward pass at these instruction indices (descending, from the instruction count to 0)."""
         L = _native.lib()
         h = ctypes.c_void_p()
         text = _text(circuit)
-        _native.check(L.gpc_tape_lower(text, len(text), int(correlation_level), ctypes.byref(h)), tape=True)
+        if cuts is None:
+            _native.check(L.gpc_tape_lower(text, len(text), int(correlation_level), ctypes.byref(h)), tape=True)
+        else:
+            c = (ctypes.c_uint64 * len(cuts))(*[int(x) for x in cuts])
+            _native.check(L.gpc_tape_lower_cuts(text, len(text), int(correlation_level), c, len(cuts),
+                                                ctypes.byref(h)), tape=True)
+        self._load(h, segment_target)
+
+    @classmethod
+    def _from_handle(cls, h, segment_target=None) -> "Tape":
+        t = cls.__new__(cls)
+        t._load(h, segment_target)
+        return t
+
+    def _load(self, h, segment_target) -> None:
+        """Copies the tape's arrays out of the gpc_tape `h` and frees it."""
+        L = _native.lib()
         try:
             v = _native.TapeView()
             _native.check(L.gpc_tape_get_view(h, ctypes.byref(v)), tape=True)
@@ -399,3 +420,54 @@ class Tape:
                 self.walk_bounds = np.array(buf[: n.value], dtype=np.int64)
         finally:
             L.gpc_tape_free(h)
+
+
+class Lowerer:
+    """Lowers circuit after circuit, each against the one before it (host only, no GPU).
+
+    With ``incremental`` the statements between the two texts' common prefix and suffix are
+    parsed again, and a time segment of the backward pass over unchanged statements is taken
+    over unless its measurements' detector bits or its noise sources changed other than by one
+    shift (gpc_lowerer_create).  Every tape equals ``Tape(circuit, cuts=lowerer.cuts)``.
+    """
+
+    def __init__(self, correlation_level: int = 2, incremental: bool = True):
+        self._h = ctypes.c_void_p()
+        _native.check(_native.lib().gpc_lowerer_create(int(correlation_level), 1 if incremental else 0,
+                                                       ctypes.byref(self._h)), tape=True)
+
+    def tape(self, circuit, segment_target: int | None = None) -> Tape:
+        h = ctypes.c_void_p()
+        text = _text(circuit)
+        _native.check(_native.lib().gpc_lowerer_lower(self._h, text, len(text), ctypes.byref(h)), tape=True)
+        return Tape._from_handle(h, segment_target)
+
+    @property
+    def stats(self) -> dict:
+        """The last lowering: incremental (lowered against the previous circuit), segments,
+        reused (segments taken over), parsed_bytes."""
+        st = _native.LowerStats()
+        _native.check(_native.lib().gpc_lowerer_stats(self._h, ctypes.byref(st), None, 0, None), tape=True)
+        return {"incremental": bool(st.incremental), "segments": int(st.segments), "reused": int(st.reused),
+                "parsed_bytes": int(st.parsed_bytes)}
+
+    @property
+    def cuts(self) -> np.ndarray:
+        """The last lowering's backward-pass cuts (descending instruction indices)."""
+        L = _native.lib()
+        n = ctypes.c_uint32()
+        _native.check(L.gpc_lowerer_stats(self._h, None, None, 0, ctypes.byref(n)), tape=True)
+        buf = (ctypes.c_uint64 * n.value)()
+        _native.check(L.gpc_lowerer_stats(self._h, None, buf, n.value, ctypes.byref(n)), tape=True)
+        return np.array(buf[: n.value], dtype=np.int64)
+
+    def close(self) -> None:
+        if getattr(self, "_h", None) is not None and self._h.value:
+            _native.lib().gpc_lowerer_free(self._h)
+        self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

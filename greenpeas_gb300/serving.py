@@ -27,9 +27,10 @@ __all__ = ["Server", "replay"]
 
 class Server:
     def __init__(self, slots: int = 4, max_batch: int = 16, hbm_budget: int = 120 << 30, correlation_level: int = 2,
-                 device: int = 0, lower_threads: int = 0):
+                 device: int = 0, lower_threads: int = 0, incremental: bool = False):
         o = _native.ServerOptions(device=device, correlation_level=int(correlation_level), slots=slots,
-                                  max_batch=max_batch, hbm_budget=int(hbm_budget), lower_threads=lower_threads)
+                                  max_batch=max_batch, hbm_budget=int(hbm_budget), lower_threads=lower_threads,
+                                  incremental=1 if incremental else 0)
         h = ctypes.c_void_p()
         _native.check(_native.lib().gpc_server_create(ctypes.byref(o), ctypes.byref(h)))
         self._h = h

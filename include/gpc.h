@@ -80,6 +80,10 @@ typedef struct gpc_options {
   int32_t heap_results;    /* 1: DEM arrays are heap copies out of a staging buffer; 0: the device copies
                               them into page-locked memory the DEM keeps (a single circuit's own arrays, a
                               batch's shared result block), while a 4 GiB page-locked pool reaches */
+  int32_t incremental;     /* 1: lower each circuit against the previous one its lowering thread lowered
+                              (branches of one circuit): only the statements that differ are parsed again,
+                              and only the time segments they change are scheduled again (see
+                              gpc_lowerer_create); the DEM is the same.  0: every circuit is lowered whole */
 } gpc_options;
 
 /* Parses `stim_text` (length `len`), sizes device buffers for it and returns
@@ -230,7 +234,9 @@ typedef struct gpc_server_options {
   uint64_t hbm_budget;       /* device bytes all workers' buffers may hold, default 120 GiB */
   uint32_t lower_threads;    /* host threads lowering requests as they arrive (0 = the cores left after one per
                                 slot, plus one: workers sleep while their batch runs) */
-  uint32_t reserved[3];
+  uint32_t incremental;      /* 1: each lowering thread lowers a request against the previous one it lowered
+                                (as gpc_options.incremental) */
+  uint32_t reserved[2];
 } gpc_server_options;
 gpc_status gpc_server_create(const gpc_server_options *options, gpc_server **out);
 gpc_status gpc_server_submit(gpc_server *server, const char *stim_text, size_t len, uint64_t *ticket);
@@ -389,8 +395,41 @@ gpc_status gpc_tape_get_view(const gpc_tape *tape, gpc_tape_view *view);
 gpc_status gpc_tape_walk_segments(const gpc_tape *tape, uint32_t target, uint32_t *bounds, uint32_t cap,
                                   uint32_t *n);
 void gpc_tape_free(gpc_tape *tape);
-/* Thread-local message of the last gpc_tape_lower failure. */
+/* Thread-local message of the last gpc_tape_lower (or gpc_tape_lower_cuts,
+ * gpc_lowerer_lower) failure. */
 const char *gpc_tape_last_error(void);
+/* The tape of a lowering whose backward pass is cut at `cuts` (instruction
+ * indices of the flattened circuit, descending from its instruction count to
+ * 0) instead of by its default segment size. */
+gpc_status gpc_tape_lower_cuts(const char *stim_text, size_t len, int32_t correlation_level, const uint64_t *cuts,
+                               uint32_t ncuts, gpc_tape **out);
+
+/* Incremental lowering (no counterpart in the reference; host only).  A
+ * lowerer keeps the last circuit it lowered.  With `incremental` != 0 it
+ * lowers the next circuit against it: the statements between the two texts'
+ * longest common prefix and suffix (whole top-level statements) are parsed
+ * again and spliced between the kept ones; the backward pass keeps the
+ * previous cuts outside that span, and a time segment over unchanged
+ * statements is taken over, not scheduled again, when its measurements'
+ * detector bits and its noise targets' sources equal the previous ones up
+ * to one shift each (a span that adds rounds shifts the detectors and ticks
+ * after it).  The tape equals gpc_tape_lower_cuts of the same text with the
+ * same cuts, byte for byte.  A changed span over more than half of the text
+ * is lowered whole.
+ *   gpc_lowerer_lower  the tape of a circuit (owned by the caller)
+ *   gpc_lowerer_stats  the last lowering: whether it was incremental, its
+ *                      segments, those taken over, the text bytes parsed;
+ *                      and its cuts (written when *ncuts <= cap) */
+typedef struct gpc_lowerer gpc_lowerer;
+typedef struct gpc_lower_stats {
+  uint32_t incremental, segments, reused, reserved;
+  uint64_t parsed_bytes;
+} gpc_lower_stats;
+gpc_status gpc_lowerer_create(int32_t correlation_level, int32_t incremental, gpc_lowerer **out);
+gpc_status gpc_lowerer_lower(gpc_lowerer *lowerer, const char *stim_text, size_t len, gpc_tape **out);
+gpc_status gpc_lowerer_stats(const gpc_lowerer *lowerer, gpc_lower_stats *stats, uint64_t *cuts, uint32_t cap,
+                             uint32_t *ncuts);
+void gpc_lowerer_free(gpc_lowerer *lowerer);
 
 #ifdef __cplusplus
 }
