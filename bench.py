@@ -14,7 +14,7 @@ Lines printed (one JSON line on rank 0):
             between steps (a 512 MiB write, outside the timed window).
   e2e    -- the same metric through the C ABI from host text to host DEM
             arrays (parse + lowering + H2D + kernels + D2H), wall clock.
-  roofline, cpu_baseline, clocks, gpu_launches, batch, grad, serve -- see main().
+  roofline, cpu_baseline, clocks, gpu_launches, batch, grad, branches, serve -- see main().
 
 ``--impl reference`` times the CPU FP64 oracle (a restatement of the
 reference's algorithm; the reference itself has no CPU path) for the same
@@ -444,6 +444,51 @@ def sweep_entry(r: dict) -> dict:
             "fallbacks": r["fallbacks"]}
 
 
+def branches_leg(gp, local: int, n_batch: int = 256, reps: int = 3) -> dict:
+    """Branches of the headline circuit (256 distinct basis-switch branches of BB [[144,12,12]] r=12,
+    ``workloads.branches``) compiled in batches of 256, end to end (host text in, DEM arrays out), by
+    a driver that lowers each circuit whole and by one whose host threads lower each circuit against
+    the previous one they lowered (``incremental``).  Host lowering alone (one thread, ``Lowerer``)
+    is timed beside them, with the share of time segments taken over and of text parsed again.  The
+    DEMs of both drivers are compared."""
+    from greenpeas_gb300.workloads import branches
+    texts = branches(n_batch)
+    out = {"workload": "bb_144_12_12_r12_uniform_p1e-3, 256 basis-switch branches (seed 5)", "circuits": len(texts)}
+    for mode in (False, True):  # one host thread, lowering only
+        lw = gp.Lowerer(2, incremental=mode)
+        for t in texts[:4]:
+            lw.lower(t)
+        reused = segs = parsed = 0
+        t0 = time.perf_counter()
+        for t in texts:
+            lw.lower(t)
+            st = lw.stats
+            reused += st["reused"]
+            segs += st["segments"]
+            parsed += st["parsed_bytes"]
+        dt = time.perf_counter() - t0
+        lw.close()
+        out["lowering_" + ("incremental" if mode else "whole")] = {
+            "ms_per_circuit": 1e3 * dt / len(texts), "segments_reused": reused / max(segs, 1),
+            "text_parsed": parsed / sum(len(t) for t in texts), "threads": 1}
+    dems = {}
+    for mode in (False, True):
+        key = "incremental" if mode else "whole"
+        drv = gp.get_driver(texts[0], device=local, incremental=mode)
+        drv.compile_batch(texts)  # warm: buffers sized, graphs captured, lowering state kept
+        t0 = time.perf_counter()
+        for _ in range(reps):
+            dems[key] = drv.compile_batch(texts)
+        dt = (time.perf_counter() - t0) / reps
+        out[key] = {"batch_e2e": {"value": len(texts) / dt, "unit": UNIT, "ms_per_batch": 1e3 * dt}}
+        del drv
+    out["same_order"] = all(dem_arrays_equal(a, b) for a, b in zip(dems["whole"], dems["incremental"]))
+    out["same_dems"] = all(a.canonical() == b.canonical() for a, b in zip(dems["whole"][:8], dems["incremental"][:8]))
+    out["speedup"] = {"batch_e2e": out["incremental"]["batch_e2e"]["value"] / out["whole"]["batch_e2e"]["value"],
+                      "lowering": out["lowering_whole"]["ms_per_circuit"] / out["lowering_incremental"]["ms_per_circuit"]}
+    return out
+
+
 def batch_workload_texts(circuits: int) -> list:
     from greenpeas_gb300.workloads import batch_surface
     return batch_surface()[:circuits]
@@ -612,6 +657,7 @@ def main() -> None:
                     help="profiling: one circuit on the global (onesweep sort) merge path, timed alone")
     ap.add_argument("--no-serve", action="store_true", help="skip the serving leg")
     ap.add_argument("--no-grad", action="store_true", help="skip the noise-rate gradient leg")
+    ap.add_argument("--no-branches", action="store_true", help="skip the incremental-lowering leg")
     ap.add_argument("--no-sweep", action="store_true", help="skip the plain-method configuration sweep")
     ap.add_argument("--serve-requests", type=int, default=10000)
     ap.add_argument("--serve-slots", type=int, default=4)
@@ -736,6 +782,8 @@ def main() -> None:
                                     device_only=args.batch_device_only)
     if not args.no_grad and world == 1:
         line["grad"] = grad_leg(gp, torch, fd_entries=64)
+    if not args.no_branches and world == 1:
+        line["branches"] = branches_leg(gp, local)
     if not args.no_serve and world == 1:
         # capacity from a burst long enough that filling and draining the
         # pipeline is a small part of it (1,000 requests: ~0.2 s, 5-15% low)

@@ -999,7 +999,11 @@ struct gpc_driver {
     // (measured on GB300 + Grace: bb12 end to end 0.41 -> 0.36 ms; a batch's lowering, one
     // circuit per thread, 17.3 -> 16.8 ms)
     lo.segment_occ = 8192;
-    lo.incremental = incremental;
+    // batches: each pool thread lowers its circuits against the previous one it lowered.  A single
+    // circuit is lowered whole, on the pool: its parse and segments run side by side, while an
+    // incremental lowering's text comparison and forward pass run on one thread (a bb12 branch:
+    // 0.16 ms whole on the pool, about twice that incremental)
+    lo.incremental = incremental && n > 1;
     gpc::HostPool &hp = host_pool();
     if (lower_scratch.size() < hp.workers() + 1) lower_scratch.resize(hp.workers() + 1);
     resize_tapes(n);

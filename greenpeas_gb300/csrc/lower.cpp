@@ -357,6 +357,11 @@ struct QState {
   }
 };
 
+// A run of equal lines of two texts: a[a, a + n) equals b[b, b + n).
+struct Run {
+  size_t a, b, n;
+};
+
 // Memoises the last split so uniform noise costs one sqrt/pow per distinct p.
 struct SplitCache {
   double p1 = -1, s1 = 0, p2 = -1, s2 = 0;
@@ -509,7 +514,12 @@ struct LowerScratch::Buffers {
     std::vector<size_t> cut;
     std::vector<int32_t> from;
   } plan;
-  Parsed mid;  // the statements parsed again
+  Parsed next;               // the new parse, assembled
+  std::vector<Parsed> gaps;  // the statements parsed again
+  std::vector<size_t> la, lb;
+  std::vector<uint64_t> ha, hb;
+  std::vector<long> vbuf, trace;
+  std::vector<Run> runs_;
   std::vector<uint32_t> runs;  // segments scheduled by this lowering
   std::vector<int64_t> dbits, dsrc;  // per reused segment: shift of its detector bits and sources
 };
@@ -580,11 +590,95 @@ void parse_stim_pieces(const char *text, size_t len, Parsed &out, std::vector<Pa
 
 namespace {
 
-// Lowers `text` against the previous circuit of S (incremental lowering):
-// re-parses the statements between the longest common prefix and suffix of
-// the two texts into S.parsed, and plans the backward pass's cuts so that
-// the previous segments over unchanged statements can be taken over.
-// Returns false (S.parsed untouched) when a full lowering is the better way.
+// Hash of one line's bytes (8 at a time, multiply-xorshift mixing); lines
+// with equal hashes are compared byte for byte before they are trusted.
+inline uint64_t line_hash(const char *p, size_t n) {
+  uint64_t h = 0x9E3779B97F4A7C15ull ^ (uint64_t)n;
+  size_t i = 0;
+  for (; i + 8 <= n; i += 8) {
+    uint64_t w;
+    memcpy(&w, p + i, 8);
+    h = (h ^ w) * 0xFF51AFD7ED558CCDull;
+    h ^= h >> 32;
+  }
+  uint64_t w = 0;
+  memcpy(&w, p + i, n - i);
+  h = (h ^ w) * 0xC4CEB9FE1A85EC53ull;
+  return h ^ (h >> 29);
+}
+
+// Line starts of text[a, b) (b is a line start or the end of the text), plus b.
+void line_starts(const char *text, size_t a, size_t b, std::vector<size_t> &out) {
+  out.clear();
+  for (size_t x = a; x < b;) {
+    out.push_back(x);
+    const void *nl = memchr(text + x, '\n', b - x);
+    x = nl ? (size_t)(static_cast<const char *>(nl) - text) + 1 : b;
+  }
+  out.push_back(b);
+}
+
+// The common runs of the sequences a[0, n) and b[0, m) along a shortest edit
+// script (Myers' greedy O((n + m) D) algorithm, "An O(ND) difference
+// algorithm and its variations", 1986), in order.  False when the script
+// needs more than dmax insertions and deletions, or the search more than
+// `budget` steps (texts that differ throughout are given up on early).
+// Round d's furthest reaching x on diagonals -d..d is kept at
+// trace[d * d + d + k] for the walk back.
+bool diff_runs(const uint64_t *a, long n, const uint64_t *b, long m, long dmax, long budget, std::vector<long> &vbuf,
+               std::vector<long> &trace, std::vector<Run> &runs) {
+  const long off = dmax + 1;
+  long work = 0;
+  vbuf.assign((size_t)(2 * dmax + 3), 0);
+  long *V = vbuf.data();
+  trace.clear();
+  long dfound = -1;
+  for (long d = 0; d <= dmax && dfound < 0; ++d) {
+    for (long k = -d; k <= d; k += 2) {
+      long x = (k == -d || (k != d && V[off + k - 1] < V[off + k + 1])) ? V[off + k + 1] : V[off + k - 1] + 1;
+      long y = x - k;
+      const long x0 = x;
+      while (x < n && y < m && a[x] == b[y]) {
+        ++x;
+        ++y;
+      }
+      work += 1 + (x - x0);
+      if (work > budget) return false;
+      V[off + k] = x;
+      if (x >= n && y >= m) {
+        dfound = d;
+        break;
+      }
+    }
+    trace.insert(trace.end(), V + off - d, V + off + d + 1);
+  }
+  if (dfound < 0) return false;
+  runs.clear();
+  long x = n, y = m;
+  for (long d = dfound; d > 0; --d) {
+    const long *P = trace.data() + (d - 1) * (d - 1) + (d - 1);  // P[k]: round d - 1, diagonal k
+    const long k = x - y;
+    const long pk = (k == -d || (k != d && P[k - 1] < P[k + 1])) ? k + 1 : k - 1;
+    const long px = P[pk], py = px - pk;
+    const long xs = pk == k + 1 ? px : px + 1;  // after the insertion (down) or the deletion (right)
+    if (x > xs) runs.push_back({(size_t)xs, (size_t)(xs - k), (size_t)(x - xs)});
+    x = px;
+    y = py;
+  }
+  if (x > 0) runs.push_back({0, 0, (size_t)x});
+  std::reverse(runs.begin(), runs.end());
+  return true;
+}
+
+// Lowers `text` against the previous circuit of S (incremental lowering).
+// The two texts are compared line by line (their common prefix and suffix
+// first, then a shortest edit script of the lines between).  Runs of equal
+// lines, shrunk to whole top-level statements, keep their parsed
+// instructions; the statements between them are parsed again; S.parsed
+// becomes the new circuit's parse.  The backward pass keeps the previous
+// cuts of every segment that lies within one unchanged run (its
+// instructions shifted) and cuts the rest afresh.  Returns false (S.parsed
+// untouched) when a full lowering is the better way.
 bool plan_incremental(const char *text, size_t len, const LowerOptions &opt, LowerScratch &S) {
   LowerScratch::Buffers &B = *S.b;
   const LowerScratch::Buffers::Prev &V = B.prev;
@@ -593,94 +687,206 @@ bool plan_incremental(const char *text, size_t len, const LowerOptions &opt, Low
     return false;
   const char *o = V.text.data();
   const size_t on = V.text.size(), mn = std::min(on, len);
+  const size_t nI0 = P.ins.size(), nT0 = P.pool.size();
+  if (2 * mn < std::max(on, len)) return false;  // one text more than twice the other: not a branch of it
   size_t lp = 0;
   while (lp < mn && o[lp] == text[lp]) ++lp;
   size_t ls = 0;
   while (ls < mn - lp && o[on - 1 - ls] == text[len - 1 - ls]) ++ls;
-  const std::vector<ParseMark> &mk = P.marks;
-  // the statement holding the first changed byte: the last mark at or before it
-  size_t k = (size_t)(std::upper_bound(mk.begin(), mk.end(), lp,
-                                       [](size_t v, const ParseMark &x) { return v < x.off; }) - mk.begin());
-  const ParseMark a = k ? mk[k - 1] : ParseMark{0, 1, 0, 0};
-  const size_t ka = k ? k - 1 : 0;  // marks kept before the changed span
-  // the first statement after the last changed byte whose line starts inside
-  // the common suffix (so the byte before it, a newline, is common too)
-  const size_t need = on - ls + 1;
-  const size_t kb = (size_t)(std::lower_bound(mk.begin(), mk.end(), need,
-                                              [](const ParseMark &x, size_t v) { return x.off < v; }) - mk.begin());
-  const ParseMark b = kb < mk.size() ? mk[kb] : ParseMark{on, P.end_line, P.ins.size(), P.pool.size()};
-  if (b.off < a.off || b.ins < a.ins || b.tpos < a.tpos) return false;
-  const size_t bn = b.off + len - on;  // where that statement starts in the new text
-  if (bn < a.off || bn > len || (bn > 0 && bn < len && text[bn - 1] != '\n')) return false;
-  // a changed span of more than half the text: parse and lower it whole
-  if (2 * (bn - a.off) > len) return false;
-  Parsed &M = B.mid;
-  M.want_marks = true;
-  try {
-    parse_stim_into(text + a.off, bn - a.off, M);
-  } catch (const Error &) {
-    return false;  // (a full parse reports the error with its line in the whole text)
-  }
-  // splice: instructions, targets and marks of [0, a) + the new span + [b, end)
-  const size_t nI0 = P.ins.size(), nT0 = P.pool.size();
-  const size_t nI = a.ins + M.ins.size() + (nI0 - b.ins), nT = a.tpos + M.pool.size() + (nT0 - b.tpos);
-  if (nT > 0xFFFFFFFFull) return false;
-  const size_t sufI = nI0 - b.ins, sufT = nT0 - b.tpos;
-  const size_t newB_I = a.ins + M.ins.size(), newB_T = a.tpos + M.pool.size();
-  if (nI > nI0) P.ins.resize(nI);
-  if (sufI) memmove(P.ins.data() + newB_I, P.ins.data() + b.ins, sufI * sizeof(Instr));
-  if (nI < nI0) P.ins.resize(nI);
-  if (nT > nT0) P.pool.resize(nT);
-  if (sufT) memmove(P.pool.data() + newB_T, P.pool.data() + b.tpos, sufT * sizeof(uint32_t));
-  if (nT < nT0) P.pool.resize(nT);
-  if (!M.pool.empty()) memcpy(P.pool.data() + a.tpos, M.pool.data(), M.pool.size() * sizeof(uint32_t));
-  for (size_t i = 0; i < M.ins.size(); ++i) {
-    P.ins[a.ins + i] = M.ins[i];
-    P.ins[a.ins + i].t0 += (uint32_t)a.tpos;
-  }
-  const int64_t dT = (int64_t)newB_T - (int64_t)b.tpos;
-  if (dT)
-    for (size_t i = newB_I; i < nI; ++i) P.ins[i].t0 = (uint32_t)((int64_t)P.ins[i].t0 + dT);
-  const size_t line_b = a.line + M.end_line - 1;  // line of the suffix's first statement in the new text
-  std::vector<ParseMark> &tail = B.mid.marks;     // (M's marks, rebased, then the suffix's)
-  for (ParseMark &x : tail) {
-    x.off += a.off;
-    x.line += a.line - 1;
-    x.ins += a.ins;
-    x.tpos += a.tpos;
-  }
-  for (size_t i = kb; i < mk.size(); ++i)
-    tail.push_back({mk[i].off + len - on, mk[i].line + line_b - b.line, mk[i].ins + newB_I - b.ins,
-                    mk[i].tpos + newB_T - b.tpos});
-  P.marks.resize(ka);
-  P.marks.insert(P.marks.end(), tail.begin(), tail.end());
-  P.end_line = P.end_line + line_b - b.line;
-  S.stats.parsed_bytes = bn - a.off;
 
-  // cuts: the previous segments wholly after the changed span (shifted by
-  // the change in instruction count) and wholly before it; the span between
-  // them is cut afresh into pieces of about segment_occ occurrences
+  // regions of equal bytes: old [o0, o1) == new [n0, n0 + o1 - o0), in order
+  struct Region {
+    size_t o0, o1, n0;
+  };
+  std::vector<Region> reg;
+  if (lp == on && lp == len) {
+    reg.push_back({0, on, 0});
+  } else {
+    // the lines between the common prefix and suffix (whole lines, so the
+    // first changed line and the last are in it)
+    size_t p0 = lp;
+    while (p0 > 0 && o[p0 - 1] != '\n') --p0;
+    size_t xo = on - ls;  // the first line start inside the common suffix (its newline common too)
+    if (ls == 0) {
+      xo = on;
+    } else {
+      const void *nl = memchr(o + xo, '\n', on - xo);
+      xo = nl ? (size_t)(static_cast<const char *>(nl) - o) + 1 : on;
+    }
+    if (xo < p0) xo = p0;
+    const size_t xn = xo + len - on;
+    if (xn < p0 || xn > len) return false;
+    std::vector<size_t> &la = B.la, &lb = B.lb;
+    line_starts(o, p0, xo, la);
+    line_starts(text, p0, xn, lb);
+    const long na = (long)la.size() - 1, nb = (long)lb.size() - 1;
+    // when the lines between the common prefix and suffix are most of the
+    // text: a sample of the new ones, each looked for near its place among
+    // the old ones (when most are missing the texts differ throughout)
+    if (2 * (xn - p0) > len) {
+      const long ns = std::min<long>(nb, 64), win = 64 + std::labs(na - nb);
+      long hits = 0;
+      for (long t = 0; t < ns; ++t) {
+        const long j = (long)(((double)t + 0.5) * (double)nb / (double)ns);
+        const long c = (long)((double)j * (double)na / (double)std::max<long>(nb, 1));
+        const size_t lj = lb[j + 1] - lb[j];
+        for (long i = std::max<long>(0, c - win); i < std::min<long>(na, c + win + 1); ++i)
+          if (la[i + 1] - la[i] == lj && memcmp(o + la[i], text + lb[j], lj) == 0) {
+            ++hits;
+            break;
+          }
+      }
+      if (2 * hits < ns) return false;
+    }
+    std::vector<uint64_t> &ha = B.ha, &hb = B.hb;
+    ha.resize((size_t)na);
+    hb.resize((size_t)nb);
+    for (long i = 0; i < na; ++i) ha[i] = line_hash(o + la[i], la[i + 1] - la[i]);
+    for (long i = 0; i < nb; ++i) hb[i] = line_hash(text + lb[i], lb[i + 1] - lb[i]);
+    std::vector<Run> &runs = B.runs_;
+    // a search of some tens of steps per line (about 0.2 ms for a text of
+    // 5,000 lines): a bound on the time spent on texts that differ throughout
+    if (!diff_runs(ha.data(), na, hb.data(), nb, std::min<long>(2048, na + nb), 32 * (na + nb) + 131072, B.vbuf,
+                   B.trace, runs))
+      return false;
+    reg.push_back({0, p0, 0});
+    for (const Run &r : runs) {
+      const size_t a0 = la[r.a], a1 = la[r.a + r.n], b0 = lb[r.b];
+      if (memcmp(o + a0, text + b0, a1 - a0) != 0) return false;  // (equal hashes, different lines)
+      reg.push_back({a0, a1, b0});
+    }
+    reg.push_back({xo, on, xn});
+  }
+  // merge touching regions with the same shift; shrink each to whole
+  // top-level statements: from the first statement boundary at or after its
+  // start to the last at or before its end (boundaries: 0, the marks, the end)
+  const std::vector<ParseMark> &mk = P.marks;
+  auto bnd_at_or_after = [&](size_t x) -> ParseMark {
+    if (x == 0) return ParseMark{0, 1, 0, 0};
+    auto it = std::lower_bound(mk.begin(), mk.end(), x, [](const ParseMark &m, size_t v) { return m.off < v; });
+    return it == mk.end() ? ParseMark{on, P.end_line, nI0, nT0} : *it;
+  };
+  auto bnd_at_or_before = [&](size_t x) -> ParseMark {
+    if (x >= on) return ParseMark{on, P.end_line, nI0, nT0};
+    auto it = std::upper_bound(mk.begin(), mk.end(), x, [](size_t v, const ParseMark &m) { return v < m.off; });
+    return it == mk.begin() ? ParseMark{0, 1, 0, 0} : *(it - 1);
+  };
+  struct Keep {
+    ParseMark s, e;  // statement boundaries in the old text
+    size_t n0;       // new offset of s
+  };
+  std::vector<Keep> keep;
+  for (size_t i = 0; i < reg.size();) {
+    Region r = reg[i++];
+    while (i < reg.size() && reg[i].o0 == r.o1 && reg[i].n0 == r.n0 + (r.o1 - r.o0)) r.o1 = reg[i++].o1;
+    if (r.o1 <= r.o0) continue;
+    const ParseMark s = bnd_at_or_after(r.o0), e = bnd_at_or_before(r.o1);
+    if (s.off >= e.off || e.off > r.o1) continue;
+    if (!keep.empty() && (s.off < keep.back().e.off || r.n0 + (s.off - r.o0) < keep.back().n0 + (keep.back().e.off - keep.back().s.off)))
+      return false;
+    keep.push_back({s, e, r.n0 + (s.off - r.o0)});
+  }
+  // the statements between kept runs, parsed again
+  size_t gap_bytes = 0;
+  {
+    size_t nprev = 0;
+    for (const Keep &k : keep) {
+      if (k.n0 < nprev) return false;
+      gap_bytes += k.n0 - nprev;
+      nprev = k.n0 + (k.e.off - k.s.off);
+    }
+    if (nprev > len) return false;
+    gap_bytes += len - nprev;
+  }
+  if (2 * gap_bytes > len) return false;  // mostly changed: parse and lower it whole
+  const size_t ngap = keep.size() + 1;
+  if (B.gaps.size() < ngap) B.gaps.resize(ngap);
+  {
+    size_t nprev = 0;
+    for (size_t g = 0; g < ngap; ++g) {
+      const size_t gend = g < keep.size() ? keep[g].n0 : len;
+      Parsed &G = B.gaps[g];
+      G.want_marks = true;
+      try {
+        parse_stim_into(text + nprev, gend - nprev, G);
+      } catch (const Error &) {
+        return false;  // (a full parse reports the error with its line in the whole text)
+      }
+      if (g < keep.size()) nprev = keep[g].n0 + (keep[g].e.off - keep[g].s.off);
+    }
+  }
+  // the new parse: gap 0, kept run 0, gap 1, ..., kept runs' instructions
+  // shifted (the old index range of each, and where it lands, for the cuts)
+  Parsed &N = B.next;
+  N.ins.clear();
+  N.marks.clear();
+  {
+    size_t ti = 0, tt = 0;
+    for (size_t g = 0; g < ngap; ++g) {
+      ti += B.gaps[g].ins.size();
+      tt += B.gaps[g].pool.size();
+    }
+    for (const Keep &k : keep) {
+      ti += k.e.ins - k.s.ins;
+      tt += k.e.tpos - k.s.tpos;
+    }
+    if (tt > 0xFFFFFFFFull) return false;
+    N.ins.reserve(ti);
+    N.pool.resize(tt);
+  }
+  struct Moved {
+    size_t o0, o1, n0;  // old instructions [o0, o1) are new [n0, n0 + o1 - o0)
+  };
+  std::vector<Moved> moved;
+  size_t tp = 0, line = 1, noff = 0;
+  for (size_t g = 0; g < ngap; ++g) {
+    const Parsed &G = B.gaps[g];
+    const size_t i0 = N.ins.size();
+    for (const Instr &in : G.ins) {
+      N.ins.push_back(in);
+      N.ins.back().t0 += (uint32_t)tp;
+    }
+    if (!G.pool.empty()) memcpy(N.pool.data() + tp, G.pool.data(), G.pool.size() * 4);
+    for (const ParseMark &x : G.marks) N.marks.push_back({x.off + noff, x.line + line - 1, x.ins + i0, x.tpos + tp});
+    tp += G.pool.size();
+    line += G.end_line - 1;
+    if (g == keep.size()) break;
+    const Keep &k = keep[g];
+    const size_t j0 = N.ins.size();
+    moved.push_back({k.s.ins, k.e.ins, j0});
+    const int64_t dt = (int64_t)tp - (int64_t)k.s.tpos;
+    for (size_t i = k.s.ins; i < k.e.ins; ++i) {
+      N.ins.push_back(P.ins[i]);
+      N.ins.back().t0 = (uint32_t)((int64_t)N.ins.back().t0 + dt);
+    }
+    if (k.e.tpos > k.s.tpos) memcpy(N.pool.data() + tp, P.pool.data() + k.s.tpos, (k.e.tpos - k.s.tpos) * 4);
+    auto m0 = std::lower_bound(mk.begin(), mk.end(), k.s.off, [](const ParseMark &m, size_t v) { return m.off < v; });
+    for (auto it = m0; it != mk.end() && it->off < k.e.off; ++it)
+      N.marks.push_back({it->off - k.s.off + k.n0, it->line - k.s.line + line, it->ins - k.s.ins + j0,
+                         it->tpos - k.s.tpos + tp});
+    tp += k.e.tpos - k.s.tpos;
+    line += k.e.line - k.s.line;
+    noff = k.n0 + (k.e.off - k.s.off);
+  }
+  N.end_line = line;
+  if (tp != N.pool.size()) return false;
+  const size_t nI = N.ins.size();
+
+  // cuts: the previous segments that lie within one kept run, moved with it;
+  // the instructions between them cut afresh into pieces of about
+  // segment_occ occurrences
   const std::vector<size_t> &oc = B.cut;
-  const int64_t dI = (int64_t)nI - (int64_t)nI0;
   std::vector<size_t> &nc = B.plan.cut;
   std::vector<int32_t> &from = B.plan.from;
-  nc.clear();
+  nc.assign(1, nI);
   from.clear();
-  nc.push_back(nI);
-  const size_t nseg0 = oc.size() - 1;
-  size_t s = 0;
-  for (; s < nseg0 && oc[s + 1] >= b.ins; ++s) {
-    nc.push_back((size_t)((int64_t)oc[s + 1] + dI));
-    from.push_back((int32_t)s);
-  }
-  size_t t = s;  // first segment wholly before the changed span
-  while (t < nseg0 && oc[t] > a.ins) ++t;
-  const size_t hi = nc.back(), lo = t < nseg0 ? oc[t] : 0;
-  if (hi > lo) {
-    const size_t so = std::max<uint32_t>(1024, opt.segment_occ);
+  const size_t so = std::max<uint32_t>(1024, opt.segment_occ);
+  auto fresh = [&](size_t lo) {  // segments over new instructions [lo, nc.back())
+    const size_t hi = nc.back();
+    if (hi <= lo) return;
     size_t acc = 0;
     for (size_t ii = hi; ii-- > lo + 1;) {
-      acc += P.ins[ii].tn;
+      acc += N.ins[ii].tn;
       if (acc >= so) {
         nc.push_back(ii);
         from.push_back(-1);
@@ -689,12 +895,26 @@ bool plan_incremental(const char *text, size_t len, const LowerOptions &opt, Low
     }
     nc.push_back(lo);
     from.push_back(-1);
+  };
+  size_t r = moved.size();
+  for (size_t s = 0; s + 1 < oc.size(); ++s) {
+    const size_t j0 = oc[s + 1], j1 = oc[s];
+    while (r > 0 && moved[r - 1].o0 > j0) --r;
+    if (r == 0 || j0 < moved[r - 1].o0 || j1 > moved[r - 1].o1 || j1 == j0) continue;
+    const Moved &m = moved[r - 1];
+    const size_t a = j0 - m.o0 + m.n0, b = j1 - m.o0 + m.n0;
+    if (b > nc.back()) return false;
+    fresh(b);
+    nc.push_back(a);
+    from.push_back((int32_t)s);
   }
-  for (; t < nseg0; ++t) {
-    nc.push_back(oc[t + 1]);
-    from.push_back((int32_t)t);
-  }
+  fresh(0);
   if (nc.back() != 0 || from.size() + 1 != nc.size()) return false;
+  P.ins.swap(N.ins);
+  P.pool.swap(N.pool);
+  P.marks.swap(N.marks);
+  P.end_line = N.end_line;
+  S.stats.parsed_bytes = gap_bytes;
   B.plan.active = true;
   return true;
 }

@@ -143,9 +143,10 @@ class Driver:
                  bucket_mean: int = 0, walk_words: int = 0, key_split: int = 0, walk_queue: int = 0,
                  walk_segment: int = 0, wait_limit_us: int = 0, test_hold_tile: int = 0,
                  test_fail_alloc: int = 0, heap_results: bool = False, incremental: bool = False):
-        """``incremental``: lower each circuit against the previous one of its lowering thread
-        (branches of one circuit re-parse only the statements that differ and reschedule only the
-        time segments those change; see ``Lowerer``).  The DEMs are the same."""
+        """``incremental``: in batches, lower each circuit against the previous one of its lowering
+        thread (branches of one circuit re-parse only the statements that differ and reschedule only
+        the time segments those change; see ``Lowerer``).  The DEMs are the same.  A single circuit
+        is lowered whole on all host threads."""
         L = _native.lib()
         self._h = ctypes.c_void_p()
         self.correlation_level = CorrelationLevel(correlation_level)
@@ -441,6 +442,14 @@ class Lowerer:
         text = _text(circuit)
         _native.check(_native.lib().gpc_lowerer_lower(self._h, text, len(text), ctypes.byref(h)), tape=True)
         return Tape._from_handle(h, segment_target)
+
+    def lower(self, circuit) -> None:
+        """Lowers ``circuit`` (the next circuit is lowered against it) without copying its tape out."""
+        h = ctypes.c_void_p()
+        text = _text(circuit)
+        L = _native.lib()
+        _native.check(L.gpc_lowerer_lower(self._h, text, len(text), ctypes.byref(h)), tape=True)
+        L.gpc_tape_free(h)
 
     @property
     def stats(self) -> dict:

@@ -7,6 +7,11 @@ instruction) draws its own p log-uniform in [1e-4, 1e-2]; every round takes
 the basis-switch branch (its Z-check CNOT layers run before its X-check
 layers) independently with probability 0.1.
 
+Branches (seed 5, 256 circuits): bivariate-bicycle [[144,12,12]] memory, 12
+rounds, uniform p=1e-3, each circuit a distinct set of basis-switch rounds
+(every round switched with probability 0.1, at least one): the branches of
+one circuit that the incremental lowering compiles against each other.
+
 Serving (seed 2): 50% surface memory with d uniform in {5, ..., 25}, rounds =
 d; 50% bivariate-bicycle memory drawn equally from [[72,12,6]],
 [[144,12,12]], [[288,12,18]] with rounds = d; each circuit with one p
@@ -49,6 +54,23 @@ def batch_surface(n: int = 256, seed: int = 0, switch_prob: float = 0.1, p_lo: f
         out.append(_surface(d).get_memory(d, 1e-3, noise="uniform",
                                           p_sampler=lambda: float(10 ** rng.uniform(lo, hi)),
                                           switch_rounds=switch))
+    return out
+
+
+def branches(n: int = 256, seed: int = 5, d: int = 12, rounds: int = 12, p: float = 1e-3,
+             switch_prob: float = 0.1) -> list[str]:
+    """Distinct branches of one circuit: bivariate-bicycle memory (d in 6, 10, 12, 18) with uniform
+    noise, each branch taking the basis-switch branch in every round independently with probability
+    ``switch_prob`` and in at least one round; no two branches alike (seeded)."""
+    rng = np.random.default_rng(seed)
+    code = _bb(d)
+    seen, out = set(), []
+    while len(out) < n:
+        sw = tuple(r for r in range(rounds) if rng.random() < switch_prob)
+        if not sw or sw in seen:
+            continue
+        seen.add(sw)
+        out.append(code.get_memory(rounds, p, noise="uniform", switch_rounds=list(sw)))
     return out
 
 

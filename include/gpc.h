@@ -80,10 +80,12 @@ typedef struct gpc_options {
   int32_t heap_results;    /* 1: DEM arrays are heap copies out of a staging buffer; 0: the device copies
                               them into page-locked memory the DEM keeps (a single circuit's own arrays, a
                               batch's shared result block), while a 4 GiB page-locked pool reaches */
-  int32_t incremental;     /* 1: lower each circuit against the previous one its lowering thread lowered
-                              (branches of one circuit): only the statements that differ are parsed again,
-                              and only the time segments they change are scheduled again (see
-                              gpc_lowerer_create); the DEM is the same.  0: every circuit is lowered whole */
+  int32_t incremental;     /* 1: in batches, each host thread lowers a circuit against the previous one it
+                              lowered (branches of one circuit): only the statements that differ are parsed
+                              again, and only the time segments they change are scheduled again (see
+                              gpc_lowerer_create); the DEMs are the same.  A single circuit is still lowered
+                              whole (on all host threads, which is faster for one circuit).  0: every
+                              circuit is lowered whole */
 } gpc_options;
 
 /* Parses `stim_text` (length `len`), sizes device buffers for it and returns

@@ -69,6 +69,7 @@ def test_added_and_removed_rounds_shift_the_later_segments():
     texts = [s.get_memory(r, 1e-3, noise="uniform") for r in (11, 12, 11, 10, 13)]
     st = lower_family(texts)
     assert all(x["incremental"] and x["reused"] >= 3 for x in st[1:])
+    assert st[2]["parsed_bytes"] == 0  # (12 rounds -> 11: a deleted round leaves nothing to parse)
 
 
 def test_bb_rounds():
@@ -112,14 +113,25 @@ def test_repeat_blocks():
     lower_family(texts, oracle=True)
 
 
-def test_same_text_again_schedules_only_the_last_statement_segment():
+def test_same_text_again_takes_over_every_segment():
     text = SurfaceCode(11).get_memory(11, 1e-3, noise="uniform")
     lw = Lowerer(2)
     t1 = lw.tape(text)
     t2 = lw.tape(text)
     st = lw.stats
-    assert st["incremental"] and st["reused"] == st["segments"] - 1
+    assert st["incremental"] and st["reused"] == st["segments"] and st["parsed_bytes"] == 0
     assert_same_tape(t1, t2)
+
+
+def test_branches_changed_in_several_places():
+    """Two branches that differ in rounds far apart: the segments between the changes are kept."""
+    s = SurfaceCode(11)
+    switches = ([], [1, 9], [2, 8], [0, 5, 10], [1, 9], [3])
+    texts = [s.get_memory(11, 1e-3, noise="uniform", switch_rounds=sw) for sw in switches]
+    st = lower_family(texts)
+    assert all(x["incremental"] for x in st[1:])
+    assert st[1]["reused"] >= 2  # (the segments wholly between rounds 1 and 9)
+    assert all(x["parsed_bytes"] < len(texts[0]) // 4 for x in st[1:])
 
 
 def test_unrelated_circuits_are_lowered_whole():
@@ -167,3 +179,38 @@ def test_bad_cuts_are_rejected():
     # any cuts give the same DEM
     compare_errors(compile_tape(ea.Tape(text, cuts=[nins, nins // 2, nins // 3, 0])),
                    dict(O.compile_text(text, 2).errors()), rel=1e-12)
+
+
+@pytest.mark.parametrize("seed", [0, 1, 2])
+def test_random_edits(seed):
+    """Random line edits (deleted, duplicated and moved blocks, changed rates, comments, blank
+    lines, a REPEAT block around some lines): each tape equals the full lowering with its cuts."""
+    rng = random.Random(seed)
+    base = SurfaceCode(7).get_memory(7, 1e-3, noise="uniform").split("\n")
+    cur = list(base)
+    texts = ["\n".join(cur)]
+    for _ in range(40):
+        j = rng.randrange(1, len(cur) - 1)
+        n = rng.randrange(1, 6)
+        op = rng.randrange(7)
+        blk = cur[j:j + n]
+        safe = not any(x.startswith(("DETECTOR", "OBSERVABLE", "M", "REPEAT", "}")) or "{" in x for x in blk)
+        if op == 0 and safe:
+            del cur[j:j + n]
+        elif op == 1 and safe:
+            cur[j:j] = blk
+        elif op == 2 and safe:
+            k = rng.randrange(1, len(cur) - 1)
+            del cur[j:j + n]
+            cur[k:k] = blk
+        elif op == 3 and "ERROR(" in cur[j]:
+            cur[j] = cur[j].split("(")[0] + f"({rng.choice(['0.002', '0.0005', '0.01'])})" + cur[j].split(")", 1)[1]
+        elif op == 4:
+            cur.insert(j, rng.choice(["", "# c", "   ", "TICK"]))
+        elif op == 5 and safe and not any("{" in x or "}" in x for x in cur):
+            cur[j:j + n] = ["REPEAT 2 {"] + ["  " + x for x in blk] + ["}"]
+        else:
+            cur.insert(j, cur[j] if not cur[j].startswith(("DETECTOR", "OBSERVABLE", "M", "REPEAT", "}")) else "# x")
+        texts.append("\n".join(cur))
+    st = lower_family(texts)
+    assert sum(x["incremental"] for x in st) >= 20
