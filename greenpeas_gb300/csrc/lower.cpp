@@ -517,7 +517,6 @@ struct LowerScratch::Buffers {
   Parsed next;               // the new parse, assembled
   std::vector<Parsed> gaps;  // the statements parsed again
   std::vector<size_t> la, lb;
-  std::vector<uint64_t> ha, hb;
   std::vector<long> vbuf, trace;
   std::vector<Run> runs_;
   std::vector<uint32_t> runs;  // segments scheduled by this lowering
@@ -590,23 +589,6 @@ void parse_stim_pieces(const char *text, size_t len, Parsed &out, std::vector<Pa
 
 namespace {
 
-// Hash of one line's bytes (8 at a time, multiply-xorshift mixing); lines
-// with equal hashes are compared byte for byte before they are trusted.
-inline uint64_t line_hash(const char *p, size_t n) {
-  uint64_t h = 0x9E3779B97F4A7C15ull ^ (uint64_t)n;
-  size_t i = 0;
-  for (; i + 8 <= n; i += 8) {
-    uint64_t w;
-    memcpy(&w, p + i, 8);
-    h = (h ^ w) * 0xFF51AFD7ED558CCDull;
-    h ^= h >> 32;
-  }
-  uint64_t w = 0;
-  memcpy(&w, p + i, n - i);
-  h = (h ^ w) * 0xC4CEB9FE1A85EC53ull;
-  return h ^ (h >> 29);
-}
-
 // Line starts of text[a, b) (b is a line start or the end of the text), plus b.
 void line_starts(const char *text, size_t a, size_t b, std::vector<size_t> &out) {
   out.clear();
@@ -618,15 +600,16 @@ void line_starts(const char *text, size_t a, size_t b, std::vector<size_t> &out)
   out.push_back(b);
 }
 
-// The common runs of the sequences a[0, n) and b[0, m) along a shortest edit
-// script (Myers' greedy O((n + m) D) algorithm, "An O(ND) difference
-// algorithm and its variations", 1986), in order.  False when the script
-// needs more than dmax insertions and deletions, or the search more than
-// `budget` steps (texts that differ throughout are given up on early).
-// Round d's furthest reaching x on diagonals -d..d is kept at
-// trace[d * d + d + k] for the walk back.
-bool diff_runs(const uint64_t *a, long n, const uint64_t *b, long m, long dmax, long budget, std::vector<long> &vbuf,
-               std::vector<long> &trace, std::vector<Run> &runs) {
+// The common runs of the sequences a[0, n) and b[0, m) (eq(x, y): a[x]
+// equals b[y]) along a shortest edit script (Myers' greedy O((n + m) D)
+// algorithm, "An O(ND) difference algorithm and its variations", 1986), in
+// order.  False when the script needs more than dmax insertions and
+// deletions, or the search more than `budget` steps (texts that differ
+// throughout are given up on early).  Round d's furthest reaching x on
+// diagonals -d..d is kept at trace[d * d + d + k] for the walk back.
+template <typename Eq>
+bool diff_runs(Eq &&eq, long n, long m, long dmax, long budget, std::vector<long> &vbuf, std::vector<long> &trace,
+               std::vector<Run> &runs) {
   const long off = dmax + 1;
   long work = 0;
   vbuf.assign((size_t)(2 * dmax + 3), 0);
@@ -638,7 +621,7 @@ bool diff_runs(const uint64_t *a, long n, const uint64_t *b, long m, long dmax, 
       long x = (k == -d || (k != d && V[off + k - 1] < V[off + k + 1])) ? V[off + k + 1] : V[off + k - 1] + 1;
       long y = x - k;
       const long x0 = x;
-      while (x < n && y < m && a[x] == b[y]) {
+      while (x < n && y < m && eq(x, y)) {
         ++x;
         ++y;
       }
@@ -738,23 +721,17 @@ bool plan_incremental(const char *text, size_t len, const LowerOptions &opt, Low
       }
       if (2 * hits < ns) return false;
     }
-    std::vector<uint64_t> &ha = B.ha, &hb = B.hb;
-    ha.resize((size_t)na);
-    hb.resize((size_t)nb);
-    for (long i = 0; i < na; ++i) ha[i] = line_hash(o + la[i], la[i + 1] - la[i]);
-    for (long i = 0; i < nb; ++i) hb[i] = line_hash(text + lb[i], lb[i + 1] - lb[i]);
+    auto same_line = [&](long x, long y) {
+      const size_t n = la[x + 1] - la[x];
+      return lb[y + 1] - lb[y] == n && memcmp(o + la[x], text + lb[y], n) == 0;
+    };
     std::vector<Run> &runs = B.runs_;
     // a search of some tens of steps per line (about 0.2 ms for a text of
     // 5,000 lines): a bound on the time spent on texts that differ throughout
-    if (!diff_runs(ha.data(), na, hb.data(), nb, std::min<long>(2048, na + nb), 32 * (na + nb) + 131072, B.vbuf,
-                   B.trace, runs))
+    if (!diff_runs(same_line, na, nb, std::min<long>(2048, na + nb), 32 * (na + nb) + 131072, B.vbuf, B.trace, runs))
       return false;
     reg.push_back({0, p0, 0});
-    for (const Run &r : runs) {
-      const size_t a0 = la[r.a], a1 = la[r.a + r.n], b0 = lb[r.b];
-      if (memcmp(o + a0, text + b0, a1 - a0) != 0) return false;  // (equal hashes, different lines)
-      reg.push_back({a0, a1, b0});
-    }
+    for (const Run &r : runs) reg.push_back({la[r.a], la[r.a + r.n], lb[r.b]});
     reg.push_back({xo, on, xn});
   }
   // merge touching regions with the same shift; shrink each to whole
@@ -815,12 +792,27 @@ bool plan_incremental(const char *text, size_t len, const LowerOptions &opt, Low
       if (g < keep.size()) nprev = keep[g].n0 + (keep[g].e.off - keep[g].s.off);
     }
   }
-  // the new parse: gap 0, kept run 0, gap 1, ..., kept runs' instructions
-  // shifted (the old index range of each, and where it lands, for the cuts)
-  Parsed &N = B.next;
-  N.ins.clear();
-  N.marks.clear();
+  // the new parse: gap 0, kept run 0, gap 1, ...  When every gap parses to
+  // as many instructions and targets as the old statements it replaces
+  // (lines changed or reordered in place), the kept runs stay where they are
+  // and the gaps are written over in S.parsed itself; otherwise the new parse
+  // is assembled in a second buffer (the old index range of each kept run,
+  // and where it lands, go to the cuts)
+  bool inplace = true;
   {
+    size_t pi = 0, pt = 0;
+    for (size_t g = 0; g < ngap && inplace; ++g) {
+      const size_t ei = g < keep.size() ? keep[g].s.ins : nI0, et = g < keep.size() ? keep[g].s.tpos : nT0;
+      inplace = B.gaps[g].ins.size() == ei - pi && B.gaps[g].pool.size() == et - pt;
+      if (g < keep.size()) {
+        pi = keep[g].e.ins;
+        pt = keep[g].e.tpos;
+      }
+    }
+  }
+  Parsed &N = B.next;
+  N.marks.clear();
+  if (!inplace) {
     size_t ti = 0, tt = 0;
     for (size_t g = 0; g < ngap; ++g) {
       ti += B.gaps[g].ins.size();
@@ -831,46 +823,57 @@ bool plan_incremental(const char *text, size_t len, const LowerOptions &opt, Low
       tt += k.e.tpos - k.s.tpos;
     }
     if (tt > 0xFFFFFFFFull) return false;
+    N.ins.clear();
     N.ins.reserve(ti);
     N.pool.resize(tt);
   }
+  Parsed &W = inplace ? P : N;  // where the new parse is written
   struct Moved {
     size_t o0, o1, n0;  // old instructions [o0, o1) are new [n0, n0 + o1 - o0)
   };
   std::vector<Moved> moved;
-  size_t tp = 0, line = 1, noff = 0;
+  size_t ni = 0, tp = 0, line = 1, noff = 0;
   for (size_t g = 0; g < ngap; ++g) {
     const Parsed &G = B.gaps[g];
-    const size_t i0 = N.ins.size();
-    for (const Instr &in : G.ins) {
-      N.ins.push_back(in);
-      N.ins.back().t0 += (uint32_t)tp;
+    if (inplace) {
+      for (size_t i = 0; i < G.ins.size(); ++i) {
+        P.ins[ni + i] = G.ins[i];
+        P.ins[ni + i].t0 += (uint32_t)tp;
+      }
+    } else {
+      for (const Instr &in : G.ins) {
+        N.ins.push_back(in);
+        N.ins.back().t0 += (uint32_t)tp;
+      }
     }
-    if (!G.pool.empty()) memcpy(N.pool.data() + tp, G.pool.data(), G.pool.size() * 4);
-    for (const ParseMark &x : G.marks) N.marks.push_back({x.off + noff, x.line + line - 1, x.ins + i0, x.tpos + tp});
+    if (!G.pool.empty()) memcpy(W.pool.data() + tp, G.pool.data(), G.pool.size() * 4);
+    for (const ParseMark &x : G.marks) N.marks.push_back({x.off + noff, x.line + line - 1, x.ins + ni, x.tpos + tp});
+    ni += G.ins.size();
     tp += G.pool.size();
     line += G.end_line - 1;
     if (g == keep.size()) break;
     const Keep &k = keep[g];
-    const size_t j0 = N.ins.size();
-    moved.push_back({k.s.ins, k.e.ins, j0});
-    const int64_t dt = (int64_t)tp - (int64_t)k.s.tpos;
-    for (size_t i = k.s.ins; i < k.e.ins; ++i) {
-      N.ins.push_back(P.ins[i]);
-      N.ins.back().t0 = (uint32_t)((int64_t)N.ins.back().t0 + dt);
+    moved.push_back({k.s.ins, k.e.ins, ni});
+    if (!inplace) {
+      const int64_t dt = (int64_t)tp - (int64_t)k.s.tpos;
+      for (size_t i = k.s.ins; i < k.e.ins; ++i) {
+        N.ins.push_back(P.ins[i]);
+        N.ins.back().t0 = (uint32_t)((int64_t)N.ins.back().t0 + dt);
+      }
+      if (k.e.tpos > k.s.tpos) memcpy(N.pool.data() + tp, P.pool.data() + k.s.tpos, (k.e.tpos - k.s.tpos) * 4);
     }
-    if (k.e.tpos > k.s.tpos) memcpy(N.pool.data() + tp, P.pool.data() + k.s.tpos, (k.e.tpos - k.s.tpos) * 4);
     auto m0 = std::lower_bound(mk.begin(), mk.end(), k.s.off, [](const ParseMark &m, size_t v) { return m.off < v; });
     for (auto it = m0; it != mk.end() && it->off < k.e.off; ++it)
-      N.marks.push_back({it->off - k.s.off + k.n0, it->line - k.s.line + line, it->ins - k.s.ins + j0,
+      N.marks.push_back({it->off - k.s.off + k.n0, it->line - k.s.line + line, it->ins - k.s.ins + ni,
                          it->tpos - k.s.tpos + tp});
+    ni += k.e.ins - k.s.ins;
     tp += k.e.tpos - k.s.tpos;
     line += k.e.line - k.s.line;
     noff = k.n0 + (k.e.off - k.s.off);
   }
-  N.end_line = line;
-  if (tp != N.pool.size()) return false;
-  const size_t nI = N.ins.size();
+  if (tp != W.pool.size() || ni != W.ins.size()) return false;
+  const size_t nI = ni;
+  const Instr *const NI = W.ins.data();
 
   // cuts: the previous segments that lie within one kept run, moved with it;
   // the instructions between them cut afresh into pieces of about
@@ -886,7 +889,7 @@ bool plan_incremental(const char *text, size_t len, const LowerOptions &opt, Low
     if (hi <= lo) return;
     size_t acc = 0;
     for (size_t ii = hi; ii-- > lo + 1;) {
-      acc += N.ins[ii].tn;
+      acc += NI[ii].tn;
       if (acc >= so) {
         nc.push_back(ii);
         from.push_back(-1);
@@ -910,10 +913,12 @@ bool plan_incremental(const char *text, size_t len, const LowerOptions &opt, Low
   }
   fresh(0);
   if (nc.back() != 0 || from.size() + 1 != nc.size()) return false;
-  P.ins.swap(N.ins);
-  P.pool.swap(N.pool);
+  if (!inplace) {
+    P.ins.swap(N.ins);
+    P.pool.swap(N.pool);
+  }
   P.marks.swap(N.marks);
-  P.end_line = N.end_line;
+  P.end_line = line;
   S.stats.parsed_bytes = gap_bytes;
   B.plan.active = true;
   return true;

@@ -103,7 +103,7 @@ gpc_status gpc_lowerer_lower(gpc_lowerer *lowerer, const char *stim_text, size_t
   *out = nullptr;
   return tape_guarded([&] {
     std::unique_ptr<gpc_tape> t(new gpc_tape{});
-    lower_like_compile(stim_text, len, lowerer->lo, t->t, lowerer->scratch);
+    gpc::lower_text(stim_text, len, lowerer->lo, t->t, lowerer->scratch);  // on this thread, as a batch's
     *out = t.release();
   });
 }

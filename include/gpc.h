@@ -418,7 +418,8 @@ gpc_status gpc_tape_lower_cuts(const char *stim_text, size_t len, int32_t correl
  * after it).  The tape equals gpc_tape_lower_cuts of the same text with the
  * same cuts, byte for byte.  A changed span over more than half of the text
  * is lowered whole.
- *   gpc_lowerer_lower  the tape of a circuit (owned by the caller)
+ *   gpc_lowerer_lower  the tape of a circuit (owned by the caller), lowered on
+ *                      the calling thread
  *   gpc_lowerer_stats  the last lowering: whether it was incremental, its
  *                      segments, those taken over, the text bytes parsed;
  *                      and its cuts (written when *ncuts <= cap) */
