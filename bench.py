@@ -444,16 +444,9 @@ def sweep_entry(r: dict) -> dict:
             "fallbacks": r["fallbacks"]}
 
 
-def branches_leg(gp, local: int, n_batch: int = 256, reps: int = 3) -> dict:
-    """Branches of the headline circuit (256 distinct basis-switch branches of BB [[144,12,12]] r=12,
-    ``workloads.branches``) compiled in batches of 256, end to end (host text in, DEM arrays out), by
-    a driver that lowers each circuit whole and by one whose host threads lower each circuit against
-    the previous one they lowered (``incremental``).  Host lowering alone (one thread, ``Lowerer``)
-    is timed beside them, with the share of time segments taken over and of text parsed again.  The
-    DEMs of both drivers are compared."""
-    from greenpeas_gb300.workloads import branches
-    texts = branches(n_batch)
-    out = {"workload": "bb_144_12_12_r12_uniform_p1e-3, 256 basis-switch branches (seed 5)", "circuits": len(texts)}
+def _incremental_family(gp, local: int, texts: list, reps: int) -> dict:
+    """One family compiled by a driver that lowers each circuit whole and by an incremental one."""
+    out = {"circuits": len(texts)}
     for mode in (False, True):  # one host thread, lowering only
         lw = gp.Lowerer(2, incremental=mode)
         for t in texts[:4]:
@@ -480,13 +473,29 @@ def branches_leg(gp, local: int, n_batch: int = 256, reps: int = 3) -> dict:
         for _ in range(reps):
             dems[key] = drv.compile_batch(texts)
         dt = (time.perf_counter() - t0) / reps
-        out[key] = {"batch_e2e": {"value": len(texts) / dt, "unit": UNIT, "ms_per_batch": 1e3 * dt}}
+        out[key] = {"batch_e2e": {"value": len(texts) / dt, "unit": UNIT, "ms_per_batch": 1e3 * dt},
+                    "host_ms_last_batch": drv.last_host_timings()}
         del drv
     out["same_order"] = all(dem_arrays_equal(a, b) for a, b in zip(dems["whole"], dems["incremental"]))
     out["same_dems"] = all(a.canonical() == b.canonical() for a, b in zip(dems["whole"][:8], dems["incremental"][:8]))
     out["speedup"] = {"batch_e2e": out["incremental"]["batch_e2e"]["value"] / out["whole"]["batch_e2e"]["value"],
                       "lowering": out["lowering_whole"]["ms_per_circuit"] / out["lowering_incremental"]["ms_per_circuit"]}
     return out
+
+
+def branches_leg(gp, local: int, n: int = 256, reps: int = 3) -> dict:
+    """Incremental lowering on two families of one circuit (BB [[144,12,12]] r=12, ``workloads``):
+    256 distinct basis-switch branches, and 256 noise what-if variants (one noise instruction's rate
+    changed per variant).  Each is compiled in batches of 256 end to end (host text in, DEM arrays
+    out) by a driver that lowers each circuit whole and by one whose host threads lower each
+    circuit against the previous one they lowered; host lowering alone (one thread, ``Lowerer``) is
+    timed beside them, with the share of time segments taken over and of text parsed again.  The
+    DEMs of both drivers are compared."""
+    from greenpeas_gb300.workloads import branches, noise_variants
+    return {"basis_switch_branches": dict(workload="bb_144_12_12_r12_uniform_p1e-3, basis-switch branches (seed 5)",
+                                          **_incremental_family(gp, local, branches(n), reps)),
+            "noise_variants": dict(workload="bb_144_12_12_r12_uniform_p1e-3, one noise rate changed (seed 6)",
+                                   **_incremental_family(gp, local, noise_variants(n), reps))}
 
 
 def batch_workload_texts(circuits: int) -> list:
@@ -692,6 +701,8 @@ def main() -> None:
             out["batch"] = batched_leg(gp, torch, local, flush, steps=max(3, min(args.steps, 10)), warmup=args.warmup,
                                        circuits=args.batch_circuits, walk_queue=args.walk_queue,
                                        device_only=args.batch_device_only)
+        if not args.no_branches:
+            out["branches"] = branches_leg(gp, local)
         if rank == 0:
             print(json.dumps(out), flush=True)
         return

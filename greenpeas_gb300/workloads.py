@@ -11,6 +11,9 @@ Branches (seed 5, 256 circuits): bivariate-bicycle [[144,12,12]] memory, 12
 rounds, uniform p=1e-3, each circuit a distinct set of basis-switch rounds
 (every round switched with probability 0.1, at least one): the branches of
 one circuit that the incremental lowering compiles against each other.
+Noise variants (seed 6, 256 circuits): the same circuit with uniform p=1e-3
+except one noise instruction per variant, drawn at random, at a rate
+log-uniform in [1e-4, 1e-2] (a what-if sweep over one channel instance).
 
 Serving (seed 2): 50% surface memory with d uniform in {5, ..., 25}, rounds =
 d; 50% bivariate-bicycle memory drawn equally from [[72,12,6]],
@@ -71,6 +74,34 @@ def branches(n: int = 256, seed: int = 5, d: int = 12, rounds: int = 12, p: floa
             continue
         seen.add(sw)
         out.append(code.get_memory(rounds, p, noise="uniform", switch_rounds=list(sw)))
+    return out
+
+
+def noise_variants(n: int = 256, seed: int = 6, d: int = 12, rounds: int = 12, p: float = 1e-3,
+                   p_lo: float = 1e-4, p_hi: float = 1e-2) -> list[str]:
+    """Variants of one circuit for a noise what-if sweep: bivariate-bicycle memory with uniform
+    noise ``p``, except that in each variant one noise instruction (one channel instance: a tick
+    and gate class), drawn at random, takes a rate log-uniform in [p_lo, p_hi] (seeded)."""
+    rng = np.random.default_rng(seed)
+    code = _bb(d)
+    count = [0]
+
+    def counting():
+        count[0] += 1
+        return p
+
+    code.get_memory(rounds, p, noise="uniform", p_sampler=counting)
+    lo, hi = np.log10(p_lo), np.log10(p_hi)
+    out = []
+    for _ in range(n):
+        k, q = int(rng.integers(count[0])), float(10 ** rng.uniform(lo, hi))
+        calls = [0]
+
+        def sample():
+            calls[0] += 1
+            return q if calls[0] - 1 == k else p
+
+        out.append(code.get_memory(rounds, p, noise="uniform", p_sampler=sample))
     return out
 
 
