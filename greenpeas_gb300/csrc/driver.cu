@@ -72,8 +72,13 @@ struct DevBuf {
   void *p = nullptr;
   size_t cap = 0;
   AllocCounter *ctr = nullptr;
+  // A buffer that grows takes half again its old size when that is more (so
+  // sizes that creep up, such as a batch's, do not reallocate every time);
+  // off where an admission budget counts the exact bytes.
+  bool slack = true;
   void ensure(size_t bytes) {
     if (bytes <= cap) return;
+    const size_t old = cap;
     if (p) {
       CK(cudaFree(p));
       if (ctr) ++ctr->frees;
@@ -84,7 +89,7 @@ struct DevBuf {
       ctr->fail_at = -1;
       throw gpc::Error(GPC_ERR_OOM, "device allocation of " + std::to_string(bytes) + " bytes failed (injected)");
     }
-    size_t want = std::max(bytes, cap + cap / 2);
+    size_t want = slack ? std::max(bytes, old + old / 2) : bytes;
     cudaError_t e = cudaMalloc(&p, want);
     if (e != cudaSuccess) {
       (void)cudaGetLastError();
@@ -114,10 +119,11 @@ struct HostBuf {
   size_t cap = 0;
   void ensure(size_t bytes) {
     if (bytes <= cap) return;
+    const size_t old = cap;  // (grows by half again, as DevBuf)
     if (p) CK(cudaFreeHost(p));
     p = nullptr;
     cap = 0;
-    size_t want = std::max(bytes, cap + cap / 2);
+    size_t want = std::max(bytes, old + old / 2);
     if (cudaHostAlloc(&p, want, cudaHostAllocDefault) != cudaSuccess) {
       (void)cudaGetLastError();
       throw gpc::Error(GPC_ERR_OOM, "pinned host allocation failed");
@@ -2173,6 +2179,7 @@ struct gpc_driver {
       d->walk_queue = walk_queue;
       d->walk_segment = walk_segment;
       d->pinned_results = pinned_results;
+      d->incremental = incremental;
       d->spin_ns = spin_ns;
       d->init_streams();
       partner = std::move(d);
@@ -2785,6 +2792,7 @@ gpc_status gpc_server_create(const gpc_server_options *options, gpc_server **out
       d->blocking_wait = true;  // and while the GPU runs the worker's batch
       d->init_streams();
       d->admit = [raw, w](size_t grow, size_t total) { raw->acquire(w, grow, total); };
+      d->arena.slack = d->tgbuf.slack = false;  // the budget counts exact bytes
       sv->drivers.push_back(std::move(d));
     }
     for (uint32_t w = 0; w < o.slots; ++w) sv->workers.emplace_back([raw, w] { raw->worker(w); });
