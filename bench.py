@@ -793,8 +793,6 @@ def main() -> None:
                                     device_only=args.batch_device_only)
     if not args.no_grad and world == 1:
         line["grad"] = grad_leg(gp, torch, fd_entries=64)
-    if not args.no_branches and world == 1:
-        line["branches"] = branches_leg(gp, local)
     if not args.no_serve and world == 1:
         # capacity from a burst long enough that filling and draining the
         # pipeline is a small part of it (1,000 requests: ~0.2 s, 5-15% low)
@@ -803,6 +801,8 @@ def main() -> None:
                                     args.serve_slots, args.serve_batch,
                                     batch_texts=batch_workload_texts(args.batch_circuits) if bl.get("plain") else None,
                                     batch_plain_e2e=bl.get("plain", {}).get("e2e", {}).get("value"))
+    if not args.no_branches and world == 1:  # (after serving: its page-locked blocks are of other sizes)
+        line["branches"] = branches_leg(gp, local)
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(text)
     print(json.dumps(line), flush=True)

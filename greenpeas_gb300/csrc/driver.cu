@@ -194,6 +194,8 @@ class PinnedPool {
   }
   void *take(size_t bytes) {
     const size_t c = class_of(bytes);
+    std::vector<void *> victims;
+    bool room = false;
     {
       std::lock_guard<std::mutex> lk(mu_);
       auto &f = free_[c];
@@ -202,9 +204,28 @@ class PinnedPool {
         f.pop_back();
         return p;
       }
-      if (total_ + c > kCapBytes) return nullptr;
-      total_ += c;
+      if (total_ + c > kCapBytes) {
+        // make room from blocks of other sizes kept free (the largest first), so
+        // that sizes of an earlier workload do not hold the pool from a later one
+        std::vector<size_t> classes;
+        for (auto &kv : free_)
+          if (!kv.second.empty()) classes.push_back(kv.first);
+        std::sort(classes.begin(), classes.end(), std::greater<size_t>());
+        for (size_t k : classes) {
+          auto &v = free_[k];
+          while (!v.empty() && total_ + c > kCapBytes) {
+            victims.push_back(v.back());
+            v.pop_back();
+            total_ -= k;
+          }
+          if (total_ + c <= kCapBytes) break;
+        }
+      }
+      room = total_ + c <= kCapBytes;
+      if (room) total_ += c;
     }
+    for (void *q : victims) cudaFreeHost(q);
+    if (!room) return nullptr;
     void *p = nullptr;
     if (cudaHostAlloc(&p, c, cudaHostAllocPortable) != cudaSuccess) {
       cudaGetLastError();
