@@ -699,6 +699,58 @@ bool plan_incremental(const char *text, size_t len, const LowerOptions &opt, Low
     if (xo < p0) xo = p0;
     const size_t xn = xo + len - on;
     if (xn < p0 || xn > len) return false;
+    reg.push_back({0, p0, 0});
+    // Texts of one length whose changes keep every line after them in place
+    // (lines changed or reordered within a span of the same bytes): compared
+    // in step, 64 bytes at a time.  A changed span runs from the start of the
+    // line of its first differing byte to a newline both texts share and
+    // after which 64 more bytes agree.
+    if (len == on) {
+      size_t x = p0, i = p0, changed = 0;
+      while (i < xo) {
+        const size_t n = std::min<size_t>(64, xo - i);
+        if (memcmp(o + i, text + i, n) == 0) {
+          i += n;
+          continue;
+        }
+        size_t d = i;
+        while (o[d] == text[d]) ++d;
+        size_t a = d;
+        while (a > x && o[a - 1] != '\n') --a;
+        size_t e = d;
+        for (;;) {
+          const void *nl = memchr(o + e, '\n', xo - e);
+          if (!nl) {
+            e = xo;
+            break;
+          }
+          const size_t q = (size_t)(static_cast<const char *>(nl) - o);
+          e = q + 1;
+          if (text[q] == '\n' && memcmp(o + e, text + e, std::min<size_t>(64, xo - e)) == 0) break;
+        }
+        if (a > x) reg.push_back({x, a, x});
+        changed += e - a;
+        x = i = e;
+      }
+      if (2 * changed <= xo - p0) {  // (else a shortest edit script may find more in common)
+        if (xo > x) reg.push_back({x, xo, x});
+        reg.push_back({xo, on, xn});
+      } else {
+        reg.resize(1);
+      }
+    }
+  }
+  if (reg.empty() || reg.back().o1 != on) {
+    size_t p0 = reg.back().o1;  // (the common prefix's lines)
+    size_t xo = on - ls;
+    if (ls == 0) {
+      xo = on;
+    } else {
+      const void *nl = memchr(o + xo, '\n', on - xo);
+      xo = nl ? (size_t)(static_cast<const char *>(nl) - o) + 1 : on;
+    }
+    if (xo < p0) xo = p0;
+    const size_t xn = xo + len - on;
     std::vector<size_t> &la = B.la, &lb = B.lb;
     line_starts(o, p0, xo, la);
     line_starts(text, p0, xn, lb);
@@ -730,7 +782,6 @@ bool plan_incremental(const char *text, size_t len, const LowerOptions &opt, Low
     // 5,000 lines): a bound on the time spent on texts that differ throughout
     if (!diff_runs(same_line, na, nb, std::min<long>(2048, na + nb), 32 * (na + nb) + 131072, B.vbuf, B.trace, runs))
       return false;
-    reg.push_back({0, p0, 0});
     for (const Run &r : runs) reg.push_back({la[r.a], la[r.a + r.n], lb[r.b]});
     reg.push_back({xo, on, xn});
   }
@@ -758,7 +809,9 @@ bool plan_incremental(const char *text, size_t len, const LowerOptions &opt, Low
     while (i < reg.size() && reg[i].o0 == r.o1 && reg[i].n0 == r.n0 + (r.o1 - r.o0)) r.o1 = reg[i++].o1;
     if (r.o1 <= r.o0) continue;
     const ParseMark s = bnd_at_or_after(r.o0), e = bnd_at_or_before(r.o1);
-    if (s.off >= e.off || e.off > r.o1) continue;
+    // (a run of fewer than 16 instructions between two changes is parsed again
+    // with them: lines swapped around it then make one span of unchanged size)
+    if (s.off >= e.off || e.off > r.o1 || e.ins - s.ins < 16) continue;
     if (!keep.empty() && (s.off < keep.back().e.off || r.n0 + (s.off - r.o0) < keep.back().n0 + (keep.back().e.off - keep.back().s.off)))
       return false;
     keep.push_back({s, e, r.n0 + (s.off - r.o0)});
