@@ -181,10 +181,11 @@ def test_bad_cuts_are_rejected():
                    dict(O.compile_text(text, 2).errors()), rel=1e-12)
 
 
-@pytest.mark.parametrize("seed", [0, 1, 2])
-def test_random_edits(seed):
+@pytest.mark.parametrize("seed,eol", [(0, "\n"), (1, "\n"), (2, "\n"), (3, "\r\n"), (4, "")])
+def test_random_edits(seed, eol):
     """Random line edits (deleted, duplicated and moved blocks, changed rates, comments, blank
-    lines, a REPEAT block around some lines): each tape equals the full lowering with its cuts."""
+    lines, a REPEAT block around some lines), with LF or CRLF line ends or no final newline:
+    each tape equals the full lowering with its cuts."""
     rng = random.Random(seed)
     base = SurfaceCode(7).get_memory(7, 1e-3, noise="uniform").split("\n")
     cur = list(base)
@@ -212,5 +213,9 @@ def test_random_edits(seed):
         else:
             cur.insert(j, cur[j] if not cur[j].startswith(("DETECTOR", "OBSERVABLE", "M", "REPEAT", "}")) else "# x")
         texts.append("\n".join(cur))
+    if eol == "\r\n":
+        texts = [t.replace("\n", "\r\n") for t in texts]
+    elif eol == "":
+        texts = [t.rstrip("\n") for t in texts]
     st = lower_family(texts)
     assert sum(x["incremental"] for x in st) >= 20
