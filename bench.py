@@ -476,21 +476,29 @@ def _incremental_family(gp, local: int, texts: list, reps: int) -> dict:
         out[key] = {"batch_e2e": {"value": len(texts) / dt, "unit": UNIT, "ms_per_batch": 1e3 * dt},
                     "host_ms_last_batch": drv.last_host_timings()}
         del drv
+    # served as a burst of requests (4 workers x 16, 13 lowering threads: lowering bounds the server)
+    from greenpeas_gb300.serving import Server, replay
+    for mode in (False, True):
+        key = "incremental" if mode else "whole"
+        with Server(slots=4, max_batch=16, incremental=mode) as srv:
+            replay(srv, [(0.0, t) for t in texts[:128]])  # warm: workers' buffers, page-locked blocks
+            rep = replay(srv, [(0.0, t) for _ in range(3) for t in texts])
+        out[key]["serve_burst"] = {"value": rep["dems_per_s"], "unit": UNIT, "requests": rep["requests"]}
     out["same_order"] = all(dem_arrays_equal(a, b) for a, b in zip(dems["whole"], dems["incremental"]))
     out["same_dems"] = all(a.canonical() == b.canonical() for a, b in zip(dems["whole"][:8], dems["incremental"][:8]))
-    out["speedup"] = {"batch_e2e": out["incremental"]["batch_e2e"]["value"] / out["whole"]["batch_e2e"]["value"],
-                      "lowering": out["lowering_whole"]["ms_per_circuit"] / out["lowering_incremental"]["ms_per_circuit"]}
+    out["speedup"] = {k: out["incremental"][k]["value"] / out["whole"][k]["value"] for k in ("batch_e2e", "serve_burst")}
+    out["speedup"]["lowering"] = out["lowering_whole"]["ms_per_circuit"] / out["lowering_incremental"]["ms_per_circuit"]
     return out
 
 
 def branches_leg(gp, local: int, n: int = 256, reps: int = 3) -> dict:
     """Incremental lowering on two families of one circuit (BB [[144,12,12]] r=12, ``workloads``):
     256 distinct basis-switch branches, and 256 noise what-if variants (one noise instruction's rate
-    changed per variant).  Each is compiled in batches of 256 end to end (host text in, DEM arrays
-    out) by a driver that lowers each circuit whole and by one whose host threads lower each
-    circuit against the previous one they lowered; host lowering alone (one thread, ``Lowerer``) is
+    changed per variant).  Each is compiled end to end (host text in, DEM arrays out) in batches of
+    256 and as a burst of 768 server requests, lowering each circuit whole and lowering it against
+    the previous one of the same host thread; host lowering alone (one thread, ``Lowerer``) is
     timed beside them, with the share of time segments taken over and of text parsed again.  The
-    DEMs of both drivers are compared."""
+    DEMs of both batch drivers are compared."""
     from greenpeas_gb300.workloads import branches, noise_variants
     return {"basis_switch_branches": dict(workload="bb_144_12_12_r12_uniform_p1e-3, basis-switch branches (seed 5)",
                                           **_incremental_family(gp, local, branches(n), reps)),
