@@ -464,38 +464,52 @@ def _incremental_family(gp, local: int, texts: list, reps: int) -> dict:
         out["lowering_" + ("incremental" if mode else "whole")] = {
             "ms_per_circuit": 1e3 * dt / len(texts), "segments_reused": reused / max(segs, 1),
             "text_parsed": parsed / sum(len(t) for t in texts), "threads": 1}
-    dems = {}
-    for mode in (False, True):
-        key = "incremental" if mode else "whole"
-        drv = gp.get_driver(texts[0], device=local, incremental=mode)
-        drv.compile_batch(texts)  # warm: buffers sized, graphs captured, lowering state kept
-        t0 = time.perf_counter()
-        for _ in range(reps):
-            dems[key] = drv.compile_batch(texts)
-        dt = (time.perf_counter() - t0) / reps
-        out[key] = {"batch_e2e": {"value": len(texts) / dt, "unit": UNIT, "ms_per_batch": 1e3 * dt},
-                    "host_ms_last_batch": drv.last_host_timings()}
-        del drv
-    # served as a burst of requests (4 workers x 16, 13 lowering threads: lowering bounds the server)
+    # both drivers and both servers stay up and are timed in turn, twice each (whole, incremental,
+    # whole, incremental), so that neither side sees only a cold or only a warm machine
     from greenpeas_gb300.serving import Server, replay
-    for mode in (False, True):
-        key = "incremental" if mode else "whole"
-        with Server(slots=4, max_batch=16, incremental=mode) as srv:
-            replay(srv, [(0.0, t) for t in texts[:128]])  # warm: workers' buffers, page-locked blocks
-            rep = replay(srv, [(0.0, t) for _ in range(3) for t in texts])
-        out[key]["serve_burst"] = {"value": rep["dems_per_s"], "unit": UNIT, "requests": rep["requests"]}
-    out["same_order"] = all(dem_arrays_equal(a, b) for a, b in zip(dems["whole"], dems["incremental"]))
-    out["same_dems"] = all(a.canonical() == b.canonical() for a, b in zip(dems["whole"][:8], dems["incremental"][:8]))
+    dems, bt, st = {}, {False: [], True: []}, {False: [], True: []}
+    drv = {m: gp.get_driver(texts[0], device=local, incremental=m) for m in (False, True)}
+    for m in (False, True):
+        drv[m].compile_batch(texts)  # warm: buffers sized, graphs captured, lowering state kept
+    for _ in range(2):
+        for m in (False, True):
+            t0 = time.perf_counter()
+            for _ in range(reps):
+                dems[m] = drv[m].compile_batch(texts)
+            bt[m].append((time.perf_counter() - t0) / reps)
+    host = {m: drv[m].last_host_timings() for m in (False, True)}
+    del drv
+    # served as bursts of requests (4 workers x 16, 13 lowering threads: lowering bounds the server)
+    srv = {m: Server(slots=4, max_batch=16, incremental=m) for m in (False, True)}
+    try:
+        for m in (False, True):
+            replay(srv[m], [(0.0, t) for t in texts[:128]])  # warm: workers' buffers, page-locked blocks
+        for _ in range(2):
+            for m in (False, True):
+                st[m].append(replay(srv[m], [(0.0, t) for _ in range(reps) for t in texts])["dems_per_s"])
+    finally:
+        for m in (False, True):
+            srv[m].close()
+    for m in (False, True):
+        ms = 1e3 * sum(bt[m]) / len(bt[m])
+        out["incremental" if m else "whole"] = {
+            "batch_e2e": {"value": len(texts) / (ms / 1e3), "unit": UNIT, "ms_per_batch": ms,
+                          "runs_ms": [1e3 * x for x in bt[m]]},
+            "serve_burst": {"value": sum(st[m]) / len(st[m]), "unit": UNIT, "requests": reps * len(texts),
+                            "runs": st[m]},
+            "host_ms_last_batch": host[m]}
+    out["same_order"] = all(dem_arrays_equal(a, b) for a, b in zip(dems[False], dems[True]))
+    out["same_dems"] = all(a.canonical() == b.canonical() for a, b in zip(dems[False][:8], dems[True][:8]))
     out["speedup"] = {k: out["incremental"][k]["value"] / out["whole"][k]["value"] for k in ("batch_e2e", "serve_burst")}
     out["speedup"]["lowering"] = out["lowering_whole"]["ms_per_circuit"] / out["lowering_incremental"]["ms_per_circuit"]
     return out
 
 
-def branches_leg(gp, local: int, n: int = 256, reps: int = 3) -> dict:
+def branches_leg(gp, local: int, n: int = 256, reps: int = 4) -> dict:
     """Incremental lowering on two families of one circuit (BB [[144,12,12]] r=12, ``workloads``):
     256 distinct basis-switch branches, and 256 noise what-if variants (one noise instruction's rate
     changed per variant).  Each is compiled end to end (host text in, DEM arrays out) in batches of
-    256 and as a burst of 768 server requests, lowering each circuit whole and lowering it against
+    256 and as bursts of 1,024 server requests, lowering each circuit whole and lowering it against
     the previous one of the same host thread; host lowering alone (one thread, ``Lowerer``) is
     timed beside them, with the share of time segments taken over and of text parsed again.  The
     DEMs of both batch drivers are compared."""
