@@ -465,27 +465,31 @@ def _incremental_family(gp, local: int, texts: list, reps: int) -> dict:
             "ms_per_circuit": 1e3 * dt / len(texts), "segments_reused": reused / max(segs, 1),
             "text_parsed": parsed / sum(len(t) for t in texts), "threads": 1}
     # both drivers and both servers stay up and are timed in turn, twice each (whole, incremental,
-    # whole, incremental), so that neither side sees only a cold or only a warm machine
+    # incremental, whole), so that neither side sees only a cold or only a warm machine
     from greenpeas_gb300.serving import Server, replay
     dems, bt, st = {}, {False: [], True: []}, {False: [], True: []}
     drv = {m: gp.get_driver(texts[0], device=local, incremental=m) for m in (False, True)}
     for m in (False, True):
         drv[m].compile_batch(texts)  # warm: buffers sized, graphs captured, lowering state kept
-    for _ in range(2):
-        for m in (False, True):
+    for order in ((False, True), (True, False)):
+        for m in order:
             t0 = time.perf_counter()
             for _ in range(reps):
                 dems[m] = drv[m].compile_batch(texts)
             bt[m].append((time.perf_counter() - t0) / reps)
     host = {m: drv[m].last_host_timings() for m in (False, True)}
     del drv
+    # (the batches' DEMs hold page-locked result blocks: compared, then let go before serving)
+    out["same_order"] = all(dem_arrays_equal(a, b) for a, b in zip(dems[False], dems[True]))
+    out["same_dems"] = all(a.canonical() == b.canonical() for a, b in zip(dems[False][:8], dems[True][:8]))
+    del dems
     # served as bursts of requests (4 workers x 16, 13 lowering threads: lowering bounds the server)
     srv = {m: Server(slots=4, max_batch=16, incremental=m) for m in (False, True)}
     try:
         for m in (False, True):
             replay(srv[m], [(0.0, t) for t in texts[:128]])  # warm: workers' buffers, page-locked blocks
-        for _ in range(2):
-            for m in (False, True):
+        for order in ((False, True), (True, False)):
+            for m in order:
                 st[m].append(replay(srv[m], [(0.0, t) for _ in range(reps) for t in texts])["dems_per_s"])
     finally:
         for m in (False, True):
@@ -498,8 +502,6 @@ def _incremental_family(gp, local: int, texts: list, reps: int) -> dict:
             "serve_burst": {"value": sum(st[m]) / len(st[m]), "unit": UNIT, "requests": reps * len(texts),
                             "runs": st[m]},
             "host_ms_last_batch": host[m]}
-    out["same_order"] = all(dem_arrays_equal(a, b) for a, b in zip(dems[False], dems[True]))
-    out["same_dems"] = all(a.canonical() == b.canonical() for a, b in zip(dems[False][:8], dems[True][:8]))
     out["speedup"] = {k: out["incremental"][k]["value"] / out["whole"][k]["value"] for k in ("batch_e2e", "serve_burst")}
     out["speedup"]["lowering"] = out["lowering_whole"]["ms_per_circuit"] / out["lowering_incremental"]["ms_per_circuit"]
     return out
