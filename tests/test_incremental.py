@@ -219,3 +219,29 @@ def test_random_edits(seed, eol):
         texts = [t.rstrip("\n") for t in texts]
     st = lower_family(texts)
     assert sum(x["incremental"] for x in st) >= 20
+
+
+@pytest.mark.parametrize("seed", [0, 1])
+def test_random_edits_of_unchanged_length(seed):
+    """Edits that keep the text's length (a rate's digit changed, lines swapped, targets of a line
+    reversed) take the in-step comparison: each tape equals the full lowering with its cuts."""
+    rng = random.Random(seed)
+    cur = SurfaceCode(7).get_memory(7, 1e-3, noise="uniform").split("\n")
+    texts = ["\n".join(cur)]
+    for _ in range(40):
+        for _ in range(rng.randrange(1, 4)):
+            j = rng.randrange(1, len(cur) - 2)
+            op = rng.randrange(3)
+            if op == 0 and "(0.00" in cur[j]:
+                k = cur[j].index("(0.00") + 5
+                cur[j] = cur[j][:k] + rng.choice("123456789") + cur[j][k + 1:]
+            elif op == 1 and not cur[j].startswith(("DETECTOR", "OBSERVABLE", "M")) \
+                    and not cur[j + 1].startswith(("DETECTOR", "OBSERVABLE", "M")):
+                cur[j], cur[j + 1] = cur[j + 1], cur[j]
+            elif op == 2 and cur[j].startswith(("H ", "R ", "X_ERROR", "DEPOLARIZE1")):
+                name, *tg = cur[j].split(" ")
+                cur[j] = " ".join([name] + tg[::-1])
+        texts.append("\n".join(cur))
+    assert len({len(t) for t in texts}) == 1
+    st = lower_family(texts)
+    assert sum(x["incremental"] for x in st) >= 30
