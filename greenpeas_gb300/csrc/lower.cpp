@@ -1040,69 +1040,38 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
   size_t occ = 0;
   std::vector<std::pair<uint32_t, uint32_t>> &detPairs = B.detPairs;  // (measurement, detector)
   std::vector<std::pair<uint32_t, uint32_t>> &obsPairs = B.obsPairs;  // (measurement, observable)
-  detPairs.clear();
-  obsPairs.clear();
   uint32_t m = 0, ndet = 0, nobs = 0;
   uint32_t nq = 0;
-  for (size_t i = 0; i < P.ins.size(); ++i) {
-    const Instr &in = P.ins[i];
-    const Gate &g = kGates[in.gate];
-    const uint32_t *t = P.pool.data() + in.t0;
-    measBase[i] = m;
-    occBase[i] = (uint32_t)occ;
-    occ += in.tn;
-    if (occ > 0xFFFFFFFFull / 4) throw Error(GPC_ERR_CAPACITY, "circuit too long");
-    // target kinds (summarised by the parser)
-    if (in.tn) {
-      if (g.kind == G_DET || g.kind == G_OBS) {
-        if (!(in.kinds & kAllRec)) throw Error(GPC_ERR_PARSE, std::string(g.name) + " takes record targets only");
-      } else if (in.kinds & kAnyRec) {
-        throw Error(GPC_ERR_UNSUPPORTED, std::string("record targets are not supported on ") + g.name);
-      } else if (g.kind == G_MPAD) {
-        if (in.maxq > 1 || (in.kinds & kAnyPau)) throw Error(GPC_ERR_PARSE, "MPAD targets must be 0 or 1");
-      } else {
-        if (g.kind == G_CORR) {
-          if (!(in.kinds & kAllPau)) throw Error(GPC_ERR_PARSE, "E takes Pauli targets");
-        } else if (in.kinds & kAnyPau) {
-          throw Error(GPC_ERR_PARSE, std::string("Pauli targets are not allowed on ") + g.name);
-        }
-        nq = std::max(nq, in.maxq + 1);
-      }
+  // checks of one instruction that need no running count: its targets' kinds
+  // (summarised by the parser), then, after the counts, its arguments
+  auto check_targets = [&](const Instr &in, const Gate &g) {
+    if (!in.tn) return;
+    if (g.kind == G_DET || g.kind == G_OBS) {
+      if (!(in.kinds & kAllRec)) throw Error(GPC_ERR_PARSE, std::string(g.name) + " takes record targets only");
+    } else if (in.kinds & kAnyRec) {
+      throw Error(GPC_ERR_UNSUPPORTED, std::string("record targets are not supported on ") + g.name);
+    } else if (g.kind == G_MPAD) {
+      if (in.maxq > 1 || (in.kinds & kAnyPau)) throw Error(GPC_ERR_PARSE, "MPAD targets must be 0 or 1");
+    } else if (g.kind == G_CORR) {
+      if (!(in.kinds & kAllPau)) throw Error(GPC_ERR_PARSE, "E takes Pauli targets");
+    } else if (in.kinds & kAnyPau) {
+      throw Error(GPC_ERR_PARSE, std::string("Pauli targets are not allowed on ") + g.name);
     }
-    switch (g.kind) {
-      case G_M:
-      case G_MR:
-      case G_MPAD:
-        m += in.tn;
-        break;
-      case G_DET:
-        for (uint32_t k = 0; k < in.tn; ++k) {
-          uint32_t back = t[k] & ~kRec;
-          if (back > m) throw Error(GPC_ERR_PARSE, "record lookback beyond the start of the circuit");
-          detPairs.push_back({m - back, ndet});
-        }
-        ++ndet;
-        break;
-      case G_OBS: {
-        double a = in.args[0];
-        if (!(a >= 0) || a != std::floor(a) || a > 1e6) throw Error(GPC_ERR_PARSE, "bad observable index");
-        uint32_t kk = (uint32_t)a;
-        for (uint32_t k = 0; k < in.tn; ++k) {
-          uint32_t back = t[k] & ~kRec;
-          if (back > m) throw Error(GPC_ERR_PARSE, "record lookback beyond the start of the circuit");
-          obsPairs.push_back({m - back, kk});
-        }
-        nobs = std::max(nobs, kk + 1);
-        break;
-      }
-      case G_C2:
-      case G_N2:  // (the parser checked that no pair names one qubit twice)
-        if (in.tn % 2) throw Error(GPC_ERR_PARSE, std::string(g.name) + " needs an even number of targets");
-        break;
-      default:
-        break;
-    }
-    // probability checks
+  };
+  // (qubits: the targets of every instruction but detectors, observables and MPAD)
+  auto counts_qubits = [](const Instr &in, const Gate &g) {
+    return in.tn && g.kind != G_DET && g.kind != G_OBS && g.kind != G_MPAD;
+  };
+  auto obs_index = [](const Instr &in) -> uint32_t {
+    const double a = in.args[0];
+    if (!(a >= 0) || a != std::floor(a) || a > 1e6) throw Error(GPC_ERR_PARSE, "bad observable index");
+    return (uint32_t)a;
+  };
+  auto check_pairs = [](const Instr &in, const Gate &g) {  // (the parser checked that no pair names one qubit twice)
+    if ((g.kind == G_C2 || g.kind == G_N2) && in.tn % 2)
+      throw Error(GPC_ERR_PARSE, std::string(g.name) + " needs an even number of targets");
+  };
+  auto check_args = [&](const Instr &in, const Gate &g) {
     auto prob = [&](double p) {
       if (!(p >= 0 && p <= 1)) throw Error(GPC_ERR_PARSE, std::string(g.name) + ": probability out of range");
     };
@@ -1115,9 +1084,158 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
       if (!pc1_independent(in.args[0], in.args[1], in.args[2], q))
         throw Error(GPC_ERR_UNSUPPORTED, "PAULI_CHANNEL_1 is not a product of independent X, Y, Z channels");
     }
-    if (g.kind == G_MPAD && in.nargs && in.args[0] > 0)
-      throw Error(GPC_ERR_UNSUPPORTED, "noisy MPAD is not supported");
+    if (g.kind == G_MPAD && in.nargs && in.args[0] > 0) throw Error(GPC_ERR_UNSUPPORTED, "noisy MPAD is not supported");
+  };
+  // the pass on one thread; it throws the first error in instruction order
+  auto forward_serial = [&] {
+    occ = 0;
+    m = ndet = nobs = nq = 0;
+    detPairs.clear();
+    obsPairs.clear();
+    for (size_t i = 0; i < P.ins.size(); ++i) {
+      const Instr &in = P.ins[i];
+      const Gate &g = kGates[in.gate];
+      const uint32_t *t = P.pool.data() + in.t0;
+      measBase[i] = m;
+      occBase[i] = (uint32_t)occ;
+      occ += in.tn;
+      if (occ > 0xFFFFFFFFull / 4) throw Error(GPC_ERR_CAPACITY, "circuit too long");
+      check_targets(in, g);
+      if (counts_qubits(in, g)) nq = std::max(nq, in.maxq + 1);
+      switch (g.kind) {
+        case G_M:
+        case G_MR:
+        case G_MPAD:
+          m += in.tn;
+          break;
+        case G_DET:
+          for (uint32_t k = 0; k < in.tn; ++k) {
+            uint32_t back = t[k] & ~kRec;
+            if (back > m) throw Error(GPC_ERR_PARSE, "record lookback beyond the start of the circuit");
+            detPairs.push_back({m - back, ndet});
+          }
+          ++ndet;
+          break;
+        case G_OBS: {
+          const uint32_t kk = obs_index(in);
+          for (uint32_t k = 0; k < in.tn; ++k) {
+            uint32_t back = t[k] & ~kRec;
+            if (back > m) throw Error(GPC_ERR_PARSE, "record lookback beyond the start of the circuit");
+            obsPairs.push_back({m - back, kk});
+          }
+          nobs = std::max(nobs, kk + 1);
+          break;
+        }
+        default:
+          check_pairs(in, g);
+          break;
+      }
+      check_args(in, g);
+    }
+  };
+  // A long circuit on the pool: its instructions in pieces, counted (and
+  // checked) in a first pass, written from the pieces' starting counts in a
+  // second.  Any error sends it back to the serial pass, which reports the
+  // first error in instruction order.
+  bool done = false;
+  const size_t nins = P.ins.size();
+  if (pool && nins >= 1024) {
+    struct Ctr {
+      uint64_t occ = 0, ndp = 0, nop = 0;
+      uint32_t m = 0, ndet = 0, nobs = 0, nq = 0;
+    };
+    const uint32_t np = (uint32_t)std::min<size_t>({(size_t)pool->workers() + 1, 16, nins / 128});
+    std::vector<Ctr> pc(np + 1);
+    auto lo_of = [&](uint32_t p) { return nins * p / np; };
+    bool ok = true;
+    try {
+      pool->run(np, [&](uint32_t p, uint32_t) {
+        Ctr c;
+        for (size_t i = lo_of(p); i < lo_of(p + 1); ++i) {
+          const Instr &in = P.ins[i];
+          const Gate &g = kGates[in.gate];
+          c.occ += in.tn;
+          check_targets(in, g);
+          if (counts_qubits(in, g)) c.nq = std::max(c.nq, in.maxq + 1);
+          switch (g.kind) {
+            case G_M:
+            case G_MR:
+            case G_MPAD:
+              c.m += in.tn;
+              break;
+            case G_DET:
+              c.ndp += in.tn;
+              ++c.ndet;
+              break;
+            case G_OBS:
+              c.nop += in.tn;
+              c.nobs = std::max(c.nobs, obs_index(in) + 1);
+              break;
+            default:
+              check_pairs(in, g);
+              break;
+          }
+          check_args(in, g);
+        }
+        pc[p + 1] = c;
+      });
+    } catch (const Error &) {
+      ok = false;
+    }
+    if (ok) {
+      for (uint32_t p = 0; p < np; ++p) {  // starting counts of each piece
+        Ctr &a = pc[p + 1];
+        const Ctr &b = pc[p];
+        nq = std::max(nq, a.nq);
+        nobs = std::max(nobs, a.nobs);
+        a.occ += b.occ;
+        a.ndp += b.ndp;
+        a.nop += b.nop;
+        a.m += b.m;
+        a.ndet += b.ndet;
+      }
+      ok = pc[np].occ <= 0xFFFFFFFFull / 4;
+    }
+    if (ok) {
+      detPairs.resize(pc[np].ndp);
+      obsPairs.resize(pc[np].nop);
+      try {
+        pool->run(np, [&](uint32_t p, uint32_t) {
+          uint32_t mm = pc[p].m, nd = pc[p].ndet;
+          size_t oc = pc[p].occ, dp = pc[p].ndp, op = pc[p].nop;
+          for (size_t i = lo_of(p); i < lo_of(p + 1); ++i) {
+            const Instr &in = P.ins[i];
+            const Gate &g = kGates[in.gate];
+            const uint32_t *t = P.pool.data() + in.t0;
+            measBase[i] = mm;
+            occBase[i] = (uint32_t)oc;
+            oc += in.tn;
+            if (g.kind == G_M || g.kind == G_MR || g.kind == G_MPAD) {
+              mm += in.tn;
+            } else if (g.kind == G_DET || g.kind == G_OBS) {
+              const uint32_t id = g.kind == G_DET ? nd++ : (uint32_t)in.args[0];
+              auto &pairs = g.kind == G_DET ? detPairs : obsPairs;
+              size_t &at = g.kind == G_DET ? dp : op;
+              for (uint32_t k = 0; k < in.tn; ++k) {
+                const uint32_t back = t[k] & ~kRec;
+                if (back > mm) throw Error(GPC_ERR_PARSE, "record lookback beyond the start of the circuit");
+                pairs[at++] = {mm - back, id};
+              }
+            }
+          }
+        });
+      } catch (const Error &) {
+        ok = false;
+      }
+    }
+    if (ok) {
+      occ = pc[np].occ;
+      m = pc[np].m;
+      ndet = pc[np].ndet;
+      done = true;
+    }
   }
+  if (!done) forward_serial();
   // sources of the noise targets: tick and class (see Tape::rec_src)
   std::vector<uint32_t> &tsrc = B.tsrc;
   if (opt.sources) {
