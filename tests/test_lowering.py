@@ -69,12 +69,21 @@ def test_large_tape_matches_oracle():
     compare_errors(compile_tape(Tape(text)), _oracle(text))
 
 
-@pytest.mark.parametrize("bad,code", [("FOO 1\n", -3), ("CX 5\n", -2), ("CX rec[-1] 0\n", -3)])
+@pytest.mark.parametrize("bad,code", [("FOO 1\n", -3), ("CX 5\n", -2), ("CX rec[-1] 0\n", -3),
+                                      ("DEPOLARIZE1(0.9) 0\n", -2), ("OBSERVABLE_INCLUDE(-1) rec[-1]\n", -2),
+                                      ("DETECTOR rec[-100000]\n", -2), ("PAULI_CHANNEL_1(0.4, 0.4, 0.4) 0\n", -3)])
 def test_large_text_error_in_a_late_piece(bad, code):
+    """Errors late in a text long enough to be parsed in pieces and counted in pieces (the
+    forward pass on the pool) are reported as the serial lowering reports them."""
     text = BBCode(12).get_memory(12, 1e-3, noise="uniform")
     with pytest.raises(GpcError) as ei:
         Tape(text + bad)
     assert ei.value.status == code
+    lines = text.count("\n") + 1
+    with pytest.raises(GpcError) as e2:
+        Tape(text + bad + text)  # the same error with a long text after it
+    assert e2.value.status == code and str(e2.value) == str(ei.value)
+    assert "line" not in str(ei.value) or f"line {lines}" in str(ei.value)
 
 
 def test_repeat_block_gives_the_tape_of_its_flattened_circuit():
