@@ -245,3 +245,25 @@ def test_random_edits_of_unchanged_length(seed):
     assert len({len(t) for t in texts}) == 1
     st = lower_family(texts)
     assert sum(x["incremental"] for x in st) >= 30
+
+
+def test_a_lowering_that_fails_after_the_text_compare_leaves_nothing_to_lower_against():
+    """A changed statement that parses but fails in the lowering (a lookback beyond the start of
+    the circuit): the error is the whole lowering's, and the next circuit is lowered whole."""
+    s = SurfaceCode(7)
+    base = s.get_memory(7, 1e-3, noise="uniform")
+    lines = base.split("\n")
+    k = len(lines) // 2
+    bad = "\n".join(lines[:k] + ["DETECTOR rec[-100000]"] + lines[k:])
+    lw = Lowerer(2)
+    lw.tape(base)
+    with pytest.raises(GpcError) as e:
+        lw.tape(bad)
+    with pytest.raises(GpcError) as e_whole:
+        ea.Tape(bad)
+    assert e.value.status == e_whole.value.status and str(e.value) == str(e_whole.value)
+    nxt = s.get_memory(7, 1e-3, noise="uniform", switch_rounds=[3])
+    assert_same_tape(lw.tape(nxt), ea.Tape(nxt, cuts=lw.cuts))
+    assert not lw.stats["incremental"]
+    assert_same_tape(lw.tape(base), ea.Tape(base, cuts=lw.cuts))
+    assert lw.stats["incremental"]
