@@ -928,18 +928,31 @@ bool plan_incremental(const char *text, size_t len, const LowerOptions &opt, Low
   const size_t nI = ni;
   const Instr *const NI = W.ins.data();
 
-  // cuts: the previous segments that lie within one kept run, moved with it;
-  // the instructions between them cut afresh into pieces of about
-  // segment_occ occurrences
+  // cuts: the previous segments that lie within one kept run, moved with it.
+  // The instructions between them are cut where the previous circuit was
+  // cut when they are as many as the previous instructions between the same
+  // segments (statements changed in place: the schedule keeps its shape),
+  // else afresh into pieces of about segment_occ occurrences.
   const std::vector<size_t> &oc = B.cut;
   std::vector<size_t> &nc = B.plan.cut;
   std::vector<int32_t> &from = B.plan.from;
   nc.assign(1, nI);
   from.clear();
   const size_t so = std::max<uint32_t>(1024, opt.segment_occ);
-  auto fresh = [&](size_t lo) {  // segments over new instructions [lo, nc.back())
+  // segments over new instructions [lo, nc.back()), which were old [olo, ohi)
+  auto fresh = [&](size_t lo, size_t olo, size_t ohi) {
     const size_t hi = nc.back();
     if (hi <= lo) return;
+    if (hi - lo == ohi - olo) {
+      for (size_t c : oc)
+        if (c > olo && c < ohi) {
+          nc.push_back(c - olo + lo);
+          from.push_back(-1);
+        }
+      nc.push_back(lo);
+      from.push_back(-1);
+      return;
+    }
     size_t acc = 0;
     for (size_t ii = hi; ii-- > lo + 1;) {
       acc += NI[ii].tn;
@@ -953,18 +966,20 @@ bool plan_incremental(const char *text, size_t len, const LowerOptions &opt, Low
     from.push_back(-1);
   };
   size_t r = moved.size();
+  size_t ohi = nI0;  // old index of nc.back()
   for (size_t s = 0; s + 1 < oc.size(); ++s) {
     const size_t j0 = oc[s + 1], j1 = oc[s];
     while (r > 0 && moved[r - 1].o0 > j0) --r;
     if (r == 0 || j0 < moved[r - 1].o0 || j1 > moved[r - 1].o1 || j1 == j0) continue;
     const Moved &m = moved[r - 1];
     const size_t a = j0 - m.o0 + m.n0, b = j1 - m.o0 + m.n0;
-    if (b > nc.back()) return false;
-    fresh(b);
+    if (b > nc.back() || j1 > ohi) return false;
+    fresh(b, j1, ohi);
     nc.push_back(a);
     from.push_back((int32_t)s);
+    ohi = j0;
   }
-  fresh(0);
+  fresh(0, 0, ohi);
   if (nc.back() != 0 || from.size() + 1 != nc.size()) return false;
   if (!inplace) {
     P.ins.swap(N.ins);
