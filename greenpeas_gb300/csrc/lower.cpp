@@ -1851,6 +1851,45 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
   for (uint32_t e = 0; e < nE; ++e) T.ep_ptoff[e + 1] = T.ep_ptoff[e] + ep_np[e];
   std::vector<uint32_t> &remap = B.remap;
   remap.assign(nprov, kNone);
+  // records in walk order: each segment's records go to their place with their
+  // points renumbered (its own points, numbered by its own assembly just
+  // before), beside the first mechanism of each record
+  const size_t R = nrec_all;
+  uint64_t mm = 0;
+  for (uint32_t s = 0; s < nseg; ++s) {
+    B.segs[s].moff0 = mm;
+    mm += B.segs[s].ncomp;
+  }
+  if (mm >= 0xFFFFFFFFull) throw Error(GPC_ERR_CAPACITY, "too many error mechanisms");
+  if (!direct) {  // (one segment wrote its records in place)
+    T.rec.resize(R);
+    T.rec_p.resize(R);
+    T.rec_src.resize(opt.sources ? R : 0);
+  }
+  T.rec_moff.resize(R + 1);
+  auto place_records = [&](uint32_t sg, uint32_t) {
+    const LowerScratch::Buffers::Segment &G = B.segs[sg];
+    const uint64_t *const src = direct ? T.rec.data() : G.rec.data();
+    uint64_t *const dst = T.rec.data() + G.roff;
+    uint32_t *const mo = T.rec_moff.data() + G.roff;
+    uint64_t m0 = G.moff0;
+    for (size_t i = 0; i < G.nrec; ++i) {
+      uint64_t d = src[i];
+      const uint32_t pa = (uint32_t)(d & kMaxPoint28) + G.poff, pb = (uint32_t)((d >> 28) & kMaxPoint28) + G.poff;
+      const uint32_t type = (uint32_t)((d >> 56) & 15u), Pb = (uint32_t)(d >> 62);
+      const bool hasB = type >= REC_DEP2_L0 || Pb != 0;
+      d = (d & ~(((uint64_t)kMaxPoint28) | ((uint64_t)kMaxPoint28 << 28))) | (uint64_t)remap[pa] |
+          ((uint64_t)(hasB ? remap[pb] : 0) << 28);
+      dst[i] = d;
+      mo[i] = (uint32_t)m0;
+      m0 += kRecComps[type];
+    }
+    if (!direct && G.nrec) {
+      memcpy(T.rec_p.data() + G.roff, G.rec_p.data(), G.nrec * 8);
+      if (opt.sources) memcpy(T.rec_src.data() + G.roff, G.rec_src.data(), G.nrec * 4);
+    }
+  };
+
   std::atomic<bool> miscount{false};
   auto assemble = [&](uint32_t sg, uint32_t) {
     LowerScratch::Buffers::Segment &G = B.segs[sg];
@@ -1887,10 +1926,15 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
     }
     if (next != T.ep_ptoff[eb]) miscount = true;
   };
-  if (pool && nseg > 1 && total >= (1u << 16))
-    pool->run(nseg, assemble);
+  // each segment's epochs, then its records, in one task per segment
+  auto assemble_and_place = [&](uint32_t sg, uint32_t slot) {
+    assemble(sg, slot);
+    place_records(sg, slot);
+  };
+  if (pool && nseg > 1)
+    pool->run(nseg, assemble_and_place);
   else
-    for (uint32_t sg = 0; sg < nseg; ++sg) assemble(sg, 0);
+    for (uint32_t sg = 0; sg < nseg; ++sg) assemble_and_place(sg, 0);
   if (miscount) throw Error(GPC_ERR_INVALID, "internal: points per epoch miscounted");
   const uint32_t next = T.ep_ptoff[nE];
   T.npoints = next;
@@ -1917,48 +1961,6 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
     e = f;
   }
   if (next > kMaxPoint28) throw Error(GPC_ERR_CAPACITY, "too many snapshot points");
-  // records in walk order: each segment's records go to their place with their
-  // points renumbered, beside the first mechanism of each record (segments on
-  // the pool)
-  const size_t R = nrec_all;
-  uint64_t mm = 0;
-  for (uint32_t s = 0; s < nseg; ++s) {
-    B.segs[s].moff0 = mm;
-    mm += B.segs[s].ncomp;
-  }
-  if (mm >= 0xFFFFFFFFull) throw Error(GPC_ERR_CAPACITY, "too many error mechanisms");
-  if (!direct) {  // (one segment wrote its records in place)
-    T.rec.resize(R);
-    T.rec_p.resize(R);
-    T.rec_src.resize(opt.sources ? R : 0);
-  }
-  T.rec_moff.resize(R + 1);
-  auto place_records = [&](uint32_t sg, uint32_t) {
-    const LowerScratch::Buffers::Segment &G = B.segs[sg];
-    const uint64_t *const src = direct ? T.rec.data() : G.rec.data();
-    uint64_t *const dst = T.rec.data() + G.roff;
-    uint32_t *const mo = T.rec_moff.data() + G.roff;
-    uint64_t m0 = G.moff0;
-    for (size_t i = 0; i < G.nrec; ++i) {
-      uint64_t d = src[i];
-      const uint32_t pa = (uint32_t)(d & kMaxPoint28) + G.poff, pb = (uint32_t)((d >> 28) & kMaxPoint28) + G.poff;
-      const uint32_t type = (uint32_t)((d >> 56) & 15u), Pb = (uint32_t)(d >> 62);
-      const bool hasB = type >= REC_DEP2_L0 || Pb != 0;
-      d = (d & ~(((uint64_t)kMaxPoint28) | ((uint64_t)kMaxPoint28 << 28))) | (uint64_t)remap[pa] |
-          ((uint64_t)(hasB ? remap[pb] : 0) << 28);
-      dst[i] = d;
-      mo[i] = (uint32_t)m0;
-      m0 += kRecComps[type];
-    }
-    if (!direct && G.nrec) {
-      memcpy(T.rec_p.data() + G.roff, G.rec_p.data(), G.nrec * 8);
-      if (opt.sources) memcpy(T.rec_src.data() + G.roff, G.rec_src.data(), G.nrec * 4);
-    }
-  };
-  if (pool && nseg > 1)
-    pool->run(nseg, place_records);
-  else
-    for (uint32_t s = 0; s < nseg; ++s) place_records(s, 0);
   T.rec_moff[R] = (uint32_t)mm;
   T.M = (uint32_t)mm;
   // injection range of each word
