@@ -357,6 +357,13 @@ struct QState {
   }
 };
 
+// Counts of a run of instructions (the forward pass's first pass), or the
+// counts before an instruction (its starting counts).
+struct FwdCount {
+  uint64_t occ = 0, ndp = 0, nop = 0;  // target occurrences, detector pairs, observable pairs
+  uint32_t m = 0, ndet = 0, nobs = 0, nq = 0;
+};
+
 // A run of equal lines of two texts: a[a, a + n) equals b[b, b + n).
 struct Run {
   size_t a, b, n;
@@ -521,6 +528,12 @@ struct LowerScratch::Buffers {
   std::vector<Run> runs_;
   std::vector<uint32_t> runs;  // segments scheduled by this lowering
   std::vector<int64_t> dbits, dsrc;  // per reused segment: shift of its detector bits and sources
+  // The forward pass done beside a parse in pieces (its arrays above), for
+  // the parse `fwd_of` of fwd_ins instructions: totals in fwd.
+  const Parsed *fwd_of = nullptr;
+  size_t fwd_ins = 0;
+  FwdCount fwd;
+  std::vector<FwdCount> fwd_pc;
 };
 
 LowerScratch::LowerScratch() : b(new Buffers) {}
@@ -533,7 +546,147 @@ void LowerScratch::forget() {
   b->plan.active = false;
 }
 
+namespace {
+
+// ---- the forward pass over a run of instructions ----------------------------
+// Checks that need no running count: an instruction's targets' kinds
+// (summarised by the parser) and, after the counts, its arguments.
+void check_targets(const Instr &in, const Gate &g) {
+  if (!in.tn) return;
+  if (g.kind == G_DET || g.kind == G_OBS) {
+    if (!(in.kinds & kAllRec)) throw Error(GPC_ERR_PARSE, std::string(g.name) + " takes record targets only");
+  } else if (in.kinds & kAnyRec) {
+    throw Error(GPC_ERR_UNSUPPORTED, std::string("record targets are not supported on ") + g.name);
+  } else if (g.kind == G_MPAD) {
+    if (in.maxq > 1 || (in.kinds & kAnyPau)) throw Error(GPC_ERR_PARSE, "MPAD targets must be 0 or 1");
+  } else if (g.kind == G_CORR) {
+    if (!(in.kinds & kAllPau)) throw Error(GPC_ERR_PARSE, "E takes Pauli targets");
+  } else if (in.kinds & kAnyPau) {
+    throw Error(GPC_ERR_PARSE, std::string("Pauli targets are not allowed on ") + g.name);
+  }
+}
+// qubits: the targets of every instruction but detectors, observables and MPAD
+bool counts_qubits(const Instr &in, const Gate &g) {
+  return in.tn && g.kind != G_DET && g.kind != G_OBS && g.kind != G_MPAD;
+}
+uint32_t obs_index(const Instr &in) {
+  const double a = in.args[0];
+  if (!(a >= 0) || a != std::floor(a) || a > 1e6) throw Error(GPC_ERR_PARSE, "bad observable index");
+  return (uint32_t)a;
+}
+void check_pairs(const Instr &in, const Gate &g) {  // (the parser checked that no pair names one qubit twice)
+  if ((g.kind == G_C2 || g.kind == G_N2) && in.tn % 2)
+    throw Error(GPC_ERR_PARSE, std::string(g.name) + " needs an even number of targets");
+}
+void check_args(const Instr &in, const Gate &g) {
+  auto prob = [&](double p) {
+    if (!(p >= 0 && p <= 1)) throw Error(GPC_ERR_PARSE, std::string(g.name) + ": probability out of range");
+  };
+  if (g.kind == G_N1 || g.kind == G_N2 || g.kind == G_CORR || ((g.kind == G_M || g.kind == G_MR || g.kind == G_MPAD) && in.nargs))
+    for (int k = 0; k < in.nargs; ++k) prob(in.args[k]);
+  if (g.kind == G_N1 && g.a == N1_DEP1 && in.args[0] > 0.75) throw Error(GPC_ERR_PARSE, "DEPOLARIZE1 p > 0.75");
+  if (g.kind == G_N2 && in.args[0] > 0.9375) throw Error(GPC_ERR_PARSE, "DEPOLARIZE2 p > 0.9375");
+  if (g.kind == G_N1 && g.a == N1_PC1) {
+    double q[3];
+    if (!pc1_independent(in.args[0], in.args[1], in.args[2], q))
+      throw Error(GPC_ERR_UNSUPPORTED, "PAULI_CHANNEL_1 is not a product of independent X, Y, Z channels");
+  }
+  if (g.kind == G_MPAD && in.nargs && in.args[0] > 0) throw Error(GPC_ERR_UNSUPPORTED, "noisy MPAD is not supported");
+}
+
+// First pass over ins[0, n): counts and checks (throws on a failed check;
+// the lookbacks are checked by the second pass).
+void forward_count(const Instr *ins, size_t n, FwdCount &c) {
+  for (size_t i = 0; i < n; ++i) {
+    const Instr &in = ins[i];
+    const Gate &g = kGates[in.gate];
+    c.occ += in.tn;
+    check_targets(in, g);
+    if (counts_qubits(in, g)) c.nq = std::max(c.nq, in.maxq + 1);
+    switch (g.kind) {
+      case G_M:
+      case G_MR:
+      case G_MPAD:
+        c.m += in.tn;
+        break;
+      case G_DET:
+        c.ndp += in.tn;
+        ++c.ndet;
+        break;
+      case G_OBS:
+        c.nop += in.tn;
+        c.nobs = std::max(c.nobs, obs_index(in) + 1);
+        break;
+      default:
+        check_pairs(in, g);
+        break;
+    }
+    check_args(in, g);
+  }
+}
+
+// Second pass over ins[0, n) (targets at tp[t0]) from the starting counts c:
+// measurement and occurrence bases at mb and ob, pairs at dp and op (throws
+// on a lookback beyond the start of the circuit).
+void forward_write(const Instr *ins, size_t n, const uint32_t *tp, const FwdCount &c, uint32_t *mb, uint32_t *ob,
+                   std::pair<uint32_t, uint32_t> *dp, std::pair<uint32_t, uint32_t> *op) {
+  uint32_t mm = c.m, nd = c.ndet;
+  uint64_t oc = c.occ;
+  for (size_t i = 0; i < n; ++i) {
+    const Instr &in = ins[i];
+    const Gate &g = kGates[in.gate];
+    const uint32_t *t = tp + in.t0;
+    mb[i] = mm;
+    ob[i] = (uint32_t)oc;
+    oc += in.tn;
+    if (g.kind == G_M || g.kind == G_MR || g.kind == G_MPAD) {
+      mm += in.tn;
+    } else if (g.kind == G_DET || g.kind == G_OBS) {
+      const bool det = g.kind == G_DET;
+      const uint32_t id = det ? nd++ : (uint32_t)in.args[0];
+      std::pair<uint32_t, uint32_t> *&at = det ? dp : op;
+      for (uint32_t k = 0; k < in.tn; ++k) {
+        const uint32_t back = t[k] & ~kRec;
+        if (back > mm) throw Error(GPC_ERR_PARSE, "record lookback beyond the start of the circuit");
+        *at++ = {mm - back, id};
+      }
+    }
+  }
+}
+
+// Running counts: pc[k + 1] holds run k's own counts; afterwards pc[k] holds
+// the counts before run k and pc[n] the totals (nq and nobs as maxima).
+void forward_prefix(std::vector<FwdCount> &pc, size_t n) {
+  for (size_t k = 0; k < n; ++k) {
+    FwdCount &a = pc[k + 1];
+    const FwdCount &b = pc[k];
+    a.occ += b.occ;
+    a.ndp += b.ndp;
+    a.nop += b.nop;
+    a.m += b.m;
+    a.ndet += b.ndet;
+    a.nq = std::max(a.nq, b.nq);
+    a.nobs = std::max(a.nobs, b.nobs);
+  }
+}
+
+// A text parsed in pieces on the pool (see parse_stim_pieces); with `fw`,
+// the forward pass runs beside it: each piece is counted and checked right
+// after it is parsed and written out beside its concatenation.  A failed
+// forward check leaves fw->fwd_of null (the lowering then reports it).
+void parse_pieces(const char *text, size_t len, Parsed &out, std::vector<Parsed> &pieces, HostPool &pool,
+                  LowerScratch::Buffers *fw);
+
+}  // namespace
+
 void parse_stim_pieces(const char *text, size_t len, Parsed &out, std::vector<Parsed> &pieces, HostPool &pool) {
+  parse_pieces(text, len, out, pieces, pool, nullptr);
+}
+
+namespace {
+void parse_pieces(const char *text, size_t len, Parsed &out, std::vector<Parsed> &pieces, HostPool &pool,
+                  LowerScratch::Buffers *fw) {
+  if (fw) fw->fwd_of = nullptr;
   constexpr size_t kPieceMin = 16 * 1024;
   const size_t want = std::min<size_t>({(size_t)pool.workers() + 1, 16, len / kPieceMin});
   // a REPEAT block may not be cut: such texts (short ones, usually) parse whole
@@ -552,8 +705,17 @@ void parse_stim_pieces(const char *text, size_t len, Parsed &out, std::vector<Pa
   const uint32_t np = (uint32_t)cut.size() - 1;
   if (pieces.size() < np) pieces.resize(np);
   for (uint32_t i = 0; i < np; ++i) pieces[i].want_marks = out.want_marks;
+  std::atomic<bool> fw_ok{fw != nullptr};
+  if (fw) fw->fwd_pc.assign(np + 1, FwdCount{});
   try {
-    pool.run(np, [&](uint32_t i, uint32_t) { parse_stim_into(text + cut[i], cut[i + 1] - cut[i], pieces[i]); });
+    pool.run(np, [&](uint32_t i, uint32_t) {
+      parse_stim_into(text + cut[i], cut[i + 1] - cut[i], pieces[i]);
+      if (fw_ok) try {
+          forward_count(pieces[i].ins.data(), pieces[i].ins.size(), fw->fwd_pc[i + 1]);
+        } catch (const Error &) {
+          fw_ok = false;
+        }
+    });
   } catch (const Error &) {
     parse_stim_into(text, len, out);  // the error again, with its line number in the whole text
     return;
@@ -575,8 +737,27 @@ void parse_stim_pieces(const char *text, size_t len, Parsed &out, std::vector<Pa
     line0 += pieces[i].end_line - 1;
   }
   out.end_line = line0 + 1;
+  if (fw_ok) {
+    forward_prefix(fw->fwd_pc, np);
+    const FwdCount &tot = fw->fwd_pc[np];
+    if (tot.occ > 0xFFFFFFFFull / 4) {
+      fw_ok = false;
+    } else {
+      fw->measBase.resize(ioff[np]);
+      fw->occBase.resize(ioff[np]);
+      fw->detPairs.resize(tot.ndp);
+      fw->obsPairs.resize(tot.nop);
+    }
+  }
   pool.run(np, [&](uint32_t i, uint32_t) {
     const Parsed &pc = pieces[i];
+    if (fw_ok) try {
+        const FwdCount &c = fw->fwd_pc[i];
+        forward_write(pc.ins.data(), pc.ins.size(), pc.pool.data(), c, fw->measBase.data() + ioff[i],
+                      fw->occBase.data() + ioff[i], fw->detPairs.data() + c.ndp, fw->obsPairs.data() + c.nop);
+      } catch (const Error &) {
+        fw_ok = false;
+      }
     if (!pc.pool.empty()) memcpy(out.pool.data() + toff[i], pc.pool.data(), pc.pool.size() * 4);
     Instr *dst = out.ins.data() + ioff[i];
     for (const Instr &in : pc.ins) {
@@ -585,7 +766,13 @@ void parse_stim_pieces(const char *text, size_t len, Parsed &out, std::vector<Pa
       ++dst;
     }
   });
+  if (fw_ok) {
+    fw->fwd = fw->fwd_pc[np];
+    fw->fwd_of = &out;
+    fw->fwd_ins = ioff[np];
+  }
 }
+}  // namespace
 
 namespace {
 
@@ -999,10 +1186,11 @@ void lower_text(const char *text, size_t len, const LowerOptions &opt, Tape &T, 
   S.stats = LowerScratch::Stats{};
   S.parsed.want_marks = opt.incremental;
   B.plan.active = false;
+  B.fwd_of = nullptr;
   if (!opt.incremental || !plan_incremental(text, len, opt, S)) {
     B.prev.valid = false;  // (a parse that fails leaves S.parsed half written)
     if (pool)
-      parse_stim_pieces(text, len, S.parsed, S.pieces, *pool);
+      parse_pieces(text, len, S.parsed, S.pieces, *pool, &B);  // (with the forward pass beside it)
     else
       parse_stim_into(text, len, S.parsed);
   }
@@ -1057,50 +1245,6 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
   std::vector<std::pair<uint32_t, uint32_t>> &obsPairs = B.obsPairs;  // (measurement, observable)
   uint32_t m = 0, ndet = 0, nobs = 0;
   uint32_t nq = 0;
-  // checks of one instruction that need no running count: its targets' kinds
-  // (summarised by the parser), then, after the counts, its arguments
-  auto check_targets = [&](const Instr &in, const Gate &g) {
-    if (!in.tn) return;
-    if (g.kind == G_DET || g.kind == G_OBS) {
-      if (!(in.kinds & kAllRec)) throw Error(GPC_ERR_PARSE, std::string(g.name) + " takes record targets only");
-    } else if (in.kinds & kAnyRec) {
-      throw Error(GPC_ERR_UNSUPPORTED, std::string("record targets are not supported on ") + g.name);
-    } else if (g.kind == G_MPAD) {
-      if (in.maxq > 1 || (in.kinds & kAnyPau)) throw Error(GPC_ERR_PARSE, "MPAD targets must be 0 or 1");
-    } else if (g.kind == G_CORR) {
-      if (!(in.kinds & kAllPau)) throw Error(GPC_ERR_PARSE, "E takes Pauli targets");
-    } else if (in.kinds & kAnyPau) {
-      throw Error(GPC_ERR_PARSE, std::string("Pauli targets are not allowed on ") + g.name);
-    }
-  };
-  // (qubits: the targets of every instruction but detectors, observables and MPAD)
-  auto counts_qubits = [](const Instr &in, const Gate &g) {
-    return in.tn && g.kind != G_DET && g.kind != G_OBS && g.kind != G_MPAD;
-  };
-  auto obs_index = [](const Instr &in) -> uint32_t {
-    const double a = in.args[0];
-    if (!(a >= 0) || a != std::floor(a) || a > 1e6) throw Error(GPC_ERR_PARSE, "bad observable index");
-    return (uint32_t)a;
-  };
-  auto check_pairs = [](const Instr &in, const Gate &g) {  // (the parser checked that no pair names one qubit twice)
-    if ((g.kind == G_C2 || g.kind == G_N2) && in.tn % 2)
-      throw Error(GPC_ERR_PARSE, std::string(g.name) + " needs an even number of targets");
-  };
-  auto check_args = [&](const Instr &in, const Gate &g) {
-    auto prob = [&](double p) {
-      if (!(p >= 0 && p <= 1)) throw Error(GPC_ERR_PARSE, std::string(g.name) + ": probability out of range");
-    };
-    if (g.kind == G_N1 || g.kind == G_N2 || g.kind == G_CORR || ((g.kind == G_M || g.kind == G_MR || g.kind == G_MPAD) && in.nargs))
-      for (int k = 0; k < in.nargs; ++k) prob(in.args[k]);
-    if (g.kind == G_N1 && g.a == N1_DEP1 && in.args[0] > 0.75) throw Error(GPC_ERR_PARSE, "DEPOLARIZE1 p > 0.75");
-    if (g.kind == G_N2 && in.args[0] > 0.9375) throw Error(GPC_ERR_PARSE, "DEPOLARIZE2 p > 0.9375");
-    if (g.kind == G_N1 && g.a == N1_PC1) {
-      double q[3];
-      if (!pc1_independent(in.args[0], in.args[1], in.args[2], q))
-        throw Error(GPC_ERR_UNSUPPORTED, "PAULI_CHANNEL_1 is not a product of independent X, Y, Z channels");
-    }
-    if (g.kind == G_MPAD && in.nargs && in.args[0] > 0) throw Error(GPC_ERR_UNSUPPORTED, "noisy MPAD is not supported");
-  };
   // the pass on one thread; it throws the first error in instruction order
   auto forward_serial = [&] {
     occ = 0;
@@ -1150,65 +1294,26 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
   };
   // A long circuit on the pool: its instructions in pieces, counted (and
   // checked) in a first pass, written from the pieces' starting counts in a
-  // second.  Any error sends it back to the serial pass, which reports the
-  // first error in instruction order.
+  // second (done beside the parse when the text was parsed in pieces).  Any
+  // error sends it back to the serial pass, which reports the first error in
+  // instruction order.
   bool done = false;
   const size_t nins = P.ins.size();
-  if (pool && nins >= 1024) {
-    struct Ctr {
-      uint64_t occ = 0, ndp = 0, nop = 0;
-      uint32_t m = 0, ndet = 0, nobs = 0, nq = 0;
-    };
+  if (B.fwd_of == &P && B.fwd_ins == nins) {
+    done = true;
+  } else if (pool && nins >= 1024) {
     const uint32_t np = (uint32_t)std::min<size_t>({(size_t)pool->workers() + 1, 16, nins / 128});
-    std::vector<Ctr> pc(np + 1);
+    std::vector<FwdCount> &pc = B.fwd_pc;
+    pc.assign(np + 1, FwdCount{});
     auto lo_of = [&](uint32_t p) { return nins * p / np; };
     bool ok = true;
     try {
-      pool->run(np, [&](uint32_t p, uint32_t) {
-        Ctr c;
-        for (size_t i = lo_of(p); i < lo_of(p + 1); ++i) {
-          const Instr &in = P.ins[i];
-          const Gate &g = kGates[in.gate];
-          c.occ += in.tn;
-          check_targets(in, g);
-          if (counts_qubits(in, g)) c.nq = std::max(c.nq, in.maxq + 1);
-          switch (g.kind) {
-            case G_M:
-            case G_MR:
-            case G_MPAD:
-              c.m += in.tn;
-              break;
-            case G_DET:
-              c.ndp += in.tn;
-              ++c.ndet;
-              break;
-            case G_OBS:
-              c.nop += in.tn;
-              c.nobs = std::max(c.nobs, obs_index(in) + 1);
-              break;
-            default:
-              check_pairs(in, g);
-              break;
-          }
-          check_args(in, g);
-        }
-        pc[p + 1] = c;
-      });
+      pool->run(np, [&](uint32_t p, uint32_t) { forward_count(P.ins.data() + lo_of(p), lo_of(p + 1) - lo_of(p), pc[p + 1]); });
     } catch (const Error &) {
       ok = false;
     }
     if (ok) {
-      for (uint32_t p = 0; p < np; ++p) {  // starting counts of each piece
-        Ctr &a = pc[p + 1];
-        const Ctr &b = pc[p];
-        nq = std::max(nq, a.nq);
-        nobs = std::max(nobs, a.nobs);
-        a.occ += b.occ;
-        a.ndp += b.ndp;
-        a.nop += b.nop;
-        a.m += b.m;
-        a.ndet += b.ndet;
-      }
+      forward_prefix(pc, np);
       ok = pc[np].occ <= 0xFFFFFFFFull / 4;
     }
     if (ok) {
@@ -1216,39 +1321,26 @@ void lower_into(const Parsed &P, const LowerOptions &opt, Tape &T, LowerScratch 
       obsPairs.resize(pc[np].nop);
       try {
         pool->run(np, [&](uint32_t p, uint32_t) {
-          uint32_t mm = pc[p].m, nd = pc[p].ndet;
-          size_t oc = pc[p].occ, dp = pc[p].ndp, op = pc[p].nop;
-          for (size_t i = lo_of(p); i < lo_of(p + 1); ++i) {
-            const Instr &in = P.ins[i];
-            const Gate &g = kGates[in.gate];
-            const uint32_t *t = P.pool.data() + in.t0;
-            measBase[i] = mm;
-            occBase[i] = (uint32_t)oc;
-            oc += in.tn;
-            if (g.kind == G_M || g.kind == G_MR || g.kind == G_MPAD) {
-              mm += in.tn;
-            } else if (g.kind == G_DET || g.kind == G_OBS) {
-              const uint32_t id = g.kind == G_DET ? nd++ : (uint32_t)in.args[0];
-              auto &pairs = g.kind == G_DET ? detPairs : obsPairs;
-              size_t &at = g.kind == G_DET ? dp : op;
-              for (uint32_t k = 0; k < in.tn; ++k) {
-                const uint32_t back = t[k] & ~kRec;
-                if (back > mm) throw Error(GPC_ERR_PARSE, "record lookback beyond the start of the circuit");
-                pairs[at++] = {mm - back, id};
-              }
-            }
-          }
+          const size_t i0 = lo_of(p);
+          forward_write(P.ins.data() + i0, lo_of(p + 1) - i0, P.pool.data(), pc[p], measBase.data() + i0,
+                        occBase.data() + i0, detPairs.data() + pc[p].ndp, obsPairs.data() + pc[p].nop);
         });
       } catch (const Error &) {
         ok = false;
       }
     }
     if (ok) {
-      occ = pc[np].occ;
-      m = pc[np].m;
-      ndet = pc[np].ndet;
+      B.fwd = pc[np];
       done = true;
     }
+  }
+  B.fwd_of = nullptr;
+  if (done) {
+    occ = B.fwd.occ;
+    m = B.fwd.m;
+    ndet = B.fwd.ndet;
+    nobs = B.fwd.nobs;
+    nq = B.fwd.nq;
   }
   if (!done) forward_serial();
   // sources of the noise targets: tick and class (see Tape::rec_src)
