@@ -245,6 +245,33 @@ struct TextParser {
       for (int i = 0; i < in.nargs; ++i) in.args[i] = args[i];
       uint32_t *const t0 = tw;
       in.t0 = (uint32_t)(t0 - out->pool.data());
+      {
+        // plain qubit indices (most targets), with the cursors in locals the
+        // compiler keeps in registers (the loop below, on the members, takes
+        // over at the first target of another kind)
+        const char *p = s, *const end = e;
+        uint32_t *w = tw;
+        while (true) {
+          while (p < end && (*p == ' ' || *p == '\t')) ++p;
+          if (p >= end) break;
+          unsigned d = (unsigned)(*p - '0');
+          if (d >= 10u) break;
+          const char *const d0 = p++;
+          uint64_t q = d;
+          while (p < end && (d = (unsigned)(*p - '0')) < 10u) {
+            q = q * 10u + d;
+            ++p;
+          }
+          if (p - d0 > 9 || q >= kMaxQubit) {
+            s = p;
+            tw = w;
+            fail(GPC_ERR_CAPACITY, "qubit index too large");
+          }
+          *w++ = (uint32_t)q;
+        }
+        s = p;
+        tw = w;
+      }
       while (true) {
         while (s < e && (*s == ' ' || *s == '\t')) ++s;
         if (s >= e) break;
