@@ -245,12 +245,14 @@ struct TextParser {
       for (int i = 0; i < in.nargs; ++i) in.args[i] = args[i];
       uint32_t *const t0 = tw;
       in.t0 = (uint32_t)(t0 - out->pool.data());
+      uint32_t plain_max = 0;
       {
         // plain qubit indices (most targets), with the cursors in locals the
         // compiler keeps in registers (the loop below, on the members, takes
         // over at the first target of another kind)
         const char *p = s, *const end = e;
         uint32_t *w = tw;
+        uint32_t mx = 0;
         while (true) {
           while (p < end && (*p == ' ' || *p == '\t')) ++p;
           if (p >= end) break;
@@ -268,10 +270,13 @@ struct TextParser {
             fail(GPC_ERR_CAPACITY, "qubit index too large");
           }
           *w++ = (uint32_t)q;
+          mx = std::max(mx, (uint32_t)q);
         }
         s = p;
         tw = w;
+        plain_max = mx;
       }
+      uint32_t *const t1 = tw;  // (targets past t1 came from the general loop)
       while (true) {
         while (s < e && (*s == ' ' || *s == '\t')) ++s;
         if (s >= e) break;
@@ -313,9 +318,10 @@ struct TextParser {
         }
       }
       in.tn = (uint32_t)(tw - t0);
-      // the target checks of the lowering, made here while the targets are in cache
-      uint32_t orv = 0, andv = 0xFFFFFFFFu, maxq = 0;
-      for (const uint32_t *p = t0; p < tw; ++p) {
+      // the target checks of the lowering, made here while the targets are in
+      // cache (plain indices from the loop above carry no kind bits)
+      uint32_t orv = 0, andv = t1 > t0 ? 0u : 0xFFFFFFFFu, maxq = plain_max;
+      for (const uint32_t *p = t1; p < tw; ++p) {
         orv |= *p;
         andv &= *p;
         maxq = std::max(maxq, *p & 0xFFFFFFu);
