@@ -245,36 +245,51 @@ struct TextParser {
       for (int i = 0; i < in.nargs; ++i) in.args[i] = args[i];
       uint32_t *const t0 = tw;
       in.t0 = (uint32_t)(t0 - out->pool.data());
-      uint32_t plain_max = 0;
+      // plain qubit indices and record targets (most targets), with the
+      // cursors in locals the compiler keeps in registers; the loop below, on
+      // the members, takes over at the first target of another kind (or one
+      // it must report)
+      uint32_t orf = 0, andf = 0xFFFFFFFFu, mx = 0;  // kind bits ORed and ANDed, the largest index
       {
-        // plain qubit indices (most targets), with the cursors in locals the
-        // compiler keeps in registers (the loop below, on the members, takes
-        // over at the first target of another kind)
         const char *p = s, *const end = e;
         uint32_t *w = tw;
-        uint32_t mx = 0;
         while (true) {
           while (p < end && (*p == ' ' || *p == '\t')) ++p;
           if (p >= end) break;
           unsigned d = (unsigned)(*p - '0');
-          if (d >= 10u) break;
-          const char *const d0 = p++;
-          uint64_t q = d;
-          while (p < end && (d = (unsigned)(*p - '0')) < 10u) {
-            q = q * 10u + d;
-            ++p;
+          if (d < 10u) {
+            const char *const d0 = p++;
+            uint64_t q = d;
+            while (p < end && (d = (unsigned)(*p - '0')) < 10u) {
+              q = q * 10u + d;
+              ++p;
+            }
+            if (p - d0 > 9 || q >= kMaxQubit) {
+              s = p;
+              tw = w;
+              fail(GPC_ERR_CAPACITY, "qubit index too large");
+            }
+            *w++ = (uint32_t)q;
+            andf = 0;
+            mx = std::max(mx, (uint32_t)q);
+            continue;
           }
-          if (p - d0 > 9 || q >= kMaxQubit) {
-            s = p;
-            tw = w;
-            fail(GPC_ERR_CAPACITY, "qubit index too large");
+          if (end - p < 7 || memcmp(p, "rec[-", 5) != 0) break;
+          const char *r = p + 5, *const k0 = r;
+          uint64_t k = 0;
+          while (r < end && (d = (unsigned)(*r - '0')) < 10u && r - k0 < 9) {
+            k = k * 10u + d;
+            ++r;
           }
-          *w++ = (uint32_t)q;
-          mx = std::max(mx, (uint32_t)q);
+          if (r >= end || *r != ']' || k == 0 || k > 0xFFFFFFFull) break;
+          p = r + 1;
+          *w++ = kRec | (uint32_t)k;
+          orf |= kRec;
+          andf &= kRec;
+          mx = std::max(mx, (uint32_t)k & 0xFFFFFFu);
         }
         s = p;
         tw = w;
-        plain_max = mx;
       }
       uint32_t *const t1 = tw;  // (targets past t1 came from the general loop)
       while (true) {
@@ -319,8 +334,8 @@ struct TextParser {
       }
       in.tn = (uint32_t)(tw - t0);
       // the target checks of the lowering, made here while the targets are in
-      // cache (plain indices from the loop above carry no kind bits)
-      uint32_t orv = 0, andv = t1 > t0 ? 0u : 0xFFFFFFFFu, maxq = plain_max;
+      // cache (those of the register loop above summed up as it went)
+      uint32_t orv = orf, andv = andf, maxq = mx;
       for (const uint32_t *p = t1; p < tw; ++p) {
         orv |= *p;
         andv &= *p;
