@@ -106,7 +106,10 @@ def test_tape_shapes():
 
 @pytest.mark.parametrize("bad,code", [("FOO 0\n", -3), ("CX 0\n", -2), ("DEPOLARIZE1(0.9) 0\n", -2),
                                       ("REPEAT 2 {\nH 0\n", -2), ("M 0\nDETECTOR rec[-2]\n", -2),
-                                      ("CX rec[-1] 0\n", -3)])
+                                      ("CX rec[-1] 0\n", -3), ("M 0\nDETECTOR rec[-0]\n", -2),
+                                      ("M 0\nDETECTOR rec[-1\n", -2), ("M 0\nDETECTOR rec[1]\n", -2),
+                                      ("M 0\nDETECTOR rec[-99999999999]\n", -2), ("M 0\nDETECTOR rec[-1]x\n", -2),
+                                      ("H 1234567890\n", -8), ("H 0 1x\n", -2)])
 def test_rejects_bad_input(bad, code):
     with pytest.raises(GpcError) as ei:
         Tape(bad)
