@@ -422,7 +422,8 @@ gpc_status gpc_tape_lower_cuts(const char *stim_text, size_t len, int32_t correl
  *                      the calling thread
  *   gpc_lowerer_stats  the last lowering: whether it was incremental, its
  *                      segments, those taken over, the text bytes parsed;
- *                      and its cuts (written when *ncuts <= cap) */
+ *                      and its cuts (written when *ncuts <= cap)
+ * A lowerer is used by one thread at a time; lowerers are independent. */
 typedef struct gpc_lowerer gpc_lowerer;
 typedef struct gpc_lower_stats {
   uint32_t incremental, segments, reused, reserved;
