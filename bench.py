@@ -726,7 +726,10 @@ def main() -> None:
                                        circuits=args.batch_circuits, walk_queue=args.walk_queue,
                                        device_only=args.batch_device_only)
         if not args.no_branches:
-            out["branches"] = branches_leg(gp, local)
+            try:
+                out["branches"] = branches_leg(gp, local)
+            except Exception as e:
+                out["branches"] = {"error": f"{type(e).__name__}: {e}"}
         if rank == 0:
             print(json.dumps(out), flush=True)
         return
@@ -826,7 +829,10 @@ def main() -> None:
                                     batch_texts=batch_workload_texts(args.batch_circuits) if bl.get("plain") else None,
                                     batch_plain_e2e=bl.get("plain", {}).get("e2e", {}).get("value"))
     if not args.no_branches and world == 1:  # (after serving: its page-locked blocks are of other sizes)
-        line["branches"] = branches_leg(gp, local)
+        try:
+            line["branches"] = branches_leg(gp, local)
+        except Exception as e:  # an auxiliary leg: its failure is reported in the line, not fatal to it
+            line["branches"] = {"error": f"{type(e).__name__}: {e}"}
     if not args.no_cpu_baseline and world == 1:
         line["cpu_baseline"] = cpu_baseline(text)
     print(json.dumps(line), flush=True)
